@@ -1,0 +1,1311 @@
+// ORACLE — test infrastructure only.
+//
+// CPU restatement of the inSilico assembly + Krylov path (reference project
+// thrueberg/inSilico, header-only C++).  This file is the checker that the
+// CUDA library is compared against; it is never linked into, called by, or
+// used as a fallback for the product library.  Only tests/, the smoke check
+// and the CPU-baseline leg of bench.py load it.
+//
+// Parity pin: the DOF numbering / sparsity output, the linear-elastic and
+// compressible neo-Hookean drivers and the mixed Poisson driver reproduce the
+// reference's golden files (reference/03-doFHandler/sparsity.{1,2,3}.ref.dat,
+// reference/06-elastic/linearElastic{2,3}D.ref.dat,
+// reference/06-elastic/compRefOut{D,N}.dat, reference/05-mixedPoisson/ref);
+// the pins are checked by tests/test_oracle_golden.py.
+//
+// Every block cites the reference file:line whose algorithm it restates.
+// Third-party arithmetic the reference delegates to Eigen 3.2.0 (small dense
+// inverse/determinant, SparseMatrix::setFromTriplets, ConjugateGradient with
+// the diagonal preconditioner) is restated from Eigen's documented algorithm.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include <array>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+enum Shape { POINT = 0, LINE = 1, TRI = 2, QUAD = 3, TET = 4, HEX = 5 };
+
+static int shapeDim(int s) {
+    switch (s) {
+        case POINT: return 0;
+        case LINE: return 1;
+        case TRI: case QUAD: return 2;
+        default: return 3;
+    }
+}
+static bool isCube(int s) { return s == LINE || s == QUAD || s == HEX; }
+
+// ---------------------------------------------------------------------------
+// 1-D Lagrange polynomials on [0,1]: base/sfun/Lagrange1D.ipp:45-100
+static void lag1d(int deg, double x, double* v, double* d) {
+    if (deg == 1) {
+        v[0] = 1. - x; v[1] = x;
+        d[0] = -1.; d[1] = 1.;
+    } else if (deg == 2) {
+        v[0] = (1. - x) * (1. - 2. * x);
+        v[1] = 4. * x * (1. - x);
+        v[2] = x * (2. * x - 1.);
+        d[0] = 4. * x - 3.;
+        d[1] = 4. - 8. * x;
+        d[2] = 4. * x - 1.;
+    } else {
+        throw std::runtime_error("lag1d: degree not supported");
+    }
+}
+static void lag1dSupport(int deg, double* p) {
+    for (int i = 0; i <= deg; ++i) p[i] = double(i) / double(deg);
+}
+
+// ---------------------------------------------------------------------------
+// Lexicographic -> hierarchic look-up: base/mesh/HierarchicOrder.hpp:161-454
+static std::vector<int> hierarchicTable(int dim, int K) {
+    const int n1 = K + 1;
+    int total = 1;
+    for (int d = 0; d < dim; ++d) total *= n1;
+    std::vector<int> T(total, -1);
+    int ctr = 0;
+    if (dim == 1) {
+        T[0] = ctr++; T[K] = ctr++;
+        for (int n = 1; n < K; ++n) T[n] = ctr++;
+    } else if (dim == 2) {
+        const int V[4] = {0, K, K * (K + 2), K * (K + 1)};
+        for (int i = 0; i < 4; ++i) T[V[i]] = ctr++;
+        const int E[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+        for (int i = 0; i < 4; ++i) {
+            const int a = V[E[i][0]], b = V[E[i][1]];
+            const int delta = (b - a) / K;
+            for (int n = 0; n < K - 1; ++n) T[(a + delta) + n * delta] = ctr++;
+        }
+        const int d1 = (V[1] - V[0]) / K, d2 = (V[3] - V[0]) / K;
+        for (int n2 = 0; n2 < K - 1; ++n2)
+            for (int n1i = 0; n1i < K - 1; ++n1i)
+                T[(V[0] + d1 + d2) + n1i * d1 + n2 * d2] = ctr++;
+    } else {
+        const int dZ = K * (K + 1) * (K + 1);
+        const int V[8] = {0, K, K * (K + 2), K * (K + 1), dZ, K + dZ, K * (K + 2) + dZ, K * (K + 1) + dZ};
+        for (int i = 0; i < 8; ++i) T[V[i]] = ctr++;
+        const int E[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+        for (int i = 0; i < 12; ++i) {
+            const int a = V[E[i][0]], b = V[E[i][1]];
+            const int delta = (b - a) / K;
+            for (int n = 0; n < K - 1; ++n) T[(a + delta) + n * delta] = ctr++;
+        }
+        const int F[6][3] = {{0, 1, 3}, {4, 5, 7}, {0, 1, 4}, {1, 2, 5}, {2, 3, 6}, {3, 0, 7}};
+        for (int i = 0; i < 6; ++i) {
+            const int a = V[F[i][0]], b = V[F[i][1]], c = V[F[i][2]];
+            const int d1 = (b - a) / K, d2 = (c - a) / K;
+            for (int n2 = 0; n2 < K - 1; ++n2)
+                for (int n1i = 0; n1i < K - 1; ++n1i) T[(a + d1 + d2) + n1i * d1 + n2 * d2] = ctr++;
+        }
+        const int d1 = (V[1] - V[0]) / K, d2 = (V[3] - V[0]) / K, d3 = (V[4] - V[0]) / K;
+        for (int n3 = 0; n3 < K - 1; ++n3)
+            for (int n2 = 0; n2 < K - 1; ++n2)
+                for (int n1i = 0; n1i < K - 1; ++n1i)
+                    T[(V[0] + d1 + d2 + d3) + n1i * d1 + n2 * d2 + n3 * d3] = ctr++;
+    }
+    return T;
+}
+
+// ---------------------------------------------------------------------------
+// Finite element function spaces (values, gradients, support points), all in
+// the hierarchic order the reference uses.
+//   tensor product: base/sfun/TensorProduct.hpp:40-58,226-333
+//   simplex P1/P2:  base/sfun/LagrangeTetrahedron.ipp:30-156 (P1 tet and the
+//                   P1 triangle/line follow the same barycentric pattern)
+struct FESpace {
+    int shape = QUAD;
+    int deg = 1;
+    int dim = 2;
+    int nfun = 4;
+    std::vector<int> H;  // lex -> hier (cubes)
+
+    void init(int s, int k) {
+        shape = s; deg = k; dim = shapeDim(s);
+        if (isCube(s)) {
+            nfun = 1;
+            for (int d = 0; d < dim; ++d) nfun *= (k + 1);
+            H = hierarchicTable(dim, k);
+        } else if (s == TET) {
+            nfun = (k == 1) ? 4 : 10;
+        } else if (s == TRI) {
+            nfun = (k == 1) ? 3 : 6;
+        } else {
+            nfun = 1;
+        }
+    }
+
+    // values + gradients in hierarchic order; grads laid out [nfun][dim]
+    void eval(const double* xi, double* val, double* grad) const {
+        if (isCube(shape)) {
+            double v1[3][4], d1[3][4];
+            for (int d = 0; d < dim; ++d) lag1d(deg, xi[d], v1[d], d1[d]);
+            const int n1 = deg + 1;
+            // recursive tensor product with the first coordinate fastest
+            std::vector<double> lv(1, 1.0), lg;  // lower-dim values / grads
+            int ldim = 0;
+            for (int D = 0; D < dim; ++D) {
+                const int nl = (int)lv.size();
+                std::vector<double> nv(nl * n1), ng(nl * n1 * (D + 1));
+                int ctr = 0;
+                for (int o = 0; o < n1; ++o)
+                    for (int in = 0; in < nl; ++in) {
+                        nv[ctr] = (D == 0) ? v1[D][o] : lv[in] * v1[D][o];
+                        for (int d = 0; d < D; ++d) ng[ctr * (D + 1) + d] = v1[D][o] * lg[in * ldim + d];
+                        ng[ctr * (D + 1) + D] = (D == 0) ? d1[D][o] : d1[D][o] * lv[in];
+                        ++ctr;
+                    }
+                lv.swap(nv); lg.swap(ng); ldim = D + 1;
+            }
+            for (int n = 0; n < nfun; ++n) {
+                const int h = H[n];
+                if (val) val[h] = lv[n];
+                if (grad) for (int d = 0; d < dim; ++d) grad[h * dim + d] = lg[n * dim + d];
+            }
+            return;
+        }
+        if (shape == TET) {
+            const double z1 = xi[0], z2 = xi[1], z3 = xi[2];
+            const double z0 = 1. - z1 - z2 - z3;
+            if (deg == 1) {
+                if (val) { val[0] = z0; val[1] = z1; val[2] = z2; val[3] = z3; }
+                if (grad) {
+                    const double g[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                    for (int i = 0; i < 4; ++i) for (int d = 0; d < 3; ++d) grad[i * 3 + d] = g[i][d];
+                }
+                return;
+            }
+            if (val) {
+                val[0] = z0 * (2. * z0 - 1.); val[1] = z1 * (2. * z1 - 1.);
+                val[2] = z2 * (2. * z2 - 1.); val[3] = z3 * (2. * z3 - 1.);
+                val[4] = 4. * z0 * z1; val[5] = 4. * z1 * z2; val[6] = 4. * z2 * z0;
+                val[7] = 4. * z0 * z3; val[8] = 4. * z1 * z3; val[9] = 4. * z2 * z3;
+            }
+            if (grad) {
+                const double dz[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                const double z[4] = {z0, z1, z2, z3};
+                for (int d = 0; d < 3; ++d) {
+                    for (int i = 0; i < 4; ++i) grad[i * 3 + d] = (4. * z[i] - 1.) * dz[i][d];
+                    grad[4 * 3 + d] = 4. * (z0 * dz[1][d] + dz[0][d] * z1);
+                    grad[5 * 3 + d] = 4. * (z1 * dz[2][d] + dz[1][d] * z2);
+                    grad[6 * 3 + d] = 4. * (z0 * dz[2][d] + dz[0][d] * z2);
+                    grad[7 * 3 + d] = 4. * (z0 * dz[3][d] + dz[0][d] * z3);
+                    grad[8 * 3 + d] = 4. * (z1 * dz[3][d] + dz[1][d] * z3);
+                    grad[9 * 3 + d] = 4. * (z2 * dz[3][d] + dz[2][d] * z3);
+                }
+            }
+            return;
+        }
+        if (shape == TRI) {  // P1 triangle (surface of a tet)
+            const double z1 = xi[0], z2 = xi[1], z0 = 1. - z1 - z2;
+            if (val) { val[0] = z0; val[1] = z1; val[2] = z2; }
+            if (grad) { grad[0] = -1; grad[1] = -1; grad[2] = 1; grad[3] = 0; grad[4] = 0; grad[5] = 1; }
+            return;
+        }
+        if (shape == POINT) { if (val) val[0] = 1.0; return; }
+        throw std::runtime_error("FESpace::eval: shape");
+    }
+
+    void support(std::vector<double>& pts) const {
+        pts.assign((size_t)nfun * std::max(dim, 1), 0.0);
+        if (isCube(shape)) {
+            double p1[4];
+            lag1dSupport(deg, p1);
+            const int n1 = deg + 1;
+            for (int n = 0; n < nfun; ++n) {
+                int r = n;
+                for (int d = 0; d < dim; ++d) { pts[H[n] * dim + d] = p1[r % n1]; r /= n1; }
+            }
+            return;
+        }
+        if (shape == TET) {
+            const double v[10][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {.5, 0, 0},
+                                     {.5, .5, 0}, {0, .5, 0}, {0, 0, .5}, {.5, 0, .5}, {0, .5, .5}};
+            for (int i = 0; i < nfun; ++i) for (int d = 0; d < 3; ++d) pts[i * 3 + d] = v[i][d];
+            return;
+        }
+        if (shape == TRI) {
+            const double v[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+            for (int i = 0; i < 3; ++i) for (int d = 0; d < 2; ++d) pts[i * 2 + d] = v[i][d];
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Quadrature rules.
+//   Gauss-Legendre on [0,1] with the reference's truncated constants:
+//     base/quad/GaussLegendre.hpp:33-37 (points = (DEG+2)/2), :115-134
+//   Tensor product, first coordinate fastest, weights multiplied:
+//     base/quad/TensorProduct.hpp:123-178
+//   Tetrahedron: base/quad/GaussTetrahedron.hpp:90-111
+struct QuadRule {
+    int dim = 0;
+    std::vector<double> w, x;  // x: [n][dim]
+    int n() const { return (int)w.size(); }
+};
+
+static void gl1d(int npts, std::vector<double>& w, std::vector<double>& x) {
+    if (npts == 1) { w = {1.0}; x = {0.5}; }
+    else if (npts == 2) { w = {0.5, 0.5}; x = {0.788675134594813, 0.211324865405187}; }
+    else if (npts == 3) { w = {0.277777777777777, 0.444444444444444, 0.277777777777777};
+                          x = {0.887298334620741, 0.5, 0.112701665379259}; }
+    else throw std::runtime_error("gl1d: unsupported number of points");
+}
+
+static QuadRule makeQuadrature(int shape, int degree) {
+    QuadRule q;
+    q.dim = shapeDim(shape);
+    if (isCube(shape)) {
+        std::vector<double> w1, x1;
+        gl1d((degree + 2) / 2, w1, x1);
+        std::vector<double> w = {1.0}, x;  // dim-0 rule
+        int ldim = 0;
+        for (int D = 0; D < q.dim; ++D) {
+            const int nl = (int)w.size(), n1 = (int)w1.size();
+            std::vector<double> nw(nl * n1), nx(nl * n1 * (D + 1));
+            for (int o = 0; o < n1; ++o)
+                for (int in = 0; in < nl; ++in) {
+                    const int idx = o * nl + in;
+                    nw[idx] = (D == 0 ? 1.0 : w[in]);
+                    for (int d = 0; d < D; ++d) nx[idx * (D + 1) + d] = x[in * ldim + d];
+                    nw[idx] = (D == 0) ? w1[o] : nw[idx] * w1[o];
+                    nx[idx * (D + 1) + D] = x1[o];
+                }
+            w.swap(nw); x.swap(nx); ldim = D + 1;
+        }
+        q.w = w; q.x = x;
+        return q;
+    }
+    if (shape == TET) {
+        if (degree <= 1) {
+            q.w = {0.166666666666666}; q.x = {0.25, 0.25, 0.25};
+        } else if (degree == 2) {
+            const double a = 0.13819660112501051518, b = 0.58541019662496845446, w = 0.04166666666666666667;
+            q.w = {w, w, w, w};
+            q.x = {a, a, a, b, a, a, a, b, a, a, a, b};
+        } else throw std::runtime_error("tet quadrature degree");
+        return q;
+    }
+    if (shape == TRI) {  // 1-point centroid rule, enough for constant tractions on P1 faces
+        q.w = {0.5}; q.x = {1.0 / 3.0, 1.0 / 3.0};
+        return q;
+    }
+    if (shape == POINT) { q.w = {1.0}; q.x = {}; return q; }
+    throw std::runtime_error("makeQuadrature: shape");
+}
+
+// ---------------------------------------------------------------------------
+// Element face tables: base/mesh/ElementFaces.hpp:282-436
+static const int QUAD_EDGES[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+static const int TET_EDGES[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 1}, {3, 2}};
+static const int HEX_EDGES[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+static const int TET_FACES[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
+static const int HEX_FACES[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+
+static int numVertices(int s) { switch (s) { case LINE: return 2; case TRI: return 3; case QUAD: return 4; case TET: return 4; case HEX: return 8; } return 1; }
+
+// n-face tables of an element shape (nface: 0 vertex, 1 edge, 2 face, 3 cell)
+static std::vector<std::vector<int>> faceTable(int s, int nface) {
+    std::vector<std::vector<int>> t;
+    const int nv = numVertices(s);
+    if (nface == 0) { for (int v = 0; v < nv; ++v) t.push_back({v}); return t; }
+    if (nface == 1) {
+        if (s == QUAD) for (auto& e : QUAD_EDGES) t.push_back({e[0], e[1]});
+        if (s == TET) for (auto& e : TET_EDGES) t.push_back({e[0], e[1]});
+        if (s == HEX) for (auto& e : HEX_EDGES) t.push_back({e[0], e[1]});
+        if (s == LINE) t.push_back({0, 1});
+        if (s == TRI) { t.push_back({0, 1}); t.push_back({1, 2}); t.push_back({2, 0}); }
+        return t;
+    }
+    if (nface == 2) {
+        if (s == QUAD) t.push_back({0, 1, 2, 3});
+        if (s == TRI) t.push_back({0, 1, 2});
+        if (s == TET) for (auto& f : TET_FACES) t.push_back({f[0], f[1], f[2]});
+        if (s == HEX) for (auto& f : HEX_FACES) t.push_back({f[0], f[1], f[2], f[3]});
+        return t;
+    }
+    if (nface == 3) {
+        std::vector<int> all;
+        for (int v = 0; v < nv; ++v) all.push_back(v);
+        if (s == TET || s == HEX) t.push_back(all);
+        return t;
+    }
+    return t;
+}
+
+// DOFs per n-face for a Lagrange element (base/fe/LagrangeElement.hpp:57-115)
+static int dofsPerNFace(int s, int K, int nface) {
+    if (nface == 0) return 1;
+    if (isCube(s)) {
+        int r = 1;
+        for (int i = 0; i < nface; ++i) r *= (K - 1);
+        return r;
+    }
+    // simplex: an n-face of dimension m carries binomial(K-1, m) interior dofs
+    if (nface == 1) return K - 1;
+    if (nface == 2) return (K - 1) * (K - 2) / 2;
+    if (nface == 3) return (K - 1) * (K - 2) * (K - 3) / 6;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+struct Problem {
+    // mesh (geometry degree 1)
+    int shape = QUAD, dim = 2, ngeom = 4;
+    std::vector<double> X;          // [nnodes][dim]
+    std::vector<int64_t> conn;      // [nelem][ngeom] hierarchic vertex order
+    int64_t nnodes = 0, nelem = 0;
+    // field
+    int fedeg = 1, ncomp = 1, nfun = 4;
+    FESpace geo, fe;
+    std::vector<int64_t> edof;      // [nelem][nfun] dof-object ids
+    int64_t ndofobj = 0;
+    // dof state per dof-object component
+    std::vector<int> status;        // 0 active, 1 constrained
+    std::vector<double> cval;       // constraint value
+    std::vector<double> uval;       // current value (values_[0])
+    std::vector<int64_t> eq;        // equation index or -1
+    int64_t neq = 0;
+    // kernel
+    int kernel = 0;                 // 0 laplace, 1 hyperelastic
+    int material = 0;               // 0 StVenant, 1 NeoHookeanCompressible
+    std::vector<double> kappa;      // per element
+    std::vector<double> lam, mu;    // per element
+    int qdeg = 2;                   // volume quadrature degree
+    // forces
+    std::vector<double> fnodal;     // [nnodes][ncomp] body force, interpolated by geometry functions
+    int bodyKind = 0;               // 0 none, 1 nodal, 2 -laplacian(cos product)
+    double cosAlpha[3] = {0, 0, 0};
+    std::vector<int64_t> nElem; std::vector<int> nFace;  // neumann faces
+    std::vector<double> nTrac;      // [nf][ncomp] constant traction per face
+    int neumannKind = 0;            // 0 none, 1 constant per face, 2 cos-product co-normal, 3 pulled-sheet
+    double neumannValue = 0.0;
+    int nsqdeg = 2;                 // surface quadrature degree
+    // assembled system (CSR of the pre-structured triplet pattern)
+    std::vector<int64_t> rowptr, colind;
+    std::vector<double> val, rhs;
+};
+
+static void geomEval(const Problem& P, int64_t e, const double* xi, double* J /*dim x dim, J[a][b]=dx_a/dxi_b*/,
+                     double* x /*dim*/) {
+    double gv[8], gg[8 * 3];
+    P.geo.eval(xi, gv, gg);
+    const int D = P.dim;
+    for (int a = 0; a < D * D; ++a) J[a] = 0.0;
+    for (int a = 0; a < D; ++a) x[a] = 0.0;
+    for (int i = 0; i < P.ngeom; ++i) {
+        const double* Xi = &P.X[P.conn[e * P.ngeom + i] * D];
+        for (int a = 0; a < D; ++a) {
+            x[a] += Xi[a] * gv[i];
+            for (int b = 0; b < D; ++b) J[a * D + b] += Xi[a] * gg[i * D + b];
+        }
+    }
+}
+
+// Inverse and determinant of a small matrix (restates Eigen's
+// computeInverseAndDetWithCheck for 2x2 / 3x3: cofactor expansion).
+static double invDet(int D, const double* A, double* Ainv) {
+    if (D == 1) { Ainv[0] = 1.0 / A[0]; return A[0]; }
+    if (D == 2) {
+        const double det = A[0] * A[3] - A[1] * A[2];
+        const double id = 1.0 / det;
+        Ainv[0] = A[3] * id; Ainv[1] = -A[1] * id; Ainv[2] = -A[2] * id; Ainv[3] = A[0] * id;
+        return det;
+    }
+    const double c00 = A[4] * A[8] - A[5] * A[7];
+    const double c10 = A[5] * A[6] - A[3] * A[8];
+    const double c20 = A[3] * A[7] - A[4] * A[6];
+    const double det = A[0] * c00 + A[1] * c10 + A[2] * c20;
+    const double id = 1.0 / det;
+    Ainv[0] = c00 * id; Ainv[1] = (A[2] * A[7] - A[1] * A[8]) * id; Ainv[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    Ainv[3] = c10 * id; Ainv[4] = (A[0] * A[8] - A[2] * A[6]) * id; Ainv[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    Ainv[6] = c20 * id; Ainv[7] = (A[1] * A[6] - A[0] * A[7]) * id; Ainv[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+    return det;
+}
+
+// Physical gradients of the FE functions at xi (base/LagrangeShapeFun.hpp:181-202,
+// base/geometry.hpp:142-220,419-445): g_M = J^{-T} grad_xi phi_M; returns signed detJ.
+static double feGradX(const Problem& P, int64_t e, const double* xi, double* g /*[nfun][dim]*/, double* xq,
+                      double* phi /*nullable [nfun]*/) {
+    const int D = P.dim;
+    double J[9], Ji[9];
+    geomEval(P, e, xi, J, xq);
+    // contraVariant = (J^T)^{-1}; detJ = det(J)
+    double JT[9];
+    for (int a = 0; a < D; ++a) for (int b = 0; b < D; ++b) JT[a * D + b] = J[b * D + a];
+    const double detJ = invDet(D, JT, Ji);  // Ji = J^{-T}
+    double gx[27 * 3];
+    P.fe.eval(xi, phi, gx);
+    for (int i = 0; i < P.nfun; ++i)
+        for (int a = 0; a < D; ++a) {
+            double s = 0.0;
+            for (int b = 0; b < D; ++b) s += Ji[a * D + b] * gx[i * D + b];
+            g[i * D + a] = s;
+        }
+    return detJ;
+}
+
+// ---------------------------------------------------------------------------
+// Material laws with a 3x3 deformation gradient (plane strain embedding for
+// 2-D: solid/Deformation.hpp:25-46).
+//   StVenant: mat/hypel/StVenant.hpp:77-114
+//   NeoHookeanCompressible: mat/hypel/NeoHookeanCompressible.hpp:77-93,128-172
+//   Voigt map: mat/TensorAlgebra.hpp:141-164
+static int voigt(int i, int j) {
+    static const int m[9] = {0, 3, 4, 1, -1, 5, -1, -1, 2};
+    return m[(i + 1) * (j + 1) - 1];
+}
+
+static double det3(const double* A) {
+    return A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7] - A[0] * A[5] * A[7] - A[1] * A[3] * A[8] -
+           A[2] * A[4] * A[6];
+}
+
+static void material(int mat, double lam, double mu, const double* F, double* S, double* C /*6x6*/) {
+    double Cg[9];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k) s += F[k * 3 + a] * F[k * 3 + b];
+            Cg[a * 3 + b] = s;
+        }
+    if (mat == 0) {
+        double E[9];
+        for (int a = 0; a < 9; ++a) E[a] = 0.5 * (Cg[a] - ((a % 4) == 0 ? 1.0 : 0.0));
+        const double trE = E[0] + E[4] + E[8];
+        for (int a = 0; a < 9; ++a) S[a] = lam * trE * ((a % 4) == 0 ? 1.0 : 0.0) + 2. * mu * E[a];
+        if (C) {
+            for (int a = 0; a < 36; ++a) C[a] = 0.0;
+            for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) C[a * 6 + b] = lam;
+            for (int i = 0; i < 3; ++i) C[i * 6 + i] += 2. * mu;
+            for (int i = 3; i < 6; ++i) C[i * 6 + i] += mu;
+        }
+        return;
+    }
+    double Ci[9];
+    invDet(3, Cg, Ci);
+    const double J = det3(F);
+    const double logJ = std::log(J);
+    for (int a = 0; a < 9; ++a) S[a] = (lam * logJ - mu) * Ci[a] + mu * ((a % 4) == 0 ? 1.0 : 0.0);
+    if (C) {
+        for (int a = 0; a < 36; ++a) C[a] = 0.0;  // unfilled slots stay as set below
+        const double fac2 = mu - lam * logJ;
+        for (int A = 0; A < 3; ++A)
+            for (int B = A; B < 3; ++B) {
+                const int AB = voigt(A, B);
+                for (int Cc = 0; Cc < 3; ++Cc)
+                    for (int D = Cc; D < 3; ++D) {
+                        const double ce = lam * Ci[A * 3 + B] * Ci[Cc * 3 + D] +
+                                          fac2 * (Ci[A * 3 + Cc] * Ci[B * 3 + D] + Ci[A * 3 + D] * Ci[B * 3 + Cc]);
+                        C[AB * 6 + voigt(Cc, D)] = ce;
+                    }
+            }
+    }
+}
+
+// Deformation gradient from the current displacement (solid/Deformation.hpp:25-46,
+// base/post/evaluateField.hpp:231-277): F = I + (sum_f grad phi_f u_f^T)^T
+static void defGrad(const Problem& P, int64_t e, const double* g, double* F) {
+    const int D = P.dim;
+    for (int a = 0; a < 9; ++a) F[a] = ((a % 4) == 0) ? 1.0 : 0.0;
+    double GU[9] = {0};  // GU[J][i]
+    for (int f = 0; f < P.nfun; ++f) {
+        const int64_t obj = P.edof[e * P.nfun + f];
+        for (int J = 0; J < D; ++J)
+            for (int i = 0; i < P.ncomp; ++i) GU[J * 3 + i] += g[f * D + J] * P.uval[obj * P.ncomp + i];
+    }
+    for (int i = 0; i < P.ncomp; ++i)
+        for (int J = 0; J < D; ++J) F[i * 3 + J] += GU[J * 3 + i];
+}
+
+// Element stiffness (Ke, row-major nloc x nloc) and internal force (Fe = +int P:grad phi)
+//   heat::Laplace::tangentStiffness heat/Laplace.hpp:113-126 ->
+//     base/kernel/Laplace.hpp:100-151
+//   heat::Laplace::residualForceHistory heat/Laplace.hpp:150-183
+//   solid::HyperElastic::tangentStiffness solid/HyperElastic.hpp:110-179,282-310
+//   solid::HyperElastic::residualForceHistory solid/HyperElastic.hpp:209-257
+static void elementKernel(const Problem& P, const QuadRule& Q, int64_t e, double* Ke, double* Fe) {
+    const int D = P.dim, nf = P.nfun, nd = P.ncomp, nloc = nf * nd;
+    if (Ke) std::fill(Ke, Ke + nloc * nloc, 0.0);
+    if (Fe) std::fill(Fe, Fe + nloc, 0.0);
+    double g[27 * 3], xq[3];
+    for (int q = 0; q < Q.n(); ++q) {
+        const double* xi = &Q.x[q * D];
+        const double w = Q.w[q];
+        const double detJ = feGradX(P, e, xi, g, xq, nullptr);
+        if (P.kernel == 0) {
+            const double kap = P.kappa[e];
+            if (Ke) {
+                const double scalar = kap * detJ * w;
+                for (int M = 0; M < nf; ++M)
+                    for (int N = 0; N < nf; ++N) {
+                        double entry = 0.0;
+                        for (int k = 0; k < D; ++k) entry += g[M * D + k] * g[N * D + k];
+                        entry *= scalar;
+                        Ke[M * nloc + N] += entry;
+                    }
+            }
+            if (Fe) {
+                double gu[3] = {0, 0, 0};
+                for (int f = 0; f < nf; ++f) {
+                    const double u = P.uval[P.edof[e * nf + f]];
+                    for (int k = 0; k < D; ++k) gu[k] += g[f * D + k] * u;
+                }
+                for (int i = 0; i < nf; ++i) {
+                    double dp = 0.0;
+                    for (int k = 0; k < D; ++k) dp += kap * gu[k] * g[i * D + k];
+                    Fe[i] += dp * detJ * w;
+                }
+            }
+        } else {
+            double F[9], S[9], C[36];
+            defGrad(P, e, g, F);
+            material(P.material, P.lam[e], P.mu[e], F, S, Ke ? C : nullptr);
+            if (Ke) {
+                for (int M = 0; M < nf; ++M)
+                    for (int N = 0; N < nf; ++N)
+                        for (int i = 0; i < nd; ++i)
+                            for (int k = 0; k < nd; ++k) {
+                                double sum = 0.0;
+                                for (int J = 0; J < nd; ++J)
+                                    for (int L = 0; L < nd; ++L) {
+                                        double ce = (i == k ? S[J * 3 + L] : 0.0);
+                                        for (int A = 0; A < nd; ++A) {
+                                            const int v1 = voigt(A, J);
+                                            for (int B = 0; B < nd; ++B)
+                                                ce += F[i * 3 + A] * C[v1 * 6 + voigt(B, L)] * F[k * 3 + B];
+                                        }
+                                        sum += g[M * D + J] * ce * g[N * D + L];
+                                    }
+                                sum *= detJ * w;
+                                Ke[(M * nd + i) * nloc + N * nd + k] += sum;
+                            }
+            }
+            if (Fe) {
+                double Pk[9];
+                for (int i = 0; i < 3; ++i)
+                    for (int J = 0; J < 3; ++J) {
+                        double s = 0.0;
+                        for (int k = 0; k < 3; ++k) s += F[i * 3 + k] * S[k * 3 + J];
+                        Pk[i * 3 + J] = s;
+                    }
+                for (int M = 0; M < nf; ++M)
+                    for (int i = 0; i < nd; ++i) {
+                        double s = 0.0;
+                        for (int J = 0; J < nd; ++J) s += Pk[i * 3 + J] * g[M * D + J];
+                        s *= detJ * w;
+                        Fe[M * nd + i] += s;
+                    }
+            }
+        }
+    }
+}
+
+// Body force (base/asmb/BodyForce.hpp:172-205): f_s += f(x) phi_s w detJ
+static void elementBody(const Problem& P, const QuadRule& Q, int64_t e, double* Fe) {
+    const int D = P.dim, nf = P.nfun, nd = P.ncomp;
+    std::fill(Fe, Fe + nf * nd, 0.0);
+    double g[27 * 3], xq[3], phi[27], gv[8], gg[24];
+    for (int q = 0; q < Q.n(); ++q) {
+        const double* xi = &Q.x[q * D];
+        const double detJ = feGradX(P, e, xi, g, xq, phi);
+        double f[3] = {0, 0, 0};
+        if (P.bodyKind == 1) {
+            P.geo.eval(xi, gv, gg);
+            for (int i = 0; i < P.ngeom; ++i)
+                for (int c = 0; c < nd; ++c) f[c] += gv[i] * P.fnodal[P.conn[e * P.ngeom + i] * nd + c];
+        } else if (P.bodyKind == 2) {
+            double fac = 0.0, u = 1.0;
+            for (int d = 0; d < D; ++d) fac += -P.cosAlpha[d] * P.cosAlpha[d];
+            for (int d = 0; d < D; ++d) u *= std::cos(P.cosAlpha[d] * xq[d]);
+            f[0] = -(fac * u);
+        }
+        for (int s = 0; s < nf; ++s)
+            for (int c = 0; c < nd; ++c) Fe[s * nd + c] += f[c] * phi[s] * Q.w[q] * detJ;
+    }
+}
+
+// Surface parametrisation of an element face (base/mesh/SurfaceElement.hpp:35-81,
+// base/geometry.hpp:313-346): geometry of the face vertices, domain-local
+// coordinate via the face's own linear functions.
+static void elementNeumann(const Problem& P, int64_t e, int face, const double* trac, double* Fe) {
+    const int D = P.dim, nf = P.nfun, nd = P.ncomp;
+    std::fill(Fe, Fe + nf * nd, 0.0);
+    const int sshape = (P.shape == QUAD) ? LINE : (P.shape == HEX ? QUAD : TRI);
+    const auto ft = faceTable(P.shape, D - 1);
+    const std::vector<int>& fv = ft[face];
+    FESpace sgeo;
+    sgeo.init(sshape, 1);
+    QuadRule SQ = makeQuadrature(sshape, P.nsqdeg);
+    std::vector<double> vsup;
+    P.geo.support(vsup);  // vertex local coordinates of the domain element
+    const int sd = D - 1;
+    double sv[4], sg[4 * 2], phi[27];
+    for (int q = 0; q < SQ.n(); ++q) {
+        const double* eta = &SQ.x[q * sd];
+        sgeo.eval(eta, sv, sg);
+        double xi[3] = {0, 0, 0}, x[3] = {0, 0, 0}, T[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        for (int v = 0; v < (int)fv.size(); ++v) {
+            const int lv = fv[v];
+            const double* Xv = &P.X[P.conn[e * P.ngeom + lv] * D];
+            for (int d = 0; d < D; ++d) {
+                xi[d] += vsup[lv * D + d] * sv[v];
+                x[d] += Xv[d] * sv[v];
+                for (int a = 0; a < sd; ++a) T[d][a] += Xv[d] * sg[v * sd + a];
+            }
+        }
+        double nrm[3];
+        if (D == 2) { nrm[0] = T[1][0]; nrm[1] = -T[0][0]; }
+        else {
+            nrm[0] = T[1][0] * T[2][1] - T[2][0] * T[1][1];
+            nrm[1] = T[2][0] * T[0][1] - T[0][0] * T[2][1];
+            nrm[2] = T[0][0] * T[1][1] - T[1][0] * T[0][1];
+        }
+        double len = 0.0;
+        for (int d = 0; d < D; ++d) len += nrm[d] * nrm[d];
+        len = std::sqrt(len);
+        for (int d = 0; d < D; ++d) nrm[d] /= len;
+        double t[3] = {0, 0, 0};
+        if (P.neumannKind == 1) {
+            for (int c = 0; c < nd; ++c) t[c] = trac[c];
+        } else if (P.neumannKind == 2) {
+            // co-normal derivative of the cos-product solution (reference/05-mixedPoisson/GivenData.hpp)
+            double gr[3];
+            for (int d = 0; d < D; ++d) {
+                gr[d] = -P.cosAlpha[d] * std::sin(P.cosAlpha[d] * x[d]);
+                for (int f = 0; f < D; ++f) if (f != d) gr[d] *= std::cos(P.cosAlpha[f] * x[f]);
+            }
+            double s = 0.0;
+            for (int d = 0; d < D; ++d) s += gr[d] * nrm[d];
+            t[0] = s;
+        } else if (P.neumannKind == 3) {
+            // reference/06-elastic/PulledSheet.hpp:60-75
+            if (std::abs(x[0] - 1.0) < 1.e-5) t[0] = P.neumannValue * (x[1] - 0.5);
+        }
+        P.fe.eval(xi, phi, nullptr);
+        for (int s = 0; s < nf; ++s)
+            for (int c = 0; c < nd; ++c) Fe[s * nd + c] += t[c] * phi[s] * SQ.w[q] * len;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// DOF-object index generation: base/dof/IndexMap.hpp:221-280,
+// base/dof/copyConnectivity.hpp:33-62, base/dof/generateDoFIndicesFromFaces.hpp:169-298
+static void generateDofs(Problem& P) {
+    P.edof.assign((size_t)P.nelem * P.nfun, -1);
+    const bool iso = (P.fedeg == 1);
+    if (iso) {
+        int64_t n = 0;
+        for (int64_t e = 0; e < P.nelem; ++e)
+            for (int i = 0; i < P.nfun; ++i) {
+                const int64_t id = P.conn[e * P.ngeom + i];
+                P.edof[e * P.nfun + i] = id;
+                n = std::max(n, id + 1);
+            }
+        P.ndofobj = n;
+        return;
+    }
+    const int D = P.dim;
+    int64_t numDoFs = 0;
+    int begin = 0;
+    for (int nface = 0; nface <= D; ++nface) {
+        const auto table = faceTable(P.shape, nface);
+        const int stride = dofsPerNFace(P.shape, P.fedeg, nface);
+        const int nfaces = (int)table.size();
+        const int coDim = D - nface;
+        if (nfaces == 0) continue;
+        if (coDim > 0) {
+            std::map<std::vector<int64_t>, std::pair<int64_t, int>> fmap;
+            for (int64_t e = 0; e < P.nelem; ++e) {
+                for (int f = 0; f < nfaces; ++f) {
+                    std::vector<int64_t> key;
+                    for (int v : table[f]) key.push_back(P.conn[e * P.ngeom + v]);
+                    std::sort(key.begin(), key.end());
+                    auto ins = fmap.insert(std::make_pair(key, std::make_pair(e, f)));
+                    if (!ins.second) {
+                        const int64_t other = ins.first->second.first;
+                        const int fo = ins.first->second.second;
+                        for (int d = 0; d < stride; ++d)
+                            P.edof[e * P.nfun + begin + f * stride + d] =
+                                P.edof[other * P.nfun + begin + fo * stride + d];
+                    } else {
+                        for (int d = 0; d < stride; ++d) P.edof[e * P.nfun + begin + f * stride + d] = numDoFs++;
+                    }
+                }
+            }
+        } else {
+            for (int64_t e = 0; e < P.nelem; ++e)
+                for (int d = 0; d < nfaces * stride; ++d) P.edof[e * P.nfun + begin + d] = numDoFs++;
+        }
+        begin += nfaces * stride;
+    }
+    P.ndofobj = numDoFs;
+}
+
+// Boundary faces = faces seen once, in sorted-key order
+// (base/mesh/createBoundaryFromUnstructured.hpp:51-109)
+static void boundaryFaces(const Problem& P, std::vector<std::pair<int64_t, int>>& out) {
+    const auto table = faceTable(P.shape, P.dim - 1);
+    std::map<std::vector<int64_t>, std::pair<int64_t, int>> bmap;
+    for (int64_t e = 0; e < P.nelem; ++e)
+        for (int f = 0; f < (int)table.size(); ++f) {
+            std::vector<int64_t> key;
+            for (int v : table[f]) key.push_back(P.conn[e * P.ngeom + v]);
+            std::sort(key.begin(), key.end());
+            auto it = bmap.find(key);
+            if (it == bmap.end()) bmap.insert(std::make_pair(key, std::make_pair(e, f)));
+            else bmap.erase(it);
+        }
+    out.clear();
+    for (auto& kv : bmap) out.push_back(kv.second);
+}
+
+// local FE dof positions belonging to a surface face (base/fe/Policies.hpp:99-204;
+// as a set: face vertices, interior dofs of the face's edges, face interior dofs)
+static std::vector<int> faceDofs(const Problem& P, int face) {
+    const int D = P.dim;
+    const auto ftab = faceTable(P.shape, D - 1);
+    const std::vector<int>& fv = ftab[face];
+    std::vector<int> out(fv.begin(), fv.end());
+    if (P.fedeg == 1) return out;
+    int begin = numVertices(P.shape);
+    const auto etab = faceTable(P.shape, 1);
+    const int es = dofsPerNFace(P.shape, P.fedeg, 1);
+    std::set<int> fvs(fv.begin(), fv.end());
+    for (int ed = 0; ed < (int)etab.size(); ++ed) {
+        if (fvs.count(etab[ed][0]) && fvs.count(etab[ed][1]))
+            for (int d = 0; d < es; ++d) out.push_back(begin + ed * es + d);
+    }
+    begin += (int)etab.size() * es;
+    if (D == 3) {
+        const int fs = dofsPerNFace(P.shape, P.fedeg, 2);
+        for (int d = 0; d < fs; ++d) out.push_back(begin + face * fs + d);
+    }
+    return out;
+}
+
+}  // namespace orc
+
+// ============================================================================
+// C API (ctypes)
+// ============================================================================
+using namespace orc;
+
+extern "C" {
+
+void* orc_create(int shape, int dim, int64_t nnodes, const double* X, int64_t nelem, const int64_t* conn,
+                 int fedeg, int ncomp) {
+    Problem* P = new Problem();
+    P->shape = shape; P->dim = dim; P->nnodes = nnodes; P->nelem = nelem;
+    P->geo.init(shape, 1);
+    P->ngeom = P->geo.nfun;
+    P->X.assign(X, X + nnodes * dim);
+    P->conn.assign(conn, conn + nelem * P->ngeom);
+    P->fedeg = fedeg; P->ncomp = ncomp;
+    P->fe.init(shape, fedeg);
+    P->nfun = P->fe.nfun;
+    generateDofs(*P);
+    const size_t nc = (size_t)P->ndofobj * ncomp;
+    P->status.assign(nc, 0);
+    P->cval.assign(nc, 0.0);
+    P->uval.assign(nc, 0.0);
+    P->eq.assign(nc, -1);
+    return P;
+}
+
+void orc_destroy(void* h) { delete (Problem*)h; }
+int64_t orc_num_dofobj(void* h) { return ((Problem*)h)->ndofobj; }
+int orc_nfun(void* h) { return ((Problem*)h)->nfun; }
+void orc_elem_dofobj(void* h, int64_t* out) {
+    Problem* P = (Problem*)h;
+    std::copy(P->edof.begin(), P->edof.end(), out);
+}
+
+// Sparsity of dof objects (base/dof/IndexMap.hpp:292-319); returns the
+// number of entries and fills (row, col) pairs when out != NULL.
+int64_t orc_dofobj_sparsity(void* h, int64_t* rows, int64_t* cols) {
+    Problem* P = (Problem*)h;
+    std::vector<std::set<int64_t>> con(P->ndofobj);
+    for (int64_t e = 0; e < P->nelem; ++e)
+        for (int a = 0; a < P->nfun; ++a)
+            for (int b = 0; b < P->nfun; ++b) con[P->edof[e * P->nfun + a]].insert(P->edof[e * P->nfun + b]);
+    int64_t n = 0;
+    for (int64_t d = 0; d < P->ndofobj; ++d)
+        for (int64_t c : con[d]) {
+            if (rows) { rows[n] = d; cols[n] = c; }
+            ++n;
+        }
+    return n;
+}
+
+// Boundary support points (base/dof/constrainBoundary.hpp:50-124): for every
+// boundary face (in the reference's order), every local dof on it.  Returns
+// the count; fills x [n][dim] and the dof-object ids when non-null.
+int64_t orc_boundary_points(void* h, double* x, int64_t* dofobj) {
+    Problem* P = (Problem*)h;
+    std::vector<std::pair<int64_t, int>> bf;
+    boundaryFaces(*P, bf);
+    std::vector<double> sup;
+    P->fe.support(sup);
+    int64_t n = 0;
+    for (auto& ef : bf) {
+        const auto loc = faceDofs(*P, ef.second);
+        for (int l : loc) {
+            if (x) {
+                double J[9], xq[3];
+                geomEval(*P, ef.first, &sup[l * P->dim], J, xq);
+                for (int d = 0; d < P->dim; ++d) x[n * P->dim + d] = xq[d];
+                dofobj[n] = P->edof[ef.first * P->nfun + l];
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+int64_t orc_boundary_faces(void* h, int64_t* elem, int* face) {
+    Problem* P = (Problem*)h;
+    std::vector<std::pair<int64_t, int>> bf;
+    boundaryFaces(*P, bf);
+    if (elem) for (size_t i = 0; i < bf.size(); ++i) { elem[i] = bf[i].first; face[i] = bf[i].second; }
+    return (int64_t)bf.size();
+}
+
+// DegreeOfFreedom::constrainValue (base/dof/DegreeOfFreedom.hpp:232-242)
+void orc_constrain(void* h, int64_t n, const int64_t* dofobj, const int* comp, const double* value) {
+    Problem* P = (Problem*)h;
+    for (int64_t i = 0; i < n; ++i) {
+        const size_t k = (size_t)dofobj[i] * P->ncomp + comp[i];
+        P->status[k] = 1;
+        P->cval[k] = value[i];
+    }
+}
+
+// scaleConstraints (base/dof/Distribute.hpp:75-81)
+void orc_scale_constraints(void* h, double factor) {
+    Problem* P = (Problem*)h;
+    for (size_t k = 0; k < P->status.size(); ++k) if (P->status[k] == 1) P->cval[k] *= factor;
+}
+
+// numberDoFsConsecutively (base/dof/numbering.hpp:44-68)
+int64_t orc_number(void* h) {
+    Problem* P = (Problem*)h;
+    int64_t c = 0;
+    for (size_t k = 0; k < P->status.size(); ++k) P->eq[k] = (P->status[k] == 0) ? c++ : -1;
+    P->neq = c;
+    return c;
+}
+void orc_eq_index(void* h, int64_t* out) {
+    Problem* P = (Problem*)h;
+    std::copy(P->eq.begin(), P->eq.end(), out);
+}
+
+void orc_set_laplace(void* h, const double* kappa, int qdeg) {
+    Problem* P = (Problem*)h;
+    P->kernel = 0; P->qdeg = qdeg;
+    P->kappa.assign(kappa, kappa + P->nelem);
+}
+void orc_set_hyperelastic(void* h, int mat, const double* lam, const double* mu, int qdeg) {
+    Problem* P = (Problem*)h;
+    P->kernel = 1; P->material = mat; P->qdeg = qdeg;
+    P->lam.assign(lam, lam + P->nelem);
+    P->mu.assign(mu, mu + P->nelem);
+}
+void orc_set_body_nodal(void* h, const double* f) {
+    Problem* P = (Problem*)h;
+    P->bodyKind = f ? 1 : 0;
+    if (f) P->fnodal.assign(f, f + P->nnodes * P->ncomp);
+}
+void orc_set_body_cosproduct(void* h, const double* alpha) {
+    Problem* P = (Problem*)h;
+    P->bodyKind = 2;
+    for (int d = 0; d < 3; ++d) P->cosAlpha[d] = alpha[d];
+}
+void orc_set_neumann(void* h, int kind, int64_t nf, const int64_t* elem, const int* face, const double* trac,
+                     double value, int sqdeg) {
+    Problem* P = (Problem*)h;
+    P->neumannKind = kind; P->neumannValue = value; P->nsqdeg = sqdeg;
+    P->nElem.assign(elem, elem + nf);
+    P->nFace.assign(face, face + nf);
+    if (trac) P->nTrac.assign(trac, trac + nf * P->ncomp);
+    else P->nTrac.assign(nf * P->ncomp, 0.0);
+}
+void orc_set_values(void* h, const double* u) {
+    Problem* P = (Problem*)h;
+    std::copy(u, u + P->uval.size(), P->uval.begin());
+}
+void orc_get_values(void* h, double* u) {
+    Problem* P = (Problem*)h;
+    std::copy(P->uval.begin(), P->uval.end(), u);
+}
+
+// Pre-structured pattern (base/solver/TripletContainer.hpp:158-301) as CSR:
+// union over elements of (active row, active col) pairs, explicit zeros kept.
+static void buildPattern(Problem& P) {
+    std::vector<std::vector<int64_t>> rows(P.neq);
+    const int nloc = P.nfun * P.ncomp;
+    std::vector<int64_t> ids;
+    for (int64_t e = 0; e < P.nelem; ++e) {
+        ids.clear();
+        for (int f = 0; f < P.nfun; ++f)
+            for (int c = 0; c < P.ncomp; ++c) {
+                const int64_t q = P.eq[P.edof[e * P.nfun + f] * P.ncomp + c];
+                if (q >= 0) ids.push_back(q);
+            }
+        (void)nloc;
+        for (int64_t r : ids) for (int64_t c : ids) rows[r].push_back(c);
+    }
+    P.rowptr.assign(P.neq + 1, 0);
+    P.colind.clear();
+    for (int64_t r = 0; r < P.neq; ++r) {
+        auto& v = rows[r];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        P.colind.insert(P.colind.end(), v.begin(), v.end());
+        P.rowptr[r + 1] = (int64_t)P.colind.size();
+        std::vector<int64_t>().swap(v);
+    }
+}
+
+// Stiffness + force assembly following base/asmb/StiffnessMatrix.hpp:159-225,
+// base/asmb/assembleMatrix.hpp:212-338 (Dirichlet columns move to the RHS as
+// b -= g K[:,c]), base/asmb/collectFromDoFs.hpp:82-136 (incremental prescribed
+// value = constraint - current), base/asmb/ForceIntegrator.hpp:37-71 (residual
+// forces with factor -1), base/asmb/BodyForce.hpp, base/asmb/NeumannForce.hpp.
+// Insertion follows TripletContainer::insert (lower_bound into the sorted
+// pattern, base/solver/TripletContainer.hpp:305-352); with nthreads > 1 the
+// element loop runs OpenMP-parallel with atomic adds (base/auxi/parallel.hpp:37-56,
+// base/solver/TripletContainer.hpp:94-102).
+int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) {
+    Problem* P = (Problem*)h;
+    buildPattern(*P);
+    const int64_t nnz = (int64_t)P->colind.size();
+    P->val.assign(nnz, 0.0);
+    P->rhs.assign(P->neq, 0.0);
+    const QuadRule Q = makeQuadrature(P->shape, P->qdeg);
+    const int nf = P->nfun, nd = P->ncomp, nloc = nf * nd;
+    // forces that do not depend on the stiffness: residual (x -1), body, Neumann
+    {
+        std::vector<double> Fe(nloc);
+        if (with_residual) {
+            for (int64_t e = 0; e < P->nelem; ++e) {
+                elementKernel(*P, Q, e, nullptr, Fe.data());
+                for (int a = 0; a < nloc; ++a) {
+                    const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
+                    if (q >= 0) P->rhs[q] += -1.0 * Fe[a];
+                }
+            }
+        }
+        if (P->bodyKind) {
+            for (int64_t e = 0; e < P->nelem; ++e) {
+                elementBody(*P, Q, e, Fe.data());
+                for (int a = 0; a < nloc; ++a) {
+                    const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
+                    if (q >= 0) P->rhs[q] += Fe[a];
+                }
+            }
+        }
+        if (P->neumannKind) {
+            for (size_t i = 0; i < P->nElem.size(); ++i) {
+                const int64_t e = P->nElem[i];
+                elementNeumann(*P, e, P->nFace[i], &P->nTrac[i * nd], Fe.data());
+                for (int a = 0; a < nloc; ++a) {
+                    const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
+                    if (q >= 0) P->rhs[q] += Fe[a];
+                }
+            }
+        }
+    }
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel if (nthreads > 1)
+#endif
+    {
+        std::vector<double> Ke((size_t)nloc * nloc);
+        std::vector<int64_t> q(nloc);
+        std::vector<double> g(nloc);
+        std::vector<int> st(nloc);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (int64_t e = 0; e < P->nelem; ++e) {
+            bool any = false;
+            for (int a = 0; a < nloc; ++a) {
+                const size_t k = (size_t)P->edof[e * nf + a / nd] * nd + a % nd;
+                q[a] = P->eq[k];
+                st[a] = P->status[k];
+                g[a] = (st[a] == 1) ? (incremental ? P->cval[k] - P->uval[k] : P->cval[k]) : 0.0;
+                any = true;
+            }
+            if (!any) continue;
+            elementKernel(*P, Q, e, Ke.data(), nullptr);
+            for (int r = 0; r < nloc; ++r) {
+                if (st[r] != 0) continue;
+                const int64_t row = q[r];
+                double bsub = 0.0;
+                for (int c = 0; c < nloc; ++c) {
+                    const double v = Ke[r * nloc + c];
+                    if (st[c] == 0) {
+                        const int64_t* b0 = &P->colind[P->rowptr[row]];
+                        const int64_t* b1 = &P->colind[P->rowptr[row + 1]];
+                        const int64_t* it = std::lower_bound(b0, b1, q[c]);
+                        if (it == b1 || *it != q[c]) throw std::runtime_error("pattern not set up");
+                        double* dst = &P->val[it - &P->colind[0]];
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                        *dst += v;
+                    } else {
+                        bsub -= g[c] * v;
+                    }
+                }
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                P->rhs[row] += bsub;
+            }
+        }
+    }
+    return nnz;
+}
+
+void orc_get_csr(void* h, int64_t* rowptr, int64_t* colind, double* val, double* rhs) {
+    Problem* P = (Problem*)h;
+    if (rowptr) std::copy(P->rowptr.begin(), P->rowptr.end(), rowptr);
+    if (colind) std::copy(P->colind.begin(), P->colind.end(), colind);
+    if (val) std::copy(P->val.begin(), P->val.end(), val);
+    if (rhs) std::copy(P->rhs.begin(), P->rhs.end(), rhs);
+}
+
+// Element matrices for parity of the element kernels: Ke (nloc x nloc) per element.
+void orc_element_matrices(void* h, int64_t e0, int64_t ne, double* out) {
+    Problem* P = (Problem*)h;
+    const QuadRule Q = makeQuadrature(P->shape, P->qdeg);
+    const int nloc = P->nfun * P->ncomp;
+    for (int64_t e = e0; e < e0 + ne; ++e) elementKernel(*P, Q, e, out + (e - e0) * nloc * nloc, nullptr);
+}
+
+// Eigen 3.2 ConjugateGradient<SparseMatrix<double>> with the default
+// DiagonalPreconditioner (base/solver/Eigen3.hpp:265-275): stop when
+// ||r||^2 < tol^2 ||b||^2 or after maxIter iterations.  Initial guess zero.
+// Works on CSR (row, col) — the matrix is symmetric, so the product equals
+// the self-adjoint product Eigen forms from the lower triangle.
+int64_t orc_cg(int64_t n, const int64_t* rowptr, const int64_t* colind, const double* val, const double* b, double tol,
+               int64_t maxIter, double* x, double* relres, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    std::vector<double> r(n), p(n), z(n), tmp(n), dinv(n);
+    const bool par = nthreads > 1;
+    (void)par;
+#ifdef _OPENMP
+#pragma omp parallel for if (par)
+#endif
+    for (int64_t i = 0; i < n; ++i) {
+        double d = 0.0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) if (colind[k] == i) d = val[k];
+        dinv[i] = (d != 0.0) ? 1.0 / d : 1.0;
+        x[i] = 0.0;
+        r[i] = b[i];
+    }
+    double rhsNorm2 = 0.0;
+    for (int64_t i = 0; i < n; ++i) rhsNorm2 += b[i] * b[i];
+    if (rhsNorm2 == 0.0) { if (relres) *relres = 0.0; return 0; }
+    const double threshold = tol * tol * rhsNorm2;
+    double resNorm2 = rhsNorm2;
+    if (resNorm2 < threshold) { if (relres) *relres = std::sqrt(resNorm2 / rhsNorm2); return 0; }
+    double absNew = 0.0;
+    for (int64_t i = 0; i < n; ++i) { p[i] = dinv[i] * r[i]; absNew += r[i] * p[i]; }
+    int64_t it = 0;
+    while (it < maxIter) {
+#ifdef _OPENMP
+#pragma omp parallel for if (par)
+#endif
+        for (int64_t i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * p[colind[k]];
+            tmp[i] = s;
+        }
+        double pAp = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : pAp) if (par)
+#endif
+        for (int64_t i = 0; i < n; ++i) pAp += p[i] * tmp[i];
+        const double alpha = absNew / pAp;
+        double rr = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : rr) if (par)
+#endif
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * tmp[i];
+            rr += r[i] * r[i];
+        }
+        resNorm2 = rr;
+        if (resNorm2 < threshold) break;
+        const double absOld = absNew;
+        double an = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : an) if (par)
+#endif
+        for (int64_t i = 0; i < n; ++i) { z[i] = dinv[i] * r[i]; an += r[i] * z[i]; }
+        absNew = an;
+        const double beta = absNew / absOld;
+#ifdef _OPENMP
+#pragma omp parallel for if (par)
+#endif
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        ++it;
+    }
+    if (relres) *relres = std::sqrt(resNorm2 / rhsNorm2);
+    return it;
+}
+
+// Scatter-back (base/dof/Distribute.hpp:139-215): active components take
+// (SET) or add (ADD) the solver value, constrained ones take their constraint.
+void orc_distribute(void* h, const double* x, int add) {
+    Problem* P = (Problem*)h;
+    for (size_t k = 0; k < P->status.size(); ++k) {
+        if (P->status[k] == 0) P->uval[k] = add ? P->uval[k] + x[P->eq[k]] : x[P->eq[k]];
+    }
+    for (size_t k = 0; k < P->status.size(); ++k)
+        if (P->status[k] == 1) P->uval[k] = P->cval[k];
+}
+
+// Error norms (base/post/ErrorNorm.hpp:84-230) against an analytic solution.
+//   kind 0: Kelvin fundamental solution of elastostatics
+//           (base/auxi/FundamentalSolution.hpp:166-253), params = {lambda, mu, y[3], dir[3]}
+//   kind 1: cos-product (reference/05-mixedPoisson/ReferenceSolution.hpp), params = alpha[3]
+//   order 0 = L2, 1 = H1 semi-norm (gradient)
+static void refsol(int kind, const double* prm, int dim, const double* x, double* u, double* gu) {
+    if (kind == 0) {
+        const double lam = prm[0], mu = prm[1];
+        const double G = mu, nu = lam / 2. / (lam + mu);
+        const double surf = (dim == 1) ? 2. : 2. * (dim - 1.) * M_PI;
+        const double fac1 = 1. / (4. * surf * G * (1. - nu));
+        const double fac2 = 3. - 4. * nu;
+        double R[3], dist = 0.0;
+        for (int d = 0; d < dim; ++d) { R[d] = x[d] - prm[2 + d]; dist += R[d] * R[d]; }
+        dist = std::sqrt(dist);
+        const double kern = (dim == 2) ? std::log(1. / dist) : 1. / dist;
+        const double pw = (dim == 2) ? dist * dist : dist * dist * dist;
+        for (int i = 0; i < dim; ++i) {
+            double s = 0.0;
+            for (int j = 0; j < dim; ++j) {
+                const double U = fac1 * ((i == j ? fac2 * kern : 0.) + (R[i] * R[j]) / pw);
+                s += U * prm[5 + j];
+            }
+            u[i] = s;
+        }
+        return;
+    }
+    double v = 1.0;
+    for (int d = 0; d < dim; ++d) v *= std::cos(prm[d] * x[d]);
+    u[0] = v;
+    if (gu) {
+        for (int d = 0; d < dim; ++d) {
+            gu[d] = -prm[d] * std::sin(prm[d] * x[d]);
+            for (int e = 0; e < dim; ++e) if (e != d) gu[d] *= std::cos(prm[e] * x[e]);
+        }
+    }
+}
+
+void orc_eval_refsol(int kind, const double* prm, int dim, int64_t n, const double* x, double* u) {
+    const int nc = (kind == 0) ? dim : 1;
+    for (int64_t i = 0; i < n; ++i) refsol(kind, prm, dim, x + i * dim, u + i * nc, nullptr);
+}
+
+double orc_error_norm(void* h, int kind, const double* prm, int order, int qdeg) {
+    Problem* P = (Problem*)h;
+    const QuadRule Q = makeQuadrature(P->shape, qdeg);
+    const int D = P->dim, nf = P->nfun, nd = P->ncomp;
+    double err2 = 0.0;
+    double g[27 * 3], phi[27], xq[3], u[3], gu[3];
+    for (int64_t e = 0; e < P->nelem; ++e) {
+        for (int q = 0; q < Q.n(); ++q) {
+            const double detJ = feGradX(*P, e, &Q.x[q * D], g, xq, phi);
+            refsol(kind, prm, D, xq, u, gu);
+            if (order == 0) {
+                for (int c = 0; c < nd; ++c) {
+                    double uh = 0.0;
+                    for (int f = 0; f < nf; ++f) uh += phi[f] * P->uval[P->edof[e * nf + f] * nd + c];
+                    const double d = uh - u[c];
+                    err2 += d * d * detJ * Q.w[q];
+                }
+            } else {
+                for (int k = 0; k < D; ++k) {
+                    double gh = 0.0;
+                    for (int f = 0; f < nf; ++f) gh += g[f * D + k] * P->uval[P->edof[e * nf + f] * nd];
+                    const double d = gh - gu[k];
+                    err2 += d * d * detJ * Q.w[q];
+                }
+            }
+        }
+    }
+    return std::sqrt(err2);
+}
+
+// Structured unit-cube meshes (tools/meshGeneration/unitCube/unitCube.hpp:85-263,
+// base/cut/DecomposeHyperCube.hpp:81-90).  kind: 0 quad, 1 hex, 2 tet (hex split
+// into six).  round6 mimics the 6-significant-digit coordinates the reference
+// writes into its SMF files.  Returns node count; element count via *nelem.
+int64_t orc_unitcube(int kind, int e1, int e2, int e3, int round6, double* X, int64_t* conn, int64_t* nelem) {
+    const int dim = (kind == 0) ? 2 : 3;
+    const int64_t n1 = e1 + 1, n2 = e2 + 1, n3 = (dim == 3) ? e3 + 1 : 1;
+    const int64_t nn = n1 * n2 * n3;
+    const int64_t ne = (int64_t)e1 * e2 * (dim == 3 ? e3 : 1) * (kind == 2 ? 6 : 1);
+    if (nelem) *nelem = ne;
+    if (!X) return nn;
+    const double h1 = 1.0 / e1, h2 = 1.0 / e2, h3 = (dim == 3) ? 1.0 / e3 : 0.0;
+    int64_t p = 0;
+    for (int64_t i3 = 0; i3 < n3; ++i3)
+        for (int64_t i2 = 0; i2 < n2; ++i2)
+            for (int64_t i1 = 0; i1 < n1; ++i1) {
+                double c[3] = {h1 * i1, h2 * i2, h3 * i3};
+                for (int d = 0; d < dim; ++d) {
+                    double v = c[d];
+                    if (round6) { char buf[64]; snprintf(buf, sizeof buf, "%g", v); v = atof(buf); }
+                    X[p * dim + d] = v;
+                }
+                ++p;
+            }
+    int64_t k = 0;
+    for (int64_t i3 = 0; i3 < (dim == 3 ? e3 : 1); ++i3)
+        for (int64_t i2 = 0; i2 < e2; ++i2)
+            for (int64_t i1 = 0; i1 < e1; ++i1) {
+                const int64_t i = i1 + i2 * n1 + i3 * n1 * n2;
+                int64_t c[8];
+                int nc = 0;
+                for (int d3 = 0; d3 <= (dim == 3 ? 1 : 0); ++d3)
+                    for (int d2 = 0; d2 <= 1; ++d2)
+                        for (int d1 = 0; d1 <= 1; ++d1) c[nc++] = i + d3 * n1 * n2 + d2 * n1 + d1;
+                if (kind == 0) {
+                    const int H[4] = {0, 1, 3, 2};
+                    for (int v = 0; v < 4; ++v) conn[k * 4 + v] = c[H[v]];
+                    ++k;
+                } else if (kind == 1) {
+                    const int H[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+                    for (int v = 0; v < 8; ++v) conn[k * 8 + v] = c[H[v]];
+                    ++k;
+                } else {
+                    static const int T[6][4] = {{0, 1, 3, 4}, {1, 3, 4, 5}, {3, 4, 5, 7}, {1, 3, 5, 2}, {3, 5, 2, 7}, {5, 2, 7, 6}};
+                    for (int s = 0; s < 6; ++s) {
+                        for (int v = 0; v < 4; ++v) conn[k * 4 + v] = c[T[s][v]];
+                        ++k;
+                    }
+                }
+            }
+    return nn;
+}
+
+}  // extern "C"
