@@ -1,0 +1,166 @@
+/*
+ * isl_gpu.h — C-ABI of the GB300 (sm_103a) assembly + Krylov library for the
+ * inSilico finite-element hot path.
+ *
+ * The reference (thrueberg/inSilico) is a header-only C++ template library
+ * with no FFI: its "plugin interface" is the duck-typed SOLVER template
+ * parameter (base::solver::Eigen3) plus the asmb call surface and the kernel
+ * functors.  Each entry point below replaces one step of that call surface;
+ * the reference file:line it stands in for is cited beside it.  A C++ adapter
+ * that satisfies the SOLVER duck type on top of this ABI is
+ * include/isl_gpu_solver.hpp.
+ *
+ * Conventions
+ *   - every function returns an isl_status (ISL_OK == 0); isl_last_error()
+ *     returns a message for the last failure on a context;
+ *   - plain pointers and sizes only; host buffers unless the name says _dev;
+ *   - a context owns all device memory it allocates and runs all work on the
+ *     stream given at creation (NULL = a stream the context creates);
+ *   - one host thread per context (not re-entrant); several contexts may
+ *     share a device;
+ *   - local element DOF order is node-major, component-minor (a = M*ncomp + i),
+ *     as in solid/HyperElastic.hpp:171 (matrix(M*nDoFs+i, N*nDoFs+k)).
+ */
+#ifndef ISL_GPU_H
+#define ISL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ISL_OK = 0,
+    ISL_ERR_ARG = 1,            /* invalid argument or call order */
+    ISL_ERR_NOMEM = 2,          /* device or host allocation failed */
+    ISL_ERR_DEGENERATE = 3,     /* an element had det J <= 0 (results still written) */
+    ISL_ERR_NOT_CONVERGED = 4,  /* solver hit max_iter before the tolerance */
+    ISL_ERR_TIMEOUT = 5,        /* a bounded device wait expired */
+    ISL_ERR_CUDA = 6,           /* CUDA runtime error */
+    ISL_ERR_NAN = 7             /* non-finite value in a reduction */
+} isl_status;
+
+/* element shapes (geometry degree 1, hierarchic vertex order of
+ * base/mesh/HierarchicOrder.hpp) */
+enum { ISL_QUAD = 3, ISL_TET = 4, ISL_HEX = 5 };
+/* kernel functors */
+enum { ISL_KERNEL_LAPLACE = 0, ISL_KERNEL_HYPERELASTIC = 1 };
+/* materials of solid::HyperElastic */
+enum { ISL_MAT_STVENANT = 0, ISL_MAT_NEOHOOKE = 1 };
+/* arithmetic of the element kernels and of the stored matrix */
+enum { ISL_PREC_FP64 = 0, ISL_PREC_FP32 = 1, ISL_PREC_MIXED = 2 };
+/* solve methods */
+enum { ISL_SOLVE_CG_FP64 = 0, ISL_SOLVE_CG_FP32_IR = 1 };
+/* phase timers reported by isl_timings (milliseconds, CUDA events) */
+enum { ISL_T_ELEMENT = 0, ISL_T_GATHER = 1, ISL_T_SOLVE = 2, ISL_T_SPMV = 3, ISL_T_PATTERN = 4, ISL_NTIMERS = 8 };
+
+typedef struct isl_ctx isl_ctx;
+
+/* Context lifetime.  stream: a cudaStream_t (NULL = create one). */
+int isl_ctx_create(isl_ctx** out, int device, void* stream);
+int isl_ctx_destroy(isl_ctx* ctx);
+const char* isl_last_error(const isl_ctx* ctx);
+
+/* Mesh: coordinates [n_nodes][dim], connectivity [n_elem][n_vertices]
+ * (int64 node ids, hierarchic order).
+ * Replaces base::io::smf::readMesh / base::Unstructured construction
+ * (base/io/smf/Reader.hpp:275-307). */
+int isl_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_nodes, const double* coords, int64_t n_elem,
+                    const int64_t* conn);
+
+/* Field of Lagrange degree fe_degree with ncomp components per DOF object;
+ * generates the DOF-object ids per element.
+ * Replaces base::dof::generate (base/dof/generate.hpp:65-115 ->
+ * base/dof/IndexMap.hpp:221-280). */
+int isl_field_create(isl_ctx* ctx, int fe_degree, int ncomp, int64_t* n_dofobj, int* n_fun);
+int isl_field_elem_dofobj(isl_ctx* ctx, int64_t* out /* [n_elem][n_fun] */);
+
+/* Boundary = faces seen once, sorted by vertex key.  Call with NULL arrays to
+ * get the count.  Replaces base::mesh::MeshBoundary::create
+ * (base/mesh/createBoundaryFromUnstructured.hpp:51-109). */
+int isl_boundary_faces(isl_ctx* ctx, int64_t* n, int64_t* elem, int* face);
+/* Support points of every boundary face DOF with its DOF object, in the
+ * order base::dof::constrainBoundary visits them
+ * (base/dof/constrainBoundary.hpp:50-124); the caller evaluates its
+ * Dirichlet functor on them and calls isl_constrain. */
+int isl_boundary_points(isl_ctx* ctx, int64_t* n, double* x /* [n][dim] */, int64_t* dofobj);
+/* DegreeOfFreedom::constrainValue (base/dof/DegreeOfFreedom.hpp:232-242) */
+int isl_constrain(isl_ctx* ctx, int64_t n, const int64_t* dofobj, const int* comp, const double* value);
+/* base::dof::scaleConstraints (base/dof/Distribute.hpp:75-81) */
+int isl_scale_constraints(isl_ctx* ctx, double factor);
+/* base::dof::numberDoFsConsecutively (base/dof/numbering.hpp:44-68) */
+int isl_number_dofs(isl_ctx* ctx, int64_t* n_active);
+/* equation index per DOF-object component (-1 if constrained) */
+int isl_dof_index(isl_ctx* ctx, int64_t* out /* [n_dofobj*ncomp] */);
+
+/* CSR pattern of active DOF pairs + element-to-slot contribution lists, built
+ * on the device.  Replaces Eigen3::registerFields ->
+ * TripletContainer::registerFields (base/solver/TripletContainer.hpp:158-301). */
+int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
+
+/* Kernel functor tabulation (per element coefficients; the reference's
+ * ConductivityFun / Material objects are evaluated per element by the caller):
+ *   heat::Laplace (heat/Laplace.hpp:113-126, base/kernel/Laplace.hpp:100-151)
+ *   solid::HyperElastic<StVenant|NeoHookeanCompressible>
+ *     (solid/HyperElastic.hpp:110-257, mat/hypel/StVenant.hpp:77-114,
+ *      mat/hypel/NeoHookeanCompressible.hpp:77-172)
+ * quad_degree: base::Quadrature<DEG,SHAPE> degree (base/Quadrature.hpp:113-143). */
+int isl_set_laplace(isl_ctx* ctx, const double* kappa /* [n_elem] */, int quad_degree);
+int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const double* mu, int quad_degree);
+/* Body force interpolated from nodal values by the geometry functions
+ * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
+int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] */);
+/* Constant traction per boundary face (base/asmb/NeumannForce.hpp:132-174);
+ * n == 0 clears it. */
+int isl_set_neumann(isl_ctx* ctx, int64_t n, const int64_t* elem, const int* face, const double* traction,
+                    int squad_degree);
+
+/* Current DOF values (DegreeOfFreedom values_[0]) [n_dofobj*ncomp]. */
+int isl_set_values(isl_ctx* ctx, const double* u);
+int isl_get_values(isl_ctx* ctx, double* u);
+
+/* Assemble the system: stiffness with Dirichlet columns moved to the RHS,
+ * body + Neumann forces and, if with_residual, the internal forces times -1.
+ * Replaces stiffnessMatrixComputation (base/asmb/StiffnessMatrix.hpp:49-87)
+ * + computeResidualForces (base/asmb/ForceIntegrator.hpp:37-71) +
+ * bodyForceComputation + neumannForceComputation + Eigen3::finishAssembly
+ * (base/solver/Eigen3.hpp:142-153).  precision: ISL_PREC_FP64 (FP64 element
+ * kernels, FP64 matrix), ISL_PREC_FP32 (FP32 tangent, FP64 forces, FP32
+ * matrix), ISL_PREC_MIXED (FP64 element kernels, FP64 + FP32 matrix copies). */
+int isl_assemble(isl_ctx* ctx, int precision, int incremental, int with_residual);
+
+/* Solve the assembled system (Eigen3::cgSolve base/solver/Eigen3.hpp:265-275:
+ * Jacobi-preconditioned CG, ||r|| <= tol ||b||, x0 = 0).
+ *   ISL_SOLVE_CG_FP64   : FP64 throughout (the plain path)
+ *   ISL_SOLVE_CG_FP32_IR: FP32 CG (FP64 dot reductions) inside FP64
+ *                         iterative refinement on the FP64 residual.
+ * max_iter <= 0 means 2N.  iters/rel_res may be NULL. */
+int isl_solve(isl_ctx* ctx, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res);
+
+/* After a solve the solution replaces the right-hand side, as in Eigen3
+ * (b_ holds x; Eigen3::getValue base/solver/Eigen3.hpp:293-296). */
+int isl_get_solution(isl_ctx* ctx, double* x /* [n_active] */);
+int isl_get_rhs(isl_ctx* ctx, double* b /* [n_active] */);
+/* Eigen3::norm: ||b||_2 / N (base/solver/Eigen3.hpp:128-138) */
+int isl_norm(isl_ctx* ctx, double* out);
+/* setDoFsFromSolver (add=0) / addToDoFsFromSolver (add=1)
+ * (base/dof/Distribute.hpp:139-215) */
+int isl_distribute(isl_ctx* ctx, int add);
+
+/* Assembled CSR (int64 row pointers / column ids, FP64 values) for parity. */
+int isl_get_csr(isl_ctx* ctx, int64_t* rowptr, int64_t* colind, double* values);
+
+/* Synchronise the context stream; per-phase timings of the last assemble /
+ * solve (ms) when timing is on. */
+int isl_sync(isl_ctx* ctx);
+int isl_set_timing(isl_ctx* ctx, int on);
+int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /* [ISL_NTIMERS] */);
+/* Average device time (ms) of one launch of the solver's SpMV kernel on the
+ * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches. */
+int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISL_GPU_H */

@@ -1,0 +1,118 @@
+"""ctypes binding of the C-ABI in include/isl_gpu.h (libisl_gpu.so).
+
+There is no fallback: if the shared library is missing or fails to load, the
+import of the GPU path raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+ISL_OK, ISL_ERR_ARG, ISL_ERR_NOMEM, ISL_ERR_DEGENERATE, ISL_ERR_NOT_CONVERGED, ISL_ERR_TIMEOUT, ISL_ERR_CUDA, ISL_ERR_NAN = range(8)
+QUAD, TET, HEX = 3, 4, 5
+KERNEL_LAPLACE, KERNEL_HYPERELASTIC = 0, 1
+MAT_STVENANT, MAT_NEOHOOKE = 0, 1
+PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
+SOLVE_CG_FP64, SOLVE_CG_FP32_IR = 0, 1
+T_ELEMENT, T_GATHER, T_SOLVE, T_SPMV, T_PATTERN, NTIMERS = 0, 1, 2, 3, 4, 8
+
+_STATUS = {
+    ISL_ERR_ARG: "invalid argument",
+    ISL_ERR_NOMEM: "out of memory",
+    ISL_ERR_DEGENERATE: "degenerate element",
+    ISL_ERR_NOT_CONVERGED: "not converged",
+    ISL_ERR_TIMEOUT: "timeout",
+    ISL_ERR_CUDA: "CUDA error",
+    ISL_ERR_NAN: "non-finite value",
+}
+
+EXPORTED = [
+    "isl_ctx_create", "isl_ctx_destroy", "isl_last_error", "isl_mesh_upload", "isl_field_create",
+    "isl_field_elem_dofobj", "isl_boundary_faces", "isl_boundary_points", "isl_constrain",
+    "isl_scale_constraints", "isl_number_dofs", "isl_dof_index", "isl_register_pattern", "isl_set_laplace",
+    "isl_set_hyperelastic", "isl_set_body_force_nodal", "isl_set_neumann", "isl_set_values", "isl_get_values",
+    "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
+    "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv",
+]
+
+
+class IslError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_I32 = C.POINTER(C.c_int)
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libisl_gpu.so; raise if it is not there (no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"{path} is missing: run insilico_gb300.build.build() (or __graft_entry__.build())")
+        _build.build()
+    L = C.CDLL(path)
+    i = C.c_int
+    L.isl_ctx_create.argtypes = [C.POINTER(_P), i, _P]
+    L.isl_ctx_destroy.argtypes = [_P]
+    L.isl_last_error.argtypes = [_P]
+    L.isl_last_error.restype = C.c_char_p
+    L.isl_mesh_upload.argtypes = [_P, i, i, C.c_int64, _D, C.c_int64, _I64]
+    L.isl_field_create.argtypes = [_P, i, i, _I64, _I32]
+    L.isl_field_elem_dofobj.argtypes = [_P, _I64]
+    L.isl_boundary_faces.argtypes = [_P, _I64, _I64, _I32]
+    L.isl_boundary_points.argtypes = [_P, _I64, _D, _I64]
+    L.isl_constrain.argtypes = [_P, C.c_int64, _I64, _I32, _D]
+    L.isl_scale_constraints.argtypes = [_P, C.c_double]
+    L.isl_number_dofs.argtypes = [_P, _I64]
+    L.isl_dof_index.argtypes = [_P, _I64]
+    L.isl_register_pattern.argtypes = [_P, _I64]
+    L.isl_set_laplace.argtypes = [_P, _D, i]
+    L.isl_set_hyperelastic.argtypes = [_P, i, _D, _D, i]
+    L.isl_set_body_force_nodal.argtypes = [_P, _D]
+    L.isl_set_neumann.argtypes = [_P, C.c_int64, _I64, _I32, _D, i]
+    L.isl_set_values.argtypes = [_P, _D]
+    L.isl_get_values.argtypes = [_P, _D]
+    L.isl_assemble.argtypes = [_P, i, i, i]
+    L.isl_solve.argtypes = [_P, i, C.c_double, C.c_int64, _I64, _D]
+    L.isl_get_solution.argtypes = [_P, _D]
+    L.isl_get_rhs.argtypes = [_P, _D]
+    L.isl_norm.argtypes = [_P, _D]
+    L.isl_distribute.argtypes = [_P, i]
+    L.isl_get_csr.argtypes = [_P, _I64, _I64, _D]
+    L.isl_sync.argtypes = [_P]
+    L.isl_set_timing.argtypes = [_P, i]
+    L.isl_timings.argtypes = [_P, _D, _I64]
+    L.isl_time_spmv.argtypes = [_P, i, i, _D]
+    for name in EXPORTED:
+        f = getattr(L, name)
+        if name != "isl_last_error":
+            f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def d(a):
+    return a.ctypes.data_as(_D)
+
+
+def i64(a):
+    return a.ctypes.data_as(_I64)
+
+
+def i32(a):
+    return a.ctypes.data_as(_I32)

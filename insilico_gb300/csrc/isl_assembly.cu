@@ -1,0 +1,919 @@
+// Device assembly for the GB300 (sm_103a) inSilico hot path.
+//
+//  * pattern_build: the CSR pattern of active DOF pairs (the reference's
+//    pre-structured triplet pattern, base/solver/TripletContainer.hpp:158-301)
+//    is built on the device by a stable radix sort of (row, col) keys of every
+//    element's active local pairs.  The sorted order doubles as the
+//    element-to-slot contribution list: slot s sums the staged element entries
+//    src[seg[s] .. seg[s+1]) in element order, the order in which the
+//    reference's serial element loop adds into a triplet
+//    (TripletContainer::insert, :305-352).  No atomics are used.
+//  * element kernels stage the packed upper triangle of every element matrix
+//    (entry-major: stage[u * nelem + e], coalesced across elements) and the
+//    element force vector; a gather kernel then forms CSR values and the RHS.
+//  * Dirichlet columns move to the RHS per element (b -= K[:,c] g_c,
+//    base/asmb/assembleMatrix.hpp:56-130) in a kernel over the elements that
+//    own a constrained DOF.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <vector>
+
+#include "isl_internal.h"
+
+namespace isl {
+
+// ---------------------------------------------------------------------------
+// small helpers
+__host__ __device__ inline int upidx(int a, int b, int n) {  // packed upper, row-major, a <= b
+    return a * n - (a * (a - 1)) / 2 + (b - a);
+}
+
+template <int D>
+__device__ inline double inv_t(const double J[D][D], double Ji[D][D]) {
+    // Ji = J^{-T}; returns det J  (signed, as the reference)
+    if (D == 2) {
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const double id = 1.0 / det;
+        Ji[0][0] = J[1][1] * id;  Ji[0][1] = -J[1][0] * id;
+        Ji[1][0] = -J[0][1] * id; Ji[1][1] = J[0][0] * id;
+        return det;
+    } else {
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const double id = 1.0 / det;
+        // (J^{-1})^T = cofactor(J) / det
+        Ji[0][0] = c00 * id; Ji[0][1] = c01 * id; Ji[0][2] = c02 * id;
+        Ji[1][0] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        Ji[1][2] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        Ji[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        Ji[2][1] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        return det;
+    }
+}
+
+// Is the geometry map affine (constant Jacobian)?  Tetrahedra always are;
+// quads/hexes when their bilinear/trilinear coefficients vanish.
+template <int SHAPE, int NG, int D>
+__device__ inline bool affine(const double X[NG][D]) {
+    if (SHAPE == ISL_TET) return true;
+    double scale = 0.0, dev = 0.0;
+    for (int d = 0; d < D; ++d) {
+        if (SHAPE == ISL_QUAD) {
+            const double t = X[0][d] - X[1][d] + X[2][d] - X[3][d];
+            dev = fmax(dev, fabs(t));
+            scale = fmax(scale, fabs(X[1][d] - X[0][d]) + fabs(X[3][d] - X[0][d]));
+        } else {
+            // hierarchic hex vertices: 0 c000, 1 c100, 2 c110, 3 c010, 4 c001, 5 c101, 6 c111, 7 c011
+            const double xy = X[0][d] - X[1][d] + X[2][d] - X[3][d];
+            const double xz = X[0][d] - X[1][d] - X[4][d] + X[5][d];
+            const double yz = X[0][d] - X[3][d] - X[4][d] + X[7][d];
+            const double xyz = -X[0][d] + X[1][d] - X[2][d] + X[3][d] + X[4][d] - X[5][d] + X[6][d] - X[7][d];
+            dev = fmax(dev, fmax(fmax(fabs(xy), fabs(xz)), fmax(fabs(yz), fabs(xyz))));
+            scale = fmax(scale, fabs(X[1][d] - X[0][d]) + fabs(X[3][d] - X[0][d]) + fabs(X[4][d] - X[0][d]));
+        }
+    }
+    return dev <= 1e-13 * scale;
+}
+
+template <int NG, int D>
+__device__ inline double jac(const double X[NG][D], const double dN[NG][D], double Ji[D][D]) {
+    double J[D][D];
+    for (int a = 0; a < D; ++a)
+        for (int b = 0; b < D; ++b) {
+            double s = 0.0;
+            for (int i = 0; i < NG; ++i) s += X[i][a] * dN[i][b];
+            J[a][b] = s;
+        }
+    return inv_t<D>(J, Ji);
+}
+
+struct ElemArgs {
+    int nelem;
+    const double* X;        // [nnodes][D]
+    const int32_t* conn;    // [NG][nelem]
+    const int32_t* edof;    // [NF][nelem]
+    const double* coef;     // [ncoef][nelem]
+    const double* u;        // per dofobj comp
+    const double* fnodal;   // [nnodes][ncomp] or null
+    int with_residual;
+    int general;            // hyperelastic: 1 = finite strain path, 0 = small-strain at u = 0
+    int material;
+    void* stageK;           // [nup][nelem] (R)
+    double* stageF;         // [nloc][nelem]
+    int* flags;
+};
+
+// ---------------------------------------------------------------------------
+// heat::Laplace element kernel, one thread per element.
+//   K[M][N] += (grad phi_M . grad phi_N) (kappa detJ w)   base/kernel/Laplace.hpp:131-148
+//   F[i]    -= kappa grad u . grad phi_i detJ w           heat/Laplace.hpp:150-183 (x -1)
+//   F[s]    += f(x) phi_s w detJ                          base/asmb/BodyForce.hpp:172-205
+template <int SHAPE, int FDEG, int NQ, typename R>
+__global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T) {
+    constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
+    constexpr int NUP = NF * (NF + 1) / 2;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.nelem) return;
+    const int E = A.nelem;
+    double X[NG][D];
+    int nodes[NG];
+#pragma unroll
+    for (int i = 0; i < NG; ++i) {
+        nodes[i] = A.conn[i * E + e];
+#pragma unroll
+        for (int d = 0; d < D; ++d) X[i][d] = A.X[(size_t)nodes[i] * D + d];
+    }
+    const double kap = A.coef[e];
+    double uloc[NF];
+    if (A.with_residual) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) uloc[f] = A.u[A.edof[f * E + e]];
+    }
+    const bool aff = affine<SHAPE, NG, D>(X);
+    double Ji[D][D], detJ = 0.0;
+    if (aff) detJ = jac<NG, D>(X, T.dN[0], Ji);
+    R acc[NUP];
+#pragma unroll
+    for (int u = 0; u < NUP; ++u) acc[u] = R(0);
+    double fe[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) fe[f] = 0.0;
+    bool bad = false;
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+        if (!aff) detJ = jac<NG, D>(X, T.dN[q], Ji);
+        bad |= !(detJ > 0.0);
+        double g[NF][D];
+#pragma unroll
+        for (int M = 0; M < NF; ++M)
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double s = 0.0;
+#pragma unroll
+                for (int b = 0; b < D; ++b) s += Ji[a][b] * T.dphi[q][M][b];
+                g[M][a] = s;
+            }
+        const double c = kap * detJ * T.w[q];
+        const R cr = R(c);
+#pragma unroll
+        for (int M = 0; M < NF; ++M)
+#pragma unroll
+            for (int N = M; N < NF; ++N) {
+                R dot = R(0);
+#pragma unroll
+                for (int k = 0; k < D; ++k) dot += R(g[M][k]) * R(g[N][k]);
+                acc[upidx(M, N, NF)] += dot * cr;
+            }
+        if (A.fnodal) {
+            double f = 0.0;
+#pragma unroll
+            for (int i = 0; i < NG; ++i) f += T.N[q][i] * A.fnodal[nodes[i]];
+#pragma unroll
+            for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
+        }
+        if (A.with_residual) {
+            double gu[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                double s = 0.0;
+#pragma unroll
+                for (int f = 0; f < NF; ++f) s += g[f][k] * uloc[f];
+                gu[k] = kap * s;
+            }
+#pragma unroll
+            for (int i = 0; i < NF; ++i) {
+                double dp = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) dp += gu[k] * g[i][k];
+                fe[i] -= dp * detJ * T.w[q];
+            }
+        }
+    }
+    if (bad) atomicOr(A.flags, 1);
+    R* SK = (R*)A.stageK;
+#pragma unroll
+    for (int u = 0; u < NUP; ++u) SK[(size_t)u * E + e] = acc[u];
+#pragma unroll
+    for (int s = 0; s < NF; ++s) A.stageF[(size_t)s * E + e] = fe[s];
+}
+
+// ---------------------------------------------------------------------------
+// solid::HyperElastic on trilinear hexahedra, 2x2x2 quadrature.
+// 8 threads per element: in phase 1 thread q evaluates quadrature point q
+// (geometry, deformation, stress, effective elasticity), in phase 2 thread M
+// accumulates row-node M's 3x3 blocks K_MN (N >= M) over the quadrature points.
+//   K[Md+i, Nd+k] += sum_JL phi_M,J (d_ik S_JL + F_iA C_AJBL F_kB) phi_N,L detJ w
+//                                           solid/HyperElastic.hpp:110-179,282-310
+//   F[Md+i] -= sum_J (F S)_iJ phi_M,J detJ w  solid/HyperElastic.hpp:209-257 (x -1)
+// Materials: StVenant mat/hypel/StVenant.hpp:77-114,
+//            NeoHookeanCompressible mat/hypel/NeoHookeanCompressible.hpp:77-172.
+// At u == 0 (F = I, S = 0) both reduce to isotropic linear elasticity and the
+// kernel uses  K_MN = c (lam g_M g_N^T + mu g_N g_M^T + mu (g_M.g_N) I).
+__device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
+    const int m = (i + 1) * (j + 1);
+    return m == 1 ? 0 : m == 4 ? 1 : m == 9 ? 2 : m == 2 ? 3 : m == 3 ? 4 : 5;
+}
+
+__device__ inline void material_eval(int mat, double lam, double mu, const double F[3][3], double S[3][3], double C[6][6]) {
+    double Cg[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Cg[a][b] = F[0][a] * F[0][b] + F[1][a] * F[1][b] + F[2][a] * F[2][b];
+    if (mat == ISL_MAT_STVENANT) {
+        double E[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) E[a][b] = 0.5 * (Cg[a][b] - (a == b ? 1.0 : 0.0));
+        const double tr = E[0][0] + E[1][1] + E[2][2];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) S[a][b] = lam * tr * (a == b ? 1.0 : 0.0) + 2.0 * mu * E[a][b];
+        for (int a = 0; a < 6; ++a)
+            for (int b = 0; b < 6; ++b) C[a][b] = (a < 3 && b < 3) ? lam : 0.0;
+        for (int i = 0; i < 3; ++i) C[i][i] += 2.0 * mu;
+        for (int i = 3; i < 6; ++i) C[i][i] += mu;
+        return;
+    }
+    double Ci[3][3];
+    const double detC = inv_t<3>(Cg, Ci);  // Cg symmetric, so Ci = Cg^{-T} = Cg^{-1}
+    (void)detC;
+    const double J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) - F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
+                     F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
+    const double lj = log(J);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) S[a][b] = (lam * lj - mu) * Ci[a][b] + mu * (a == b ? 1.0 : 0.0);
+    const double f2 = mu - lam * lj;
+    for (int A = 0; A < 3; ++A)
+        for (int B = A; B < 3; ++B)
+            for (int Cc = 0; Cc < 3; ++Cc)
+                for (int Dd = Cc; Dd < 3; ++Dd)
+                    C[voigt(A, B)][voigt(Cc, Dd)] =
+                        lam * Ci[A][B] * Ci[Cc][Dd] + f2 * (Ci[A][Cc] * Ci[B][Dd] + Ci[A][Dd] * Ci[B][Cc]);
+}
+
+template <typename R, int EPB>
+__global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const Tab<3, 8, 8, 8> T) {
+    constexpr int NLOC = 24;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // shared layout (element index fastest to keep banks distinct)
+    double* sX = (double*)smem_raw;                 // [8][3][EPB]
+    double* su = sX + 8 * 3 * EPB;                  // [8][3][EPB]
+    double* sfq = su + 8 * 3 * EPB;                 // [8 q][8 node][3][EPB] residual contributions
+    R* sg = (R*)(sfq + (A.general ? 8 * 8 * 3 * EPB : 0));  // [8 q][8 node][3][EPB]
+    R* sc = sg + 8 * 8 * 3 * EPB;                   // [8][EPB]
+    R* sA = sc + 8 * EPB;                           // [8 q][81][EPB] (general only)
+
+    const int el = threadIdx.x % EPB, role = threadIdx.x / EPB;
+    const int E = A.nelem;
+    const int e = blockIdx.x * EPB + el;
+    const bool valid = e < E;
+    const int ec = valid ? e : E - 1;
+    {
+        const int node = A.conn[role * E + ec];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sX[(role * 3 + d) * EPB + el] = A.X[(size_t)node * 3 + d];
+        if (A.general) {
+            const int obj = A.edof[role * E + ec];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) su[(role * 3 + d) * EPB + el] = A.u[(size_t)obj * 3 + d];
+        }
+    }
+    __syncthreads();
+    const double lam = A.coef[ec], mu = A.coef[E + ec];
+    // ---- phase 1: quadrature point q = role
+    {
+        const int q = role;
+        double X[8][3];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) X[i][d] = sX[(i * 3 + d) * EPB + el];
+        double Ji[3][3];
+        const double detJ = jac<8, 3>(X, T.dN[q], Ji);
+        if (valid && !(detJ > 0.0)) atomicOr(A.flags, 1);
+        double g[8][3];
+#pragma unroll
+        for (int M = 0; M < 8; ++M)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) g[M][a] = Ji[a][0] * T.dphi[q][M][0] + Ji[a][1] * T.dphi[q][M][1] + Ji[a][2] * T.dphi[q][M][2];
+        const double c = detJ * T.w[q];
+#pragma unroll
+        for (int M = 0; M < 8; ++M)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) sg[((q * 8 + M) * 3 + a) * EPB + el] = R(g[M][a]);
+        sc[q * EPB + el] = R(c);
+        if (A.general) {
+            double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+            for (int f = 0; f < 8; ++f)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const double uf = su[(f * 3 + i) * EPB + el];
+#pragma unroll
+                    for (int J = 0; J < 3; ++J) F[i][J] += g[f][J] * uf;
+                }
+            double S[3][3], C[6][6];
+            material_eval(A.material, lam, mu, F, S, C);
+            bool nan = false;
+            // residual contribution of this quadrature point: c (F S)_iJ g_N,J
+            double P[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int J = 0; J < 3; ++J) P[i][J] = F[i][0] * S[0][J] + F[i][1] * S[1][J] + F[i][2] * S[2][J];
+#pragma unroll
+            for (int N = 0; N < 8; ++N)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const double v = (P[i][0] * g[N][0] + P[i][1] * g[N][1] + P[i][2] * g[N][2]) * c;
+                    nan |= !(v == v);
+                    sfq[((q * 8 + N) * 3 + i) * EPB + el] = v;
+                }
+            if (valid && nan) atomicOr(A.flags, 2);
+            // effective elasticity A[iJ][kL] = d_ik S_JL + F_iA C_V(A,J)V(B,L) F_kB
+            for (int i = 0; i < 3; ++i)
+                for (int J = 0; J < 3; ++J)
+                    for (int k = 0; k < 3; ++k)
+                        for (int L = 0; L < 3; ++L) {
+                            double s = (i == k) ? S[J][L] : 0.0;
+                            for (int Aa = 0; Aa < 3; ++Aa) {
+                                const int v1 = voigt(Aa, J);
+                                double t = 0.0;
+                                for (int B = 0; B < 3; ++B) t += C[v1][voigt(B, L)] * F[k][B];
+                                s += F[i][Aa] * t;
+                            }
+                            sA[((q * 81) + ((i * 3 + J) * 9 + k * 3 + L)) * EPB + el] = R(s);
+                        }
+        }
+    }
+    __syncthreads();
+    // ---- phase 2: row node M = role
+    const int M = role;
+    R acc[8][9];
+#pragma unroll
+    for (int N = 0; N < 8; ++N)
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[N][t] = R(0);
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+        const R c = sc[q * EPB + el];
+        R gM[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) gM[a] = sg[((q * 8 + M) * 3 + a) * EPB + el];
+        if (!A.general) {
+            const R cl = c * R(lam), cm = c * R(mu);
+            R a_[3], b_[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) { a_[i] = cl * gM[i]; b_[i] = cm * gM[i]; }
+#pragma unroll
+            for (int N = 0; N < 8; ++N) {
+                if (N < M) continue;
+                R gN[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) gN[a] = sg[((q * 8 + N) * 3 + a) * EPB + el];
+                const R db = b_[0] * gN[0] + b_[1] * gN[1] + b_[2] * gN[2];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) acc[N][i * 3 + k] += a_[i] * gN[k] + b_[k] * gN[i] + (i == k ? db : R(0));
+            }
+        } else {
+            // h[i][k][L] = c sum_J gM_J A[iJ][kL]
+            R h[3][3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                    for (int L = 0; L < 3; ++L) {
+                        R s = R(0);
+#pragma unroll
+                        for (int J = 0; J < 3; ++J) s += gM[J] * sA[((q * 81) + ((i * 3 + J) * 9 + k * 3 + L)) * EPB + el];
+                        h[i][k][L] = s * c;
+                    }
+#pragma unroll
+            for (int N = 0; N < 8; ++N) {
+                if (N < M) continue;
+                R gN[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) gN[a] = sg[((q * 8 + N) * 3 + a) * EPB + el];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) acc[N][i * 3 + k] += h[i][k][0] * gN[0] + h[i][k][1] * gN[1] + h[i][k][2] * gN[2];
+            }
+        }
+    }
+    if (!valid) return;
+    R* SK = (R*)A.stageK;
+#pragma unroll
+    for (int N = 0; N < 8; ++N) {
+        if (N < M) continue;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int a = 3 * M + i, b = 3 * N + k;
+                if (a <= b) SK[(size_t)upidx(a, b, NLOC) * E + e] = acc[N][i * 3 + k];
+            }
+    }
+    // forces of row node M: -(internal) + body
+    double fe[3] = {0.0, 0.0, 0.0};
+    if (A.general && A.with_residual) {
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) fe[i] -= sfq[((q * 8 + M) * 3 + i) * EPB + el];
+    }
+    if (A.fnodal) {
+        for (int q = 0; q < 8; ++q) {
+            double f[3] = {0, 0, 0};
+            for (int i = 0; i < 8; ++i) {
+                const int node = A.conn[i * E + e];
+                for (int d = 0; d < 3; ++d) f[d] += T.N[q][i] * A.fnodal[(size_t)node * 3 + d];
+            }
+            // detJ w = c (recomputed in FP64 from the geometry)
+            double X[8][3], Ji[3][3];
+            for (int i = 0; i < 8; ++i)
+                for (int d = 0; d < 3; ++d) X[i][d] = sX[(i * 3 + d) * EPB + el];
+            const double c = jac<8, 3>(X, T.dN[q], Ji) * T.w[q];
+            for (int d = 0; d < 3; ++d) fe[d] += f[d] * T.phi[q][M] * c;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) A.stageF[(size_t)(3 * M + i) * E + e] = fe[i];
+}
+
+// ---------------------------------------------------------------------------
+// Neumann tractions (base/asmb/NeumannForce.hpp:132-174): one thread per
+// element owning Neumann faces; f_s += t phi_s(xi(eta)) w |J_s|.
+template <int NF, int NCOMP>
+struct FaceArgs {
+    int nelem, n_neu, nfaces, nsq, nfv, dim;
+    const double* X;
+    const int32_t* conn;
+    const int32_t* neu_elem;
+    const int32_t* neu_off;
+    const int32_t* neu_face;
+    const double* trac;
+    double* stageF;
+    int fv[6][4];
+    double w[9];
+    double dS[9][4][2];
+    double phi[6][9][NF];
+};
+
+template <int NF, int NCOMP, int NG, int D>
+__global__ void k_neumann(const FaceArgs<NF, NCOMP> A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.n_neu) return;
+    const int e = A.neu_elem[k];
+    const int E = A.nelem;
+    double fe[NF][NCOMP];
+    for (int s = 0; s < NF; ++s)
+        for (int c = 0; c < NCOMP; ++c) fe[s][c] = 0.0;
+    for (int j = A.neu_off[k]; j < A.neu_off[k + 1]; ++j) {
+        const int f = A.neu_face[j];
+        double Xv[4][3];
+        for (int v = 0; v < A.nfv; ++v) {
+            const int node = A.conn[A.fv[f][v] * E + e];
+            for (int d = 0; d < D; ++d) Xv[v][d] = A.X[(size_t)node * D + d];
+        }
+        for (int q = 0; q < A.nsq; ++q) {
+            double Tg[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+            for (int v = 0; v < A.nfv; ++v)
+                for (int d = 0; d < D; ++d)
+                    for (int a = 0; a < D - 1; ++a) Tg[d][a] += Xv[v][d] * A.dS[q][v][a];
+            double len;
+            if (D == 2) len = sqrt(Tg[0][0] * Tg[0][0] + Tg[1][0] * Tg[1][0]);
+            else {
+                const double n0 = Tg[1][0] * Tg[2][1] - Tg[2][0] * Tg[1][1];
+                const double n1 = Tg[2][0] * Tg[0][1] - Tg[0][0] * Tg[2][1];
+                const double n2 = Tg[0][0] * Tg[1][1] - Tg[1][0] * Tg[0][1];
+                len = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+            }
+            for (int s = 0; s < NF; ++s) {
+                const double wgt = A.phi[f][q][s] * A.w[q] * len;
+                for (int c = 0; c < NCOMP; ++c) fe[s][c] += A.trac[j * NCOMP + c] * wgt;
+            }
+        }
+    }
+    for (int s = 0; s < NF; ++s)
+        for (int c = 0; c < NCOMP; ++c) A.stageF[(size_t)(s * NCOMP + c) * E + e] += fe[s][c];
+}
+
+// ---------------------------------------------------------------------------
+// Dirichlet lift over elements that own constrained DOFs:
+//   F[a] -= sum_c K[a][c] g_c,  g_c = constraint (- current value if incremental)
+template <typename R>
+__global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun, int ncomp, const int32_t* edof,
+                       const uint8_t* status, const double* cval, const double* u, int incremental, const R* stageK,
+                       double* stageF) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlift) return;
+    const int e = lift_elem[k];
+    const int nloc = nfun * ncomp;
+    double g[30];
+    bool act[30];
+    bool any = false;
+    for (int a = 0; a < nloc; ++a) {
+        const size_t kk = (size_t)edof[(a / ncomp) * nelem + e] * ncomp + a % ncomp;
+        act[a] = status[kk] == 0;
+        g[a] = act[a] ? 0.0 : (incremental ? cval[kk] - u[kk] : cval[kk]);
+        any |= (g[a] != 0.0);
+    }
+    if (!any) return;
+    for (int a = 0; a < nloc; ++a) {
+        if (!act[a]) continue;
+        double s = 0.0;
+        for (int b = 0; b < nloc; ++b) {
+            if (act[b] || g[b] == 0.0) continue;
+            const int uidx = a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc);
+            s += (double)stageK[(size_t)uidx * nelem + e] * g[b];
+        }
+        stageF[(size_t)a * nelem + e] -= s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// gather: CSR value of slot s = sum of its staged contributions, in element order
+template <typename RS>
+__global__ void k_gather_mat(int nnz, const int32_t* __restrict__ seg, const int32_t* __restrict__ src,
+                             const RS* __restrict__ stage, double* __restrict__ v64, float* __restrict__ v32) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nnz; s += gridDim.x * blockDim.x) {
+        const int lo = seg[s], hi = seg[s + 1];
+        RS acc = RS(0);
+        for (int k = lo; k < hi; ++k) acc += stage[src[k]];
+        if (v64) v64[s] = (double)acc;
+        if (v32) v32[s] = (float)acc;
+    }
+}
+
+__global__ void k_gather_vec(int neq, const int32_t* __restrict__ seg, const int32_t* __restrict__ src,
+                             const double* __restrict__ stageF, double* __restrict__ rhs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < neq; i += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int k = seg[i]; k < seg[i + 1]; ++k) acc += stageF[src[k]];
+        rhs[i] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pattern build kernels
+__device__ inline int local_eq(const int32_t* edof, const int32_t* eq, int nelem, int ncomp, int e, int a) {
+    return eq[(size_t)edof[(a / ncomp) * nelem + e] * ncomp + a % ncomp];
+}
+
+__global__ void k_gen_pairs(int nelem, int ncomp, int nloc, const int32_t* edof, const int32_t* eq, uint64_t* keys,
+                            int32_t* vals, unsigned long long* nvalid) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nelem * nloc) return;
+    const int e = (int)(t / nloc), a = (int)(t % nloc);
+    const int qa = local_eq(edof, eq, nelem, ncomp, e, a);
+    int cnt = 0;
+    for (int b = 0; b < nloc; ++b) {
+        const int qb = local_eq(edof, eq, nelem, ncomp, e, b);
+        const size_t idx = ((size_t)e * nloc + a) * nloc + b;  // element-major: stable sort keeps element order
+        if (qa >= 0 && qb >= 0) {
+            keys[idx] = ((uint64_t)(uint32_t)qa << 32) | (uint32_t)qb;
+            vals[idx] = (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc)) * nelem + e;
+            ++cnt;
+        } else {
+            keys[idx] = ~0ull;
+            vals[idx] = -1;
+        }
+    }
+    if (cnt) atomicAdd(nvalid, (unsigned long long)cnt);
+}
+
+__global__ void k_heads(long long n, const uint64_t* keys, int32_t* flag) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_fill_csr(long long n, const uint64_t* keys, const int32_t* flag, const int32_t* slot, int32_t* colind,
+                           int32_t* seg, int32_t* rowptr, int32_t* diag) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    const int s = slot[i];
+    const uint32_t row = (uint32_t)(keys[i] >> 32), col = (uint32_t)(keys[i] & 0xffffffffu);
+    colind[s] = (int32_t)col;
+    seg[s] = (int32_t)i;
+    if (i == 0 || (uint32_t)(keys[i - 1] >> 32) != row) rowptr[row] = s;
+    if (row == col) diag[row] = s;
+}
+
+__global__ void k_gen_vec(int nelem, int ncomp, int nloc, const int32_t* edof, const int32_t* eq, uint32_t* keys,
+                          int32_t* vals) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nelem * nloc) return;
+    const int e = (int)(t / nloc), a = (int)(t % nloc);
+    const int q = local_eq(edof, eq, nelem, ncomp, e, a);
+    keys[t] = q >= 0 ? (uint32_t)q : 0xffffffffu;
+    vals[t] = a * nelem + e;
+}
+
+__global__ void k_seg_vec(long long n, const uint32_t* keys, int32_t* seg) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (keys[i] == 0xffffffffu) return;
+    if (i == 0 || keys[i] != keys[i - 1]) seg[keys[i]] = (int32_t)i;
+}
+
+static int bits_for(uint64_t v) {
+    int b = 1;
+    while ((1ull << b) <= v) ++b;
+    return b;
+}
+
+static inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+int pattern_build(isl_ctx* c) {
+    cudaStream_t st = c->stream;
+    cudaEvent_t t0 = c->ev[0], t1 = c->ev[1];
+    cudaEventRecord(t0, st);
+    const int E = (int)c->nelem, nloc = c->nloc;
+    const long long npairs = (long long)E * nloc * nloc;
+    if (npairs >= (1ll << 31)) ISL_FAIL(c, ISL_ERR_ARG, "mesh too large for 32-bit contribution lists");
+    if ((long long)c->nup * E >= (1ll << 31)) ISL_FAIL(c, ISL_ERR_ARG, "mesh too large for 32-bit staging");
+    DBuf<uint64_t> kin, kout;
+    DBuf<int32_t> vin;
+    DBuf<unsigned long long> dcount;
+    ISL_CHECK_CUDA(c, kin.alloc(npairs));
+    ISL_CHECK_CUDA(c, kout.alloc(npairs));
+    ISL_CHECK_CUDA(c, vin.alloc(npairs));
+    ISL_CHECK_CUDA(c, c->dsrc.alloc(npairs));
+    ISL_CHECK_CUDA(c, dcount.alloc(1));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(dcount.p, 0, 8, st));
+    k_gen_pairs<<<nblk((long long)E * nloc, 256), 256, 0, st>>>(E, c->ncomp, nloc, c->dedof.p, c->deq.p, kin.p, vin.p, dcount.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    const int end_bit = 32 + bits_for((uint64_t)c->neq);
+    size_t tmp_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, kin.p, kout.p, vin.p, c->dsrc.p, (int)npairs, 0, end_bit, st);
+    DBuf<unsigned char> tmp;
+    ISL_CHECK_CUDA(c, tmp.alloc(tmp_bytes));
+    ISL_CHECK_CUDA(c, cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, kin.p, kout.p, vin.p, c->dsrc.p, (int)npairs, 0, end_bit, st));
+    unsigned long long nvalid = 0;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&nvalid, dcount.p, 8, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    kin.release();
+    vin.release();
+    c->ncontrib = (int64_t)nvalid;
+    // heads + exclusive scan -> slot ids
+    DBuf<int32_t> flag, slot;
+    ISL_CHECK_CUDA(c, flag.alloc(nvalid));
+    ISL_CHECK_CUDA(c, slot.alloc(nvalid));
+    k_heads<<<nblk(nvalid, 256), 256, 0, st>>>((long long)nvalid, kout.p, flag.p);
+    size_t sb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, sb, flag.p, slot.p, (int)nvalid, st);
+    if (sb > tmp.n) { ISL_CHECK_CUDA(c, tmp.alloc(sb)); }
+    ISL_CHECK_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, sb, flag.p, slot.p, (int)nvalid, st));
+    int32_t last_slot = 0, last_flag = 0;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&last_slot, slot.p + nvalid - 1, 4, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&last_flag, flag.p + nvalid - 1, 4, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    const int64_t nnz = (int64_t)last_slot + last_flag;
+    c->nnz = nnz;
+    ISL_CHECK_CUDA(c, c->dcolind.alloc(nnz));
+    ISL_CHECK_CUDA(c, c->dseg.alloc(nnz + 1));
+    ISL_CHECK_CUDA(c, c->drowptr.alloc(c->neq + 1));
+    ISL_CHECK_CUDA(c, c->ddiag.alloc(c->neq));
+    k_fill_csr<<<nblk(nvalid, 256), 256, 0, st>>>((long long)nvalid, kout.p, flag.p, slot.p, c->dcolind.p, c->dseg.p,
+                                                   c->drowptr.p, c->ddiag.p);
+    const int32_t tail_seg = (int32_t)nvalid, tail_row = (int32_t)nnz;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dseg.p + nnz, &tail_seg, 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->drowptr.p + c->neq, &tail_row, 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    kout.release();
+    flag.release();
+    slot.release();
+    // vector contributions (eq <- element local entries), element order within an equation
+    const long long nv = (long long)E * nloc;
+    DBuf<uint32_t> vk_in, vk_out;
+    DBuf<int32_t> vv_in;
+    ISL_CHECK_CUDA(c, vk_in.alloc(nv));
+    ISL_CHECK_CUDA(c, vk_out.alloc(nv));
+    ISL_CHECK_CUDA(c, vv_in.alloc(nv));
+    ISL_CHECK_CUDA(c, c->dsrcF.alloc(nv));
+    ISL_CHECK_CUDA(c, c->dsegF.alloc(c->neq + 1));
+    k_gen_vec<<<nblk(nv, 256), 256, 0, st>>>(E, c->ncomp, nloc, c->dedof.p, c->deq.p, vk_in.p, vv_in.p);
+    size_t vb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, vb, vk_in.p, vk_out.p, vv_in.p, c->dsrcF.p, (int)nv, 0, 32, st);
+    if (vb > tmp.n) { ISL_CHECK_CUDA(c, tmp.alloc(vb)); }
+    ISL_CHECK_CUDA(c, cub::DeviceRadixSort::SortPairs(tmp.p, vb, vk_in.p, vk_out.p, vv_in.p, c->dsrcF.p, (int)nv, 0, 32, st));
+    k_seg_vec<<<nblk(nv, 256), 256, 0, st>>>(nv, vk_out.p, c->dsegF.p);
+    // number of valid vector contributions = position of the first invalid key
+    int64_t nvF = 0;
+    {
+        std::vector<int32_t> dummy;
+        // count on host via the total of active local entries
+        std::vector<int32_t> heq = c->heq;
+        for (int64_t e = 0; e < c->nelem; ++e)
+            for (int a = 0; a < nloc; ++a)
+                if (heq[(size_t)c->hedof[e * c->nfun + a / c->ncomp] * c->ncomp + a % c->ncomp] >= 0) ++nvF;
+    }
+    c->ncontribF = nvF;
+    const int32_t tailF = (int32_t)nvF;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dsegF.p + c->neq, &tailF, 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    cudaEventRecord(t1, st);
+    cudaEventSynchronize(t1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    c->tms[ISL_T_PATTERN] = ms;
+    c->tcount[ISL_T_PATTERN] = 1;
+    // staging + system buffers
+    ISL_CHECK_CUDA(c, c->dstageF.alloc((size_t)nloc * E));
+    ISL_CHECK_CUDA(c, c->drhs.alloc(c->neq));
+    ISL_CHECK_CUDA(c, c->dsol.alloc(c->neq));
+    c->have64 = c->have32 = false;
+    c->solved = false;
+    return ISL_OK;
+}
+
+// ---------------------------------------------------------------------------
+template <int SHAPE, int FDEG, int NQ>
+static void fill_tab(Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ>& T, const HostTab& h) {
+    constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
+    for (int q = 0; q < NQ; ++q) {
+        T.w[q] = h.w[q];
+        for (int f = 0; f < NF; ++f) {
+            T.phi[q][f] = h.phi[q * NF + f];
+            for (int d = 0; d < D; ++d) T.dphi[q][f][d] = h.dphi[(q * NF + f) * D + d];
+        }
+        for (int i = 0; i < NG; ++i) {
+            T.N[q][i] = h.N[q * NG + i];
+            for (int d = 0; d < D; ++d) T.dN[q][i][d] = h.dN[(q * NG + i) * D + d];
+        }
+    }
+}
+
+template <int SHAPE, int FDEG, int NQ, typename R>
+static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
+    HostTab h;
+    if (!make_host_tables(SHAPE, FDEG, c->qdeg, h) || h.nq != NQ) ISL_FAIL(c, ISL_ERR_ARG, "quadrature");
+    Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T;
+    fill_tab<SHAPE, FDEG, NQ>(T, h);
+    k_laplace<SHAPE, FDEG, NQ, R><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    return ISL_OK;
+}
+
+template <typename R>
+static int dispatch_laplace(isl_ctx* c, const ElemArgs& A) {
+    HostTab h;
+    if (!make_host_tables(c->shape, c->fedeg, c->qdeg, h)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
+    const int nq = h.nq;
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && nq == 4) return launch_laplace<ISL_QUAD, 1, 4, R>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && nq == 9) return launch_laplace<ISL_QUAD, 1, 9, R>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && nq == 9) return launch_laplace<ISL_QUAD, 2, 9, R>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && nq == 4) return launch_laplace<ISL_QUAD, 2, 4, R>(c, A);
+    if (c->shape == ISL_HEX && c->fedeg == 1 && nq == 8) return launch_laplace<ISL_HEX, 1, 8, R>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 2 && nq == 4) return launch_laplace<ISL_TET, 2, 4, R>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 1 && nq == 1) return launch_laplace<ISL_TET, 1, 1, R>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 1 && nq == 4) return launch_laplace<ISL_TET, 1, 4, R>(c, A);
+    ISL_FAIL(c, ISL_ERR_ARG, "Laplace: unsupported element / quadrature combination");
+}
+
+template <typename R>
+static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
+    if (!(c->shape == ISL_HEX && c->fedeg == 1)) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: only trilinear hexahedra on the device");
+    HostTab h;
+    if (!make_host_tables(ISL_HEX, 1, c->qdeg, h) || h.nq != 8) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: 2x2x2 quadrature required");
+    Tab<3, 8, 8, 8> T;
+    fill_tab<ISL_HEX, 1, 8>(T, h);
+    constexpr int EPB = 32;
+    const size_t base = (size_t)8 * 3 * EPB * 8 * 2;
+    size_t smem = base + (A.general ? (size_t)8 * 8 * 3 * EPB * 8 : 0) + (size_t)8 * 8 * 3 * EPB * sizeof(R) +
+                  (size_t)8 * EPB * sizeof(R) + (A.general ? (size_t)8 * 81 * EPB * sizeof(R) : 0);
+    int epb_run = EPB;
+    if (smem > 200 * 1024) {
+        // general FP64: halve the elements per block
+        constexpr int EPB2 = 16;
+        size_t smem2 = (size_t)8 * 3 * EPB2 * 8 * 2 + (size_t)8 * 8 * 3 * EPB2 * 8 + (size_t)8 * 8 * 3 * EPB2 * sizeof(R) +
+                       (size_t)8 * EPB2 * sizeof(R) + (size_t)8 * 81 * EPB2 * sizeof(R);
+        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(k_hyper_hex8<R, EPB2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        k_hyper_hex8<R, EPB2><<<nblk(c->nelem, EPB2), EPB2 * 8, smem2, c->stream>>>(A, T);
+        epb_run = EPB2;
+    } else {
+        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(k_hyper_hex8<R, EPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_hyper_hex8<R, EPB><<<nblk(c->nelem, EPB), EPB * 8, smem, c->stream>>>(A, T);
+    }
+    (void)epb_run;
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    return ISL_OK;
+}
+
+template <int NF, int NCOMP, int NG, int D>
+static int launch_neumann(isl_ctx* c) {
+    FaceTab ft;
+    if (!make_face_tables(c->shape, c->fedeg, c->sqdeg, ft) || ft.nf != NF || ft.nsq > 9)
+        ISL_FAIL(c, ISL_ERR_ARG, "Neumann tables");
+    FaceArgs<NF, NCOMP> A;
+    memset(&A, 0, sizeof(A));
+    A.nelem = (int)c->nelem; A.n_neu = (int)c->n_neu_elem; A.nfaces = ft.nfaces; A.nsq = ft.nsq; A.nfv = ft.nfv; A.dim = D;
+    A.X = c->dX.p; A.conn = c->dconn.p; A.neu_elem = c->dneu_elem.p; A.neu_off = c->dneu_off.p; A.neu_face = c->dneu_face.p;
+    A.trac = c->dneu_trac.p; A.stageF = c->dstageF.p;
+    for (int f = 0; f < ft.nfaces; ++f)
+        for (int v = 0; v < ft.nfv; ++v) A.fv[f][v] = ft.fv[f * ft.nfv + v];
+    for (int q = 0; q < ft.nsq; ++q) {
+        A.w[q] = ft.w[q];
+        for (int v = 0; v < ft.nfv; ++v)
+            for (int a = 0; a < D - 1; ++a) A.dS[q][v][a] = ft.dS[(q * ft.nfv + v) * (D - 1) + a];
+    }
+    for (int f = 0; f < ft.nfaces; ++f)
+        for (int q = 0; q < ft.nsq; ++q)
+            for (int s = 0; s < NF; ++s) A.phi[f][q][s] = ft.phi[(f * ft.nsq + q) * NF + s];
+    k_neumann<NF, NCOMP, NG, D><<<nblk(c->n_neu_elem, 64), 64, 0, c->stream>>>(A);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    return ISL_OK;
+}
+
+static int dispatch_neumann(isl_ctx* c) {
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && c->ncomp == 1) return launch_neumann<4, 1, 4, 2>(c);
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && c->ncomp == 2) return launch_neumann<4, 2, 4, 2>(c);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && c->ncomp == 1) return launch_neumann<9, 1, 4, 2>(c);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && c->ncomp == 2) return launch_neumann<9, 2, 4, 2>(c);
+    if (c->shape == ISL_HEX && c->fedeg == 1 && c->ncomp == 1) return launch_neumann<8, 1, 8, 3>(c);
+    if (c->shape == ISL_HEX && c->fedeg == 1 && c->ncomp == 3) return launch_neumann<8, 3, 8, 3>(c);
+    ISL_FAIL(c, ISL_ERR_ARG, "Neumann: unsupported element");
+}
+
+int assemble_device(isl_ctx* c, int precision, int incremental, int with_residual) {
+    cudaStream_t st = c->stream;
+    const int E = (int)c->nelem;
+    // the tangent (stiffness) is staged in FP32 only for ISL_PREC_FP32
+    const bool k32 = (precision == ISL_PREC_FP32);
+    if (k32) {
+        ISL_CHECK_CUDA(c, c->dstageK32.alloc((size_t)c->nup * E));
+    } else {
+        ISL_CHECK_CUDA(c, c->dstageK64.alloc((size_t)c->nup * E));
+    }
+    if (precision != ISL_PREC_FP32) ISL_CHECK_CUDA(c, c->dval64.alloc(c->nnz));
+    if (precision != ISL_PREC_FP64) ISL_CHECK_CUDA(c, c->dval32.alloc(c->nnz));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p, 0, sizeof(int), st));
+    if (c->timing) cudaEventRecord(c->ev[0], st);
+    ElemArgs A;
+    A.nelem = E;
+    A.X = c->dX.p;
+    A.conn = c->dconn.p;
+    A.edof = c->dedof.p;
+    A.coef = c->dcoef.p;
+    A.u = c->du.p;
+    A.fnodal = c->has_body ? c->dfnodal.p : nullptr;
+    A.with_residual = with_residual && c->u_nonzero;
+    A.general = c->u_nonzero ? 1 : 0;
+    A.material = c->material;
+    A.stageK = k32 ? (void*)c->dstageK32.p : (void*)c->dstageK64.p;
+    A.stageF = c->dstageF.p;
+    A.flags = c->dflags.p;
+    int rc;
+    if (c->kernel == ISL_KERNEL_LAPLACE) rc = k32 ? dispatch_laplace<float>(c, A) : dispatch_laplace<double>(c, A);
+    else rc = k32 ? dispatch_hyper<float>(c, A) : dispatch_hyper<double>(c, A);
+    if (rc != ISL_OK) return rc;
+    if (c->n_neu_elem > 0) {
+        rc = dispatch_neumann(c);
+        if (rc != ISL_OK) return rc;
+    }
+    if (c->n_lift > 0) {
+        if (k32)
+            k_lift<float><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
+                                                              c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK32.p, c->dstageF.p);
+        else
+            k_lift<double><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
+                                                               c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK64.p, c->dstageF.p);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+    }
+    if (c->timing) cudaEventRecord(c->ev[1], st);
+    const unsigned gblocks = (unsigned)std::min<long long>(nblk(c->nnz, 256), (long long)c->sm_count * 8);
+    if (k32)
+        k_gather_mat<float><<<gblocks, 256, 0, st>>>((int)c->nnz, c->dseg.p, c->dsrc.p, c->dstageK32.p, nullptr, c->dval32.p);
+    else
+        k_gather_mat<double><<<gblocks, 256, 0, st>>>((int)c->nnz, c->dseg.p, c->dsrc.p, c->dstageK64.p, c->dval64.p,
+                                                      precision == ISL_PREC_MIXED ? c->dval32.p : nullptr);
+    const unsigned vblocks = (unsigned)std::min<long long>(nblk(c->neq, 256), (long long)c->sm_count * 8);
+    k_gather_vec<<<vblocks, 256, 0, st>>>((int)c->neq, c->dsegF.p, c->dsrcF.p, c->dstageF.p, c->drhs.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    if (c->timing) cudaEventRecord(c->ev[2], st);
+    int flags = 0;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&flags, c->dflags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    if (c->timing) {
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        c->tms[ISL_T_ELEMENT] += a; c->tcount[ISL_T_ELEMENT]++;
+        c->tms[ISL_T_GATHER] += b; c->tcount[ISL_T_GATHER]++;
+    }
+    c->have64 = (precision != ISL_PREC_FP32);
+    c->have32 = (precision != ISL_PREC_FP64);
+    c->solved = false;
+    if (flags & 2) ISL_FAIL(c, ISL_ERR_NAN, "non-finite stress (det F <= 0?)");
+    if (flags & 1) ISL_FAIL(c, ISL_ERR_DEGENERATE, "element with det J <= 0");
+    return ISL_OK;
+}
+
+}  // namespace isl

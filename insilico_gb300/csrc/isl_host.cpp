@@ -1,0 +1,849 @@
+// Host side of the GB300 assembly + Krylov library: context lifetime, the DOF
+// pipeline (DOF-object ids, boundary, constraints, numbering), reference
+// element tables, coefficient upload and the extern "C" entry points of
+// include/isl_gpu.h.  Device work lives in isl_assembly.cu and isl_solver.cu.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "isl_internal.h"
+
+using isl::DBuf;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Reference elements.  Functions are ordered hierarchically (vertices, edge
+// interiors, face interiors, cell interior), the order the reference uses for
+// Lagrange elements (base/mesh/HierarchicOrder.hpp:161-454).
+
+int sdim(int shape) { return shape == ISL_QUAD ? 2 : 3; }
+
+// 1-D Lagrange basis on [0,1] at equidistant nodes 0, 1/k, .., 1
+void lagrange1(int k, double x, double* v, double* d) {
+    if (k == 1) {
+        v[0] = 1.0 - x; v[1] = x;
+        d[0] = -1.0; d[1] = 1.0;
+    } else {  // k == 2, nodes 0, 1/2, 1
+        v[0] = (1.0 - x) * (1.0 - 2.0 * x); d[0] = 4.0 * x - 3.0;
+        v[1] = 4.0 * x * (1.0 - x);         d[1] = 4.0 - 8.0 * x;
+        v[2] = x * (2.0 * x - 1.0);         d[2] = 4.0 * x - 1.0;
+    }
+}
+
+// hierarchic position of every tensor-product node (multi-index i with the
+// first coordinate fastest), for degree k in 2-D or 3-D
+std::vector<int> cube_positions(int dim, int k) {
+    const int n1 = k + 1;
+    const int total = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+    std::vector<int> pos(total, -1);
+    auto lin = [&](int i, int j, int l) { return i + n1 * (j + n1 * l); };
+    int c = 0;
+    if (dim == 2) {
+        const int cx[4] = {0, k, k, 0}, cy[4] = {0, 0, k, k};
+        for (int v = 0; v < 4; ++v) pos[lin(cx[v], cy[v], 0)] = c++;
+        for (int e = 0; e < 4; ++e) {  // edges v -> v+1, walked from the first vertex
+            const int a = e, b = (e + 1) % 4;
+            for (int t = 1; t < k; ++t) {
+                const int x = cx[a] + (cx[b] - cx[a]) / k * t, y = cy[a] + (cy[b] - cy[a]) / k * t;
+                pos[lin(x, y, 0)] = c++;
+            }
+        }
+        for (int j = 1; j < k; ++j)
+            for (int i = 1; i < k; ++i) pos[lin(i, j, 0)] = c++;
+        return pos;
+    }
+    const int cx[8] = {0, k, k, 0, 0, k, k, 0}, cy[8] = {0, 0, k, k, 0, 0, k, k}, cz[8] = {0, 0, 0, 0, k, k, k, k};
+    for (int v = 0; v < 8; ++v) pos[lin(cx[v], cy[v], cz[v])] = c++;
+    const int E[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+    for (auto& ed : E)
+        for (int t = 1; t < k; ++t) {
+            const int a = ed[0], b = ed[1];
+            pos[lin(cx[a] + (cx[b] - cx[a]) / k * t, cy[a] + (cy[b] - cy[a]) / k * t, cz[a] + (cz[b] - cz[a]) / k * t)] = c++;
+        }
+    const int F[6][3] = {{0, 1, 3}, {4, 5, 7}, {0, 1, 4}, {1, 2, 5}, {2, 3, 6}, {3, 0, 7}};  // origin, u-end, v-end
+    for (auto& f : F)
+        for (int t2 = 1; t2 < k; ++t2)
+            for (int t1 = 1; t1 < k; ++t1) {
+                const int o = f[0], u = f[1], w = f[2];
+                const int x = cx[o] + (cx[u] - cx[o]) / k * t1 + (cx[w] - cx[o]) / k * t2;
+                const int y = cy[o] + (cy[u] - cy[o]) / k * t1 + (cy[w] - cy[o]) / k * t2;
+                const int z = cz[o] + (cz[u] - cz[o]) / k * t1 + (cz[w] - cz[o]) / k * t2;
+                pos[lin(x, y, z)] = c++;
+            }
+    for (int l = 1; l < k; ++l)
+        for (int j = 1; j < k; ++j)
+            for (int i = 1; i < k; ++i) pos[lin(i, j, l)] = c++;
+    return pos;
+}
+
+// values + gradients of the degree-k Lagrange element of a shape at xi
+void element_eval(int shape, int k, const double* xi, std::vector<double>& v, std::vector<double>& g, int& nf) {
+    if (shape == ISL_TET) {
+        const double b1 = xi[0], b2 = xi[1], b3 = xi[2], b0 = 1.0 - b1 - b2 - b3;
+        const double db[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        const double b[4] = {b0, b1, b2, b3};
+        if (k == 1) {
+            nf = 4; v.assign(4, 0); g.assign(12, 0);
+            for (int i = 0; i < 4; ++i) { v[i] = b[i]; for (int d = 0; d < 3; ++d) g[i * 3 + d] = db[i][d]; }
+            return;
+        }
+        nf = 10; v.assign(10, 0); g.assign(30, 0);
+        for (int i = 0; i < 4; ++i) {
+            v[i] = b[i] * (2.0 * b[i] - 1.0);
+            for (int d = 0; d < 3; ++d) g[i * 3 + d] = (4.0 * b[i] - 1.0) * db[i][d];
+        }
+        const int P[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};  // mid-edge functions 4..9
+        for (int m = 0; m < 6; ++m) {
+            const int i = P[m][0], j = P[m][1];
+            v[4 + m] = 4.0 * b[i] * b[j];
+            for (int d = 0; d < 3; ++d) g[(4 + m) * 3 + d] = 4.0 * (b[i] * db[j][d] + db[i][d] * b[j]);
+        }
+        return;
+    }
+    const int dim = sdim(shape), n1 = k + 1;
+    double v1[3][3], d1[3][3];
+    for (int d = 0; d < dim; ++d) lagrange1(k, xi[d], v1[d], d1[d]);
+    const std::vector<int> pos = cube_positions(dim, k);
+    nf = (int)pos.size();
+    v.assign(nf, 0); g.assign(nf * dim, 0);
+    for (int n = 0; n < nf; ++n) {
+        int idx[3] = {n % n1, (n / n1) % n1, n / (n1 * n1)};
+        double val = 1.0;
+        for (int d = 0; d < dim; ++d) val *= v1[d][idx[d]];
+        v[pos[n]] = val;
+        for (int a = 0; a < dim; ++a) {
+            double gg = 1.0;
+            for (int d = 0; d < dim; ++d) gg *= (d == a) ? d1[d][idx[d]] : v1[d][idx[d]];
+            g[pos[n] * dim + a] = gg;
+        }
+    }
+}
+
+// Quadrature: Gauss-Legendre on [0,1] with the reference's 15-digit constants
+// (base/quad/GaussLegendre.hpp:115-134), tensor products with the first
+// coordinate fastest (base/quad/TensorProduct.hpp:123-178), and the
+// tetrahedron rules of base/quad/GaussTetrahedron.hpp:90-111.
+bool quadrature(int shape, int qdeg, std::vector<double>& w, std::vector<double>& x) {
+    w.clear(); x.clear();
+    if (shape == ISL_TET) {
+        if (qdeg <= 1) { w = {0.166666666666666}; x = {0.25, 0.25, 0.25}; return true; }
+        if (qdeg == 2) {
+            const double a = 0.13819660112501051518, b = 0.58541019662496845446, c = 0.04166666666666666667;
+            w = {c, c, c, c};
+            x = {a, a, a, b, a, a, a, b, a, a, a, b};
+            return true;
+        }
+        return false;
+    }
+    std::vector<double> w1, x1;
+    switch ((qdeg + 2) / 2) {
+        case 1: w1 = {1.0}; x1 = {0.5}; break;
+        case 2: w1 = {0.5, 0.5}; x1 = {0.788675134594813, 0.211324865405187}; break;
+        case 3: w1 = {0.277777777777777, 0.444444444444444, 0.277777777777777};
+                x1 = {0.887298334620741, 0.5, 0.112701665379259}; break;
+        default: return false;
+    }
+    const int dim = (shape == 0) ? 1 : sdim(shape);
+    const int n = (int)w1.size();
+    int total = 1;
+    for (int d = 0; d < dim; ++d) total *= n;
+    w.resize(total); x.resize((size_t)total * dim);
+    for (int p = 0; p < total; ++p) {
+        int r = p;
+        double ww = 1.0;
+        for (int d = 0; d < dim; ++d) {
+            const int i = r % n; r /= n;
+            ww = (d == 0) ? w1[i] : ww * w1[i];
+            x[(size_t)p * dim + d] = x1[i];
+        }
+        w[p] = ww;
+    }
+    return true;
+}
+
+}  // namespace
+
+namespace isl {
+
+bool make_host_tables(int shape, int fedeg, int qdeg, HostTab& t) {
+    t = HostTab();
+    if (!quadrature(shape, qdeg, t.w, t.xi)) return false;
+    t.dim = sdim(shape);
+    t.nq = (int)t.w.size();
+    std::vector<double> v, g;
+    int nf = 0, ng = 0;
+    for (int q = 0; q < t.nq; ++q) {
+        const double* xi = &t.xi[(size_t)q * t.dim];
+        element_eval(shape, fedeg, xi, v, g, nf);
+        t.phi.insert(t.phi.end(), v.begin(), v.end());
+        t.dphi.insert(t.dphi.end(), g.begin(), g.end());
+        element_eval(shape, 1, xi, v, g, ng);
+        t.N.insert(t.N.end(), v.begin(), v.end());
+        t.dN.insert(t.dN.end(), g.begin(), g.end());
+    }
+    t.nf = nf;
+    t.ng = ng;
+    return true;
+}
+
+// element face tables (base/mesh/ElementFaces.hpp:282-436)
+static const int kQuadEdges[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+static const int kTetFaces[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
+static const int kHexFaces[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+
+static void vertex_local_coords(int shape, std::vector<double>& c) {
+    if (shape == ISL_QUAD) c = {0, 0, 1, 0, 1, 1, 0, 1};
+    else if (shape == ISL_HEX) c = {0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0, 0, 0, 1, 1, 0, 1, 1, 1, 1, 0, 1, 1};
+    else c = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+}
+
+bool make_face_tables(int shape, int fedeg, int sqdeg, FaceTab& t) {
+    t = FaceTab();
+    t.dim = sdim(shape);
+    std::vector<double> sw, sx;
+    int sshape;
+    if (shape == ISL_QUAD) { t.nfaces = 4; t.nfv = 2; sshape = 0; }
+    else if (shape == ISL_HEX) { t.nfaces = 6; t.nfv = 4; sshape = ISL_QUAD; }
+    else return false;  // triangle faces are not needed by the configured workloads
+    if (!quadrature(sshape, sqdeg, sw, sx)) return false;
+    t.nsq = (int)sw.size();
+    t.w = sw;
+    for (int f = 0; f < t.nfaces; ++f)
+        for (int v = 0; v < t.nfv; ++v) t.fv.push_back(shape == ISL_QUAD ? kQuadEdges[f][v] : kHexFaces[f][v]);
+    std::vector<double> vc;
+    vertex_local_coords(shape, vc);
+    const int sd = t.dim - 1;
+    // surface geometry functions: line [1-e, e] or hierarchic bilinear quad
+    t.dS.assign((size_t)t.nsq * t.nfv * sd, 0.0);
+    std::vector<double> sval((size_t)t.nsq * t.nfv);
+    for (int q = 0; q < t.nsq; ++q) {
+        if (sd == 1) {
+            const double e = sx[q];
+            sval[q * 2 + 0] = 1 - e; sval[q * 2 + 1] = e;
+            t.dS[(q * 2 + 0)] = -1; t.dS[(q * 2 + 1)] = 1;
+        } else {
+            const double a = sx[q * 2], b = sx[q * 2 + 1];
+            const double vv[4] = {(1 - a) * (1 - b), a * (1 - b), a * b, (1 - a) * b};
+            const double da[4] = {-(1 - b), (1 - b), b, -b}, db[4] = {-(1 - a), -a, a, (1 - a)};
+            for (int v = 0; v < 4; ++v) {
+                sval[q * 4 + v] = vv[v];
+                t.dS[(q * 4 + v) * 2 + 0] = da[v];
+                t.dS[(q * 4 + v) * 2 + 1] = db[v];
+            }
+        }
+    }
+    std::vector<double> v, g;
+    int nf = 0;
+    for (int f = 0; f < t.nfaces; ++f)
+        for (int q = 0; q < t.nsq; ++q) {
+            double xi[3] = {0, 0, 0};
+            for (int k = 0; k < t.nfv; ++k) {
+                const int lv = t.fv[f * t.nfv + k];
+                for (int d = 0; d < t.dim; ++d) xi[d] += vc[lv * t.dim + d] * sval[q * t.nfv + k];
+            }
+            element_eval(shape, fedeg, xi, v, g, nf);
+            t.phi.insert(t.phi.end(), v.begin(), v.end());
+        }
+    t.nf = nf;
+    return true;
+}
+
+}  // namespace isl
+
+// ===========================================================================
+// DOF pipeline helpers
+namespace {
+
+int num_vertices(int shape) { return shape == ISL_HEX ? 8 : 4; }
+
+// n-face vertex tables of an element (n = 0 vertices, 1 edges, 2 faces, 3 cell)
+std::vector<std::vector<int>> nfaces(int shape, int n) {
+    static const int tetE[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 1}, {3, 2}};
+    static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+    std::vector<std::vector<int>> t;
+    const int nv = num_vertices(shape);
+    if (n == 0) { for (int v = 0; v < nv; ++v) t.push_back({v}); return t; }
+    if (n == 1) {
+        if (shape == ISL_QUAD) for (auto& e : isl::kQuadEdges) t.push_back({e[0], e[1]});
+        if (shape == ISL_TET) for (auto& e : tetE) t.push_back({e[0], e[1]});
+        if (shape == ISL_HEX) for (auto& e : hexE) t.push_back({e[0], e[1]});
+        return t;
+    }
+    if (n == 2) {
+        if (shape == ISL_QUAD) t.push_back({0, 1, 2, 3});
+        if (shape == ISL_TET) for (auto& f : isl::kTetFaces) t.push_back({f[0], f[1], f[2]});
+        if (shape == ISL_HEX) for (auto& f : isl::kHexFaces) t.push_back({f[0], f[1], f[2], f[3]});
+        return t;
+    }
+    if (n == 3 && shape != ISL_QUAD) {
+        std::vector<int> all(nv);
+        std::iota(all.begin(), all.end(), 0);
+        t.push_back(all);
+    }
+    return t;
+}
+
+// interior DOFs of an n-face of a degree-k Lagrange element
+int interior_dofs(int shape, int k, int n) {
+    if (n == 0) return 1;
+    if (shape == ISL_TET) {
+        if (n == 1) return k - 1;
+        if (n == 2) return (k - 1) * (k - 2) / 2;
+        return (k - 1) * (k - 2) * (k - 3) / 6;
+    }
+    int r = 1;
+    for (int i = 0; i < n; ++i) r *= (k - 1);
+    return r;
+}
+
+using Key = std::array<int64_t, 4>;
+
+Key face_key(const int64_t* ev, const std::vector<int>& f) {
+    Key k = {INT64_MAX, INT64_MAX, INT64_MAX, INT64_MAX};
+    for (size_t i = 0; i < f.size(); ++i) k[i] = ev[f[i]];
+    std::sort(k.begin(), k.begin() + f.size());
+    return k;
+}
+
+// Group identical faces: returns, for every (element, face) slot, the slot of
+// its first occurrence in element-major order, and the sorted order of keys.
+void group_faces(const std::vector<Key>& keys, std::vector<int64_t>& first, std::vector<int64_t>& order) {
+    const int64_t n = (int64_t)keys.size();
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return keys[a] < keys[b]; });
+    first.assign(n, -1);
+    int64_t i = 0;
+    while (i < n) {
+        int64_t j = i;
+        while (j < n && keys[order[j]] == keys[order[i]]) ++j;
+        const int64_t f0 = order[i];  // stable sort: the smallest slot of the group comes first
+        for (int64_t k = i; k < j; ++k) first[order[k]] = f0;
+        i = j;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int isl_ctx_create(isl_ctx** out, int device, void* stream) {
+    if (!out) return ISL_ERR_ARG;
+    *out = nullptr;
+    isl_ctx* c = new isl_ctx();
+    c->device = device;
+    if (device < 0) {  // host-only context: DOF pipeline without a GPU
+        *out = c;
+        return ISL_OK;
+    }
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete c; return ISL_ERR_CUDA; }
+    if (stream) c->stream = (cudaStream_t)stream;
+    else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return ISL_ERR_CUDA; }
+        c->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMallocHost(&c->hscal, sizeof(isl::CGScal)) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    if (c->dflags.alloc(4) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
+    cudaMemsetAsync(c->dflags.p, 0, 4 * sizeof(int), c->stream);
+    *out = c;
+    return ISL_OK;
+}
+
+int isl_ctx_destroy(isl_ctx* c) {
+    if (!c) return ISL_ERR_ARG;
+    if (c->device < 0) { delete c; return ISL_OK; }
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
+    if (c->hscal) cudaFreeHost(c->hscal);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ISL_OK;
+}
+
+const char* isl_last_error(const isl_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int isl_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn) {
+    if (!c) return ISL_ERR_ARG;
+    if (!(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) ISL_FAIL(c, ISL_ERR_ARG, "unsupported shape");
+    if (dim != sdim(shape)) ISL_FAIL(c, ISL_ERR_ARG, "dim does not match shape");
+    if (n_nodes <= 0 || n_elem <= 0 || !X || !conn) ISL_FAIL(c, ISL_ERR_ARG, "empty mesh");
+    if (n_nodes >= INT32_MAX || n_elem >= INT32_MAX) ISL_FAIL(c, ISL_ERR_ARG, "mesh too large for 32-bit ids");
+    c->shape = shape; c->dim = dim; c->nnodes = n_nodes; c->nelem = n_elem;
+    c->ngeom = num_vertices(shape);
+    c->hX.assign(X, X + n_nodes * dim);
+    c->hconn.assign(conn, conn + n_elem * c->ngeom);
+    for (int64_t i = 0; i < n_elem * c->ngeom; ++i)
+        if (conn[i] < 0 || conn[i] >= n_nodes) ISL_FAIL(c, ISL_ERR_ARG, "connectivity out of range");
+    c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false;
+    if (c->device < 0) return ISL_OK;
+    cudaSetDevice(c->device);
+    std::vector<int32_t> soa((size_t)n_elem * c->ngeom);
+    for (int64_t e = 0; e < n_elem; ++e)
+        for (int v = 0; v < c->ngeom; ++v) soa[(size_t)v * n_elem + e] = (int32_t)conn[e * c->ngeom + v];
+    ISL_CHECK_CUDA(c, c->dX.alloc(n_nodes * dim));
+    ISL_CHECK_CUDA(c, c->dconn.alloc(soa.size()));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dX.p, X, n_nodes * dim * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dconn.p, soa.data(), soa.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+// DOF-object ids.  Isoparametric fields copy the node ids
+// (base/dof/copyConnectivity.hpp:33-62); otherwise vertices, edges, faces and
+// cells are numbered by first visit in element order, shared n-faces copying
+// the ids of their first occurrence (base/dof/generateDoFIndicesFromFaces.hpp:169-298).
+int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, int* n_fun) {
+    if (!c || c->nelem == 0) return ISL_ERR_ARG;
+    if (fe_degree < 1 || fe_degree > 3 || ncomp < 1 || ncomp > 3) ISL_FAIL(c, ISL_ERR_ARG, "unsupported field");
+    if (c->shape == ISL_TET && fe_degree > 2) ISL_FAIL(c, ISL_ERR_ARG, "tet degree > 2 unsupported");
+    c->fedeg = fe_degree; c->ncomp = ncomp;
+    const int D = c->dim;
+    int nf = 0;
+    for (int n = 0; n <= D; ++n) nf += (int)nfaces(c->shape, n).size() * interior_dofs(c->shape, fe_degree, n);
+    c->nfun = nf;
+    c->nloc = nf * ncomp;
+    c->nup = c->nloc * (c->nloc + 1) / 2;
+    const int64_t E = c->nelem;
+    c->hedof.assign((size_t)E * nf, -1);
+    if (fe_degree == 1) {
+        int64_t mx = 0;
+        for (int64_t i = 0; i < E * nf; ++i) { c->hedof[i] = c->hconn[i]; mx = std::max(mx, c->hconn[i] + 1); }
+        c->ndofobj = mx;
+    } else {
+        int64_t counter = 0;
+        int begin = 0;
+        for (int n = 0; n <= D; ++n) {
+            const auto tab = nfaces(c->shape, n);
+            const int stride = interior_dofs(c->shape, fe_degree, n);
+            const int nfc = (int)tab.size();
+            if (nfc == 0) continue;
+            if (n < D) {
+                std::vector<Key> keys((size_t)E * nfc);
+                for (int64_t e = 0; e < E; ++e)
+                    for (int f = 0; f < nfc; ++f) keys[e * nfc + f] = face_key(&c->hconn[e * c->ngeom], tab[f]);
+                std::vector<int64_t> first, order;
+                group_faces(keys, first, order);
+                for (int64_t s = 0; s < E * nfc; ++s) {
+                    const int64_t e = s / nfc, f = s % nfc;
+                    const int64_t s0 = first[s];
+                    const int64_t e0 = s0 / nfc, f0 = s0 % nfc;
+                    for (int d = 0; d < stride; ++d) {
+                        int64_t& dst = c->hedof[e * nf + begin + f * stride + d];
+                        dst = (s0 == s) ? counter++ : c->hedof[e0 * nf + begin + f0 * stride + d];
+                    }
+                }
+            } else {
+                for (int64_t e = 0; e < E; ++e)
+                    for (int d = 0; d < nfc * stride; ++d) c->hedof[e * nf + begin + d] = counter++;
+            }
+            begin += nfc * stride;
+        }
+        c->ndofobj = counter;
+    }
+    const size_t ndc = (size_t)c->ndofobj * ncomp;
+    c->status.assign(ndc, 0);
+    c->cval.assign(ndc, 0.0);
+    c->hu.assign(ndc, 0.0);
+    c->heq.assign(ndc, -1);
+    c->numbered = false;
+    c->u_nonzero = false;
+    c->nnz = 0;
+    if (n_dofobj) *n_dofobj = c->ndofobj;
+    if (n_fun) *n_fun = nf;
+    if (c->device < 0) return ISL_OK;
+    std::vector<int32_t> soa((size_t)E * nf);
+    for (int64_t e = 0; e < E; ++e)
+        for (int f = 0; f < nf; ++f) soa[(size_t)f * E + e] = (int32_t)c->hedof[e * nf + f];
+    ISL_CHECK_CUDA(c, c->dedof.alloc(soa.size()));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dedof.p, soa.data(), soa.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, c->du.alloc(ndc));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->du.p, 0, ndc * sizeof(double), c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (n_dofobj) *n_dofobj = c->ndofobj;
+    if (n_fun) *n_fun = nf;
+    return ISL_OK;
+}
+
+int isl_field_elem_dofobj(isl_ctx* c, int64_t* out) {
+    if (!c || !c->fedeg || !out) return ISL_ERR_ARG;
+    std::copy(c->hedof.begin(), c->hedof.end(), out);
+    return ISL_OK;
+}
+
+static void boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) {
+    const auto tab = nfaces(c->shape, c->dim - 1);
+    const int nfc = (int)tab.size();
+    const int64_t E = c->nelem;
+    std::vector<Key> keys((size_t)E * nfc);
+    for (int64_t e = 0; e < E; ++e)
+        for (int f = 0; f < nfc; ++f) keys[e * nfc + f] = face_key(&c->hconn[e * c->ngeom], tab[f]);
+    std::vector<int64_t> first, order;
+    group_faces(keys, first, order);
+    out.clear();
+    const int64_t n = (int64_t)order.size();
+    int64_t i = 0;
+    while (i < n) {
+        int64_t j = i;
+        while (j < n && keys[order[j]] == keys[order[i]]) ++j;
+        if (j - i == 1) out.push_back({order[i] / nfc, (int)(order[i] % nfc)});
+        i = j;
+    }
+}
+
+int isl_boundary_faces(isl_ctx* c, int64_t* n, int64_t* elem, int* face) {
+    if (!c || !c->nelem || !n) return ISL_ERR_ARG;
+    std::vector<std::pair<int64_t, int>> bf;
+    boundary_list(c, bf);
+    *n = (int64_t)bf.size();
+    if (elem && face)
+        for (size_t i = 0; i < bf.size(); ++i) { elem[i] = bf[i].first; face[i] = bf[i].second; }
+    return ISL_OK;
+}
+
+// local FE positions on a boundary face: its vertices, interior DOFs of the
+// element edges inside the face, and (3-D) the face's own interior DOFs
+static std::vector<int> face_local_dofs(isl_ctx* c, int face) {
+    const auto ftab = nfaces(c->shape, c->dim - 1);
+    const std::vector<int>& fv = ftab[face];
+    std::vector<int> out(fv.begin(), fv.end());
+    if (c->fedeg == 1) return out;
+    int begin = num_vertices(c->shape);
+    const auto etab = nfaces(c->shape, 1);
+    const int es = interior_dofs(c->shape, c->fedeg, 1);
+    for (size_t ed = 0; ed < etab.size(); ++ed) {
+        const bool in0 = std::find(fv.begin(), fv.end(), etab[ed][0]) != fv.end();
+        const bool in1 = std::find(fv.begin(), fv.end(), etab[ed][1]) != fv.end();
+        if (in0 && in1)
+            for (int d = 0; d < es; ++d) out.push_back(begin + (int)ed * es + d);
+    }
+    begin += (int)etab.size() * es;
+    if (c->dim == 3) {
+        const int fs = interior_dofs(c->shape, c->fedeg, 2);
+        for (int d = 0; d < fs; ++d) out.push_back(begin + face * fs + d);
+    }
+    return out;
+}
+
+int isl_boundary_points(isl_ctx* c, int64_t* n, double* x, int64_t* dofobj) {
+    if (!c || !c->fedeg || !n) return ISL_ERR_ARG;
+    std::vector<std::pair<int64_t, int>> bf;
+    boundary_list(c, bf);
+    // support points: FE nodes on the reference element
+    std::vector<double> sup;
+    {
+        const int D = c->dim;
+        if (c->shape == ISL_TET) {
+            const double tv[10][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {.5, 0, 0},
+                                      {.5, .5, 0}, {0, .5, 0}, {0, 0, .5}, {.5, 0, .5}, {0, .5, .5}};
+            for (int i = 0; i < c->nfun; ++i) for (int d = 0; d < 3; ++d) sup.push_back(tv[i][d]);
+        } else {
+            const int k = c->fedeg, n1 = k + 1;
+            const auto pos = cube_positions(D, k);
+            sup.assign((size_t)c->nfun * D, 0.0);
+            for (size_t m = 0; m < pos.size(); ++m) {
+                int r = (int)m;
+                for (int d = 0; d < D; ++d) { sup[pos[m] * D + d] = double(r % n1) / k; r /= n1; }
+            }
+        }
+    }
+    int64_t cnt = 0;
+    for (auto& ef : bf) {
+        const auto loc = face_local_dofs(c, ef.second);
+        for (int l : loc) {
+            if (x && dofobj) {
+                std::vector<double> v, g;
+                int ng = 0;
+                element_eval(c->shape, 1, &sup[(size_t)l * c->dim], v, g, ng);
+                for (int d = 0; d < c->dim; ++d) {
+                    double s = 0.0;
+                    for (int i = 0; i < ng; ++i) s += c->hX[c->hconn[ef.first * c->ngeom + i] * c->dim + d] * v[i];
+                    x[cnt * c->dim + d] = s;
+                }
+                dofobj[cnt] = c->hedof[ef.first * c->nfun + l];
+            }
+            ++cnt;
+        }
+    }
+    *n = cnt;
+    return ISL_OK;
+}
+
+int isl_constrain(isl_ctx* c, int64_t n, const int64_t* dofobj, const int* comp, const double* value) {
+    if (!c || !c->fedeg || (n > 0 && (!dofobj || !comp || !value))) return ISL_ERR_ARG;
+    for (int64_t i = 0; i < n; ++i) {
+        if (dofobj[i] < 0 || dofobj[i] >= c->ndofobj || comp[i] < 0 || comp[i] >= c->ncomp)
+            ISL_FAIL(c, ISL_ERR_ARG, "constraint index out of range");
+        const size_t k = (size_t)dofobj[i] * c->ncomp + comp[i];
+        if (c->numbered && c->status[k] == 0) ISL_FAIL(c, ISL_ERR_ARG, "cannot constrain an active DOF after numbering");
+        c->status[k] = 1;
+        c->cval[k] = value[i];
+    }
+    if (c->dcval.p) {
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p, c->cval.data(), c->cval.size() * 8, cudaMemcpyHostToDevice, c->stream));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return ISL_OK;
+}
+
+int isl_scale_constraints(isl_ctx* c, double factor) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    for (size_t k = 0; k < c->status.size(); ++k) if (c->status[k]) c->cval[k] *= factor;
+    if (c->dcval.p) {
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p, c->cval.data(), c->cval.size() * 8, cudaMemcpyHostToDevice, c->stream));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return ISL_OK;
+}
+
+// consecutive numbering of ACTIVE components in DOF-object order
+int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    int64_t k = 0;
+    for (size_t i = 0; i < c->status.size(); ++i) c->heq[i] = c->status[i] == 0 ? (int32_t)k++ : -1;
+    if (k >= INT32_MAX) ISL_FAIL(c, ISL_ERR_ARG, "too many DOFs for 32-bit indices");
+    c->neq = k;
+    c->numbered = true;
+    if (n_active) *n_active = k;
+    c->nnz = 0;
+    if (c->device < 0) return ISL_OK;
+    const size_t ndc = c->status.size();
+    ISL_CHECK_CUDA(c, c->deq.alloc(ndc));
+    ISL_CHECK_CUDA(c, c->dstatus.alloc(ndc));
+    ISL_CHECK_CUDA(c, c->dcval.alloc(ndc));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->deq.p, c->heq.data(), ndc * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dstatus.p, c->status.data(), ndc, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p, c->cval.data(), ndc * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (n_active) *n_active = k;
+    c->nnz = 0;
+    return ISL_OK;
+}
+
+int isl_dof_index(isl_ctx* c, int64_t* out) {
+    if (!c || !c->numbered || !out) return ISL_ERR_ARG;
+    for (size_t i = 0; i < c->heq.size(); ++i) out[i] = c->heq[i];
+    return ISL_OK;
+}
+
+int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
+    if (!c || !c->numbered) return ISL_ERR_ARG;
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: the pattern is built on the device");
+    if (c->neq == 0) ISL_FAIL(c, ISL_ERR_ARG, "no active DOFs");
+    cudaSetDevice(c->device);
+    // elements with a constrained local DOF (Dirichlet lift candidates)
+    std::vector<int32_t> lift;
+    for (int64_t e = 0; e < c->nelem; ++e) {
+        bool any = false;
+        for (int f = 0; f < c->nfun && !any; ++f)
+            for (int i = 0; i < c->ncomp; ++i)
+                if (c->status[(size_t)c->hedof[e * c->nfun + f] * c->ncomp + i]) { any = true; break; }
+        if (any) lift.push_back((int32_t)e);
+    }
+    c->n_lift = (int64_t)lift.size();
+    ISL_CHECK_CUDA(c, c->dlift_elem.alloc(lift.size()));
+    if (!lift.empty())
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dlift_elem.p, lift.data(), lift.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    int st = isl::pattern_build(c);
+    if (st != ISL_OK) return st;
+    if (nnz) *nnz = c->nnz;
+    return ISL_OK;
+}
+
+int isl_set_laplace(isl_ctx* c, const double* kappa, int quad_degree) {
+    if (!c || !c->fedeg || !kappa) return ISL_ERR_ARG;
+    if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "Laplace needs a scalar field");
+    c->kernel = ISL_KERNEL_LAPLACE;
+    c->qdeg = quad_degree;
+    ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, kappa, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    return ISL_OK;
+}
+
+int isl_set_hyperelastic(isl_ctx* c, int material, const double* lambda, const double* mu, int quad_degree) {
+    if (!c || !c->fedeg || !lambda || !mu) return ISL_ERR_ARG;
+    if (c->ncomp != c->dim) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic needs ncomp == dim");
+    if (material != ISL_MAT_STVENANT && material != ISL_MAT_NEOHOOKE) ISL_FAIL(c, ISL_ERR_ARG, "material");
+    c->kernel = ISL_KERNEL_HYPERELASTIC;
+    c->material = material;
+    c->qdeg = quad_degree;
+    ISL_CHECK_CUDA(c, c->dcoef.alloc(2 * c->nelem));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, lambda, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p + c->nelem, mu, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    return ISL_OK;
+}
+
+int isl_set_body_force_nodal(isl_ctx* c, const double* f) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    if (!f) { c->has_body = false; return ISL_OK; }
+    ISL_CHECK_CUDA(c, c->dfnodal.alloc(c->nnodes * c->ncomp));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dfnodal.p, f, c->nnodes * c->ncomp * 8, cudaMemcpyHostToDevice, c->stream));
+    c->has_body = true;
+    return ISL_OK;
+}
+
+int isl_set_neumann(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, const double* traction, int squad_degree) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    c->n_neu_elem = 0;
+    if (n <= 0) return ISL_OK;
+    if (!elem || !face || !traction) return ISL_ERR_ARG;
+    if (c->shape == ISL_TET) ISL_FAIL(c, ISL_ERR_ARG, "Neumann faces on tetrahedra are not supported");
+    const int nfc = c->shape == ISL_QUAD ? 4 : 6;
+    std::vector<int64_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    for (int64_t i = 0; i < n; ++i)
+        if (elem[i] < 0 || elem[i] >= c->nelem || face[i] < 0 || face[i] >= nfc) ISL_FAIL(c, ISL_ERR_ARG, "Neumann face out of range");
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return elem[a] < elem[b]; });
+    std::vector<int32_t> el, off, fc;
+    std::vector<double> tr;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t i = idx[k];
+        if (el.empty() || el.back() != elem[i]) { el.push_back((int32_t)elem[i]); off.push_back((int32_t)k); }
+        fc.push_back(face[i]);
+        for (int d = 0; d < c->ncomp; ++d) tr.push_back(traction[i * c->ncomp + d]);
+    }
+    off.push_back((int32_t)n);
+    c->n_neu_elem = (int64_t)el.size();
+    c->sqdeg = squad_degree;
+    ISL_CHECK_CUDA(c, c->dneu_elem.alloc(el.size()));
+    ISL_CHECK_CUDA(c, c->dneu_off.alloc(off.size()));
+    ISL_CHECK_CUDA(c, c->dneu_face.alloc(fc.size()));
+    ISL_CHECK_CUDA(c, c->dneu_trac.alloc(tr.size()));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_elem.p, el.data(), el.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_face.p, fc.data(), fc.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_trac.p, tr.data(), tr.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_set_values(isl_ctx* c, const double* u) {
+    if (!c || !c->fedeg || !u) return ISL_ERR_ARG;
+    const size_t n = (size_t)c->ndofobj * c->ncomp;
+    c->u_nonzero = false;
+    for (size_t i = 0; i < n; ++i) if (u[i] != 0.0) { c->u_nonzero = true; break; }
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->du.p, u, n * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_get_values(isl_ctx* c, double* u) {
+    if (!c || !c->fedeg || !u) return ISL_ERR_ARG;
+    const size_t n = (size_t)c->ndofobj * c->ncomp;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(u, c->du.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) {
+    if (!c || !c->nnz || c->kernel < 0) ISL_FAIL(c, ISL_ERR_ARG, "assemble: pattern or kernel not set");
+    if (precision < ISL_PREC_FP64 || precision > ISL_PREC_MIXED) ISL_FAIL(c, ISL_ERR_ARG, "precision");
+    cudaSetDevice(c->device);
+    return isl::assemble_device(c, precision, incremental, with_residual);
+}
+
+int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res) {
+    if (!c || !c->nnz) ISL_FAIL(c, ISL_ERR_ARG, "solve: nothing assembled");
+    if (method == ISL_SOLVE_CG_FP64 && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "solve: no FP64 matrix assembled");
+    if (method == ISL_SOLVE_CG_FP32_IR && !(c->have64 && c->have32) && !(c->have32 && c->kernel == ISL_KERNEL_HYPERELASTIC))
+        ISL_FAIL(c, ISL_ERR_ARG, "solve: mixed solve needs FP64 and FP32 matrices (ISL_PREC_MIXED)");
+    if (!(tol >= 0.0)) ISL_FAIL(c, ISL_ERR_ARG, "tol");
+    cudaSetDevice(c->device);
+    return isl::solve_device(c, method, tol, max_iter, iters, rel_res);
+}
+
+int isl_get_solution(isl_ctx* c, double* x) {
+    if (!c || !c->nnz || !x) return ISL_ERR_ARG;
+    const double* src = c->solved ? c->dsol.p : c->drhs.p;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(x, src, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_get_rhs(isl_ctx* c, double* b) {
+    if (!c || !c->nnz || !b) return ISL_ERR_ARG;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(b, c->drhs.p, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_norm(isl_ctx* c, double* out) {
+    if (!c || !c->nnz || !out) return ISL_ERR_ARG;
+    std::vector<double> b(c->neq);
+    int st = isl_get_solution(c, b.data());
+    if (st) return st;
+    double s = 0.0;
+    for (double v : b) s += v * v;
+    *out = std::sqrt(s) / (double)c->neq;
+    return ISL_OK;
+}
+
+int isl_distribute(isl_ctx* c, int add) {
+    if (!c || !c->solved) ISL_FAIL(c, ISL_ERR_ARG, "distribute: no solution");
+    cudaSetDevice(c->device);
+    int st = isl::distribute_device(c, add);
+    if (st == ISL_OK) c->u_nonzero = true;
+    return st;
+}
+
+int isl_get_csr(isl_ctx* c, int64_t* rowptr, int64_t* colind, double* values) {
+    if (!c || !c->nnz) return ISL_ERR_ARG;
+    if (rowptr) {
+        std::vector<int32_t> t(c->neq + 1);
+        ISL_CHECK_CUDA(c, cudaMemcpy(t.data(), c->drowptr.p, t.size() * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < t.size(); ++i) rowptr[i] = t[i];
+    }
+    if (colind) {
+        std::vector<int32_t> t(c->nnz);
+        ISL_CHECK_CUDA(c, cudaMemcpy(t.data(), c->dcolind.p, t.size() * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < t.size(); ++i) colind[i] = t[i];
+    }
+    if (values) {
+        if (c->have64) {
+            ISL_CHECK_CUDA(c, cudaMemcpy(values, c->dval64.p, c->nnz * 8, cudaMemcpyDeviceToHost));
+        } else if (c->have32) {
+            std::vector<float> t(c->nnz);
+            ISL_CHECK_CUDA(c, cudaMemcpy(t.data(), c->dval32.p, t.size() * 4, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < t.size(); ++i) values[i] = t[i];
+        } else {
+            ISL_FAIL(c, ISL_ERR_ARG, "no values assembled");
+        }
+    }
+    return ISL_OK;
+}
+
+int isl_sync(isl_ctx* c) {
+    if (!c) return ISL_ERR_ARG;
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_set_timing(isl_ctx* c, int on) {
+    if (!c) return ISL_ERR_ARG;
+    c->timing = on != 0;
+    for (int i = 0; i < ISL_NTIMERS; ++i) { c->tms[i] = 0; c->tcount[i] = 0; }
+    return ISL_OK;
+}
+
+int isl_timings(isl_ctx* c, double* ms, int64_t* counts) {
+    if (!c) return ISL_ERR_ARG;
+    for (int i = 0; i < ISL_NTIMERS; ++i) {
+        if (ms) ms[i] = c->tms[i];
+        if (counts) counts[i] = c->tcount[i];
+    }
+    return ISL_OK;
+}
+
+int isl_time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
+    if (!c || !c->nnz || !ms || nrep <= 0) return ISL_ERR_ARG;
+    return isl::time_spmv(c, precision, nrep, ms);
+}
+
+}  // extern "C"

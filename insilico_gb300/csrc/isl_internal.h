@@ -1,0 +1,202 @@
+// Internal state of an isl_ctx and helpers shared by the host and device
+// translation units of the GB300 assembly + Krylov library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/isl_gpu.h"
+
+namespace isl {
+
+// ---------------------------------------------------------------------------
+// Element traits (geometry degree 1, field degree FDEG)
+template <int SHAPE, int FDEG>
+struct ET;
+template <> struct ET<ISL_QUAD, 1> { static constexpr int D = 2, NG = 4, NF = 4; };
+template <> struct ET<ISL_QUAD, 2> { static constexpr int D = 2, NG = 4, NF = 9; };
+template <> struct ET<ISL_HEX, 1> { static constexpr int D = 3, NG = 8, NF = 8; };
+template <> struct ET<ISL_TET, 1> { static constexpr int D = 3, NG = 4, NF = 4; };
+template <> struct ET<ISL_TET, 2> { static constexpr int D = 3, NG = 4, NF = 10; };
+
+// Reference-element tables handed to the element kernels by value.
+template <int D, int NG, int NF, int NQ>
+struct Tab {
+    double w[NQ];
+    double phi[NQ][NF];
+    double dphi[NQ][NF][D];
+    double N[NQ][NG];
+    double dN[NQ][NG][D];
+};
+
+// Host-side reference tables (any size), filled by shape tables code.
+struct HostTab {
+    int dim = 0, nq = 0, nf = 0, ng = 0;
+    std::vector<double> w, xi, phi, dphi, N, dN;
+};
+bool make_host_tables(int shape, int fedeg, int qdeg, HostTab& t);
+// surface (face) tables for Neumann integration: per local face, per surface qp:
+// FE values of the domain element at the mapped point, weights, and the face
+// geometry function gradients (for the metric)
+struct FaceTab {
+    int nfaces = 0, nsq = 0, nfv = 0, nf = 0, dim = 0;
+    std::vector<int> fv;        // [nfaces][nfv] local vertex ids of the face
+    std::vector<double> w;      // [nsq]
+    std::vector<double> phi;    // [nfaces][nsq][nf]
+    std::vector<double> dS;     // [nsq][nfv][dim-1] face geometry gradients
+};
+bool make_face_tables(int shape, int fedeg, int sqdeg, FaceTab& t);
+
+// ---------------------------------------------------------------------------
+// Device buffer with RAII
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        if (count == n && p) return cudaSuccess;
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        else p = nullptr;
+        return e;
+    }
+};
+
+// CG workspace for one precision
+struct CGWork {
+    void* x = nullptr;  // solution (T)
+    void* r = nullptr;
+    void* p = nullptr;
+    void* q = nullptr;  // A p
+    void* dinv = nullptr;
+    size_t n = 0;
+};
+
+// scalar block shared by the CG kernels (device)
+struct CGScal {
+    double absNew, pAp, alpha, beta, rr, rz, threshold, rhsNorm2;
+    int done;
+    int iters;
+    int bad;
+    int pad;
+    unsigned int ticket1, ticket2;
+};
+
+}  // namespace isl
+
+struct isl_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int sm_count = 0;
+
+    // mesh
+    int shape = 0, dim = 0, ngeom = 0;
+    int64_t nnodes = 0, nelem = 0;
+    std::vector<double> hX;
+    std::vector<int64_t> hconn;  // [nelem][ngeom]
+    isl::DBuf<double> dX;        // [nnodes][dim]
+    isl::DBuf<int32_t> dconn;    // SoA [ngeom][nelem]
+
+    // field
+    int fedeg = 0, ncomp = 0, nfun = 0, nloc = 0, nup = 0;
+    int64_t ndofobj = 0;
+    std::vector<int64_t> hedof;  // [nelem][nfun]
+    isl::DBuf<int32_t> dedof;    // SoA [nfun][nelem]
+    std::vector<uint8_t> status; // per dofobj comp: 0 active, 1 constrained
+    std::vector<double> cval;
+    std::vector<double> hu;      // host mirror of values (valid when u_on_host)
+    std::vector<int32_t> heq;
+    int64_t neq = 0;
+    bool numbered = false;
+    isl::DBuf<int32_t> deq;      // per dofobj comp
+    isl::DBuf<uint8_t> dstatus;
+    isl::DBuf<double> dcval;
+    isl::DBuf<double> du;        // current values per dofobj comp
+    bool u_nonzero = false;
+
+    // kernel data
+    int kernel = -1, material = 0, qdeg = 2, sqdeg = 2;
+    isl::DBuf<double> dcoef;     // SoA [ncoef][nelem]
+    bool has_body = false;
+    isl::DBuf<double> dfnodal;   // [nnodes][ncomp]
+    // Neumann: faces grouped by element
+    int64_t n_neu_elem = 0;
+    isl::DBuf<int32_t> dneu_elem, dneu_off, dneu_face;
+    isl::DBuf<double> dneu_trac;
+    // elements with at least one constrained local DOF (for the Dirichlet lift)
+    int64_t n_lift = 0;
+    isl::DBuf<int32_t> dlift_elem;
+
+    // pattern
+    int64_t nnz = 0, ncontrib = 0, ncontribF = 0;
+    isl::DBuf<int32_t> drowptr, dcolind, ddiag, dseg, dsrc, dsegF, dsrcF;
+    // staged element matrices/vectors (SoA)
+    isl::DBuf<double> dstageK64;
+    isl::DBuf<float> dstageK32;
+    isl::DBuf<double> dstageF;
+    // assembled system
+    isl::DBuf<double> dval64;
+    isl::DBuf<float> dval32;
+    bool have64 = false, have32 = false;
+    isl::DBuf<double> drhs;      // b (FP64)
+    isl::DBuf<double> dsol;      // x (FP64)
+    bool solved = false;
+
+    // status word written by kernels (bit 0: det J <= 0, bit 1: NaN)
+    isl::DBuf<int> dflags;
+
+    // solver workspace
+    isl::DBuf<double> w64;       // FP64 vectors
+    isl::DBuf<float> w32;        // FP32 vectors
+    isl::DBuf<double> dpart;     // block partial sums
+    isl::DBuf<isl::CGScal> dscal;
+    isl::CGScal* hscal = nullptr;  // pinned host mirror
+    int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row
+
+    // timing
+    bool timing = false;
+    double tms[ISL_NTIMERS] = {0};
+    int64_t tcount[ISL_NTIMERS] = {0};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// status helpers
+#define ISL_CHECK_CUDA(ctx, call)                                                        \
+    do {                                                                                 \
+        cudaError_t _e = (call);                                                         \
+        if (_e != cudaSuccess) {                                                         \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(_e);             \
+            return (_e == cudaErrorMemoryAllocation) ? ISL_ERR_NOMEM : ISL_ERR_CUDA;     \
+        }                                                                                \
+    } while (0)
+
+#define ISL_FAIL(ctx, code, msg) \
+    do {                         \
+        (ctx)->err = (msg);      \
+        return (code);           \
+    } while (0)
+
+namespace isl {
+// device-side entry points implemented in the .cu files
+int pattern_build(isl_ctx* c);
+int assemble_device(isl_ctx* c, int precision, int incremental, int with_residual);
+int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
+int distribute_device(isl_ctx* c, int add);
+int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
+}  // namespace isl

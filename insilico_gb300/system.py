@@ -1,0 +1,212 @@
+"""Host-side mirror of the reference's assembly/solver call surface over the C-ABI.
+
+The reference drives one boundary value problem as (reference/06-elastic/
+linearElastic.cpp:80-216, heat/PoissonDriver.hpp:153-210,
+solid/CompressibleDriver.hpp:156-214):
+
+    dof::generate -> MeshBoundary::create -> constrainBoundary ->
+    numberDoFsConsecutively -> Eigen3 solver(N) -> registerFields ->
+    stiffnessMatrixComputation / computeResidualForces / bodyForceComputation /
+    neumannForceComputation -> finishAssembly -> cgSolve -> setDoFsFromSolver
+
+:class:`System` exposes the same steps, each a call into libisl_gpu.so; the
+device keeps mesh, pattern, matrix and iterate resident between calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import IslError
+
+
+class System:
+    """One mesh + field + assembled system on one GPU (an isl_ctx)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        self.L = A.load()
+        h = C.c_void_p()
+        st = self.L.isl_ctx_create(C.byref(h), device, C.c_void_p(stream) if stream else None)
+        if st != A.ISL_OK:
+            raise IslError(st, "isl_ctx_create failed")
+        self.h = h
+        self.neq = 0
+        self.nnz = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.isl_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st, what=""):
+        if st != A.ISL_OK:
+            msg = self.L.isl_last_error(self.h)
+            raise IslError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- mesh / field / DOFs ------------------------------------------------
+    def upload_mesh(self, shape: int, X: np.ndarray, conn: np.ndarray):
+        self.X = np.ascontiguousarray(X, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int64)
+        self.shape, self.dim = shape, self.X.shape[1]
+        self.nnodes, self.nelem = len(self.X), len(self.conn)
+        self._chk(self.L.isl_mesh_upload(self.h, shape, self.dim, self.nnodes, A.d(self.X), self.nelem, A.i64(self.conn)),
+                  "isl_mesh_upload")
+
+    def create_field(self, fe_degree: int, ncomp: int):
+        n = C.c_int64()
+        nf = C.c_int()
+        self._chk(self.L.isl_field_create(self.h, fe_degree, ncomp, C.byref(n), C.byref(nf)), "isl_field_create")
+        self.fedeg, self.ncomp, self.ndofobj, self.nfun = fe_degree, ncomp, n.value, nf.value
+        return self.ndofobj
+
+    def elem_dofobj(self):
+        out = np.zeros((self.nelem, self.nfun), dtype=np.int64)
+        self._chk(self.L.isl_field_elem_dofobj(self.h, A.i64(out)))
+        return out
+
+    def boundary_faces(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_boundary_faces(self.h, C.byref(n), None, None))
+        e = np.zeros(n.value, dtype=np.int64)
+        f = np.zeros(n.value, dtype=np.int32)
+        self._chk(self.L.isl_boundary_faces(self.h, C.byref(n), A.i64(e), A.i32(f)))
+        return e, f
+
+    def boundary_points(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_boundary_points(self.h, C.byref(n), None, None))
+        x = np.zeros((n.value, self.dim))
+        dof = np.zeros(n.value, dtype=np.int64)
+        self._chk(self.L.isl_boundary_points(self.h, C.byref(n), A.d(x), A.i64(dof)))
+        return x, dof
+
+    def constrain(self, dofobj, comp, value):
+        dofobj = np.ascontiguousarray(dofobj, dtype=np.int64)
+        comp = np.ascontiguousarray(comp, dtype=np.int32)
+        value = np.ascontiguousarray(value, dtype=np.float64)
+        self._chk(self.L.isl_constrain(self.h, len(dofobj), A.i64(dofobj), A.i32(comp), A.d(value)), "isl_constrain")
+
+    def constrain_boundary(self, fun: Callable[[np.ndarray], tuple]):
+        """constrainBoundary: fun(x [n,dim]) -> (mask [n, ncomp] bool, values [n, ncomp])."""
+        x, dof = self.boundary_points()
+        mask, vals = fun(x)
+        mask = np.asarray(mask, dtype=bool).reshape(len(x), self.ncomp)
+        vals = np.broadcast_to(np.asarray(vals, dtype=np.float64), mask.shape)
+        rows, comps = np.nonzero(mask)
+        self.constrain(dof[rows], comps, vals[rows, comps])
+
+    def scale_constraints(self, factor: float):
+        self._chk(self.L.isl_scale_constraints(self.h, factor))
+
+    def number_dofs(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_number_dofs(self.h, C.byref(n)), "isl_number_dofs")
+        self.neq = n.value
+        return self.neq
+
+    def dof_index(self):
+        out = np.zeros(self.ndofobj * self.ncomp, dtype=np.int64)
+        self._chk(self.L.isl_dof_index(self.h, A.i64(out)))
+        return out
+
+    def register_pattern(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_register_pattern(self.h, C.byref(n)), "isl_register_pattern")
+        self.nnz = n.value
+        return self.nnz
+
+    # -- kernels / forces ----------------------------------------------------
+    def set_laplace(self, kappa, quad_degree: int):
+        self._kappa = np.ascontiguousarray(kappa, dtype=np.float64)
+        self._chk(self.L.isl_set_laplace(self.h, A.d(self._kappa), quad_degree), "isl_set_laplace")
+
+    def set_hyperelastic(self, material: str, lam, mu, quad_degree: int):
+        m = {"stvenant": A.MAT_STVENANT, "neohooke": A.MAT_NEOHOOKE}[material]
+        self._lam = np.ascontiguousarray(lam, dtype=np.float64)
+        self._mu = np.ascontiguousarray(mu, dtype=np.float64)
+        self._chk(self.L.isl_set_hyperelastic(self.h, m, A.d(self._lam), A.d(self._mu), quad_degree), "isl_set_hyperelastic")
+
+    def set_body_force_nodal(self, f):
+        if f is None:
+            self._chk(self.L.isl_set_body_force_nodal(self.h, None))
+            return
+        self._f = np.ascontiguousarray(f, dtype=np.float64)
+        self._chk(self.L.isl_set_body_force_nodal(self.h, A.d(self._f)), "isl_set_body_force_nodal")
+
+    def set_neumann(self, elem, face, traction, squad_degree: int = 2):
+        e = np.ascontiguousarray(elem, dtype=np.int64)
+        f = np.ascontiguousarray(face, dtype=np.int32)
+        t = np.ascontiguousarray(np.broadcast_to(traction, (len(e), self.ncomp)), dtype=np.float64)
+        self._chk(self.L.isl_set_neumann(self.h, len(e), A.i64(e), A.i32(f), A.d(t), squad_degree), "isl_set_neumann")
+
+    def set_values(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self._chk(self.L.isl_set_values(self.h, A.d(u)))
+
+    def values(self):
+        out = np.zeros(self.ndofobj * self.ncomp)
+        self._chk(self.L.isl_get_values(self.h, A.d(out)))
+        return out
+
+    # -- assembly / solve ------------------------------------------------------
+    def assemble(self, precision: int = A.PREC_FP64, incremental: bool = True, with_residual: bool = False):
+        self._chk(self.L.isl_assemble(self.h, precision, int(incremental), int(with_residual)), "isl_assemble")
+
+    def solve(self, method: int = A.SOLVE_CG_FP64, tol: float = 1e-10, max_iter: int = 0, check: bool = True):
+        it = C.c_int64()
+        rr = C.c_double()
+        st = self.L.isl_solve(self.h, method, tol, max_iter, C.byref(it), C.byref(rr))
+        if check:
+            self._chk(st, "isl_solve")
+        return it.value, rr.value, st
+
+    def solution(self):
+        x = np.zeros(self.neq)
+        self._chk(self.L.isl_get_solution(self.h, A.d(x)))
+        return x
+
+    def rhs(self):
+        b = np.zeros(self.neq)
+        self._chk(self.L.isl_get_rhs(self.h, A.d(b)))
+        return b
+
+    def norm(self):
+        v = C.c_double()
+        self._chk(self.L.isl_norm(self.h, C.byref(v)))
+        return v.value
+
+    def distribute(self, add: bool = False):
+        self._chk(self.L.isl_distribute(self.h, int(add)), "isl_distribute")
+
+    def csr(self, values: bool = True):
+        rp = np.zeros(self.neq + 1, dtype=np.int64)
+        ci = np.zeros(self.nnz, dtype=np.int64)
+        v = np.zeros(self.nnz) if values else None
+        self._chk(self.L.isl_get_csr(self.h, A.i64(rp), A.i64(ci), A.d(v) if values else None), "isl_get_csr")
+        return rp, ci, v
+
+    def sync(self):
+        self._chk(self.L.isl_sync(self.h))
+
+    def set_timing(self, on: bool):
+        self._chk(self.L.isl_set_timing(self.h, int(on)))
+
+    def timings(self):
+        ms = np.zeros(A.NTIMERS)
+        cnt = np.zeros(A.NTIMERS, dtype=np.int64)
+        self._chk(self.L.isl_timings(self.h, A.d(ms), A.i64(cnt)))
+        return ms, cnt
+
+    def time_spmv(self, precision: int, nrep: int = 20) -> float:
+        v = C.c_double()
+        self._chk(self.L.isl_time_spmv(self.h, precision, nrep, C.byref(v)), "isl_time_spmv")
+        return v.value

@@ -1,0 +1,184 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Meshes follow the reference's unit-cube generator connectivity
+(tools/meshGeneration/unitCube/unitCube.hpp:85-263): nodes numbered with the
+first coordinate fastest, element corners in hierarchic order, hexahedra split
+into six tetrahedra by base/cut/DecomposeHyperCube.hpp:81-90.  Random fields
+come from a counter-based Philox generator, one stream per field, seeded by
+one 64-bit value per configuration.
+
+Configurations (sizes can be scaled down for tests with ``n=``):
+  c1  2-D Poisson (heat::Laplace), Q1 quads 64x64, kappa = exp(N(0, 0.5)) per
+      element, nodal source U[0,1], homogeneous Dirichlet on all edges, 2x2 Gauss
+  c2  3-D linear elasticity (HyperElastic at u = 0), hex8 64^3, E log-uniform
+      [1e3, 1e5], nu U[0.2, 0.45] per element, x = 0 clamped, traction
+      (1, 0, 0) on x = 1, 2x2x2 Gauss
+  c3  3-D Poisson, tet10 on 64^3 cubes split into 6 tets, interior nodes
+      jittered by U[-0.2h, 0.2h], kappa lognormal (sigma = 1), nodal source
+      U[0,1], Dirichlet on all faces, 4-point Gauss
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _abi as A
+
+SEED_BASE = 0x15111C0
+
+HEX_FACES = np.array([[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7]])
+QUAD_EDGES = np.array([[0, 1], [1, 2], [2, 3], [3, 0]])
+TET_SPLIT = np.array([[0, 1, 3, 4], [1, 3, 4, 5], [3, 4, 5, 7], [1, 3, 5, 2], [3, 5, 2, 7], [5, 2, 7, 6]])
+HEX_LEX_OF_HIER = np.array([0, 1, 3, 2, 4, 5, 7, 6])
+
+
+def rng(seed: int, stream: int) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(np.random.SeedSequence([seed, stream])))
+
+
+def unit_cube(kind: str, n1: int, n2: int, n3: int = 0):
+    """Structured unit square / cube mesh; kind in {'quad', 'hex', 'tet'}."""
+    if kind == "quad":
+        xs, ys = np.linspace(0, 1, n1 + 1), np.linspace(0, 1, n2 + 1)
+        xs = np.arange(n1 + 1) * (1.0 / n1)
+        ys = np.arange(n2 + 1) * (1.0 / n2)
+        Y, Xg = np.meshgrid(ys, xs, indexing="ij")
+        X = np.stack([Xg.ravel(), Y.ravel()], axis=1)
+        j, i = np.meshgrid(np.arange(n2), np.arange(n1), indexing="ij")
+        base = (i + j * (n1 + 1)).ravel()
+        conn = np.stack([base, base + 1, base + 1 + (n1 + 1), base + (n1 + 1)], axis=1)
+        return X, conn.astype(np.int64)
+    xs = np.arange(n1 + 1) * (1.0 / n1)
+    ys = np.arange(n2 + 1) * (1.0 / n2)
+    zs = np.arange(n3 + 1) * (1.0 / n3)
+    Z, Y, Xg = np.meshgrid(zs, ys, xs, indexing="ij")
+    X = np.stack([Xg.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    k, j, i = np.meshgrid(np.arange(n3), np.arange(n2), np.arange(n1), indexing="ij")
+    b = (i + (n1 + 1) * (j + (n2 + 1) * k)).ravel()
+    sx, sy = 1, n1 + 1
+    sz = (n1 + 1) * (n2 + 1)
+    lex = np.stack([b, b + sx, b + sy, b + sx + sy, b + sz, b + sx + sz, b + sy + sz, b + sx + sy + sz], axis=1)
+    if kind == "hex":
+        conn = lex[:, [0, 1, 3, 2, 4, 5, 7, 6]]
+        return X, conn.astype(np.int64)
+    # the split table numbers corners hierarchically; map to lexicographic corners
+    conn = lex[:, HEX_LEX_OF_HIER[TET_SPLIT]].reshape(-1, 4)
+    return X, conn.astype(np.int64)
+
+
+def faces_on_plane(shape: int, X, conn, elem, face, axis: int, value: float, tol: float = 1e-9):
+    """Select boundary faces whose vertices all lie on x[axis] == value."""
+    table = HEX_FACES if shape == A.HEX else QUAD_EDGES
+    verts = conn[elem[:, None], table[face]]
+    on = np.all(np.abs(X[verts, axis] - value) < tol, axis=1)
+    return elem[on], face[on]
+
+
+@dataclass
+class Problem:
+    name: str
+    shape: int
+    X: np.ndarray
+    conn: np.ndarray
+    fedeg: int
+    ncomp: int
+    kernel: str                       # 'laplace' | 'hyperelastic'
+    qdeg: int
+    kappa: Optional[np.ndarray] = None
+    lam: Optional[np.ndarray] = None
+    mu: Optional[np.ndarray] = None
+    material: str = "stvenant"
+    body: Optional[np.ndarray] = None  # nodal [nnodes, ncomp]
+    dirichlet: Optional[Callable] = None  # x -> (mask [n, ncomp], values)
+    neumann_plane: Optional[tuple] = None  # (axis, value, traction vector)
+    tol: float = 1e-10
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nelem(self):
+        return len(self.conn)
+
+
+def _all_boundary(ncomp):
+    def f(x):
+        return np.ones((len(x), ncomp), dtype=bool), 0.0
+    return f
+
+
+def _clamp_x0(ncomp):
+    def f(x):
+        m = np.abs(x[:, 0]) < 1e-9
+        return np.repeat(m[:, None], ncomp, axis=1), 0.0
+    return f
+
+
+def lame(E, nu):
+    """mat/Lame.hpp:28-49"""
+    return E * nu / (1.0 + nu) / (1.0 - 2.0 * nu), E / 2.0 / (1.0 + nu)
+
+
+def config(name: str, n: Optional[int] = None, seed: Optional[int] = None) -> Problem:
+    idx = {"c1": 0, "c2": 1, "c3": 2}[name]
+    s = SEED_BASE + idx if seed is None else seed
+    if name == "c1":
+        n = n or 64
+        X, conn = unit_cube("quad", n, n)
+        kappa = np.exp(rng(s, 0).normal(0.0, 0.5, len(conn)))
+        f = rng(s, 1).uniform(0.0, 1.0, len(X))[:, None]
+        return Problem("c1", A.QUAD, X, conn, 1, 1, "laplace", 2, kappa=kappa, body=f,
+                       dirichlet=_all_boundary(1), tol=1e-10, meta={"n": n})
+    if name == "c2":
+        n = n or 64
+        X, conn = unit_cube("hex", n, n, n)
+        E = 10.0 ** rng(s, 0).uniform(3.0, 5.0, len(conn))
+        nu = rng(s, 1).uniform(0.2, 0.45, len(conn))
+        lam, mu = lame(E, nu)
+        return Problem("c2", A.HEX, X, conn, 1, 3, "hyperelastic", 3, lam=lam, mu=mu, material="stvenant",
+                       dirichlet=_clamp_x0(3), neumann_plane=(0, 1.0, np.array([1.0, 0.0, 0.0])), tol=1e-10,
+                       meta={"n": n})
+    n = n or 64
+    X, conn = unit_cube("tet", n, n, n)
+    h = 1.0 / n
+    interior = np.all((X > 1e-9) & (X < 1 - 1e-9), axis=1)
+    jit = rng(s, 2).uniform(-0.2 * h, 0.2 * h, X.shape) * interior[:, None]
+    # a jitter of 0.2h per coordinate can invert a few of the slim tets; the
+    # vertices of an inverted tet go back to their grid position (repeat until
+    # every tet has positive volume)
+    for _ in range(20):
+        Y = X + jit
+        a, b, c, d = (Y[conn[:, i]] for i in range(4))
+        bad = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a) <= 0.0
+        if not bad.any():
+            break
+        jit[np.unique(conn[bad])] = 0.0
+    X = X + jit
+    kappa = np.exp(rng(s, 0).normal(0.0, 1.0, len(conn)))
+    f = rng(s, 1).uniform(0.0, 1.0, len(X))[:, None]
+    return Problem("c3", A.TET, X, conn, 2, 1, "laplace", 2, kappa=kappa, body=f, dirichlet=_all_boundary(1),
+                   tol=1e-10, meta={"n": n})
+
+
+def setup_system(p: Problem, sys=None):
+    """Drive the C-ABI through the reference's setup sequence for problem p."""
+    from .system import System
+    S = sys or System()
+    S.upload_mesh(p.shape, p.X, p.conn)
+    S.create_field(p.fedeg, p.ncomp)
+    if p.dirichlet is not None:
+        S.constrain_boundary(p.dirichlet)
+    S.number_dofs()
+    S.register_pattern()
+    if p.kernel == "laplace":
+        S.set_laplace(p.kappa, p.qdeg)
+    else:
+        S.set_hyperelastic(p.material, p.lam, p.mu, p.qdeg)
+    if p.body is not None:
+        S.set_body_force_nodal(p.body)
+    if p.neumann_plane is not None:
+        e, f = S.boundary_faces()
+        axis, value, t = p.neumann_plane
+        e, f = faces_on_plane(p.shape, p.X, p.conn, e, f, axis, value)
+        S.set_neumann(e, f, t, 2)
+    return S

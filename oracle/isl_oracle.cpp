@@ -1298,9 +1298,12 @@ int64_t orc_unitcube(int kind, int e1, int e2, int e3, int round6, double* X, in
                     for (int v = 0; v < 8; ++v) conn[k * 8 + v] = c[H[v]];
                     ++k;
                 } else {
+                    // the split table is in hierarchic corner numbering; the
+                    // hierarchic <-> lexicographic map of a hex is an involution
                     static const int T[6][4] = {{0, 1, 3, 4}, {1, 3, 4, 5}, {3, 4, 5, 7}, {1, 3, 5, 2}, {3, 5, 2, 7}, {5, 2, 7, 6}};
+                    static const int H[8] = {0, 1, 3, 2, 4, 5, 7, 6};
                     for (int s = 0; s < 6; ++s) {
-                        for (int v = 0; v < 4; ++v) conn[k * 4 + v] = c[T[s][v]];
+                        for (int v = 0; v < 4; ++v) conn[k * 4 + v] = c[H[T[s][v]]];
                         ++k;
                     }
                 }
