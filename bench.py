@@ -1,0 +1,336 @@
+"""Benchmark of the GB300 assembly + Krylov hot path (one JSON line on rank 0).
+
+Workload (N=1): 3-D linear elasticity, hex8 64^3 (65^3 nodes, 811,200 active
+DOFs, 63.7M nonzeros), per-element E log-uniform [1e3, 1e5] and nu U[0.2, 0.45],
+face x = 0 clamped, traction (1, 0, 0) on x = 1, 2x2x2 Gauss.  One step =
+assemble K and f (FP64 element kernels, FP64 + FP32 CSR) + FP32 CG inside FP64
+iterative refinement to the tolerance at which the solution is within 1e-8
+relative L2 of the FP64 reference solution.  The plain FP64 GPU path (FP64 CG)
+is measured at its own tolerance for the same error bar and reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 64]
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement; the reference itself needs Eigen/Boost that are not
+available) with all host threads on the same workload and metric.
+Multi-GPU: replicas only (each rank solves its own copy; no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembly GDOF/s & solve time at rel err≤1e-8 vs plain FP64 GPU; p50/p99 latency"
+UNIT = "DOF/s"
+ERR_BAR = 1e-8
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(name="spmv_fp32_c2"):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"{name}.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch"):
+                    return float(line.split("=")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                t = [x.strip() for x in line.split(",")]
+                if len(t) >= 9:
+                    rows.append(t)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        load = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def spmv_bytes(nnz, n, v):
+    """Algorithmic bytes of one CSR SpMV: nnz (v + 4) + 4 (N + 1) + 2 N v."""
+    return nnz * (v + 4) + 4 * (n + 1) + 2 * n * v
+
+
+def calibrate(S, method, x_ref, tols):
+    """Loosest tolerance whose solution is within ERR_BAR of the FP64 reference."""
+    from insilico_gb300 import _abi as A
+    for tol in tols:
+        it, rr, _ = S.solve(method, tol=tol)
+        x = S.solution()
+        err = float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))
+        if err <= ERR_BAR:
+            return tol, err, it
+    return tols[-1], err, it
+
+
+def cpu_sample(p, S, iters_ref, threads):
+    """Reference algorithm (oracle port) on host cores: assembly of a slab of
+    the mesh (scaled to all elements) + CG iterations on the same CSR matrix
+    (scaled to the iteration count the solve needs)."""
+    import oracle as O
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import oracle_problem
+    n = p.meta["n"]
+    slab = max(1, min(n, 4096 // (n * n) if n * n <= 4096 else 1))
+    X, conn = W.unit_cube("hex", n, n, slab)
+    sub = W.Problem("slab", p.shape, X * np.array([1.0, 1.0, slab / n]), conn, p.fedeg, p.ncomp, p.kernel, p.qdeg,
+                    lam=p.lam[: len(conn)], mu=p.mu[: len(conn)], material=p.material, dirichlet=p.dirichlet)
+    P, _ = oracle_problem(sub, assemble=False)
+    t0 = time.perf_counter()
+    P.assemble(incremental=True, nthreads=threads)
+    t_asm = (time.perf_counter() - t0) * (p.nelem / len(conn))
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    k = 8
+    t0 = time.perf_counter()
+    O.cg(rp, ci, v, b, tol=0.0, max_iter=k, nthreads=threads)
+    t_it = (time.perf_counter() - t0) / k
+    total = t_asm + iters_ref * t_it
+    return {"value": S.neq / total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle assembly of a {n}x{n}x{slab} slab ({len(conn)} of {p.nelem} elements, scaled) + "
+                      f"{k} Jacobi-CG iterations on the full {S.neq}-DOF matrix (scaled to {iters_ref} iterations)",
+            "assembly_s_est": t_asm, "cg_iter_s": t_it}
+
+
+def run_reference(args):
+    """--impl reference: reference algorithm on host cores, same workload/metric."""
+    from insilico_gb300 import workloads as W
+    import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import oracle_problem
+    threads = os.cpu_count() or 1
+    n = args.n
+    p = W.config("c2", n=n)
+    # bounded sample per step: a slab of the mesh, assembled and solved with the
+    # reference algorithm; throughput in active DOFs per second of the slab
+    slab = max(1, min(n, 8))
+    X, conn = W.unit_cube("hex", n, n, slab)
+    sub = W.Problem("slab", p.shape, X * np.array([1.0, 1.0, slab / n]), conn, p.fedeg, p.ncomp, p.kernel, p.qdeg,
+                    lam=p.lam[: len(conn)], mu=p.mu[: len(conn)], material=p.material, dirichlet=p.dirichlet,
+                    neumann_plane=p.neumann_plane)
+    vals = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        P, (rp, ci, v, b) = oracle_problem(sub)
+        O.cg(rp, ci, v, b, tol=1e-10, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            vals.append(P.neq / dt)
+    val = float(statistics.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox)",
+            "config": {"workload": f"c2 hex8 elasticity slab {n}x{n}x{slab} of the {n}^3 mesh (bounded CPU sample)",
+                       "parallelism": "replicas", "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n}x{n}x{slab} slab of the c2 mesh: oracle assembly (OpenMP, {threads} threads) "
+                                       f"+ Jacobi CG to 1e-10 per step"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import workloads as W
+
+    A.load(build_if_missing=True)
+    p = W.config("c2", n=args.n)
+    from insilico_gb300.system import System
+    S = W.setup_system(p, System(device=local))
+    neq, nnz = S.neq, S.nnz
+    # FP64 reference solution (tight tolerance) and the plain path's calibration
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x_ref = S.solution()
+    tols = [1e-9, 1e-10, 1e-11, 1e-12]
+    tol64, err64, it64 = calibrate(S, A.SOLVE_CG_FP64, x_ref, tols)
+    tolm, errm, itm = calibrate(S, A.SOLVE_CG_FP32_IR, x_ref, tols)
+
+    def step_mixed():
+        S.assemble(A.PREC_MIXED)
+        return S.solve(A.SOLVE_CG_FP32_IR, tol=tolm)
+
+    def step_plain():
+        S.assemble(A.PREC_FP64)
+        return S.solve(A.SOLVE_CG_FP64, tol=tol64)
+
+    for _ in range(args.warmup):
+        step_mixed()
+    launches0 = S.launch_count()
+    clk = Clocks(local)
+    if pg:
+        pg.barrier()
+    S.sync()
+    S.mark(0)
+    its = []
+    for _ in range(args.steps):
+        its.append(step_mixed()[0])
+    S.mark(1)
+    S.sync()
+    ms_total = S.elapsed_ms(0, 1)
+    clocks = clk.stop()
+    launches = S.launch_count() - launches0
+    x_m = S.solution()
+    err_m = float(np.linalg.norm(x_m - x_ref) / np.linalg.norm(x_ref))
+    if pg:
+        import torch
+        t = torch.tensor([ms_total], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = neq * world / (ms_step / 1e3)
+
+    # phase split of one mixed step and the plain FP64 path
+    S.set_timing(True)
+    step_mixed()
+    ms, cnt = S.timings()
+    S.set_timing(False)
+    asm_ms = ms[A.T_ELEMENT] + ms[A.T_GATHER]
+    solve_ms_m = ms[A.T_SOLVE]
+    S.mark(2)
+    for _ in range(2):
+        it_plain = step_plain()[0]
+    S.mark(3)
+    plain_ms = S.elapsed_ms(2, 3) / 2
+    S.set_timing(True)
+    step_plain()
+    ms64, _ = S.timings()
+    S.set_timing(False)
+    asm64_ms = ms64[A.T_ELEMENT] + ms64[A.T_GATHER]
+
+    # dominant kernel: FP32 SpMV of the inner CG, timed alone (CUDA events)
+    spmv32_ms = S.time_spmv(A.PREC_FP32, 50)
+    spmv64_ms = S.time_spmv(A.PREC_FP64, 50)
+    hbm, src = peaks()
+    b32 = spmv_bytes(nnz, neq, 4)
+    ach = b32 / (spmv32_ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+
+    # e2e through the C-ABI with host buffers: per step upload the element
+    # material table, assemble, solve, download the solution
+    lam, mu = p.lam.copy(), p.mu.copy()
+    for _ in range(1):
+        S.set_hyperelastic(p.material, lam, mu, p.qdeg)
+        step_mixed()
+        S.solution()
+    S.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.set_hyperelastic(p.material, lam, mu, p.qdeg)
+        step_mixed()
+        S.solution()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e = {"value": neq * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lam.nbytes + mu.nbytes),
+           "d2h_bytes_per_step": int(neq * 8), "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_sample(p, S, it64, os.cpu_count() or 1)
+        except Exception as ex:  # reported, not fatal
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Philox; no dataset)",
+        "config": {"workload": f"c2 hex8 linear elasticity {args.n}^3, mixed FP32 CG + FP64 refinement",
+                   "active_dofs": neq, "nnz": nnz, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (FP64 CSR %.0f MB)" % (nnz * 12 / 1e6)},
+        "assembly_gdofs": neq / (asm_ms * 1e-3) / 1e9, "assembly_ms": asm_ms, "solve_ms": solve_ms_m,
+        "solve_tol": tolm, "inner_iters_per_step": int(np.median(its)), "rel_err_vs_fp64": err_m,
+        "plain_fp64": {"ms_per_step": plain_ms, "dofs_per_s": neq / (plain_ms * 1e-3), "assembly_ms": asm64_ms,
+                       "solve_ms": ms64[A.T_SOLVE], "iters": it_plain, "solve_tol": tol64, "rel_err_vs_fp64": err64},
+        "speedup_vs_plain_fp64": plain_ms / ms_step,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": traffic, "kernel": "k_spmv_pap<float> (inner FP32 CG SpMV)",
+                     "bytes_per_launch": b32, "ms_per_launch": spmv32_ms, "peak_source": src,
+                     "fp64_spmv": {"ms_per_launch": spmv64_ms,
+                                   "achieved": spmv_bytes(nnz, neq, 8) / (spmv64_ms * 1e-3) / 1e9}},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    S.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

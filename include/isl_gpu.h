@@ -133,8 +133,10 @@ int isl_assemble(isl_ctx* ctx, int precision, int incremental, int with_residual
 /* Solve the assembled system (Eigen3::cgSolve base/solver/Eigen3.hpp:265-275:
  * Jacobi-preconditioned CG, ||r|| <= tol ||b||, x0 = 0).
  *   ISL_SOLVE_CG_FP64   : FP64 throughout (the plain path)
- *   ISL_SOLVE_CG_FP32_IR: FP32 CG (FP64 dot reductions) inside FP64
- *                         iterative refinement on the FP64 residual.
+ *   ISL_SOLVE_CG_FP32_IR: FP32 CG (FP64 dot reductions) with FP64 reliable
+ *                         updates: the FP64 residual b - A64 x replaces the
+ *                         iterated one each time it has dropped 10x; ends
+ *                         when the FP64 residual meets the tolerance.
  * max_iter <= 0 means 2N.  iters/rel_res may be NULL. */
 int isl_solve(isl_ctx* ctx, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res);
 
@@ -156,6 +158,22 @@ int isl_get_csr(isl_ctx* ctx, int64_t* rowptr, int64_t* colind, double* values);
 int isl_sync(isl_ctx* ctx);
 int isl_set_timing(isl_ctx* ctx, int on);
 int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /* [ISL_NTIMERS] */);
+/* Solver options.  ISL_OPT_BLOCK_SOLVER (default 1): the mixed solve uses a
+ * 3x3 node-block copy of the FP32 matrix with block-Jacobi preconditioning
+ * when every DOF object's three components are all active or all
+ * constrained; 0 keeps the scalar CSR + Jacobi path.  ISL_OPT_BLOCKED (read
+ * only through isl_get_option) tells whether the pattern is node-blocked. */
+enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1 };
+int isl_set_option(isl_ctx* ctx, int key, int64_t value);
+int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
+
+/* Device-side marks on the context stream (CUDA events, 8 slots) and the
+ * elapsed time between two of them, for timing regions from the host. */
+int isl_mark(isl_ctx* ctx, int slot);
+int isl_elapsed(isl_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Number of kernel launches (graph kernel nodes included) issued by the
+ * context since creation. */
+int isl_launch_count(isl_ctx* ctx, int64_t* n);
 /* Average device time (ms) of one launch of the solver's SpMV kernel on the
  * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches. */
 int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);

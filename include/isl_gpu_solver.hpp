@@ -1,0 +1,152 @@
+// isl_gpu_solver.hpp — header-only C++ adapter over the C-ABI (isl_gpu.h)
+// that satisfies the duck-typed SOLVER interface of the reference
+// (base::solver::Eigen3, base/solver/Eigen3.hpp:64-342) for the operations the
+// hot path needs, plus the asmb entry points as member calls:
+//
+//   reference                                         adapter
+//   Eigen3(size_t N)                         base/solver/Eigen3.hpp:71-77    Gb300Solver(ctx) after numberDoFs()
+//   registerFields<FTB>(fb)                  :332-336                         registerFields()
+//   stiffnessMatrixComputation<FTB>(...)     base/asmb/StiffnessMatrix.hpp:49-87   assemble(...)
+//   computeResidualForces<FTB>(...)          base/asmb/ForceIntegrator.hpp:37-71   assemble(..., with_residual)
+//   finishAssembly()                         :142-153                         finishAssembly() (no-op)
+//   int cgSolve()                            :265-275                         cgSolve()
+//   number getValue(i)                       :293-296                         getValue(i)
+//   double norm(), norm(first, last)         :128-138                         norm(), norm(first, last)
+//   insertToLHS / insertToRHS                :81-124                          not offered: assembly runs on the device
+//
+// Errors: the reference aborts through VERIFY_MSG (base/verify.hpp:63-65);
+// the adapter throws isl::gpu_error carrying the isl_status code instead.
+#pragma once
+
+#include <cmath>
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "isl_gpu.h"
+
+namespace isl {
+
+struct gpu_error : std::runtime_error {
+    int code;
+    gpu_error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(isl_ctx* ctx, int st, const char* what) {
+    if (st != ISL_OK) throw gpu_error(st, std::string(what) + ": " + isl_last_error(ctx));
+}
+
+// Owns one isl_ctx: mesh, field, DOF state, pattern, system and solution on one GPU.
+class Gb300Solver {
+public:
+    explicit Gb300Solver(int device = 0, void* stream = nullptr) {
+        int st = isl_ctx_create(&ctx_, device, stream);
+        if (st != ISL_OK) throw gpu_error(st, "isl_ctx_create");
+    }
+    ~Gb300Solver() { if (ctx_) isl_ctx_destroy(ctx_); }
+    Gb300Solver(const Gb300Solver&) = delete;
+    Gb300Solver& operator=(const Gb300Solver&) = delete;
+
+    isl_ctx* ctx() { return ctx_; }
+
+    // ---- mesh / field / DOFs (base::Unstructured, base::dof::generate, ...)
+    void mesh(int shape, int dim, const std::vector<double>& X, const std::vector<int64_t>& conn, int nv) {
+        check(ctx_, isl_mesh_upload(ctx_, shape, dim, (int64_t)X.size() / dim, X.data(), (int64_t)conn.size() / nv, conn.data()),
+              "isl_mesh_upload");
+    }
+    int64_t field(int fe_degree, int ncomp) {
+        int64_t n = 0;
+        int nf = 0;
+        check(ctx_, isl_field_create(ctx_, fe_degree, ncomp, &n, &nf), "isl_field_create");
+        ncomp_ = ncomp;
+        return n;
+    }
+    // constrainBoundary with a functor f(const double* x, int comp, double& value) -> bool
+    template <typename DIRIFUN>
+    void constrainBoundary(int dim, DIRIFUN f) {
+        int64_t n = 0;
+        check(ctx_, isl_boundary_points(ctx_, &n, nullptr, nullptr), "isl_boundary_points");
+        std::vector<double> x((size_t)n * dim);
+        std::vector<int64_t> dof(n);
+        check(ctx_, isl_boundary_points(ctx_, &n, x.data(), dof.data()), "isl_boundary_points");
+        std::vector<int64_t> d;
+        std::vector<int> c;
+        std::vector<double> v;
+        for (int64_t i = 0; i < n; ++i)
+            for (int k = 0; k < ncomp_; ++k) {
+                double val = 0.0;
+                if (f(&x[(size_t)i * dim], k, val)) { d.push_back(dof[i]); c.push_back(k); v.push_back(val); }
+            }
+        check(ctx_, isl_constrain(ctx_, (int64_t)d.size(), d.data(), c.data(), v.data()), "isl_constrain");
+    }
+    std::size_t numberDoFs() {
+        int64_t n = 0;
+        check(ctx_, isl_number_dofs(ctx_, &n), "isl_number_dofs");
+        n_ = (std::size_t)n;
+        return n_;
+    }
+    void registerFields() {
+        int64_t nnz = 0;
+        check(ctx_, isl_register_pattern(ctx_, &nnz), "isl_register_pattern");
+    }
+
+    // ---- kernels (per-element tabulated coefficients)
+    void laplace(const std::vector<double>& kappa, int quad_degree) {
+        check(ctx_, isl_set_laplace(ctx_, kappa.data(), quad_degree), "isl_set_laplace");
+    }
+    void hyperElastic(int material, const std::vector<double>& lam, const std::vector<double>& mu, int quad_degree) {
+        check(ctx_, isl_set_hyperelastic(ctx_, material, lam.data(), mu.data(), quad_degree), "isl_set_hyperelastic");
+    }
+    void bodyForceNodal(const std::vector<double>& f) {
+        check(ctx_, isl_set_body_force_nodal(ctx_, f.data()), "isl_set_body_force_nodal");
+    }
+
+    // ---- assembly + solve (SOLVER duck type)
+    void assemble(int precision = ISL_PREC_FP64, bool incremental = true, bool with_residual = false) {
+        check(ctx_, isl_assemble(ctx_, precision, incremental, with_residual), "isl_assemble");
+        cache_.clear();
+    }
+    void finishAssembly(bool = true) {}
+    int cgSolve(double tol = 2.220446049250313e-16) {
+        int64_t it = 0;
+        double rr = 0.0;
+        const int st = isl_solve(ctx_, ISL_SOLVE_CG_FP64, tol, 0, &it, &rr);
+        if (st != ISL_OK && st != ISL_ERR_NOT_CONVERGED) check(ctx_, st, "isl_solve");
+        cache_.clear();
+        return (int)it;
+    }
+    int cgSolveMixed(double tol) {
+        int64_t it = 0;
+        double rr = 0.0;
+        check(ctx_, isl_solve(ctx_, ISL_SOLVE_CG_FP32_IR, tol, 0, &it, &rr), "isl_solve");
+        cache_.clear();
+        return (int)it;
+    }
+    double getValue(std::size_t i) {
+        fill();
+        return cache_.at(i);
+    }
+    double norm() { return norm(0, n_); }
+    double norm(std::size_t first, std::size_t last) {
+        fill();
+        double s = 0.0;
+        for (std::size_t i = first; i < last; ++i) s += cache_[i] * cache_[i];
+        return std::sqrt(s) / (double)(last - first);
+    }
+    void setDoFsFromSolver() { check(ctx_, isl_distribute(ctx_, 0), "isl_distribute"); }
+    void addToDoFsFromSolver() { check(ctx_, isl_distribute(ctx_, 1), "isl_distribute"); }
+
+private:
+    void fill() {
+        if (cache_.size() == n_) return;
+        cache_.resize(n_);
+        check(ctx_, isl_get_solution(ctx_, cache_.data()), "isl_get_solution");
+    }
+    isl_ctx* ctx_ = nullptr;
+    int ncomp_ = 1;
+    std::size_t n_ = 0;
+    std::vector<double> cache_;
+};
+
+}  // namespace isl

@@ -34,8 +34,10 @@ EXPORTED = [
     "isl_scale_constraints", "isl_number_dofs", "isl_dof_index", "isl_register_pattern", "isl_set_laplace",
     "isl_set_hyperelastic", "isl_set_body_force_nodal", "isl_set_neumann", "isl_set_values", "isl_get_values",
     "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
-    "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv",
+    "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
+    "isl_set_option", "isl_get_option",
 ]
+OPT_BLOCK_SOLVER, OPT_BLOCKED = 0, 1
 
 
 class IslError(RuntimeError):
@@ -98,6 +100,11 @@ def load(build_if_missing: bool = False):
     L.isl_set_timing.argtypes = [_P, i]
     L.isl_timings.argtypes = [_P, _D, _I64]
     L.isl_time_spmv.argtypes = [_P, i, i, _D]
+    L.isl_mark.argtypes = [_P, i]
+    L.isl_elapsed.argtypes = [_P, i, i, _D]
+    L.isl_launch_count.argtypes = [_P, _I64]
+    L.isl_set_option.argtypes = [_P, i, C.c_int64]
+    L.isl_get_option.argtypes = [_P, i, _I64]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "isl_last_error":

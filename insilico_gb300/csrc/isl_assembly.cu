@@ -282,31 +282,69 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
             for (int d = 0; d < 3; ++d) su[(role * 3 + d) * EPB + el] = A.u[(size_t)obj * 3 + d];
         }
     }
-    __syncthreads();
-    const double lam = A.coef[ec], mu = A.coef[E + ec];
-    // ---- phase 1: quadrature point q = role
-    {
-        const int q = role;
+    // affine elements (parallelepipeds): one FP64 Jacobian per element, by role 0
+    __shared__ double sJi[10][EPB];
+    __shared__ int saff[EPB];
+    if (role == 0) {
         double X[8][3];
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int d = 0; d < 3; ++d) X[i][d] = sX[(i * 3 + d) * EPB + el];
-        double Ji[3][3];
-        const double detJ = jac<8, 3>(X, T.dN[q], Ji);
+        const bool aff = affine<ISL_HEX, 8, 3>(X);
+        saff[el] = aff;
+        if (aff) {
+            double Ji[3][3];
+            sJi[9][el] = jac<8, 3>(X, T.dN[0], Ji);
+#pragma unroll
+            for (int a = 0; a < 9; ++a) sJi[a][el] = Ji[a / 3][a % 3];
+        }
+    }
+    __syncthreads();
+    const double lam = A.coef[ec], mu = A.coef[E + ec];
+    // ---- phase 1: quadrature point q = role
+    {
+        const int q = role;
+        double Ji[3][3], detJ;
+        if (saff[el]) {
+#pragma unroll
+            for (int a = 0; a < 9; ++a) Ji[a / 3][a % 3] = sJi[a][el];
+            detJ = sJi[9][el];
+        } else {
+            double X[8][3];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) X[i][d] = sX[(i * 3 + d) * EPB + el];
+            detJ = jac<8, 3>(X, T.dN[q], Ji);
+        }
         if (valid && !(detJ > 0.0)) atomicOr(A.flags, 1);
-        double g[8][3];
-#pragma unroll
-        for (int M = 0; M < 8; ++M)
-#pragma unroll
-            for (int a = 0; a < 3; ++a) g[M][a] = Ji[a][0] * T.dphi[q][M][0] + Ji[a][1] * T.dphi[q][M][1] + Ji[a][2] * T.dphi[q][M][2];
         const double c = detJ * T.w[q];
-#pragma unroll
-        for (int M = 0; M < 8; ++M)
-#pragma unroll
-            for (int a = 0; a < 3; ++a) sg[((q * 8 + M) * 3 + a) * EPB + el] = R(g[M][a]);
         sc[q * EPB + el] = R(c);
+        if (!A.general) {
+            // small-strain path: gradients only needed in R
+            R Jr[3][3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) Jr[a][b] = R(Ji[a][b]);
+#pragma unroll
+            for (int M = 0; M < 8; ++M)
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    sg[((q * 8 + M) * 3 + a) * EPB + el] =
+                        Jr[a][0] * R(T.dphi[q][M][0]) + Jr[a][1] * R(T.dphi[q][M][1]) + Jr[a][2] * R(T.dphi[q][M][2]);
+        }
         if (A.general) {
+            double g[8][3];
+#pragma unroll
+            for (int M = 0; M < 8; ++M)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) g[M][a] = Ji[a][0] * T.dphi[q][M][0] + Ji[a][1] * T.dphi[q][M][1] + Ji[a][2] * T.dphi[q][M][2];
+#pragma unroll
+            for (int M = 0; M < 8; ++M)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) sg[((q * 8 + M) * 3 + a) * EPB + el] = R(g[M][a]);
             double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 #pragma unroll
             for (int f = 0; f < 8; ++f)
@@ -514,6 +552,7 @@ __global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun,
     if (k >= nlift) return;
     const int e = lift_elem[k];
     const int nloc = nfun * ncomp;
+    if (nloc > 30) return;
     double g[30];
     bool act[30];
     bool any = false;
@@ -680,12 +719,25 @@ int pattern_build(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dseg.alloc(nnz + 1));
     ISL_CHECK_CUDA(c, c->drowptr.alloc(c->neq + 1));
     ISL_CHECK_CUDA(c, c->ddiag.alloc(c->neq));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->ddiag.p, 0, c->neq * 4, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->drowptr.p, 0xff, (c->neq + 1) * 4, st));
     k_fill_csr<<<nblk(nvalid, 256), 256, 0, st>>>((long long)nvalid, kout.p, flag.p, slot.p, c->dcolind.p, c->dseg.p,
                                                    c->drowptr.p, c->ddiag.p);
     const int32_t tail_seg = (int32_t)nvalid, tail_row = (int32_t)nnz;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dseg.p + nnz, &tail_seg, 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->drowptr.p + c->neq, &tail_row, 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    {
+        // every active row owns its diagonal, so every row pointer is set; check
+        // monotonicity before any kernel indexes with them
+        std::vector<int32_t> rp(c->neq + 1);
+        ISL_CHECK_CUDA(c, cudaMemcpy(rp.data(), c->drowptr.p, rp.size() * 4, cudaMemcpyDeviceToHost));
+        bool ok = rp[0] == 0 && rp[c->neq] == nnz;
+        for (int64_t i = 0; ok && i < c->neq; ++i) ok = rp[i] >= 0 && rp[i] < rp[i + 1];
+        if (!ok) ISL_FAIL(c, ISL_ERR_ARG, "pattern build: inconsistent row pointers");
+        const int brc = block_pattern(c, rp);
+        if (brc != ISL_OK) return brc;
+    }
     kout.release();
     flag.release();
     slot.release();
@@ -759,6 +811,7 @@ static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
     fill_tab<SHAPE, FDEG, NQ>(T, h);
     k_laplace<SHAPE, FDEG, NQ, R><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
     ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
     return ISL_OK;
 }
 
@@ -804,6 +857,7 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
     }
     (void)epb_run;
     ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
     return ISL_OK;
 }
 
@@ -829,6 +883,7 @@ static int launch_neumann(isl_ctx* c) {
             for (int s = 0; s < NF; ++s) A.phi[f][q][s] = ft.phi[(f * ft.nsq + q) * NF + s];
     k_neumann<NF, NCOMP, NG, D><<<nblk(c->n_neu_elem, 64), 64, 0, c->stream>>>(A);
     ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
     return ISL_OK;
 }
 
@@ -886,6 +941,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
             k_lift<double><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
                                                                c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK64.p, c->dstageF.p);
         ISL_CHECK_CUDA(c, cudaGetLastError());
+        c->launches += 1;
     }
     if (c->timing) cudaEventRecord(c->ev[1], st);
     const unsigned gblocks = (unsigned)std::min<long long>(nblk(c->nnz, 256), (long long)c->sm_count * 8);
@@ -897,6 +953,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     const unsigned vblocks = (unsigned)std::min<long long>(nblk(c->neq, 256), (long long)c->sm_count * 8);
     k_gather_vec<<<vblocks, 256, 0, st>>>((int)c->neq, c->dsegF.p, c->dsrcF.p, c->dstageF.p, c->drhs.p);
     ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 2;
     if (c->timing) cudaEventRecord(c->ev[2], st);
     int flags = 0;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(&flags, c->dflags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -910,6 +967,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     }
     c->have64 = (precision != ISL_PREC_FP32);
     c->have32 = (precision != ISL_PREC_FP64);
+    c->asm_serial++;
     c->solved = false;
     if (flags & 2) ISL_FAIL(c, ISL_ERR_NAN, "non-finite stress (det F <= 0?)");
     if (flags & 1) ISL_FAIL(c, ISL_ERR_DEGENERATE, "element with det J <= 0");

@@ -350,6 +350,7 @@ int isl_ctx_create(isl_ctx** out, int device, void* stream) {
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaMallocHost(&c->hscal, sizeof(isl::CGScal)) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
+    for (auto& ev : c->mark) cudaEventCreate(&ev);
     if (c->dflags.alloc(4) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
     cudaMemsetAsync(c->dflags.p, 0, 4 * sizeof(int), c->stream);
     *out = c;
@@ -362,6 +363,7 @@ int isl_ctx_destroy(isl_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
+    for (auto& ev : c->mark) if (ev) cudaEventDestroy(ev);
     if (c->hscal) cudaFreeHost(c->hscal);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -844,6 +846,40 @@ int isl_timings(isl_ctx* c, double* ms, int64_t* counts) {
 int isl_time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     if (!c || !c->nnz || !ms || nrep <= 0) return ISL_ERR_ARG;
     return isl::time_spmv(c, precision, nrep, ms);
+}
+
+int isl_mark(isl_ctx* c, int slot) {
+    if (!c || c->device < 0 || slot < 0 || slot >= 8) return ISL_ERR_ARG;
+    ISL_CHECK_CUDA(c, cudaEventRecord(c->mark[slot], c->stream));
+    return ISL_OK;
+}
+
+int isl_elapsed(isl_ctx* c, int a, int b, double* ms) {
+    if (!c || c->device < 0 || a < 0 || a >= 8 || b < 0 || b >= 8 || !ms) return ISL_ERR_ARG;
+    ISL_CHECK_CUDA(c, cudaEventSynchronize(c->mark[b]));
+    float t = 0.f;
+    ISL_CHECK_CUDA(c, cudaEventElapsedTime(&t, c->mark[a], c->mark[b]));
+    *ms = t;
+    return ISL_OK;
+}
+
+int isl_launch_count(isl_ctx* c, int64_t* n) {
+    if (!c || !n) return ISL_ERR_ARG;
+    *n = c->launches;
+    return ISL_OK;
+}
+
+int isl_set_option(isl_ctx* c, int key, int64_t value) {
+    if (!c) return ISL_ERR_ARG;
+    if (key == ISL_OPT_BLOCK_SOLVER) { c->use_block = value != 0; return ISL_OK; }
+    ISL_FAIL(c, ISL_ERR_ARG, "unknown or read-only option");
+}
+
+int isl_get_option(isl_ctx* c, int key, int64_t* value) {
+    if (!c || !value) return ISL_ERR_ARG;
+    if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
+    if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
+    ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
 }
 
 }  // extern "C"

@@ -88,7 +88,7 @@ struct CGWork {
 
 // scalar block shared by the CG kernels (device)
 struct CGScal {
-    double absNew, pAp, alpha, beta, rr, rz, threshold, rhsNorm2;
+    double absNew, absOld, pAp, alpha, beta, rr, rz, threshold, rhsNorm2;
     int done;
     int iters;
     int bad;
@@ -158,6 +158,17 @@ struct isl_ctx {
     isl::DBuf<double> dsol;      // x (FP64)
     bool solved = false;
 
+    // node-blocked (3x3) FP32 copy of the matrix for the mixed solver: used
+    // when every DOF object has all three components active or all constrained
+    bool blocked = false;
+    bool use_block = true;
+    int64_t nbr = 0, nblk = 0;
+    isl::DBuf<int32_t> dbptr, dbcol, dbrow;
+    isl::DBuf<float> dbval;      // SoA [9][nblk]
+    isl::DBuf<float> dbinv;      // SoA [9][nbr] inverse diagonal blocks
+    int64_t asm_serial = 0, bsr_serial = -1;
+    int bspmv_lpb = 0;
+
     // status word written by kernels (bit 0: det J <= 0, bit 1: NaN)
     isl::DBuf<int> dflags;
 
@@ -174,6 +185,8 @@ struct isl_ctx {
     double tms[ISL_NTIMERS] = {0};
     int64_t tcount[ISL_NTIMERS] = {0};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t mark[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int64_t launches = 0;  // kernels launched (graph nodes included)
 };
 
 // status helpers
@@ -199,4 +212,5 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
 int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int distribute_device(isl_ctx* c, int add);
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
+int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
 }  // namespace isl

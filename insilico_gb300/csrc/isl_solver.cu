@@ -5,19 +5,23 @@
 // (base/solver/Eigen3.hpp:265-275): x0 = 0, z = D^{-1} r, stop when
 // ||r||^2 < tol^2 ||b||^2 or after max_iter iterations.
 //
-// One iteration = three kernels, all on the context stream:
-//   k_spmv_pap : q = A p and p.q             (last block: alpha)
+// One iteration = three kernels on the context stream:
+//   k_cg_dir   : p = D^{-1} r + beta p          (beta = 0 on the first pass)
+//   k_spmv_pap : q = A p and p.q                (last block: alpha)
 //   k_cg_update: x += alpha p, r -= alpha q,  r.r and r.D^{-1}r
-//                                            (last block: convergence, beta)
-//   k_cg_dir   : p = D^{-1} r + beta p
+//                                               (last block: convergence, beta)
 // Block partial sums are reduced by the last block to finish (a ticket
-// counter, not an atomic on the data), in a fixed order, so results are
-// bit-reproducible.  Iterations are captured into a CUDA graph of CHUNK
-// iterations that is replayed until the device-side done flag is set.
+// counter orders the blocks; no atomics touch the data), in a fixed order, so
+// results are bit-reproducible.  CHUNK iterations are captured once into a
+// CUDA graph that is replayed until the device-side done flag is set.
 //
-// The mixed method runs the same kernels in FP32 (dot products accumulated in
-// FP64) inside FP64 iterative refinement: r64 = b - A64 x64 in FP64, inner
-// FP32 CG on A32 d = r64/||r64||, x64 += ||r64|| d.
+// The mixed method is CG in FP32 (vectors and matrix values; dot products
+// reduced in FP64) with reliable updates in FP64: whenever the iterated FP32
+// residual has dropped by a factor 10 since the last update (or has met the
+// tolerance), the FP32 increment is folded into the FP64 iterate, the true
+// residual r = b - A64 x is formed in FP64 and replaces the iterated one, and
+// the iteration continues with the same search direction.  The solve ends
+// when the true FP64 residual meets the tolerance.
 #include <cmath>
 #include <vector>
 
@@ -31,7 +35,7 @@ constexpr int CHUNK = 32;
 template <typename T>
 __device__ inline T ld(const T* p) { return __ldg(p); }
 
-// fixed-order block reduction of a double (deterministic)
+// fixed-order block reduction of a double (deterministic); result in thread 0
 __device__ inline double block_sum(double v, double* sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -43,10 +47,10 @@ __device__ inline double block_sum(double v, double* sh) {
         t = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     }
-    return t;  // valid in thread 0
+    return t;
 }
 
-// the last block to arrive reduces part[0..gridDim.x) for each of nv values
+// true in every thread of the last block to finish
 __device__ inline bool last_block(unsigned int* ticket) {
     __shared__ bool amLast;
     __threadfence();
@@ -76,7 +80,7 @@ __device__ inline TX row_dot(int row, const int* __restrict__ rowptr, const int*
     return acc;
 }
 
-// q = A p; partial p.q; last block computes alpha = absNew / p.q
+// q = A p; partial p.q; last block: alpha = absNew / p.q
 template <typename TV, typename TX, int LPR>
 __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
                                                  const TV* __restrict__ val, const TX* __restrict__ p, TX* __restrict__ q,
@@ -130,13 +134,12 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->iters += 1;
+            S->absOld = S->absNew;
+            S->beta = trz / S->absNew;
+            S->absNew = trz;
             if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
             else if (trr < S->threshold) S->done = 1;
             else if (S->iters >= max_iter) S->done = 2;
-            else {
-                S->beta = trz / S->absNew;
-                S->absNew = trz;
-            }
             S->ticket2 = 0;
         }
     }
@@ -150,20 +153,21 @@ __global__ void __launch_bounds__(BS) k_cg_dir(int n, const TX* __restrict__ r, 
     for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) p[i] = dinv[i] * r[i] + beta * p[i];
 }
 
-// setup: x = 0, r = b, p = D^{-1} b, absNew = r.p, rhsNorm2 = b.b
-template <typename TX>
-__global__ void __launch_bounds__(BS) k_cg_init(int n, const TX* __restrict__ b, TX* __restrict__ x, TX* __restrict__ r,
-                                                TX* __restrict__ p, const TX* __restrict__ dinv, CGScal* S, double* part, double tol) {
+// x = 0, r = b, p = 0, beta = 0, absNew = r.D^{-1}r, rhsNorm2 = b.b (FP64)
+template <typename TB, typename TX>
+__global__ void __launch_bounds__(BS) k_cg_init(int n, const TB* __restrict__ b, TX* __restrict__ x, TX* __restrict__ r,
+                                                TX* __restrict__ p, const TX* __restrict__ dinv, CGScal* S, double* part,
+                                                double tol) {
     __shared__ double sh[32];
     double bb = 0.0, bz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
-        const TX bi = b[i];
+        const TB bi = b[i];
+        const TX ri = (TX)bi;
         x[i] = TX(0);
-        r[i] = bi;
-        const TX zi = dinv[i] * bi;
-        p[i] = zi;
+        r[i] = ri;
+        p[i] = TX(0);
         bb += (double)bi * (double)bi;
-        bz += (double)bi * (double)zi;
+        bz += (double)ri * (double)(dinv[i] * ri);
     }
     const double b1 = block_sum(bb, sh);
     const double b2 = block_sum(bz, sh);
@@ -175,6 +179,8 @@ __global__ void __launch_bounds__(BS) k_cg_init(int n, const TX* __restrict__ b,
             S->rhsNorm2 = tbb;
             S->threshold = tol * tol * tbb;
             S->absNew = tbz;
+            S->absOld = tbz;
+            S->beta = 0.0;
             S->rr = tbb;
             S->iters = 0;
             S->bad = !(tbb == tbb);
@@ -193,7 +199,15 @@ __global__ void k_dinv(int n, const int* __restrict__ diag, const TV* __restrict
     }
 }
 
-// r64 = b - A64 x64 ; partial ||r||^2
+// reliable update, part 1: fold the FP32 increment into the FP64 iterate
+__global__ void k_fold(int n, float* __restrict__ x32, double* __restrict__ x64) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x64[i] += (double)x32[i];
+        x32[i] = 0.0f;
+    }
+}
+
+// r64 = b - A64 x64 ; last block: ||r64||^2 -> *out
 template <int LPR>
 __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
                                                    const double* __restrict__ val, const double* __restrict__ x,
@@ -219,12 +233,31 @@ __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict_
     }
 }
 
-__global__ void k_scale_to32(int n, const double* __restrict__ r, double s, float* __restrict__ r32) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) r32[i] = (float)(r[i] * s);
-}
-
-__global__ void k_axpy32to64(int n, double a, const float* __restrict__ d, double* __restrict__ x) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += a * (double)d[i];
+// reliable update, part 2: r32 = r64; beta = (r.z)_new / (r.z)_previous; resume
+__global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restrict__ r64, float* __restrict__ r32,
+                                                  const float* __restrict__ dinv, CGScal* S, double* part) {
+    __shared__ double sh[32];
+    double rr = 0.0, rz = 0.0;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+        const float ri = (float)r64[i];
+        r32[i] = ri;
+        rr += (double)ri * (double)ri;
+        rz += (double)ri * (double)(dinv[i] * ri);
+    }
+    const double b1 = block_sum(rr, sh);
+    const double b2 = block_sum(rz, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (last_block(&S->ticket2)) {
+        const double trr = reduce_parts(part, gridDim.x, 2, 0, sh);
+        const double trz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        if (threadIdx.x == 0) {
+            S->rr = trr;
+            S->beta = trz / S->absOld;
+            S->absNew = trz;
+            S->done = 0;
+            S->ticket2 = 0;
+        }
+    }
 }
 
 __global__ void k_copy64(int n, const double* __restrict__ a, double* __restrict__ b) {
@@ -232,10 +265,6 @@ __global__ void k_copy64(int n, const double* __restrict__ a, double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-struct Launch {
-    unsigned grid;
-};
-
 static unsigned vec_grid(isl_ctx* c) { return (unsigned)c->sm_count * (2048 / BS); }
 
 template <typename TV, typename TX>
@@ -272,6 +301,7 @@ static int autotune_lpr(isl_ctx* c, const TV* val, const TX* p, TX* q, CGScal* S
     const int cand[4] = {4, 8, 16, 32};
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
+    c->launches += 24;
     for (int k = 0; k < 4; ++k) {
         const int lpr = cand[k];
         launch_spmv<TV, TX>(lpr, vec_grid(c), c->stream, (int)c->neq, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
@@ -287,47 +317,32 @@ static int autotune_lpr(isl_ctx* c, const TV* val, const TX* p, TX* q, CGScal* S
     return best;
 }
 
-// Run CG on (val, b) of type TV/TX with workspace vectors; returns status.
+// one CHUNK of iterations (dir, spmv, update) captured into a graph
 template <typename TV, typename TX>
-static int run_cg(isl_ctx* c, const TV* val, const TX* b, TX* x, TX* r, TX* p, TX* q, TX* dinv, double tol, int64_t max_iter,
-                  int lpr, int64_t* iters, double* rr_out, double* rhs2_out, bool* not_converged) {
+static int capture_chunk(isl_ctx* c, const TV* val, TX* x, TX* r, TX* p, TX* q, const TX* dinv, int lpr, int max_iter,
+                         cudaGraphExec_t* exec) {
     cudaStream_t st = c->stream;
     const int n = (int)c->neq;
+    const unsigned grid = vec_grid(c);
     CGScal* S = c->dscal.p;
     double* part = c->dpart.p;
-    const unsigned grid = vec_grid(c);
-    const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
-    k_dinv<TV, TX><<<grid, BS, 0, st>>>(n, c->ddiag.p, val, dinv);
-    ISL_CHECK_CUDA(c, cudaMemsetAsync(S, 0, sizeof(CGScal), st));
-    k_cg_init<TX><<<grid, BS, 0, st>>>(n, b, x, r, p, dinv, S, part, tol);
-    ISL_CHECK_CUDA(c, cudaGetLastError());
-    // capture one chunk of iterations
     cudaGraph_t graph;
-    cudaGraphExec_t exec;
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < CHUNK; ++k) {
-        launch_spmv<TV, TX>(lpr, grid, st, n, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
-        k_cg_update<TX><<<grid, BS, 0, st>>>(n, x, r, p, q, dinv, S, part, mi);
         k_cg_dir<TX><<<grid, BS, 0, st>>>(n, r, dinv, p, S);
+        launch_spmv<TV, TX>(lpr, grid, st, n, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
+        k_cg_update<TX><<<grid, BS, 0, st>>>(n, x, r, p, q, dinv, S, part, max_iter);
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
-    ISL_CHECK_CUDA(c, cudaGraphInstantiate(&exec, graph, 0));
-    int rc = ISL_OK;
-    for (;;) {
-        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->hscal, S, sizeof(CGScal), cudaMemcpyDeviceToHost, st));
-        ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
-        if (c->hscal->done) break;
-        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; break; }
-    }
-    cudaGraphExecDestroy(exec);
+    cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
-    if (rc != ISL_OK) ISL_FAIL(c, rc, "graph launch failed");
-    const CGScal& h = *c->hscal;
-    if (iters) *iters = h.iters;
-    if (rr_out) *rr_out = h.rr;
-    if (rhs2_out) *rhs2_out = h.rhsNorm2;
-    if (not_converged) *not_converged = (h.done == 2);
-    if (h.bad) ISL_FAIL(c, ISL_ERR_NAN, "CG breakdown (non-finite reduction)");
+    ISL_CHECK_CUDA(c, e);
+    return ISL_OK;
+}
+
+static int read_scal(isl_ctx* c) {
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->hscal, c->dscal.p, sizeof(CGScal), cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
 }
 
@@ -340,82 +355,541 @@ static int ensure_work(isl_ctx* c) {
     return ISL_OK;
 }
 
-int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
-    int st_ = ensure_work(c);
-    if (st_ != ISL_OK) return st_;
+// plain FP64 CG
+static int solve_fp64(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
     cudaStream_t st = c->stream;
     const size_t n = (size_t)c->neq;
-    if (max_iter <= 0) max_iter = 2 * (int64_t)n;
-    if (c->timing) cudaEventRecord(c->ev[0], st);
     double* W = c->w64.p;
-    double *x = W, *r = W + n, *p = W + 2 * n, *q = W + 3 * n, *dinv = W + 4 * n, *r64 = W + 5 * n;
-    int rc = ISL_OK;
-    int64_t total_it = 0;
+    double *x = W, *r = W + n, *p = W + 2 * n, *q = W + 3 * n, *dinv = W + 4 * n;
+    if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, q, c->dscal.p, c->dpart.p);
+    const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    const unsigned grid = vec_grid(c);
+    k_dinv<double, double><<<grid, BS, 0, st>>>((int)n, c->ddiag.p, c->dval64.p, dinv);
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, sizeof(CGScal), st));
+    k_cg_init<double, double><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x, r, p, dinv, c->dscal.p, c->dpart.p, tol);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 2;
+    cudaGraphExec_t exec;
+    int rc = capture_chunk<double, double>(c, c->dval64.p, x, r, p, q, dinv, c->spmv_lpr64, mi, &exec);
+    if (rc != ISL_OK) return rc;
+    const int64_t max_replays = (int64_t)mi / CHUNK + 3;
+    int64_t replays = 0;
+    for (;;) {
+        rc = read_scal(c);
+        if (rc != ISL_OK) break;
+        if (c->hscal->done) break;
+        if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "CG made no progress"; break; }
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
+        c->launches += 3 * CHUNK;
+    }
+    cudaGraphExecDestroy(exec);
+    if (rc != ISL_OK) return rc;
+    const CGScal& h = *c->hscal;
+    if (h.bad) ISL_FAIL(c, ISL_ERR_NAN, "CG breakdown (non-finite reduction)");
+    *iters = h.iters;
+    *rel = h.rhsNorm2 > 0 ? std::sqrt(h.rr / h.rhsNorm2) : 0.0;
+    *nc = (h.done == 2);
+    k_copy64<<<grid, BS, 0, st>>>((int)n, x, c->dsol.p);
+    c->launches += 1;
+    return ISL_OK;
+}
+
+// FP32 CG with FP64 reliable updates
+static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
+    cudaStream_t st = c->stream;
+    const size_t n = (size_t)c->neq;
+    double* W = c->w64.p;
+    double *x64 = W, *r64 = W + n;
+    float* V = c->w32.p;
+    float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n;
+    if (!c->spmv_lpr32) {
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, n * 4, st));
+        c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, p32, q32, c->dscal.p, c->dpart.p);
+    }
+    if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
+    const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    const unsigned grid = vec_grid(c);
+    CGScal* S = c->dscal.p;
+    double* dres = (double*)(c->dscal.p + 1);
+    unsigned* ticket = &(c->dscal.p + 1)->ticket1;
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
+    k_dinv<float, float><<<grid, BS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
+    k_cg_init<double, float><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x32, r32, p32, d32, S, c->dpart.p, tol);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 2;
+    cudaGraphExec_t exec;
+    int rc = capture_chunk<float, float>(c, c->dval32.p, x32, r32, p32, q32, d32, c->spmv_lpr32, mi, &exec);
+    if (rc != ISL_OK) return rc;
+    rc = read_scal(c);
+    const double bnorm2 = c->hscal->rhsNorm2;
+    double rr_last = bnorm2, rr_true = bnorm2;
+    const double delta2 = 1e-2;  // reliable update when the iterated residual dropped 10x
+    const int64_t max_replays = (int64_t)mi / CHUNK + 64;
+    int64_t replays = 0;
+    bool converged = (bnorm2 == 0.0);
+    while (rc == ISL_OK && !converged) {
+        if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "mixed CG made no progress"; break; }
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
+        c->launches += 3 * CHUNK;
+        rc = read_scal(c);
+        if (rc != ISL_OK) break;
+        const CGScal h = *c->hscal;
+        if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
+        const bool at_max = h.iters >= mi;
+        if (h.done || h.rr < delta2 * rr_last || at_max) {
+            // reliable update: true residual in FP64
+            k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
+            launch_residual(c->spmv_lpr64, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64,
+                            c->dpart.p, ticket, dres);
+            c->launches += 2;
+            ISL_CHECK_CUDA(c, cudaMemcpyAsync(&rr_true, dres, 8, cudaMemcpyDeviceToHost, st));
+            ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+            if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
+            if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
+            if (at_max) { *nc = true; break; }
+            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p);
+            c->launches += 1;
+            rr_last = rr_true;
+        }
+    }
+    cudaGraphExecDestroy(exec);
+    if (rc != ISL_OK) return rc;
+    if (!converged && bnorm2 > 0) *nc = true;
+    rc = read_scal(c);
+    if (rc != ISL_OK) return rc;
+    *iters = c->hscal->iters;
+    *rel = bnorm2 > 0 ? std::sqrt(rr_true / bnorm2) : 0.0;
+    k_copy64<<<grid, BS, 0, st>>>((int)n, x64, c->dsol.p);
+    c->launches += 1;
+    return ISL_OK;
+}
+
+
+// ===========================================================================
+// Node-blocked (3x3 BSR) FP32 path of the mixed solver.  Every DOF object of
+// a 3-component field with all components active gives three consecutive
+// equations, so the CSR pattern is the node graph times 3x3 blocks.  The
+// block copy stores 4 bytes of column index per 9 values (4.4 bytes per
+// nonzero instead of 8), and the preconditioner inverts the 3x3 diagonal
+// blocks (block Jacobi).
+__global__ void k_bsr_pattern(int nbr, const int* __restrict__ rowptr, const int* __restrict__ colind, int* __restrict__ bptr,
+                              int* __restrict__ bcol, int* __restrict__ brow, int* __restrict__ bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbr; i += gridDim.x * blockDim.x) {
+        const int r0 = rowptr[3 * i], len = rowptr[3 * i + 1] - r0;
+        const int b0 = r0 / 9;
+        bptr[i] = b0;
+        if (i == nbr - 1) bptr[nbr] = rowptr[3 * nbr] / 9;
+        if (r0 % 9 != 0 || len % 3 != 0 || rowptr[3 * i + 2] - rowptr[3 * i + 1] != len ||
+            rowptr[3 * i + 3] - rowptr[3 * i + 2] != len) {
+            atomicOr(bad, 1);
+            continue;
+        }
+        for (int k = 0; k < len / 3; ++k) {
+            const int j3 = colind[r0 + 3 * k];
+            if (j3 % 3 != 0) atomicOr(bad, 1);
+            for (int r = 0; r < 3; ++r)
+                for (int cc = 0; cc < 3; ++cc)
+                    if (colind[rowptr[3 * i + r] + 3 * k + cc] != j3 + cc) atomicOr(bad, 1);
+            bcol[b0 + k] = j3 / 3;
+            brow[b0 + k] = i;
+        }
+    }
+}
+
+__global__ void k_bsr_values(int nblk, const int* __restrict__ brow, const int* __restrict__ bptr, const int* __restrict__ rowptr,
+                             const float* __restrict__ v32, float* __restrict__ bv) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblk; b += gridDim.x * blockDim.x) {
+        const int i = brow[b], k = b - bptr[i];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const int o = rowptr[3 * i + r] + 3 * k;
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) bv[(size_t)(r * 3 + cc) * nblk + b] = v32[o + cc];
+        }
+    }
+}
+
+// inverse of the 3x3 diagonal blocks, computed in FP64 from the FP64 values
+// when they exist
+template <typename TV>
+__global__ void k_block_jacobi(int nbr, const int* __restrict__ rowptr, const int* __restrict__ diag, const TV* __restrict__ val,
+                               float* __restrict__ binv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbr; i += gridDim.x * blockDim.x) {
+        const int k = (diag[3 * i] - rowptr[3 * i]) / 3;
+        double A[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int cc = 0; cc < 3; ++cc) A[r][cc] = (double)val[rowptr[3 * i + r] + 3 * k + cc];
+        const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+        const double c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+        const double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+        const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+        double Bi[3][3];
+        if (det != 0.0 && det == det) {
+            const double id = 1.0 / det;
+            Bi[0][0] = c00 * id; Bi[1][0] = c01 * id; Bi[2][0] = c02 * id;
+            Bi[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
+            Bi[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
+            Bi[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) * id;
+            Bi[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
+            Bi[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
+            Bi[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
+        } else {
+            for (int r = 0; r < 3; ++r)
+                for (int cc = 0; cc < 3; ++cc) Bi[r][cc] = (r == cc) ? 1.0 : 0.0;
+        }
+        for (int r = 0; r < 3; ++r)
+            for (int cc = 0; cc < 3; ++cc) binv[(size_t)(r * 3 + cc) * nbr + i] = (float)Bi[r][cc];
+    }
+}
+
+// q = A p (BSR, LPB lanes per block row); partial p.q; last block: alpha
+template <int LPB>
+__global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                  const float* __restrict__ bv, int nblk, const float* __restrict__ p,
+                                                  float* __restrict__ q, CGScal* S, double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x % LPB;
+    const int grp = (blockIdx.x * BS + threadIdx.x) / LPB, ngrp = gridDim.x * BS / LPB;
+    double loc = 0.0;
+    for (int i = grp; i < nbr; i += ngrp) {
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        const int lo = bptr[i], hi = bptr[i + 1];
+        for (int k = lo + lane; k < hi; k += LPB) {
+            const int j = __ldg(bcol + k);
+            const float x0 = __ldg(p + 3 * j), x1 = __ldg(p + 3 * j + 1), x2 = __ldg(p + 3 * j + 2);
+            a0 += __ldg(bv + k) * x0 + __ldg(bv + (size_t)nblk + k) * x1 + __ldg(bv + 2 * (size_t)nblk + k) * x2;
+            a1 += __ldg(bv + 3 * (size_t)nblk + k) * x0 + __ldg(bv + 4 * (size_t)nblk + k) * x1 + __ldg(bv + 5 * (size_t)nblk + k) * x2;
+            a2 += __ldg(bv + 6 * (size_t)nblk + k) * x0 + __ldg(bv + 7 * (size_t)nblk + k) * x1 + __ldg(bv + 8 * (size_t)nblk + k) * x2;
+        }
+#pragma unroll
+        for (int o = LPB / 2; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o, LPB);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o, LPB);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o, LPB);
+        }
+        if (lane == 0) {
+            q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
+            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+        }
+    }
+    const double bsum = block_sum(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    if (last_block(&S->ticket1)) {
+        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        if (threadIdx.x == 0) {
+            S->pAp = tot;
+            S->alpha = S->absNew / tot;
+            S->ticket1 = 0;
+        }
+    }
+}
+
+__device__ inline void bj_apply(const float* __restrict__ binv, int nbr, int i, const float r[3], float z[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        z[a] = binv[(size_t)(a * 3) * nbr + i] * r[0] + binv[(size_t)(a * 3 + 1) * nbr + i] * r[1] +
+               binv[(size_t)(a * 3 + 2) * nbr + i] * r[2];
+}
+
+__global__ void __launch_bounds__(BS) k_cg_update_b3(int nbr, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+                                                     const float* __restrict__ q, const float* __restrict__ binv, CGScal* S,
+                                                     double* part, int max_iter) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const float alpha = (float)S->alpha;
+    float rr = 0.f, rz = 0.f;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
+        float ri[3], zi[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            x[3 * i + a] += alpha * p[3 * i + a];
+            ri[a] = r[3 * i + a] - alpha * q[3 * i + a];
+            r[3 * i + a] = ri[a];
+        }
+        bj_apply(binv, nbr, i, ri, zi);
+        rr += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
+        rz += ri[0] * zi[0] + ri[1] * zi[1] + ri[2] * zi[2];
+    }
+    const double b1 = block_sum((double)rr, sh);
+    const double b2 = block_sum((double)rz, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (last_block(&S->ticket2)) {
+        const double trr = reduce_parts(part, gridDim.x, 2, 0, sh);
+        const double trz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        if (threadIdx.x == 0) {
+            S->rr = trr;
+            S->iters += 1;
+            S->absOld = S->absNew;
+            S->beta = trz / S->absNew;
+            S->absNew = trz;
+            if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
+            else if (trr < S->threshold) S->done = 1;
+            else if (S->iters >= max_iter) S->done = 2;
+            S->ticket2 = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BS) k_cg_dir_b3(int nbr, const float* __restrict__ r, const float* __restrict__ binv,
+                                                  float* __restrict__ p, const CGScal* S) {
+    if (S->done) return;
+    const float beta = (float)S->beta;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
+        const float ri[3] = {r[3 * i], r[3 * i + 1], r[3 * i + 2]};
+        float zi[3];
+        bj_apply(binv, nbr, i, ri, zi);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[3 * i + a] = zi[a] + beta * p[3 * i + a];
+    }
+}
+
+// x = 0, r = b, p = 0, absNew = r.B^{-1}r; with restart != 0 only r = r64 and
+// beta = (r.z)_new / (r.z)_previous (reliable update)
+__global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
+                                                   float* __restrict__ p, const float* __restrict__ binv, CGScal* S, double* part,
+                                                   double tol, int restart) {
+    __shared__ double sh[32];
+    double bb = 0.0, bz = 0.0;
+    for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
+        float ri[3], zi[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double bi = b[3 * i + a];
+            ri[a] = (float)bi;
+            r[3 * i + a] = ri[a];
+            if (!restart) { x[3 * i + a] = 0.f; p[3 * i + a] = 0.f; bb += bi * bi; }
+            else bb += (double)ri[a] * (double)ri[a];
+        }
+        bj_apply(binv, nbr, i, ri, zi);
+        bz += (double)ri[0] * zi[0] + (double)ri[1] * zi[1] + (double)ri[2] * zi[2];
+    }
+    const double b1 = block_sum(bb, sh);
+    const double b2 = block_sum(bz, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (last_block(&S->ticket2)) {
+        const double tbb = reduce_parts(part, gridDim.x, 2, 0, sh);
+        const double tbz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        if (threadIdx.x == 0) {
+            if (!restart) {
+                S->rhsNorm2 = tbb;
+                S->threshold = tol * tol * tbb;
+                S->absNew = tbz;
+                S->absOld = tbz;
+                S->beta = 0.0;
+                S->rr = tbb;
+                S->iters = 0;
+                S->bad = !(tbb == tbb);
+                S->done = (tbb == 0.0 || tbb < S->threshold || S->bad) ? 1 : 0;
+                S->ticket1 = 0;
+            } else {
+                S->rr = tbb;
+                S->beta = tbz / S->absOld;
+                S->absNew = tbz;
+                S->done = 0;
+            }
+            S->ticket2 = 0;
+        }
+    }
+}
+
+static void launch_bspmv(int lpb, unsigned grid, cudaStream_t st, isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
+    const int nbr = (int)c->nbr, nblk = (int)c->nblk;
+    switch (lpb) {
+        case 4: k_bspmv_pap<4><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
+        case 8: k_bspmv_pap<8><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
+        case 16: k_bspmv_pap<16><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
+        default: k_bspmv_pap<32><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
+    }
+}
+
+static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
+    const int cand[4] = {4, 8, 16, 32};
+    if (c->nbr < 8000) return 8;
+    int best = 8;
+    float bestms = 1e30f;
+    cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
+    c->launches += 24;
+    for (int k = 0; k < 4; ++k) {
+        launch_bspmv(cand[k], vec_grid(c), c->stream, c, p, q, S, part);
+        cudaEventRecord(c->ev[2], c->stream);
+        for (int r = 0; r < 5; ++r) launch_bspmv(cand[k], vec_grid(c), c->stream, c, p, q, S, part);
+        cudaEventRecord(c->ev[3], c->stream);
+        cudaEventSynchronize(c->ev[3]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        if (ms < bestms) { bestms = ms; best = cand[k]; }
+    }
+    return best;
+}
+
+// detect the node-blocked structure and build the block pattern (setup)
+int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
+    c->blocked = false;
+    if (c->ncomp != 3 || c->neq % 3 != 0) return ISL_OK;
+    for (int64_t o = 0; o < c->ndofobj; ++o) {
+        const uint8_t s0 = c->status[(size_t)o * 3];
+        if (c->status[(size_t)o * 3 + 1] != s0 || c->status[(size_t)o * 3 + 2] != s0) return ISL_OK;
+    }
+    const int64_t nbr = c->neq / 3;
+    for (int64_t i = 0; i < nbr; ++i) {
+        const int32_t len = rp[3 * i + 1] - rp[3 * i];
+        if (rp[3 * i] % 9 || len % 3 || rp[3 * i + 2] - rp[3 * i + 1] != len || rp[3 * i + 3] - rp[3 * i + 2] != len) return ISL_OK;
+    }
+    c->nbr = nbr;
+    c->nblk = c->nnz / 9;
+    ISL_CHECK_CUDA(c, c->dbptr.alloc(nbr + 1));
+    ISL_CHECK_CUDA(c, c->dbcol.alloc(c->nblk));
+    ISL_CHECK_CUDA(c, c->dbrow.alloc(c->nblk));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), c->stream));
+    k_bsr_pattern<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, c->drowptr.p, c->dcolind.p, c->dbptr.p, c->dbcol.p, c->dbrow.p,
+                                                     c->dflags.p + 1);
+    int bad = 0;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&bad, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->launches += 1;
+    c->blocked = (bad == 0);
+    c->bsr_serial = -1;
+    c->bspmv_lpb = 0;
+    return ISL_OK;
+}
+
+// refresh the block values and the block-Jacobi inverses after an assembly
+static int ensure_bsr(isl_ctx* c) {
+    if (c->bsr_serial == c->asm_serial) return ISL_OK;
+    ISL_CHECK_CUDA(c, c->dbval.alloc((size_t)9 * c->nblk));
+    ISL_CHECK_CUDA(c, c->dbinv.alloc((size_t)9 * c->nbr));
+    const unsigned grid = vec_grid(c);
+    k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p, c->dbval.p);
+    if (c->have64)
+        k_block_jacobi<double><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval64.p, c->dbinv.p);
+    else
+        k_block_jacobi<float><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval32.p, c->dbinv.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 2;
+    c->bsr_serial = c->asm_serial;
+    return ISL_OK;
+}
+
+// mixed solve on the block copy: FP32 block-Jacobi CG with FP64 reliable updates
+static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
+    int rc = ensure_bsr(c);
+    if (rc != ISL_OK) return rc;
+    cudaStream_t st = c->stream;
+    const size_t n = (size_t)c->neq;
+    const int nbr = (int)c->nbr;
+    double* W = c->w64.p;
+    double *x64 = W, *r64 = W + n;
+    float* V = c->w32.p;
+    float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n;
+    if (!c->bspmv_lpb) {
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, n * 4, st));
+        c->bspmv_lpb = autotune_lpb(c, p32, q32, c->dscal.p, c->dpart.p);
+    }
+    if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
+    const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    const unsigned grid = vec_grid(c);
+    CGScal* S = c->dscal.p;
+    double* dres = (double*)(c->dscal.p + 1);
+    unsigned* ticket = &(c->dscal.p + 1)->ticket1;
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
+    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < CHUNK; ++k) {
+        k_cg_dir_b3<<<grid, BS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
+        launch_bspmv(c->bspmv_lpb, grid, st, c, p32, q32, S, c->dpart.p);
+        k_cg_update_b3<<<grid, BS, 0, st>>>(nbr, x32, r32, p32, q32, c->dbinv.p, S, c->dpart.p, mi);
+    }
+    ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
+    {
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ISL_CHECK_CUDA(c, e);
+    }
+    rc = read_scal(c);
+    const double bnorm2 = c->hscal->rhsNorm2;
+    double rr_last = bnorm2, rr_true = bnorm2;
+    const double delta2 = 1e-2;
+    const int64_t max_replays = (int64_t)mi / CHUNK + 64;
+    int64_t replays = 0;
+    bool converged = (bnorm2 == 0.0);
+    while (rc == ISL_OK && !converged) {
+        if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "mixed CG made no progress"; break; }
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
+        c->launches += 3 * CHUNK;
+        rc = read_scal(c);
+        if (rc != ISL_OK) break;
+        const CGScal h = *c->hscal;
+        if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
+        const bool at_max = h.iters >= mi;
+        if (h.done || h.rr < delta2 * rr_last || at_max) {
+            k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
+            launch_residual(c->spmv_lpr64, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64,
+                            c->dpart.p, ticket, dres);
+            c->launches += 2;
+            ISL_CHECK_CUDA(c, cudaMemcpyAsync(&rr_true, dres, 8, cudaMemcpyDeviceToHost, st));
+            ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+            if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
+            if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
+            if (at_max) { *nc = true; break; }
+            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 1);
+            c->launches += 1;
+            rr_last = rr_true;
+        }
+    }
+    cudaGraphExecDestroy(exec);
+    if (rc != ISL_OK) return rc;
+    if (!converged && bnorm2 > 0) *nc = true;
+    rc = read_scal(c);
+    if (rc != ISL_OK) return rc;
+    *iters = c->hscal->iters;
+    *rel = bnorm2 > 0 ? std::sqrt(rr_true / bnorm2) : 0.0;
+    k_copy64<<<grid, BS, 0, st>>>((int)n, x64, c->dsol.p);
+    c->launches += 1;
+    return ISL_OK;
+}
+
+int time_bspmv(isl_ctx* c, int nrep, double* ms) {
+    int rc = ensure_bsr(c);
+    if (rc != ISL_OK) return rc;
+    const size_t n = (size_t)c->neq;
+    CGScal* S = c->dscal.p;
+    float* V = c->w32.p;
+    cudaStream_t st = c->stream;
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(S, 0, sizeof(CGScal), st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
+    if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    cudaEventRecord(c->ev[2], st);
+    for (int r = 0; r < nrep; ++r) launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    cudaEventRecord(c->ev[3], st);
+    c->launches += nrep + 1;
+    ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
+    *ms = t / nrep;
+    return ISL_OK;
+}
+
+int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
+    int rc = ensure_work(c);
+    if (rc != ISL_OK) return rc;
+    cudaStream_t st = c->stream;
+    if (max_iter <= 0) max_iter = 2 * (int64_t)c->neq;
+    if (c->timing) cudaEventRecord(c->ev[0], st);
+    int64_t it = 0;
     double rel = 0.0;
     bool nc = false;
-    if (method == ISL_SOLVE_CG_FP64) {
-        if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, q, c->dscal.p, c->dpart.p);
-        double rr = 0, b2 = 0;
-        rc = run_cg<double, double>(c, c->dval64.p, c->drhs.p, x, r, p, q, dinv, tol, max_iter, c->spmv_lpr64, &total_it, &rr, &b2, &nc);
-        if (rc != ISL_OK) return rc;
-        rel = b2 > 0 ? std::sqrt(rr / b2) : 0.0;
-        k_copy64<<<vec_grid(c), BS, 0, st>>>((int)n, x, c->dsol.p);
-    } else {
-        // FP64 iterative refinement around FP32 CG
-        float* V = c->w32.p;
-        float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n, *b32 = V + 5 * n;
-        if (!c->spmv_lpr32) c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, b32, q32, c->dscal.p, c->dpart.p);
-        if (!c->spmv_lpr64 && c->have64)
-            c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, q, c->dscal.p, c->dpart.p);
-        const bool exact64 = c->have64;  // FP64 residual operator available
-        ISL_CHECK_CUDA(c, cudaMemsetAsync(x, 0, n * 8, st));
-        double* dres = (double*)(c->dscal.p + 1);  // scratch scalar slot
-        unsigned* ticket = &(c->dscal.p + 1)->ticket1;
-        ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p + 1, 0, sizeof(CGScal), st));
-        // b norm
-        k_copy64<<<vec_grid(c), BS, 0, st>>>((int)n, c->drhs.p, r64);
-        double bnorm2 = 0.0;
-        {
-            std::vector<double> hb(n);
-            ISL_CHECK_CUDA(c, cudaMemcpyAsync(hb.data(), c->drhs.p, n * 8, cudaMemcpyDeviceToHost, st));
-            ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
-            for (double v : hb) bnorm2 += v * v;
-        }
-        double rnorm2 = bnorm2;
-        const double eta = 1e-4;  // inner relative tolerance
-        const int max_outer = 60;
-        if (bnorm2 == 0.0) {
-            ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dsol.p, 0, n * 8, st));
-        } else {
-            for (int outer = 0; outer < max_outer; ++outer) {
-                if (rnorm2 <= tol * tol * bnorm2) break;
-                if (total_it >= max_iter) { nc = true; break; }
-                const double rn = std::sqrt(rnorm2);
-                k_scale_to32<<<vec_grid(c), BS, 0, st>>>((int)n, r64, 1.0 / rn, b32);
-                int64_t it = 0;
-                bool inc = false;
-                rc = run_cg<float, float>(c, c->dval32.p, b32, d32, r32, p32, q32, x32 /*dinv*/, eta, max_iter - total_it,
-                                          c->spmv_lpr32, &it, nullptr, nullptr, &inc);
-                if (rc != ISL_OK) return rc;
-                total_it += it;
-                k_axpy32to64<<<vec_grid(c), BS, 0, st>>>((int)n, rn, d32, x);
-                if (!exact64) {
-                    // no FP64 operator: refinement residual from the FP32 matrix is not
-                    // FP64-accurate; stop after one inner solve
-                    rnorm2 = 0.0;
-                    break;
-                }
-                launch_residual(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x, c->drhs.p, r64,
-                                c->dpart.p, ticket, dres);
-                ISL_CHECK_CUDA(c, cudaMemcpyAsync(&rnorm2, dres, 8, cudaMemcpyDeviceToHost, st));
-                ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
-                if (!(rnorm2 == rnorm2)) ISL_FAIL(c, ISL_ERR_NAN, "refinement residual is not finite");
-            }
-        }
-        rel = bnorm2 > 0 ? std::sqrt(rnorm2 / bnorm2) : 0.0;
-        if (rel > tol && exact64) nc = true;
-        k_copy64<<<vec_grid(c), BS, 0, st>>>((int)n, x, c->dsol.p);
-    }
+    if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
+    else if (c->blocked && c->use_block && c->have64) rc = solve_mixed_b3(c, tol, max_iter, &it, &rel, &nc);
+    else rc = solve_mixed(c, tol, max_iter, &it, &rel, &nc);
+    if (rc != ISL_OK) return rc;
     ISL_CHECK_CUDA(c, cudaGetLastError());
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
     if (c->timing) {
@@ -427,7 +901,7 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
         c->tcount[ISL_T_SOLVE]++;
     }
     c->solved = true;
-    if (iters) *iters = total_it;
+    if (iters) *iters = it;
     if (relres) *relres = rel;
     if (nc) ISL_FAIL(c, ISL_ERR_NOT_CONVERGED, "solver did not reach the tolerance");
     return ISL_OK;
@@ -445,6 +919,7 @@ int distribute_device(isl_ctx* c, int add) {
     const int64_t ndc = c->ndofobj * c->ncomp;
     k_distribute<<<vec_grid(c), BS, 0, c->stream>>>(ndc, c->deq.p, c->dstatus.p, c->dcval.p, c->dsol.p, c->du.p, add);
     ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
 }
@@ -456,9 +931,14 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     CGScal* S = c->dscal.p;
     cudaStream_t st = c->stream;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(S, 0, sizeof(CGScal), st));
+    if (precision == ISL_PREC_FP32 && c->blocked && c->use_block) {
+        if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
+        return time_bspmv(c, nrep, ms);
+    }
     if (precision == ISL_PREC_FP32) {
         if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
         float* V = c->w32.p;
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
         if (!c->spmv_lpr32) c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, V + 2 * n, V + 3 * n, S, c->dpart.p);
         launch_spmv<float, float>(c->spmv_lpr32, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval32.p, V + 2 * n, V + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[2], st);
@@ -468,6 +948,7 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     } else {
         if (!c->have64) ISL_FAIL(c, ISL_ERR_ARG, "no FP64 matrix");
         double* W = c->w64.p;
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(W + 2 * n, 0, n * 8, st));
         if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
         launch_spmv<double, double>(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[2], st);
@@ -475,6 +956,7 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
             launch_spmv<double, double>(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[3], st);
     }
+    c->launches += nrep + 1;
     ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
     float t = 0.f;
     cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);

@@ -210,3 +210,24 @@ class System:
         v = C.c_double()
         self._chk(self.L.isl_time_spmv(self.h, precision, nrep, C.byref(v)), "isl_time_spmv")
         return v.value
+
+    def mark(self, slot: int):
+        self._chk(self.L.isl_mark(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = C.c_double()
+        self._chk(self.L.isl_elapsed(self.h, a, b, C.byref(v)))
+        return v.value
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._chk(self.L.isl_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def set_option(self, key: int, value: int):
+        self._chk(self.L.isl_set_option(self.h, key, value), "isl_set_option")
+
+    def get_option(self, key: int) -> int:
+        v = C.c_int64()
+        self._chk(self.L.isl_get_option(self.h, key, C.byref(v)), "isl_get_option")
+        return v.value

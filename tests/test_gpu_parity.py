@@ -1,0 +1,194 @@
+"""GPU parity against the oracle, through the C-ABI (libisl_gpu.so).
+
+Bars:
+  * DOF numbering and CSR pattern: bit-exact.
+  * FP64 matrix entries: |K_gpu - K_oracle| <= 1e-12 max(|K_oracle|, 1e-12 max|K|).
+  * RHS: same bar.
+  * FP64 CG solution vs the oracle's CG solution (both to 1e-13): rel L2 <= 1e-9.
+  * Mixed FP32-CG + FP64 refinement to 1e-12: rel L2 error vs FP64 <= 1e-8.
+  * Assembly and solve are bit-reproducible run to run (no atomics).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from insilico_gb300 import _abi as A
+from insilico_gb300 import workloads as W
+
+from helpers import oracle_problem, rel_entry_err
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("c1", 12), ("c2", 4), ("c3", 3), ("c1", 1), ("c2", 1)]
+
+
+@pytest.fixture(scope="module")
+def systems():
+    out = {}
+    yield out
+    for S in out.values():
+        S.close()
+
+
+def gpu_problem(p):
+    S = W.setup_system(p)
+    return S
+
+
+@pytest.mark.parametrize("name,n", CASES)
+def test_pattern_values_rhs_match_oracle(name, n):
+    p = W.config(name, n=n)
+    S = gpu_problem(p)
+    P, (rp, ci, v, b) = oracle_problem(p)
+    assert S.neq == P.neq
+    np.testing.assert_array_equal(S.dof_index(), P.eq_index())
+    S.assemble(A.PREC_FP64)
+    grp, gci, gv = S.csr()
+    np.testing.assert_array_equal(grp, rp)
+    np.testing.assert_array_equal(gci, ci)
+    assert rel_entry_err(gv, v) <= 1e-12
+    gb = S.rhs()
+    assert np.max(np.abs(gb - b)) <= 1e-12 * max(np.max(np.abs(b)), 1e-300)
+    S.close()
+
+
+@pytest.mark.parametrize("name,n", [("c1", 12), ("c2", 4), ("c3", 3)])
+def test_cg_fp64_and_mixed_solution(name, n):
+    p = W.config(name, n=n)
+    S = gpu_problem(p)
+    P, (rp, ci, v, b) = oracle_problem(p)
+    xo, _, _ = O.cg(rp, ci, v, b, tol=1e-13)
+    S.assemble(A.PREC_MIXED)
+    it, rr, _ = S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    assert np.linalg.norm(x64 - xo) <= 1e-9 * np.linalg.norm(xo)
+    it2, rr2, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xm = S.solution()
+    assert rr2 <= 1e-12
+    assert np.linalg.norm(xm - xo) <= 1e-8 * np.linalg.norm(xo)
+    S.close()
+
+
+@pytest.mark.parametrize("name,n", [("c1", 16), ("c2", 5)])
+def test_bitwise_reproducible(name, n):
+    p = W.config(name, n=n)
+    S = gpu_problem(p)
+    S.assemble(A.PREC_FP64)
+    _, _, v1 = S.csr()
+    b1 = S.rhs()
+    S.solve(A.SOLVE_CG_FP64, tol=1e-12)
+    x1 = S.solution()
+    S.assemble(A.PREC_FP64)
+    _, _, v2 = S.csr()
+    b2 = S.rhs()
+    S.solve(A.SOLVE_CG_FP64, tol=1e-12)
+    x2 = S.solution()
+    assert np.array_equal(v1, v2) and np.array_equal(b1, b2) and np.array_equal(x1, x2)
+    S.close()
+
+
+@pytest.mark.parametrize("name,n", [("c1", 10), ("c2", 3), ("c3", 2)])
+def test_fp32_assembly_close_to_fp64(name, n):
+    p = W.config(name, n=n)
+    S = gpu_problem(p)
+    S.assemble(A.PREC_FP64)
+    _, _, v64 = S.csr()
+    b64 = S.rhs()
+    S.assemble(A.PREC_FP32)
+    _, _, v32 = S.csr()
+    assert rel_entry_err(v32, v64, floor_frac=1e-6) <= 2e-6
+    np.testing.assert_allclose(S.rhs(), b64, rtol=0, atol=1e-12 * np.abs(b64).max())
+    S.close()
+
+
+@pytest.mark.parametrize("material", ["stvenant", "neohooke"])
+def test_hyperelastic_tangent_and_residual_at_displacement(material):
+    p = W.config("c2", n=3)
+    p.material = material
+    S = gpu_problem(p)
+    P, _ = oracle_problem(p, assemble=False)
+    rs = np.random.default_rng(7)
+    u = 0.02 * rs.standard_normal(S.ndofobj * 3)
+    # constrained components carry their constraint value (zero on the clamp)
+    eq = S.dof_index()
+    u[eq < 0] = 0.0
+    S.set_values(u)
+    P.set_values(u)
+    rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+    S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+    grp, gci, gv = S.csr()
+    np.testing.assert_array_equal(gci, ci)
+    assert rel_entry_err(gv, v) <= 1e-11
+    gb = S.rhs()
+    assert np.max(np.abs(gb - b)) <= 1e-11 * np.max(np.abs(b))
+    # FP32 tangent, FP64 residual
+    S.assemble(A.PREC_FP32, incremental=True, with_residual=True)
+    assert np.max(np.abs(S.rhs() - b)) <= 1e-11 * np.max(np.abs(b))
+    S.close()
+
+
+def test_degenerate_element_reports_status():
+    X = np.array([[0, 0], [1, 0], [2, 0], [3, 0]], dtype=float)  # collinear: det J = 0
+    from insilico_gb300.system import System
+    S = System()
+    S.upload_mesh(A.QUAD, X, np.array([[0, 1, 2, 3]]))
+    S.create_field(1, 1)
+    S.number_dofs()
+    S.register_pattern()
+    S.set_laplace(np.ones(1), 2)
+    with pytest.raises(A.IslError) as ei:
+        S.assemble(A.PREC_FP64)
+    assert ei.value.code == A.ISL_ERR_DEGENERATE
+    S.close()
+
+
+def test_max_iter_reports_not_converged():
+    p = W.config("c1", n=16)
+    S = gpu_problem(p)
+    S.assemble(A.PREC_FP64)
+    it, rr, st = S.solve(A.SOLVE_CG_FP64, tol=1e-14, max_iter=3, check=False)
+    assert st == A.ISL_ERR_NOT_CONVERGED and it == 3
+    S.close()
+
+
+def test_block_and_scalar_mixed_paths_agree():
+    p = W.config("c2", n=4)
+    S = gpu_problem(p)
+    assert S.get_option(A.OPT_BLOCKED) == 1
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xb = S.solution()
+    S.set_option(A.OPT_BLOCK_SOLVER, 0)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xs = S.solution()
+    assert np.linalg.norm(xb - x64) <= 1e-8 * np.linalg.norm(x64)
+    assert np.linalg.norm(xs - x64) <= 1e-8 * np.linalg.norm(x64)
+    S.close()
+
+
+def test_partially_constrained_nodes_use_scalar_path():
+    # x = 1 face pulls u_x only (PulledSheet-style): nodes there are partly active
+    p = W.config("c2", n=3)
+    base = p.dirichlet
+
+    def diri(x):
+        m, v = base(x)
+        m = m.copy()
+        m[np.abs(x[:, 0] - 1.0) < 1e-9, 0] = True
+        vals = np.zeros(m.shape)
+        vals[np.abs(x[:, 0] - 1.0) < 1e-9, 0] = 0.01
+        return m, vals
+    p.dirichlet = diri
+    p.neumann_plane = None
+    S = gpu_problem(p)
+    assert S.get_option(A.OPT_BLOCKED) == 0
+    P, (rp, ci, v, b) = oracle_problem(p)
+    S.assemble(A.PREC_MIXED)
+    np.testing.assert_array_equal(S.csr(values=False)[1], ci)
+    assert np.max(np.abs(S.rhs() - b)) <= 1e-12 * np.max(np.abs(b))
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xo, _, _ = O.cg(rp, ci, v, b, tol=1e-13)
+    assert np.linalg.norm(S.solution() - xo) <= 1e-8 * np.linalg.norm(xo)
+    S.close()
