@@ -136,7 +136,10 @@ int isl_assemble(isl_ctx* ctx, int precision, int incremental, int with_residual
  *   ISL_SOLVE_CG_FP32_IR: FP32 CG (FP64 dot reductions) with FP64 reliable
  *                         updates: the FP64 residual b - A64 x replaces the
  *                         iterated one each time it has dropped 10x; ends
- *                         when the FP64 residual meets the tolerance.
+ *                         when the FP64 residual meets the tolerance.  After
+ *                         an ISL_PREC_FP32 assembly (no FP64 matrix) it is a
+ *                         plain FP32 CG on the iterated residual, the inexact
+ *                         linear solve of a Newton step whose residual is FP64.
  * max_iter <= 0 means 2N.  iters/rel_res may be NULL. */
 int isl_solve(isl_ctx* ctx, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res);
 
@@ -171,6 +174,9 @@ int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
  * elapsed time between two of them, for timing regions from the host. */
 int isl_mark(isl_ctx* ctx, int slot);
 int isl_elapsed(isl_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Free and total device memory (cudaMemGetInfo) of a device, for admission
+ * control of served requests. */
+int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes);
 /* Number of kernel launches (graph kernel nodes included) issued by the
  * context since creation. */
 int isl_launch_count(isl_ctx* ctx, int64_t* n);

@@ -365,8 +365,10 @@ int isl_ctx_destroy(isl_ctx* c) {
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
     for (auto& ev : c->mark) if (ev) cudaEventDestroy(ev);
     if (c->hscal) cudaFreeHost(c->hscal);
-    if (c->own_stream) cudaStreamDestroy(c->stream);
-    delete c;
+    cudaStream_t own = c->own_stream ? c->stream : nullptr;
+    delete c;  // frees the device buffers (stream-ordered)
+    cudaStreamSynchronize(cudaStreamPerThread);
+    if (own) cudaStreamDestroy(own);
     return ISL_OK;
 }
 
@@ -754,8 +756,8 @@ int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) 
 int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res) {
     if (!c || !c->nnz) ISL_FAIL(c, ISL_ERR_ARG, "solve: nothing assembled");
     if (method == ISL_SOLVE_CG_FP64 && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "solve: no FP64 matrix assembled");
-    if (method == ISL_SOLVE_CG_FP32_IR && !(c->have64 && c->have32) && !(c->have32 && c->kernel == ISL_KERNEL_HYPERELASTIC))
-        ISL_FAIL(c, ISL_ERR_ARG, "solve: mixed solve needs FP64 and FP32 matrices (ISL_PREC_MIXED)");
+    if (method == ISL_SOLVE_CG_FP32_IR && !c->have32)
+        ISL_FAIL(c, ISL_ERR_ARG, "solve: the FP32 solve needs an FP32 matrix (ISL_PREC_MIXED or ISL_PREC_FP32)");
     if (!(tol >= 0.0)) ISL_FAIL(c, ISL_ERR_ARG, "tol");
     cudaSetDevice(c->device);
     return isl::solve_device(c, method, tol, max_iter, iters, rel_res);
@@ -880,6 +882,20 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
+}
+
+int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return ISL_ERR_ARG;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cudaSetDevice(device) != cudaSuccess) return ISL_ERR_CUDA;
+    size_t f = 0, t = 0;
+    const cudaError_t e = cudaMemGetInfo(&f, &t);
+    cudaSetDevice(cur);
+    if (e != cudaSuccess) return ISL_ERR_CUDA;
+    *free_bytes = (int64_t)f;
+    *total_bytes = (int64_t)t;
+    return ISL_OK;
 }
 
 }  // extern "C"

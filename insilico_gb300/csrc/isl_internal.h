@@ -51,7 +51,11 @@ struct FaceTab {
 bool make_face_tables(int shape, int fedeg, int sqdeg, FaceTab& t);
 
 // ---------------------------------------------------------------------------
-// Device buffer with RAII
+// Device buffer with RAII.  Memory comes from the stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync on the per-thread stream), so allocating or
+// freeing never synchronises the device: contexts serving concurrent requests
+// keep overlapping.  Buffers are only released after the owning context's
+// stream has been synchronised.
 template <typename T>
 struct DBuf {
     T* p = nullptr;
@@ -61,7 +65,7 @@ struct DBuf {
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, cudaStreamPerThread);
         p = nullptr;
         n = 0;
     }
@@ -69,7 +73,8 @@ struct DBuf {
         if (count == n && p) return cudaSuccess;
         release();
         if (count == 0) return cudaSuccess;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), cudaStreamPerThread);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamPerThread);
         if (e == cudaSuccess) n = count;
         else p = nullptr;
         return e;

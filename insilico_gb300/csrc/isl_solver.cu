@@ -406,7 +406,9 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
         ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, n * 4, st));
         c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, p32, q32, c->dscal.p, c->dpart.p);
     }
-    if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
+    const bool exact64 = c->have64;  // without the FP64 matrix: plain FP32 CG (inexact Newton tangents)
+    if (exact64 && !c->spmv_lpr64)
+        c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
     const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
     const unsigned grid = vec_grid(c);
     CGScal* S = c->dscal.p;
@@ -437,6 +439,17 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
         const CGScal h = *c->hscal;
         if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
         const bool at_max = h.iters >= mi;
+        if (!exact64) {
+            if (h.done || at_max) {
+                k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
+                c->launches += 1;
+                rr_true = h.rr;
+                converged = h.done == 1;
+                if (!converged) *nc = true;
+                break;
+            }
+            continue;
+        }
         if (h.done || h.rr < delta2 * rr_last || at_max) {
             // reliable update: true residual in FP64
             k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);

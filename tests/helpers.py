@@ -43,3 +43,37 @@ def rel_entry_err(a, b, floor_frac=1e-12):
     b = np.asarray(b, dtype=np.float64)
     scale = np.maximum(np.abs(b), floor_frac * np.abs(b).max())
     return float(np.max(np.abs(a - b) / scale))
+
+
+def oracle_newton(req, rtol=1e-10, max_newton=30, lin_tol=1e-12):
+    """The served Newton problem on the oracle: neo-Hookean hex8 cube, x = 0
+    clamped, u_x prescribed on x = 1, load steps scaled as
+    solid/CompressibleDriver.hpp:165-172, Newton as :180-211."""
+    X, conn = W.unit_cube("hex", req.side, req.side, req.side)
+    P = O.Problem(O.HEX, X, conn, 1, 3)
+    x, d = P.boundary_points()
+    first = req.pull / req.load_steps
+    dofs, comps, vals = [], [], []
+    for xi, di in zip(x, d):
+        if abs(xi[0]) < 1e-9:
+            for c in range(3):
+                dofs.append(di); comps.append(c); vals.append(0.0)
+        if abs(xi[0] - 1.0) < 1e-9:
+            dofs.append(di); comps.append(0); vals.append(first)
+    P.constrain(dofs, comps, vals)
+    neq = P.number()
+    ne = len(conn)
+    P.set_hyperelastic("neohooke", np.full(ne, req.lam), np.full(ne, req.mu), 3)
+    norm0 = None
+    for step in range(req.load_steps):
+        P.scale_constraints(float(step + 1) if step == 0 else (step + 1) / step)
+        for it in range(max_newton):
+            rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+            conv1 = np.linalg.norm(b) / neq
+            if it == 0:
+                norm0 = conv1
+            if conv1 <= rtol * norm0 and it > 0:
+                break
+            xs, _, _ = O.cg(rp, ci, v, b, tol=lin_tol)
+            P.distribute(xs, add=True)
+    return P.values()
