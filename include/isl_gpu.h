@@ -69,6 +69,22 @@ const char* isl_last_error(const isl_ctx* ctx);
 int isl_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_nodes, const double* coords, int64_t n_elem,
                     const int64_t* conn);
 
+/* Batch of independent meshes in one context (the batched-instances path):
+ * node_off / elem_off [n_inst+1] delimit each instance's nodes and elements
+ * in the concatenated coords / conn (conn holds global node ids; an element
+ * only uses nodes of its own instance).  DOF objects and equations are
+ * numbered per instance exactly as for a single mesh and concatenated; the
+ * assembly runs over all instances in the same launches, and isl_solve runs
+ * one CG per instance (own scalars, own convergence) in the same launches.
+ * No reference counterpart: the reference assembles one mesh at a time. */
+int isl_batch_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_inst, const int64_t* node_off, const double* coords,
+                          const int64_t* elem_off, const int64_t* conn);
+/* n_inst, equation offsets [n_inst+1] and DOF-object offsets [n_inst+1] of the
+ * instances (either array may be NULL). */
+int isl_batch_info(isl_ctx* ctx, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off);
+/* Per-instance CG iterations and final relative residuals of the last solve. */
+int isl_batch_solve_stats(isl_ctx* ctx, int64_t* iters, double* rel_res);
+
 /* Field of Lagrange degree fe_degree with ncomp components per DOF object;
  * generates the DOF-object ids per element.
  * Replaces base::dof::generate (base/dof/generate.hpp:65-115 ->

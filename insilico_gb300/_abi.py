@@ -35,7 +35,8 @@ EXPORTED = [
     "isl_set_hyperelastic", "isl_set_body_force_nodal", "isl_set_neumann", "isl_set_values", "isl_get_values",
     "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
     "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
-    "isl_set_option", "isl_get_option", "isl_device_memory",
+    "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
+    "isl_batch_solve_stats",
 ]
 OPT_BLOCK_SOLVER, OPT_BLOCKED = 0, 1
 
@@ -106,6 +107,9 @@ def load(build_if_missing: bool = False):
     L.isl_set_option.argtypes = [_P, i, C.c_int64]
     L.isl_get_option.argtypes = [_P, i, _I64]
     L.isl_device_memory.argtypes = [i, _I64, _I64]
+    L.isl_batch_mesh_upload.argtypes = [_P, i, i, C.c_int64, _I64, _D, _I64, _I64]
+    L.isl_batch_info.argtypes = [_P, _I64, _I64, _I64]
+    L.isl_batch_solve_stats.argtypes = [_P, _I64, _D]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "isl_last_error":

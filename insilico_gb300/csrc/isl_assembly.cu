@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
             for (int d = 0; d < 3; ++d) su[(role * 3 + d) * EPB + el] = A.u[(size_t)obj * 3 + d];
         }
     }
+    __syncthreads();
     // affine elements (parallelepipeds): one FP64 Jacobian per element, by role 0
     __shared__ double sJi[10][EPB];
     __shared__ int saff[EPB];

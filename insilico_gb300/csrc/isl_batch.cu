@@ -1,0 +1,462 @@
+// Batched Krylov solve: many independent instances (disjoint row ranges of
+// one block-diagonal system) each run their own Jacobi-preconditioned CG with
+// their own scalars, convergence test and iteration count, in the same
+// kernel launches.  Thread blocks are assigned to row ranges of a single
+// instance; each instance's reductions are summed by the last of its blocks
+// (per-instance ticket), in a fixed order.  CHUNK iterations are captured
+// into one CUDA graph and replayed until every instance is done; blocks of
+// finished instances return at once.
+//
+// Mixed method: FP32 CG with FP64 reliable updates per instance, inside the
+// graph: an instance whose iterated residual dropped 10x (or met the
+// tolerance) folds its FP32 increment into the FP64 iterate, recomputes its
+// FP64 residual b - A64 x and resumes; it finishes when the FP64 residual
+// meets the tolerance.
+#include <cmath>
+#include <vector>
+
+#include "isl_device.cuh"
+#include "isl_internal.h"
+
+namespace isl {
+
+namespace {
+
+constexpr int BBS = 256;
+constexpr int BCHUNK = 32;
+constexpr int ROWS_PER_BLOCK = 2048;
+
+// per-instance scalar slots in dbs [slot][ninst]
+enum { S_ABSNEW, S_ABSOLD, S_ALPHA, S_BETA, S_RR, S_THRESH, S_RHS2, S_RRLAST, S_NS };
+// per-instance int slots in dbi [slot][ninst]
+enum { I_DONE, I_ITERS, I_BAD, I_UPDATE, I_NI };
+// ticket slots in dbt [slot][ninst]; slot 3 element 0 counts remaining instances
+enum { T_SPMV, T_UPD, T_RES, T_NT };
+
+struct BArgs {
+    int ninst;
+    const int* blk_inst;
+    const int* blk_r0;
+    const int* blk_r1;
+    const int* inst_blk;  // [ninst+1]
+    double* s;            // [S_NS][ninst]
+    int* iv;              // [I_NI][ninst]
+    unsigned* t;          // [T_NT][ninst]
+    int* remaining;
+    double* part;         // [2][nblocks]
+    int max_iter;
+    double tol;
+};
+
+__device__ inline double& SS(const BArgs& a, int slot, int k) { return a.s[(size_t)slot * a.ninst + k]; }
+__device__ inline int& II(const BArgs& a, int slot, int k) { return a.iv[(size_t)slot * a.ninst + k]; }
+
+__device__ inline void finish(const BArgs& a, int k, int code) {
+    if (II(a, I_DONE, k) == 0) {
+        II(a, I_DONE, k) = code;
+        atomicSub(a.remaining, 1);
+    }
+}
+
+__device__ inline double inst_sum(const BArgs& a, int k, int off, double* sh) {
+    const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
+    double v = 0.0;
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) v += __ldcg(a.part + (size_t)off * gridDim.x + i);
+    return block_sum(v, sh);
+}
+
+template <typename TB, typename TX>
+__global__ void __launch_bounds__(BBS) kb_init(BArgs a, const TB* __restrict__ b, TX* __restrict__ x, TX* __restrict__ r,
+                                               TX* __restrict__ p, const TX* __restrict__ dinv) {
+    __shared__ double sh[32];
+    const int k = a.blk_inst[blockIdx.x], r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    double bb = 0.0, bz = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+        const TB bi = b[i];
+        const TX ri = (TX)bi;
+        x[i] = TX(0);
+        r[i] = ri;
+        p[i] = TX(0);
+        bb += (double)bi * (double)bi;
+        bz += (double)ri * (double)(dinv[i] * ri);
+    }
+    const double s1 = block_sum(bb, sh), s2 = block_sum(bz, sh);
+    if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[gridDim.x + blockIdx.x] = s2; }
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {
+        const double tbb = inst_sum(a, k, 0, sh), tbz = inst_sum(a, k, 1, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_RHS2, k) = tbb;
+            SS(a, S_THRESH, k) = a.tol * a.tol * tbb;
+            SS(a, S_ABSNEW, k) = tbz;
+            SS(a, S_ABSOLD, k) = tbz;
+            SS(a, S_BETA, k) = 0.0;
+            SS(a, S_RR, k) = tbb;
+            SS(a, S_RRLAST, k) = tbb;
+            II(a, I_ITERS, k) = 0;
+            II(a, I_UPDATE, k) = 0;
+            II(a, I_BAD, k) = !(tbb == tbb);
+            if (tbb == 0.0 || !(tbb == tbb)) finish(a, k, 1);
+            a.t[T_UPD * a.ninst + k] = 0;
+        }
+    }
+}
+
+template <typename TX>
+__global__ void __launch_bounds__(BBS) kb_dir(BArgs a, const TX* __restrict__ r, const TX* __restrict__ dinv, TX* __restrict__ p) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k)) return;
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    const TX beta = (TX)SS(a, S_BETA, k);
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) p[i] = dinv[i] * r[i] + beta * p[i];
+}
+
+template <typename TV, typename TX, int LPR>
+__global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                                               const TV* __restrict__ val, const TX* __restrict__ p, TX* __restrict__ q) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k)) return;
+    __shared__ double sh[32];
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+    const int wgrp = grp - grp % (32 / LPR);  // warp-uniform loop (full-mask shuffles)
+    double loc = 0.0;
+    for (int base = r0 + wgrp; base < r1; base += BBS / LPR) {
+        const int row = base + (grp - wgrp);
+        const bool act = row < r1;
+        TX acc = TX(0);
+        if (act)
+            for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += LPR) acc += (TX)__ldg(val + j) * __ldg(p + __ldg(colind + j));
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+        if (act && lane == 0) {
+            q[row] = acc;
+            loc += (double)(p[row] * acc);
+        }
+    }
+    const double s1 = block_sum(loc, sh);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
+        const double tot = inst_sum(a, k, 0, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_ALPHA, k) = SS(a, S_ABSNEW, k) / tot;
+            a.t[T_SPMV * a.ninst + k] = 0;
+        }
+    }
+}
+
+// mixed = 1: convergence or a 10x drop of the iterated residual requests a
+// reliable update instead of finishing
+template <typename TX>
+__global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX* __restrict__ r, const TX* __restrict__ p,
+                                                 const TX* __restrict__ q, const TX* __restrict__ dinv, int mixed) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k)) return;
+    __shared__ double sh[32];
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    const TX alpha = (TX)SS(a, S_ALPHA, k);
+    TX rr = TX(0), rz = TX(0);
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+        x[i] += alpha * p[i];
+        const TX ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        rr += ri * ri;
+        rz += ri * (dinv[i] * ri);
+    }
+    const double s1 = block_sum((double)rr, sh), s2 = block_sum((double)rz, sh);
+    if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[gridDim.x + blockIdx.x] = s2; }
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {
+        const double trr = inst_sum(a, k, 0, sh), trz = inst_sum(a, k, 1, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_RR, k) = trr;
+            const int it = ++II(a, I_ITERS, k);
+            SS(a, S_ABSOLD, k) = SS(a, S_ABSNEW, k);
+            SS(a, S_BETA, k) = trz / SS(a, S_ABSNEW, k);
+            SS(a, S_ABSNEW, k) = trz;
+            if (!(trr == trr) || !(trz == trz)) { II(a, I_BAD, k) = 1; finish(a, k, 3); }
+            else if (!mixed) {
+                if (trr < SS(a, S_THRESH, k)) finish(a, k, 1);
+                else if (it >= a.max_iter) finish(a, k, 2);
+            } else if (trr < SS(a, S_THRESH, k) || trr < 1e-2 * SS(a, S_RRLAST, k) || it >= a.max_iter) {
+                II(a, I_UPDATE, k) = 1;
+            }
+            a.t[T_UPD * a.ninst + k] = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BBS) kb_fold(BArgs a, float* __restrict__ x32, double* __restrict__ x64) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+        x64[i] += (double)x32[i];
+        x32[i] = 0.0f;
+    }
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(BBS) kb_residual(BArgs a, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                                                   const double* __restrict__ val, const double* __restrict__ x,
+                                                   const double* __restrict__ b, double* __restrict__ r) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
+    __shared__ double sh[32];
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+    const int wgrp = grp - grp % (32 / LPR);
+    double loc = 0.0;
+    for (int base = r0 + wgrp; base < r1; base += BBS / LPR) {
+        const int row = base + (grp - wgrp);
+        const bool act = row < r1;
+        double acc = 0.0;
+        if (act)
+            for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += LPR) acc += __ldg(val + j) * __ldg(x + __ldg(colind + j));
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+        if (act && lane == 0) {
+            const double ri = b[row] - acc;
+            r[row] = ri;
+            loc += ri * ri;
+        }
+    }
+    const double s1 = block_sum(loc, sh);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_RES * a.ninst + k], cnt)) {
+        const double tot = inst_sum(a, k, 0, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_RRLAST, k) = tot;
+            SS(a, S_RR, k) = tot;
+            if (!(tot == tot)) { II(a, I_BAD, k) = 1; finish(a, k, 3); }
+            else if (tot <= a.tol * a.tol * SS(a, S_RHS2, k)) finish(a, k, 1);
+            else if (II(a, I_ITERS, k) >= a.max_iter) finish(a, k, 2);
+            a.t[T_RES * a.ninst + k] = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BBS) kb_restart(BArgs a, const double* __restrict__ r64, float* __restrict__ r32,
+                                                  const float* __restrict__ dinv) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
+    __shared__ double sh[32];
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    double rz = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+        const float ri = (float)r64[i];
+        r32[i] = ri;
+        rz += (double)ri * (double)(dinv[i] * ri);
+    }
+    const double s1 = block_sum(rz, sh);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
+        const double tot = inst_sum(a, k, 0, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_BETA, k) = tot / SS(a, S_ABSOLD, k);
+            SS(a, S_ABSNEW, k) = tot;
+            II(a, I_UPDATE, k) = 0;
+            a.t[T_SPMV * a.ninst + k] = 0;
+        }
+    }
+}
+
+template <typename TV, typename TX>
+__global__ void kb_dinv(int n, const int* __restrict__ diag, const TV* __restrict__ val, TX* __restrict__ dinv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const TV d = val[diag[i]];
+        dinv[i] = (d != TV(0)) ? TX(1) / (TX)d : TX(1);
+    }
+}
+
+__global__ void kb_copy(int n, const double* __restrict__ a, double* __restrict__ b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+template <typename TV, typename TX>
+void launch_kb_spmv(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, const int* rp, const int* ci, const TV* v,
+                    const TX* p, TX* q) {
+    switch (lpr) {
+        case 2: kb_spmv<TV, TX, 2><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+        case 4: kb_spmv<TV, TX, 4><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+        case 8: kb_spmv<TV, TX, 8><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+        case 16: kb_spmv<TV, TX, 16><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+        default: kb_spmv<TV, TX, 32><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+    }
+}
+
+void launch_kb_residual(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, const int* rp, const int* ci, const double* v,
+                        const double* x, const double* b, double* r) {
+    switch (lpr) {
+        case 2: kb_residual<2><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
+        case 4: kb_residual<4><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
+        case 8: kb_residual<8><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
+        case 16: kb_residual<16><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
+        default: kb_residual<32><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
+    }
+}
+
+int pick_lpr(isl_ctx* c) {
+    const double avg = (double)c->nnz / (double)c->neq;
+    int l = 2;
+    while (l < 32 && l < avg / 2) l *= 2;
+    return l;
+}
+
+// block -> (instance, row range) map and per-instance state buffers
+int ensure_batch_state(isl_ctx* c) {
+    if (c->nbblocks > 0 && (int64_t)c->inst_iters.size() == c->ninst) return ISL_OK;
+    std::vector<int32_t> bi, b0, b1, ib(c->ninst + 1, 0);
+    for (int64_t k = 0; k < c->ninst; ++k) {
+        const int64_t r0 = c->inst_eq_off[k], r1 = c->inst_eq_off[k + 1];
+        ib[k] = (int32_t)bi.size();
+        if (r1 <= r0) {  // an instance with no active DOF still owns one (empty) block
+            bi.push_back((int32_t)k); b0.push_back((int32_t)r0); b1.push_back((int32_t)r0);
+            continue;
+        }
+        for (int64_t r = r0; r < r1; r += ROWS_PER_BLOCK) {
+            bi.push_back((int32_t)k);
+            b0.push_back((int32_t)r);
+            b1.push_back((int32_t)std::min<int64_t>(r + ROWS_PER_BLOCK, r1));
+        }
+    }
+    ib[c->ninst] = (int32_t)bi.size();
+    c->nbblocks = (int64_t)bi.size();
+    ISL_CHECK_CUDA(c, c->dblk_inst.alloc(bi.size()));
+    ISL_CHECK_CUDA(c, c->dblk_row0.alloc(bi.size()));
+    ISL_CHECK_CUDA(c, c->dblk_row1.alloc(bi.size()));
+    ISL_CHECK_CUDA(c, c->dinst_blk.alloc(ib.size()));
+    ISL_CHECK_CUDA(c, c->dbs.alloc((size_t)S_NS * c->ninst));
+    ISL_CHECK_CUDA(c, c->dbi.alloc((size_t)I_NI * c->ninst + 1));
+    ISL_CHECK_CUDA(c, c->dbt.alloc((size_t)T_NT * c->ninst));
+    ISL_CHECK_CUDA(c, c->dbpart.alloc((size_t)2 * bi.size()));
+    cudaStream_t st = c->stream;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_inst.p, bi.data(), bi.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row0.p, b0.data(), b0.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row1.p, b1.data(), b1.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dinst_blk.p, ib.data(), ib.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    c->inst_iters.assign(c->ninst, 0);
+    c->inst_relres.assign(c->ninst, 0.0);
+    return ISL_OK;
+}
+
+}  // namespace
+
+int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
+    int rc = ensure_batch_state(c);
+    if (rc != ISL_OK) return rc;
+    const size_t n = (size_t)c->neq;
+    if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
+    if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
+    cudaStream_t st = c->stream;
+    const unsigned grid = (unsigned)c->nbblocks;
+    const int ni = (int)c->ninst;
+    BArgs a;
+    a.ninst = ni;
+    a.blk_inst = c->dblk_inst.p;
+    a.blk_r0 = c->dblk_row0.p;
+    a.blk_r1 = c->dblk_row1.p;
+    a.inst_blk = c->dinst_blk.p;
+    a.s = c->dbs.p;
+    a.iv = c->dbi.p;
+    a.t = c->dbt.p;
+    a.remaining = c->dbi.p + (size_t)I_NI * ni;
+    a.part = c->dbpart.p;
+    a.max_iter = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    a.tol = tol;
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbs.p, 0, (size_t)S_NS * ni * 8, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbi.p, 0, ((size_t)I_NI * ni + 1) * 4, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbt.p, 0, (size_t)T_NT * ni * 4, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(a.remaining, &ni, 4, cudaMemcpyHostToDevice, st));
+    const int lpr = pick_lpr(c);
+    const unsigned vg = (unsigned)c->sm_count * 8;
+    const bool mixed = (method == ISL_SOLVE_CG_FP32_IR);
+    if (mixed && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "batched mixed solve needs the FP64 matrix (ISL_PREC_MIXED)");
+    double* W = c->w64.p;
+    float* V = c->w32.p;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    if (!mixed) {
+        double *x = W, *r = W + n, *p = W + 2 * n, *q = W + 3 * n, *dinv = W + 4 * n;
+        kb_dinv<double, double><<<vg, BBS, 0, st>>>((int)n, c->ddiag.p, c->dval64.p, dinv);
+        kb_init<double, double><<<grid, BBS, 0, st>>>(a, c->drhs.p, x, r, p, dinv);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+        ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < BCHUNK; ++k) {
+            kb_dir<double><<<grid, BBS, 0, st>>>(a, r, dinv, p);
+            launch_kb_spmv<double, double>(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, p, q);
+            kb_update<double><<<grid, BBS, 0, st>>>(a, x, r, p, q, dinv, 0);
+        }
+        ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
+    } else {
+        double *x64 = W, *r64 = W + n;
+        float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n;
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
+        kb_dinv<float, float><<<vg, BBS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
+        kb_init<double, float><<<grid, BBS, 0, st>>>(a, c->drhs.p, x32, r32, p32, d32);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+        ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < BCHUNK; ++k) {
+            kb_dir<float><<<grid, BBS, 0, st>>>(a, r32, d32, p32);
+            launch_kb_spmv<float, float>(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval32.p, p32, q32);
+            kb_update<float><<<grid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
+            kb_fold<<<grid, BBS, 0, st>>>(a, x32, x64);
+            launch_kb_residual(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64);
+            kb_restart<<<grid, BBS, 0, st>>>(a, r64, r32, d32);
+        }
+        ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
+    }
+    c->launches += 2;
+    {
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ISL_CHECK_CUDA(c, e);
+    }
+    const int per_iter = mixed ? 6 : 3;
+    const int64_t max_replays = (int64_t)a.max_iter / BCHUNK + 8;
+    int remaining = ni;
+    int64_t replays = 0;
+    rc = ISL_OK;
+    for (;;) {
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(&remaining, a.remaining, 4, cudaMemcpyDeviceToHost, st));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+        if (remaining <= 0) break;
+        if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "batched CG made no progress"; break; }
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
+        c->launches += (int64_t)per_iter * BCHUNK;
+    }
+    cudaGraphExecDestroy(exec);
+    if (rc != ISL_OK) return rc;
+    kb_copy<<<vg, BBS, 0, st>>>((int)n, W, c->dsol.p);  // x (plain) or x64 (mixed) both live at W
+    c->launches += 1;
+    std::vector<int> hi((size_t)I_NI * ni);
+    std::vector<double> hs((size_t)S_NS * ni);
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(hi.data(), c->dbi.p, hi.size() * 4, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(hs.data(), c->dbs.p, hs.size() * 8, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    int64_t itmax = 0;
+    double relmax = 0.0;
+    bool nc = false, bad = false;
+    for (int k = 0; k < ni; ++k) {
+        const int done = hi[(size_t)I_DONE * ni + k];
+        c->inst_iters[k] = hi[(size_t)I_ITERS * ni + k];
+        const double rhs2 = hs[(size_t)S_RHS2 * ni + k];
+        c->inst_relres[k] = rhs2 > 0 ? std::sqrt(hs[(size_t)S_RR * ni + k] / rhs2) : 0.0;
+        itmax = std::max<int64_t>(itmax, c->inst_iters[k]);
+        relmax = std::max(relmax, c->inst_relres[k]);
+        nc |= (done == 2);
+        bad |= (done == 3) || hi[(size_t)I_BAD * ni + k];
+    }
+    if (iters) *iters = itmax;
+    if (relres) *relres = relmax;
+    c->solved = true;
+    if (bad) ISL_FAIL(c, ISL_ERR_NAN, "batched CG breakdown in an instance");
+    if (nc) ISL_FAIL(c, ISL_ERR_NOT_CONVERGED, "an instance did not reach the tolerance");
+    return ISL_OK;
+}
+
+}  // namespace isl

@@ -374,7 +374,22 @@ int isl_ctx_destroy(isl_ctx* c) {
 
 const char* isl_last_error(const isl_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem,
+                            const int64_t* conn, int64_t n_inst, const int64_t* node_off, const int64_t* elem_off);
+
 int isl_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn) {
+    const int64_t no[2] = {0, n_nodes}, eo[2] = {0, n_elem};
+    return mesh_upload_impl(c, shape, dim, n_nodes, X, n_elem, conn, 1, no, eo);
+}
+
+int isl_batch_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_inst, const int64_t* node_off, const double* X,
+                          const int64_t* elem_off, const int64_t* conn) {
+    if (!c || n_inst <= 0 || !node_off || !elem_off) return ISL_ERR_ARG;
+    return mesh_upload_impl(c, shape, dim, node_off[n_inst], X, elem_off[n_inst], conn, n_inst, node_off, elem_off);
+}
+
+static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem,
+                            const int64_t* conn, int64_t n_inst, const int64_t* node_off, const int64_t* elem_off) {
     if (!c) return ISL_ERR_ARG;
     if (!(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) ISL_FAIL(c, ISL_ERR_ARG, "unsupported shape");
     if (dim != sdim(shape)) ISL_FAIL(c, ISL_ERR_ARG, "dim does not match shape");
@@ -384,8 +399,16 @@ int isl_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_nodes, const doubl
     c->ngeom = num_vertices(shape);
     c->hX.assign(X, X + n_nodes * dim);
     c->hconn.assign(conn, conn + n_elem * c->ngeom);
-    for (int64_t i = 0; i < n_elem * c->ngeom; ++i)
-        if (conn[i] < 0 || conn[i] >= n_nodes) ISL_FAIL(c, ISL_ERR_ARG, "connectivity out of range");
+    if (node_off[0] != 0 || elem_off[0] != 0) ISL_FAIL(c, ISL_ERR_ARG, "instance offsets must start at 0");
+    for (int64_t k = 0; k < n_inst; ++k) {
+        if (node_off[k + 1] <= node_off[k] || elem_off[k + 1] <= elem_off[k]) ISL_FAIL(c, ISL_ERR_ARG, "empty instance");
+        for (int64_t i = elem_off[k] * c->ngeom; i < elem_off[k + 1] * c->ngeom; ++i)
+            if (conn[i] < node_off[k] || conn[i] >= node_off[k + 1])
+                ISL_FAIL(c, ISL_ERR_ARG, "connectivity out of range (elements must use their own instance's nodes)");
+    }
+    c->ninst = n_inst;
+    c->inst_node_off.assign(node_off, node_off + n_inst + 1);
+    c->inst_elem_off.assign(elem_off, elem_off + n_inst + 1);
     c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false;
     if (c->device < 0) return ISL_OK;
     cudaSetDevice(c->device);
@@ -417,40 +440,50 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->nup = c->nloc * (c->nloc + 1) / 2;
     const int64_t E = c->nelem;
     c->hedof.assign((size_t)E * nf, -1);
+    c->inst_dof_off.assign(c->ninst + 1, 0);
     if (fe_degree == 1) {
         int64_t mx = 0;
         for (int64_t i = 0; i < E * nf; ++i) { c->hedof[i] = c->hconn[i]; mx = std::max(mx, c->hconn[i] + 1); }
         c->ndofobj = mx;
+        c->inst_dof_off = c->inst_node_off;
+        c->inst_dof_off[c->ninst] = mx;
     } else {
+        // numbered per instance (each instance exactly as the reference numbers
+        // a single mesh), instances concatenated
         int64_t counter = 0;
-        int begin = 0;
-        for (int n = 0; n <= D; ++n) {
-            const auto tab = nfaces(c->shape, n);
-            const int stride = interior_dofs(c->shape, fe_degree, n);
-            const int nfc = (int)tab.size();
-            if (nfc == 0) continue;
-            if (n < D) {
-                std::vector<Key> keys((size_t)E * nfc);
-                for (int64_t e = 0; e < E; ++e)
-                    for (int f = 0; f < nfc; ++f) keys[e * nfc + f] = face_key(&c->hconn[e * c->ngeom], tab[f]);
-                std::vector<int64_t> first, order;
-                group_faces(keys, first, order);
-                for (int64_t s = 0; s < E * nfc; ++s) {
-                    const int64_t e = s / nfc, f = s % nfc;
-                    const int64_t s0 = first[s];
-                    const int64_t e0 = s0 / nfc, f0 = s0 % nfc;
-                    for (int d = 0; d < stride; ++d) {
-                        int64_t& dst = c->hedof[e * nf + begin + f * stride + d];
-                        dst = (s0 == s) ? counter++ : c->hedof[e0 * nf + begin + f0 * stride + d];
+        for (int64_t k = 0; k < c->ninst; ++k) {
+            c->inst_dof_off[k] = counter;
+            const int64_t e_lo = c->inst_elem_off[k], e_hi = c->inst_elem_off[k + 1], Ek = e_hi - e_lo;
+            int begin = 0;
+            for (int n = 0; n <= D; ++n) {
+                const auto tab = nfaces(c->shape, n);
+                const int stride = interior_dofs(c->shape, fe_degree, n);
+                const int nfc = (int)tab.size();
+                if (nfc == 0) continue;
+                if (n < D) {
+                    std::vector<Key> keys((size_t)Ek * nfc);
+                    for (int64_t e = 0; e < Ek; ++e)
+                        for (int f = 0; f < nfc; ++f) keys[e * nfc + f] = face_key(&c->hconn[(e_lo + e) * c->ngeom], tab[f]);
+                    std::vector<int64_t> first, order;
+                    group_faces(keys, first, order);
+                    for (int64_t s = 0; s < Ek * nfc; ++s) {
+                        const int64_t e = e_lo + s / nfc, f = s % nfc;
+                        const int64_t s0 = first[s];
+                        const int64_t e0 = e_lo + s0 / nfc, f0 = s0 % nfc;
+                        for (int d = 0; d < stride; ++d) {
+                            int64_t& dst = c->hedof[e * nf + begin + f * stride + d];
+                            dst = (s0 == s) ? counter++ : c->hedof[e0 * nf + begin + f0 * stride + d];
+                        }
                     }
+                } else {
+                    for (int64_t e = e_lo; e < e_hi; ++e)
+                        for (int d = 0; d < nfc * stride; ++d) c->hedof[e * nf + begin + d] = counter++;
                 }
-            } else {
-                for (int64_t e = 0; e < E; ++e)
-                    for (int d = 0; d < nfc * stride; ++d) c->hedof[e * nf + begin + d] = counter++;
+                begin += nfc * stride;
             }
-            begin += nfc * stride;
         }
         c->ndofobj = counter;
+        c->inst_dof_off[c->ninst] = counter;
     }
     const size_t ndc = (size_t)c->ndofobj * ncomp;
     c->status.assign(ndc, 0);
@@ -460,6 +493,14 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->numbered = false;
     c->u_nonzero = false;
     c->nnz = 0;
+    c->pattern_ready = false;
+    c->have64 = c->have32 = c->solved = false;
+    // buffers sized by the previous field (a context reused for a new problem)
+    c->dcval.release(); c->deq.release(); c->dstatus.release();
+    c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
+    c->nbblocks = 0;
+    c->inst_iters.clear(); c->inst_relres.clear();
+    c->blocked = false;
     if (n_dofobj) *n_dofobj = c->ndofobj;
     if (n_fun) *n_fun = nf;
     if (c->device < 0) return ISL_OK;
@@ -611,12 +652,20 @@ int isl_scale_constraints(isl_ctx* c, double factor) {
 int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     int64_t k = 0;
-    for (size_t i = 0; i < c->status.size(); ++i) c->heq[i] = c->status[i] == 0 ? (int32_t)k++ : -1;
+    c->inst_eq_off.assign(c->ninst + 1, 0);
+    int64_t inst = 0;
+    for (size_t i = 0; i < c->status.size(); ++i) {
+        while (inst < c->ninst && (int64_t)i >= c->inst_dof_off[inst + 1] * c->ncomp) c->inst_eq_off[++inst] = k;
+        c->heq[i] = c->status[i] == 0 ? (int32_t)k++ : -1;
+    }
+    while (inst < c->ninst) c->inst_eq_off[++inst] = k;
     if (k >= INT32_MAX) ISL_FAIL(c, ISL_ERR_ARG, "too many DOFs for 32-bit indices");
     c->neq = k;
     c->numbered = true;
     if (n_active) *n_active = k;
     c->nnz = 0;
+    c->pattern_ready = false;
+    c->nbblocks = 0;
     if (c->device < 0) return ISL_OK;
     const size_t ndc = c->status.size();
     ISL_CHECK_CUDA(c, c->deq.alloc(ndc));
@@ -640,8 +689,16 @@ int isl_dof_index(isl_ctx* c, int64_t* out) {
 int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
     if (!c || !c->numbered) return ISL_ERR_ARG;
     if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: the pattern is built on the device");
-    if (c->neq == 0) ISL_FAIL(c, ISL_ERR_ARG, "no active DOFs");
     cudaSetDevice(c->device);
+    c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
+    c->nbblocks = 0;
+    if (c->neq == 0) {  // every DOF constrained: an empty system, as the reference's Eigen3(0)
+        c->nnz = 0;
+        c->pattern_ready = true;
+        c->blocked = false;
+        if (nnz) *nnz = 0;
+        return ISL_OK;
+    }
     // elements with a constrained local DOF (Dirichlet lift candidates)
     std::vector<int32_t> lift;
     for (int64_t e = 0; e < c->nelem; ++e) {
@@ -657,6 +714,7 @@ int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
         ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dlift_elem.p, lift.data(), lift.size() * 4, cudaMemcpyHostToDevice, c->stream));
     int st = isl::pattern_build(c);
     if (st != ISL_OK) return st;
+    c->pattern_ready = true;
     if (nnz) *nnz = c->nnz;
     return ISL_OK;
 }
@@ -747,14 +805,28 @@ int isl_get_values(isl_ctx* c, double* u) {
 }
 
 int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) {
-    if (!c || !c->nnz || c->kernel < 0) ISL_FAIL(c, ISL_ERR_ARG, "assemble: pattern or kernel not set");
+    if (!c) return ISL_ERR_ARG;
+    if (!c->pattern_ready || c->kernel < 0) ISL_FAIL(c, ISL_ERR_ARG, "assemble: pattern or kernel not set");
     if (precision < ISL_PREC_FP64 || precision > ISL_PREC_MIXED) ISL_FAIL(c, ISL_ERR_ARG, "precision");
+    if (c->neq == 0) {
+        c->have64 = precision != ISL_PREC_FP32;
+        c->have32 = precision != ISL_PREC_FP64;
+        c->solved = false;
+        return ISL_OK;
+    }
     cudaSetDevice(c->device);
     return isl::assemble_device(c, precision, incremental, with_residual);
 }
 
 int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res) {
-    if (!c || !c->nnz) ISL_FAIL(c, ISL_ERR_ARG, "solve: nothing assembled");
+    if (!c) return ISL_ERR_ARG;
+    if (!c->pattern_ready || !(c->have64 || c->have32)) ISL_FAIL(c, ISL_ERR_ARG, "solve: nothing assembled");
+    if (c->neq == 0) {
+        c->solved = true;
+        if (iters) *iters = 0;
+        if (rel_res) *rel_res = 0.0;
+        return ISL_OK;
+    }
     if (method == ISL_SOLVE_CG_FP64 && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "solve: no FP64 matrix assembled");
     if (method == ISL_SOLVE_CG_FP32_IR && !c->have32)
         ISL_FAIL(c, ISL_ERR_ARG, "solve: the FP32 solve needs an FP32 matrix (ISL_PREC_MIXED or ISL_PREC_FP32)");
@@ -764,7 +836,9 @@ int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* ite
 }
 
 int isl_get_solution(isl_ctx* c, double* x) {
-    if (!c || !c->nnz || !x) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready) return ISL_ERR_ARG;
+    if (c->neq == 0) return ISL_OK;
+    if (!x) return ISL_ERR_ARG;
     const double* src = c->solved ? c->dsol.p : c->drhs.p;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(x, src, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -772,14 +846,17 @@ int isl_get_solution(isl_ctx* c, double* x) {
 }
 
 int isl_get_rhs(isl_ctx* c, double* b) {
-    if (!c || !c->nnz || !b) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready) return ISL_ERR_ARG;
+    if (c->neq == 0) return ISL_OK;
+    if (!b) return ISL_ERR_ARG;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(b, c->drhs.p, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
 }
 
 int isl_norm(isl_ctx* c, double* out) {
-    if (!c || !c->nnz || !out) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready || !out) return ISL_ERR_ARG;
+    if (c->neq == 0) { *out = 0.0; return ISL_OK; }
     std::vector<double> b(c->neq);
     int st = isl_get_solution(c, b.data());
     if (st) return st;
@@ -790,7 +867,8 @@ int isl_norm(isl_ctx* c, double* out) {
 }
 
 int isl_distribute(isl_ctx* c, int add) {
-    if (!c || !c->solved) ISL_FAIL(c, ISL_ERR_ARG, "distribute: no solution");
+    if (!c) return ISL_ERR_ARG;
+    if (!c->solved) ISL_FAIL(c, ISL_ERR_ARG, "distribute: no solution");
     cudaSetDevice(c->device);
     int st = isl::distribute_device(c, add);
     if (st == ISL_OK) c->u_nonzero = true;
@@ -798,7 +876,11 @@ int isl_distribute(isl_ctx* c, int add) {
 }
 
 int isl_get_csr(isl_ctx* c, int64_t* rowptr, int64_t* colind, double* values) {
-    if (!c || !c->nnz) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready) return ISL_ERR_ARG;
+    if (c->neq == 0) {
+        if (rowptr) rowptr[0] = 0;
+        return ISL_OK;
+    }
     if (rowptr) {
         std::vector<int32_t> t(c->neq + 1);
         ISL_CHECK_CUDA(c, cudaMemcpy(t.data(), c->drowptr.p, t.size() * 4, cudaMemcpyDeviceToHost));
@@ -846,7 +928,7 @@ int isl_timings(isl_ctx* c, double* ms, int64_t* counts) {
 }
 
 int isl_time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
-    if (!c || !c->nnz || !ms || nrep <= 0) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep <= 0) return ISL_ERR_ARG;
     return isl::time_spmv(c, precision, nrep, ms);
 }
 
@@ -895,6 +977,29 @@ int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {
     if (e != cudaSuccess) return ISL_ERR_CUDA;
     *free_bytes = (int64_t)f;
     *total_bytes = (int64_t)t;
+    return ISL_OK;
+}
+
+int isl_batch_info(isl_ctx* c, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off) {
+    if (!c || !n_inst) return ISL_ERR_ARG;
+    *n_inst = c->ninst;
+    if (eq_off) {
+        if (!c->numbered) ISL_FAIL(c, ISL_ERR_ARG, "batch info: DOFs not numbered");
+        std::copy(c->inst_eq_off.begin(), c->inst_eq_off.end(), eq_off);
+    }
+    if (dofobj_off) {
+        if (!c->fedeg) ISL_FAIL(c, ISL_ERR_ARG, "batch info: no field");
+        std::copy(c->inst_dof_off.begin(), c->inst_dof_off.end(), dofobj_off);
+    }
+    return ISL_OK;
+}
+
+int isl_batch_solve_stats(isl_ctx* c, int64_t* iters, double* rel_res) {
+    if (!c || c->inst_iters.empty()) return ISL_ERR_ARG;
+    for (int64_t k = 0; k < c->ninst; ++k) {
+        if (iters) iters[k] = c->inst_iters[k];
+        if (rel_res) rel_res[k] = c->inst_relres[k];
+    }
     return ISL_OK;
 }
 

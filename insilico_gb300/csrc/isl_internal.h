@@ -94,6 +94,7 @@ struct CGWork {
 // scalar block shared by the CG kernels (device)
 struct CGScal {
     double absNew, absOld, pAp, alpha, beta, rr, rz, threshold, rhsNorm2;
+    double rrtrig;  // mixed CG: stop for a reliable update when rr falls below (0 = never)
     int done;
     int iters;
     int bad;
@@ -109,6 +110,12 @@ struct isl_ctx {
     bool own_stream = false;
     std::string err;
     int sm_count = 0;
+
+    // instances: a context holds one mesh or a batch of independent meshes
+    // (disjoint node/element ranges); DOF objects and equations are numbered
+    // per instance and concatenated
+    int64_t ninst = 1;
+    std::vector<int64_t> inst_node_off, inst_elem_off, inst_dof_off, inst_eq_off;
 
     // mesh
     int shape = 0, dim = 0, ngeom = 0;
@@ -149,6 +156,7 @@ struct isl_ctx {
     isl::DBuf<int32_t> dlift_elem;
 
     // pattern
+    bool pattern_ready = false;  // true after isl_register_pattern (also for an empty system)
     int64_t nnz = 0, ncontrib = 0, ncontribF = 0;
     isl::DBuf<int32_t> drowptr, dcolind, ddiag, dseg, dsrc, dsegF, dsrcF;
     // staged element matrices/vectors (SoA)
@@ -173,6 +181,16 @@ struct isl_ctx {
     isl::DBuf<float> dbinv;      // SoA [9][nbr] inverse diagonal blocks
     int64_t asm_serial = 0, bsr_serial = -1;
     int bspmv_lpb = 0;
+
+    // batched CG (ninst > 1): row ranges of thread blocks and per-instance state
+    isl::DBuf<int32_t> dinst_row, dblk_inst, dblk_row0, dblk_row1, dinst_blk;
+    isl::DBuf<double> dbs;        // per-instance scalars [16][ninst]
+    isl::DBuf<int32_t> dbi;       // per-instance ints   [8][ninst]
+    isl::DBuf<unsigned int> dbt;  // per-instance tickets [4][ninst]
+    isl::DBuf<double> dbpart;     // per-block partials [2][nblocks]
+    int64_t nbblocks = 0;
+    std::vector<int64_t> inst_iters;
+    std::vector<double> inst_relres;
 
     // status word written by kernels (bit 0: det J <= 0, bit 1: NaN)
     isl::DBuf<int> dflags;
@@ -218,4 +236,5 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
 int distribute_device(isl_ctx* c, int add);
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
 int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
+int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 }  // namespace isl

@@ -26,55 +26,26 @@
 #include <vector>
 
 #include "isl_internal.h"
+#include "isl_device.cuh"
 
 namespace isl {
 
 constexpr int BS = 256;
 constexpr int CHUNK = 32;
+// reliable update when the iterated residual has dropped 10x (squared: 1e-2)
+constexpr double kDelta2 = 1e-2;
 
-template <typename T>
-__device__ inline T ld(const T* p) { return __ldg(p); }
-
-// fixed-order block reduction of a double (deterministic); result in thread 0
-__device__ inline double block_sum(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) sh[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (w == 0) {
-        t = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    }
-    return t;
-}
-
-// true in every thread of the last block to finish
-__device__ inline bool last_block(unsigned int* ticket) {
-    __shared__ bool amLast;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned t = atomicAdd(ticket, 1u);
-        amLast = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    return amLast;
-}
-
-__device__ inline double reduce_parts(const double* part, int n, int stride, int off, double* sh) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(part + (size_t)i * stride + off);
-    return block_sum(s, sh);
-}
-
+// Row dot product by a group of LPR lanes.  Every lane of the warp must call it
+// the same number of times (the shuffles use the full-warp mask); lanes of a
+// group without a row pass active = false and contribute zero.
 template <typename TV, typename TX, int LPR>
-__device__ inline TX row_dot(int row, const int* __restrict__ rowptr, const int* __restrict__ colind,
+__device__ inline TX row_dot(int row, bool active, const int* __restrict__ rowptr, const int* __restrict__ colind,
                              const TV* __restrict__ val, const TX* __restrict__ p, int lane) {
     TX acc = TX(0);
-    const int lo = rowptr[row], hi = rowptr[row + 1];
-    for (int k = lo + lane; k < hi; k += LPR) acc += (TX)ld(val + k) * ld(p + ld(colind + k));
+    if (active) {
+        const int lo = rowptr[row], hi = rowptr[row + 1];
+        for (int k = lo + lane; k < hi; k += LPR) acc += (TX)ld(val + k) * ld(p + ld(colind + k));
+    }
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
     return acc;
@@ -89,10 +60,13 @@ __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ 
     __shared__ double sh[32];
     const int lane = threadIdx.x % LPR;
     const int grp = (blockIdx.x * BS + threadIdx.x) / LPR, ngrp = gridDim.x * BS / LPR;
+    const int wgrp = grp - grp % (32 / LPR);  // first group of this warp: the loop is warp-uniform
     double loc = 0.0;
-    for (int row = grp; row < n; row += ngrp) {
-        const TX acc = row_dot<TV, TX, LPR>(row, rowptr, colind, val, p, lane);
-        if (lane == 0) {
+    for (int base = wgrp; base < n; base += ngrp) {
+        const int row = base + (grp - wgrp);
+        const bool act = row < n;
+        const TX acc = row_dot<TV, TX, LPR>(row, act, rowptr, colind, val, p, lane);
+        if (act && lane == 0) {
             q[row] = acc;
             loc += (double)(p[row] * acc);
         }
@@ -139,6 +113,7 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
             S->absNew = trz;
             if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
             else if (trr < S->threshold) S->done = 1;
+            else if (trr < S->rrtrig) S->done = 3;
             else if (S->iters >= max_iter) S->done = 2;
             S->ticket2 = 0;
         }
@@ -157,7 +132,7 @@ __global__ void __launch_bounds__(BS) k_cg_dir(int n, const TX* __restrict__ r, 
 template <typename TB, typename TX>
 __global__ void __launch_bounds__(BS) k_cg_init(int n, const TB* __restrict__ b, TX* __restrict__ x, TX* __restrict__ r,
                                                 TX* __restrict__ p, const TX* __restrict__ dinv, CGScal* S, double* part,
-                                                double tol) {
+                                                double tol, double trig) {
     __shared__ double sh[32];
     double bb = 0.0, bz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
@@ -178,6 +153,7 @@ __global__ void __launch_bounds__(BS) k_cg_init(int n, const TB* __restrict__ b,
         if (threadIdx.x == 0) {
             S->rhsNorm2 = tbb;
             S->threshold = tol * tol * tbb;
+            S->rrtrig = trig * tbb;
             S->absNew = tbz;
             S->absOld = tbz;
             S->beta = 0.0;
@@ -216,10 +192,13 @@ __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict_
     __shared__ double sh[32];
     const int lane = threadIdx.x % LPR;
     const int grp = (blockIdx.x * BS + threadIdx.x) / LPR, ngrp = gridDim.x * BS / LPR;
+    const int wgrp = grp - grp % (32 / LPR);
     double loc = 0.0;
-    for (int row = grp; row < n; row += ngrp) {
-        const double ax = row_dot<double, double, LPR>(row, rowptr, colind, val, x, lane);
-        if (lane == 0) {
+    for (int base = wgrp; base < n; base += ngrp) {
+        const int row = base + (grp - wgrp);
+        const bool act = row < n;
+        const double ax = row_dot<double, double, LPR>(row, act, rowptr, colind, val, x, lane);
+        if (act && lane == 0) {
             const double ri = b[row] - ax;
             r[row] = ri;
             loc += ri * ri;
@@ -235,7 +214,7 @@ __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict_
 
 // reliable update, part 2: r32 = r64; beta = (r.z)_new / (r.z)_previous; resume
 __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restrict__ r64, float* __restrict__ r32,
-                                                  const float* __restrict__ dinv, CGScal* S, double* part) {
+                                                  const float* __restrict__ dinv, CGScal* S, double* part, double rrtrig) {
     __shared__ double sh[32];
     double rr = 0.0, rz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
@@ -254,6 +233,7 @@ __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restric
             S->rr = trr;
             S->beta = trz / S->absOld;
             S->absNew = trz;
+            S->rrtrig = rrtrig;
             S->done = 0;
             S->ticket2 = 0;
         }
@@ -366,7 +346,7 @@ static int solve_fp64(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, 
     const unsigned grid = vec_grid(c);
     k_dinv<double, double><<<grid, BS, 0, st>>>((int)n, c->ddiag.p, c->dval64.p, dinv);
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, sizeof(CGScal), st));
-    k_cg_init<double, double><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x, r, p, dinv, c->dscal.p, c->dpart.p, tol);
+    k_cg_init<double, double><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x, r, p, dinv, c->dscal.p, c->dpart.p, tol, 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 2;
     cudaGraphExec_t exec;
@@ -417,7 +397,8 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_dinv<float, float><<<grid, BS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
-    k_cg_init<double, float><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x32, r32, p32, d32, S, c->dpart.p, tol);
+    k_cg_init<double, float><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x32, r32, p32, d32, S, c->dpart.p, tol,
+                                                   c->have64 ? kDelta2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 2;
     cudaGraphExec_t exec;
@@ -425,9 +406,8 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     if (rc != ISL_OK) return rc;
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
-    double rr_last = bnorm2, rr_true = bnorm2;
-    const double delta2 = 1e-2;  // reliable update when the iterated residual dropped 10x
-    const int64_t max_replays = (int64_t)mi / CHUNK + 64;
+    double rr_true = bnorm2;
+    const int64_t max_replays = (int64_t)mi + 64;
     int64_t replays = 0;
     bool converged = (bnorm2 == 0.0);
     while (rc == ISL_OK && !converged) {
@@ -450,7 +430,7 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
             }
             continue;
         }
-        if (h.done || h.rr < delta2 * rr_last || at_max) {
+        if (h.done || at_max) {
             // reliable update: true residual in FP64
             k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
             launch_residual(c->spmv_lpr64, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64,
@@ -461,9 +441,8 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p);
+            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p, kDelta2 * rr_true);
             c->launches += 1;
-            rr_last = rr_true;
         }
     }
     cudaGraphExecDestroy(exec);
@@ -565,10 +544,13 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, const int* __restrict
     __shared__ double sh[32];
     const int lane = threadIdx.x % LPB;
     const int grp = (blockIdx.x * BS + threadIdx.x) / LPB, ngrp = gridDim.x * BS / LPB;
+    const int wgrp = grp - grp % (32 / LPB);  // warp-uniform loop (full-mask shuffles below)
     double loc = 0.0;
-    for (int i = grp; i < nbr; i += ngrp) {
+    for (int base = wgrp; base < nbr; base += ngrp) {
+        const int i = base + (grp - wgrp);
+        const bool act = i < nbr;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        const int lo = bptr[i], hi = bptr[i + 1];
+        const int lo = act ? bptr[i] : 0, hi = act ? bptr[i + 1] : 0;
         for (int k = lo + lane; k < hi; k += LPB) {
             const int j = __ldg(bcol + k);
             const float x0 = __ldg(p + 3 * j), x1 = __ldg(p + 3 * j + 1), x2 = __ldg(p + 3 * j + 2);
@@ -582,7 +564,7 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, const int* __restrict
             a1 += __shfl_xor_sync(0xffffffffu, a1, o, LPB);
             a2 += __shfl_xor_sync(0xffffffffu, a2, o, LPB);
         }
-        if (lane == 0) {
+        if (act && lane == 0) {
             q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
             loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
         }
@@ -639,6 +621,7 @@ __global__ void __launch_bounds__(BS) k_cg_update_b3(int nbr, float* __restrict_
             S->absNew = trz;
             if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
             else if (trr < S->threshold) S->done = 1;
+            else if (trr < S->rrtrig) S->done = 3;
             else if (S->iters >= max_iter) S->done = 2;
             S->ticket2 = 0;
         }
@@ -662,7 +645,7 @@ __global__ void __launch_bounds__(BS) k_cg_dir_b3(int nbr, const float* __restri
 // beta = (r.z)_new / (r.z)_previous (reliable update)
 __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
                                                    float* __restrict__ p, const float* __restrict__ binv, CGScal* S, double* part,
-                                                   double tol, int restart) {
+                                                   double tol, int restart, double trig) {
     __shared__ double sh[32];
     double bb = 0.0, bz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
@@ -688,6 +671,7 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
             if (!restart) {
                 S->rhsNorm2 = tbb;
                 S->threshold = tol * tol * tbb;
+                S->rrtrig = trig * tbb;
                 S->absNew = tbz;
                 S->absOld = tbz;
                 S->beta = 0.0;
@@ -700,6 +684,7 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
                 S->rr = tbb;
                 S->beta = tbz / S->absOld;
                 S->absNew = tbz;
+                S->rrtrig = trig;
                 S->done = 0;
             }
             S->ticket2 = 0;
@@ -808,7 +793,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     unsigned* ticket = &(c->dscal.p + 1)->ticket1;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
-    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0);
+    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0, kDelta2);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     cudaGraph_t graph;
@@ -827,9 +812,8 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     }
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
-    double rr_last = bnorm2, rr_true = bnorm2;
-    const double delta2 = 1e-2;
-    const int64_t max_replays = (int64_t)mi / CHUNK + 64;
+    double rr_true = bnorm2;
+    const int64_t max_replays = (int64_t)mi + 64;
     int64_t replays = 0;
     bool converged = (bnorm2 == 0.0);
     while (rc == ISL_OK && !converged) {
@@ -841,7 +825,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
         const CGScal h = *c->hscal;
         if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
         const bool at_max = h.iters >= mi;
-        if (h.done || h.rr < delta2 * rr_last || at_max) {
+        if (h.done || at_max) {
             k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
             launch_residual(c->spmv_lpr64, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64,
                             c->dpart.p, ticket, dres);
@@ -851,9 +835,8 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 1);
+            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 1, kDelta2 * rr_true);
             c->launches += 1;
-            rr_last = rr_true;
         }
     }
     cudaGraphExecDestroy(exec);
@@ -899,7 +882,11 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
     int64_t it = 0;
     double rel = 0.0;
     bool nc = false;
-    if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
+    if (c->ninst > 1) {
+        rc = solve_batched(c, method, tol, max_iter, &it, &rel);
+        nc = (rc == ISL_ERR_NOT_CONVERGED);
+        if (rc == ISL_ERR_NOT_CONVERGED) rc = ISL_OK;
+    } else if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
     else if (c->blocked && c->use_block && c->have64) rc = solve_mixed_b3(c, tol, max_iter, &it, &rel, &nc);
     else rc = solve_mixed(c, tol, max_iter, &it, &rel, &nc);
     if (rc != ISL_OK) return rc;

@@ -231,3 +231,35 @@ class System:
         v = C.c_int64()
         self._chk(self.L.isl_get_option(self.h, key, C.byref(v)), "isl_get_option")
         return v.value
+
+    # -- batches of independent meshes -----------------------------------------
+    def upload_batch(self, shape: int, meshes):
+        """meshes: list of (X [n_i, dim], conn [E_i, nv] with local node ids)."""
+        node_off = np.zeros(len(meshes) + 1, dtype=np.int64)
+        elem_off = np.zeros(len(meshes) + 1, dtype=np.int64)
+        for k, (X, conn) in enumerate(meshes):
+            node_off[k + 1] = node_off[k] + len(X)
+            elem_off[k + 1] = elem_off[k] + len(conn)
+        self.X = np.ascontiguousarray(np.concatenate([m[0] for m in meshes]), dtype=np.float64)
+        self.conn = np.ascontiguousarray(np.concatenate([m[1] + node_off[k] for k, m in enumerate(meshes)]), dtype=np.int64)
+        self.shape, self.dim = shape, self.X.shape[1]
+        self.nnodes, self.nelem = len(self.X), len(self.conn)
+        self.node_off, self.elem_off = node_off, elem_off
+        self._chk(self.L.isl_batch_mesh_upload(self.h, shape, self.dim, len(meshes), A.i64(node_off), A.d(self.X),
+                                               A.i64(elem_off), A.i64(self.conn)), "isl_batch_mesh_upload")
+
+    def batch_info(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_batch_info(self.h, C.byref(n), None, None))
+        eq = np.zeros(n.value + 1, dtype=np.int64)
+        do = np.zeros(n.value + 1, dtype=np.int64)
+        self._chk(self.L.isl_batch_info(self.h, C.byref(n), A.i64(eq) if self.neq else None, A.i64(do)))
+        return eq, do
+
+    def batch_stats(self):
+        n = C.c_int64()
+        self._chk(self.L.isl_batch_info(self.h, C.byref(n), None, None))
+        it = np.zeros(n.value, dtype=np.int64)
+        rr = np.zeros(n.value)
+        self._chk(self.L.isl_batch_solve_stats(self.h, A.i64(it), A.d(rr)))
+        return it, rr

@@ -77,3 +77,21 @@ def oracle_newton(req, rtol=1e-10, max_newton=30, lin_tol=1e-12):
             xs, _, _ = O.cg(rp, ci, v, b, tol=lin_tol)
             P.distribute(xs, add=True)
     return P.values()
+
+
+def csr_entry_err(rowptr, colind, a, b):
+    """Max |a_ij - b_ij| / max(|b_ij|, sqrt(|b_ii b_jj|)) over the CSR pattern.
+
+    The diagonal geometric mean bounds |K_ij| of an SPD matrix, so entries that
+    are small only through cancellation of element contributions are measured
+    against the scale of their row and column instead of their own size."""
+    rowptr = np.asarray(rowptr)
+    colind = np.asarray(colind)
+    n = len(rowptr) - 1
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    diag = np.zeros(n)
+    on = rows == colind
+    diag[rows[on]] = np.abs(b[on])
+    scale = np.maximum(np.abs(b), np.sqrt(diag[rows] * diag[colind]))
+    scale = np.maximum(scale, 1e-300)
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / scale))

@@ -1,0 +1,61 @@
+"""Batched instances on the GPU: several independent 2-D heat problems of
+different sizes in one context.  Each instance's DOF numbering and CSR block
+must be bit-identical to solving it alone (the reference numbering of that
+mesh), its matrix entries within 1e-12 of the oracle, and its CG solution
+(own scalars and convergence) within 1e-8 of the oracle's solution."""
+import numpy as np
+import pytest
+
+import oracle as O
+from insilico_gb300 import _abi as A
+from insilico_gb300 import workloads as W
+from insilico_gb300.system import System
+
+from helpers import csr_entry_err, oracle_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def instance(side, deg, seed):
+    X, conn = W.unit_cube("quad", side, side)
+    g = W.rng(seed, 0)
+    kappa = np.exp(g.normal(0.0, 0.5, len(conn)))
+    f = W.rng(seed, 1).uniform(0.0, 1.0, len(X))[:, None]
+    return W.Problem("inst", A.QUAD, X, conn, deg, 1, "laplace", 2 * deg, kappa=kappa, body=f,
+                     dirichlet=lambda x: (np.ones((len(x), 1), dtype=bool), 0.0), tol=1e-10)
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_batch_matches_single_instances(deg):
+    probs = [instance(s, deg, 100 + s) for s in (3, 9, 5, 16, 2)]
+    S = System()
+    S.upload_batch(A.QUAD, [(p.X, p.conn) for p in probs])
+    S.create_field(deg, 1)
+    S.constrain_boundary(lambda x: (np.ones((len(x), 1), dtype=bool), 0.0))
+    S.number_dofs()
+    S.register_pattern()
+    S.set_laplace(np.concatenate([p.kappa for p in probs]), 2 * deg)
+    S.set_body_force_nodal(np.concatenate([p.body for p in probs]))
+    eq_off, _ = S.batch_info()
+    S.assemble(A.PREC_MIXED)
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    S.solve(A.SOLVE_CG_FP64, tol=1e-12)
+    x64 = S.solution()
+    it64, _ = S.batch_stats()
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xm = S.solution()
+    for k, p in enumerate(probs):
+        P, (orp, oci, ov, ob) = oracle_problem(p)
+        r0, r1 = eq_off[k], eq_off[k + 1]
+        assert r1 - r0 == P.neq
+        lrp = rp[r0:r1 + 1] - rp[r0]
+        np.testing.assert_array_equal(lrp, orp)
+        np.testing.assert_array_equal(ci[rp[r0]:rp[r1]] - r0, oci)
+        assert csr_entry_err(orp, oci, v[rp[r0]:rp[r1]], ov) <= 1e-12
+        assert np.max(np.abs(b[r0:r1] - ob)) <= 1e-12 * np.max(np.abs(ob))
+        xo, ito, _ = O.cg(orp, oci, ov, ob, tol=1e-13)
+        assert np.linalg.norm(x64[r0:r1] - xo) <= 1e-9 * np.linalg.norm(xo)
+        assert np.linalg.norm(xm[r0:r1] - xo) <= 1e-8 * np.linalg.norm(xo)
+        assert abs(it64[k] - O.cg(orp, oci, ov, ob, tol=1e-12)[1]) <= 2
+    S.close()
