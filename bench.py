@@ -104,6 +104,10 @@ def spmv_bytes(nnz, n, v):
     return nnz * (v + 4) + 4 * (n + 1) + 2 * n * v
 
 
+def log(*a):
+    print("[bench]", *a, file=sys.stderr, flush=True)
+
+
 def calibrate(S, method, x_ref, tols):
     """Loosest tolerance whose solution is within ERR_BAR of the FP64 reference."""
     from insilico_gb300 import _abi as A
@@ -111,6 +115,7 @@ def calibrate(S, method, x_ref, tols):
         it, rr, _ = S.solve(method, tol=tol)
         x = S.solution()
         err = float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))
+        log(f"calibrate method={method} tol={tol:g} iters={it} err={err:.3e}")
         if err <= ERR_BAR:
             return tol, err, it
     return tols[-1], err, it
@@ -192,6 +197,9 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: setup + the mixed steps only (no calibration, plain arm, e2e or CPU legs)")
+    ap.add_argument("--tol", type=float, default=1e-10)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -214,6 +222,14 @@ def main():
     from insilico_gb300.system import System
     S = W.setup_system(p, System(device=local))
     neq, nnz = S.neq, S.nnz
+    log(f"setup neq={neq} nnz={nnz} blocked={S.get_option(A.OPT_BLOCKED)}")
+    if args.profile:
+        for k in range(args.warmup + args.steps):
+            S.assemble(A.PREC_MIXED)
+            it, rr, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=args.tol)
+            log(f"profile step {k}: iters {it} relres {rr:.2e}")
+        S.close()
+        return
     # FP64 reference solution (tight tolerance) and the plain path's calibration
     S.assemble(A.PREC_MIXED)
     S.solve(A.SOLVE_CG_FP64, tol=1e-13)
@@ -255,6 +271,7 @@ def main():
         ms_total = float(t.item())
     ms_step = ms_total / args.steps
     value = neq * world / (ms_step / 1e3)
+    log(f"timed: {ms_step:.2f} ms/step, inner iters {its}, err {err_m:.3e}")
 
     # phase split of one mixed step and the plain FP64 path
     S.set_timing(True)
@@ -275,10 +292,22 @@ def main():
     asm64_ms = ms64[A.T_ELEMENT] + ms64[A.T_GATHER]
 
     # dominant kernel: FP32 SpMV of the inner CG, timed alone (CUDA events)
+    S.assemble(A.PREC_MIXED)
     spmv32_ms = S.time_spmv(A.PREC_FP32, 50)
     spmv64_ms = S.time_spmv(A.PREC_FP64, 50)
+    kernels = S.time_kernels(30)
+    log("kernel ms:", {k: round(v, 4) for k, v in kernels.items()})
     hbm, src = peaks()
-    b32 = spmv_bytes(nnz, neq, 4)
+    blocked = S.get_option(A.OPT_BLOCKED)
+    if blocked:
+        # 3x3 blocks: 36 B of values + 4 B of column id per block, x and y once
+        nblk, nslot = S.get_option(A.OPT_NBLOCKS), S.get_option(A.OPT_NSLOTS)
+        b32 = nblk * 40 + 2 * neq * 4 + 8 * ((neq // 3 + 31) // 32)
+        kname = "k_bspmv_pap (sliced-ELL 3x3 FP32 blocks, inner CG SpMV)"
+    else:
+        nblk = nslot = 0
+        b32 = spmv_bytes(nnz, neq, 4)
+        kname = "k_spmv_pap<float> (FP32 CSR, inner CG SpMV)"
     ach = b32 / (spmv32_ms * 1e-3) / 1e9
     traffic = ncu_traffic()
 
@@ -319,11 +348,12 @@ def main():
                        "solve_ms": ms64[A.T_SOLVE], "iters": it_plain, "solve_tol": tol64, "rel_err_vs_fp64": err64},
         "speedup_vs_plain_fp64": plain_ms / ms_step,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                     "traffic": traffic, "kernel": "k_spmv_pap<float> (inner FP32 CG SpMV)",
+                     "traffic": traffic, "kernel": kname, "blocks": nblk, "slots": nslot,
                      "bytes_per_launch": b32, "ms_per_launch": spmv32_ms, "peak_source": src,
                      "fp64_spmv": {"ms_per_launch": spmv64_ms,
                                    "achieved": spmv_bytes(nnz, neq, 8) / (spmv64_ms * 1e-3) / 1e9}},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": int(launches),
+        "kernel_ms": kernels,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -180,9 +180,11 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
 /* Solver options.  ISL_OPT_BLOCK_SOLVER (default 1): the mixed solve uses a
  * 3x3 node-block copy of the FP32 matrix with block-Jacobi preconditioning
  * when every DOF object's three components are all active or all
- * constrained; 0 keeps the scalar CSR + Jacobi path.  ISL_OPT_BLOCKED (read
- * only through isl_get_option) tells whether the pattern is node-blocked. */
-enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1 };
+ * constrained; 0 keeps the scalar CSR + Jacobi path.  Read-only through
+ * isl_get_option: ISL_OPT_BLOCKED (the pattern is node-blocked),
+ * ISL_OPT_NBLOCKS (stored 3x3 blocks), ISL_OPT_NSLOTS (block slots of the
+ * sliced-ELL copy, padding included). */
+enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 
@@ -199,6 +201,13 @@ int isl_launch_count(isl_ctx* ctx, int64_t* n);
 /* Average device time (ms) of one launch of the solver's SpMV kernel on the
  * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches. */
 int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
+
+/* Warm per-kernel device time (ms per launch, CUDA events over nrep launches)
+ * of the solver's kernels on the current system: ms[0] FP32 block SpMV,
+ * ms[1] block-Jacobi update, ms[2] block-Jacobi direction, ms[3] FP64 CSR
+ * SpMV, ms[4] FP64 update, ms[5] FP64 direction, ms[6] FP64 residual, ms[7]
+ * the autotuned block SpMV variant (-1 entries: not applicable). */
+int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
 
 #ifdef __cplusplus
 }

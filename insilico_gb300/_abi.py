@@ -36,9 +36,9 @@ EXPORTED = [
     "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
     "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
-    "isl_batch_solve_stats",
+    "isl_batch_solve_stats", "isl_time_kernels",
 ]
-OPT_BLOCK_SOLVER, OPT_BLOCKED = 0, 1
+OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS = 0, 1, 2, 3
 
 
 class IslError(RuntimeError):
@@ -110,6 +110,7 @@ def load(build_if_missing: bool = False):
     L.isl_batch_mesh_upload.argtypes = [_P, i, i, C.c_int64, _I64, _D, _I64, _I64]
     L.isl_batch_info.argtypes = [_P, _I64, _I64, _I64]
     L.isl_batch_solve_stats.argtypes = [_P, _I64, _D]
+    L.isl_time_kernels.argtypes = [_P, i, _D]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "isl_last_error":

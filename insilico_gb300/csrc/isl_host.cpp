@@ -963,6 +963,8 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (!c || !value) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
+    if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }
+    if (key == ISL_OPT_NSLOTS) { *value = c->blocked ? c->nslot : 0; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
 }
 
@@ -1001,6 +1003,12 @@ int isl_batch_solve_stats(isl_ctx* c, int64_t* iters, double* rel_res) {
         if (rel_res) rel_res[k] = c->inst_relres[k];
     }
     return ISL_OK;
+}
+
+int isl_time_kernels(isl_ctx* c, int nrep, double* ms) {
+    if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep <= 0) return ISL_ERR_ARG;
+    cudaSetDevice(c->device);
+    return isl::time_kernels(c, nrep, ms);
 }
 
 }  // extern "C"

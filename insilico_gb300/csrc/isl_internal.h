@@ -177,7 +177,14 @@ struct isl_ctx {
     bool use_block = true;
     int64_t nbr = 0, nblk = 0;
     isl::DBuf<int32_t> dbptr, dbcol, dbrow;
-    isl::DBuf<float> dbval;      // SoA [9][nblk]
+    // sliced-ELL copy of the blocks for the SpMV: block rows in slices of 32,
+    // each slice padded to its longest row, stored column-major (slot =
+    // slice_off + k*32 + lane) so a warp reads every block position coalesced
+    int64_t nslice = 0, nslot = 0;
+    isl::DBuf<int32_t> dsoff, dswid, dscol, dsdst;
+    isl::DBuf<float> dsval;      // [slot/32][9][32]: the 9 values of a group of 32 slots contiguous
+    isl::DBuf<float> dbval;      // block-row CSR copy: SoA [9][nblk]
+    int bspmv_kind = 0;          // autotuned: 1..3 sliced-ELL (unroll 1,2,4), 4/8/16 block-row CSR lanes per row
     isl::DBuf<float> dbinv;      // SoA [9][nbr] inverse diagonal blocks
     int64_t asm_serial = 0, bsr_serial = -1;
     int bspmv_lpb = 0;
@@ -235,6 +242,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
 int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int distribute_device(isl_ctx* c, int add);
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
+int time_kernels(isl_ctx* c, int nrep, double* ms);
 int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 }  // namespace isl

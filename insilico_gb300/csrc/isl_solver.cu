@@ -92,7 +92,27 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
     __shared__ double sh[32];
     const TX alpha = (TX)S->alpha;
     TX rr = TX(0), rz = TX(0);
-    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+    const int stride = gridDim.x * BS;
+    int i = blockIdx.x * BS + threadIdx.x;
+    // four entries per pass, loads issued together: the grid is small (see
+    // upd_grid), so each thread keeps several loads in flight
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        TX pv[4], qv[4], rv[4], dv[4], xv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            pv[k] = ld(p + i + k * stride); qv[k] = ld(q + i + k * stride); dv[k] = ld(dinv + i + k * stride);
+            rv[k] = r[i + k * stride]; xv[k] = x[i + k * stride];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[i + k * stride] = xv[k] + alpha * pv[k];
+            const TX ri = rv[k] - alpha * qv[k];
+            r[i + k * stride] = ri;
+            rr += ri * ri;
+            rz += ri * (dv[k] * ri);
+        }
+    }
+    for (; i < n; i += stride) {
         x[i] += alpha * p[i];
         const TX ri = r[i] - alpha * q[i];
         r[i] = ri;
@@ -103,8 +123,8 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
     const double b2 = block_sum((double)rz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
-        const double trr = reduce_parts(part, gridDim.x, 2, 0, sh);
-        const double trz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        double trr, trz;
+        reduce_parts2(part, gridDim.x, sh, trr, trz);
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->iters += 1;
@@ -148,8 +168,8 @@ __global__ void __launch_bounds__(BS) k_cg_init(int n, const TB* __restrict__ b,
     const double b2 = block_sum(bz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
-        const double tbb = reduce_parts(part, gridDim.x, 2, 0, sh);
-        const double tbz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        double tbb, tbz;
+        reduce_parts2(part, gridDim.x, sh, tbb, tbz);
         if (threadIdx.x == 0) {
             S->rhsNorm2 = tbb;
             S->threshold = tol * tol * tbb;
@@ -227,8 +247,8 @@ __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restric
     const double b2 = block_sum(rz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
-        const double trr = reduce_parts(part, gridDim.x, 2, 0, sh);
-        const double trz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        double trr, trz;
+        reduce_parts2(part, gridDim.x, sh, trr, trz);
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->beta = trz / S->absOld;
@@ -246,6 +266,11 @@ __global__ void k_copy64(int n, const double* __restrict__ a, double* __restrict
 
 // ---------------------------------------------------------------------------
 static unsigned vec_grid(isl_ctx* c) { return (unsigned)c->sm_count * (2048 / BS); }
+// grid of the CG update kernels: two blocks per SM keep the reduction tail
+// (one partial per block, last-block ticket) short
+static unsigned upd_grid(const isl_ctx* c, long long n) {
+    return (unsigned)std::max<long long>(1, std::min<long long>((n + BS - 1) / BS, 2LL * c->sm_count));
+}
 
 template <typename TV, typename TX>
 static void launch_spmv(int lpr, unsigned grid, cudaStream_t st, int n, const int* rp, const int* ci, const TV* v, const TX* p,
@@ -308,10 +333,12 @@ static int capture_chunk(isl_ctx* c, const TV* val, TX* x, TX* r, TX* p, TX* q, 
     double* part = c->dpart.p;
     cudaGraph_t graph;
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    // the direction update has no reduction: one thread per entry, full grid
+    const unsigned gdir = (unsigned)std::max<long long>(1, ((long long)n + BS - 1) / BS);
     for (int k = 0; k < CHUNK; ++k) {
-        k_cg_dir<TX><<<grid, BS, 0, st>>>(n, r, dinv, p, S);
+        k_cg_dir<TX><<<gdir, BS, 0, st>>>(n, r, dinv, p, S);
         launch_spmv<TV, TX>(lpr, grid, st, n, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
-        k_cg_update<TX><<<grid, BS, 0, st>>>(n, x, r, p, q, dinv, S, part, max_iter);
+        k_cg_update<TX><<<upd_grid(c, n), BS, 0, st>>>(n, x, r, p, q, dinv, S, part, max_iter);
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
@@ -330,7 +357,9 @@ static int ensure_work(isl_ctx* c) {
     const size_t n = (size_t)c->neq;
     if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
     if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
-    if (!c->dpart.p) ISL_CHECK_CUDA(c, c->dpart.alloc((size_t)2 * vec_grid(c) + 64));
+    // partial sums: two per block of every grid used (at most 16 blocks per SM)
+    const size_t maxgrid = (size_t)16 * c->sm_count;
+    if (c->dpart.n < 2 * maxgrid + 64) ISL_CHECK_CUDA(c, c->dpart.alloc(2 * maxgrid + 64));
     if (!c->dscal.p) ISL_CHECK_CUDA(c, c->dscal.alloc(2));
     return ISL_OK;
 }
@@ -490,14 +519,54 @@ __global__ void k_bsr_pattern(int nbr, const int* __restrict__ rowptr, const int
 }
 
 __global__ void k_bsr_values(int nblk, const int* __restrict__ brow, const int* __restrict__ bptr, const int* __restrict__ rowptr,
-                             const float* __restrict__ v32, float* __restrict__ bv) {
+                             const float* __restrict__ v32, const int* __restrict__ sdst, float* __restrict__ sv,
+                             float* __restrict__ bv) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblk; b += gridDim.x * blockDim.x) {
         const int i = brow[b], k = b - bptr[i];
+        const size_t slot = (size_t)sdst[b];
+        const size_t g = slot >> 5, l = slot & 31;
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
             const int o = rowptr[3 * i + r] + 3 * k;
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) bv[(size_t)(r * 3 + cc) * nblk + b] = v32[o + cc];
+            for (int cc = 0; cc < 3; ++cc) {
+                const float v = v32[o + cc];
+                sv[(g * 9 + r * 3 + cc) * 32 + l] = v;
+                bv[(size_t)(r * 3 + cc) * nblk + b] = v;
+            }
+        }
+    }
+}
+
+// slice widths (longest block row of each slice of 32)
+__global__ void k_sell_width(int nbr, int nslice, const int* __restrict__ bptr, int* __restrict__ swid) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslice; s += gridDim.x * blockDim.x) {
+        int w = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int i = s * 32 + l;
+            if (i < nbr) w = max(w, bptr[i + 1] - bptr[i]);
+        }
+        swid[s] = w;
+    }
+}
+
+// column ids of every slot (padding slots point at a valid column and keep
+// value 0) and the slot of every stored block
+__global__ void k_sell_fill(int nbr, int nslice, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                            const int* __restrict__ soff, const int* __restrict__ swid, int* __restrict__ scol,
+                            int* __restrict__ sdst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nslice * 32; i += gridDim.x * blockDim.x) {
+        const int s = i / 32, l = i % 32;
+        const int w = swid[s], o = soff[s];
+        const int len = (i < nbr) ? bptr[i + 1] - bptr[i] : 0;
+        for (int k = 0; k < w; ++k) {
+            const int slot = o + k * 32 + l;
+            if (k < len) {
+                scol[slot] = bcol[bptr[i] + k];
+                sdst[bptr[i] + k] = slot;
+            } else {
+                scol[slot] = (i < nbr) ? i : 0;
+            }
         }
     }
 }
@@ -531,15 +600,58 @@ __global__ void k_block_jacobi(int nbr, const int* __restrict__ rowptr, const in
                 for (int cc = 0; cc < 3; ++cc) Bi[r][cc] = (r == cc) ? 1.0 : 0.0;
         }
         for (int r = 0; r < 3; ++r)
-            for (int cc = 0; cc < 3; ++cc) binv[(size_t)(r * 3 + cc) * nbr + i] = (float)Bi[r][cc];
+            for (int cc = 0; cc < 3; ++cc) binv[(size_t)i * 9 + r * 3 + cc] = (float)Bi[r][cc];
     }
 }
 
-// q = A p (BSR, LPB lanes per block row); partial p.q; last block: alpha
+// q = A p on the sliced-ELL blocks, one warp per slice and one lane per block
+// row (no shuffles: every lane owns its three outputs); partial p.q; last
+// block: alpha
 template <int LPB>
-__global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
-                                                  const float* __restrict__ bv, int nblk, const float* __restrict__ p,
-                                                  float* __restrict__ q, CGScal* S, double* part) {
+__global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int* __restrict__ soff, const int* __restrict__ swid,
+                                                  const int* __restrict__ scol, const float* __restrict__ sv, long long nslot,
+                                                  const float* __restrict__ p, float* __restrict__ q, CGScal* S, double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
+    double loc = 0.0;
+    for (int s = warp; s < nslice; s += nwarps) {
+        const int i = s * 32 + lane;
+        const int o = soff[s], w = swid[s];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll LPB
+        for (int k = 0; k < w; ++k) {
+            const int slot = o + k * 32 + lane;
+            const int j = __ldg(scol + slot);
+            const float* v = sv + (size_t)(slot >> 5) * 288 + lane;  // group of 32 slots: [9][32]
+            const float x0 = __ldg(p + 3 * j), x1 = __ldg(p + 3 * j + 1), x2 = __ldg(p + 3 * j + 2);
+            a0 += __ldg(v) * x0 + __ldg(v + 32) * x1 + __ldg(v + 64) * x2;
+            a1 += __ldg(v + 96) * x0 + __ldg(v + 128) * x1 + __ldg(v + 160) * x2;
+            a2 += __ldg(v + 192) * x0 + __ldg(v + 224) * x1 + __ldg(v + 256) * x2;
+        }
+        if (i < nbr) {
+            q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
+            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+        }
+    }
+    const double bsum = block_sum(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    if (last_block(&S->ticket1)) {
+        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        if (threadIdx.x == 0) {
+            S->pAp = tot;
+            S->alpha = S->absNew / tot;
+            S->ticket1 = 0;
+        }
+    }
+}
+
+// q = A p on the block-row CSR copy: LPB lanes per block row
+template <int LPB>
+__global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                     const float* __restrict__ bv, int nblk, const float* __restrict__ p,
+                                                     float* __restrict__ q, CGScal* S, double* part) {
     if (S->done) return;
     __shared__ double sh[32];
     const int lane = threadIdx.x % LPB;
@@ -582,62 +694,89 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, const int* __restrict
 }
 
 __device__ inline void bj_apply(const float* __restrict__ binv, int nbr, int i, const float r[3], float z[3]) {
+    (void)nbr;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        z[a] = binv[(size_t)(a * 3) * nbr + i] * r[0] + binv[(size_t)(a * 3 + 1) * nbr + i] * r[1] +
-               binv[(size_t)(a * 3 + 2) * nbr + i] * r[2];
+        z[a] = binv[(size_t)i * 9 + a * 3] * r[0] + binv[(size_t)i * 9 + a * 3 + 1] * r[1] + binv[(size_t)i * 9 + a * 3 + 2] * r[2];
 }
 
-__global__ void __launch_bounds__(BS) k_cg_update_b3(int nbr, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
-                                                     const float* __restrict__ q, const float* __restrict__ binv, CGScal* S,
-                                                     double* part, int max_iter) {
+// Block-Jacobi vector kernels, one thread per DOF: a block of 192 threads
+// covers 64 whole nodes, so the three residual components of a node are
+// exchanged through shared memory and every global access is coalesced.
+constexpr int NBS = 192;
+
+// one thread per node: the node's three residual entries, search direction,
+// A p and its inverse diagonal block are all loaded at once (no shared-memory
+// exchange, no barrier in the data path).  Two blocks per SM stride over the
+// nodes: fewer blocks shorten the reduction tail (partials + last-block
+// ticket), which dominates a kernel that streams ~30 MB
+constexpr int NODE_BS = 256;
+static unsigned node_grid(const isl_ctx* c, long long nbr) {
+    return (unsigned)std::max<long long>(1, std::min<long long>((nbr + NODE_BS - 1) / NODE_BS, 2LL * c->sm_count));
+}
+__global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __restrict__ x, float* __restrict__ r,
+                                                           const float* __restrict__ p, const float* __restrict__ q,
+                                                           const float* __restrict__ binv, CGScal* S, double* part,
+                                                           int max_iter) {
     if (S->done) return;
     __shared__ double sh[32];
     const float alpha = (float)S->alpha;
     float rr = 0.f, rz = 0.f;
-    for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
-        float ri[3], zi[3];
+    for (int i = blockIdx.x * NODE_BS + threadIdx.x; i < nbr; i += gridDim.x * NODE_BS) {
+        const size_t d = 3 * (size_t)i;
+        float b[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) b[k] = ld(binv + 9 * (size_t)i + k);
+        float rv[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            x[3 * i + a] += alpha * p[3 * i + a];
-            ri[a] = r[3 * i + a] - alpha * q[3 * i + a];
-            r[3 * i + a] = ri[a];
+            x[d + a] += alpha * ld(p + d + a);
+            rv[a] = r[d + a] - alpha * ld(q + d + a);
         }
-        bj_apply(binv, nbr, i, ri, zi);
-        rr += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
-        rz += ri[0] * zi[0] + ri[1] * zi[1] + ri[2] * zi[2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            r[d + a] = rv[a];
+            const float z = b[3 * a] * rv[0] + b[3 * a + 1] * rv[1] + b[3 * a + 2] * rv[2];
+            rr += rv[a] * rv[a];
+            rz += rv[a] * z;
+        }
     }
     const double b1 = block_sum((double)rr, sh);
     const double b2 = block_sum((double)rz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
-    if (last_block(&S->ticket2)) {
-        const double trr = reduce_parts(part, gridDim.x, 2, 0, sh);
-        const double trz = reduce_parts(part, gridDim.x, 2, 1, sh);
-        if (threadIdx.x == 0) {
-            S->rr = trr;
-            S->iters += 1;
-            S->absOld = S->absNew;
-            S->beta = trz / S->absNew;
-            S->absNew = trz;
-            if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
-            else if (trr < S->threshold) S->done = 1;
-            else if (trr < S->rrtrig) S->done = 3;
-            else if (S->iters >= max_iter) S->done = 2;
-            S->ticket2 = 0;
-        }
+    if (!last_block(&S->ticket2)) return;
+    double trr, trz;
+    reduce_parts2(part, gridDim.x, sh, trr, trz);
+    if (threadIdx.x == 0) {
+        S->rr = trr;
+        S->iters += 1;
+        S->absOld = S->absNew;
+        S->beta = trz / S->absNew;
+        S->absNew = trz;
+        if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
+        else if (trr < S->threshold) S->done = 1;
+        else if (trr < S->rrtrig) S->done = 3;
+        else if (S->iters >= max_iter) S->done = 2;
+        S->ticket2 = 0;
     }
 }
 
-__global__ void __launch_bounds__(BS) k_cg_dir_b3(int nbr, const float* __restrict__ r, const float* __restrict__ binv,
-                                                  float* __restrict__ p, const CGScal* S) {
+__global__ void __launch_bounds__(NBS) k_cg_dir_b3(int nbr, const float* __restrict__ r, const float* __restrict__ binv,
+                                                   float* __restrict__ p, const CGScal* S) {
     if (S->done) return;
+    __shared__ float sr[NBS];
     const float beta = (float)S->beta;
-    for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
-        const float ri[3] = {r[3 * i], r[3 * i + 1], r[3 * i + 2]};
-        float zi[3];
-        bj_apply(binv, nbr, i, ri, zi);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) p[3 * i + a] = zi[a] + beta * p[3 * i + a];
+    const int n = 3 * nbr;
+    for (int base = blockIdx.x * NBS; base < n; base += gridDim.x * NBS) {
+        const int d = base + threadIdx.x;
+        sr[threadIdx.x] = (d < n) ? r[d] : 0.f;
+        __syncthreads();
+        if (d < n) {
+            const int a = threadIdx.x % 3, n0 = threadIdx.x - a, node = d / 3;
+            const float* B = binv + (size_t)node * 9 + a * 3;
+            p[d] = B[0] * sr[n0] + B[1] * sr[n0 + 1] + B[2] * sr[n0 + 2] + beta * p[d];
+        }
+        __syncthreads();
     }
 }
 
@@ -665,8 +804,8 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
     const double b2 = block_sum(bz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
-        const double tbb = reduce_parts(part, gridDim.x, 2, 0, sh);
-        const double tbz = reduce_parts(part, gridDim.x, 2, 1, sh);
+        double tbb, tbz;
+        reduce_parts2(part, gridDim.x, sh, tbb, tbz);
         if (threadIdx.x == 0) {
             if (!restart) {
                 S->rhsNorm2 = tbb;
@@ -692,27 +831,39 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
     }
 }
 
-static void launch_bspmv(int lpb, unsigned grid, cudaStream_t st, isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
-    const int nbr = (int)c->nbr, nblk = (int)c->nblk;
-    switch (lpb) {
-        case 4: k_bspmv_pap<4><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
-        case 8: k_bspmv_pap<8><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
-        case 16: k_bspmv_pap<16><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
-        default: k_bspmv_pap<32><<<grid, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nblk, p, q, S, part); break;
+static unsigned sell_grid(isl_ctx* c) {
+    const long long need = (c->nslice + (BS / 32) - 1) / (BS / 32);
+    return (unsigned)std::max<long long>(1, std::min<long long>(need, (long long)c->sm_count * (2048 / BS)));
+}
+
+// kind 1..3: sliced-ELL with slice-loop unroll 1, 2, 4; kind 4, 8, 16: block-row
+// CSR with that many lanes per block row
+static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
+    (void)grid;
+    const int nbr = (int)c->nbr, ns = (int)c->nslice, nb = (int)c->nblk;
+    const unsigned g = sell_grid(c), gv = vec_grid(c);
+    switch (kind) {
+        case 1: k_bspmv_pap<1><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
+        case 3: k_bspmv_pap<4><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
+        case 4: k_brow_spmv<4><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
+        case 8: k_brow_spmv<8><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
+        case 16: k_brow_spmv<16><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
+        default: k_bspmv_pap<2><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
     }
 }
 
+// autotune of the block SpMV (format and row mapping) on the current matrix
 static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
-    const int cand[4] = {4, 8, 16, 32};
-    if (c->nbr < 8000) return 8;
-    int best = 8;
+    const int cand[6] = {1, 2, 3, 4, 8, 16};
+    if (c->nbr < 8000) return 2;
+    int best = 2;
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
-    c->launches += 24;
-    for (int k = 0; k < 4; ++k) {
-        launch_bspmv(cand[k], vec_grid(c), c->stream, c, p, q, S, part);
+    c->launches += 36;
+    for (int k = 0; k < 6; ++k) {
+        launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
         cudaEventRecord(c->ev[2], c->stream);
-        for (int r = 0; r < 5; ++r) launch_bspmv(cand[k], vec_grid(c), c->stream, c, p, q, S, part);
+        for (int r = 0; r < 5; ++r) launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
         cudaEventRecord(c->ev[3], c->stream);
         cudaEventSynchronize(c->ev[3]);
         float ms = 0.f;
@@ -750,16 +901,41 @@ int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
     c->blocked = (bad == 0);
     c->bsr_serial = -1;
     c->bspmv_lpb = 0;
+    if (!c->blocked) return ISL_OK;
+    // sliced-ELL layout
+    c->nslice = (nbr + 31) / 32;
+    ISL_CHECK_CUDA(c, c->dswid.alloc(c->nslice));
+    ISL_CHECK_CUDA(c, c->dsoff.alloc(c->nslice + 1));
+    k_sell_width<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, (int)c->nslice, c->dbptr.p, c->dswid.p);
+    std::vector<int32_t> wid(c->nslice), off(c->nslice + 1, 0);
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(wid.data(), c->dswid.p, wid.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    int64_t tot = 0;
+    for (int64_t s2 = 0; s2 < c->nslice; ++s2) { off[s2] = (int32_t)tot; tot += (int64_t)wid[s2] * 32; }
+    if (tot >= INT32_MAX) { c->blocked = false; return ISL_OK; }
+    off[c->nslice] = (int32_t)tot;
+    c->nslot = tot;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dsoff.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, c->dscol.alloc(tot));
+    ISL_CHECK_CUDA(c, c->dsdst.alloc(c->nblk));
+    k_sell_fill<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, (int)c->nslice, c->dbptr.p, c->dbcol.p, c->dsoff.p, c->dswid.p,
+                                                   c->dscol.p, c->dsdst.p);
+    ISL_CHECK_CUDA(c, c->dsval.alloc((size_t)9 * tot));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dsval.p, 0, (size_t)9 * tot * 4, c->stream));
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->launches += 2;
     return ISL_OK;
 }
 
 // refresh the block values and the block-Jacobi inverses after an assembly
 static int ensure_bsr(isl_ctx* c) {
     if (c->bsr_serial == c->asm_serial) return ISL_OK;
-    ISL_CHECK_CUDA(c, c->dbval.alloc((size_t)9 * c->nblk));
     ISL_CHECK_CUDA(c, c->dbinv.alloc((size_t)9 * c->nbr));
+    ISL_CHECK_CUDA(c, c->dbval.alloc((size_t)9 * c->nblk));
     const unsigned grid = vec_grid(c);
-    k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p, c->dbval.p);
+    k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p, c->dsdst.p,
+                                             c->dsval.p, c->dbval.p);
     if (c->have64)
         k_block_jacobi<double><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval64.p, c->dbinv.p);
     else
@@ -796,13 +972,16 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0, kDelta2);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
+    // DOF-linear vector kernels: one wave of 192-thread blocks
     cudaGraph_t graph;
     cudaGraphExec_t exec;
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);  // one pass, no reduction
+    const unsigned nbn = node_grid(c, nbr);
     for (int k = 0; k < CHUNK; ++k) {
-        k_cg_dir_b3<<<grid, BS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
+        k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
         launch_bspmv(c->bspmv_lpb, grid, st, c, p32, q32, S, c->dpart.p);
-        k_cg_update_b3<<<grid, BS, 0, st>>>(nbr, x32, r32, p32, q32, c->dbinv.p, S, c->dpart.p, mi);
+        k_cg_update_b3n<<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, q32, c->dbinv.p, S, c->dpart.p, mi);
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     {
@@ -961,6 +1140,75 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     float t = 0.f;
     cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
     *ms = t / nrep;
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    return ISL_OK;
+}
+
+__global__ void k_fill(int64_t n, float* __restrict__ a, float v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+__global__ void k_fill64(int64_t n, double* __restrict__ a, double v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+// Warm per-kernel timing of one CG iteration's kernels (CUDA events around nrep
+// back-to-back launches each).  ms[0] block SpMV (autotuned kind), ms[1]
+// block-Jacobi update, ms[2] block-Jacobi direction, ms[3] FP64 CSR SpMV,
+// ms[4] FP64 update, ms[5] FP64 direction, ms[6] FP64 residual, ms[7] = the
+// chosen block SpMV kind (or -1 when the pattern is not node-blocked).
+int time_kernels(isl_ctx* c, int nrep, double* ms) {
+    int rc = ensure_work(c);
+    if (rc != ISL_OK) return rc;
+    cudaStream_t st = c->stream;
+    const size_t n = (size_t)c->neq;
+    const unsigned grid = vec_grid(c);
+    CGScal h;
+    memset(&h, 0, sizeof(h));
+    h.absNew = 1.0; h.absOld = 1.0; h.alpha = 1e-6; h.beta = 0.5; h.threshold = -1.0; h.rrtrig = -1.0;
+    auto reset = [&]() { return cudaMemcpyAsync(c->dscal.p, &h, sizeof(h), cudaMemcpyHostToDevice, st); };
+    auto timeit = [&](auto&& launch) -> double {
+        reset();
+        launch();
+        cudaEventRecord(c->ev[2], st);
+        for (int r = 0; r < nrep; ++r) launch();
+        cudaEventRecord(c->ev[3], st);
+        cudaEventSynchronize(c->ev[3]);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
+        return t / nrep;
+    };
+    const int mi = INT32_MAX - 1;
+    for (int k = 0; k < 8; ++k) ms[k] = -1.0;
+    if (c->blocked && c->have32) {
+        rc = ensure_bsr(c);
+        if (rc != ISL_OK) return rc;
+        float* V = c->w32.p;
+        float *x = V, *r = V + n, *p = V + 2 * n, *q = V + 3 * n;
+        k_fill<<<grid, BS, 0, st>>>((int64_t)(4 * n), V, 1.0f);
+        if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, p, q, c->dscal.p, c->dpart.p);
+        const int nbr = (int)c->nbr;
+        ms[0] = timeit([&] { launch_bspmv(c->bspmv_lpb, grid, st, c, p, q, c->dscal.p, c->dpart.p); });
+        const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);
+        const unsigned nbn = node_grid(c, nbr);
+        ms[1] = timeit([&] { k_cg_update_b3n<<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, q, c->dbinv.p, c->dscal.p, c->dpart.p, mi); });
+        ms[2] = timeit([&] { k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r, c->dbinv.p, p, c->dscal.p); });
+        ms[7] = c->bspmv_lpb;
+    }
+    if (c->have64) {
+        double* W = c->w64.p;
+        double *x = W, *r = W + n, *p = W + 2 * n, *q = W + 3 * n, *dinv = W + 4 * n, *r64 = W + 5 * n;
+        k_fill64<<<grid, BS, 0, st>>>((int64_t)(6 * n), W, 1.0);
+        if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, p, q, c->dscal.p, c->dpart.p);
+        const int lpr = c->spmv_lpr64;
+        double* dres = (double*)(c->dscal.p + 1);
+        unsigned* ticket = &(c->dscal.p + 1)->ticket1;
+        ms[3] = timeit([&] { launch_spmv<double, double>(lpr, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, p, q, c->dscal.p, c->dpart.p); });
+        ms[4] = timeit([&] { k_cg_update<double><<<upd_grid(c, n), BS, 0, st>>>((int)n, x, r, p, q, dinv, c->dscal.p, c->dpart.p, mi); });
+        const unsigned gdir = (unsigned)std::max<long long>(1, ((long long)n + BS - 1) / BS);
+        ms[5] = timeit([&] { k_cg_dir<double><<<gdir, BS, 0, st>>>((int)n, r, dinv, p, c->dscal.p); });
+        ms[6] = timeit([&] { launch_residual(lpr, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x, c->drhs.p, r64, c->dpart.p, ticket, dres); });
+    }
+    c->launches += 7 * (nrep + 1);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     return ISL_OK;
 }

@@ -263,3 +263,9 @@ class System:
         rr = np.zeros(n.value)
         self._chk(self.L.isl_batch_solve_stats(self.h, A.i64(it), A.d(rr)))
         return it, rr
+
+    def time_kernels(self, nrep: int = 20):
+        ms = np.zeros(8)
+        self._chk(self.L.isl_time_kernels(self.h, nrep, A.d(ms)), "isl_time_kernels")
+        keys = ["block_spmv32", "update_b3", "dir_b3", "spmv64", "update64", "dir64", "residual64", "block_kind"]
+        return dict(zip(keys, ms.tolist()))
