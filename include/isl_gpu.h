@@ -38,7 +38,8 @@ typedef enum {
     ISL_ERR_NOT_CONVERGED = 4,  /* solver hit max_iter before the tolerance */
     ISL_ERR_TIMEOUT = 5,        /* a bounded device wait expired */
     ISL_ERR_CUDA = 6,           /* CUDA runtime error */
-    ISL_ERR_NAN = 7             /* non-finite value in a reduction */
+    ISL_ERR_NAN = 7,            /* non-finite value in a reduction */
+    ISL_ERR_CAPACITY = 8        /* input larger than a fixed capacity (isl_cg_solve_noalloc) */
 } isl_status;
 
 /* element shapes (geometry degree 1, hierarchic vertex order of
@@ -208,6 +209,39 @@ int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
  * SpMV, ms[4] FP64 update, ms[5] FP64 direction, ms[6] FP64 residual, ms[7]
  * the autotuned block SpMV variant (-1 entries: not applicable). */
 int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
+
+/* Allocation-free FP64 CG.  This entry point has no counterpart in the
+ * reference; it serves callers that must not allocate device memory while
+ * they solve: an application that owns all device memory through its own
+ * pool or arena (a cudaMalloc there fails or fragments the pool), and
+ * time-stepping or control loops that solve every step, where cudaMalloc /
+ * cudaFree would synchronise the device and stall the loop.
+ *
+ * Same algorithm as isl_solve(ISL_SOLVE_CG_FP64): Jacobi-preconditioned CG,
+ * x0 = 0, stops when ||r|| <= tol ||b|| or after max_iter iterations
+ * (max_iter <= 0 means 2n).  Every pointer is a caller-owned device pointer on
+ * `device`: the n x n CSR matrix (rowptr[n+1], colind[nnz], val[nnz]), b[n]
+ * and the output x[n].  `stream` is a cudaStream_t (NULL: the default
+ * stream); the call returns once the solve has finished.  iters/rel_res may
+ * be NULL.
+ *
+ * The work vectors live in one scratch array compiled into the library's
+ * device code: ISL_NOALLOC_MAX_N entries for each of its four vectors plus
+ * the partial sums, about 2.1 MiB that every GPU loading the library holds
+ * until the process exits.  n > ISL_NOALLOC_MAX_N returns ISL_ERR_CAPACITY
+ * before any device work.  The call makes no cudaMalloc / cudaFree and no
+ * other allocating call.
+ *
+ * The first call on a device looks the scratch array up on that device
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls on a device share the one array, and
+ * it keeps the last call's contents: each call clears what has to start at
+ * zero, but calls that overlap on the GPU (other streams or host threads)
+ * race on it and must be serialised by the caller. */
+#define ISL_NOALLOC_MAX_N 65536
+int isl_cg_solve_noalloc(int device, void* stream, int n, const int32_t* rowptr, const int32_t* colind,
+                         const double* val, const double* b, double* x, double tol, int64_t max_iter,
+                         int64_t* iters, double* rel_res);
 
 #ifdef __cplusplus
 }

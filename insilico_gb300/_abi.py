@@ -10,7 +10,9 @@ import os
 
 from . import build as _build
 
-ISL_OK, ISL_ERR_ARG, ISL_ERR_NOMEM, ISL_ERR_DEGENERATE, ISL_ERR_NOT_CONVERGED, ISL_ERR_TIMEOUT, ISL_ERR_CUDA, ISL_ERR_NAN = range(8)
+(ISL_OK, ISL_ERR_ARG, ISL_ERR_NOMEM, ISL_ERR_DEGENERATE, ISL_ERR_NOT_CONVERGED, ISL_ERR_TIMEOUT, ISL_ERR_CUDA, ISL_ERR_NAN,
+ ISL_ERR_CAPACITY) = range(9)
+NOALLOC_MAX_N = 65536  # ISL_NOALLOC_MAX_N
 QUAD, TET, HEX = 3, 4, 5
 KERNEL_LAPLACE, KERNEL_HYPERELASTIC = 0, 1
 MAT_STVENANT, MAT_NEOHOOKE = 0, 1
@@ -26,6 +28,7 @@ _STATUS = {
     ISL_ERR_TIMEOUT: "timeout",
     ISL_ERR_CUDA: "CUDA error",
     ISL_ERR_NAN: "non-finite value",
+    ISL_ERR_CAPACITY: "larger than a fixed capacity",
 }
 
 EXPORTED = [
@@ -36,7 +39,7 @@ EXPORTED = [
     "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
     "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
-    "isl_batch_solve_stats", "isl_time_kernels",
+    "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc",
 ]
 OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS = 0, 1, 2, 3
 
@@ -111,6 +114,8 @@ def load(build_if_missing: bool = False):
     L.isl_batch_info.argtypes = [_P, _I64, _I64, _I64]
     L.isl_batch_solve_stats.argtypes = [_P, _I64, _D]
     L.isl_time_kernels.argtypes = [_P, i, _D]
+    # device pointers are passed as integers (c_void_p)
+    L.isl_cg_solve_noalloc.argtypes = [i, _P, i, _P, _P, _P, _P, _P, C.c_double, C.c_int64, _I64, _D]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "isl_last_error":

@@ -23,6 +23,7 @@
 // the iteration continues with the same search direction.  The solve ends
 // when the true FP64 residual meets the tolerance.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "isl_internal.h"
@@ -1214,3 +1215,137 @@ int time_kernels(isl_ctx* c, int nrep, double* ms) {
 }
 
 }  // namespace isl
+
+// ---------------------------------------------------------------------------
+// isl_cg_solve_noalloc: the FP64 Jacobi CG above (same init, direction, SpMV
+// and update kernels) on caller-owned device buffers, with its work vectors in
+// a fixed device array instead of memory allocated per call.
+//
+// Scratch layout (doubles): the CG scalars (256 bytes), two partial sums per
+// block of the largest grid, then r, p, q and the inverse diagonal, each
+// ISL_NOALLOC_MAX_N long.  The iterate is the caller's x.
+namespace {
+constexpr int NA_MAX_N = ISL_NOALLOC_MAX_N;
+constexpr int NA_MAX_BLOCKS = 4096;
+constexpr int NA_MAX_DEVICES = 64;
+constexpr size_t NA_PART_OFF = 32;
+constexpr size_t NA_VEC_OFF = NA_PART_OFF + 2 * (size_t)NA_MAX_BLOCKS;
+constexpr size_t NA_WORDS = NA_VEC_OFF + 4 * (size_t)NA_MAX_N;
+static_assert(sizeof(isl::CGScal) <= NA_PART_OFF * sizeof(double), "CG scalars exceed their scratch slot");
+static_assert(NA_VEC_OFF % 32 == 0, "vectors start on 256-byte boundaries");
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[NA_WORDS];
+
+namespace isl {
+namespace {
+
+// diagonal of a caller CSR row (first stored entry with col == row); rows
+// without a nonzero diagonal get 1, as the Jacobi preconditioner above does
+__global__ void k_noalloc_dinv(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                               const double* __restrict__ val, double* __restrict__ dinv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (colind[k] == i) { d = val[k]; break; }
+        dinv[i] = (d != 0.0) ? 1.0 / d : 1.0;
+    }
+}
+
+struct NoallocDevice {
+    double* base = nullptr;  // device address of g_noalloc_scratch on this device
+    int sms = 0;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[NA_MAX_DEVICES];
+
+// once per device, with that device current: the scratch array's address
+int noalloc_setup(int device, NoallocDevice* out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoallocDevice& e = g_noalloc_dev[device];
+    if (!e.base) {
+        double* ptr = nullptr;
+        if (cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return ISL_ERR_CUDA;
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
+            return ISL_ERR_CUDA;
+        e.sms = sms;
+        e.base = ptr;
+    }
+    *out = e;
+    return ISL_OK;
+}
+
+int noalloc_cg(const NoallocDevice& dv, cudaStream_t st, int n, const int* rowptr, const int* colind, const double* val,
+               const double* b, double* x, double tol, int64_t max_iter, int64_t* iters, double* rel_res) {
+    CGScal* S = reinterpret_cast<CGScal*>(dv.base);
+    double* part = dv.base + NA_PART_OFF;
+    double* r = dv.base + NA_VEC_OFF;
+    double *p = r + NA_MAX_N, *q = p + NA_MAX_N, *dinv = q + NA_MAX_N;
+    // SpMV variant by the mean row length (lanes per row)
+    int nnz = 0;
+    if (cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ISL_ERR_CUDA;
+    if (nnz < 0) return ISL_ERR_ARG;
+    const double avg = (double)nnz / n;
+    const int lpr = avg <= 6 ? 2 : avg <= 12 ? 4 : avg <= 24 ? 8 : avg <= 48 ? 16 : 32;
+    const int mi = (int)std::min<int64_t>(max_iter <= 0 ? 2 * (int64_t)n : max_iter, INT32_MAX - 1);
+    const unsigned gvec = (unsigned)std::min(8 * dv.sms, NA_MAX_BLOCKS);
+    const unsigned gupd = (unsigned)std::max(1, std::min((n + BS - 1) / BS, 2 * dv.sms));
+    const unsigned gdir = (unsigned)((n + BS - 1) / BS);
+    // the scalars hold the reduction tickets, the counters and the done flag:
+    // they must start at zero; every vector is written before it is read
+    if (cudaMemsetAsync(S, 0, sizeof(CGScal), st) != cudaSuccess) return ISL_ERR_CUDA;
+    k_noalloc_dinv<<<gdir, BS, 0, st>>>(n, rowptr, colind, val, dinv);
+    k_cg_init<double, double><<<gvec, BS, 0, st>>>(n, b, x, r, p, dinv, S, part, tol, 0.0);
+    if (cudaGetLastError() != cudaSuccess) return ISL_ERR_CUDA;
+    CGScal h;
+    const int64_t max_rounds = (int64_t)mi / CHUNK + 3;
+    for (int64_t round = 0;; ++round) {
+        if (cudaMemcpyAsync(&h, S, sizeof(CGScal), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return ISL_ERR_CUDA;
+        if (h.done) break;
+        if (round > max_rounds) return ISL_ERR_TIMEOUT;
+        for (int k = 0; k < CHUNK; ++k) {
+            k_cg_dir<double><<<gdir, BS, 0, st>>>(n, r, dinv, p, S);
+            launch_spmv<double, double>(lpr, gvec, st, n, rowptr, colind, val, p, q, S, part);
+            k_cg_update<double><<<gupd, BS, 0, st>>>(n, x, r, p, q, dinv, S, part, mi);
+        }
+        if (cudaGetLastError() != cudaSuccess) return ISL_ERR_CUDA;
+    }
+    if (iters) *iters = h.iters;
+    if (rel_res) *rel_res = h.rhsNorm2 > 0 ? std::sqrt(h.rr / h.rhsNorm2) : 0.0;
+    if (h.bad) return ISL_ERR_NAN;
+    if (h.done == 2) return ISL_ERR_NOT_CONVERGED;
+    return ISL_OK;
+}
+
+}  // namespace
+}  // namespace isl
+
+extern "C" int isl_cg_solve_noalloc(int device, void* stream, int n, const int32_t* rowptr, const int32_t* colind,
+                                    const double* val, const double* b, double* x, double tol, int64_t max_iter,
+                                    int64_t* iters, double* rel_res) {
+    if (n < 0 || !(tol >= 0.0)) return ISL_ERR_ARG;
+    if (n > ISL_NOALLOC_MAX_N) return ISL_ERR_CAPACITY;
+    if (n == 0) {
+        if (iters) *iters = 0;
+        if (rel_res) *rel_res = 0.0;
+        return ISL_OK;
+    }
+    if (!rowptr || !colind || !val || !b || !x) return ISL_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess) return ISL_ERR_CUDA;
+    if (device < 0 || device >= ndev || device >= NA_MAX_DEVICES) return ISL_ERR_ARG;
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return ISL_ERR_CUDA;
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) return ISL_ERR_CUDA;
+    isl::NoallocDevice dv;
+    int rc = isl::noalloc_setup(device, &dv);
+    if (rc == ISL_OK)
+        rc = isl::noalloc_cg(dv, (cudaStream_t)stream, n, rowptr, colind, val, b, x, tol, max_iter, iters, rel_res);
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}
