@@ -648,6 +648,63 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int
     }
 }
 
+// Same product with the loads of U slots issued before any of them is used:
+// U column indices and 9U values, then the 3U gathers of p, then the FMAs in
+// slot order (bit-identical sums to the kernel above).  More bytes in flight
+// per lane for the latency-bound stream; MINB bounds the registers.
+template <int U, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, const int* __restrict__ soff,
+                                                          const int* __restrict__ swid, const int* __restrict__ scol,
+                                                          const float* __restrict__ sv, const float* __restrict__ p,
+                                                          float* __restrict__ q, CGScal* S, double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
+    double loc = 0.0;
+    for (int s = warp; s < nslice; s += nwarps) {
+        const int i = s * 32 + lane;
+        const int o = soff[s], w = swid[s];  // o: multiple of 32; w: warp-uniform
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int k = 0; k < w; k += U) {
+            int j[U];
+            float v[U][9];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    j[u] = __ldg(scol + o + (k + u) * 32 + lane);
+                    const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) v[u][e] = __ldg(vp + 32 * e);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    const float x0 = __ldg(p + 3 * j[u]), x1 = __ldg(p + 3 * j[u] + 1), x2 = __ldg(p + 3 * j[u] + 2);
+                    a0 += v[u][0] * x0 + v[u][1] * x1 + v[u][2] * x2;
+                    a1 += v[u][3] * x0 + v[u][4] * x1 + v[u][5] * x2;
+                    a2 += v[u][6] * x0 + v[u][7] * x1 + v[u][8] * x2;
+                }
+            }
+        }
+        if (i < nbr) {
+            q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
+            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+        }
+    }
+    const double bsum = block_sum(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    if (last_block(&S->ticket1)) {
+        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        if (threadIdx.x == 0) {
+            S->pAp = tot;
+            S->alpha = S->absNew / tot;
+            S->ticket1 = 0;
+        }
+    }
+}
+
 // q = A p on the block-row CSR copy: LPB lanes per block row
 template <int LPB>
 __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
@@ -837,8 +894,9 @@ static unsigned sell_grid(isl_ctx* c) {
     return (unsigned)std::max<long long>(1, std::min<long long>(need, (long long)c->sm_count * (2048 / BS)));
 }
 
-// kind 1..3: sliced-ELL with slice-loop unroll 1, 2, 4; kind 4, 8, 16: block-row
-// CSR with that many lanes per block row
+// kind 1..3: sliced-ELL with slice-loop unroll 1, 2, 4; kind 5..7: sliced-ELL
+// with the loads of 2, 4, 8 slots batched; kind 4, 8, 16: block-row CSR with
+// that many lanes per block row
 static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
     (void)grid;
     const int nbr = (int)c->nbr, ns = (int)c->nslice, nb = (int)c->nblk;
@@ -846,6 +904,9 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
     switch (kind) {
         case 1: k_bspmv_pap<1><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
         case 3: k_bspmv_pap<4><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
+        case 5: k_bspmv_batch<2, 4><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, p, q, S, part); break;
+        case 6: k_bspmv_batch<4, 3><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, p, q, S, part); break;
+        case 7: k_bspmv_batch<8, 2><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, p, q, S, part); break;
         case 4: k_brow_spmv<4><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
         case 8: k_brow_spmv<8><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
         case 16: k_brow_spmv<16><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
@@ -855,13 +916,13 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 
 // autotune of the block SpMV (format and row mapping) on the current matrix
 static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
-    const int cand[6] = {1, 2, 3, 4, 8, 16};
+    const int cand[9] = {1, 2, 3, 5, 6, 7, 4, 8, 16};
     if (c->nbr < 8000) return 2;
     int best = 2;
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
-    c->launches += 36;
-    for (int k = 0; k < 6; ++k) {
+    c->launches += 54;
+    for (int k = 0; k < 9; ++k) {
         launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
         cudaEventRecord(c->ev[2], c->stream);
         for (int r = 0; r < 5; ++r) launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
