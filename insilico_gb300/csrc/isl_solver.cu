@@ -921,11 +921,11 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
     int best = 2;
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
-    c->launches += 54;
+    c->launches += 9 * 21;
     for (int k = 0; k < 9; ++k) {
         launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
         cudaEventRecord(c->ev[2], c->stream);
-        for (int r = 0; r < 5; ++r) launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
+        for (int r = 0; r < 20; ++r) launch_bspmv(cand[k], 0, c->stream, c, p, q, S, part);
         cudaEventRecord(c->ev[3], c->stream);
         cudaEventSynchronize(c->ev[3]);
         float ms = 0.f;
