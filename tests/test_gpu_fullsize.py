@@ -1,0 +1,213 @@
+"""Parity at the full config sizes, through the C-ABI.
+
+* c1 (Q1 Poisson 64^2): the whole system against the oracle (pattern
+  bit-exact, entries and RHS to 1e-12, CG solutions to 1e-9 / 1e-8).
+* c2 (hex8 elasticity 64^3, 811,200 DOFs) and c3 (tet10 Poisson 64^3,
+  2,146,689 DOF objects): properties that do not depend on size:
+  - patch parity: the rows of sampled DOFs (a vertex and, for tet10, the edge
+    DOFs incident to it) equal the oracle's assembly of only the elements
+    touching that vertex.  DOFs are mapped through (element, local function).
+    The patch constrains what lies on the domain boundary, as the full problem
+    does;
+  - exact symmetry of the assembled matrix;
+  - the null space of the operator on rows away from constrained DOFs:
+    constants for the Laplacian; translations and infinitesimal rotations for
+    linear elasticity;
+  - the returned solutions: the FP64 residual ||b - A x|| recomputed on the
+    host, and the FP64 and mixed solutions within 1e-8 of a tight FP64 solve.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle as O
+from insilico_gb300 import _abi as A
+from insilico_gb300 import workloads as W
+
+from helpers import csr_entry_err, oracle_problem
+
+pytestmark = pytest.mark.gpu
+
+ENTRY_TOL = 1e-12
+TET_EDGES = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]  # local edges of tet10 DOF objects 4..9
+
+
+def on_cube_boundary(x):
+    return np.any((np.abs(x) < 1e-9) | (np.abs(x - 1.0) < 1e-9), axis=1)
+
+
+def patch_problem(p, elems):
+    """The elements `elems` of problem p as a problem of their own: same
+    coordinates, coefficients, sources and boundary conditions."""
+    nodes, inv = np.unique(p.conn[elems], return_inverse=True)
+    conn = inv.reshape(len(elems), -1).astype(np.int64)
+    kw = {}
+    if p.kappa is not None:
+        kw["kappa"] = p.kappa[elems]
+    if p.lam is not None:
+        kw["lam"], kw["mu"] = p.lam[elems], p.mu[elems]
+    if p.name == "c2":
+        diri = p.dirichlet  # clamps x = 0, a function of the coordinates
+    else:
+        ncomp = p.ncomp
+
+        def diri(x):
+            return np.repeat(on_cube_boundary(x)[:, None], ncomp, axis=1), 0.0
+    return W.Problem("patch", p.shape, p.X[nodes], conn, p.fedeg, p.ncomp, p.kernel, p.qdeg, material=p.material,
+                     body=None if p.body is None else p.body[nodes], dirichlet=diri, neumann_plane=p.neumann_plane, **kw)
+
+
+def check_patch_rows(p, S, rp, ci, v, b, nsample=24, seed=7):
+    """Rows of sampled vertex DOF objects (and, for tet10, the edge DOF objects
+    incident to them) against the oracle's assembly of their element stars."""
+    conn = p.conn
+    nvert = conn.shape[1]
+    edof_full = S.elem_dofobj()
+    eq_full = S.dof_index()
+    g = np.random.default_rng(seed)
+    verts = g.choice(np.unique(conn), size=nsample, replace=False)
+    if p.name == "c2":
+        # rows on the traction face and next to the clamped face
+        x1 = np.nonzero(np.abs(p.X[:, 0] - 1.0) < 1e-9)[0]
+        x0n = np.nonzero(np.abs(p.X[:, 0] - 1.0 / p.meta["n"]) < 1e-9)[0]
+        verts = np.concatenate([verts, g.choice(x1, 4, replace=False), g.choice(x0n, 4, replace=False)])
+    vs = set(verts.tolist())
+    star = np.unique(np.nonzero(np.isin(conn, verts))[0])
+    P, (srp, sci, sv, sb) = oracle_problem(patch_problem(p, star))
+    edof_sub, eq_sub = P.elem_dofobj(), P.eq_index()
+    nc = p.ncomp
+    s2f, rows = {}, set()
+    for t, e in enumerate(star):
+        for a in range(edof_full.shape[1]):
+            if a < nvert:
+                mine = conn[e, a] in vs
+            else:
+                i, j = TET_EDGES[a - nvert]
+                mine = conn[e, i] in vs or conn[e, j] in vs
+            if mine:
+                rows.add(int(edof_full[e, a]))
+            for k in range(nc):
+                es, ef = eq_sub[edof_sub[t, a] * nc + k], eq_full[edof_full[e, a] * nc + k]
+                assert (es < 0) == (ef < 0)
+                if es >= 0:
+                    assert s2f.setdefault(int(es), int(ef)) == ef
+    f2s = {f: s_ for s_, f in s2f.items()}
+
+    def full_diag(r):
+        return v[rp[r]:rp[r + 1]][ci[rp[r]:rp[r + 1]] == r][0]
+
+    bmax = np.max(np.abs(b))
+    checked = 0
+    for obj in sorted(rows):
+        for k in range(nc):
+            ef = int(eq_full[obj * nc + k])
+            if ef < 0:
+                continue
+            es = f2s[ef]
+            gcols, gvals = ci[rp[ef]:rp[ef + 1]], v[rp[ef]:rp[ef + 1]]
+            scols = np.array([s2f[int(c)] for c in sci[srp[es]:srp[es + 1]]])
+            order = np.argsort(scols)
+            scols, svals = scols[order], sv[srp[es]:srp[es + 1]][order]
+            np.testing.assert_array_equal(gcols, scols)
+            dscale = np.sqrt(abs(full_diag(ef)) * np.abs([full_diag(int(c)) for c in gcols]))
+            assert np.max(np.abs(gvals - svals) / np.maximum(np.abs(svals), dscale)) <= ENTRY_TOL
+            assert abs(b[ef] - sb[es]) <= ENTRY_TOL * max(abs(sb[es]), 1e-3 * bmax)
+            checked += 1
+    assert checked >= nsample
+    return checked
+
+
+def interior_rows(S, eq, ncomp):
+    """Equations whose rows meet no constrained DOF (every element around them
+    has only active DOFs)."""
+    edof = S.elem_dofobj()
+    con = (eq.reshape(-1, ncomp) < 0).any(axis=1)
+    touch = np.zeros(len(con), dtype=bool)
+    touch[np.unique(edof[con[edof].any(axis=1)])] = True
+    objs = np.nonzero(~touch & ~con)[0]
+    return eq.reshape(-1, ncomp)[objs].ravel()
+
+
+def check_solutions(S, A64, b, tol):
+    """FP64 and mixed solves: host FP64 residual within 10 tol (the solver's
+    own test is on its iterated or device residual) and both solutions within
+    1e-8 of a tight FP64 solve."""
+    bn = np.linalg.norm(b)
+    S.solve(A.SOLVE_CG_FP64, tol=tol)
+    x64 = S.solution()
+    assert np.linalg.norm(b - A64 @ x64) <= 10 * tol * bn
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=tol)
+    xm = S.solution()
+    assert np.linalg.norm(b - A64 @ xm) <= 10 * tol * bn
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    xt = S.solution()
+    assert np.linalg.norm(xm - xt) <= 1e-8 * np.linalg.norm(xt)
+    assert np.linalg.norm(x64 - xt) <= 1e-8 * np.linalg.norm(xt)
+
+
+def test_c1_full_size_against_oracle():
+    p = W.config("c1")
+    S = W.setup_system(p)
+    P, (rp, ci, v, b) = oracle_problem(p)
+    assert S.neq == P.neq == 3969
+    S.assemble(A.PREC_FP64)
+    grp, gci, gv = S.csr()
+    np.testing.assert_array_equal(grp, rp)
+    np.testing.assert_array_equal(gci, ci)
+    assert len(gci) == 34969
+    assert csr_entry_err(rp, ci, gv, v) <= ENTRY_TOL
+    gb = S.rhs()
+    assert np.max(np.abs(gb - b)) <= ENTRY_TOL * np.max(np.abs(b))
+    S.solve(A.SOLVE_CG_FP64, tol=1e-12)
+    xo, _, _ = O.cg(rp, ci, v, b, tol=1e-13)
+    assert np.linalg.norm(S.solution() - xo) <= 1e-9 * np.linalg.norm(xo)
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    assert np.linalg.norm(S.solution() - xo) <= 1e-8 * np.linalg.norm(xo)
+    S.close()
+
+
+def null_modes(p, S, eq):
+    """Fields the operator annihilates away from constraints."""
+    if p.kernel == "laplace":
+        return [np.ones(S.neq)]
+    act = eq >= 0
+    Xn = np.repeat(p.X, 3, axis=0)[act]  # node coordinates of each active equation
+    comp = np.tile(np.arange(3), len(p.X))[act]
+    modes = [(comp == a).astype(float) for a in range(3)]  # translations
+    for a in range(3):  # infinitesimal rotations u = w x X
+        w = np.zeros(3)
+        w[a] = 1.0
+        rot = np.cross(np.broadcast_to(w, Xn.shape), Xn)
+        modes.append(rot[np.arange(S.neq), comp])
+    return modes
+
+
+@pytest.mark.parametrize("name", ["c2", "c3"])
+def test_full_size_properties(name):
+    p = W.config(name)
+    S = W.setup_system(p)
+    if name == "c2":
+        assert S.neq == 811200 and S.nnz == 63695790
+    else:
+        assert S.ndofobj == 2146689
+    S.assemble(A.PREC_FP64)
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    assert check_patch_rows(p, S, rp, ci, v, b) > 0
+    # symmetry: both triangles come from the same staged entries
+    A64 = sp.csr_matrix((v, ci, rp), shape=(S.neq, S.neq))
+    D = (A64 - A64.T).tocsr()
+    D.eliminate_zeros()
+    assert D.nnz == 0
+    # null space on rows away from constrained DOFs
+    eq = S.dof_index()
+    rows = interior_rows(S, eq, p.ncomp)
+    assert len(rows) > S.neq // 2
+    absrow = abs(A64) @ np.ones(S.neq)
+    for u in null_modes(p, S, eq):
+        r = A64 @ u
+        assert np.max(np.abs(r[rows]) / (absrow[rows] * max(1.0, np.max(np.abs(u))))) <= 1e-12
+    check_solutions(S, A64, b, tol=1e-10)
+    S.close()
