@@ -211,3 +211,78 @@ def test_full_size_properties(name):
         assert np.max(np.abs(r[rows]) / (absrow[rows] * max(1.0, np.max(np.abs(u))))) <= 1e-12
     check_solutions(S, A64, b, tol=1e-10)
     S.close()
+
+
+def poisson_instance(side, deg, seed):
+    """One c4 instance: unit square, kappa_e = exp(N(0, 0.5)), nodal source U[0, 1], g = 0."""
+    X, conn = W.unit_cube("quad", side, side)
+    kappa = np.exp(W.rng(seed, 0).normal(0.0, 0.5, len(conn)))
+    f = W.rng(seed, 1).uniform(0.0, 1.0, len(X))[:, None]
+    return W.Problem("inst", A.QUAD, X, conn, deg, 1, "laplace", 2 * deg, kappa=kappa, body=f,
+                     dirichlet=lambda x: (np.ones((len(x), 1), dtype=bool), 0.0), tol=1e-8)
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_c4_batch_at_full_instance_sizes(deg):
+    """Batched instances at the c4 extremes (side 8 to 256): each instance's
+    numbering, pattern and FP64 values are bitwise those of the instance solved
+    alone; FP64 and mixed solves meet 1e-8 with their own convergence, and the
+    mixed solution is within 1e-8 of the tight FP64 one."""
+    from insilico_gb300.system import System
+    sides = [256, 8, 131, 64, 9]
+    probs = [poisson_instance(s, deg, 500 + s) for s in sides]
+    S = System()
+    S.upload_batch(A.QUAD, [(p.X, p.conn) for p in probs])
+    S.create_field(deg, 1)
+    S.constrain_boundary(lambda x: (np.ones((len(x), 1), dtype=bool), 0.0))
+    S.number_dofs()
+    S.register_pattern()
+    S.set_laplace(np.concatenate([p.kappa for p in probs]), 2 * deg)
+    S.set_body_force_nodal(np.concatenate([p.body for p in probs]))
+    eq_off, _ = S.batch_info()
+    S.assemble(A.PREC_MIXED)
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    xt = S.solution()
+    S.solve(A.SOLVE_CG_FP64, tol=1e-8)
+    x64 = S.solution()
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-8)
+    xm = S.solution()
+    it, _ = S.batch_stats()
+    for k, p in enumerate(probs):
+        r0, r1 = eq_off[k], eq_off[k + 1]
+        one = W.setup_system(p)
+        one.assemble(A.PREC_FP64)
+        orp, oci, ov = one.csr()
+        assert one.neq == r1 - r0
+        np.testing.assert_array_equal(rp[r0:r1 + 1] - rp[r0], orp)
+        np.testing.assert_array_equal(ci[rp[r0]:rp[r1]] - r0, oci)
+        np.testing.assert_array_equal(v[rp[r0]:rp[r1]], ov)
+        np.testing.assert_array_equal(b[r0:r1], one.rhs())
+        one.close()
+        Ak = sp.csr_matrix((ov, oci, orp), shape=(r1 - r0, r1 - r0))
+        bk, tk = b[r0:r1], xt[r0:r1]
+        assert np.linalg.norm(bk - Ak @ x64[r0:r1]) <= 10 * 1e-8 * np.linalg.norm(bk)
+        assert np.linalg.norm(bk - Ak @ xm[r0:r1]) <= 10 * 1e-8 * np.linalg.norm(bk)
+        # at a residual tolerance the solution error follows the conditioning:
+        # the mixed solve must be as accurate as the FP64 solve at that tolerance
+        e64 = np.linalg.norm(x64[r0:r1] - tk)
+        assert np.linalg.norm(xm[r0:r1] - tk) <= max(1e-8 * np.linalg.norm(tk), 10 * e64)
+        assert it[k] > 0
+    S.close()
+
+
+def test_c5_requests_at_full_size():
+    """Served neo-Hookean requests at the largest c5 sides: the plain FP64 and
+    the mixed servers converge and agree within 1e-8."""
+    from insilico_gb300 import serve
+    reqs = [serve.Request(0, side=48, mu=0.37), serve.Request(1, side=29, mu=6.1)]
+    out = {}
+    for mixed in (False, True):
+        solver = serve.NewtonSolver(mixed=mixed)
+        out[mixed] = [solver.run(serve.Request(r.rid, r.side, r.mu)) for r in reqs]
+        solver.close()
+    for rp_, rm in zip(out[False], out[True]):
+        assert rp_.converged and rm.converged
+        assert np.linalg.norm(rm.u - rp_.u) <= 1e-8 * np.linalg.norm(rp_.u)
