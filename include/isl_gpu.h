@@ -184,8 +184,14 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * constrained; 0 keeps the scalar CSR + Jacobi path.  Read-only through
  * isl_get_option: ISL_OPT_BLOCKED (the pattern is node-blocked),
  * ISL_OPT_NBLOCKS (stored 3x3 blocks), ISL_OPT_NSLOTS (block slots of the
- * sliced-ELL copy, padding included). */
-enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3 };
+ * sliced-ELL copy, padding included).  ISL_OPT_PERSISTENT selects the
+ * one-launch CG kernels of the mixed solve: 0 never (CUDA graphs of separate
+ * kernels), 1 (default) for small systems, where launch latency dominates:
+ * a scalar system of at most 65,536 equations is solved whole, FP64 reliable
+ * updates included, by one thread-block cluster; a node-blocked system of at
+ * most 32,768 nodes runs its iterations in a persistent cooperative kernel.
+ * 2: the persistent block kernel at every size. */
+enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 

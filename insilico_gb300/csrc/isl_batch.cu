@@ -60,9 +60,7 @@ __device__ inline void finish(const BArgs& a, int k, int code) {
 
 __device__ inline double inst_sum(const BArgs& a, int k, int off, double* sh) {
     const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
-    double v = 0.0;
-    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) v += __ldcg(a.part + (size_t)off * gridDim.x + i);
-    return block_sum(v, sh);
+    return reduce_parts(a.part + (size_t)off * gridDim.x + b0, b1 - b0, 1, 0, sh);
 }
 
 template <typename TB, typename TX>
@@ -120,7 +118,7 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
     const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
     const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
     const int wgrp = grp - grp % (32 / LPR);  // warp-uniform loop (full-mask shuffles)
-    double loc = 0.0;
+    TX loc = TX(0);  // in the vectors' precision; warp sums are added in FP64
     for (int base = r0 + wgrp; base < r1; base += BBS / LPR) {
         const int row = base + (grp - wgrp);
         const bool act = row < r1;
@@ -131,10 +129,10 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
         for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
         if (act && lane == 0) {
             q[row] = acc;
-            loc += (double)(p[row] * acc);
+            loc += p[row] * acc;
         }
     }
-    const double s1 = block_sum(loc, sh);
+    const double s1 = block_sum_t(loc, sh);
     if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
@@ -164,7 +162,7 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
         rr += ri * ri;
         rz += ri * (dinv[i] * ri);
     }
-    const double s1 = block_sum((double)rr, sh), s2 = block_sum((double)rz, sh);
+    const double s1 = block_sum_t(rr, sh), s2 = block_sum_t(rz, sh);
     if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[gridDim.x + blockIdx.x] = s2; }
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {

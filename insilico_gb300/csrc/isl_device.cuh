@@ -9,6 +9,55 @@ namespace isl {
 template <typename T>
 __device__ inline T ld(const T* p) { return __ldg(p); }
 
+// Loads with a cache hint for data streamed once per kernel (not kept in L1)
+__device__ __forceinline__ float ld_stream(const float* p) {
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int ld_stream(const int* p) {
+    int v;
+    asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+// Software barrier across the blocks of a cooperative launch (every block is
+// resident).  bar[0] counts arrivals, bar[1] is the generation.  Thread 0 of
+// each block arrives with a release add (after the block barrier, so it
+// publishes the writes of the whole block) and polls the generation with
+// acquire loads, with an iteration limit: on expiry it sets *fault and the
+// barrier reports false in every thread of the block.  A block that sees
+// *fault set also reports false, so all blocks leave.  After the barrier,
+// ordinary loads see every block's writes from before it (the acquire and
+// the block barrier order them); only the non-coherent load path must not be
+// used for data written inside the same launch.
+constexpr unsigned GRID_SYNC_LIMIT = 1u << 22;
+__device__ inline bool grid_sync(unsigned* bar, int* fault) {
+    __shared__ int gs_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        unsigned gen, prev;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(prev) : "l"(bar) : "memory");
+        if (prev + 1u == gridDim.x) {
+            bar[0] = 0u;
+            asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(bar + 1), "r"(gen + 1u) : "memory");
+        } else {
+            unsigned it = 0, g;
+            for (;;) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+                if (g != gen) break;
+                if (++it > GRID_SYNC_LIMIT || *(volatile int*)fault) { ok = 0; atomicExch(fault, 1); break; }
+            }
+        }
+        if (*(volatile int*)fault) ok = 0;
+        gs_ok = ok;
+    }
+    __syncthreads();
+    return gs_ok != 0;
+}
+
 // fixed-order block reduction of a double (deterministic); result in thread 0
 __device__ inline double block_sum(double v, double* sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -54,41 +103,74 @@ __device__ inline bool last_of(unsigned int* ticket, unsigned int count) {
     return amLastOf;
 }
 
-// Sum of part[i*stride + off], i < n, by one block: the loads of a thread are
-// issued together (unrolled) before they are added, in a fixed order.
+// Block sum of FP32 values: each warp adds its lanes in FP32 (the precision of
+// the values), the warp sums are added in FP64 by warp 0.  FP64 arithmetic
+// runs at 1/64 of the FP32 rate on this GPU, so the FP64 part is kept to one
+// warp.  Fixed order; the result is valid in warp 0 (thread 0).
+__device__ inline double block_sum_f(float v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = (double)v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+
+// the block sum matching the precision of the summed values
+__device__ inline double block_sum_t(float v, double* sh) { return block_sum_f(v, sh); }
+__device__ inline double block_sum_t(double v, double* sh) { return block_sum(v, sh); }
+
+// Sum of part[i*stride + off], i < n, by warp 0 of the calling block: each lane
+// issues eight loads before adding them, then a fixed shuffle tree.  The
+// result is valid in warp 0 (thread 0); the other warps return 0.
 __device__ inline double reduce_parts(const double* part, int n, int stride, int off, double* sh) {
+    (void)sh;
+    if (threadIdx.x >= 32) return 0.0;
+    const int l = threadIdx.x;
     double s = 0.0;
-    int i = threadIdx.x;
-    for (; i + 3 * (int)blockDim.x < n; i += 4 * blockDim.x) {
-        const double a = __ldcg(part + (size_t)i * stride + off);
-        const double b = __ldcg(part + (size_t)(i + blockDim.x) * stride + off);
-        const double c = __ldcg(part + (size_t)(i + 2 * blockDim.x) * stride + off);
-        const double d = __ldcg(part + (size_t)(i + 3 * blockDim.x) * stride + off);
-        s += (a + b) + (c + d);
+    for (int base = 0; base < n; base += 256) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * 32 + l;
+            v[u] = i < n ? __ldcg(part + (size_t)i * stride + off) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
     }
-    for (; i < n; i += blockDim.x) s += __ldcg(part + (size_t)i * stride + off);
-    return block_sum(s, sh);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
 }
 
-// The two interleaved sums part[2i], part[2i+1] (i < n) in one pass.
+// The two interleaved sums part[2i], part[2i+1] (i < n), by warp 0 as above.
 __device__ inline void reduce_parts2(const double* part, int n, double* sh, double& out0, double& out1) {
-    double s0 = 0.0, s1 = 0.0;
+    (void)sh;
+    out0 = out1 = 0.0;
+    if (threadIdx.x >= 32) return;
+    const int l = threadIdx.x;
     const double2* p2 = reinterpret_cast<const double2*>(part);
-    int i = threadIdx.x;
-    for (; i + 3 * (int)blockDim.x < n; i += 4 * blockDim.x) {
-        const double2 a = __ldcg(p2 + i), b = __ldcg(p2 + i + blockDim.x);
-        const double2 c = __ldcg(p2 + i + 2 * blockDim.x), d = __ldcg(p2 + i + 3 * blockDim.x);
-        s0 += (a.x + b.x) + (c.x + d.x);
-        s1 += (a.y + b.y) + (c.y + d.y);
+    double s0 = 0.0, s1 = 0.0;
+    for (int base = 0; base < n; base += 256) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * 32 + l;
+            v[u] = i < n ? __ldcg(p2 + i) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { s0 += v[u].x; s1 += v[u].y; }
     }
-    for (; i < n; i += blockDim.x) {
-        const double2 a = __ldcg(p2 + i);
-        s0 += a.x;
-        s1 += a.y;
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
     }
-    out0 = block_sum(s0, sh);
-    out1 = block_sum(s1, sh);
+    out0 = s0;
+    out1 = s1;
 }
-
 
 }  // namespace isl

@@ -98,7 +98,7 @@ struct CGScal {
     int done;
     int iters;
     int bad;
-    int pad;
+    int fault;   // persistent CG: a grid barrier timed out
     unsigned int ticket1, ticket2;
 };
 
@@ -175,6 +175,10 @@ struct isl_ctx {
     // when every DOF object has all three components active or all constrained
     bool blocked = false;
     bool use_block = true;
+    int use_persist = 1;         // one-launch CG kernels: 0 never, 1 for small systems, 2 always where supported
+    int cluster_size = -1;       // CTAs of the small-system cluster solve (-1: not yet probed, 0: unavailable)
+    int persist_grid = -1;       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)
+    isl::DBuf<unsigned int> dbar; // grid barrier of the persistent kernel: arrivals, generation
     int64_t nbr = 0, nblk = 0;
     isl::DBuf<int32_t> dbptr, dbcol, dbrow;
     // sliced-ELL copy of the blocks for the SpMV: block rows in slices of 32,

@@ -26,6 +26,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "isl_internal.h"
 #include "isl_device.cuh"
 
@@ -62,17 +64,17 @@ __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ 
     const int lane = threadIdx.x % LPR;
     const int grp = (blockIdx.x * BS + threadIdx.x) / LPR, ngrp = gridDim.x * BS / LPR;
     const int wgrp = grp - grp % (32 / LPR);  // first group of this warp: the loop is warp-uniform
-    double loc = 0.0;
+    TX loc = TX(0);  // accumulated in the vectors' precision, summed across warps in FP64
     for (int base = wgrp; base < n; base += ngrp) {
         const int row = base + (grp - wgrp);
         const bool act = row < n;
         const TX acc = row_dot<TV, TX, LPR>(row, act, rowptr, colind, val, p, lane);
         if (act && lane == 0) {
             q[row] = acc;
-            loc += (double)(p[row] * acc);
+            loc += p[row] * acc;
         }
     }
-    const double bs = block_sum(loc, sh);
+    const double bs = block_sum_t(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
     if (last_block(&S->ticket1)) {
         const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
@@ -120,8 +122,8 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
         rr += ri * ri;
         rz += ri * (dinv[i] * ri);
     }
-    const double b1 = block_sum((double)rr, sh);
-    const double b2 = block_sum((double)rz, sh);
+    const double b1 = block_sum_t(rr, sh);
+    const double b2 = block_sum_t(rz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
         double trr, trz;
@@ -362,6 +364,10 @@ static int ensure_work(isl_ctx* c) {
     const size_t maxgrid = (size_t)16 * c->sm_count;
     if (c->dpart.n < 2 * maxgrid + 64) ISL_CHECK_CUDA(c, c->dpart.alloc(2 * maxgrid + 64));
     if (!c->dscal.p) ISL_CHECK_CUDA(c, c->dscal.alloc(2));
+    if (!c->dbar.p) {
+        ISL_CHECK_CUDA(c, c->dbar.alloc(2));
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbar.p, 0, 2 * sizeof(unsigned), c->stream));
+    }
     return ISL_OK;
 }
 
@@ -405,7 +411,300 @@ static int solve_fp64(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, 
 }
 
 // FP32 CG with FP64 reliable updates
+// ---------------------------------------------------------------------------
+// Small scalar systems: the whole mixed solve in one thread-block cluster.
+// The CTAs of one cluster split the rows; hardware cluster barriers separate
+// the phases and the partial sums are exchanged through distributed shared
+// memory, every CTA adding the CTAs' sums in rank order (so all CTAs hold the
+// same scalars).  The FP32 iterations and the FP64 reliable updates (fold,
+// b - A64 x, restart) all run inside the one launch, with the recurrences of
+// the graph path (k_cg_dir, k_spmv_pap, k_cg_update, k_fold, k_residual64,
+// k_restart32).
+namespace cgrp = cooperative_groups;
+constexpr int CL_BS = 1024;
+constexpr int CLUSTER_MAX_N = 65536;
+
+// row . v with plain (coherent) loads of v: v is written inside the launch
+template <typename TV, typename TX, int LPR>
+__device__ inline TX row_dot_c(int row, bool active, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                               const TV* __restrict__ val, const TX* v, int lane) {
+    TX acc = TX(0);
+    if (active) {
+        const int lo = __ldg(rowptr + row), hi = __ldg(rowptr + row + 1);
+        for (int k = lo + lane; k < hi; k += LPR) acc += (TX)__ldg(val + k) * v[__ldg(colind + k)];
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+    return acc;
+}
+
+// sums of (a, b) over all threads of the cluster, in a fixed order: each CTA
+// reduces its threads (one pass for both values; the warps in the values'
+// precision, the warp sums in FP64 by one warp), lane k of warp 0 reads CTA
+// k's pair through distributed shared memory, and a fixed shuffle tree adds
+// the CTAs (so every CTA holds the same totals).  The slot cycles, so a CTA
+// never rewrites a slot that a peer may still read.
+template <typename T>
+__device__ inline void cluster_sum2(T a, T b, double (*red)[2], int& slot, double* sh, double* bc, double& ta, double& tb) {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {  // within a warp in the values' own precision
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    __syncthreads();  // sh is free (previous users are done)
+    if (l == 0) { sh[2 * w] = (double)a; sh[2 * w + 1] = (double)b; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (int)(blockDim.x >> 5);
+        double u = l < nw ? sh[2 * l] : 0.0, v = l < nw ? sh[2 * l + 1] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            u += __shfl_xor_sync(0xffffffffu, u, o);
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        }
+        if (l == 0) { red[slot][0] = u; red[slot][1] = v; }
+    }
+    cl.sync();
+    if (w == 0) {
+        const int n = (int)cl.num_blocks();
+        double u = 0.0, v = 0.0;
+        if (l < n) {
+            const double* peer = cl.map_shared_rank(&red[slot][0], l);
+            u = peer[0];
+            v = peer[1];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            u += __shfl_xor_sync(0xffffffffu, u, o);
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        }
+        if (l == 0) { bc[0] = u; bc[1] = v; }
+    }
+    __syncthreads();
+    ta = bc[0];
+    tb = bc[1];
+    slot = (slot + 1) & 3;
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                                                         const float* __restrict__ val32, const double* __restrict__ val64,
+                                                         const double* __restrict__ b, const float* __restrict__ dinv,
+                                                         float* x32, float* r32, float* p32, float* q32, double* x64,
+                                                         double* r64, CGScal* S, int max_iter, int exact64) {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    __shared__ double sh[2 * (CL_BS / 32)];
+    __shared__ double red[4][2];
+    __shared__ double bc[2];
+    const int rank = (int)cl.block_rank(), ncta = (int)cl.num_blocks();
+    const int r0 = (int)((long long)n * rank / ncta), r1 = (int)((long long)n * (rank + 1) / ncta);
+    const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR, ngrp = CL_BS / LPR;
+    const int wgrp = grp - grp % (32 / LPR);  // first row group of this warp: row loops stay warp-uniform
+    int slot = 0;
+    double rz = S->absNew, rz_old = S->absOld, beta = S->beta, rr = S->rr;
+    const double thr = S->threshold;
+    double trig = S->rrtrig, rr_true = S->rhsNorm2;
+    int iters = S->iters, done = S->done, bad = 0;
+    double t0, t1;
+    while (!done) {
+        // p = D^-1 r + beta p
+        const float fb = (float)beta;
+        for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) p32[i] = dinv[i] * r32[i] + fb * p32[i];
+        cl.sync();
+        // q = A p, p.q
+        float loc = 0.f;
+        for (int base = r0 + wgrp; base < r1; base += ngrp) {
+            const int row = base + (grp - wgrp);
+            const bool act = row < r1;
+            const float acc = row_dot_c<float, float, LPR>(row, act, rowptr, colind, val32, p32, lane);
+            if (act && lane == 0) {
+                q32[row] = acc;
+                loc += p32[row] * acc;
+            }
+        }
+        cluster_sum2(loc, 0.f, red, slot, sh, bc, t0, t1);
+        const float alpha = (float)(rz / t0);
+        // x += alpha p, r -= alpha q; r.r, r.z
+        float frr = 0.f, frz = 0.f;
+        for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) {
+            x32[i] += alpha * p32[i];
+            const float ri = r32[i] - alpha * q32[i];
+            r32[i] = ri;
+            frr += ri * ri;
+            frz += ri * (dinv[i] * ri);
+        }
+        cluster_sum2(frr, frz, red, slot, sh, bc, t0, t1);
+        iters += 1;
+        rr = t0;
+        rz_old = rz;
+        beta = t1 / rz;
+        rz = t1;
+        if (!(t0 == t0) || !(t1 == t1)) { bad = 1; done = 1; break; }
+        const bool conv_it = t0 < thr;
+        if (!exact64) {
+            // FP32 CG on the iterated residual (inexact Newton steps)
+            if (conv_it) done = 1;
+            else if (iters >= max_iter) done = 2;
+            if (done) {
+                rr_true = t0;
+                for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) { x64[i] += (double)x32[i]; x32[i] = 0.f; }
+            }
+            continue;
+        }
+        if (conv_it || t0 < trig || iters >= max_iter) {
+            // reliable update: fold the FP32 increment, true residual in FP64
+            for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) { x64[i] += (double)x32[i]; x32[i] = 0.f; }
+            cl.sync();
+            double lt = 0.0;
+            for (int base = r0 + wgrp; base < r1; base += ngrp) {
+                const int row = base + (grp - wgrp);
+                const bool act = row < r1;
+                const double ax = row_dot_c<double, double, LPR>(row, act, rowptr, colind, val64, x64, lane);
+                if (act && lane == 0) {
+                    const double ri = b[row] - ax;
+                    r64[row] = ri;
+                    lt += ri * ri;
+                }
+            }
+            cluster_sum2(lt, 0.0, red, slot, sh, bc, t0, t1);
+            rr_true = t0;
+            if (!(rr_true == rr_true)) { bad = 1; done = 1; break; }
+            if (rr_true <= thr) { done = 1; break; }
+            if (iters >= max_iter) { done = 2; break; }
+            // restart from the true residual, keeping the search direction
+            double lrr = 0.0, lrz = 0.0;
+            for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) {
+                const float ri = (float)r64[i];
+                r32[i] = ri;
+                lrr += (double)ri * (double)ri;
+                lrz += (double)ri * (double)(dinv[i] * ri);
+            }
+            cluster_sum2(lrr, lrz, red, slot, sh, bc, t0, t1);
+            rr = t0;
+            beta = t1 / rz_old;
+            rz = t1;
+            trig = kDelta2 * rr_true;
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        S->rr = rr;
+        S->rz = rr_true;
+        S->iters = iters;
+        S->absOld = rz_old;
+        S->absNew = rz;
+        S->beta = beta;
+        if (bad) S->bad = 1;
+        S->done = done;
+    }
+    // no CTA may leave while a peer can still read its shared memory
+    cl.sync();
+}
+
+template <int LPR>
+static cudaError_t launch_cluster(int ncta, cudaStream_t st, int n, const int* rp, const int* ci, const float* v32,
+                                  const double* v64, const double* b, const float* dinv, float* x32, float* r32, float* p32,
+                                  float* q32, double* x64, double* r64, CGScal* S, int mi, int exact64) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ncta);
+    cfg.blockDim = dim3(CL_BS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ncta;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cg_cluster<LPR>, n, rp, ci, v32, v64, b, dinv, x32, r32, p32, q32, x64, r64, S, mi,
+                              exact64);
+}
+
+// CTAs of the cluster: 16 where the device allows that size, else 8; 0 when
+// cluster launches are unavailable
+template <int LPR>
+static int probe_cluster(isl_ctx* c) {
+    int ok = 0;
+    if (cudaDeviceGetAttribute(&ok, cudaDevAttrClusterLaunch, c->device) != cudaSuccess || !ok) return 0;
+    cudaFuncSetAttribute(k_cg_cluster<LPR>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int ncta : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(ncta);
+        cfg.blockDim = dim3(CL_BS);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = ncta;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_cg_cluster<LPR>, &cfg) == cudaSuccess && nclusters > 0) return ncta;
+    }
+    cudaGetLastError();
+    return 0;
+}
+
+static int cluster_ctas(isl_ctx* c) {
+    if (c->cluster_size < 0) {
+        // every LPR variant shares the size limits; probe all so that each can be launched
+        int a = probe_cluster<2>(c), b = probe_cluster<4>(c), d = probe_cluster<8>(c), e = probe_cluster<16>(c),
+            f = probe_cluster<32>(c);
+        c->cluster_size = std::min(std::min(std::min(a, b), std::min(d, e)), f);
+        cudaGetLastError();
+    }
+    return c->cluster_size;
+}
+
+static int solve_mixed_cluster(isl_ctx* c, int ncta, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
+    cudaStream_t st = c->stream;
+    const int n = (int)c->neq;
+    double* W = c->w64.p;
+    double *x64 = W, *r64 = W + n;
+    float* V = c->w32.p;
+    float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n;
+    const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    const unsigned grid = vec_grid(c);
+    CGScal* S = c->dscal.p;
+    const int exact64 = c->have64 ? 1 : 0;
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, sizeof(CGScal), st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, (size_t)n * 8, st));
+    k_dinv<float, float><<<grid, BS, 0, st>>>(n, c->ddiag.p, c->dval32.p, d32);
+    k_cg_init<double, float><<<grid, BS, 0, st>>>(n, c->drhs.p, x32, r32, p32, d32, S, c->dpart.p, tol, exact64 ? kDelta2 : 0.0);
+    // lanes per row: from the mean row length, but few enough that the rows of
+    // one CTA take a single pass of its threads
+    const double avg = (double)c->nnz / (double)n;
+    int lpr = 2;
+    while (lpr < 32 && lpr < avg / 2) lpr *= 2;
+    const int rows_per_cta = (n + ncta - 1) / ncta;
+    while (lpr > 2 && (long long)rows_per_cta * lpr > CL_BS) lpr /= 2;
+    cudaError_t e;
+    switch (lpr) {
+        case 2: e = launch_cluster<2>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
+        case 4: e = launch_cluster<4>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
+        case 8: e = launch_cluster<8>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
+        case 16: e = launch_cluster<16>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
+        default: e = launch_cluster<32>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
+    }
+    ISL_CHECK_CUDA(c, e);
+    c->launches += 3;
+    int rc = read_scal(c);
+    if (rc != ISL_OK) return rc;
+    const CGScal& h = *c->hscal;
+    if (h.bad) ISL_FAIL(c, ISL_ERR_NAN, "CG breakdown (non-finite reduction)");
+    const double bnorm2 = h.rhsNorm2;
+    *iters = h.iters;
+    *rel = bnorm2 > 0 ? std::sqrt((h.iters > 0 ? h.rz : bnorm2) / bnorm2) : 0.0;
+    *nc = (h.done == 2);
+    k_copy64<<<grid, BS, 0, st>>>(n, x64, c->dsol.p);
+    c->launches += 1;
+    return ISL_OK;
+}
+
 static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
+    if (c->use_persist != 0 && c->neq <= CLUSTER_MAX_N) {
+        const int ncta = cluster_ctas(c);
+        if (ncta > 0) return solve_mixed_cluster(c, ncta, tol, max_iter, iters, rel, nc);
+    }
     cudaStream_t st = c->stream;
     const size_t n = (size_t)c->neq;
     double* W = c->w64.p;
@@ -616,7 +915,7 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int
     __shared__ double sh[32];
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    double loc = 0.0;
+    float loc = 0.f;
     for (int s = warp; s < nslice; s += nwarps) {
         const int i = s * 32 + lane;
         const int o = soff[s], w = swid[s];
@@ -633,10 +932,10 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int
         }
         if (i < nbr) {
             q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
-            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+            loc += p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2;
         }
     }
-    const double bsum = block_sum(loc, sh);
+    const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
         const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
@@ -651,17 +950,17 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int
 // Same product with the loads of U slots issued before any of them is used:
 // U column indices and 9U values, then the 3U gathers of p, then the FMAs in
 // slot order (bit-identical sums to the kernel above).  More bytes in flight
-// per lane for the latency-bound stream; MINB bounds the registers.
-template <int U, int MINB>
-__global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, const int* __restrict__ soff,
-                                                          const int* __restrict__ swid, const int* __restrict__ scol,
-                                                          const float* __restrict__ sv, const float* __restrict__ p,
-                                                          float* __restrict__ q, CGScal* S, double* part) {
-    if (S->done) return;
-    __shared__ double sh[32];
+// per lane for the latency-bound stream; the values and column ids are read
+// once per product and bypass L1.  COH: p is written inside the same kernel
+// (persistent CG), so it is read with ordinary (coherent) loads instead of
+// the non-coherent path.
+template <int U, bool COH>
+__device__ __forceinline__ float bspmv_slices(int nbr, int nslice, const int* __restrict__ soff,
+                                               const int* __restrict__ swid, const int* __restrict__ scol,
+                                               const float* __restrict__ sv, const float* p, float* q, int warp,
+                                               int nwarps) {
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    double loc = 0.0;
+    float loc = 0.f;
     for (int s = warp; s < nslice; s += nwarps) {
         const int i = s * 32 + lane;
         const int o = soff[s], w = swid[s];  // o: multiple of 32; w: warp-uniform
@@ -672,16 +971,18 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    j[u] = __ldg(scol + o + (k + u) * 32 + lane);
+                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane);
                     const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) v[u][e] = __ldg(vp + 32 * e);
+                    for (int e = 0; e < 9; ++e) v[u][e] = ld_stream(vp + 32 * e);
                 }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    const float x0 = __ldg(p + 3 * j[u]), x1 = __ldg(p + 3 * j[u] + 1), x2 = __ldg(p + 3 * j[u] + 2);
+                    const float* pj = p + 3 * j[u];
+                    const float x0 = COH ? pj[0] : __ldg(pj), x1 = COH ? pj[1] : __ldg(pj + 1),
+                                x2 = COH ? pj[2] : __ldg(pj + 2);
                     a0 += v[u][0] * x0 + v[u][1] * x1 + v[u][2] * x2;
                     a1 += v[u][3] * x0 + v[u][4] * x1 + v[u][5] * x2;
                     a2 += v[u][6] * x0 + v[u][7] * x1 + v[u][8] * x2;
@@ -690,10 +991,24 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
         }
         if (i < nbr) {
             q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
-            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+            const float* pi = p + 3 * i;
+            const float p0 = pi[0], p1 = pi[1], p2 = pi[2];
+            loc += p0 * a0 + p1 * a1 + p2 * a2;
         }
     }
-    const double bsum = block_sum(loc, sh);
+    return loc;
+}
+
+template <int U, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, const int* __restrict__ soff,
+                                                          const int* __restrict__ swid, const int* __restrict__ scol,
+                                                          const float* __restrict__ sv, const float* __restrict__ p,
+                                                          float* __restrict__ q, CGScal* S, double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
+    const float loc = bspmv_slices<U, false>(nbr, nslice, soff, swid, scol, sv, p, q, warp, nwarps);
+    const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
         const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
@@ -715,7 +1030,7 @@ __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restr
     const int lane = threadIdx.x % LPB;
     const int grp = (blockIdx.x * BS + threadIdx.x) / LPB, ngrp = gridDim.x * BS / LPB;
     const int wgrp = grp - grp % (32 / LPB);  // warp-uniform loop (full-mask shuffles below)
-    double loc = 0.0;
+    float loc = 0.f;
     for (int base = wgrp; base < nbr; base += ngrp) {
         const int i = base + (grp - wgrp);
         const bool act = i < nbr;
@@ -736,10 +1051,10 @@ __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restr
         }
         if (act && lane == 0) {
             q[3 * i] = a0; q[3 * i + 1] = a1; q[3 * i + 2] = a2;
-            loc += (double)(p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2);
+            loc += p[3 * i] * a0 + p[3 * i + 1] * a1 + p[3 * i + 2] * a2;
         }
     }
-    const double bsum = block_sum(loc, sh);
+    const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
         const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
@@ -799,8 +1114,8 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
             rz += rv[a] * z;
         }
     }
-    const double b1 = block_sum((double)rr, sh);
-    const double b2 = block_sum((double)rz, sh);
+    const double b1 = block_sum_f(rr, sh);
+    const double b2 = block_sum_f(rz, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (!last_block(&S->ticket2)) return;
     double trr, trz;
@@ -840,6 +1155,123 @@ __global__ void __launch_bounds__(NBS) k_cg_dir_b3(int nbr, const float* __restr
 
 // x = 0, r = b, p = 0, absNew = r.B^{-1}r; with restart != 0 only r = r64 and
 // beta = (r.z)_new / (r.z)_previous (reliable update)
+// Persistent mixed block CG: the iterations (direction, SpMV, update) of
+// one chunk run inside a single cooperative launch, with a grid barrier after
+// each phase.  Every block sums the partials of all blocks itself, in a fixed
+// order, so all blocks hold the same alpha, beta and decisions without a
+// ticket; the arithmetic per element is that of k_cg_dir_b3, k_bspmv_batch
+// and k_cg_update_b3n.  Vectors written inside the kernel are read with
+// ordinary loads, never the non-coherent path.  Block 0 leaves the scalar record as k_cg_update_b3n does (done 1:
+// converged, 2: iteration limit, 3: reliable update due, 0: chunk used up).
+constexpr int PERSIST_U = 8;
+constexpr int PERSIST_CHUNK = 1024;
+// below this many nodes the separate kernels are launch-bound and the
+// persistent kernel is the faster path; above it the graph path is
+constexpr int PERSIST_MAX_NBR = 32768;
+__global__ void __launch_bounds__(BS, 2) k_cg_persist_b3(int nbr, int nslice, const int* __restrict__ soff,
+                                                         const int* __restrict__ swid, const int* __restrict__ scol,
+                                                         const float* __restrict__ sv, const float* __restrict__ binv,
+                                                         float* x, float* r, float* p, float* q, CGScal* S, double* part,
+                                                         unsigned* bar, int max_iter, int chunk) {
+    __shared__ double sh[32];
+    __shared__ double bc[2];
+    if (S->done) return;
+    const int G = gridDim.x;
+    double rz = S->absNew, beta = S->beta, rz_old = S->absOld, rr = S->rr;
+    int iters = S->iters;
+    const double thr = S->threshold, trig = S->rrtrig;
+    const int tid = blockIdx.x * BS + threadIdx.x, nthr = G * BS;
+    double* ppq = part;      // [G]: p.q per block
+    double* prz = part + G;  // [2G]: r.r, r.z per block
+    int done = 0, bad = 0;
+    for (int step = 0; step < chunk && !done; ++step) {
+        // p = B^-1 r + beta p
+        const float fb = (float)beta;
+        for (int i = tid; i < nbr; i += nthr) {
+            const float r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+            const float* B = binv + 9 * (size_t)i;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                p[3 * i + a] = __ldg(B + 3 * a) * r0 + __ldg(B + 3 * a + 1) * r1 + __ldg(B + 3 * a + 2) * r2 +
+                               fb * p[3 * i + a];
+        }
+        if (!grid_sync(bar, &S->fault)) return;
+        // q = A p, p.q
+        const float loc = bspmv_slices<PERSIST_U, true>(nbr, nslice, soff, swid, scol, sv, p, q, tid >> 5, nthr >> 5);
+        const double bsum = block_sum_f(loc, sh);
+        if (threadIdx.x == 0) ppq[blockIdx.x] = bsum;
+        if (!grid_sync(bar, &S->fault)) return;
+        const double pap = reduce_parts(ppq, G, 1, 0, sh);
+        if (threadIdx.x == 0) bc[0] = pap;
+        __syncthreads();
+        const float alpha = (float)(rz / bc[0]);
+        // x += alpha p, r -= alpha q; r.r and r.z with z = B^-1 r
+        float frr = 0.f, frz = 0.f;
+        for (int i = tid; i < nbr; i += nthr) {
+            const float* B = binv + 9 * (size_t)i;
+            float b9[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) b9[k] = __ldg(B + k);
+            float rv[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const int d = 3 * i + a;
+                x[d] += alpha * p[d];
+                rv[a] = r[d] - alpha * q[d];
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                r[3 * i + a] = rv[a];
+                const float z = b9[3 * a] * rv[0] + b9[3 * a + 1] * rv[1] + b9[3 * a + 2] * rv[2];
+                frr += rv[a] * rv[a];
+                frz += rv[a] * z;
+            }
+        }
+        const double b1 = block_sum_f(frr, sh);
+        const double b2 = block_sum_f(frz, sh);
+        if (threadIdx.x == 0) { prz[2 * blockIdx.x] = b1; prz[2 * blockIdx.x + 1] = b2; }
+        if (!grid_sync(bar, &S->fault)) return;
+        double trr, trz;
+        reduce_parts2(prz, G, sh, trr, trz);
+        if (threadIdx.x == 0) { bc[0] = trr; bc[1] = trz; }
+        __syncthreads();
+        trr = bc[0];
+        trz = bc[1];
+        __syncthreads();
+        iters += 1;
+        rr = trr;
+        rz_old = rz;
+        beta = trz / rz;
+        rz = trz;
+        if (!(trr == trr) || !(trz == trz)) { bad = 1; done = 1; }
+        else if (trr < thr) done = 1;
+        else if (trr < trig) done = 3;
+        else if (iters >= max_iter) done = 2;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S->rr = rr;
+        S->iters = iters;
+        S->absOld = rz_old;
+        S->beta = beta;
+        S->absNew = rz;
+        if (bad) S->bad = 1;
+        S->done = done;
+    }
+}
+
+// blocks of the persistent kernel: as many as can be resident (at most two
+// per SM), 0 where cooperative launches are unavailable
+static int persist_grid(isl_ctx* c) {
+    if (c->persist_grid >= 0) return c->persist_grid;
+    int coop = 0, nb = 0;
+    c->persist_grid = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device) == cudaSuccess && coop &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_persist_b3, BS, 0) == cudaSuccess && nb > 0)
+        c->persist_grid = std::min(nb, 2) * c->sm_count;
+    cudaGetLastError();
+    return c->persist_grid;
+}
+
 __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
                                                    float* __restrict__ p, const float* __restrict__ binv, CGScal* S, double* part,
                                                    double tol, int restart, double trig) {
@@ -1034,9 +1466,12 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0, kDelta2);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
-    // DOF-linear vector kernels: one wave of 192-thread blocks
+    const bool want_persist = c->use_persist == 2 || (c->use_persist == 1 && nbr <= PERSIST_MAX_NBR);
+    const int pgrid = want_persist ? persist_grid(c) : 0;
     cudaGraph_t graph;
-    cudaGraphExec_t exec;
+    cudaGraphExec_t exec = nullptr;
+    if (pgrid == 0) {
+    // DOF-linear vector kernels: one wave of 192-thread blocks
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);  // one pass, no reduction
     const unsigned nbn = node_grid(c, nbr);
@@ -1051,6 +1486,18 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
         cudaGraphDestroy(graph);
         ISL_CHECK_CUDA(c, e);
     }
+    }
+    int p_nslice = (int)c->nslice, p_chunk = PERSIST_CHUNK;
+    const int* p_soff = c->dsoff.p;
+    const int* p_swid = c->dswid.p;
+    const int* p_scol = c->dscol.p;
+    const float* p_sv = c->dsval.p;
+    const float* p_binv = c->dbinv.p;
+    double* p_part = c->dpart.p;
+    unsigned* p_bar = c->dbar.p;
+    int p_nbr = nbr, p_mi = mi;
+    void* pargs[] = {&p_nbr, &p_nslice, &p_soff, &p_swid, &p_scol, &p_sv, &p_binv, &x32, &r32, &p32, &q32, &S, &p_part,
+                     &p_bar, &p_mi, &p_chunk};
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
     double rr_true = bnorm2;
@@ -1059,11 +1506,21 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     bool converged = (bnorm2 == 0.0);
     while (rc == ISL_OK && !converged) {
         if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "mixed CG made no progress"; break; }
-        if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
-        c->launches += 3 * CHUNK;
+        if (pgrid > 0) {
+            // the barrier starts from zero (a barrier that timed out leaves it mid-count)
+            if (cudaMemsetAsync(c->dbar.p, 0, 2 * sizeof(unsigned), st) != cudaSuccess ||
+                cudaLaunchCooperativeKernel((const void*)k_cg_persist_b3, dim3(pgrid), dim3(BS), pargs, 0, st) != cudaSuccess) {
+                rc = ISL_ERR_CUDA; c->err = "persistent CG launch failed"; break;
+            }
+            c->launches += 1;
+        } else {
+            if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
+            c->launches += 3 * CHUNK;
+        }
         rc = read_scal(c);
         if (rc != ISL_OK) break;
         const CGScal h = *c->hscal;
+        if (h.fault) { rc = ISL_ERR_TIMEOUT; c->err = "persistent CG: a grid barrier timed out"; break; }
         if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
         const bool at_max = h.iters >= mi;
         if (h.done || at_max) {
@@ -1080,7 +1537,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             c->launches += 1;
         }
     }
-    cudaGraphExecDestroy(exec);
+    if (exec) cudaGraphExecDestroy(exec);
     if (rc != ISL_OK) return rc;
     if (!converged && bnorm2 > 0) *nc = true;
     rc = read_scal(c);

@@ -169,6 +169,75 @@ def test_block_and_scalar_mixed_paths_agree():
     S.close()
 
 
+@pytest.mark.parametrize("n", [3, 10])
+def test_persistent_and_graph_block_cg_agree(n):
+    """The persistent cooperative CG kernel and the graph of separate kernels
+    run the same recurrences: same iteration count, solutions within 1e-8 of
+    FP64, and each path bitwise reproducible."""
+    p = W.config("c2", n=n)
+    S = gpu_problem(p)
+    assert S.get_option(A.OPT_PERSISTENT) == 1
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    out = {}
+    for persist in (2, 0):
+        S.set_option(A.OPT_PERSISTENT, persist)
+        it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        x = S.solution()
+        it2, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        assert it2 == it and np.array_equal(S.solution(), x)
+        assert rel <= 1e-12
+        assert np.linalg.norm(x - x64) <= 1e-8 * np.linalg.norm(x64)
+        out[persist] = (it, x)
+    assert abs(out[2][0] - out[0][0]) <= max(2, out[0][0] // 50)
+    S.close()
+
+
+@pytest.mark.parametrize("name,n", [("c1", 40), ("c3", 5), ("c1", 1)])
+def test_cluster_and_graph_scalar_cg_agree(name, n):
+    """Small scalar systems are solved whole by one thread-block cluster; the
+    graph of separate kernels runs the same recurrences.  Both meet the
+    tolerance and agree within 1e-8, with and without the FP64 matrix."""
+    p = W.config(name, n=n)
+    S = gpu_problem(p)
+    assert S.neq <= 65536
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    out = {}
+    for persist in (1, 0):
+        S.set_option(A.OPT_PERSISTENT, persist)
+        it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        x = S.solution()
+        S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        assert np.array_equal(S.solution(), x)
+        assert rel <= 1e-12
+        assert np.linalg.norm(x - x64) <= 1e-8 * np.linalg.norm(x64)
+        out[persist] = it
+    assert abs(out[1] - out[0]) <= max(2, out[0] // 50)
+    # FP32 tangent only: plain FP32 CG on the iterated residual
+    S.assemble(A.PREC_FP32)
+    res = {}
+    for persist in (1, 0):
+        S.set_option(A.OPT_PERSISTENT, persist)
+        it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-6)
+        res[persist] = (it, S.solution())
+        assert rel <= 1e-6
+    assert abs(res[1][0] - res[0][0]) <= max(2, res[0][0] // 20)
+    assert np.linalg.norm(res[1][1] - res[0][1]) <= 1e-5 * np.linalg.norm(res[0][1])
+    S.close()
+
+
+def test_persistent_option_range():
+    S = gpu_problem(W.config("c1", n=4))
+    with pytest.raises(A.IslError):
+        S.set_option(A.OPT_PERSISTENT, 3)
+    S.set_option(A.OPT_PERSISTENT, 2)
+    assert S.get_option(A.OPT_PERSISTENT) == 2
+    S.close()
+
+
 def test_partially_constrained_nodes_use_scalar_path():
     # x = 1 face pulls u_x only (PulledSheet-style): nodes there are partly active
     p = W.config("c2", n=3)
