@@ -9,8 +9,9 @@
 //    reference's serial element loop adds into a triplet
 //    (TripletContainer::insert, :305-352).  No atomics are used.
 //  * element kernels stage the packed upper triangle of every element matrix
-//    (entry-major: stage[u * nelem + e], coalesced across elements) and the
-//    element force vector; a gather kernel then forms CSR values and the RHS.
+//    (element-major: stage[e * nup + u], so that the contributions a CSR row
+//    gathers from one element lie together) and the element force vector
+//    (entry-major); a gather kernel then forms CSR values and the RHS.
 //  * Dirichlet columns move to the RHS per element (b -= K[:,c] g_c,
 //    base/asmb/assembleMatrix.hpp:56-130) in a kernel over the elements that
 //    own a constrained DOF.
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
     if (bad) atomicOr(A.flags, 1);
     R* SK = (R*)A.stageK;
 #pragma unroll
-    for (int u = 0; u < NUP; ++u) SK[(size_t)u * E + e] = acc[u];
+    for (int u = 0; u < NUP; ++u) SK[(size_t)e * NUP + u] = acc[u];
 #pragma unroll
     for (int s = 0; s < NF; ++s) A.stageF[(size_t)s * E + e] = fe[s];
 }
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int a = 3 * M + i, b = 3 * N + k;
-                if (a <= b) SK[(size_t)upidx(a, b, NLOC) * E + e] = acc[N][i * 3 + k];
+                if (a <= b) SK[(size_t)e * (NLOC * (NLOC + 1) / 2) + upidx(a, b, NLOC)] = acc[N][i * 3 + k];
             }
     }
     // forces of row node M: -(internal) + body
@@ -482,6 +483,90 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) A.stageF[(size_t)(3 * M + i) * E + e] = fe[i];
+}
+
+// ---------------------------------------------------------------------------
+// Linear elasticity (HyperElastic<StVenant> at u = 0) on affine hexahedra,
+// one thread per element.  With a constant Jacobian the quadrature sum of
+// k_hyper_hex8 factors:
+//   W_ik^{MN} = sum_q w_q detJ g_M,i(q) g_N,k(q)
+//             = detJ sum_ab Ji[i][a] I_ab^{MN} Ji[k][b],
+//   I_ab^{MN} = sum_q w_q dphi_q,M,a dphi_q,N,b   (the reference rule, FP64),
+//   K[3M+i][3N+k] = lam W_ik + mu (W_ki + delta_ik tr W)
+// -- the same sum in another order: about 2.9k FP64 operations per element
+// instead of 7.5k (FP64 runs at 2 operations per clock per SM here).
+struct AffineHexTab {
+    double I[36][9];  // (M <= N) pairs in row order, [a][b]
+    double dN0[8][3];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_elast_affine_hex8(const ElemArgs A, const AffineHexTab T) {
+    constexpr int NLOC = 24;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int E = A.nelem;
+    if (e >= E) return;
+    double X[8][3];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int node = A.conn[i * E + e];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) X[i][d] = A.X[(size_t)node * 3 + d];
+    }
+    double Ji[3][3];
+    const double detJ = jac<8, 3>(X, T.dN0, Ji);
+    if (!(detJ > 0.0)) atomicOr(A.flags, 1);
+    const double lam = A.coef[e], mu = A.coef[E + e];
+    R* SK = (R*)A.stageK;
+    int pr = 0;
+#pragma unroll 1
+    for (int M = 0; M < 8; ++M) {
+#pragma unroll 1
+        for (int N = M; N < 8; ++N, ++pr) {
+            const double* I = T.I[pr];
+            double T1[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) T1[i][b] = Ji[i][0] * I[b] + Ji[i][1] * I[3 + b] + Ji[i][2] * I[6 + b];
+            double W[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) W[i][k] = detJ * (T1[i][0] * Ji[k][0] + T1[i][1] * Ji[k][1] + T1[i][2] * Ji[k][2]);
+            const double tr = W[0][0] + W[1][1] + W[2][2];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int a = 3 * M + i, b = 3 * N + k;
+                    if (a <= b) SK[(size_t)e * (NLOC * (NLOC + 1) / 2) + upidx(a, b, NLOC)] = R(lam * W[i][k] + mu * (W[k][i] + (i == k ? tr : 0.0)));
+                }
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NLOC; ++f) A.stageF[(size_t)f * E + e] = 0.0;
+}
+
+// every hexahedron a parallelepiped (the test of affine<ISL_HEX> on the host)
+static bool mesh_is_affine_hex(const isl_ctx* c) {
+    const int64_t E = c->nelem;
+    for (int64_t e = 0; e < E; ++e) {
+        const int64_t* v = &c->hconn[(size_t)e * 8];
+        double dev = 0.0, scale = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double x[8];
+            for (int i = 0; i < 8; ++i) x[i] = c->hX[(size_t)v[i] * 3 + d];
+            const double xy = x[0] - x[1] + x[2] - x[3];
+            const double xz = x[0] - x[1] - x[4] + x[5];
+            const double yz = x[0] - x[3] - x[4] + x[7];
+            const double xyz = -x[0] + x[1] - x[2] + x[3] + x[4] - x[5] + x[6] - x[7];
+            dev = std::max(dev, std::max(std::max(std::fabs(xy), std::fabs(xz)), std::max(std::fabs(yz), std::fabs(xyz))));
+            scale = std::max(scale, std::fabs(x[1] - x[0]) + std::fabs(x[3] - x[0]) + std::fabs(x[4] - x[0]));
+        }
+        if (!(dev <= 1e-13 * scale)) return false;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -570,7 +655,7 @@ __global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun,
         for (int b = 0; b < nloc; ++b) {
             if (act[b] || g[b] == 0.0) continue;
             const int uidx = a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc);
-            s += (double)stageK[(size_t)uidx * nelem + e] * g[b];
+            s += (double)stageK[(size_t)e * (nloc * (nloc + 1) / 2) + uidx] * g[b];
         }
         stageF[(size_t)a * nelem + e] -= s;
     }
@@ -617,7 +702,7 @@ __global__ void k_gen_pairs(int nelem, int ncomp, int nloc, const int32_t* edof,
         const size_t idx = ((size_t)e * nloc + a) * nloc + b;  // element-major: stable sort keeps element order
         if (qa >= 0 && qb >= 0) {
             keys[idx] = ((uint64_t)(uint32_t)qa << 32) | (uint32_t)qb;
-            vals[idx] = (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc)) * nelem + e;
+            vals[idx] = e * (nloc * (nloc + 1) / 2) + (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc));
             ++cnt;
         } else {
             keys[idx] = ~0ull;
@@ -839,6 +924,26 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
     if (!make_host_tables(ISL_HEX, 1, c->qdeg, h) || h.nq != 8) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: 2x2x2 quadrature required");
     Tab<3, 8, 8, 8> T;
     fill_tab<ISL_HEX, 1, 8>(T, h);
+    if (c->mesh_affine < 0) c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
+    if (!A.general && !A.fnodal && c->mesh_affine == 1) {
+        // small strain on parallelepipeds: reference integrals times the constant Jacobian
+        AffineHexTab AT;
+        int pr = 0;
+        for (int M = 0; M < 8; ++M)
+            for (int N = M; N < 8; ++N, ++pr)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        double s = 0.0;
+                        for (int q = 0; q < 8; ++q) s += T.w[q] * T.dphi[q][M][a] * T.dphi[q][N][b];
+                        AT.I[pr][a * 3 + b] = s;
+                    }
+        for (int i = 0; i < 8; ++i)
+            for (int d = 0; d < 3; ++d) AT.dN0[i][d] = T.dN[0][i][d];
+        k_elast_affine_hex8<R><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, AT);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+        c->launches += 1;
+        return ISL_OK;
+    }
     constexpr int EPB = 32;
     const size_t base = (size_t)8 * 3 * EPB * 8 * 2;
     size_t smem = base + (A.general ? (size_t)8 * 8 * 3 * EPB * 8 : 0) + (size_t)8 * 8 * 3 * EPB * sizeof(R) +

@@ -409,7 +409,7 @@ static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, con
     c->ninst = n_inst;
     c->inst_node_off.assign(node_off, node_off + n_inst + 1);
     c->inst_elem_off.assign(elem_off, elem_off + n_inst + 1);
-    c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false;
+    c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false; c->mesh_affine = -1;
     if (c->device < 0) return ISL_OK;
     cudaSetDevice(c->device);
     std::vector<int32_t> soa((size_t)n_elem * c->ngeom);
