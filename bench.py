@@ -376,6 +376,20 @@ def run_batch(args, rank, world, local, pg):
 
     for _ in range(args.warmup):
         step(True)
+    if args.profile:
+        # one mixed step inside the profiler range (ncu --profile-from-start off)
+        import ctypes
+        cudart = ctypes.CDLL("libcudart.so.13")  # already loaded by libisl_gpu.so
+        for S in systems:
+            S.sync()
+        cudart.cudaProfilerStart()
+        step(True)
+        for S in systems:
+            S.sync()
+        cudart.cudaProfilerStop()
+        for S in systems:
+            S.close()
+        return
     # accuracy: mixed vs FP64 (tight) per group
     errs = []
     for S in systems:

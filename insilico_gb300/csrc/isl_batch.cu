@@ -119,17 +119,47 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
     const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
     const int wgrp = grp - grp % (32 / LPR);  // warp-uniform loop (full-mask shuffles)
     TX loc = TX(0);  // in the vectors' precision; warp sums are added in FP64
-    for (int base = r0 + wgrp; base < r1; base += BBS / LPR) {
-        const int row = base + (grp - wgrp);
-        const bool act = row < r1;
-        TX acc = TX(0);
-        if (act)
-            for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += LPR) acc += (TX)__ldg(val + j) * __ldg(p + __ldg(colind + j));
+    // RU rows per lane group at a time: their index, value and p loads are
+    // issued together, so a block keeps RU times more rows in flight (the
+    // sums of each row keep the order of a one-row loop)
+    constexpr int RU = 4;
+    const int stride = BBS / LPR;
+    for (int base = r0 + wgrp; base < r1; base += RU * stride) {
+        int j[RU], e[RU];
+        TX acc[RU];
 #pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
-        if (act && lane == 0) {
-            q[row] = acc;
-            loc += p[row] * acc;
+        for (int u = 0; u < RU; ++u) {
+            const int row = base + (grp - wgrp) + u * stride;
+            const bool act = row < r1;
+            j[u] = act ? __ldg(rowptr + row) + lane : 0;
+            e[u] = act ? __ldg(rowptr + row + 1) : 0;
+            acc[u] = TX(0);
+        }
+        for (;;) {
+            int cj[RU];
+            TV vv[RU];
+#pragma unroll
+            for (int u = 0; u < RU; ++u)
+                if (j[u] < e[u]) { cj[u] = __ldg(colind + j[u]); vv[u] = __ldg(val + j[u]); }
+            bool more = false;
+#pragma unroll
+            for (int u = 0; u < RU; ++u)
+                if (j[u] < e[u]) {
+                    acc[u] += (TX)vv[u] * __ldg(p + cj[u]);
+                    j[u] += LPR;
+                    more |= j[u] < e[u];
+                }
+            if (!more) break;
+        }
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+#pragma unroll
+            for (int o = LPR / 2; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o, LPR);
+            const int row = base + (grp - wgrp) + u * stride;
+            if (row < r1 && lane == 0) {
+                q[row] = acc[u];
+                loc += p[row] * acc[u];
+            }
         }
     }
     const double s1 = block_sum_t(loc, sh);
