@@ -274,3 +274,27 @@ def test_empty_system_every_dof_constrained():
     S.distribute()
     assert np.all(S.values() == 0.0)
     S.close()
+
+
+@pytest.mark.parametrize("material", ["stvenant", "neohooke"])
+def test_hex8_non_affine_mesh_matches_oracle(material):
+    """Distorted hexahedra (no element a parallelepiped) take the quadrature-
+    loop kernel; parallelepipeds take the closed-form one.  Both match the
+    oracle: pattern bit-exact, entries and RHS to 1e-12, solution to 1e-8."""
+    p = W.config("c2", n=4)
+    p.material = material
+    g = np.random.default_rng(11)
+    interior = np.all((p.X > 1e-9) & (p.X < 1 - 1e-9), axis=1)
+    p.X = p.X + 0.08 / 4 * g.uniform(-1.0, 1.0, p.X.shape) * interior[:, None]
+    S = gpu_problem(p)
+    P, (rp, ci, v, b) = oracle_problem(p)
+    S.assemble(A.PREC_MIXED)
+    grp, gci, gv = S.csr()
+    np.testing.assert_array_equal(grp, rp)
+    np.testing.assert_array_equal(gci, ci)
+    assert csr_entry_err(rp, ci, gv, v) <= 1e-12
+    assert np.max(np.abs(S.rhs() - b)) <= 1e-12 * np.max(np.abs(b))
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    xo, _, _ = O.cg(rp, ci, v, b, tol=1e-13)
+    assert np.linalg.norm(S.solution() - xo) <= 1e-8 * np.linalg.norm(xo)
+    S.close()
