@@ -821,6 +821,9 @@ int pattern_build(isl_ctx* c) {
         bool ok = rp[0] == 0 && rp[c->neq] == nnz;
         for (int64_t i = 0; ok && i < c->neq; ++i) ok = rp[i] >= 0 && rp[i] < rp[i + 1];
         if (!ok) ISL_FAIL(c, ISL_ERR_ARG, "pattern build: inconsistent row pointers");
+        // kept for sizing the one-cluster solve of small systems
+        c->hrp_small.clear();
+        if (c->neq <= 65536) c->hrp_small = rp;
         const int brc = block_pattern(c, rp);
         if (brc != ISL_OK) return brc;
     }

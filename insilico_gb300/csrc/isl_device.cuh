@@ -103,6 +103,19 @@ __device__ inline bool last_of(unsigned int* ticket, unsigned int count) {
     return amLastOf;
 }
 
+// a / b computed once by thread 0 and read by every thread of the block: an
+// FP64 division is a sequence of FP64 operations, which run at 1/64 of the
+// FP32 rate, so a block-wide division costs microseconds.  All threads of the
+// block must call it (it holds two block barriers).
+__device__ inline double block_div(double a, double b) {
+    __shared__ double bd;
+    if (threadIdx.x == 0) bd = a / b;
+    __syncthreads();
+    const double v = bd;
+    __syncthreads();
+    return v;
+}
+
 // Block sum of FP32 values: each warp adds its lanes in FP32 (the precision of
 // the values), the warp sums are added in FP64 by warp 0.  FP64 arithmetic
 // runs at 1/64 of the FP32 rate on this GPU, so the FP64 part is kept to one

@@ -175,6 +175,7 @@ struct isl_ctx {
     // when every DOF object has all three components active or all constrained
     bool blocked = false;
     bool use_block = true;
+    std::vector<int32_t> hrp_small;  // host row pointers of a system small enough for the one-cluster solve
     int mesh_affine = -1;        // every element a parallelepiped / parallelogram (-1: not yet checked)
     int use_persist = 1;         // one-launch CG kernels: 0 never, 1 for small systems, 2 always where supported
     int cluster_size = -1;       // CTAs of the small-system cluster solve (-1: not yet probed, 0: unavailable)

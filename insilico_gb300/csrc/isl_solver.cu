@@ -485,6 +485,96 @@ __device__ inline void cluster_sum2(T a, T b, double (*red)[2], int& slot, doubl
     slot = (slot + 1) & 3;
 }
 
+// Scalar state of the one-cluster CG.  Thread 0 of each CTA holds it (every
+// CTA computes the same values from the same sums); the other threads get
+// alpha and beta in FP32 and a control code through shared memory, so the
+// FP64 divisions and tests run once per CTA instead of once per thread.
+struct ClusterScalars {
+    double rz, rz_old, beta, rr, thr, trig, rr_true;
+    int iters, max_iter, exact64, bad;
+};
+enum { CTL_GO = 0, CTL_DONE = 1, CTL_MAX = 2, CTL_UPDATE = 3, CTL_BAD = 4 };
+
+__device__ inline float cs_alpha(ClusterScalars& s, double pap, float* sf) {
+    if (threadIdx.x == 0) sf[0] = (float)(s.rz / pap);
+    __syncthreads();
+    return sf[0];  // rewritten only after later barriers
+}
+
+// after the (r.r, r.z) sums of an iteration; beta for the next direction in sf[1]
+__device__ inline int cs_update(ClusterScalars& s, double trr, double trz, float* sf, int* si) {
+    if (threadIdx.x == 0) {
+        s.iters += 1;
+        s.rr = trr;
+        s.rz_old = s.rz;
+        s.beta = trz / s.rz;
+        s.rz = trz;
+        int ctl = CTL_GO;
+        if (!(trr == trr) || !(trz == trz)) { s.bad = 1; ctl = CTL_BAD; }
+        else if (!s.exact64) {
+            // FP32 CG on the iterated residual (inexact Newton steps)
+            if (trr < s.thr) ctl = CTL_DONE;
+            else if (s.iters >= s.max_iter) ctl = CTL_MAX;
+            if (ctl != CTL_GO) s.rr_true = trr;
+        } else if (trr < s.thr || trr < s.trig || s.iters >= s.max_iter) {
+            ctl = CTL_UPDATE;
+        }
+        sf[1] = (float)s.beta;
+        si[0] = ctl;
+    }
+    __syncthreads();
+    return si[0];
+}
+
+// after the FP64 residual of a reliable update: converged, iteration limit,
+// breakdown, or a restart from the true residual with the same direction
+__device__ inline int cs_residual(ClusterScalars& s, double rr_true, double rr_restart, double rz_restart, float* sf, int* si) {
+    if (threadIdx.x == 0) {
+        s.rr_true = rr_true;
+        int ctl = CTL_GO;
+        if (!(rr_true == rr_true)) { s.bad = 1; ctl = CTL_BAD; }
+        else if (rr_true <= s.thr) ctl = CTL_DONE;
+        else if (s.iters >= s.max_iter) ctl = CTL_MAX;
+        else {
+            s.rr = rr_restart;
+            s.beta = rz_restart / s.rz_old;
+            s.rz = rz_restart;
+            s.trig = kDelta2 * rr_true;
+            sf[1] = (float)s.beta;
+        }
+        si[0] = ctl;
+    }
+    __syncthreads();
+    return si[0];
+}
+
+__device__ inline ClusterScalars cs_load(const CGScal* S, int max_iter, int exact64) {
+    ClusterScalars s;
+    s.rz = S->absNew;
+    s.rz_old = S->absOld;
+    s.beta = S->beta;
+    s.rr = S->rr;
+    s.thr = S->threshold;
+    s.trig = S->rrtrig;
+    s.rr_true = S->rhsNorm2;
+    s.iters = S->iters;
+    s.max_iter = max_iter;
+    s.exact64 = exact64;
+    s.bad = 0;
+    return s;
+}
+
+__device__ inline void cs_store(const ClusterScalars& s, int done, CGScal* S) {
+    S->rr = s.rr;
+    S->rz = s.rr_true;
+    S->iters = s.iters;
+    S->absOld = s.rz_old;
+    S->absNew = s.rz;
+    S->beta = s.beta;
+    if (s.bad) S->bad = 1;
+    S->done = done;
+}
+
 template <int LPR>
 __global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
                                                          const float* __restrict__ val32, const double* __restrict__ val64,
@@ -500,14 +590,16 @@ __global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __res
     const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR, ngrp = CL_BS / LPR;
     const int wgrp = grp - grp % (32 / LPR);  // first row group of this warp: row loops stay warp-uniform
     int slot = 0;
-    double rz = S->absNew, rz_old = S->absOld, beta = S->beta, rr = S->rr;
-    const double thr = S->threshold;
-    double trig = S->rrtrig, rr_true = S->rhsNorm2;
-    int iters = S->iters, done = S->done, bad = 0;
+    __shared__ float sf[2];
+    __shared__ int si[1];
+    ClusterScalars sc = cs_load(S, max_iter, exact64);
+    int done = S->done;
+    if (threadIdx.x == 0) sf[1] = (float)sc.beta;
+    __syncthreads();
     double t0, t1;
     while (!done) {
         // p = D^-1 r + beta p
-        const float fb = (float)beta;
+        const float fb = sf[1];
         for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) p32[i] = dinv[i] * r32[i] + fb * p32[i];
         cl.sync();
         // q = A p, p.q
@@ -522,7 +614,7 @@ __global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __res
             }
         }
         cluster_sum2(loc, 0.f, red, slot, sh, bc, t0, t1);
-        const float alpha = (float)(rz / t0);
+        const float alpha = cs_alpha(sc, t0, sf);
         // x += alpha p, r -= alpha q; r.r, r.z
         float frr = 0.f, frz = 0.f;
         for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) {
@@ -533,28 +625,20 @@ __global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __res
             frz += ri * (dinv[i] * ri);
         }
         cluster_sum2(frr, frz, red, slot, sh, bc, t0, t1);
-        iters += 1;
-        rr = t0;
-        rz_old = rz;
-        beta = t1 / rz;
-        rz = t1;
-        if (!(t0 == t0) || !(t1 == t1)) { bad = 1; done = 1; break; }
-        const bool conv_it = t0 < thr;
+        const int ctl = cs_update(sc, t0, t1, sf, si);
+        if (ctl == CTL_BAD) { done = 1; break; }
         if (!exact64) {
-            // FP32 CG on the iterated residual (inexact Newton steps)
-            if (conv_it) done = 1;
-            else if (iters >= max_iter) done = 2;
-            if (done) {
-                rr_true = t0;
+            if (ctl != CTL_GO) {
                 for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) { x64[i] += (double)x32[i]; x32[i] = 0.f; }
+                done = ctl;
             }
             continue;
         }
-        if (conv_it || t0 < trig || iters >= max_iter) {
+        if (ctl == CTL_UPDATE) {
             // reliable update: fold the FP32 increment, true residual in FP64
             for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) { x64[i] += (double)x32[i]; x32[i] = 0.f; }
             cl.sync();
-            double lt = 0.0;
+            double lt = 0.0, lrr = 0.0, lrz = 0.0;
             for (int base = r0 + wgrp; base < r1; base += ngrp) {
                 const int row = base + (grp - wgrp);
                 const bool act = row < r1;
@@ -563,40 +647,172 @@ __global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster(int n, const int* __res
                     const double ri = b[row] - ax;
                     r64[row] = ri;
                     lt += ri * ri;
+                    // the restart residual (FP32) and its sums, from the same pass
+                    const float rf = (float)ri;
+                    r32[row] = rf;
+                    lrr += (double)rf * (double)rf;
+                    lrz += (double)rf * (double)(dinv[row] * rf);
                 }
             }
-            cluster_sum2(lt, 0.0, red, slot, sh, bc, t0, t1);
-            rr_true = t0;
-            if (!(rr_true == rr_true)) { bad = 1; done = 1; break; }
-            if (rr_true <= thr) { done = 1; break; }
-            if (iters >= max_iter) { done = 2; break; }
-            // restart from the true residual, keeping the search direction
-            double lrr = 0.0, lrz = 0.0;
-            for (int i = r0 + (int)threadIdx.x; i < r1; i += CL_BS) {
-                const float ri = (float)r64[i];
-                r32[i] = ri;
-                lrr += (double)ri * (double)ri;
-                lrz += (double)ri * (double)(dinv[i] * ri);
-            }
-            cluster_sum2(lrr, lrz, red, slot, sh, bc, t0, t1);
-            rr = t0;
-            beta = t1 / rz_old;
-            rz = t1;
-            trig = kDelta2 * rr_true;
+            cluster_sum2(lt, lrr, red, slot, sh, bc, t0, t1);
+            const double rr_true = t0, rr_restart = t1;
+            cluster_sum2(lrz, 0.0, red, slot, sh, bc, t0, t1);
+            const int c2 = cs_residual(sc, rr_true, rr_restart, t0, sf, si);
+            if (c2 != CTL_GO) { done = c2 == CTL_MAX ? 2 : 1; break; }
         }
     }
-    if (rank == 0 && threadIdx.x == 0) {
-        S->rr = rr;
-        S->rz = rr_true;
-        S->iters = iters;
-        S->absOld = rz_old;
-        S->absNew = rz;
-        S->beta = beta;
-        if (bad) S->bad = 1;
-        S->done = done;
-    }
+    if (rank == 0 && threadIdx.x == 0) cs_store(sc, done, S);
     // no CTA may leave while a peer can still read its shared memory
     cl.sync();
+}
+
+// The same solve with the cluster's rows kept on chip: each CTA copies its
+// slice of the FP32 CSR matrix and of x, r, p, q and D^-1 into shared memory
+// once; the SpMV reads the p entries of other CTAs through distributed shared
+// memory (owner rank = column / chunk).  Only the FP64 reliable updates read
+// the FP64 matrix and the FP64 iterate from global memory.  Used when a CTA's
+// slice fits in shared memory.
+template <int LPR>
+__global__ void __launch_bounds__(CL_BS, 1) k_cg_cluster_smem(int n, int chunk, const int* __restrict__ rowptr,
+                                                              const int* __restrict__ colind, const float* __restrict__ val32,
+                                                              const double* __restrict__ val64, const double* __restrict__ b,
+                                                              const float* __restrict__ dinvg, double* x64, CGScal* S,
+                                                              int max_iter, int exact64, int max_nnz) {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double sh[2 * (CL_BS / 32)];
+    __shared__ double red[4][2];
+    __shared__ double bc[2];
+    const int rank = (int)cl.block_rank();
+    const int r0 = min(n, rank * chunk), r1 = min(n, r0 + chunk), nloc = r1 - r0;
+    int* rp = (int*)smem;                // [chunk + 1]
+    int* cs = rp + (chunk + 1);          // [max_nnz]
+    float* vs = (float*)(cs + max_nnz);  // [max_nnz]
+    float* xs = vs + max_nnz;            // [chunk] each: x, r, p, q, D^-1
+    float* rs = xs + chunk;
+    float* ps = rs + chunk;
+    float* qs = ps + chunk;
+    float* ds = qs + chunk;
+    const int base = rowptr[r0];
+    const int nnzl = rowptr[r1] - base;
+    for (int i = (int)threadIdx.x; i <= nloc; i += CL_BS) rp[i] = rowptr[r0 + i] - base;
+    for (int k = (int)threadIdx.x; k < nnzl; k += CL_BS) { cs[k] = colind[base + k]; vs[k] = val32[base + k]; }
+    for (int i = (int)threadIdx.x; i < nloc; i += CL_BS) {
+        xs[i] = 0.f;
+        rs[i] = (float)b[r0 + i];
+        ps[i] = 0.f;
+        ds[i] = dinvg[r0 + i];
+    }
+    const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR, ngrp = CL_BS / LPR;
+    const int wgrp = grp - grp % (32 / LPR);  // row loops stay warp-uniform
+    int slot = 0;
+    __shared__ float sf[2];
+    __shared__ int si[1];
+    ClusterScalars sc = cs_load(S, max_iter, exact64);
+    int done = S->done;
+    if (threadIdx.x == 0) sf[1] = (float)sc.beta;
+    double t0, t1;
+    cl.sync();
+    while (!done) {
+        // p = D^-1 r + beta p
+        const float fb = sf[1];
+        for (int i = (int)threadIdx.x; i < nloc; i += CL_BS) ps[i] = ds[i] * rs[i] + fb * ps[i];
+        cl.sync();
+        // q = A p (p of other CTAs through distributed shared memory), p.q
+        float loc = 0.f;
+        for (int bi = wgrp; bi < nloc; bi += ngrp) {
+            const int row = bi + (grp - wgrp);
+            const bool act = row < nloc;
+            float acc = 0.f;
+            if (act)
+                for (int k = rp[row] + lane; k < rp[row + 1]; k += LPR) {
+                    const int c = cs[k], owner = c / chunk, li = c - owner * chunk;
+                    const float pv = owner == rank ? ps[li] : *cl.map_shared_rank(ps + li, owner);
+                    acc += vs[k] * pv;
+                }
+#pragma unroll
+            for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+            if (act && lane == 0) {
+                qs[row] = acc;
+                loc += ps[row] * acc;
+            }
+        }
+        cluster_sum2(loc, 0.f, red, slot, sh, bc, t0, t1);
+        const float alpha = cs_alpha(sc, t0, sf);
+        // x += alpha p, r -= alpha q; r.r, r.z
+        float frr = 0.f, frz = 0.f;
+        for (int i = (int)threadIdx.x; i < nloc; i += CL_BS) {
+            xs[i] += alpha * ps[i];
+            const float ri = rs[i] - alpha * qs[i];
+            rs[i] = ri;
+            frr += ri * ri;
+            frz += ri * (ds[i] * ri);
+        }
+        cluster_sum2(frr, frz, red, slot, sh, bc, t0, t1);
+        const int ctl = cs_update(sc, t0, t1, sf, si);
+        if (ctl == CTL_BAD) { done = 1; break; }
+        if (!exact64) {
+            if (ctl != CTL_GO) {
+                for (int i = (int)threadIdx.x; i < nloc; i += CL_BS) { x64[r0 + i] += (double)xs[i]; xs[i] = 0.f; }
+                done = ctl;
+            }
+            continue;
+        }
+        if (ctl == CTL_UPDATE) {
+            // reliable update: fold, true residual in FP64 from global memory;
+            // the rounded residual and its sums for a restart come from the same pass
+            for (int i = (int)threadIdx.x; i < nloc; i += CL_BS) { x64[r0 + i] += (double)xs[i]; xs[i] = 0.f; }
+            cl.sync();
+            double lt = 0.0, lrr = 0.0, lrz = 0.0;
+            for (int bi = wgrp; bi < nloc; bi += ngrp) {
+                const int row = bi + (grp - wgrp);
+                const bool act = row < nloc;
+                const double ax = row_dot_c<double, double, LPR>(r0 + row, act, rowptr, colind, val64, x64, lane);
+                if (act && lane == 0) {
+                    const double ri = b[r0 + row] - ax;
+                    lt += ri * ri;
+                    const float rf = (float)ri;
+                    rs[row] = rf;
+                    lrr += (double)rf * (double)rf;
+                    lrz += (double)rf * (double)(ds[row] * rf);
+                }
+            }
+            cluster_sum2(lt, lrr, red, slot, sh, bc, t0, t1);
+            const double rr_true = t0, rr_restart = t1;
+            cluster_sum2(lrz, 0.0, red, slot, sh, bc, t0, t1);
+            const int c2 = cs_residual(sc, rr_true, rr_restart, t0, sf, si);
+            if (c2 != CTL_GO) { done = c2 == CTL_MAX ? 2 : 1; break; }
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) cs_store(sc, done, S);
+    // no CTA may leave while a peer can still read its shared memory
+    cl.sync();
+}
+
+template <int LPR>
+static cudaError_t launch_cluster_smem(int ncta, size_t smem, cudaStream_t st, int n, int chunk, const int* rp, const int* ci,
+                                       const float* v32, const double* v64, const double* b, const float* dinv, double* x64,
+                                       CGScal* S, int mi, int exact64, int max_nnz) {
+    cudaError_t e = cudaFuncSetAttribute(k_cg_cluster_smem<LPR>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cg_cluster_smem<LPR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ncta);
+    cfg.blockDim = dim3(CL_BS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ncta;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&nclusters, k_cg_cluster_smem<LPR>, &cfg);
+    if (e != cudaSuccess) return e;
+    if (nclusters < 1) return cudaErrorInvalidConfiguration;
+    return cudaLaunchKernelEx(&cfg, k_cg_cluster_smem<LPR>, n, chunk, rp, ci, v32, v64, b, dinv, x64, S, mi, exact64, max_nnz);
 }
 
 template <int LPR>
@@ -677,7 +893,30 @@ static int solve_mixed_cluster(isl_ctx* c, int ncta, double tol, int64_t max_ite
     while (lpr < 32 && lpr < avg / 2) lpr *= 2;
     const int rows_per_cta = (n + ncta - 1) / ncta;
     while (lpr > 2 && (long long)rows_per_cta * lpr > CL_BS) lpr /= 2;
-    cudaError_t e;
+    cudaError_t e = cudaErrorInvalidConfiguration;
+    // on-chip variant when each CTA's slice fits in shared memory
+    size_t smem = 0;
+    int max_nnz = 0;
+    const int chunk = rows_per_cta;
+    if ((int64_t)c->hrp_small.size() == (int64_t)n + 1) {
+        for (int r = 0; r < ncta; ++r) {
+            const int a0 = std::min(n, r * chunk), a1 = std::min(n, a0 + chunk);
+            max_nnz = std::max(max_nnz, c->hrp_small[a1] - c->hrp_small[a0]);
+        }
+        smem = (size_t)4 * (chunk + 1) + (size_t)8 * max_nnz + (size_t)20 * chunk;
+    }
+    const bool onchip = smem > 0 && smem <= (size_t)200 * 1024;
+    if (onchip) {
+        switch (lpr) {
+            case 2: e = launch_cluster_smem<2>(ncta, smem, st, n, chunk, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x64, S, mi, exact64, max_nnz); break;
+            case 4: e = launch_cluster_smem<4>(ncta, smem, st, n, chunk, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x64, S, mi, exact64, max_nnz); break;
+            case 8: e = launch_cluster_smem<8>(ncta, smem, st, n, chunk, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x64, S, mi, exact64, max_nnz); break;
+            case 16: e = launch_cluster_smem<16>(ncta, smem, st, n, chunk, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x64, S, mi, exact64, max_nnz); break;
+            default: e = launch_cluster_smem<32>(ncta, smem, st, n, chunk, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x64, S, mi, exact64, max_nnz); break;
+        }
+        if (e != cudaSuccess) cudaGetLastError();  // not launchable here: the global-memory variant runs
+    }
+    if (e != cudaSuccess)
     switch (lpr) {
         case 2: e = launch_cluster<2>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
         case 4: e = launch_cluster<4>(ncta, st, n, c->drowptr.p, c->dcolind.p, c->dval32.p, c->dval64.p, c->drhs.p, d32, x32, r32, p32, q32, x64, r64, S, mi, exact64); break;
@@ -1204,7 +1443,7 @@ __global__ void __launch_bounds__(BS, 2) k_cg_persist_b3(int nbr, int nslice, co
         const double pap = reduce_parts(ppq, G, 1, 0, sh);
         if (threadIdx.x == 0) bc[0] = pap;
         __syncthreads();
-        const float alpha = (float)(rz / bc[0]);
+        const float alpha = (float)block_div(rz, bc[0]);
         // x += alpha p, r -= alpha q; r.r and r.z with z = B^-1 r
         float frr = 0.f, frz = 0.f;
         for (int i = tid; i < nbr; i += nthr) {
@@ -1241,7 +1480,7 @@ __global__ void __launch_bounds__(BS, 2) k_cg_persist_b3(int nbr, int nslice, co
         iters += 1;
         rr = trr;
         rz_old = rz;
-        beta = trz / rz;
+        beta = block_div(trz, rz);
         rz = trz;
         if (!(trr == trr) || !(trz == trz)) { bad = 1; done = 1; }
         else if (trr < thr) done = 1;
