@@ -190,8 +190,12 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * a scalar system of at most 65,536 equations is solved whole, FP64 reliable
  * updates included, by one thread-block cluster; a node-blocked system of at
  * most 32,768 nodes runs its iterations in a persistent cooperative kernel.
- * 2: the persistent block kernel at every size. */
-enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4 };
+ * 2: the persistent block kernel at every size.  ISL_OPT_BARRIER_TEST (test
+ * hook, write-only, one-shot): the next persistent launch starts with its grid
+ * barrier armed so that it cannot complete; its bounded wait runs out and the
+ * solve returns ISL_ERR_TIMEOUT with the context still usable. */
+enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
+       ISL_OPT_BARRIER_TEST = 5 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 

@@ -956,6 +956,7 @@ int isl_launch_count(isl_ctx* c, int64_t* n) {
 int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (!c) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { c->use_block = value != 0; return ISL_OK; }
+    if (key == ISL_OPT_BARRIER_TEST) { c->barrier_test = value != 0; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) {
         if (value < 0 || value > 2) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_PERSISTENT takes 0, 1 or 2");
         c->use_persist = (int)value;

@@ -179,7 +179,8 @@ struct isl_ctx {
     int mesh_affine = -1;        // every element a parallelepiped / parallelogram (-1: not yet checked)
     int use_persist = 1;         // one-launch CG kernels: 0 never, 1 for small systems, 2 always where supported
     int cluster_size = -1;       // CTAs of the small-system cluster solve (-1: not yet probed, 0: unavailable)
-    int persist_grid = -1;       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)
+    int persist_grid = -1;
+    bool barrier_test = false;   // test hook: the next persistent launch finds its grid barrier pre-armed (never completes)       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)
     isl::DBuf<unsigned int> dbar; // grid barrier of the persistent kernel: arrivals, generation
     int64_t nbr = 0, nblk = 0;
     isl::DBuf<int32_t> dbptr, dbcol, dbrow;

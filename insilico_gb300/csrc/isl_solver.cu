@@ -1746,8 +1746,14 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     while (rc == ISL_OK && !converged) {
         if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "mixed CG made no progress"; break; }
         if (pgrid > 0) {
-            // the barrier starts from zero (a barrier that timed out leaves it mid-count)
-            if (cudaMemsetAsync(c->dbar.p, 0, 2 * sizeof(unsigned), st) != cudaSuccess ||
+            // the barrier starts from zero (a barrier that timed out leaves it
+            // mid-count); the test hook arms it with an arrival count that the
+            // grid never reaches
+            const unsigned armed[2] = {0x40000000u, 0u};
+            const bool arm = c->barrier_test;
+            c->barrier_test = false;
+            if ((arm ? cudaMemcpyAsync(c->dbar.p, armed, sizeof(armed), cudaMemcpyHostToDevice, st)
+                     : cudaMemsetAsync(c->dbar.p, 0, 2 * sizeof(unsigned), st)) != cudaSuccess ||
                 cudaLaunchCooperativeKernel((const void*)k_cg_persist_b3, dim3(pgrid), dim3(BS), pargs, 0, st) != cudaSuccess) {
                 rc = ISL_ERR_CUDA; c->err = "persistent CG launch failed"; break;
             }

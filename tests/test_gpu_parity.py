@@ -298,3 +298,24 @@ def test_hex8_non_affine_mesh_matches_oracle(material):
     xo, _, _ = O.cg(rp, ci, v, b, tol=1e-13)
     assert np.linalg.norm(S.solution() - xo) <= 1e-8 * np.linalg.norm(xo)
     S.close()
+
+
+def test_persistent_barrier_timeout_reports_status():
+    """Failure path of the persistent kernel's grid barrier, without a GPU
+    fault: the test hook arms the barrier so that it cannot complete, the
+    bounded wait runs out, the solve returns ISL_ERR_TIMEOUT, and the context
+    then solves normally."""
+    p = W.config("c2", n=3)
+    S = gpu_problem(p)
+    S.assemble(A.PREC_MIXED)
+    S.set_option(A.OPT_PERSISTENT, 2)
+    it_ok, _, st = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-10)
+    assert st == A.ISL_OK
+    x_ok = S.solution()
+    S.set_option(A.OPT_BARRIER_TEST, 1)
+    _, _, st = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-10, check=False)
+    assert st == A.ISL_ERR_TIMEOUT
+    it, _, st = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-10)
+    assert st == A.ISL_OK and it == it_ok
+    assert np.array_equal(S.solution(), x_ok)
+    S.close()
