@@ -124,6 +124,16 @@ WORKLOAD_DESC = {
 }
 
 
+def max_over_ranks(value, pg):
+    """The largest value over all ranks (replicas: the slowest rank's time)."""
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def spmv_bytes(nnz, n, v):
     """Algorithmic bytes of one CSR SpMV: nnz (v + 4) + 4 (N + 1) + 2 N v."""
     return nnz * (v + 4) + 4 * (n + 1) + 2 * n * v
@@ -555,11 +565,7 @@ def run_single(args, rank, world, local, pg):
     launches = S.launch_count() - launches0
     x_m = S.solution()
     err_m = float(np.linalg.norm(x_m - x_ref) / np.linalg.norm(x_ref))
-    if pg:
-        import torch
-        t = torch.tensor([ms_total], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, pg)
     ms_step = ms_total / args.steps
     value = neq * world / (ms_step / 1e3)
     log(f"timed: {ms_step:.2f} ms/step, inner iters {its}, err {err_m:.3e}")
