@@ -25,6 +25,10 @@ namespace {
 constexpr int BBS = 256;
 constexpr int BCHUNK = 32;
 constexpr int ROWS_PER_BLOCK = 2048;
+// the reliable-update kernels split every row block of a listed instance into
+// SUB row ranges, one CTA each, so that an instance's FP64 residual spreads
+// over many SMs (FP64 runs at about 2 operations per clock per SM)
+constexpr int SUB = 8;
 
 // per-instance scalar slots in dbs [slot][ninst]
 enum { S_ABSNEW, S_ABSOLD, S_ALPHA, S_BETA, S_RR, S_THRESH, S_RHS2, S_RRLAST, S_NS };
@@ -43,7 +47,11 @@ struct BArgs {
     int* iv;              // [I_NI][ninst]
     unsigned* t;          // [T_NT][ninst]
     int* remaining;
-    double* part;         // [2][nblocks]
+    double* part;         // [SUB][nblocks]
+    int* wl;              // [ninst] instances that need a reliable update this iteration
+    int* wl_n;            // appends of the current iteration
+    int* wl_cur;          // entries of the list being processed
+    int* wl_cum;          // [ninst+1] row blocks of the listed instances before each entry
     int max_iter;
     double tol;
 };
@@ -209,85 +217,129 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
                 else if (it >= a.max_iter) finish(a, k, 2);
             } else if (trr < SS(a, S_THRESH, k) || trr < 1e-2 * SS(a, S_RRLAST, k) || it >= a.max_iter) {
                 II(a, I_UPDATE, k) = 1;
+                a.wl[atomicAdd(a.wl_n, 1)] = k;  // list order varies; each instance's sums do not
             }
             a.t[T_UPD * a.ninst + k] = 0;
         }
     }
 }
 
-__global__ void __launch_bounds__(BBS) kb_fold(BArgs a, float* __restrict__ x32, double* __restrict__ x64) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
-    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
-        x64[i] += (double)x32[i];
-        x32[i] = 0.0f;
+// The reliable updates of the listed instances.  kb_wl_scan turns the list
+// into row-block offsets (one block); the kernels below run on a small fixed
+// grid over (listed row block, sub-range) items, so an iteration in which no
+// instance updates costs almost nothing.
+__global__ void __launch_bounds__(BBS) kb_wl_scan(BArgs a) {
+    __shared__ int sums[BBS];
+    const int n = *a.wl_n;
+    const int per = (n + BBS - 1) / BBS, i0 = min(n, (int)threadIdx.x * per), i1 = min(n, i0 + per);
+    int loc = 0;
+    for (int i = i0; i < i1; ++i) {
+        const int k = a.wl[i];
+        loc += a.inst_blk[k + 1] - a.inst_blk[k];
+    }
+    sums[threadIdx.x] = loc;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive scan of the 256 segment sums
+        int acc = 0;
+        for (int t = 0; t < BBS; ++t) { const int v = sums[t]; sums[t] = acc; acc += v; }
+        a.wl_cum[n] = acc;
+        *a.wl_cur = n;
+        *a.wl_n = 0;
+    }
+    __syncthreads();
+    int acc = sums[threadIdx.x];
+    for (int i = i0; i < i1; ++i) {
+        a.wl_cum[i] = acc;
+        const int k = a.wl[i];
+        acc += a.inst_blk[k + 1] - a.inst_blk[k];
     }
 }
 
-template <int LPR>
-__global__ void __launch_bounds__(BBS) kb_residual(BArgs a, const int* __restrict__ rowptr, const int* __restrict__ colind,
-                                                   const double* __restrict__ val, const double* __restrict__ x,
-                                                   const double* __restrict__ b, double* __restrict__ r) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
+// item w: listed row block w / SUB, sub-range w % SUB; false past the end
+__device__ inline bool wl_item(const BArgs& a, int w, int& k, int& blk, int& r0, int& r1) {
+    const int n = *a.wl_cur;
+    if (n == 0 || w >= a.wl_cum[n] * SUB) return false;
+    const int li = w / SUB, sub = w % SUB;
+    int lo = 0, hi = n;  // largest lo with wl_cum[lo] <= li
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (a.wl_cum[mid] <= li) lo = mid; else hi = mid;
+    }
+    k = a.wl[lo];
+    blk = a.inst_blk[k] + (li - a.wl_cum[lo]);
+    const int b0 = a.blk_r0[blk], len = a.blk_r1[blk] - b0;
+    r0 = b0 + (int)((long long)len * sub / SUB);
+    r1 = b0 + (int)((long long)len * (sub + 1) / SUB);
+    return true;
+}
+
+__global__ void __launch_bounds__(BBS) kb_fold_w(BArgs a, float* __restrict__ x32, double* __restrict__ x64) {
+    int k, blk, r0, r1;
+    for (int w = blockIdx.x; wl_item(a, w, k, blk, r0, r1); w += gridDim.x)
+        for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+            x64[i] += (double)x32[i];
+            x32[i] = 0.0f;
+        }
+}
+
+// r = b - A64 x on the listed instances (one thread per row); the last item of
+// an instance sums its items' partials in order and decides: converged,
+// iteration limit, or restart
+__global__ void __launch_bounds__(BBS) kb_residual_w(BArgs a, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                                                     const double* __restrict__ val, const double* __restrict__ x,
+                                                     const double* __restrict__ b, double* __restrict__ r) {
     __shared__ double sh[32];
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
-    const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
-    const int wgrp = grp - grp % (32 / LPR);
-    double loc = 0.0;
-    for (int base = r0 + wgrp; base < r1; base += BBS / LPR) {
-        const int row = base + (grp - wgrp);
-        const bool act = row < r1;
-        double acc = 0.0;
-        if (act)
-            for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += LPR) acc += __ldg(val + j) * __ldg(x + __ldg(colind + j));
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
-        if (act && lane == 0) {
+    int k, blk, r0, r1;
+    for (int w = blockIdx.x; wl_item(a, w, k, blk, r0, r1); w += gridDim.x) {
+        double loc = 0.0;
+        for (int row = r0 + threadIdx.x; row < r1; row += BBS) {
+            double acc = 0.0;
+            for (int j = rowptr[row]; j < rowptr[row + 1]; ++j) acc += __ldg(val + j) * x[__ldg(colind + j)];
             const double ri = b[row] - acc;
             r[row] = ri;
             loc += ri * ri;
         }
-    }
-    const double s1 = block_sum(loc, sh);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
-    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
-    if (last_of(&a.t[T_RES * a.ninst + k], cnt)) {
-        const double tot = inst_sum(a, k, 0, sh);
-        if (threadIdx.x == 0) {
-            SS(a, S_RRLAST, k) = tot;
-            SS(a, S_RR, k) = tot;
-            if (!(tot == tot)) { II(a, I_BAD, k) = 1; finish(a, k, 3); }
-            else if (tot <= a.tol * a.tol * SS(a, S_RHS2, k)) finish(a, k, 1);
-            else if (II(a, I_ITERS, k) >= a.max_iter) finish(a, k, 2);
-            a.t[T_RES * a.ninst + k] = 0;
+        const double s1 = block_sum(loc, sh);
+        if (threadIdx.x == 0) a.part[(size_t)blk * SUB + (w % SUB)] = s1;
+        const unsigned cnt = (unsigned)(a.inst_blk[k + 1] - a.inst_blk[k]) * SUB;
+        if (last_of(&a.t[T_RES * a.ninst + k], cnt)) {
+            const double tot = reduce_parts(a.part + (size_t)a.inst_blk[k] * SUB, (int)cnt, 1, 0, sh);
+            if (threadIdx.x == 0) {
+                SS(a, S_RRLAST, k) = tot;
+                SS(a, S_RR, k) = tot;
+                if (!(tot == tot)) { II(a, I_BAD, k) = 1; finish(a, k, 3); }
+                else if (tot <= a.tol * a.tol * SS(a, S_RHS2, k)) finish(a, k, 1);
+                else if (II(a, I_ITERS, k) >= a.max_iter) finish(a, k, 2);
+                a.t[T_RES * a.ninst + k] = 0;
+            }
         }
     }
 }
 
-__global__ void __launch_bounds__(BBS) kb_restart(BArgs a, const double* __restrict__ r64, float* __restrict__ r32,
-                                                  const float* __restrict__ dinv) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k) || !II(a, I_UPDATE, k)) return;
+// restart of the listed instances that did not finish: r32 = r64, r.z, beta
+__global__ void __launch_bounds__(BBS) kb_restart_w(BArgs a, const double* __restrict__ r64, float* __restrict__ r32,
+                                                    const float* __restrict__ dinv) {
     __shared__ double sh[32];
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
-    double rz = 0.0;
-    for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
-        const float ri = (float)r64[i];
-        r32[i] = ri;
-        rz += (double)ri * (double)(dinv[i] * ri);
-    }
-    const double s1 = block_sum(rz, sh);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
-    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
-    if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
-        const double tot = inst_sum(a, k, 0, sh);
-        if (threadIdx.x == 0) {
-            SS(a, S_BETA, k) = tot / SS(a, S_ABSOLD, k);
-            SS(a, S_ABSNEW, k) = tot;
-            II(a, I_UPDATE, k) = 0;
-            a.t[T_SPMV * a.ninst + k] = 0;
+    int k, blk, r0, r1;
+    for (int w = blockIdx.x; wl_item(a, w, k, blk, r0, r1); w += gridDim.x) {
+        if (II(a, I_DONE, k)) continue;  // decided by the residual kernel, the same for all its items
+        double rz = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
+            const float ri = (float)r64[i];
+            r32[i] = ri;
+            rz += (double)ri * (double)(dinv[i] * ri);
+        }
+        const double s1 = block_sum(rz, sh);
+        if (threadIdx.x == 0) a.part[(size_t)blk * SUB + (w % SUB)] = s1;
+        const unsigned cnt = (unsigned)(a.inst_blk[k + 1] - a.inst_blk[k]) * SUB;
+        if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
+            const double tot = reduce_parts(a.part + (size_t)a.inst_blk[k] * SUB, (int)cnt, 1, 0, sh);
+            if (threadIdx.x == 0) {
+                SS(a, S_BETA, k) = tot / SS(a, S_ABSOLD, k);
+                SS(a, S_ABSNEW, k) = tot;
+                II(a, I_UPDATE, k) = 0;
+                a.t[T_SPMV * a.ninst + k] = 0;
+            }
         }
     }
 }
@@ -313,17 +365,6 @@ void launch_kb_spmv(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, con
         case 8: kb_spmv<TV, TX, 8><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
         case 16: kb_spmv<TV, TX, 16><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
         default: kb_spmv<TV, TX, 32><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
-    }
-}
-
-void launch_kb_residual(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, const int* rp, const int* ci, const double* v,
-                        const double* x, const double* b, double* r) {
-    switch (lpr) {
-        case 2: kb_residual<2><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
-        case 4: kb_residual<4><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
-        case 8: kb_residual<8><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
-        case 16: kb_residual<16><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
-        default: kb_residual<32><<<grid, BBS, 0, st>>>(a, rp, ci, v, x, b, r); break;
     }
 }
 
@@ -360,7 +401,8 @@ int ensure_batch_state(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dbs.alloc((size_t)S_NS * c->ninst));
     ISL_CHECK_CUDA(c, c->dbi.alloc((size_t)I_NI * c->ninst + 1));
     ISL_CHECK_CUDA(c, c->dbt.alloc((size_t)T_NT * c->ninst));
-    ISL_CHECK_CUDA(c, c->dbpart.alloc((size_t)2 * bi.size()));
+    ISL_CHECK_CUDA(c, c->dbpart.alloc((size_t)SUB * bi.size()));
+    ISL_CHECK_CUDA(c, c->dbwl.alloc((size_t)2 * c->ninst + 3));
     cudaStream_t st = c->stream;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_inst.p, bi.data(), bi.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row0.p, b0.data(), b0.size() * 4, cudaMemcpyHostToDevice, st));
@@ -394,14 +436,20 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     a.t = c->dbt.p;
     a.remaining = c->dbi.p + (size_t)I_NI * ni;
     a.part = c->dbpart.p;
+    a.wl = c->dbwl.p;
+    a.wl_n = c->dbwl.p + ni;
+    a.wl_cur = c->dbwl.p + ni + 1;
+    a.wl_cum = c->dbwl.p + ni + 2;
     a.max_iter = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
     a.tol = tol;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbs.p, 0, (size_t)S_NS * ni * 8, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbi.p, 0, ((size_t)I_NI * ni + 1) * 4, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbt.p, 0, (size_t)T_NT * ni * 4, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbwl.p, 0, ((size_t)2 * ni + 3) * 4, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(a.remaining, &ni, 4, cudaMemcpyHostToDevice, st));
     const int lpr = pick_lpr(c);
     const unsigned vg = (unsigned)c->sm_count * 8;
+    const unsigned wgrid = (unsigned)c->sm_count * 4;  // the reliable-update worklist kernels
     const bool mixed = (method == ISL_SOLVE_CG_FP32_IR);
     if (mixed && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "batched mixed solve needs the FP64 matrix (ISL_PREC_MIXED)");
     double* W = c->w64.p;
@@ -432,9 +480,11 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
             kb_dir<float><<<grid, BBS, 0, st>>>(a, r32, d32, p32);
             launch_kb_spmv<float, float>(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval32.p, p32, q32);
             kb_update<float><<<grid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
-            kb_fold<<<grid, BBS, 0, st>>>(a, x32, x64);
-            launch_kb_residual(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64);
-            kb_restart<<<grid, BBS, 0, st>>>(a, r64, r32, d32);
+            // reliable updates of the instances kb_update listed
+            kb_wl_scan<<<1, BBS, 0, st>>>(a);
+            kb_fold_w<<<wgrid, BBS, 0, st>>>(a, x32, x64);
+            kb_residual_w<<<wgrid, BBS, 0, st>>>(a, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64);
+            kb_restart_w<<<wgrid, BBS, 0, st>>>(a, r64, r32, d32);
         }
         ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     }
@@ -444,7 +494,7 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         cudaGraphDestroy(graph);
         ISL_CHECK_CUDA(c, e);
     }
-    const int per_iter = mixed ? 6 : 3;
+    const int per_iter = mixed ? 7 : 3;
     const int64_t max_replays = (int64_t)a.max_iter / BCHUNK + 8;
     int remaining = ni;
     int64_t replays = 0;

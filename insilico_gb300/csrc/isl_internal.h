@@ -201,7 +201,8 @@ struct isl_ctx {
     isl::DBuf<double> dbs;        // per-instance scalars [16][ninst]
     isl::DBuf<int32_t> dbi;       // per-instance ints   [8][ninst]
     isl::DBuf<unsigned int> dbt;  // per-instance tickets [4][ninst]
-    isl::DBuf<double> dbpart;     // per-block partials [2][nblocks]
+    isl::DBuf<double> dbpart;     // per-block partials [8][nblocks]
+    isl::DBuf<int32_t> dbwl;      // reliable-update worklist: instances, append count, count, block offsets
     int64_t nbblocks = 0;
     std::vector<int64_t> inst_iters;
     std::vector<double> inst_relres;
