@@ -311,17 +311,28 @@ Key face_key(const int64_t* ev, const std::vector<int>& f) {
 // Group identical faces: returns, for every (element, face) slot, the slot of
 // its first occurrence in element-major order, and the sorted order of keys.
 void group_faces(const std::vector<Key>& keys, std::vector<int64_t>& first, std::vector<int64_t>& order) {
+    // sort contiguous (key, slot) records: the slot breaks ties, which is the
+    // order of a stable sort of the slots by key
+    struct Rec {
+        Key k;
+        int64_t s;
+        bool operator<(const Rec& o) const { return k < o.k || (k == o.k && s < o.s); }
+    };
     const int64_t n = (int64_t)keys.size();
+    std::vector<Rec> rec((size_t)n);
+    for (int64_t i = 0; i < n; ++i) rec[i] = {keys[i], i};
+    std::sort(rec.begin(), rec.end());
     order.resize(n);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return keys[a] < keys[b]; });
     first.assign(n, -1);
     int64_t i = 0;
     while (i < n) {
         int64_t j = i;
-        while (j < n && keys[order[j]] == keys[order[i]]) ++j;
-        const int64_t f0 = order[i];  // stable sort: the smallest slot of the group comes first
-        for (int64_t k = i; k < j; ++k) first[order[k]] = f0;
+        while (j < n && rec[j].k == rec[i].k) ++j;
+        const int64_t f0 = rec[i].s;  // the smallest slot of the group comes first
+        for (int64_t k = i; k < j; ++k) {
+            order[k] = rec[k].s;
+            first[rec[k].s] = f0;
+        }
         i = j;
     }
 }
@@ -410,6 +421,7 @@ static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, con
     c->inst_node_off.assign(node_off, node_off + n_inst + 1);
     c->inst_elem_off.assign(elem_off, elem_off + n_inst + 1);
     c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false; c->mesh_affine = -1;
+    c->bf_valid = false; c->bf_cache.clear();
     if (c->device < 0) return ISL_OK;
     cudaSetDevice(c->device);
     std::vector<int32_t> soa((size_t)n_elem * c->ngeom);
@@ -524,6 +536,7 @@ int isl_field_elem_dofobj(isl_ctx* c, int64_t* out) {
 }
 
 static void boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) {
+    if (c->bf_valid) { out = c->bf_cache; return; }
     const auto tab = nfaces(c->shape, c->dim - 1);
     const int nfc = (int)tab.size();
     const int64_t E = c->nelem;
@@ -541,6 +554,8 @@ static void boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out)
         if (j - i == 1) out.push_back({order[i] / nfc, (int)(order[i] % nfc)});
         i = j;
     }
+    c->bf_cache = out;
+    c->bf_valid = true;
 }
 
 int isl_boundary_faces(isl_ctx* c, int64_t* n, int64_t* elem, int* face) {
@@ -599,17 +614,25 @@ int isl_boundary_points(isl_ctx* c, int64_t* n, double* x, int64_t* dofobj) {
             }
         }
     }
+    // geometry shape values at every local support point, and the local DOF
+    // positions of every face, evaluated once
+    std::vector<std::vector<double>> gv((size_t)c->nfun);
+    int ng = 0;
+    for (int l = 0; l < c->nfun; ++l) {
+        std::vector<double> g;
+        element_eval(c->shape, 1, &sup[(size_t)l * c->dim], gv[l], g, ng);
+    }
+    const int nfc = (int)nfaces(c->shape, c->dim - 1).size();
+    std::vector<std::vector<int>> floc((size_t)nfc);
+    for (int f = 0; f < nfc; ++f) floc[f] = face_local_dofs(c, f);
     int64_t cnt = 0;
     for (auto& ef : bf) {
-        const auto loc = face_local_dofs(c, ef.second);
-        for (int l : loc) {
+        for (int l : floc[ef.second]) {
             if (x && dofobj) {
-                std::vector<double> v, g;
-                int ng = 0;
-                element_eval(c->shape, 1, &sup[(size_t)l * c->dim], v, g, ng);
+                const int64_t* ev = &c->hconn[ef.first * c->ngeom];
                 for (int d = 0; d < c->dim; ++d) {
                     double s = 0.0;
-                    for (int i = 0; i < ng; ++i) s += c->hX[c->hconn[ef.first * c->ngeom + i] * c->dim + d] * v[i];
+                    for (int i = 0; i < ng; ++i) s += c->hX[ev[i] * c->dim + d] * gv[l][i];
                     x[cnt * c->dim + d] = s;
                 }
                 dofobj[cnt] = c->hedof[ef.first * c->nfun + l];

@@ -129,6 +129,8 @@ struct isl_ctx {
     int fedeg = 0, ncomp = 0, nfun = 0, nloc = 0, nup = 0;
     int64_t ndofobj = 0;
     std::vector<int64_t> hedof;  // [nelem][nfun]
+    std::vector<std::pair<int64_t, int>> bf_cache;  // boundary (element, face) list of the current mesh
+    bool bf_valid = false;
     isl::DBuf<int32_t> dedof;    // SoA [nfun][nelem]
     std::vector<uint8_t> status; // per dofobj comp: 0 active, 1 constrained
     std::vector<double> cval;
