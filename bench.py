@@ -113,6 +113,7 @@ def l2_flush(device):
 
 
 # sliced-ELL / block-row SpMV variants by autotune kind (isl_solver.cu)
+SSPMV_KERNEL = {102: "k_sspmv_batch<2,8>", 104: "k_sspmv_batch<4,8>", 108: "k_sspmv_batch<8,6>"}
 BSPMV_KERNEL = {1: "k_bspmv_pap<1>", 2: "k_bspmv_pap<2>", 3: "k_bspmv_pap<4>", 5: "k_bspmv_batch<2,4>",
                 6: "k_bspmv_batch<4,3>", 7: "k_bspmv_batch<8,2>", 4: "k_brow_spmv<4>", 8: "k_brow_spmv<8>",
                 16: "k_brow_spmv<16>"}
@@ -603,9 +604,14 @@ def run_single(args, rank, world, local, pg):
         kname = BSPMV_KERNEL.get(int(kernels["block_kind"]), "k_bspmv") + \
             " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV, autotuned variant)"
     else:
-        nblk = nslot = 0
+        nblk, nslot = 0, S.get_option(A.OPT_SCALAR_SLOTS)
         b32 = spmv_bytes(nnz, neq, 4)
-        kname = "k_spmv_pap<float> (FP32 CSR, inner CG SpMV)"
+        kind = S.get_option(A.OPT_SPMV32_KIND)
+        if kind >= 100:
+            kname = SSPMV_KERNEL.get(kind, "k_sspmv_batch") + \
+                " (scalar sliced-ELL FP32, rows length-sorted in windows of 2048, inner CG SpMV, autotuned)"
+        else:
+            kname = f"k_spmv_pap<float,float,{kind}> (FP32 CSR, {kind} lanes per row, inner CG SpMV, autotuned)"
     ach = b32 / (spmv32_ms * 1e-3) / 1e9
     traffic = ncu_traffic(f"spmv_fp32_{args.workload}")
 

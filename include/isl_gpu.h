@@ -193,9 +193,16 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * 2: the persistent block kernel at every size.  ISL_OPT_BARRIER_TEST (test
  * hook, write-only, one-shot): the next persistent launch starts with its grid
  * barrier armed so that it cannot complete; its bounded wait runs out and the
- * solve returns ISL_ERR_TIMEOUT with the context still usable. */
+ * solve returns ISL_ERR_TIMEOUT with the context still usable.
+ * ISL_OPT_SPMV32_KIND: the FP32 SpMV of the scalar mixed solve, 0 (default)
+ * autotuned on the matrix, 2, 4, 8, 16 or 32 CSR with that many lanes per
+ * row, 102, 104 or 108 the sliced-ELL copy with 2, 4 or 8 slots of loads in
+ * flight per lane (only where the copy exists); read back, the kind in use
+ * (0 before the first mixed solve).  ISL_OPT_SCALAR_SLOTS (read-only): slots
+ * of the scalar sliced-ELL copy, padding included; 0 when there is none
+ * (node-blocked, batched, or fewer than 20,000 equations). */
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
-       ISL_OPT_BARRIER_TEST = 5 };
+       ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 

@@ -41,7 +41,8 @@ EXPORTED = [
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc",
 ]
-OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST = 0, 1, 2, 3, 4, 5
+(OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
+ OPT_SCALAR_SLOTS) = 0, 1, 2, 3, 4, 5, 6, 7
 
 
 class IslError(RuntimeError):

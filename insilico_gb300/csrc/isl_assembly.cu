@@ -826,6 +826,8 @@ int pattern_build(isl_ctx* c) {
         if (c->neq <= 65536) c->hrp_small = rp;
         const int brc = block_pattern(c, rp);
         if (brc != ISL_OK) return brc;
+        const int src = scalar_sell_pattern(c, rp);
+        if (src != ISL_OK) return src;
     }
     kout.release();
     flag.release();

@@ -186,4 +186,61 @@ __device__ inline void reduce_parts2(const double* part, int n, double* sh, doub
     out1 = s1;
 }
 
+// Block-wide forms of the two sums above, for the last block of a large grid:
+// every one of the NT threads of the block must call them (they hold block
+// barriers).  Thread t loads entries t, t + NT, ... (eight in flight), so a
+// grid of up to 8 NT blocks is read in one round trip instead of one per 256
+// entries; each warp adds its lanes by a fixed shuffle tree and thread 0 adds
+// the warp sums in warp order.  Fixed order; the result is valid in thread 0.
+template <int NT>
+__device__ inline double reduce_parts_blk(const double* part, int n, int stride, int off, double* sh) {
+    static_assert(NT % 32 == 0 && NT / 32 <= 32, "sh holds one double per warp");
+    double s = 0.0;
+    for (int base = 0; base < n; base += 8 * NT) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * NT + (int)threadIdx.x;
+            v[u] = i < n ? __ldcg(part + (size_t)i * stride + off) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncthreads();  // sh may still be read by an earlier block sum
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) t += sh[w];
+    return t;
+}
+
+template <int NT>
+__device__ inline void reduce_parts2_blk(const double* part, int n, double* sh, double& out0, double& out1) {
+    static_assert(NT % 32 == 0 && NT / 16 <= 32, "sh holds two doubles per warp");
+    const double2* p2 = reinterpret_cast<const double2*>(part);
+    double s0 = 0.0, s1 = 0.0;
+    for (int base = 0; base < n; base += 8 * NT) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * NT + (int)threadIdx.x;
+            v[u] = i < n ? __ldcg(p2 + i) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { s0 += v[u].x; s1 += v[u].y; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) { sh[2 * (threadIdx.x >> 5)] = s0; sh[2 * (threadIdx.x >> 5) + 1] = s1; }
+    __syncthreads();
+    out0 = out1 = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) { out0 += sh[2 * w]; out1 += sh[2 * w + 1]; }
+}
+
 }  // namespace isl

@@ -985,6 +985,13 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
         c->use_persist = (int)value;
         return ISL_OK;
     }
+    if (key == ISL_OPT_SPMV32_KIND) {
+        if (value < 0 || value > 108 || !isl::spmv32_kind_valid(c, (int)value))
+            ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_SPMV32_KIND: 0, CSR lanes per row 2..32, or 102/104/108 with a sliced-ELL copy");
+        c->spmv32_forced = (int)value;
+        c->spmv_lpr32 = (int)value;
+        return ISL_OK;
+    }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown or read-only option");
 }
 
@@ -995,6 +1002,8 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
     if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }
     if (key == ISL_OPT_NSLOTS) { *value = c->blocked ? c->nslot : 0; return ISL_OK; }
+    if (key == ISL_OPT_SPMV32_KIND) { *value = c->spmv_lpr32; return ISL_OK; }
+    if (key == ISL_OPT_SCALAR_SLOTS) { *value = c->ss_nslot; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
 }
 

@@ -198,6 +198,15 @@ struct isl_ctx {
     int64_t asm_serial = 0, bsr_serial = -1;
     int bspmv_lpb = 0;
 
+    // scalar sliced-ELL copy of the FP32 matrix for the mixed solver of a
+    // system that is not node-blocked: rows sorted by length (longest first)
+    // within windows of 2048 rows, slices of 32 sorted rows padded to their
+    // longest row, slots column-major (slot = slice_off + k*32 + lane)
+    int64_t ss_nslice = 0, ss_nslot = 0;
+    isl::DBuf<int32_t> dss_off, dss_wid, dss_row, dss_col, dss_pos;
+    isl::DBuf<float> dss_val;
+    int64_t ss_serial = -1;      // assembly whose values the copy holds
+
     // batched CG (ninst > 1): row ranges of thread blocks and per-instance state
     isl::DBuf<int32_t> dinst_row, dblk_inst, dblk_row0, dblk_row1, dinst_blk;
     isl::DBuf<double> dbs;        // per-instance scalars [16][ninst]
@@ -218,7 +227,8 @@ struct isl_ctx {
     isl::DBuf<double> dpart;     // block partial sums
     isl::DBuf<isl::CGScal> dscal;
     isl::CGScal* hscal = nullptr;  // pinned host mirror
-    int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row
+    int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row (FP32: 100 + U = sliced-ELL, U slots in flight)
+    int spmv32_forced = 0;               // FP32 SpMV kind set through ISL_OPT_SPMV32_KIND (0: autotune)
 
     // timing
     bool timing = false;
@@ -254,5 +264,7 @@ int distribute_device(isl_ctx* c, int add);
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
 int time_kernels(isl_ctx* c, int nrep, double* ms);
 int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
+int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
+bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 }  // namespace isl

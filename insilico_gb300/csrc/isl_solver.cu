@@ -23,7 +23,9 @@
 // the iteration continues with the same search direction.  The solve ends
 // when the true FP64 residual meets the tolerance.
 #include <cmath>
+#include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -77,7 +79,7 @@ __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ 
     const double bs = block_sum_t(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
     if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
         if (threadIdx.x == 0) {
             S->pAp = tot;
             S->alpha = S->absNew / tot;
@@ -127,7 +129,7 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
         double trr, trz;
-        reduce_parts2(part, gridDim.x, sh, trr, trz);
+        reduce_parts2_blk<BS>(part, gridDim.x, sh, trr, trz);
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->iters += 1;
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict_
     const double bs = block_sum(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
     if (last_block(ticket)) {
-        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
         if (threadIdx.x == 0) { *out = tot; *ticket = 0; }
     }
 }
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restric
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (last_block(&S->ticket2)) {
         double trr, trz;
-        reduce_parts2(part, gridDim.x, sh, trr, trz);
+        reduce_parts2_blk<BS>(part, gridDim.x, sh, trr, trz);
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->beta = trz / S->absOld;
@@ -298,6 +300,130 @@ static void launch_residual(int lpr, unsigned grid, cudaStream_t st, int n, cons
     }
 }
 
+// q = A p and p.q on the scalar sliced-ELL copy (one warp per slice of 32
+// sorted rows, one lane per row).  The loads of U slots (column id and value,
+// 128 coalesced bytes per warp each, L1 bypassed) are issued before their U
+// gathers of p, so every lane keeps 8U bytes of the stream in flight; the
+// FMAs then run in slot order, so the sums do not depend on U.  Padding slots
+// hold value 0 and a valid column.  The stream is latency-bound: the variants
+// run at full occupancy (U = 2, 4: 8 blocks of 256 per SM within 32
+// registers; U = 8: 6 blocks), which measured faster on the GB300 than deeper
+// batches at lower occupancy.
+template <int U, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int* __restrict__ soff,
+                                                          const int* __restrict__ swid, const int* __restrict__ srow,
+                                                          const int* __restrict__ scol, const float* __restrict__ sv,
+                                                          const float* __restrict__ p, float* __restrict__ q, CGScal* S,
+                                                          double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
+    float loc = 0.f;
+    for (int s = warp; s < nslice; s += nwarps) {
+        const int o = soff[s] + lane, w = swid[s];  // w: warp-uniform
+        float acc = 0.f;
+        for (int k = 0; k < w; k += U) {
+            int j[U];
+            float v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    j[u] = ld_stream(scol + o + (k + u) * 32);
+                    v[u] = ld_stream(sv + o + (k + u) * 32);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (k + u < w) acc += v[u] * __ldg(p + j[u]);
+        }
+        const int row = srow[s * 32 + lane];
+        if (row >= 0) {
+            q[row] = acc;
+            loc += p[row] * acc;
+        }
+    }
+    const double bsum = block_sum_f(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    if (last_block(&S->ticket1)) {
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
+        if (threadIdx.x == 0) {
+            S->pAp = tot;
+            S->alpha = S->absNew / tot;
+            S->ticket1 = 0;
+        }
+    }
+}
+
+static unsigned ssell_grid(const isl_ctx* c, unsigned per_sm) {
+    const long long need = (c->ss_nslice + (BS / 32) - 1) / (BS / 32);
+    return (unsigned)std::max<long long>(1, std::min<long long>(need, (long long)per_sm * c->sm_count));
+}
+
+// FP32 SpMV of the mixed solver: kind 2..32 = CSR with that many lanes per
+// row, kind 100 + U = the sliced-ELL copy with U slots of loads in flight
+static void launch_spmv32(isl_ctx* c, int kind, unsigned grid, cudaStream_t st, const float* p, float* q, CGScal* S,
+                          double* part) {
+    const int ns = (int)c->ss_nslice;
+    switch (kind) {
+        case 102: k_sspmv_batch<2, 8><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
+        case 104: k_sspmv_batch<4, 8><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
+        case 108: k_sspmv_batch<8, 6><<<ssell_grid(c, 6), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
+        default: launch_spmv<float, float>(kind, grid, st, (int)c->neq, c->drowptr.p, c->dcolind.p, c->dval32.p, p, q, S, part); break;
+    }
+}
+
+bool spmv32_kind_valid(const isl_ctx* c, int kind) {
+    if (kind == 0 || kind == 2 || kind == 4 || kind == 8 || kind == 16 || kind == 32) return true;
+    return (kind == 102 || kind == 104 || kind == 108) && c->ss_nslice > 0;
+}
+
+// FP32 values into the scalar sliced-ELL slots (padding slots stay zero)
+__global__ void k_ssell_values(int n, const int* __restrict__ rowptr, const int* __restrict__ spos,
+                               const float* __restrict__ val, float* __restrict__ sv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int lo = rowptr[i], hi = rowptr[i + 1], s0 = spos[i];
+        for (int k = lo; k < hi; ++k) sv[s0 + (k - lo) * 32] = val[k];
+    }
+}
+
+// refresh the sliced-ELL values after an assembly
+static int ensure_ssell(isl_ctx* c) {
+    if (c->ss_nslice == 0 || c->ss_serial == c->asm_serial) return ISL_OK;
+    k_ssell_values<<<vec_grid(c), BS, 0, c->stream>>>((int)c->neq, c->drowptr.p, c->dss_pos.p, c->dval32.p, c->dss_val.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    c->ss_serial = c->asm_serial;
+    return ISL_OK;
+}
+
+// Autotune of the FP32 SpMV: CSR lanes per row and, when the sliced-ELL copy
+// exists, its batch depths; each candidate timed over 20 launches on the
+// current matrix, the fastest kept.  Chosen once per context.
+static int autotune_spmv32(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
+    if (c->spmv32_forced && spmv32_kind_valid(c, c->spmv32_forced)) return c->spmv32_forced;
+    const double avg = (double)c->nnz / (double)c->neq;
+    int best = 2;
+    while (best < 32 && best < avg / 2) best *= 2;
+    if (c->neq < 20000) return best;  // too small to time meaningfully
+    int cand[7] = {4, 8, 16, 32, 102, 104, 108};
+    const int ncand = c->ss_nslice > 0 ? 7 : 4;
+    float bestms = 1e30f;
+    cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
+    c->launches += 21 * ncand;
+    for (int k = 0; k < ncand; ++k) {
+        launch_spmv32(c, cand[k], vec_grid(c), c->stream, p, q, S, part);
+        cudaEventRecord(c->ev[2], c->stream);
+        for (int r = 0; r < 20; ++r) launch_spmv32(c, cand[k], vec_grid(c), c->stream, p, q, S, part);
+        cudaEventRecord(c->ev[3], c->stream);
+        cudaEventSynchronize(c->ev[3]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        if (ms < bestms) { bestms = ms; best = cand[k]; }
+    }
+    return best;
+}
+
 // Autotune of the SpMV row mapping (lanes per row): time each candidate on the
 // current matrix, keep the fastest.  Chosen once per context and precision.
 template <typename TV, typename TX>
@@ -340,7 +466,10 @@ static int capture_chunk(isl_ctx* c, const TV* val, TX* x, TX* r, TX* p, TX* q, 
     const unsigned gdir = (unsigned)std::max<long long>(1, ((long long)n + BS - 1) / BS);
     for (int k = 0; k < CHUNK; ++k) {
         k_cg_dir<TX><<<gdir, BS, 0, st>>>(n, r, dinv, p, S);
-        launch_spmv<TV, TX>(lpr, grid, st, n, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
+        if constexpr (std::is_same<TV, float>::value)
+            launch_spmv32(c, lpr, grid, st, p, q, S, part);
+        else
+            launch_spmv<TV, TX>(lpr, grid, st, n, c->drowptr.p, c->dcolind.p, val, p, q, S, part);
         k_cg_update<TX><<<upd_grid(c, n), BS, 0, st>>>(n, x, r, p, q, dinv, S, part, max_iter);
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
@@ -950,9 +1079,11 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     double *x64 = W, *r64 = W + n;
     float* V = c->w32.p;
     float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n;
+    int rc = ensure_ssell(c);
+    if (rc != ISL_OK) return rc;
     if (!c->spmv_lpr32) {
         ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, n * 4, st));
-        c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, p32, q32, c->dscal.p, c->dpart.p);
+        c->spmv_lpr32 = autotune_spmv32(c, p32, q32, c->dscal.p, c->dpart.p);
     }
     const bool exact64 = c->have64;  // without the FP64 matrix: plain FP32 CG (inexact Newton tangents)
     if (exact64 && !c->spmv_lpr64)
@@ -970,7 +1101,7 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 2;
     cudaGraphExec_t exec;
-    int rc = capture_chunk<float, float>(c, c->dval32.p, x32, r32, p32, q32, d32, c->spmv_lpr32, mi, &exec);
+    rc = capture_chunk<float, float>(c, c->dval32.p, x32, r32, p32, q32, d32, c->spmv_lpr32, mi, &exec);
     if (rc != ISL_OK) return rc;
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
@@ -1177,7 +1308,7 @@ __global__ void __launch_bounds__(BS) k_bspmv_pap(int nbr, int nslice, const int
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
         if (threadIdx.x == 0) {
             S->pAp = tot;
             S->alpha = S->absNew / tot;
@@ -1250,7 +1381,7 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
         if (threadIdx.x == 0) {
             S->pAp = tot;
             S->alpha = S->absNew / tot;
@@ -1296,7 +1427,7 @@ __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restr
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
         if (threadIdx.x == 0) {
             S->pAp = tot;
             S->alpha = S->absNew / tot;
@@ -1358,7 +1489,7 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
     if (!last_block(&S->ticket2)) return;
     double trr, trz;
-    reduce_parts2(part, gridDim.x, sh, trr, trz);
+    reduce_parts2_blk<NODE_BS>(part, gridDim.x, sh, trr, trz);
     if (threadIdx.x == 0) {
         S->rr = trr;
         S->iters += 1;
@@ -1661,6 +1792,80 @@ int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
     return ISL_OK;
 }
 
+// column ids of the scalar sliced-ELL slots (padding: the row's own column,
+// or column 0 in a padding row) and the first slot of every row
+__global__ void k_ssell_fill(int nslice, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                             const int* __restrict__ soff, const int* __restrict__ swid, const int* __restrict__ srow,
+                             int* __restrict__ scol, int* __restrict__ spos) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nslice * 32; i += gridDim.x * blockDim.x) {
+        const int s = i / 32, l = i % 32;
+        const int row = srow[i];
+        const int o = soff[s] + l, w = swid[s];
+        const int lo = row >= 0 ? rowptr[row] : 0;
+        const int len = row >= 0 ? rowptr[row + 1] - lo : 0;
+        if (row >= 0) spos[row] = o;
+        for (int k = 0; k < w; ++k) scol[o + k * 32] = k < len ? colind[lo + k] : (row >= 0 ? row : 0);
+    }
+}
+
+// Scalar sliced-ELL copy of a system that is not node-blocked (setup).  Rows
+// are sorted by length, longest first and stably, within windows of 2048 rows
+// (a multiple of 32, so no slice spans two windows); the sort keeps the
+// padding near zero while the rows of a slice stay within 2048 of each other,
+// so the gathers of p keep their locality.  Batched systems are left out.
+int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
+    c->ss_nslice = c->ss_nslot = 0;
+    c->ss_serial = -1;
+    c->dss_off.release(); c->dss_wid.release(); c->dss_row.release();
+    c->dss_col.release(); c->dss_pos.release(); c->dss_val.release();
+    const int64_t n = c->neq;
+    if (c->blocked || c->ninst > 1 || n < 20000) return ISL_OK;
+    constexpr int64_t WIN = 2048;
+    const int64_t nslice = (n + 31) / 32;
+    std::vector<int32_t> row((size_t)nslice * 32, -1), wid((size_t)nslice), off((size_t)nslice + 1);
+    std::vector<int32_t> idx;
+    for (int64_t w0 = 0; w0 < n; w0 += WIN) {
+        const int64_t w1 = std::min(n, w0 + WIN);
+        idx.resize((size_t)(w1 - w0));
+        for (int64_t i = w0; i < w1; ++i) idx[(size_t)(i - w0)] = (int32_t)i;
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+        for (int64_t i = w0; i < w1; ++i) row[(size_t)i] = idx[(size_t)(i - w0)];
+    }
+    int64_t tot = 0;
+    for (int64_t s = 0; s < nslice; ++s) {
+        int32_t w = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int32_t r = row[(size_t)(s * 32 + l)];
+            if (r >= 0) w = std::max(w, rp[r + 1] - rp[r]);
+        }
+        wid[(size_t)s] = w;
+        off[(size_t)s] = (int32_t)tot;
+        tot += (int64_t)w * 32;
+        if (tot >= INT32_MAX) return ISL_OK;  // too large for 32-bit slots: CSR only
+    }
+    off[(size_t)nslice] = (int32_t)tot;
+    cudaStream_t st = c->stream;
+    ISL_CHECK_CUDA(c, c->dss_off.alloc(nslice + 1));
+    ISL_CHECK_CUDA(c, c->dss_wid.alloc(nslice));
+    ISL_CHECK_CUDA(c, c->dss_row.alloc(nslice * 32));
+    ISL_CHECK_CUDA(c, c->dss_pos.alloc(n));
+    ISL_CHECK_CUDA(c, c->dss_col.alloc(tot));
+    ISL_CHECK_CUDA(c, c->dss_val.alloc(tot));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_wid.p, wid.data(), wid.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_row.p, row.data(), row.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dss_val.p, 0, (size_t)tot * 4, st));
+    k_ssell_fill<<<vec_grid(c), BS, 0, st>>>((int)nslice, c->drowptr.p, c->dcolind.p, c->dss_off.p, c->dss_wid.p,
+                                             c->dss_row.p, c->dss_col.p, c->dss_pos.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));  // the host vectors above go out of scope
+    c->launches += 1;
+    c->ss_nslice = nslice;
+    c->ss_nslot = tot;
+    return ISL_OK;
+}
+
 // refresh the block values and the block-Jacobi inverses after an assembly
 static int ensure_bsr(isl_ctx* c) {
     if (c->bsr_serial == c->asm_serial) return ISL_OK;
@@ -1882,11 +2087,12 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
         if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
         float* V = c->w32.p;
         ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
-        if (!c->spmv_lpr32) c->spmv_lpr32 = autotune_lpr<float, float>(c, c->dval32.p, V + 2 * n, V + 3 * n, S, c->dpart.p);
-        launch_spmv<float, float>(c->spmv_lpr32, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval32.p, V + 2 * n, V + 3 * n, S, c->dpart.p);
+        rc = ensure_ssell(c);
+        if (rc != ISL_OK) return rc;
+        if (!c->spmv_lpr32) c->spmv_lpr32 = autotune_spmv32(c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+        launch_spmv32(c, c->spmv_lpr32, vec_grid(c), st, V + 2 * n, V + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[2], st);
-        for (int r = 0; r < nrep; ++r)
-            launch_spmv<float, float>(c->spmv_lpr32, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval32.p, V + 2 * n, V + 3 * n, S, c->dpart.p);
+        for (int r = 0; r < nrep; ++r) launch_spmv32(c, c->spmv_lpr32, vec_grid(c), st, V + 2 * n, V + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[3], st);
     } else {
         if (!c->have64) ISL_FAIL(c, ISL_ERR_ARG, "no FP64 matrix");

@@ -264,6 +264,70 @@ def test_partially_constrained_nodes_use_scalar_path():
     S.close()
 
 
+def _pulled_sheet(n):
+    """hex8 elasticity with the x = 1 face pulled in u_x only: nodes there are
+    partly active, so the system is not node-blocked."""
+    p = W.config("c2", n=n)
+    base = p.dirichlet
+
+    def diri(x):
+        m, v = base(x)
+        m = m.copy()
+        m[np.abs(x[:, 0] - 1.0) < 1e-9, 0] = True
+        vals = np.zeros(m.shape)
+        vals[np.abs(x[:, 0] - 1.0) < 1e-9, 0] = 0.01
+        return m, vals
+    p.dirichlet = diri
+    p.neumann_plane = None
+    return p
+
+
+@pytest.mark.parametrize("case", ["c3", "sheet"])
+def test_scalar_sliced_ell_and_csr_agree(case):
+    """The sliced-ELL copy of a scalar (not node-blocked) system holds every
+    stored entry once (padding < 10 %); its SpMV sums each row in slot order
+    whatever the batch depth, so the three depths give bitwise identical
+    solves; CSR and sliced-ELL both meet the tolerance and agree with FP64."""
+    p = W.config("c3", n=16) if case == "c3" else _pulled_sheet(20)
+    S = gpu_problem(p)
+    assert S.get_option(A.OPT_BLOCKED) == 0 and S.neq >= 20000
+    S.assemble(A.PREC_MIXED)
+    nnz = len(S.csr(values=False)[1])
+    slots = S.get_option(A.OPT_SCALAR_SLOTS)
+    assert nnz <= slots <= 1.1 * nnz
+    S.set_option(A.OPT_PERSISTENT, 0)  # graph path (the cluster path has its own SpMV)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    out = {}
+    for kind in (4, 102, 104, 108):
+        S.set_option(A.OPT_SPMV32_KIND, kind)
+        it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        assert S.get_option(A.OPT_SPMV32_KIND) == kind
+        x = S.solution()
+        assert rel <= 1e-12
+        assert np.linalg.norm(x - x64) <= 1e-8 * np.linalg.norm(x64)
+        out[kind] = (it, x)
+    for kind in (102, 108):
+        assert out[kind][0] == out[104][0] and np.array_equal(out[kind][1], out[104][1])
+    assert abs(out[104][0] - out[4][0]) <= max(2, out[4][0] // 50)
+    # autotuned choice is one of the candidates and solves to the same bar
+    S.set_option(A.OPT_SPMV32_KIND, 0)
+    it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    assert S.get_option(A.OPT_SPMV32_KIND) in (4, 8, 16, 32, 102, 104, 108)
+    assert np.linalg.norm(S.solution() - x64) <= 1e-8 * np.linalg.norm(x64)
+    S.close()
+
+
+def test_spmv32_kind_option_range():
+    S = gpu_problem(W.config("c2", n=4))  # node-blocked: no scalar sliced-ELL copy
+    assert S.get_option(A.OPT_SCALAR_SLOTS) == 0
+    for bad in (3, 104, 116, -1):
+        with pytest.raises(A.IslError):
+            S.set_option(A.OPT_SPMV32_KIND, bad)
+    S.set_option(A.OPT_SPMV32_KIND, 8)
+    S.close()
+
+
 def test_empty_system_every_dof_constrained():
     p = W.config("c1", n=1)  # a single quad: all four nodes on the Dirichlet boundary
     S = gpu_problem(p)
