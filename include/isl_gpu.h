@@ -200,9 +200,13 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * flight per lane (only where the copy exists); read back, the kind in use
  * (0 before the first mixed solve).  ISL_OPT_SCALAR_SLOTS (read-only): slots
  * of the scalar sliced-ELL copy, padding included; 0 when there is none
- * (node-blocked, batched, or fewer than 20,000 equations). */
+ * (node-blocked, batched, or fewer than 20,000 equations).
+ * ISL_OPT_HOST_SETUP (default 0): with a device, isl_field_create numbers the
+ * DOF objects of fields of degree > 1 and isl_boundary_faces /
+ * isl_boundary_points find the boundary on the GPU (sorts and scans, the
+ * same ids and order as the host rules); 1 runs both on the host. */
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
-       ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7 };
+       ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 

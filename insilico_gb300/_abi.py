@@ -42,7 +42,7 @@ EXPORTED = [
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
- OPT_SCALAR_SLOTS) = 0, 1, 2, 3, 4, 5, 6, 7
+ OPT_SCALAR_SLOTS, OPT_HOST_SETUP) = 0, 1, 2, 3, 4, 5, 6, 7, 8
 
 
 class IslError(RuntimeError):

@@ -453,7 +453,31 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     const int64_t E = c->nelem;
     c->hedof.assign((size_t)E * nf, -1);
     c->inst_dof_off.assign(c->ninst + 1, 0);
-    if (fe_degree == 1) {
+    // the shared n-faces of every level, for the device numbering
+    std::vector<isl::DeviceLevel> levels;
+    int max_nfc = 0;
+    if (fe_degree > 1) {
+        int begin = 0;
+        for (int n = 0; n <= D; ++n) {
+            const auto tab = nfaces(c->shape, n);
+            isl::DeviceLevel lv;
+            lv.nfc = (int)tab.size();
+            lv.stride = interior_dofs(c->shape, fe_degree, n);
+            lv.begin = begin;
+            lv.w = n < D ? (int)(lv.nfc ? tab[0].size() : 0) : 0;
+            for (int f = 0; f < lv.nfc && n < D; ++f)
+                for (int i = 0; i < lv.w; ++i) lv.v[f][i] = tab[f][i];
+            begin += lv.nfc * lv.stride;
+            max_nfc = std::max(max_nfc, lv.nfc);
+            if (lv.nfc) levels.push_back(lv);
+        }
+    }
+    const bool on_device = fe_degree > 1 && !c->host_setup && isl::device_setup_fits(c, max_nfc);
+    if (on_device) {
+        cudaSetDevice(c->device);
+        const int rc = isl::device_dofobj_numbering(c, levels, nf);
+        if (rc != ISL_OK) return rc;
+    } else if (fe_degree == 1) {
         int64_t mx = 0;
         for (int64_t i = 0; i < E * nf; ++i) { c->hedof[i] = c->hconn[i]; mx = std::max(mx, c->hconn[i] + 1); }
         c->ndofobj = mx;
@@ -516,11 +540,14 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     if (n_dofobj) *n_dofobj = c->ndofobj;
     if (n_fun) *n_fun = nf;
     if (c->device < 0) return ISL_OK;
-    std::vector<int32_t> soa((size_t)E * nf);
-    for (int64_t e = 0; e < E; ++e)
-        for (int f = 0; f < nf; ++f) soa[(size_t)f * E + e] = (int32_t)c->hedof[e * nf + f];
-    ISL_CHECK_CUDA(c, c->dedof.alloc(soa.size()));
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dedof.p, soa.data(), soa.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    std::vector<int32_t> soa;
+    if (!on_device) {  // the device numbering leaves dedof on the device
+        soa.resize((size_t)E * nf);
+        for (int64_t e = 0; e < E; ++e)
+            for (int f = 0; f < nf; ++f) soa[(size_t)f * E + e] = (int32_t)c->hedof[e * nf + f];
+        ISL_CHECK_CUDA(c, c->dedof.alloc(soa.size()));
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dedof.p, soa.data(), soa.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    }
     ISL_CHECK_CUDA(c, c->du.alloc(ndc));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->du.p, 0, ndc * sizeof(double), c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -535,11 +562,27 @@ int isl_field_elem_dofobj(isl_ctx* c, int64_t* out) {
     return ISL_OK;
 }
 
-static void boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) {
-    if (c->bf_valid) { out = c->bf_cache; return; }
+static int boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) {
+    if (c->bf_valid) { out = c->bf_cache; return ISL_OK; }
     const auto tab = nfaces(c->shape, c->dim - 1);
     const int nfc = (int)tab.size();
     const int64_t E = c->nelem;
+    if (!c->host_setup && isl::device_setup_fits(c, nfc)) {
+        isl::DeviceLevel lv;
+        lv.nfc = nfc;
+        lv.w = (int)tab[0].size();
+        for (int f = 0; f < nfc; ++f)
+            for (int i = 0; i < lv.w; ++i) lv.v[f][i] = tab[f][i];
+        std::vector<int64_t> slots;
+        cudaSetDevice(c->device);
+        const int rc = isl::device_boundary_slots(c, lv, slots);
+        if (rc != ISL_OK) return rc;
+        out.resize(slots.size());
+        for (size_t i = 0; i < slots.size(); ++i) out[i] = {slots[i] / nfc, (int)(slots[i] % nfc)};
+        c->bf_cache = out;
+        c->bf_valid = true;
+        return ISL_OK;
+    }
     std::vector<Key> keys((size_t)E * nfc);
     for (int64_t e = 0; e < E; ++e)
         for (int f = 0; f < nfc; ++f) keys[e * nfc + f] = face_key(&c->hconn[e * c->ngeom], tab[f]);
@@ -556,12 +599,14 @@ static void boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out)
     }
     c->bf_cache = out;
     c->bf_valid = true;
+    return ISL_OK;
 }
 
 int isl_boundary_faces(isl_ctx* c, int64_t* n, int64_t* elem, int* face) {
     if (!c || !c->nelem || !n) return ISL_ERR_ARG;
     std::vector<std::pair<int64_t, int>> bf;
-    boundary_list(c, bf);
+    const int rc = boundary_list(c, bf);
+    if (rc != ISL_OK) return rc;
     *n = (int64_t)bf.size();
     if (elem && face)
         for (size_t i = 0; i < bf.size(); ++i) { elem[i] = bf[i].first; face[i] = bf[i].second; }
@@ -595,7 +640,8 @@ static std::vector<int> face_local_dofs(isl_ctx* c, int face) {
 int isl_boundary_points(isl_ctx* c, int64_t* n, double* x, int64_t* dofobj) {
     if (!c || !c->fedeg || !n) return ISL_ERR_ARG;
     std::vector<std::pair<int64_t, int>> bf;
-    boundary_list(c, bf);
+    const int brc = boundary_list(c, bf);
+    if (brc != ISL_OK) return brc;
     // support points: FE nodes on the reference element
     std::vector<double> sup;
     {
@@ -985,6 +1031,12 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
         c->use_persist = (int)value;
         return ISL_OK;
     }
+    if (key == ISL_OPT_HOST_SETUP) {
+        c->host_setup = value != 0;
+        c->bf_valid = false;
+        c->bf_cache.clear();
+        return ISL_OK;
+    }
     if (key == ISL_OPT_SPMV32_KIND) {
         if (value < 0 || value > 108 || !isl::spmv32_kind_valid(c, (int)value))
             ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_SPMV32_KIND: 0, CSR lanes per row 2..32, or 102/104/108 with a sliced-ELL copy");
@@ -1003,6 +1055,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }
     if (key == ISL_OPT_NSLOTS) { *value = c->blocked ? c->nslot : 0; return ISL_OK; }
     if (key == ISL_OPT_SPMV32_KIND) { *value = c->spmv_lpr32; return ISL_OK; }
+    if (key == ISL_OPT_HOST_SETUP) { *value = c->host_setup; return ISL_OK; }
     if (key == ISL_OPT_SCALAR_SLOTS) { *value = c->ss_nslot; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
 }

@@ -131,6 +131,7 @@ struct isl_ctx {
     std::vector<int64_t> hedof;  // [nelem][nfun]
     std::vector<std::pair<int64_t, int>> bf_cache;  // boundary (element, face) list of the current mesh
     bool bf_valid = false;
+    bool host_setup = false;     // DOF numbering and boundary detection on the host even with a device
     isl::DBuf<int32_t> dedof;    // SoA [nfun][nelem]
     std::vector<uint8_t> status; // per dofobj comp: 0 active, 1 constrained
     std::vector<double> cval;
@@ -181,8 +182,8 @@ struct isl_ctx {
     int mesh_affine = -1;        // every element a parallelepiped / parallelogram (-1: not yet checked)
     int use_persist = 1;         // one-launch CG kernels: 0 never, 1 for small systems, 2 always where supported
     int cluster_size = -1;       // CTAs of the small-system cluster solve (-1: not yet probed, 0: unavailable)
-    int persist_grid = -1;
-    bool barrier_test = false;   // test hook: the next persistent launch finds its grid barrier pre-armed (never completes)       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)
+    int persist_grid = -1;       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)
+    bool barrier_test = false;   // test hook: the next persistent launch finds its grid barrier pre-armed (never completes)
     isl::DBuf<unsigned int> dbar; // grid barrier of the persistent kernel: arrivals, generation
     int64_t nbr = 0, nblk = 0;
     isl::DBuf<int32_t> dbptr, dbcol, dbrow;
@@ -265,6 +266,16 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
 int time_kernels(isl_ctx* c, int nrep, double* ms);
 int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
 int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
+// One level of n-faces for the device DOF numbering: nfc faces per element of
+// w vertices each (w = 0: the cell itself, not grouped), `stride` DOFs per
+// face starting at local DOF position `begin`.
+struct DeviceLevel {
+    int nfc = 0, w = 0, stride = 0, begin = 0;
+    int v[12][4] = {};
+};
+bool device_setup_fits(const isl_ctx* c, int nfc);
+int device_dofobj_numbering(isl_ctx* c, const std::vector<DeviceLevel>& levels, int nf);
+int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t>& slots);
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 }  // namespace isl
