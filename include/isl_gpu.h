@@ -170,6 +170,23 @@ int isl_norm(isl_ctx* ctx, double* out);
  * (base/dof/Distribute.hpp:139-215) */
 int isl_distribute(isl_ctx* ctx, int add);
 
+/* Post-processing (base/post/ErrorNorm.hpp).  The reference evaluates a host
+ * function of x at every quadrature point; here the caller evaluates it at the
+ * points isl_quadrature_points returns and passes the table.
+ * isl_quadrature_points: physical coordinates x[(e*nq + q)*dim + d] of the
+ * points of Quadrature<quad_degree, SHAPE> (base/Quadrature.hpp:132-141) on
+ * every element, x = sum_i N_i(xi_q) X_i; x NULL: only *n_points = nelem*nq.
+ * isl_error_norm: base::post::errorComputation<order>
+ * (base/post/ErrorNorm.hpp:84-123, functor :300-330) for the field's current
+ * values (isl_set_values / isl_distribute):
+ *   order 0: ref[(e*nq + q)*ncomp + c] = u_c(x_eq); *error = L2 norm of u - u_h
+ *   order 1: ref[((e*nq + q)*ncomp + c)*dim + d] = d u_c / d x_d;
+ *            *error = H1 semi-norm of u - u_h
+ * i.e. sqrt(sum_e sum_q |ref - approx|^2 detJ w), detJ signed as the
+ * reference.  Computed on the device; reproducible bit for bit. */
+int isl_quadrature_points(isl_ctx* ctx, int quad_degree, int64_t* n_points, double* x);
+int isl_error_norm(isl_ctx* ctx, int order, int quad_degree, const double* ref, double* error);
+
 /* Assembled CSR (int64 row pointers / column ids, FP64 values) for parity. */
 int isl_get_csr(isl_ctx* ctx, int64_t* rowptr, int64_t* colind, double* values);
 

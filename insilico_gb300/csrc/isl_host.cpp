@@ -944,6 +944,20 @@ int isl_distribute(isl_ctx* c, int add) {
     return st;
 }
 
+int isl_quadrature_points(isl_ctx* c, int quad_degree, int64_t* n_points, double* x) {
+    if (!c || !c->fedeg || !n_points) return ISL_ERR_ARG;
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: post-processing runs on the device");
+    cudaSetDevice(c->device);
+    return isl::quadrature_points_device(c, quad_degree, n_points, x);
+}
+
+int isl_error_norm(isl_ctx* c, int order, int quad_degree, const double* ref, double* error) {
+    if (!c || !c->fedeg || !ref || !error || (order != 0 && order != 1)) return ISL_ERR_ARG;
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: post-processing runs on the device");
+    cudaSetDevice(c->device);
+    return isl::error_norm_device(c, order, quad_degree, ref, error);
+}
+
 int isl_get_csr(isl_ctx* c, int64_t* rowptr, int64_t* colind, double* values) {
     if (!c || !c->pattern_ready) return ISL_ERR_ARG;
     if (c->neq == 0) {

@@ -274,6 +274,8 @@ struct DeviceLevel {
     int v[12][4] = {};
 };
 bool device_setup_fits(const isl_ctx* c, int nfc);
+int quadrature_points_device(isl_ctx* c, int qdeg, int64_t* n, double* x);
+int error_norm_device(isl_ctx* c, int order, int qdeg, const double* ref, double* err);
 int device_dofobj_numbering(isl_ctx* c, const std::vector<DeviceLevel>& levels, int nf);
 int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t>& slots);
 bool spmv32_kind_valid(const isl_ctx* c, int kind);

@@ -187,6 +187,23 @@ class System:
     def distribute(self, add: bool = False):
         self._chk(self.L.isl_distribute(self.h, int(add)), "isl_distribute")
 
+    # -- post-processing (base/post/ErrorNorm.hpp) -----------------------------
+    def quadrature_points(self, quad_degree: int) -> np.ndarray:
+        """Physical coordinates of the quadrature points, [nelem * nq, dim]."""
+        n = C.c_int64()
+        self._chk(self.L.isl_quadrature_points(self.h, quad_degree, C.byref(n), None), "isl_quadrature_points")
+        x = np.zeros((n.value, self.dim))
+        self._chk(self.L.isl_quadrature_points(self.h, quad_degree, C.byref(n), A.d(x)), "isl_quadrature_points")
+        return x
+
+    def error_norm(self, order: int, quad_degree: int, ref) -> float:
+        """errorComputation<order> against ref tabulated at quadrature_points():
+        order 0 [npoints, ncomp] values, order 1 [npoints, ncomp, dim] gradients."""
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        v = C.c_double()
+        self._chk(self.L.isl_error_norm(self.h, order, quad_degree, A.d(r), C.byref(v)), "isl_error_norm")
+        return v.value
+
     def csr(self, values: bool = True):
         rp = np.zeros(self.neq + 1, dtype=np.int64)
         ci = np.zeros(self.nnz, dtype=np.int64)
