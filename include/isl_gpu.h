@@ -187,6 +187,28 @@ int isl_distribute(isl_ctx* ctx, int add);
 int isl_quadrature_points(isl_ctx* ctx, int quad_degree, int64_t* n_points, double* x);
 int isl_error_norm(isl_ctx* ctx, int order, int quad_degree, const double* ref, double* error);
 
+/* Mesh and field I/O with the reference's text layouts; every host thread
+ * converts numbers (the file is cut at line boundaries).
+ * isl_mesh_read_smf: base::io::smf::readMesh (base/io/smf/Reader.hpp:36-41,
+ * 98-313) followed by isl_mesh_upload: the header must name the shape
+ * ("! elementShape", matched as a lower-case substring) and its node count
+ * ("! elementNumPoints"); "#" comment lines around the header; "!
+ * externalNodes" / "! externalElements" files opened as given; per node line
+ * the first dim numbers, per element line the 0-based node indices in file
+ * order.  Errors: ISL_ERR_ARG with the reference's messages.
+ * isl_mesh_get: counts and host copies of the mesh (either array may be NULL).
+ * isl_mesh_write_smf: base::io::smf::writeMesh (base/io/smf/Writer.hpp:60-140).
+ * isl_write_vtk: base::io::vtk::LegacyWriter (base/io/vtk/LegacyWriter.hpp)
+ * writeUnstructuredGrid, then, when point_name is given, writePointData of
+ * the field's current values at the geometry nodes, and, when cell_name is
+ * given, writeCellData of cell_values: per cell a cell_rows x cell_cols
+ * matrix (row-major, at most 3 x 3) or, with 0 x 0, one plain double. */
+int isl_mesh_read_smf(isl_ctx* ctx, const char* path, int shape);
+int isl_mesh_get(isl_ctx* ctx, int64_t* n_nodes, int64_t* n_elem, double* coords, int64_t* conn);
+int isl_mesh_write_smf(isl_ctx* ctx, const char* path);
+int isl_write_vtk(isl_ctx* ctx, const char* path, const char* point_name, const char* cell_name, int cell_rows,
+                  int cell_cols, const double* cell_values);
+
 /* Assembled CSR (int64 row pointers / column ids, FP64 values) for parity. */
 int isl_get_csr(isl_ctx* ctx, int64_t* rowptr, int64_t* colind, double* values);
 

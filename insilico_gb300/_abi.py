@@ -40,7 +40,7 @@ EXPORTED = [
     "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc", "isl_quadrature_points",
-    "isl_error_norm",
+    "isl_error_norm", "isl_mesh_read_smf", "isl_mesh_get", "isl_mesh_write_smf", "isl_write_vtk",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP) = 0, 1, 2, 3, 4, 5, 6, 7, 8
@@ -103,6 +103,10 @@ def load(build_if_missing: bool = False):
     L.isl_distribute.argtypes = [_P, i]
     L.isl_quadrature_points.argtypes = [_P, i, _I64, _D]
     L.isl_error_norm.argtypes = [_P, i, i, _D, _D]
+    L.isl_mesh_read_smf.argtypes = [_P, C.c_char_p, i]
+    L.isl_mesh_get.argtypes = [_P, _I64, _I64, _D, _I64]
+    L.isl_mesh_write_smf.argtypes = [_P, C.c_char_p]
+    L.isl_write_vtk.argtypes = [_P, C.c_char_p, C.c_char_p, C.c_char_p, i, i, _D]
     L.isl_get_csr.argtypes = [_P, _I64, _I64, _D]
     L.isl_sync.argtypes = [_P]
     L.isl_set_timing.argtypes = [_P, i]

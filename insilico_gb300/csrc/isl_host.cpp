@@ -860,6 +860,10 @@ int isl_set_values(isl_ctx* c, const double* u) {
     const size_t n = (size_t)c->ndofobj * c->ncomp;
     c->u_nonzero = false;
     for (size_t i = 0; i < n; ++i) if (u[i] != 0.0) { c->u_nonzero = true; break; }
+    if (c->device < 0) {  // host-only context: the values stay on the host (I/O)
+        c->hu.assign(u, u + n);
+        return ISL_OK;
+    }
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->du.p, u, n * 8, cudaMemcpyHostToDevice, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
@@ -868,6 +872,11 @@ int isl_set_values(isl_ctx* c, const double* u) {
 int isl_get_values(isl_ctx* c, double* u) {
     if (!c || !c->fedeg || !u) return ISL_ERR_ARG;
     const size_t n = (size_t)c->ndofobj * c->ncomp;
+    if (c->device < 0) {
+        if (c->hu.size() != n) return ISL_ERR_ARG;
+        std::copy(c->hu.begin(), c->hu.end(), u);
+        return ISL_OK;
+    }
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(u, c->du.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;

@@ -187,6 +187,35 @@ class System:
     def distribute(self, add: bool = False):
         self._chk(self.L.isl_distribute(self.h, int(add)), "isl_distribute")
 
+    # -- mesh / field I/O (base/io/smf, base/io/vtk) ---------------------------
+    def read_smf(self, path: str, shape: int):
+        """smf::readMesh into the context (replaces upload_mesh)."""
+        self._chk(self.L.isl_mesh_read_smf(self.h, str(path).encode(), shape), "isl_mesh_read_smf")
+        nn, ne = C.c_int64(), C.c_int64()
+        self._chk(self.L.isl_mesh_get(self.h, C.byref(nn), C.byref(ne), None, None), "isl_mesh_get")
+        dim = 2 if shape == A.QUAD else 3
+        X = np.zeros((nn.value, dim))
+        conn = np.zeros((ne.value, 8 if shape == A.HEX else 4), dtype=np.int64)
+        self._chk(self.L.isl_mesh_get(self.h, None, None, A.d(X), A.i64(conn)), "isl_mesh_get")
+        self.X, self.conn, self.shape, self.dim = X, conn, shape, dim
+        return X, conn
+
+    def write_smf(self, path: str):
+        self._chk(self.L.isl_mesh_write_smf(self.h, str(path).encode()), "isl_mesh_write_smf")
+
+    def write_vtk(self, path: str, point_name=None, cell_name=None, cell_values=None):
+        """LegacyWriter: grid, the field's values at the nodes (point_name), and
+        per-cell data: [ncells] plain scalars or [ncells, r, c] matrices."""
+        rows = cols = 0
+        cv = None
+        if cell_name is not None:
+            cv = np.ascontiguousarray(cell_values, dtype=np.float64)
+            if cv.ndim == 3:
+                rows, cols = cv.shape[1], cv.shape[2]
+        self._chk(self.L.isl_write_vtk(self.h, str(path).encode(), point_name.encode() if point_name else None,
+                                       cell_name.encode() if cell_name else None, rows, cols,
+                                       A.d(cv) if cv is not None else None), "isl_write_vtk")
+
     # -- post-processing (base/post/ErrorNorm.hpp) -----------------------------
     def quadrature_points(self, quad_degree: int) -> np.ndarray:
         """Physical coordinates of the quadrature points, [nelem * nq, dim]."""

@@ -313,9 +313,10 @@ def linear_elastic(dim: int, X, conn, E=1000.0, nu=0.25):
 
 
 def compressible(X, conn, E=1000.0, nu=0.3, max_iter=30, load_steps=5, pull=3.0, traction=1000.0,
-                 disp_controlled=True, tolerance=1e-12):
+                 disp_controlled=True, tolerance=1e-12, return_values=False):
     """Newton history of reference/06-elastic/compressible.cpp (2-D, Q2,
-    NeoHookeanCompressible, PulledSheet boundary conditions)."""
+    NeoHookeanCompressible, PulledSheet boundary conditions); with
+    return_values, also the final DOF values [ndofobj * 2]."""
     lam, mu = lame(E, nu)
     P = Problem(QUAD, X, conn, 2, 2)
     first_pull = pull / load_steps
@@ -354,6 +355,8 @@ def compressible(X, conn, E=1000.0, nu=0.3, max_iter=30, load_steps=5, pull=3.0,
             it += 1
             if conv2 < tolerance:
                 break
+    if return_values:
+        return neq, rows, P.values()
     return neq, rows
 
 

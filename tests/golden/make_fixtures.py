@@ -14,6 +14,8 @@ Pins extracted (file paths relative to the reference project):
   reference/06-elastic/compRefOut{D,N}.dat           -> Newton history tables
   reference/05-mixedPoisson/ref                      -> ndofs, L2, H1
   reference/05-mixedPoisson/square_020.smf           -> canonical mesh hash
+  reference/06-elastic/quad.020.{D,N}ref.vtk         -> sha256 + count of the grid lines and of
+                                                        the POINT_DATA section lines
 """
 import glob
 import hashlib
@@ -50,6 +52,22 @@ def read_smf(path):
     X = np.array([[float(t) for t in l.split()] for l in lines[1:1 + nn]])
     conn = np.array([[int(t) for t in l.split()] for l in lines[1 + nn:1 + nn + ne]], dtype=np.int64)
     return X, conn
+
+
+def canon_lines(lines, zero=1e-10):
+    """Lines with every number of magnitude below `zero` written as "~0": the
+    round-off residue of quantities that vanish (e.g. a displacement on a
+    symmetry line) differs between builds, everything else is kept verbatim."""
+    out = []
+    for l in lines:
+        toks = []
+        for t in l.split(" "):
+            try:
+                toks.append("~0" if t and abs(float(t)) < zero else t)
+            except ValueError:
+                toks.append(t)
+        out.append(" ".join(toks))
+    return out
 
 
 def table(path):
@@ -91,6 +109,17 @@ def main(ref):
         txt = f.read().splitlines()
     out["mixedPoisson"] = {"ndofs": int(txt[0].split()[-1]), "L2": float(txt[1].split()[-1]),
                            "H1": float(txt[2].split()[-1]), "volume": float(txt[3].split()[-1])}
+    out["vtk"] = {}
+    for tag in ("D", "N"):
+        rel = "reference/06-elastic/quad.020.%sref.vtk" % tag
+        with open(os.path.join(ref, rel)) as f:
+            lines = f.read().splitlines()
+        ip = next(i for i, l in enumerate(lines) if l.startswith("POINT_DATA"))
+        ic = next((i for i, l in enumerate(lines) if l.startswith("CELL_DATA")), len(lines))
+        out["vtk"][tag] = {"file": rel, "grid_lines": ip, "grid_sha256": lines_hash(lines[:ip]),
+                           "point_lines": ic - ip, "point_sha256": lines_hash(lines[ip:ic]),
+                           "point_canon_sha256": lines_hash(canon_lines(lines[ip:ic])),
+                           "point_head": lines[ip:ip + 4]}
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_pins.json"))

@@ -1,0 +1,136 @@
+"""SMF and legacy VTK I/O of the product (host-only contexts, no GPU): the
+reference's text layouts, pinned to the reference's fixture meshes (mesh
+hashes) and to its VTK golden files of reference/06-elastic (SHA-256 of the
+grid lines and of the POINT_DATA section)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle as O
+from insilico_gb300 import _abi as A
+from insilico_gb300.system import System
+
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+from make_fixtures import canon_lines, lines_hash, mesh_hash  # noqa: E402
+
+
+def _pad3(X):
+    Y = np.zeros((len(X), 3))
+    Y[:, : X.shape[1]] = X
+    return Y
+
+
+def _host(shape, X, conn):
+    S = System(device=-1)
+    S.upload_mesh(shape, X, conn)
+    return S
+
+
+@pytest.mark.parametrize("rel,kind,n", [
+    ("reference/03-doFHandler/square_20.smf", "quad", 20), ("reference/06-elastic/quad.040.smf", "quad", 40),
+    ("reference/06-elastic/cube.008.smf", "hex", 8), ("reference/06-elastic/cube.016.smf", "hex", 16),
+])
+def test_smf_write_read_round_trip_matches_reference_meshes(pins, tmp_path, rel, kind, n):
+    """writeMesh then readMesh reproduces the reference's fixture mesh exactly"""
+    shape = A.QUAD if kind == "quad" else A.HEX
+    X, conn = O.unitcube(kind, *([n] * (2 if kind == "quad" else 3)), round6=True)
+    path = tmp_path / "m.smf"
+    _host(shape, X, conn).write_smf(path)
+    text = path.read_text().splitlines()
+    assert text[0] == "! elementShape " + ("quadrilateral" if kind == "quad" else "hexahedron")
+    assert text[2] == f"{len(X)}  {len(conn)}"
+    S = System(device=-1)
+    Y, c2 = S.read_smf(path, shape)
+    np.testing.assert_array_equal(c2, conn)
+    assert np.array_equal(Y, X)
+    got = mesh_hash(_pad3(Y) if kind == "quad" else Y, c2)
+    assert got == pins["meshes"][rel]["sha256"]
+
+
+def test_smf_reader_header_rules_and_external_files(tmp_path):
+    """comments around the header, header lines in any order, trailing tokens
+    ignored, external node and element files; the oracle's reading of the
+    same mesh agrees"""
+    X, conn = O.unitcube("quad", 3, 2)
+    nodes = "".join(f"{float(x[0])!r} {float(x[1])!r} 0 extra\n" for x in X)
+    elems = "".join(" ".join(str(v) for v in c) + "\n" for c in conn)
+    body = f"{len(X)} {len(conn)} trailing\n"
+    text = "# a comment\n! elementNumPoints 4\n! elementShape Quadrilateral_2D\n# after\n" + body + nodes + elems
+    p = tmp_path / "a.smf"
+    p.write_text(text)
+    S = System(device=-1)
+    Y, c2 = S.read_smf(p, A.QUAD)
+    assert np.array_equal(Y, X)
+    np.testing.assert_array_equal(c2, conn)
+    Xo, co = O.read_smf_text(text.replace(" extra", "").replace(" trailing", ""))
+    assert np.array_equal(Xo[:, :2], Y) and np.array_equal(co, c2)
+    (tmp_path / "n.xyz").write_text(nodes)
+    (tmp_path / "e.txt").write_text(elems)
+    q = tmp_path / "b.smf"
+    q.write_text(f"! elementShape quadrilateral\n! elementNumPoints 4\n! externalNodes {tmp_path / 'n.xyz'}\n"
+                 f"! externalElements {tmp_path / 'e.txt'}\n{len(X)} {len(conn)}\n")
+    Y2, c3 = System(device=-1).read_smf(q, A.QUAD)
+    assert np.array_equal(Y2, X) and np.array_equal(c3, conn)
+
+
+@pytest.mark.parametrize("header", [
+    "! elementShape hexahedron\n! elementNumPoints 4\n",      # wrong shape
+    "! elementShape quadrilateral\n! elementNumPoints 9\n",   # wrong node count
+    "! elementShape quadrilateral\n",                         # missing elementNumPoints
+])
+def test_smf_reader_rejects_bad_headers(tmp_path, header):
+    p = tmp_path / "bad.smf"
+    p.write_text(header + "4 1\n0 0 0\n1 0 0\n1 1 0\n0 1 0\n0 1 2 3\n")
+    with pytest.raises(A.IslError):
+        System(device=-1).read_smf(p, A.QUAD)
+
+
+@pytest.mark.parametrize("tag,disp,trac", [("D", True, 1000.0), ("N", False, 300.0)])
+def test_vtk_matches_reference_golden(pins, tmp_path, tag, disp, trac):
+    """LegacyWriter output of reference/06-elastic/compressible.cpp's final
+    load step (quad.020.0005.vtk, compared against quad.020.{D,N}ref.vtk):
+    the grid lines and the displacement POINT_DATA section, bit for bit up to
+    round-off zeros (the vertical displacement on the x axis of the pulled
+    sheet is 1e-17 here and 1e-14 in the reference's build; both print as
+    noise).  The traction-controlled run matches without that allowance."""
+    pin = pins["vtk"][tag]
+    X, conn = O.unitcube("quad", 20, 20, round6=True)
+    _, _, u = O.compressible(X, conn, traction=trac, disp_controlled=disp, return_values=True)
+    S = _host(A.QUAD, X, conn)
+    S.create_field(2, 2)
+    S.set_values(u)
+    path = tmp_path / "out.vtk"
+    S.write_vtk(path, point_name="disp")
+    lines = path.read_text().splitlines()
+    ip = pin["grid_lines"]
+    assert lines[ip] == "POINT_DATA 441"
+    assert lines_hash(lines[:ip]) == pin["grid_sha256"]
+    assert lines[ip:ip + 4] == pin["point_head"]
+    assert len(lines) - ip == pin["point_lines"]
+    assert lines_hash(canon_lines(lines[ip:])) == pin["point_canon_sha256"]
+    if tag == "N":
+        assert lines_hash(lines[ip:]) == pin["point_sha256"]
+
+
+def test_vtk_cell_data_layouts(tmp_path):
+    """cell data: plain doubles, vectors and 2x2 / 3x3 tensors padded to 3-D as
+    base/io/raw/ascii.hpp:24-49 writes them"""
+    X, conn = O.unitcube("quad", 2, 1)
+    S = _host(A.QUAD, X, conn)
+    S.create_field(1, 1)
+    S.set_values(np.arange(len(X), dtype=float) * 0.5)
+    p = tmp_path / "c.vtk"
+    S.write_vtk(p, point_name="u", cell_name="s", cell_values=np.array([1.5, -2.0]))
+    t = p.read_text().splitlines()
+    i = t.index("POINT_DATA 6")
+    assert t[i + 1:i + 4] == ["SCALARS u float ", "LOOKUP_TABLE default ", "0 "]
+    j = t.index("CELL_DATA 2")
+    assert t[j + 1:] == ["SCALARS s float ", "LOOKUP_TABLE default ", "1.5", "-2"]
+    S.write_vtk(p, cell_name="sig", cell_values=np.array([[[1.0, 2.0], [3.0, 4.0]], [[5.0, 6.0], [7.0, 8.0]]]))
+    t = p.read_text().splitlines()
+    j = t.index("CELL_DATA 2")
+    assert t[j + 1:] == ["TENSORS sig float ", "1 2 0 3 4 0 0 0 0 ", "5 6 0 7 8 0 0 0 0 "]
+    assert t[t.index("CELLS 2 10") + 1] == "4 0 1 4 3 "
+    assert t[t.index("CELL_TYPES 2") + 1] == "9"
