@@ -304,6 +304,74 @@ def run_serve(args, rank, world, local, pg):
 W_SEED_WARM = 0x15111C0 + 40
 
 
+def run_heat(args, rank, world, local, pg):
+    """heat: nonlinear heat conduction (heat::Static, FenicsTest conductivity
+    (1 + u)^3) on the n x n unit square in Q2; n = 200 is the square_200 mesh of
+    reference/04-heat/nonlinearHeat.cpp.  One step is the whole Newton run from
+    u = 0: assemble the non-symmetric tangent and the residual, BiCGSTAB to
+    1e-13, add the increment (4 assemblies, 3 solves)."""
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import workloads as W
+    from insilico_gb300.system import System
+    A.load(build_if_missing=True)
+    n = args.n or 200
+    X, conn = W.unit_cube("quad", n, n)
+    S = System(device=local)
+    t0 = time.perf_counter()
+    ndofs = W.heat_setup(S, X, conn)
+    t_setup = time.perf_counter() - t0
+    zeros = np.zeros(S.ndofobj)
+
+    def step():
+        S.set_values(zeros)
+        return W.heat_newton(S, ndofs)
+    for _ in range(max(3, args.warmup)):
+        rows = step()
+    S.sync()
+    clk = Clocks(local)
+    l0 = S.launch_count()
+    S.set_timing(True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rows = step()
+        S.sync()
+        times.append(time.perf_counter() - t0)
+    ms, cnt = S.timings()
+    S.set_timing(False)
+    clocks = clk.stop()
+    launches = S.launch_count() - l0
+    s_step = max_over_ranks(float(np.median(times)), pg)
+    newton = len(rows) - 1
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle as O
+        t0 = time.perf_counter()
+        nc, rows_c, _, _ = O.nonlinear_heat(X, conn)
+        tc = time.perf_counter() - t0
+        cpu = {"value": nc / tc, "unit": "DOF/s", "cores": 1, "kind": "port",
+               "sample": f"the whole Newton run on the same {n}x{n} Q2 mesh: oracle assembly (1 thread) + "
+                         f"scipy SuperLU of the non-symmetric tangent, {len(rows_c) - 1} iterations, {tc:.1f} s"}
+    line = {"metric": "nonlinear heat Newton run (heat::Static, BiCGSTAB) DOF/s", "value": ndofs * world / s_step,
+            "unit": "DOF/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": s_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (unit square; no dataset)",
+            "config": {"workload": f"heat: Q2 heat::Static FenicsTest m=3 on the {n}x{n} unit square, u=0 at x=0, "
+                                   f"u=1 at x=1, Newton to 1e-8, BiCGSTAB (Jacobi) to 1e-13",
+                       "dofs": int(ndofs), "elements": int(len(conn)), "parallelism": "single",
+                       "l2": "matrix and vectors resident; per step the DOF values are reset from the host"},
+            "newton_iters": newton, "residuals": [r[1] for r in rows], "setup_s": t_setup,
+            "phase_ms_per_step": {"element": ms[A.T_ELEMENT] / args.steps, "gather": ms[A.T_GATHER] / args.steps,
+                                  "solve": ms[A.T_SOLVE] / args.steps},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ndofs * world / s_step, "unit": "DOF/s", "h2d_bytes_per_step": int(zeros.nbytes),
+                    "d2h_bytes_per_step": int(2 * newton * ndofs * 8 + ndofs * 8)},
+            "clocks": clocks, "gpu_launches": int(launches // max(1, args.steps))}
+    S.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def batch_instances(count, seed):
     """c4 instances: side U{8..256}, degree Q1/Q2 with p = 0.5, per instance
     kappa_e = exp(N(0, 0.5)) and nodal source U[0, 1] (seeded streams)."""
@@ -455,9 +523,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=0, help="mesh size (default: the workload's own, 64)")
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "heat"],
                     help="c2 (default, the headline): hex8 elasticity 64^3; c1: Q1 Poisson 64^2; c3: tet10 Poisson "
-                         "64^3; c4: 4096 batched Q1/Q2 Poisson instances; c5: served neo-Hookean Newton requests")
+                         "64^3; c4: 4096 batched Q1/Q2 Poisson instances; c5: served neo-Hookean Newton requests; "
+                         "heat: nonlinear heat Newton run (heat::Static, BiCGSTAB), square 200")
     ap.add_argument("--requests", type=int, default=48, help="c5: requests per run")
     ap.add_argument("--slots", type=int, default=8, help="c5: server slots")
     ap.add_argument("--instances", type=int, default=4096, help="c4: batched instances")
@@ -480,6 +549,8 @@ def main():
         pg = dist
     if args.workload == "c5":
         run_serve(args, rank, world, local, pg)
+    elif args.workload == "heat":
+        run_heat(args, rank, world, local, pg)
     elif args.workload == "c4":
         run_batch(args, rank, world, local, pg)
     else:

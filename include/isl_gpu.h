@@ -46,13 +46,15 @@ typedef enum {
  * base/mesh/HierarchicOrder.hpp) */
 enum { ISL_QUAD = 3, ISL_TET = 4, ISL_HEX = 5 };
 /* kernel functors */
-enum { ISL_KERNEL_LAPLACE = 0, ISL_KERNEL_HYPERELASTIC = 1 };
+enum { ISL_KERNEL_LAPLACE = 0, ISL_KERNEL_HYPERELASTIC = 1, ISL_KERNEL_HEAT_STATIC = 2 };
 /* materials of solid::HyperElastic */
 enum { ISL_MAT_STVENANT = 0, ISL_MAT_NEOHOOKE = 1 };
+/* mat::thermal materials of heat::Static: IsotropicConstant, FenicsTest */
+enum { ISL_THERMAL_CONSTANT = 0, ISL_THERMAL_FENICS = 1 };
 /* arithmetic of the element kernels and of the stored matrix */
 enum { ISL_PREC_FP64 = 0, ISL_PREC_FP32 = 1, ISL_PREC_MIXED = 2 };
 /* solve methods */
-enum { ISL_SOLVE_CG_FP64 = 0, ISL_SOLVE_CG_FP32_IR = 1 };
+enum { ISL_SOLVE_CG_FP64 = 0, ISL_SOLVE_CG_FP32_IR = 1, ISL_SOLVE_BICGSTAB = 2 };
 /* phase timers reported by isl_timings (milliseconds, CUDA events) */
 enum { ISL_T_ELEMENT = 0, ISL_T_GATHER = 1, ISL_T_SOLVE = 2, ISL_T_SPMV = 3, ISL_T_PATTERN = 4, ISL_NTIMERS = 8 };
 
@@ -125,6 +127,14 @@ int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
  * quad_degree: base::Quadrature<DEG,SHAPE> degree (base/Quadrature.hpp:113-143). */
 int isl_set_laplace(isl_ctx* ctx, const double* kappa /* [n_elem] */, int quad_degree);
 int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const double* mu, int quad_degree);
+/* heat::Static (heat/Static.hpp:98-225), the nonlinear heat conduction kernel,
+ * with an isotropic mat::thermal material per element: ISL_THERMAL_CONSTANT
+ * (IsotropicConstant, param = conductivity) or ISL_THERMAL_FENICS
+ * (FenicsTest, K(u) = (1 + u)^m, param = m; mat/thermal/FenicsTest.hpp).
+ * Scalar fields.  Its tangent is not symmetric: the element matrices are
+ * staged whole (the contribution lists are rebuilt once, at the next
+ * isl_assemble) and the system is solved with ISL_SOLVE_BICGSTAB. */
+int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_elem] */, int quad_degree);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
 int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] */);
@@ -157,6 +167,12 @@ int isl_assemble(isl_ctx* ctx, int precision, int incremental, int with_residual
  *                         an ISL_PREC_FP32 assembly (no FP64 matrix) it is a
  *                         plain FP32 CG on the iterated residual, the inexact
  *                         linear solve of a Newton step whose residual is FP64.
+ *   ISL_SOLVE_BICGSTAB  : FP64 BiCGSTAB for non-symmetric systems (the
+ *                         recurrences of Eigen 3.2's BiCGSTAB, which the
+ *                         reference's biCGStabSolve calls,
+ *                         base/solver/Eigen3.hpp:277-289), with a Jacobi
+ *                         preconditioner instead of IncompleteLUT; x0 = 0,
+ *                         ||r|| <= tol ||b||.
  * max_iter <= 0 means 2N.  iters/rel_res may be NULL. */
 int isl_solve(isl_ctx* ctx, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res);
 

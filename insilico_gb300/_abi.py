@@ -14,10 +14,11 @@ from . import build as _build
  ISL_ERR_CAPACITY) = range(9)
 NOALLOC_MAX_N = 65536  # ISL_NOALLOC_MAX_N
 QUAD, TET, HEX = 3, 4, 5
-KERNEL_LAPLACE, KERNEL_HYPERELASTIC = 0, 1
+KERNEL_LAPLACE, KERNEL_HYPERELASTIC, KERNEL_HEAT_STATIC = 0, 1, 2
 MAT_STVENANT, MAT_NEOHOOKE = 0, 1
+THERMAL_CONSTANT, THERMAL_FENICS = 0, 1
 PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
-SOLVE_CG_FP64, SOLVE_CG_FP32_IR = 0, 1
+SOLVE_CG_FP64, SOLVE_CG_FP32_IR, SOLVE_BICGSTAB = 0, 1, 2
 T_ELEMENT, T_GATHER, T_SOLVE, T_SPMV, T_PATTERN, NTIMERS = 0, 1, 2, 3, 4, 8
 
 _STATUS = {
@@ -41,6 +42,7 @@ EXPORTED = [
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc", "isl_quadrature_points",
     "isl_error_norm", "isl_mesh_read_smf", "isl_mesh_get", "isl_mesh_write_smf", "isl_write_vtk",
+    "isl_set_heat_static",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP) = 0, 1, 2, 3, 4, 5, 6, 7, 8
@@ -104,6 +106,7 @@ def load(build_if_missing: bool = False):
     L.isl_quadrature_points.argtypes = [_P, i, _I64, _D]
     L.isl_error_norm.argtypes = [_P, i, i, _D, _D]
     L.isl_mesh_read_smf.argtypes = [_P, C.c_char_p, i]
+    L.isl_set_heat_static.argtypes = [_P, i, _D, i]
     L.isl_mesh_get.argtypes = [_P, _I64, _I64, _D, _I64]
     L.isl_mesh_write_smf.argtypes = [_P, C.c_char_p]
     L.isl_write_vtk.argtypes = [_P, C.c_char_p, C.c_char_p, C.c_char_p, i, i, _D]

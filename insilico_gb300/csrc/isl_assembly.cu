@@ -204,6 +204,114 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 }
 
 // ---------------------------------------------------------------------------
+// heat::Static element kernel (heat/Static.hpp:98-225), one thread per element,
+// with the isotropic materials of mat/thermal: IsotropicConstant (K = k I,
+// K' = 0) and FenicsTest (K = (1 + u)^m I, K' = m (1 + u)^(m-1) I,
+// mat/thermal/FenicsTest.hpp:47-60).  The tangent is not symmetric, so the
+// whole NF x NF matrix is staged (element-major, stage[e NF^2 + i NF + j]):
+//   K[i][j] += detJ w sum_K (g_iK k g_jK + g_iK k' gu_K phi_j)
+//   F[i]    -= detJ w sum_K g_iK k gu_K                (residual, x -1)
+//   F[s]    += f(x) phi_s w detJ                        (body force)
+template <int SHAPE, int FDEG, int NQ>
+__global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T) {
+    constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.nelem) return;
+    const int E = A.nelem;
+    double X[NG][D];
+    int nodes[NG];
+#pragma unroll
+    for (int i = 0; i < NG; ++i) {
+        nodes[i] = A.conn[i * E + e];
+#pragma unroll
+        for (int d = 0; d < D; ++d) X[i][d] = A.X[(size_t)nodes[i] * D + d];
+    }
+    const double prm = A.coef[e];
+    double uloc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) uloc[f] = A.u[A.edof[f * E + e]];
+    double K[NF][NF];
+#pragma unroll
+    for (int i = 0; i < NF; ++i)
+#pragma unroll
+        for (int j = 0; j < NF; ++j) K[i][j] = 0.0;
+    double fe[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) fe[f] = 0.0;
+    bool bad = false;
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+        double Ji[D][D];
+        const double detJ = jac<NG, D>(X, T.dN[q], Ji);
+        bad |= !(detJ > 0.0);
+        double g[NF][D];
+#pragma unroll
+        for (int M = 0; M < NF; ++M)
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double s = 0.0;
+#pragma unroll
+                for (int b = 0; b < D; ++b) s += Ji[a][b] * T.dphi[q][M][b];
+                g[M][a] = s;
+            }
+        double u = 0.0, gu[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) gu[k] = 0.0;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            u += T.phi[q][f] * uloc[f];
+#pragma unroll
+            for (int k = 0; k < D; ++k) gu[k] += g[f][k] * uloc[f];
+        }
+        double k0, k1;
+        if (A.material == ISL_THERMAL_FENICS) {
+            k0 = pow(1.0 + u, prm);
+            k1 = prm * pow(1.0 + u, prm - 1.0);
+        } else {
+            k0 = prm;
+            k1 = 0.0;
+        }
+        const double dw = detJ * T.w[q];
+#pragma unroll
+        for (int i = 0; i < NF; ++i)
+#pragma unroll
+            for (int j = 0; j < NF; ++j) {
+                double entry = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    entry += g[i][k] * k0 * g[j][k];
+                    entry += g[i][k] * k1 * gu[k] * T.phi[q][j];
+                }
+                K[i][j] += dw * entry;
+            }
+        if (A.with_residual) {
+#pragma unroll
+            for (int i = 0; i < NF; ++i) {
+                double sum = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) sum += g[i][k] * k0 * gu[k];
+                fe[i] -= sum * dw;
+            }
+        }
+        if (A.fnodal) {
+            double f = 0.0;
+#pragma unroll
+            for (int i = 0; i < NG; ++i) f += T.N[q][i] * A.fnodal[nodes[i]];
+#pragma unroll
+            for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
+        }
+    }
+    if (bad) atomicOr(A.flags, 1);
+    double* SK = (double*)A.stageK;
+#pragma unroll
+    for (int i = 0; i < NF; ++i)
+#pragma unroll
+        for (int j = 0; j < NF; ++j) SK[((size_t)e * NF + i) * NF + j] = K[i][j];
+#pragma unroll
+    for (int s = 0; s < NF; ++s) A.stageF[(size_t)s * E + e] = fe[s];
+}
+
+// ---------------------------------------------------------------------------
 // solid::HyperElastic on trilinear hexahedra, 2x2x2 quadrature.
 // 8 threads per element: in phase 1 thread q evaluates quadrature point q
 // (geometry, deformation, stress, effective elasticity), in phase 2 thread M
@@ -633,7 +741,7 @@ __global__ void k_neumann(const FaceArgs<NF, NCOMP> A) {
 template <typename R>
 __global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun, int ncomp, const int32_t* edof,
                        const uint8_t* status, const double* cval, const double* u, int incremental, const R* stageK,
-                       double* stageF) {
+                       double* stageF, int full) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nlift) return;
     const int e = lift_elem[k];
@@ -654,8 +762,9 @@ __global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun,
         double s = 0.0;
         for (int b = 0; b < nloc; ++b) {
             if (act[b] || g[b] == 0.0) continue;
-            const int uidx = a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc);
-            s += (double)stageK[(size_t)e * (nloc * (nloc + 1) / 2) + uidx] * g[b];
+            const size_t kidx = full ? ((size_t)e * nloc + a) * nloc + b
+                                     : (size_t)e * (nloc * (nloc + 1) / 2) + (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc));
+            s += (double)stageK[kidx] * g[b];
         }
         stageF[(size_t)a * nelem + e] -= s;
     }
@@ -690,8 +799,10 @@ __device__ inline int local_eq(const int32_t* edof, const int32_t* eq, int nelem
     return eq[(size_t)edof[(a / ncomp) * nelem + e] * ncomp + a % ncomp];
 }
 
+// full: the element stage holds whole nloc x nloc matrices (non-symmetric
+// kernels), else packed upper triangles
 __global__ void k_gen_pairs(int nelem, int ncomp, int nloc, const int32_t* edof, const int32_t* eq, uint64_t* keys,
-                            int32_t* vals, unsigned long long* nvalid) {
+                            int32_t* vals, unsigned long long* nvalid, int full) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nelem * nloc) return;
     const int e = (int)(t / nloc), a = (int)(t % nloc);
@@ -702,7 +813,7 @@ __global__ void k_gen_pairs(int nelem, int ncomp, int nloc, const int32_t* edof,
         const size_t idx = ((size_t)e * nloc + a) * nloc + b;  // element-major: stable sort keeps element order
         if (qa >= 0 && qb >= 0) {
             keys[idx] = ((uint64_t)(uint32_t)qa << 32) | (uint32_t)qb;
-            vals[idx] = e * (nloc * (nloc + 1) / 2) + (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc));
+            vals[idx] = full ? (int32_t)idx : e * (nloc * (nloc + 1) / 2) + (a <= b ? upidx(a, b, nloc) : upidx(b, a, nloc));
             ++cnt;
         } else {
             keys[idx] = ~0ull;
@@ -772,7 +883,9 @@ int pattern_build(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dsrc.alloc(npairs));
     ISL_CHECK_CUDA(c, dcount.alloc(1));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(dcount.p, 0, 8, st));
-    k_gen_pairs<<<nblk((long long)E * nloc, 256), 256, 0, st>>>(E, c->ncomp, nloc, c->dedof.p, c->deq.p, kin.p, vin.p, dcount.p);
+    k_gen_pairs<<<nblk((long long)E * nloc, 256), 256, 0, st>>>(E, c->ncomp, nloc, c->dedof.p, c->deq.p, kin.p, vin.p, dcount.p,
+                                                                c->stage_full ? 1 : 0);
+    c->pattern_full = c->stage_full;
     ISL_CHECK_CUDA(c, cudaGetLastError());
     const int end_bit = 32 + bits_for((uint64_t)c->neq);
     size_t tmp_bytes = 0;
@@ -922,6 +1035,33 @@ static int dispatch_laplace(isl_ctx* c, const ElemArgs& A) {
     ISL_FAIL(c, ISL_ERR_ARG, "Laplace: unsupported element / quadrature combination");
 }
 
+template <int SHAPE, int FDEG, int NQ>
+static int launch_heat_static(isl_ctx* c, const ElemArgs& A) {
+    HostTab h;
+    if (!make_host_tables(SHAPE, FDEG, c->qdeg, h) || h.nq != NQ) ISL_FAIL(c, ISL_ERR_ARG, "quadrature");
+    Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T;
+    fill_tab<SHAPE, FDEG, NQ>(T, h);
+    k_heat_static<SHAPE, FDEG, NQ><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    return ISL_OK;
+}
+
+static int dispatch_heat_static(isl_ctx* c, ElemArgs A, int with_residual) {
+    HostTab h;
+    if (!make_host_tables(c->shape, c->fedeg, c->qdeg, h)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
+    A.with_residual = with_residual;  // the tangent depends on u even where the residual vanishes
+    const int nq = h.nq;
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && nq == 4) return launch_heat_static<ISL_QUAD, 1, 4>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 1 && nq == 9) return launch_heat_static<ISL_QUAD, 1, 9>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && nq == 4) return launch_heat_static<ISL_QUAD, 2, 4>(c, A);
+    if (c->shape == ISL_QUAD && c->fedeg == 2 && nq == 9) return launch_heat_static<ISL_QUAD, 2, 9>(c, A);
+    if (c->shape == ISL_HEX && c->fedeg == 1 && nq == 8) return launch_heat_static<ISL_HEX, 1, 8>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 1 && nq == 1) return launch_heat_static<ISL_TET, 1, 1>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 2 && nq == 4) return launch_heat_static<ISL_TET, 2, 4>(c, A);
+    ISL_FAIL(c, ISL_ERR_ARG, "heat::Static: unsupported element / quadrature combination");
+}
+
 template <typename R>
 static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
     if (!(c->shape == ISL_HEX && c->fedeg == 1)) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: only trilinear hexahedra on the device");
@@ -1011,12 +1151,14 @@ static int dispatch_neumann(isl_ctx* c) {
 int assemble_device(isl_ctx* c, int precision, int incremental, int with_residual) {
     cudaStream_t st = c->stream;
     const int E = (int)c->nelem;
-    // the tangent (stiffness) is staged in FP32 only for ISL_PREC_FP32
-    const bool k32 = (precision == ISL_PREC_FP32);
+    // the tangent (stiffness) is staged in FP32 only for ISL_PREC_FP32 (not for
+    // heat::Static, whose kernel runs in FP64 only)
+    const bool k32 = (precision == ISL_PREC_FP32) && c->kernel != ISL_KERNEL_HEAT_STATIC;
+    const size_t nstage = c->stage_full ? (size_t)c->nloc * c->nloc : (size_t)c->nup;
     if (k32) {
-        ISL_CHECK_CUDA(c, c->dstageK32.alloc((size_t)c->nup * E));
+        ISL_CHECK_CUDA(c, c->dstageK32.alloc(nstage * E));
     } else {
-        ISL_CHECK_CUDA(c, c->dstageK64.alloc((size_t)c->nup * E));
+        ISL_CHECK_CUDA(c, c->dstageK64.alloc(nstage * E));
     }
     if (precision != ISL_PREC_FP32) ISL_CHECK_CUDA(c, c->dval64.alloc(c->nnz));
     if (precision != ISL_PREC_FP64) ISL_CHECK_CUDA(c, c->dval32.alloc(c->nnz));
@@ -1038,6 +1180,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.flags = c->dflags.p;
     int rc;
     if (c->kernel == ISL_KERNEL_LAPLACE) rc = k32 ? dispatch_laplace<float>(c, A) : dispatch_laplace<double>(c, A);
+    else if (c->kernel == ISL_KERNEL_HEAT_STATIC) rc = dispatch_heat_static(c, A, with_residual);
     else rc = k32 ? dispatch_hyper<float>(c, A) : dispatch_hyper<double>(c, A);
     if (rc != ISL_OK) return rc;
     if (c->n_neu_elem > 0) {
@@ -1047,10 +1190,12 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     if (c->n_lift > 0) {
         if (k32)
             k_lift<float><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
-                                                              c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK32.p, c->dstageF.p);
+                                                              c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK32.p, c->dstageF.p,
+                                                              c->stage_full ? 1 : 0);
         else
             k_lift<double><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
-                                                               c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK64.p, c->dstageF.p);
+                                                               c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK64.p, c->dstageF.p,
+                                                               c->stage_full ? 1 : 0);
         ISL_CHECK_CUDA(c, cudaGetLastError());
         c->launches += 1;
     }

@@ -21,6 +21,22 @@ __device__ __forceinline__ int ld_stream(const int* p) {
     return v;
 }
 
+// Row dot product of a CSR matrix by a group of LPR lanes.  Every lane of the
+// warp must call it the same number of times (the shuffles use the full-warp
+// mask); lanes of a group without a row pass active = false and contribute 0.
+template <typename TV, typename TX, int LPR>
+__device__ inline TX row_dot(int row, bool active, const int* __restrict__ rowptr, const int* __restrict__ colind,
+                             const TV* __restrict__ val, const TX* __restrict__ p, int lane) {
+    TX acc = TX(0);
+    if (active) {
+        const int lo = rowptr[row], hi = rowptr[row + 1];
+        for (int k = lo + lane; k < hi; k += LPR) acc += (TX)ld(val + k) * ld(p + ld(colind + k));
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+    return acc;
+}
+
 // Software barrier across the blocks of a cooperative launch (every block is
 // resident).  bar[0] counts arrivals, bar[1] is the generation.  Thread 0 of
 // each block arrives with a release add (after the block barrier, so it

@@ -793,8 +793,22 @@ int isl_set_laplace(isl_ctx* c, const double* kappa, int quad_degree) {
     if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "Laplace needs a scalar field");
     c->kernel = ISL_KERNEL_LAPLACE;
     c->qdeg = quad_degree;
+    c->stage_full = false;
     ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, kappa, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    return ISL_OK;
+}
+
+int isl_set_heat_static(isl_ctx* c, int material, const double* param, int quad_degree) {
+    if (!c || !c->fedeg || !param) return ISL_ERR_ARG;
+    if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "heat::Static needs a scalar field");
+    if (material != ISL_THERMAL_CONSTANT && material != ISL_THERMAL_FENICS) ISL_FAIL(c, ISL_ERR_ARG, "thermal material");
+    c->kernel = ISL_KERNEL_HEAT_STATIC;
+    c->material = material;
+    c->qdeg = quad_degree;
+    c->stage_full = true;
+    ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, param, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
     return ISL_OK;
 }
 
@@ -804,6 +818,7 @@ int isl_set_hyperelastic(isl_ctx* c, int material, const double* lambda, const d
     if (material != ISL_MAT_STVENANT && material != ISL_MAT_NEOHOOKE) ISL_FAIL(c, ISL_ERR_ARG, "material");
     c->kernel = ISL_KERNEL_HYPERELASTIC;
     c->material = material;
+    c->stage_full = false;
     c->qdeg = quad_degree;
     ISL_CHECK_CUDA(c, c->dcoef.alloc(2 * c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, lambda, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
@@ -893,6 +908,10 @@ int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) 
         return ISL_OK;
     }
     cudaSetDevice(c->device);
+    if (c->pattern_full != c->stage_full) {  // the kernel changed between symmetric and full staging
+        const int st = isl::pattern_build(c);
+        if (st != ISL_OK) return st;
+    }
     return isl::assemble_device(c, precision, incremental, with_residual);
 }
 
@@ -905,7 +924,12 @@ int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* ite
         if (rel_res) *rel_res = 0.0;
         return ISL_OK;
     }
-    if (method == ISL_SOLVE_CG_FP64 && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "solve: no FP64 matrix assembled");
+    if (method < ISL_SOLVE_CG_FP64 || method > ISL_SOLVE_BICGSTAB) ISL_FAIL(c, ISL_ERR_ARG, "solve: unknown method");
+    if ((method == ISL_SOLVE_CG_FP64 || method == ISL_SOLVE_BICGSTAB) && !c->have64)
+        ISL_FAIL(c, ISL_ERR_ARG, "solve: no FP64 matrix assembled");
+    if (method == ISL_SOLVE_BICGSTAB && c->ninst > 1) ISL_FAIL(c, ISL_ERR_ARG, "solve: BiCGSTAB on one system only");
+    if (method != ISL_SOLVE_BICGSTAB && c->stage_full)
+        ISL_FAIL(c, ISL_ERR_ARG, "solve: the heat::Static tangent is not symmetric; use ISL_SOLVE_BICGSTAB");
     if (method == ISL_SOLVE_CG_FP32_IR && !c->have32)
         ISL_FAIL(c, ISL_ERR_ARG, "solve: the FP32 solve needs an FP32 matrix (ISL_PREC_MIXED or ISL_PREC_FP32)");
     if (!(tol >= 0.0)) ISL_FAIL(c, ISL_ERR_ARG, "tol");

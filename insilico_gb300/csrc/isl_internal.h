@@ -147,6 +147,8 @@ struct isl_ctx {
 
     // kernel data
     int kernel = -1, material = 0, qdeg = 2, sqdeg = 2;
+    bool stage_full = false;     // the kernel's element matrices are not symmetric: staged whole
+    bool pattern_full = false;   // the contribution lists index whole element matrices
     isl::DBuf<double> dcoef;     // SoA [ncoef][nelem]
     bool has_body = false;
     isl::DBuf<double> dfnodal;   // [nnodes][ncomp]
@@ -226,6 +228,8 @@ struct isl_ctx {
     isl::DBuf<double> w64;       // FP64 vectors
     isl::DBuf<float> w32;        // FP32 vectors
     isl::DBuf<double> dpart;     // block partial sums
+    isl::DBuf<double> wbi;       // BiCGSTAB vectors (10 N)
+    isl::DBuf<double> dbis;      // BiCGSTAB scalars
     isl::DBuf<isl::CGScal> dscal;
     isl::CGScal* hscal = nullptr;  // pinned host mirror
     int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row (FP32: 100 + U = sliced-ELL, U slots in flight)
@@ -280,4 +284,5 @@ int device_dofobj_numbering(isl_ctx* c, const std::vector<DeviceLevel>& levels, 
 int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t>& slots);
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
+int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc);
 }  // namespace isl

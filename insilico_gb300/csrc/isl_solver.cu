@@ -40,22 +40,6 @@ constexpr int CHUNK = 32;
 // reliable update when the iterated residual has dropped 10x (squared: 1e-2)
 constexpr double kDelta2 = 1e-2;
 
-// Row dot product by a group of LPR lanes.  Every lane of the warp must call it
-// the same number of times (the shuffles use the full-warp mask); lanes of a
-// group without a row pass active = false and contribute zero.
-template <typename TV, typename TX, int LPR>
-__device__ inline TX row_dot(int row, bool active, const int* __restrict__ rowptr, const int* __restrict__ colind,
-                             const TV* __restrict__ val, const TX* __restrict__ p, int lane) {
-    TX acc = TX(0);
-    if (active) {
-        const int lo = rowptr[row], hi = rowptr[row + 1];
-        for (int k = lo + lane; k < hi; k += LPR) acc += (TX)ld(val + k) * ld(p + ld(colind + k));
-    }
-#pragma unroll
-    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
-    return acc;
-}
-
 // q = A p; partial p.q; last block: alpha = absNew / p.q
 template <typename TV, typename TX, int LPR>
 __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
@@ -2034,7 +2018,8 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
         rc = solve_batched(c, method, tol, max_iter, &it, &rel);
         nc = (rc == ISL_ERR_NOT_CONVERGED);
         if (rc == ISL_ERR_NOT_CONVERGED) rc = ISL_OK;
-    } else if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
+    } else if (method == ISL_SOLVE_BICGSTAB) rc = solve_bicgstab(c, tol, max_iter, &it, &rel, &nc);
+    else if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
     else if (c->blocked && c->use_block && c->have64) rc = solve_mixed_b3(c, tol, max_iter, &it, &rel, &nc);
     else rc = solve_mixed(c, tol, max_iter, &it, &rel, &nc);
     if (rc != ISL_OK) return rc;

@@ -129,6 +129,13 @@ class System:
         self._kappa = np.ascontiguousarray(kappa, dtype=np.float64)
         self._chk(self.L.isl_set_laplace(self.h, A.d(self._kappa), quad_degree), "isl_set_laplace")
 
+    def set_heat_static(self, material: str, param, quad_degree: int):
+        """heat::Static with mat::thermal IsotropicConstant ("constant", param =
+        conductivity) or FenicsTest ("fenics", param = m), per element."""
+        m = {"constant": A.THERMAL_CONSTANT, "fenics": A.THERMAL_FENICS}[material]
+        self._thermal = np.ascontiguousarray(param, dtype=np.float64)
+        self._chk(self.L.isl_set_heat_static(self.h, m, A.d(self._thermal), quad_degree), "isl_set_heat_static")
+
     def set_hyperelastic(self, material: str, lam, mu, quad_degree: int):
         m = {"stvenant": A.MAT_STVENANT, "neohooke": A.MAT_NEOHOOKE}[material]
         self._lam = np.ascontiguousarray(lam, dtype=np.float64)

@@ -182,3 +182,72 @@ def setup_system(p: Problem, sys=None):
         e, f = faces_on_plane(p.shape, p.X, p.conn, e, f, axis, value)
         S.set_neumann(e, f, t, 2)
     return S
+
+
+# ---------------------------------------------------------------------------
+# Nonlinear heat conduction (heat::Static), reference/04-heat/nonlinearHeat.cpp
+def heat_reference_solution(x, m):
+    """u = ((2^(m+1) - 1) x + 1)^(1/(m+1)) - 1 (nonlinearHeat.cpp:37-44) and its
+    gradient, at points x [n, dim]."""
+    fac = 2.0 ** (m + 1.0)
+    mant = (fac - 1.0) * x[:, 0] + 1.0
+    u = mant ** (1.0 / (m + 1.0)) - 1.0
+    g = np.zeros_like(x)
+    g[:, 0] = (fac - 1.0) / (m + 1.0) * mant ** (1.0 / (m + 1.0) - 1.0)
+    return u, g
+
+
+def nonlinear_heat(S, X, conn, m=3.0, max_iter=10, tolerance=1e-8, qdeg=5, lin_tol=1e-13, method=None):
+    """The Newton loop of reference/04-heat/nonlinearHeat.cpp:166-211 through the
+    C-ABI: Q2 heat::Static with FenicsTest conductivity (1 + u)^m, u = 0 at
+    x = 0 and u = 1 at x = 1 (simpleBC :48-61); per iteration assemble the
+    tangent and the residual, stop when |R| = ||b|| / N < tolerance, solve the
+    non-symmetric system (BiCGSTAB to lin_tol on the GPU; SuperLU there), stop
+    when |x| < tolerance, add the increment to the DOFs.  Returns
+    (ndofs, [(iter, |R|, |x| or None)], L2 error of errorComputation<0>)."""
+    n = heat_setup(S, X, conn, m, qdeg)
+    rows = heat_newton(S, n, max_iter, tolerance, lin_tol, method)
+    xq = S.quadrature_points(qdeg)
+    u, _ = heat_reference_solution(xq, m)
+    return n, rows, S.error_norm(0, qdeg, u[:, None])
+
+
+def heat_setup(S, X, conn, m=3.0, qdeg=5):
+    """mesh, Q2 field, simpleBC constraints (nonlinearHeat.cpp:48-61), numbering,
+    pattern and the FenicsTest heat::Static kernel; returns the DOF count"""
+    S.upload_mesh(A.QUAD, X, conn)
+    S.create_field(2, 1)
+
+    def bc(x):
+        left = np.abs(x[:, 0]) < 1e-5
+        right = np.abs(x[:, 0] - 1.0) < 1e-5
+        return (left | right)[:, None], np.where(right, 1.0, 0.0)[:, None]
+    S.constrain_boundary(bc)
+    n = S.number_dofs()
+    S.register_pattern()
+    S.set_heat_static("fenics", np.full(len(conn), m), qdeg)
+    return n
+
+
+def heat_newton(S, n, max_iter=10, tolerance=1e-8, lin_tol=1e-13, method=None):
+    """Newton iterations of nonlinearHeat.cpp:166-207 from the context's current
+    DOF values; returns [(iter, |R|, |x| or None)]"""
+    if method is None:
+        method = A.SOLVE_BICGSTAB
+    rows = []
+    it = 0
+    while it < max_iter:
+        S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+        rn = S.norm()
+        if rn < tolerance:
+            rows.append((it, rn, None))
+            break
+        S.solve(method, tol=lin_tol)
+        xn = S.norm()
+        if xn < tolerance:
+            rows.append((it, rn, xn))
+            break
+        rows.append((it, rn, xn))
+        S.distribute(add=True)
+        it += 1
+    return rows

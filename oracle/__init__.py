@@ -67,6 +67,7 @@ def lib():
         L.orc_eq_index.argtypes = [_P, _I64]
         L.orc_set_laplace.argtypes = [_P, _D, C.c_int]
         L.orc_set_hyperelastic.argtypes = [_P, C.c_int, _D, _D, C.c_int]
+        L.orc_set_heat_static.argtypes = [_P, C.c_int, _D, C.c_int]
         L.orc_set_body_nodal.argtypes = [_P, _D]
         L.orc_set_body_cosproduct.argtypes = [_P, _D]
         L.orc_set_neumann.argtypes = [_P, C.c_int, C.c_int64, _I64, _I32, _D, C.c_double, C.c_int]
@@ -198,6 +199,12 @@ class Problem:
         self._lam = np.ascontiguousarray(lam, dtype=np.float64)
         self._mu = np.ascontiguousarray(mu, dtype=np.float64)
         self.L.orc_set_hyperelastic(self.h, {"stvenant": 0, "neohooke": 1}[material], _d(self._lam), _d(self._mu), qdeg)
+
+    def set_heat_static(self, material, param, qdeg):
+        """heat::Static with mat::thermal::IsotropicConstant ("constant", param =
+        conductivity) or FenicsTest ("fenics", param = exponent m), per element."""
+        self._thermal = np.ascontiguousarray(param, dtype=np.float64)
+        self.L.orc_set_heat_static(self.h, {"constant": 0, "fenics": 1}[material], _d(self._thermal), qdeg)
 
     def set_body_nodal(self, f):
         self._f = np.ascontiguousarray(f, dtype=np.float64)
@@ -358,6 +365,41 @@ def compressible(X, conn, E=1000.0, nu=0.3, max_iter=30, load_steps=5, pull=3.0,
     if return_values:
         return neq, rows, P.values()
     return neq, rows
+
+
+def nonlinear_heat(X, conn, m=3.0, max_iter=10, tolerance=1e-8, qdeg=5):
+    """reference/04-heat/nonlinearHeat.cpp: Q2 heat::Static with FenicsTest
+    conductivity (1 + u)^m, u = 0 at x = 0 and u = 1 at x = 1, Newton with a
+    direct solve of the non-symmetric tangent (SuperLU there, scipy's SuperLU
+    here).  Returns (ndofs, [(iter, |R|, |x| or None)], L2 error)."""
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.linalg import splu
+    P = Problem(QUAD, X, conn, 2, 1)
+    x, d = P.boundary_points()
+    left = np.abs(x[:, 0]) < 1e-5
+    right = np.abs(x[:, 0] - 1.0) < 1e-5
+    sel = left | right
+    P.constrain(d[sel], np.zeros(sel.sum()), np.where(right[sel], 1.0, 0.0))
+    n = P.number()
+    P.set_heat_static("fenics", np.full(len(conn), m), qdeg)
+    rows = []
+    it = 0
+    while it < max_iter:
+        rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+        rn = np.linalg.norm(b) / n
+        if rn < tolerance:
+            rows.append((it, rn, None))
+            break
+        xs = splu(csr_matrix((v, ci, rp), shape=(n, n)).tocsc()).solve(b)
+        xn = np.linalg.norm(xs) / n
+        if xn < tolerance:
+            rows.append((it, rn, xn))
+            break
+        rows.append((it, rn, xn))
+        P.distribute(xs, add=True)
+        it += 1
+    prm = np.array([m])
+    return n, rows, P.error_norm(2, prm, 0, qdeg), P
 
 
 def mixed_poisson(X, conn, alpha=(3.0, 5.0, 4.0)):

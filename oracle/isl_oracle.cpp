@@ -377,10 +377,11 @@ struct Problem {
     std::vector<int64_t> eq;        // equation index or -1
     int64_t neq = 0;
     // kernel
-    int kernel = 0;                 // 0 laplace, 1 hyperelastic
-    int material = 0;               // 0 StVenant, 1 NeoHookeanCompressible
+    int kernel = 0;                 // 0 laplace, 1 hyperelastic, 2 heat::Static
+    int material = 0;               // 0 StVenant, 1 NeoHookeanCompressible; heat::Static: 0 IsotropicConstant, 1 FenicsTest
     std::vector<double> kappa;      // per element
     std::vector<double> lam, mu;    // per element
+    std::vector<double> thermal;    // per element: conductivity (IsotropicConstant) or exponent m (FenicsTest)
     int qdeg = 2;                   // volume quadrature degree
     // forces
     std::vector<double> fnodal;     // [nnodes][ncomp] body force, interpolated by geometry functions
@@ -543,7 +544,48 @@ static void elementKernel(const Problem& P, const QuadRule& Q, int64_t e, double
         const double* xi = &Q.x[q * D];
         const double w = Q.w[q];
         const double detJ = feGradX(P, e, xi, g, xq, nullptr);
-        if (P.kernel == 0) {
+        if (P.kernel == 2) {
+            // heat::Static (heat/Static.hpp:98-225) with an isotropic material:
+            //   IsotropicConstant mat/thermal/IsotropicConstant.hpp: K = k I, K' = 0
+            //   FenicsTest mat/thermal/FenicsTest.hpp:47-60: K = (1+u)^m I, K' = m (1+u)^(m-1) I
+            // K[i,j] += detJ w sum_KL (g_iK K_KL g_jL + g_iK K'_KL gu_L phi_j)
+            // F[i]   += detJ w sum_KL g_iK K_KL gu_L
+            double phi[27], gphi[27 * 3], xq2[3];
+            feGradX(P, e, xi, gphi, xq2, phi);
+            double u = 0.0, gu[3] = {0, 0, 0};
+            for (int f = 0; f < nf; ++f) {
+                const double uf = P.uval[P.edof[e * nf + f]];
+                u += phi[f] * uf;
+                for (int k = 0; k < D; ++k) gu[k] += g[f * D + k] * uf;
+            }
+            double k0, k1;
+            if (P.material == 1) {
+                const double m = P.thermal[e];
+                k0 = std::pow(1.0 + u, m);
+                k1 = m * std::pow(1.0 + u, m - 1.0);
+            } else {
+                k0 = P.thermal[e];
+                k1 = 0.0;
+            }
+            if (Ke) {
+                for (int i = 0; i < nf; ++i)
+                    for (int j = 0; j < nf; ++j) {
+                        double entry = 0.0;
+                        for (int K = 0; K < D; ++K) {
+                            entry += g[i * D + K] * k0 * g[j * D + K];
+                            entry += g[i * D + K] * k1 * gu[K] * phi[j];
+                        }
+                        Ke[i * nloc + j] += detJ * w * entry;
+                    }
+            }
+            if (Fe) {
+                for (int i = 0; i < nf; ++i) {
+                    double sum = 0.0;
+                    for (int K = 0; K < D; ++K) sum += g[i * D + K] * k0 * gu[K];
+                    Fe[i] += sum * detJ * w;
+                }
+            }
+        } else if (P.kernel == 0) {
             const double kap = P.kappa[e];
             if (Ke) {
                 const double scalar = kap * detJ * w;
@@ -921,6 +963,11 @@ void orc_set_hyperelastic(void* h, int mat, const double* lam, const double* mu,
     P->lam.assign(lam, lam + P->nelem);
     P->mu.assign(mu, mu + P->nelem);
 }
+void orc_set_heat_static(void* h, int mat, const double* param, int qdeg) {
+    Problem* P = (Problem*)h;
+    P->kernel = 2; P->material = mat; P->qdeg = qdeg;
+    P->thermal.assign(param, param + P->nelem);
+}
 void orc_set_body_nodal(void* h, const double* f) {
     Problem* P = (Problem*)h;
     P->bodyKind = f ? 1 : 0;
@@ -1206,6 +1253,18 @@ static void refsol(int kind, const double* prm, int dim, const double* x, double
                 s += U * prm[5 + j];
             }
             u[i] = s;
+        }
+        return;
+    }
+    if (kind == 2) {
+        // reference/04-heat/nonlinearHeat.cpp:37-44: u = ((2^(m+1) - 1) x + 1)^(1/(m+1)) - 1
+        const double m = prm[0];
+        const double fac = std::pow(2.0, m + 1.0);
+        const double mantissa = (fac - 1.0) * x[0] + 1.0;
+        u[0] = std::pow(mantissa, 1. / (m + 1.0)) - 1.0;
+        if (gu) {
+            gu[0] = (fac - 1.0) / (m + 1.0) * std::pow(mantissa, 1. / (m + 1.0) - 1.0);
+            for (int d = 1; d < dim; ++d) gu[d] = 0.0;
         }
         return;
     }

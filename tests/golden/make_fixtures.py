@@ -14,6 +14,8 @@ Pins extracted (file paths relative to the reference project):
   reference/06-elastic/compRefOut{D,N}.dat           -> Newton history tables
   reference/05-mixedPoisson/ref                      -> ndofs, L2, H1
   reference/05-mixedPoisson/square_020.smf           -> canonical mesh hash
+  reference/04-heat/square_200.smf                   -> canonical mesh hash
+  reference/04-heat/nonlinearHeat.ref.dat            -> dofs, Newton |R|/|x| history, L2 error
   reference/06-elastic/quad.020.{D,N}ref.vtk         -> sha256 + count of the grid lines and of
                                                         the POINT_DATA section lines
 """
@@ -89,7 +91,8 @@ def main(ref):
         out["sparsity"][str(d)] = {"lines": len(data), "sha256": lines_hash(data),
                                    "head": data[:12], "tail": data[-6:]}
     smfs = [os.path.join(ref, "reference/03-doFHandler/square_20.smf"),
-            os.path.join(ref, "reference/05-mixedPoisson/square_020.smf")]
+            os.path.join(ref, "reference/05-mixedPoisson/square_020.smf"),
+            os.path.join(ref, "reference/04-heat/square_200.smf")]
     smfs += sorted(glob.glob(os.path.join(ref, "reference/06-elastic/quad.*.smf")))
     smfs += sorted(glob.glob(os.path.join(ref, "reference/06-elastic/cube.*.smf")))
     for p in smfs:
@@ -109,6 +112,18 @@ def main(ref):
         txt = f.read().splitlines()
     out["mixedPoisson"] = {"ndofs": int(txt[0].split()[-1]), "L2": float(txt[1].split()[-1]),
                            "H1": float(txt[2].split()[-1]), "volume": float(txt[3].split()[-1])}
+    # reference/04-heat/nonlinearHeat.ref.dat: dof count, Newton |R| / |x| per
+    # iteration, iteration count, L2 error
+    with open(os.path.join(ref, "reference/04-heat/nonlinearHeat.ref.dat")) as f:
+        txt = f.read()
+    import re
+    newton = []
+    for mt in re.finditer(r"(\d+):\s+\|R\| = ([0-9.eE+-]+)(?:,\s+\|x\| = ([0-9.eE+-]+))?", txt):
+        newton.append([int(mt.group(1)), float(mt.group(2)), float(mt.group(3)) if mt.group(3) else None])
+    out["nonlinearHeat"] = {"ndofs": int(re.search(r"Number of dofs (\d+)", txt).group(1)),
+                            "newton": newton,
+                            "iterations": int(re.search(r"Converged to given tolerance in (\d+)", txt).group(1)),
+                            "L2": float(re.search(r"L2-error = ([0-9.eE+-]+)", txt).group(1))}
     out["vtk"] = {}
     for tag in ("D", "N"):
         rel = "reference/06-elastic/quad.020.%sref.vtk" % tag

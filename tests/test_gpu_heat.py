@@ -1,0 +1,103 @@
+"""heat::Static (nonlinear heat conduction) and BiCGSTAB on the GPU: the
+non-symmetric tangent and residual against the oracle, the BiCGSTAB solution
+against a direct solve, and the whole Newton run of
+reference/04-heat/nonlinearHeat.cpp against its golden output."""
+import numpy as np
+import pytest
+
+import oracle as O
+from insilico_gb300 import _abi as A
+from insilico_gb300 import workloads as W
+from insilico_gb300.system import System
+
+from helpers import csr_entry_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _both(kind, shape, deg, sizes, material, seed):
+    """the same heat::Static problem on the GPU and on the oracle, at random
+    nonnegative DOF values (u > -1 for the FenicsTest law)"""
+    X, conn = W.unit_cube(kind, *sizes)
+    rng = np.random.default_rng(seed)
+    prm = rng.uniform(1.0, 3.0, len(conn))
+    S = System(device=0)
+    S.upload_mesh(shape, X, conn)
+    S.create_field(deg, 1)
+    mask_fun = lambda x: ((np.abs(x[:, 0]) < 1e-9)[:, None], np.full((len(x), 1), 0.25))  # noqa: E731
+    S.constrain_boundary(mask_fun)
+    S.number_dofs()
+    S.register_pattern()
+    S.set_heat_static(material, prm, 2)
+    u = rng.uniform(0.0, 0.5, S.ndofobj)
+    S.set_values(u)
+    P = O.Problem({A.QUAD: O.QUAD, A.TET: O.TET, A.HEX: O.HEX}[shape], X, conn, deg, 1)
+    x, d = P.boundary_points()
+    on = np.abs(x[:, 0]) < 1e-9
+    P.constrain(d[on], np.zeros(on.sum()), np.full(on.sum(), 0.25))
+    P.number()
+    P.set_heat_static(material, prm, 2)
+    P.set_values(u)
+    return S, P
+
+
+@pytest.mark.parametrize("kind,shape,deg,sizes", [
+    ("quad", A.QUAD, 2, (6, 5)), ("quad", A.QUAD, 1, (9, 7)), ("tet", A.TET, 2, (3, 2, 2)), ("hex", A.HEX, 1, (3, 3, 2)),
+])
+@pytest.mark.parametrize("material", ["fenics", "constant"])
+def test_heat_static_tangent_and_residual_match_oracle(kind, shape, deg, sizes, material):
+    S, P = _both(kind, shape, deg, sizes, material, 5)
+    S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+    rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+    srp, sci, sv = S.csr()
+    np.testing.assert_array_equal(srp, rp)
+    np.testing.assert_array_equal(sci, ci)
+    assert csr_entry_err(rp, ci, sv, v) <= 1e-12
+    assert np.max(np.abs(S.rhs() - b)) <= 1e-12 * np.max(np.abs(b))
+    if material == "fenics":
+        # the tangent is not symmetric
+        import scipy.sparse as sp
+        Am = sp.csr_matrix((sv, sci, srp))
+        assert abs(Am - Am.T).max() > 1e-6 * abs(Am).max()
+    S.close()
+
+
+def test_bicgstab_solves_the_nonsymmetric_system():
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve
+    S, P = _both("quad", A.QUAD, 2, (16, 12), "fenics", 9)
+    S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    it, rel, _ = S.solve(A.SOLVE_BICGSTAB, tol=1e-13)
+    assert 0 < it < len(b) and rel <= 1e-13
+    x = S.solution()
+    xd = spsolve(sp.csc_matrix(sp.csr_matrix((v, ci, rp))), b)
+    assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
+    # bitwise reproducible, and CG refuses the non-symmetric tangent
+    S.solve(A.SOLVE_BICGSTAB, tol=1e-13)
+    assert np.array_equal(S.solution(), x)
+    with pytest.raises(A.IslError):
+        S.solve(A.SOLVE_CG_FP64, tol=1e-10)
+    S.close()
+
+
+def test_nonlinear_heat_matches_reference_golden(pins):
+    """reference/04-heat/nonlinearHeat.cpp on square_200.smf (Q2, 159,999
+    DOFs): Newton |R| and |x| per iteration, iteration count and L2 error, to
+    the 6 digits of nonlinearHeat.ref.dat"""
+    ref = pins["nonlinearHeat"]
+    X, conn = O.unitcube("quad", 200, 200, round6=True)
+    S = System(device=0)
+    n, rows, l2 = W.nonlinear_heat(S, X, conn)
+    assert n == ref["ndofs"]
+    assert len(rows) == len(ref["newton"]) and len(rows) - 1 == ref["iterations"]
+    for got, want in zip(rows, ref["newton"]):
+        assert got[0] == want[0]
+        assert got[1] == pytest.approx(want[1], rel=2e-5)
+        if want[2] is None:
+            assert got[2] is None
+        else:
+            assert got[2] == pytest.approx(want[2], rel=2e-5)
+    assert l2 == pytest.approx(ref["L2"], rel=2e-5)
+    S.close()

@@ -86,3 +86,23 @@ def test_mixed_poisson(pins):
     assert n == ref["ndofs"]
     assert l2 == pytest.approx(ref["L2"], rel=2e-5)
     assert h1 == pytest.approx(ref["H1"], rel=2e-5)
+
+
+def test_nonlinear_heat(pins):
+    """reference/04-heat/nonlinearHeat.cpp on square_200.smf: Q2 heat::Static
+    with FenicsTest conductivity, Newton with a direct solve of the
+    non-symmetric tangent"""
+    ref = pins["nonlinearHeat"]
+    X, conn = O.unitcube("quad", 200, 200, round6=True)
+    assert mesh_hash(_pad3(X), conn) == pins["meshes"]["reference/04-heat/square_200.smf"]["sha256"]
+    n, rows, l2, _ = O.nonlinear_heat(X, conn)
+    assert n == ref["ndofs"]
+    assert len(rows) == len(ref["newton"]) and len(rows) - 1 == ref["iterations"]
+    for got, want in zip(rows, ref["newton"]):
+        assert got[0] == want[0]
+        assert got[1] == pytest.approx(want[1], rel=2e-5)
+        if want[2] is None:
+            assert got[2] is None
+        else:
+            assert got[2] == pytest.approx(want[2], rel=2e-5)
+    assert l2 == pytest.approx(ref["L2"], rel=2e-5)
