@@ -309,7 +309,7 @@ def run_heat(args, rank, world, local, pg):
     (1 + u)^3) on the n x n unit square in Q2; n = 200 is the square_200 mesh of
     reference/04-heat/nonlinearHeat.cpp.  One step is the whole Newton run from
     u = 0: assemble the non-symmetric tangent and the residual, BiCGSTAB to
-    1e-13, add the increment (4 assemblies, 3 solves)."""
+    1e-11, add the increment (4 assemblies, 3 solves)."""
     from insilico_gb300 import _abi as A
     from insilico_gb300 import workloads as W
     from insilico_gb300.system import System
@@ -322,9 +322,12 @@ def run_heat(args, rank, world, local, pg):
     t_setup = time.perf_counter() - t0
     zeros = np.zeros(S.ndofobj)
 
+    lin = []
+
     def step():
         S.set_values(zeros)
-        return W.heat_newton(S, ndofs)
+        lin.clear()
+        return W.heat_newton(S, ndofs, lin_iters=lin)
     for _ in range(max(3, args.warmup)):
         rows = step()
     S.sync()
@@ -357,10 +360,11 @@ def run_heat(args, rank, world, local, pg):
             "ms_per_step": s_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (unit square; no dataset)",
             "config": {"workload": f"heat: Q2 heat::Static FenicsTest m=3 on the {n}x{n} unit square, u=0 at x=0, "
-                                   f"u=1 at x=1, Newton to 1e-8, BiCGSTAB (Jacobi) to 1e-13",
+                                   f"u=1 at x=1, Newton to 1e-8, BiCGSTAB (Jacobi) to 1e-11",
                        "dofs": int(ndofs), "elements": int(len(conn)), "parallelism": "single",
                        "l2": "matrix and vectors resident; per step the DOF values are reset from the host"},
             "newton_iters": newton, "residuals": [r[1] for r in rows], "setup_s": t_setup,
+            "bicgstab_iters": list(lin), "bicgstab_spmv": int(S.get_option(A.OPT_BICGSTAB_KIND)),
             "phase_ms_per_step": {"element": ms[A.T_ELEMENT] / args.steps, "gather": ms[A.T_GATHER] / args.steps,
                                   "solve": ms[A.T_SOLVE] / args.steps},
             "cpu_baseline": cpu,

@@ -259,9 +259,14 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * ISL_OPT_HOST_SETUP (default 0): with a device, isl_field_create numbers the
  * DOF objects of fields of degree > 1 and isl_boundary_faces /
  * isl_boundary_points find the boundary on the GPU (sorts and scans, the
- * same ids and order as the host rules); 1 runs both on the host. */
+ * same ids and order as the host rules); 1 runs both on the host.
+ * ISL_OPT_BICGSTAB_KIND: the FP64 SpMV of ISL_SOLVE_BICGSTAB, 0 (default)
+ * autotuned per pattern, 2, 4, 8 or 16 CSR lanes per row, 102, 104 or 108
+ * the sliced-ELL copy with FP64 values (where it exists); read back, the kind
+ * of the last solve. */
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
-       ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8 };
+       ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
+       ISL_OPT_BICGSTAB_KIND = 9 };
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 

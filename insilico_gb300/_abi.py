@@ -45,7 +45,7 @@ EXPORTED = [
     "isl_set_heat_static",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
- OPT_SCALAR_SLOTS, OPT_HOST_SETUP) = 0, 1, 2, 3, 4, 5, 6, 7, 8
+ OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND) = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
 
 
 class IslError(RuntimeError):

@@ -886,6 +886,7 @@ int pattern_build(isl_ctx* c) {
     k_gen_pairs<<<nblk((long long)E * nloc, 256), 256, 0, st>>>(E, c->ncomp, nloc, c->dedof.p, c->deq.p, kin.p, vin.p, dcount.p,
                                                                 c->stage_full ? 1 : 0);
     c->pattern_full = c->stage_full;
+    c->pattern_serial++;
     ISL_CHECK_CUDA(c, cudaGetLastError());
     const int end_bit = 32 + bits_for((uint64_t)c->neq);
     size_t tmp_bytes = 0;

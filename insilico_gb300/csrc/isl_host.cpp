@@ -1078,6 +1078,12 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
         c->use_persist = (int)value;
         return ISL_OK;
     }
+    if (key == ISL_OPT_BICGSTAB_KIND) {
+        if (value < 0 || value > 108 || !isl::bicgstab_kind_valid(c, (int)value))
+            ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_BICGSTAB_KIND: 0, CSR lanes per row 2..16, or 102/104/108 with a sliced-ELL copy");
+        c->bicg_forced = (int)value;
+        return ISL_OK;
+    }
     if (key == ISL_OPT_HOST_SETUP) {
         c->host_setup = value != 0;
         c->bf_valid = false;
@@ -1103,6 +1109,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_NSLOTS) { *value = c->blocked ? c->nslot : 0; return ISL_OK; }
     if (key == ISL_OPT_SPMV32_KIND) { *value = c->spmv_lpr32; return ISL_OK; }
     if (key == ISL_OPT_HOST_SETUP) { *value = c->host_setup; return ISL_OK; }
+    if (key == ISL_OPT_BICGSTAB_KIND) { *value = c->bicg_lpr; return ISL_OK; }
     if (key == ISL_OPT_SCALAR_SLOTS) { *value = c->ss_nslot; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
 }

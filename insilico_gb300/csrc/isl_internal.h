@@ -230,6 +230,11 @@ struct isl_ctx {
     isl::DBuf<double> dpart;     // block partial sums
     isl::DBuf<double> wbi;       // BiCGSTAB vectors (10 N)
     isl::DBuf<double> dbis;      // BiCGSTAB scalars
+    int bicg_lpr = 0;            // BiCGSTAB SpMV kind (autotuned per pattern): CSR lanes per row, 100 + U sliced-ELL
+    int bicg_forced = 0;         // kind set through ISL_OPT_BICGSTAB_KIND (0: autotune)
+    isl::DBuf<double> dss_val64; // FP64 values of the scalar sliced-ELL copy (BiCGSTAB)
+    int64_t ss_serial64 = -1, ss_val64_pattern = -1;
+    int64_t bicg_serial = -1, pattern_serial = 0;
     isl::DBuf<isl::CGScal> dscal;
     isl::CGScal* hscal = nullptr;  // pinned host mirror
     int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row (FP32: 100 + U = sliced-ELL, U slots in flight)
@@ -285,4 +290,5 @@ int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc);
+bool bicgstab_kind_valid(const isl_ctx* c, int kind);
 }  // namespace isl

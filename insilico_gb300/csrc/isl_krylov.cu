@@ -108,6 +108,72 @@ __global__ void __launch_bounds__(KB) k_bi_spmv(int n, const int* __restrict__ r
     }
 }
 
+// The same product on the scalar sliced-ELL copy (rows length-sorted within
+// windows of 2048, one lane per row, slots column-major) with FP64 values: the
+// loads of U slots are issued before their gathers, so each lane keeps 12U
+// bytes of the stream in flight.
+template <int U, int MINB>
+__global__ void __launch_bounds__(KB, MINB) k_bi_sspmv(int nslice, const int* __restrict__ soff, const int* __restrict__ swid,
+                                                    const int* __restrict__ srow, const int* __restrict__ scol,
+                                                    const double* __restrict__ sv, const double* __restrict__ in,
+                                                    double* __restrict__ out, const double* __restrict__ a,
+                                                    const double* __restrict__ b, int mode, BiScal* S, double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * KB + threadIdx.x) >> 5, nwarps = gridDim.x * (KB / 32);
+    double d1 = 0.0, d2 = 0.0;
+    for (int s = warp; s < nslice; s += nwarps) {
+        const int o = soff[s] + lane, w = swid[s];
+        double acc = 0.0;
+        for (int k = 0; k < w; k += U) {
+            int j[U];
+            double v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    j[u] = ld_stream(scol + o + (k + u) * 32);
+                    v[u] = __ldcs(sv + o + (k + u) * 32);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (k + u < w) acc += v[u] * __ldg(in + j[u]);
+        }
+        const int row = srow[s * 32 + lane];
+        if (row >= 0) {
+            out[row] = acc;
+            d1 += (a ? a[row] : acc) * acc;
+            if (b) d2 += b[row] * acc;
+        }
+    }
+    const double b1 = block_sum(d1, sh);
+    const double b2 = block_sum(d2, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (last_block(&S->ticket)) {
+        double t1, t2;
+        reduce_parts2_blk<KB>(part, gridDim.x, sh, t1, t2);
+        if (threadIdx.x == 0) {
+            if (mode == 0) {
+                S->alpha = S->rho / t1;
+                if (!(S->alpha == S->alpha) || isinf(S->alpha)) { S->bad = 1; S->done = 1; }
+            } else {
+                S->w = t1 > 0.0 ? t2 / t1 : 0.0;
+            }
+            S->ticket = 0;
+        }
+    }
+}
+
+// FP64 values into the sliced-ELL slots (padding slots stay zero)
+__global__ void k_ssell_values64(int n, const int* __restrict__ rowptr, const int* __restrict__ spos,
+                                 const double* __restrict__ val, double* __restrict__ sv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int lo = rowptr[i], hi = rowptr[i + 1], s0 = spos[i];
+        for (int k = lo; k < hi; ++k) sv[s0 + (k - lo) * 32] = val[k];
+    }
+}
+
 // x += alpha y + w z, r = s - w t; r.r and r0.r; the last block: convergence,
 // the next rho and beta, or a restart request
 __global__ void __launch_bounds__(KB) k_bi_update(int n, double* __restrict__ x, double* __restrict__ r,
@@ -210,22 +276,41 @@ __global__ void k_bi_zero(int n, double* __restrict__ x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = 0.0;
 }
 
-template <int LPR>
-void launch_iter(cudaStream_t st, unsigned grid, int n, const isl_ctx* c, double* const* V, BiScal* S, double* part) {
-    double *x = V[0], *r = V[1], *r0 = V[2], *p = V[3], *v = V[4], *y = V[5], *s_ = V[6], *z = V[7], *t = V[8],
-           *dinv = V[9];
+// the SpMV of BiCGSTAB: kind 2..16 = CSR with that many lanes per row,
+// 100 + U = the sliced-ELL copy with U slots in flight
+void launch_bi_spmv(const isl_ctx* c, int kind, unsigned grid, const double* in, double* out, const double* a,
+                    const double* b, int mode, BiScal* S, double* part) {
+    cudaStream_t st = c->stream;
+    const int n = (int)c->neq;
     const int* rp = c->drowptr.p;
     const int* ci = c->dcolind.p;
     const double* val = c->dval64.p;
+    auto gs = [&](long long per_sm) {
+        return (unsigned)std::max<long long>(1, std::min<long long>((c->ss_nslice + 7) / 8, per_sm * c->sm_count));
+    };
+    switch (kind) {
+        case 2: k_bi_spmv<2><<<grid, KB, 0, st>>>(n, rp, ci, val, in, out, a, b, mode, S, part); break;
+        case 4: k_bi_spmv<4><<<grid, KB, 0, st>>>(n, rp, ci, val, in, out, a, b, mode, S, part); break;
+        case 8: k_bi_spmv<8><<<grid, KB, 0, st>>>(n, rp, ci, val, in, out, a, b, mode, S, part); break;
+        case 16: k_bi_spmv<16><<<grid, KB, 0, st>>>(n, rp, ci, val, in, out, a, b, mode, S, part); break;
+        case 102: k_bi_sspmv<2, 6><<<gs(6), KB, 0, st>>>((int)c->ss_nslice, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val64.p, in, out, a, b, mode, S, part); break;
+        case 104: k_bi_sspmv<4, 6><<<gs(6), KB, 0, st>>>((int)c->ss_nslice, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val64.p, in, out, a, b, mode, S, part); break;
+        default: k_bi_sspmv<8, 4><<<gs(4), KB, 0, st>>>((int)c->ss_nslice, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val64.p, in, out, a, b, mode, S, part); break;
+    }
+}
+
+void launch_iter(cudaStream_t st, unsigned grid, int n, const isl_ctx* c, int kind, double* const* V, BiScal* S,
+                 double* part) {
+    double *x = V[0], *r = V[1], *r0 = V[2], *p = V[3], *v = V[4], *y = V[5], *s_ = V[6], *z = V[7], *t = V[8],
+           *dinv = V[9];
     k_bi_dir<<<grid, KB, 0, st>>>(n, r, v, dinv, p, y, S);
-    k_bi_spmv<LPR><<<grid, KB, 0, st>>>(n, rp, ci, val, y, v, r0, nullptr, 0, S, part);
+    launch_bi_spmv(c, kind, grid, y, v, r0, nullptr, 0, S, part);
     k_bi_s<<<grid, KB, 0, st>>>(n, r, v, dinv, s_, z, S);
-    k_bi_spmv<LPR><<<grid, KB, 0, st>>>(n, rp, ci, val, z, t, nullptr, s_, 1, S, part);
+    launch_bi_spmv(c, kind, grid, z, t, nullptr, s_, 1, S, part);
     k_bi_update<<<grid, KB, 0, st>>>(n, x, r, r0, y, z, s_, t, S, part);
 }
 
-template <int LPR>
-int run_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
+int run_bicgstab(isl_ctx* c, int kind, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
     cudaStream_t st = c->stream;
     const int n = (int)c->neq;
     const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((n + KB - 1) / KB, 4LL * c->sm_count));
@@ -245,8 +330,8 @@ int run_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, doubl
     k_bi_dinv<<<grid, KB, 0, st>>>(n, c->ddiag.p, c->dval64.p, V[9]);
     k_bi_zero<<<grid, KB, 0, st>>>(n, V[0]);
     // |b|^2 first, then the start with the absolute threshold tol^2 |b|^2
-    k_bi_start<LPR><<<grid, KB, 0, st>>>(n, c->drowptr.p, c->dcolind.p, c->dval64.p, c->drhs.p, V[0], V[1], V[2], V[3],
-                                         V[4], 0, S, part);
+    k_bi_start<4><<<grid, KB, 0, st>>>(n, c->drowptr.p, c->dcolind.p, c->dval64.p, c->drhs.p, V[0], V[1], V[2], V[3],
+                                       V[4], 0, S, part);
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(&h, S, sizeof h, cudaMemcpyDeviceToHost, st));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
     c->launches += 3;
@@ -257,7 +342,7 @@ int run_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, doubl
     cudaGraph_t graph;
     cudaGraphExec_t exec;
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < BI_CHUNK; ++k) launch_iter<LPR>(st, grid, n, c, V, S, part);
+    for (int k = 0; k < BI_CHUNK; ++k) launch_iter(st, grid, n, c, kind, V, S, part);
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -274,8 +359,8 @@ int run_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, doubl
         if (h.bad) { rc = ISL_ERR_NAN; c->err = "BiCGSTAB breakdown (non-finite scalar)"; break; }
         if (h.done == 2) {  // r0.r vanished: restart from the true residual
             ++restarts;
-            k_bi_start<LPR><<<grid, KB, 0, st>>>(n, c->drowptr.p, c->dcolind.p, c->dval64.p, c->drhs.p, V[0], V[1],
-                                                 V[2], V[3], V[4], 1, S, part);
+            k_bi_start<4><<<grid, KB, 0, st>>>(n, c->drowptr.p, c->dcolind.p, c->dval64.p, c->drhs.p, V[0], V[1],
+                                               V[2], V[3], V[4], 1, S, part);
             c->launches += 1;
             if (cudaMemcpyAsync(&h, S, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "BiCGSTAB scalars"; break; }
@@ -291,19 +376,70 @@ int run_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, doubl
     return ISL_OK;
 }
 
+// time the SpMV candidates on the current matrix (20 launches each, CUDA
+// events): CSR with 2, 4, 8, 16 lanes per row and, where the sliced-ELL copy
+// exists, its batch depths 2, 4, 8; keep the fastest
+int tune_kind(isl_ctx* c) {
+    const int n = (int)c->neq;
+    if (n < 20000) {
+        const double avg = (double)c->nnz / (double)std::max<int64_t>(1, c->neq);
+        int lpr = 2;
+        while (lpr < 16 && lpr < avg / 4) lpr *= 2;
+        return lpr;
+    }
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((n + KB - 1) / KB, 4LL * c->sm_count));
+    if (c->wbi.n < (size_t)10 * n && c->wbi.alloc((size_t)10 * n) != cudaSuccess) return 4;
+    if (c->dbis.n < 16 && c->dbis.alloc(16) != cudaSuccess) return 4;
+    BiScal* S = reinterpret_cast<BiScal*>(c->dbis.p);
+    cudaMemsetAsync(S, 0, sizeof(BiScal), c->stream);
+    cudaMemsetAsync(c->wbi.p, 0, (size_t)n * 8, c->stream);
+    const double* in = c->wbi.p;
+    double* out = c->wbi.p + n;
+    const int cand[7] = {2, 4, 8, 16, 102, 104, 108};
+    const int ncand = c->ss_nslice > 0 ? 7 : 4;
+    int best = 4;
+    float bestms = 1e30f;
+    for (int k = 0; k < ncand; ++k) {
+        launch_bi_spmv(c, cand[k], grid, in, out, nullptr, nullptr, 1, S, c->dpart.p);
+        cudaEventRecord(c->ev[2], c->stream);
+        for (int r = 0; r < 20; ++r) launch_bi_spmv(c, cand[k], grid, in, out, nullptr, nullptr, 1, S, c->dpart.p);
+        cudaEventRecord(c->ev[3], c->stream);
+        cudaEventSynchronize(c->ev[3]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        if (ms < bestms) { bestms = ms; best = cand[k]; }
+    }
+    c->launches += 21 * ncand;
+    return best;
+}
+
 }  // namespace
 
+bool bicgstab_kind_valid(const isl_ctx* c, int kind) {
+    if (kind == 0 || kind == 2 || kind == 4 || kind == 8 || kind == 16) return true;
+    return (kind == 102 || kind == 104 || kind == 108) && c->ss_nslice > 0;
+}
+
 int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
-    const double avg = (double)c->nnz / (double)std::max<int64_t>(1, c->neq);
-    int lpr = 2;
-    while (lpr < 32 && lpr < avg / 2) lpr *= 2;
-    switch (lpr) {
-        case 2: return run_bicgstab<2>(c, tol, max_iter, iters, rel, nc);
-        case 4: return run_bicgstab<4>(c, tol, max_iter, iters, rel, nc);
-        case 8: return run_bicgstab<8>(c, tol, max_iter, iters, rel, nc);
-        case 16: return run_bicgstab<16>(c, tol, max_iter, iters, rel, nc);
-        default: return run_bicgstab<32>(c, tol, max_iter, iters, rel, nc);
+    if (c->ss_nslice > 0 && c->ss_serial64 != c->asm_serial) {  // FP64 values of the sliced-ELL copy
+        ISL_CHECK_CUDA(c, c->dss_val64.alloc(c->ss_nslot));
+        if (c->ss_val64_pattern != c->pattern_serial) {
+            ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dss_val64.p, 0, (size_t)c->ss_nslot * 8, c->stream));
+            c->ss_val64_pattern = c->pattern_serial;
+        }
+        k_ssell_values64<<<(unsigned)c->sm_count * 8, KB, 0, c->stream>>>((int)c->neq, c->drowptr.p, c->dss_pos.p,
+                                                                           c->dval64.p, c->dss_val64.p);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+        c->launches += 1;
+        c->ss_serial64 = c->asm_serial;
     }
+    if (c->bicg_forced && bicgstab_kind_valid(c, c->bicg_forced)) {
+        c->bicg_lpr = c->bicg_forced;
+    } else if (!c->bicg_lpr || c->bicg_serial != c->pattern_serial) {
+        c->bicg_lpr = tune_kind(c);
+        c->bicg_serial = c->pattern_serial;
+    }
+    return run_bicgstab(c, c->bicg_lpr, tol, max_iter, iters, rel, nc);
 }
 
 }  // namespace isl

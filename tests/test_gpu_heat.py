@@ -101,3 +101,29 @@ def test_nonlinear_heat_matches_reference_golden(pins):
             assert got[2] == pytest.approx(want[2], rel=2e-5)
     assert l2 == pytest.approx(ref["L2"], rel=2e-5)
     S.close()
+
+
+def test_bicgstab_sliced_ell_and_csr_agree():
+    """a heat::Static tangent above the sliced-ELL threshold: the CSR and the
+    sliced-ELL SpMV solve it to the tolerance and agree with the direct solve"""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve
+    S, P = _both("quad", A.QUAD, 2, (80, 70), "fenics", 13)
+    assert S.neq >= 20000 and S.get_option(A.OPT_SCALAR_SLOTS) >= S.nnz
+    S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+    rp, ci, v = S.csr()
+    b = S.rhs()
+    xd = spsolve(sp.csc_matrix(sp.csr_matrix((v, ci, rp))), b)
+    out = {}
+    for kind in (4, 104, 108):
+        S.set_option(A.OPT_BICGSTAB_KIND, kind)
+        it, rel, _ = S.solve(A.SOLVE_BICGSTAB, tol=1e-12)
+        assert S.get_option(A.OPT_BICGSTAB_KIND) == kind and rel <= 1e-12
+        out[kind] = S.solution()
+        assert np.linalg.norm(out[kind] - xd) <= 1e-8 * np.linalg.norm(xd)
+    # slot-order sums do not depend on the batch depth
+    assert np.array_equal(out[104], out[108])
+    S.set_option(A.OPT_BICGSTAB_KIND, 0)
+    S.solve(A.SOLVE_BICGSTAB, tol=1e-12)
+    assert S.get_option(A.OPT_BICGSTAB_KIND) in (2, 4, 8, 16, 102, 104, 108)
+    S.close()
