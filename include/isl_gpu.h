@@ -135,6 +135,25 @@ int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const
  * staged whole (the contribution lists are rebuilt once, at the next
  * isl_assemble) and the system is solved with ISL_SOLVE_BICGSTAB. */
 int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_elem] */, int quad_degree);
+/* Time integration by a linear multi-step method: the inertia terms of
+ * base::time::computeInertiaTerms (base/time/ReactionTerms.hpp:62-79,
+ * ReactionTerms::operator() :185-254) and the DOF history
+ * (DegreeOfFreedom::pushHistory).
+ * isl_set_history: keep the DOF values of the last nhist (<= 4) steps, zeroed.
+ * isl_push_history: shift them back one step and store the current values as
+ * the latest.
+ * isl_set_inertia: the next assemblies add lhs_weight * M to the matrix and
+ * M h to the right-hand side, with M_ij = int density phi_i phi_j detJ w
+ * (base/kernel/Mass.hpp, the kernel's quadrature) and h = sum_s weights[s]
+ * x^(s), x^(0) the current values, x^(s) the values s steps back.  For a
+ * MultiStep method at time step k: lhs_weight = systemMassWeight(k) / dt and
+ * weights[s] = -reactionWeights(k)[s] / dt (incremental; weights[0] = 0
+ * otherwise).  Scalar kernels (Laplace, heat::Static); density NULL turns the
+ * terms off. */
+int isl_set_history(isl_ctx* ctx, int nhist);
+int isl_push_history(isl_ctx* ctx);
+int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double lhs_weight, int nweights,
+                    const double* weights);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
 int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] */);

@@ -107,6 +107,11 @@ struct ElemArgs {
     void* stageK;           // [nup][nelem] (R)
     double* stageF;         // [nloc][nelem]
     int* flags;
+    // inertia terms of a multi-step method (base/time/ReactionTerms.hpp):
+    // K += mass_w rho M, F += rho M h, h = the weighted DOF history; rho null: none
+    const double* rho;      // [nelem]
+    double mass_w;
+    const double* hvec;     // per dofobj comp
 };
 
 // ---------------------------------------------------------------------------
@@ -138,6 +143,12 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
     const bool aff = affine<SHAPE, NG, D>(X);
     double Ji[D][D], detJ = 0.0;
     if (aff) detJ = jac<NG, D>(X, T.dN[0], Ji);
+    double hloc[NF];
+    const double rho = A.rho ? A.rho[e] : 0.0;
+    if (A.rho) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) hloc[f] = A.hvec[A.edof[f * E + e]];
+    }
     R acc[NUP];
 #pragma unroll
     for (int u = 0; u < NUP; ++u) acc[u] = R(0);
@@ -177,6 +188,18 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 #pragma unroll
             for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
         }
+        if (A.rho) {  // base/kernel/Mass.hpp: M[i][j] += rho phi_i phi_j detJ w
+            const double m = rho * detJ * T.w[q];
+            double hq = 0.0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) hq += T.phi[q][f] * hloc[f];
+#pragma unroll
+            for (int M = 0; M < NF; ++M) {
+#pragma unroll
+                for (int N = M; N < NF; ++N) acc[upidx(M, N, NF)] += R(A.mass_w * m * T.phi[q][M] * T.phi[q][N]);
+                fe[M] += m * T.phi[q][M] * hq;
+            }
+        }
         if (A.with_residual) {
             double gu[D];
 #pragma unroll
@@ -204,6 +227,36 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 }
 
 // ---------------------------------------------------------------------------
+// Weighted DOF history of a multi-step method (ReactionTerms.hpp,
+// CollectWeightedHistory): h = w0 x^(0) + w1 x^(1) + ... with x^(0) the
+// current values and x^(s) = hist[s - 1] the values s steps back.
+__global__ void k_hist_combine(int64_t n, const double* __restrict__ u, const double* __restrict__ hist, int nw,
+                               double w0, double w1, double w2, double w3, double w4, double* __restrict__ h) {
+    const double w[5] = {w0, w1, w2, w3, w4};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = nw > 0 ? w[0] * u[i] : 0.0;
+        for (int k = 1; k < nw; ++k) s += w[k] * hist[(size_t)(k - 1) * n + i];
+        h[i] = s;
+    }
+}
+
+// history shift (base::dof::pushHistory): hist[s] = hist[s - 1], hist[0] = u
+__global__ void k_hist_push(int64_t n, int nhist, const double* __restrict__ u, double* __restrict__ hist) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int s = nhist - 1; s > 0; --s) hist[(size_t)s * n + i] = hist[(size_t)(s - 1) * n + i];
+        hist[i] = u[i];
+    }
+}
+
+int push_history_device(isl_ctx* c) {
+    const int64_t n = c->ndofobj * c->ncomp;
+    k_hist_push<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(n, c->nhist, c->du.p, c->dhist.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    return ISL_OK;
+}
+
+// ---------------------------------------------------------------------------
 // heat::Static element kernel (heat/Static.hpp:98-225), one thread per element,
 // with the isotropic materials of mat/thermal: IsotropicConstant (K = k I,
 // K' = 0) and FenicsTest (K = (1 + u)^m I, K' = m (1 + u)^(m-1) I,
@@ -227,9 +280,13 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
         for (int d = 0; d < D; ++d) X[i][d] = A.X[(size_t)nodes[i] * D + d];
     }
     const double prm = A.coef[e];
-    double uloc[NF];
+    double uloc[NF], hloc[NF];
 #pragma unroll
-    for (int f = 0; f < NF; ++f) uloc[f] = A.u[A.edof[f * E + e]];
+    for (int f = 0; f < NF; ++f) {
+        uloc[f] = A.u[A.edof[f * E + e]];
+        hloc[f] = A.rho ? A.hvec[A.edof[f * E + e]] : 0.0;
+    }
+    const double rho = A.rho ? A.rho[e] : 0.0;
     double K[NF][NF];
 #pragma unroll
     for (int i = 0; i < NF; ++i)
@@ -299,6 +356,18 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
             for (int i = 0; i < NG; ++i) f += T.N[q][i] * A.fnodal[nodes[i]];
 #pragma unroll
             for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
+        }
+        if (A.rho) {  // base/kernel/Mass.hpp: M[i][j] += rho phi_i phi_j detJ w
+            const double m = rho * dw;
+            double hq = 0.0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) hq += T.phi[q][f] * hloc[f];
+#pragma unroll
+            for (int i = 0; i < NF; ++i) {
+#pragma unroll
+                for (int j = 0; j < NF; ++j) K[i][j] += A.mass_w * m * T.phi[q][i] * T.phi[q][j];
+                fe[i] += m * T.phi[q][i] * hq;
+            }
         }
     }
     if (bad) atomicOr(A.flags, 1);
@@ -1179,6 +1248,23 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.stageK = k32 ? (void*)c->dstageK32.p : (void*)c->dstageK64.p;
     A.stageF = c->dstageF.p;
     A.flags = c->dflags.p;
+    A.rho = nullptr;
+    A.mass_w = 0.0;
+    A.hvec = nullptr;
+    if (c->inertia) {
+        if (c->kernel == ISL_KERNEL_HYPERELASTIC) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar kernels only");
+        // h = sum_s w_s x^(s): x^(0) the current values, x^(s) the s-th stored step
+        const int64_t ndc = c->ndofobj * c->ncomp;
+        ISL_CHECK_CUDA(c, c->dhvec.alloc(ndc));
+        k_hist_combine<<<(unsigned)c->sm_count * 8, 256, 0, st>>>(ndc, c->du.p, c->dhist.p, c->nhist_w, c->hist_w[0],
+                                                                 c->hist_w[1], c->hist_w[2], c->hist_w[3], c->hist_w[4],
+                                                                 c->dhvec.p);
+        ISL_CHECK_CUDA(c, cudaGetLastError());
+        c->launches += 1;
+        A.rho = c->drho.p;
+        A.mass_w = c->mass_w;
+        A.hvec = c->dhvec.p;
+    }
     int rc;
     if (c->kernel == ISL_KERNEL_LAPLACE) rc = k32 ? dispatch_laplace<float>(c, A) : dispatch_laplace<double>(c, A);
     else if (c->kernel == ISL_KERNEL_HEAT_STATIC) rc = dispatch_heat_static(c, A, with_residual);

@@ -533,6 +533,7 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->have64 = c->have32 = c->solved = false;
     // buffers sized by the previous field (a context reused for a new problem)
     c->dcval.release(); c->deq.release(); c->dstatus.release();
+    c->inertia = false; c->nhist = 0; c->dhist.release();
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
     c->inst_iters.clear(); c->inst_relres.clear();
@@ -809,6 +810,46 @@ int isl_set_heat_static(isl_ctx* c, int material, const double* param, int quad_
     c->stage_full = true;
     ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, param, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    return ISL_OK;
+}
+
+int isl_set_history(isl_ctx* c, int nhist) {
+    if (!c || !c->fedeg || nhist < 0 || nhist > 4) ISL_FAIL(c, ISL_ERR_ARG, "isl_set_history: 0..4 past steps");
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context");
+    cudaSetDevice(c->device);
+    const size_t n = (size_t)c->ndofobj * c->ncomp;
+    c->nhist = nhist;
+    if (nhist == 0) { c->dhist.release(); return ISL_OK; }
+    ISL_CHECK_CUDA(c, c->dhist.alloc(n * nhist));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dhist.p, 0, n * nhist * 8, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_push_history(isl_ctx* c) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    if (c->nhist == 0) ISL_FAIL(c, ISL_ERR_ARG, "isl_push_history: no history (isl_set_history)");
+    cudaSetDevice(c->device);
+    const int rc = isl::push_history_device(c);
+    if (rc != ISL_OK) return rc;
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+int isl_set_inertia(isl_ctx* c, const double* density, double lhs_weight, int nweights, const double* weights) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    if (!density) { c->inertia = false; return ISL_OK; }
+    if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar fields only");
+    if (nweights < 0 || nweights > 5 || nweights > c->nhist + 1 || (nweights > 0 && !weights))
+        ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: at most 5 weights and at most the stored history + 1");
+    cudaSetDevice(c->device);
+    ISL_CHECK_CUDA(c, c->drho.alloc(c->nelem));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->drho.p, density, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->inertia = true;
+    c->mass_w = lhs_weight;
+    c->nhist_w = nweights;
+    for (int k = 0; k < 5; ++k) c->hist_w[k] = k < nweights ? weights[k] : 0.0;
     return ISL_OK;
 }
 

@@ -148,6 +148,13 @@ struct isl_ctx {
     // kernel data
     int kernel = -1, material = 0, qdeg = 2, sqdeg = 2;
     bool stage_full = false;     // the kernel's element matrices are not symmetric: staged whole
+    // inertia terms of a multi-step method (isl_set_inertia) and the DOF history
+    bool inertia = false;
+    double mass_w = 0.0;         // LHS weight of the mass matrix (a0 / (b0 dt))
+    int nhist_w = 0;             // history weights in use (index 0: current values)
+    double hist_w[5] = {0, 0, 0, 0, 0};
+    int nhist = 0;               // stored past steps
+    isl::DBuf<double> drho, dhist, dhvec;  // density per element, [nhist][ndofobj*ncomp], weighted history
     bool pattern_full = false;   // the contribution lists index whole element matrices
     isl::DBuf<double> dcoef;     // SoA [ncoef][nelem]
     bool has_body = false;
@@ -268,6 +275,7 @@ struct isl_ctx {
 namespace isl {
 // device-side entry points implemented in the .cu files
 int pattern_build(isl_ctx* c);
+int push_history_device(isl_ctx* c);
 int assemble_device(isl_ctx* c, int precision, int incremental, int with_residual);
 int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int distribute_device(isl_ctx* c, int add);

@@ -136,6 +136,24 @@ class System:
         self._thermal = np.ascontiguousarray(param, dtype=np.float64)
         self._chk(self.L.isl_set_heat_static(self.h, m, A.d(self._thermal), quad_degree), "isl_set_heat_static")
 
+    # -- time integration (base/time/ReactionTerms.hpp) -------------------------
+    def set_history(self, nhist: int):
+        self._chk(self.L.isl_set_history(self.h, nhist), "isl_set_history")
+
+    def push_history(self):
+        self._chk(self.L.isl_push_history(self.h), "isl_push_history")
+
+    def set_inertia(self, density, lhs_weight: float, weights):
+        """computeInertiaTerms: lhs_weight * M into the matrix, M (sum_s w_s x^(s))
+        into the right-hand side; density None turns them off."""
+        if density is None:
+            self._chk(self.L.isl_set_inertia(self.h, None, 0.0, 0, None), "isl_set_inertia")
+            return
+        self._rho = np.ascontiguousarray(density, dtype=np.float64)
+        self._hw = np.ascontiguousarray(weights, dtype=np.float64)
+        self._chk(self.L.isl_set_inertia(self.h, A.d(self._rho), float(lhs_weight), len(self._hw), A.d(self._hw)),
+                  "isl_set_inertia")
+
     def set_hyperelastic(self, material: str, lam, mu, quad_degree: int):
         m = {"stvenant": A.MAT_STVENANT, "neohooke": A.MAT_NEOHOOKE}[material]
         self._lam = np.ascontiguousarray(lam, dtype=np.float64)

@@ -255,3 +255,56 @@ def heat_newton(S, n, max_iter=10, tolerance=1e-8, lin_tol=1e-11, method=None, l
         S.distribute(add=True)
         it += 1
     return rows
+
+
+# ---------------------------------------------------------------------------
+# Linear multi-step time integration (base/time/BDF.hpp, MultiStep.hpp)
+# BDF LHS weights a_0..a_q as base/time/BDF.hpp:95-104 defines them (its
+# 4th-order row carries +4/3 where the table in its comment has -4/3; the
+# coded values are the reference's behaviour).
+BDF_WEIGHTS = {1: [1.0, -1.0], 2: [1.5, -2.0, 0.5], 3: [11.0 / 6.0, -3.0, 1.5, -1.0 / 3.0],
+               4: [25.0 / 12.0, -4.0, 3.0, 4.0 / 3.0, 1.0 / 4.0]}
+
+
+def bdf_weights(order: int, step: int):
+    """systemMassWeight(step) and reactionWeights(step) of BDF<order>
+    (base/time/MultiStep.hpp:104-127): the order ramps up over the first steps,
+    q = order while step + 2 >= q + 1, else one lower (LHSWeights :28-44)."""
+    q = order
+    while q > 1 and step + 2 < q + 1:
+        q -= 1
+    a = BDF_WEIGHTS[q]
+    return a[0], list(a)
+
+
+def inertia_weights(order: int, step: int, dt: float, incremental: bool = True):
+    """lhs weight and history weights of isl_set_inertia for BDF<order> at a
+    step (ReactionTerms.hpp:214-248): a0 / dt and -a_s / dt, the current values'
+    weight dropped when not incremental"""
+    a0, a = bdf_weights(order, step)
+    w = [-x / dt for x in a]
+    if not incremental:
+        w[0] = 0.0
+    return a0 / dt, w
+
+
+def unsteady_heat(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None):
+    """Implicit BDF time stepping of rho du/dt - div(k grad u) = f on the
+    context's problem (scalar kernel already set, initial values in the DOFs):
+    per step one Newton iteration from the current values (the Laplace problem
+    is linear in u), then pushHistory.  Returns the DOF values after every
+    step."""
+    if method is None:
+        method = A.SOLVE_CG_FP64
+    out = []
+    S.set_history(order)
+    S.push_history()
+    for k in range(steps):
+        mw, w = inertia_weights(order, k, dt)
+        S.set_inertia(rho, mw, w[: order + 1])
+        S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+        S.solve(method, tol=lin_tol)
+        S.distribute(add=True)
+        S.push_history()
+        out.append(S.values())
+    return out

@@ -382,6 +382,12 @@ struct Problem {
     std::vector<double> kappa;      // per element
     std::vector<double> lam, mu;    // per element
     std::vector<double> thermal;    // per element: conductivity (IsotropicConstant) or exponent m (FenicsTest)
+    // inertia terms of a multi-step method (base/time/ReactionTerms.hpp:185-254)
+    bool inertia = false;
+    std::vector<double> rho;        // per element density
+    double massW = 0.0;             // LHS weight a0 / (b0 dt)
+    std::vector<double> histW;      // weight of x^(s), s = 0 (current), 1, ...
+    std::vector<double> hist;       // [nhist][ndofobj*ncomp] past DOF values, latest first
     int qdeg = 2;                   // volume quadrature degree
     // forces
     std::vector<double> fnodal;     // [nnodes][ncomp] body force, interpolated by geometry functions
@@ -650,6 +656,19 @@ static void elementKernel(const Problem& P, const QuadRule& Q, int64_t e, double
                     }
             }
         }
+    }
+}
+
+// Mass matrix (base/kernel/Mass.hpp:72-101): M[i][j] += rho phi_i phi_j detJ w
+static void elementMass(const Problem& P, const QuadRule& Q, int64_t e, double* Me) {
+    const int D = P.dim, nf = P.nfun;
+    std::fill(Me, Me + nf * nf, 0.0);
+    double g[27 * 3], xq[3], phi[27];
+    for (int q = 0; q < Q.n(); ++q) {
+        const double detJ = feGradX(P, e, &Q.x[q * D], g, xq, phi);
+        const double scalar = P.rho[e] * detJ * Q.w[q];
+        for (int M = 0; M < nf; ++M)
+            for (int N = 0; N < nf; ++N) Me[M * nf + N] += scalar * phi[M] * phi[N];
     }
 }
 
@@ -963,6 +982,16 @@ void orc_set_hyperelastic(void* h, int mat, const double* lam, const double* mu,
     P->lam.assign(lam, lam + P->nelem);
     P->mu.assign(mu, mu + P->nelem);
 }
+void orc_set_inertia(void* h, const double* rho, double massW, int nw, const double* w, int nhist, const double* hist) {
+    Problem* P = (Problem*)h;
+    P->inertia = rho != nullptr;
+    if (!rho) return;
+    P->rho.assign(rho, rho + P->nelem);
+    P->massW = massW;
+    P->histW.assign(w, w + nw);
+    const size_t ndc = (size_t)P->ndofobj * P->ncomp;
+    P->hist.assign(hist, hist + ndc * nhist);
+}
 void orc_set_heat_static(void* h, int mat, const double* param, int qdeg) {
     Problem* P = (Problem*)h;
     P->kernel = 2; P->material = mat; P->qdeg = qdeg;
@@ -1096,6 +1125,33 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
             }
             if (!any) continue;
             elementKernel(*P, Q, e, Ke.data(), nullptr);
+            if (P->inertia) {
+                // ReactionTerms: (a0/(b0 dt)) M into the matrix (lifted with the
+                // stiffness), M h into the forces, h = sum_s w_s x^(s)
+                std::vector<double> Me((size_t)nloc * nloc), he(nloc);
+                elementMass(*P, Q, e, Me.data());
+                const size_t ndc = (size_t)P->ndofobj * nd;
+                for (int a = 0; a < nloc; ++a) {
+                    const size_t k = (size_t)P->edof[e * nf + a / nd] * nd + a % nd;
+                    double h = 0.0;
+                    for (size_t sidx = 0; sidx < P->histW.size(); ++sidx)
+                        h += P->histW[sidx] * (sidx == 0 ? P->uval[k] : P->hist[(sidx - 1) * ndc + k]);
+                    he[a] = h;
+                }
+                for (int r = 0; r < nloc; ++r) {
+                    double fr = 0.0;
+                    for (int c2 = 0; c2 < nloc; ++c2) {
+                        Ke[r * nloc + c2] += P->massW * Me[r * nloc + c2];
+                        fr += Me[r * nloc + c2] * he[c2];
+                    }
+                    if (st[r] == 0) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                        P->rhs[q[r]] += fr;
+                    }
+                }
+            }
             for (int r = 0; r < nloc; ++r) {
                 if (st[r] != 0) continue;
                 const int64_t row = q[r];
