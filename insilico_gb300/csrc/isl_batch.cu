@@ -33,7 +33,7 @@ constexpr int SUB = 8;
 // per-instance scalar slots in dbs [slot][ninst]
 enum { S_ABSNEW, S_ABSOLD, S_ALPHA, S_BETA, S_RR, S_THRESH, S_RHS2, S_RRLAST, S_NS };
 // per-instance int slots in dbi [slot][ninst]
-enum { I_DONE, I_ITERS, I_BAD, I_UPDATE, I_NI };
+enum { I_DONE, I_ITERS, I_BAD, I_UPDATE, I_RESET, I_NI };
 // ticket slots in dbt [slot][ninst]; slot 3 element 0 counts remaining instances
 enum { T_SPMV, T_UPD, T_RES, T_NT };
 
@@ -54,6 +54,8 @@ struct BArgs {
     int* wl_cum;          // [ninst+1] row blocks of the listed instances before each entry
     int max_iter;
     double tol;
+    const int* blk_s0;    // batched sliced-ELL copy: slices of every row block
+    const int* blk_s1;
 };
 
 __device__ inline double& SS(const BArgs& a, int slot, int k) { return a.s[(size_t)slot * a.ninst + k]; }
@@ -168,6 +170,56 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
                 q[row] = acc[u];
                 loc += p[row] * acc[u];
             }
+        }
+    }
+    const double s1 = block_sum_t(loc, sh);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
+    if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
+        const double tot = inst_sum(a, k, 0, sh);
+        if (threadIdx.x == 0) {
+            SS(a, S_ALPHA, k) = SS(a, S_ABSNEW, k) / tot;
+            a.t[T_SPMV * a.ninst + k] = 0;
+        }
+    }
+}
+
+// q = A p on the batched sliced-ELL copy: a row block's rows are sorted by
+// length into slices of 32 (one lane per row); the block's 8 warps take its
+// slices in turn and keep the loads of U slots in flight per lane.  The
+// instance's p.q follows as in kb_spmv.
+template <int U, int MINB>
+__global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __restrict__ soff, const int* __restrict__ swid,
+                                                   const int* __restrict__ srow, const int* __restrict__ scol,
+                                                   const float* __restrict__ sv, const float* __restrict__ p,
+                                                   float* __restrict__ q) {
+    const int k = a.blk_inst[blockIdx.x];
+    if (II(a, I_DONE, k)) return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sl0 = a.blk_s0[blockIdx.x], sl1 = a.blk_s1[blockIdx.x];
+    float loc = 0.f;
+    for (int s = sl0 + warp; s < sl1; s += BBS / 32) {
+        const int o = soff[s] + lane, w = swid[s];
+        float acc = 0.f;
+        for (int kk = 0; kk < w; kk += U) {
+            int j[U];
+            float v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (kk + u < w) {
+                    j[u] = ld_stream(scol + o + (kk + u) * 32);
+                    v[u] = ld_stream(sv + o + (kk + u) * 32);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (kk + u < w) acc += v[u] * __ldg(p + j[u]);
+        }
+        const int row = srow[s * 32 + lane];
+        if (row >= 0) {
+            q[row] = acc;
+            loc += p[row] * acc;
         }
     }
     const double s1 = block_sum_t(loc, sh);
@@ -305,6 +357,10 @@ __global__ void __launch_bounds__(BBS) kb_residual_w(BArgs a, const int* __restr
         if (last_of(&a.t[T_RES * a.ninst + k], cnt)) {
             const double tot = reduce_parts(a.part + (size_t)a.inst_blk[k] * SUB, (int)cnt, 1, 0, sh);
             if (threadIdx.x == 0) {
+                // a true residual that has not dropped since the last update
+                // means the FP32 directions have lost conjugacy: restart them
+                const double prev = SS(a, S_RRLAST, k);
+                II(a, I_RESET, k) = (prev > 0.0 && tot >= prev) ? 1 : 0;
                 SS(a, S_RRLAST, k) = tot;
                 SS(a, S_RR, k) = tot;
                 if (!(tot == tot)) { II(a, I_BAD, k) = 1; finish(a, k, 3); }
@@ -335,7 +391,7 @@ __global__ void __launch_bounds__(BBS) kb_restart_w(BArgs a, const double* __res
         if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
             const double tot = reduce_parts(a.part + (size_t)a.inst_blk[k] * SUB, (int)cnt, 1, 0, sh);
             if (threadIdx.x == 0) {
-                SS(a, S_BETA, k) = tot / SS(a, S_ABSOLD, k);
+                SS(a, S_BETA, k) = II(a, I_RESET, k) ? 0.0 : tot / SS(a, S_ABSOLD, k);
                 SS(a, S_ABSNEW, k) = tot;
                 II(a, I_UPDATE, k) = 0;
                 a.t[T_SPMV * a.ninst + k] = 0;
@@ -365,6 +421,17 @@ void launch_kb_spmv(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, con
         case 8: kb_spmv<TV, TX, 8><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
         case 16: kb_spmv<TV, TX, 16><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
         default: kb_spmv<TV, TX, 32><<<grid, BBS, 0, st>>>(a, rp, ci, v, p, q); break;
+    }
+}
+
+// FP32 SpMV of the batched mixed solve: kind 2..32 CSR lanes per row,
+// 100 + U the batched sliced-ELL copy
+void launch_kb_spmv32(isl_ctx* c, int kind, unsigned grid, cudaStream_t st, const BArgs& a, const float* p, float* q) {
+    switch (kind) {
+        case 102: kb_sspmv<2, 8><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
+        case 104: kb_sspmv<4, 8><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
+        case 108: kb_sspmv<8, 6><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
+        default: launch_kb_spmv<float, float>(kind, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval32.p, p, q); break;
     }
 }
 
@@ -442,6 +509,8 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     a.wl_cum = c->dbwl.p + ni + 2;
     a.max_iter = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
     a.tol = tol;
+    a.blk_s0 = nullptr;
+    a.blk_s1 = nullptr;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbs.p, 0, (size_t)S_NS * ni * 8, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbi.p, 0, ((size_t)I_NI * ni + 1) * 4, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbt.p, 0, (size_t)T_NT * ni * 4, st));
@@ -475,10 +544,57 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         kb_dinv<float, float><<<vg, BBS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
         kb_init<double, float><<<grid, BBS, 0, st>>>(a, c->drhs.p, x32, r32, p32, d32);
         ISL_CHECK_CUDA(c, cudaGetLastError());
+        if (!c->bsell_built) {  // the batched sliced-ELL copy, once per pattern
+            std::vector<int32_t> b0((size_t)c->nbblocks), b1((size_t)c->nbblocks), s0, s1;
+            ISL_CHECK_CUDA(c, cudaMemcpyAsync(b0.data(), c->dblk_row0.p, b0.size() * 4, cudaMemcpyDeviceToHost, st));
+            ISL_CHECK_CUDA(c, cudaMemcpyAsync(b1.data(), c->dblk_row1.p, b1.size() * 4, cudaMemcpyDeviceToHost, st));
+            ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+            rc = batch_sell_pattern(c, b0, b1, s0, s1);
+            if (rc != ISL_OK) return rc;
+            if (c->ss_nslice > 0) {
+                ISL_CHECK_CUDA(c, c->dblk_s0.alloc(s0.size()));
+                ISL_CHECK_CUDA(c, c->dblk_s1.alloc(s1.size()));
+                ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_s0.p, s0.data(), s0.size() * 4, cudaMemcpyHostToDevice, st));
+                ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_s1.p, s1.data(), s1.size() * 4, cudaMemcpyHostToDevice, st));
+                ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+            }
+            c->bsell_built = true;
+            c->bspmv32 = 0;
+        }
+        rc = ensure_ssell(c);
+        if (rc != ISL_OK) return rc;
+        if (c->ss_nslice > 0) {
+            a.blk_s0 = c->dblk_s0.p;
+            a.blk_s1 = c->dblk_s1.p;
+        }
+        if (c->spmv32_forced > 0 && (c->spmv32_forced < 100 || c->ss_nslice > 0)) {
+            c->bspmv32 = c->spmv32_forced;
+        } else if (!c->bspmv32) {
+            // autotune: each candidate over 5 launches on the freshly started
+            // iteration (they only write q and the instances' alpha, which the
+            // first iteration recomputes)
+            const int cand[4] = {lpr, 102, 104, 108};
+            const int ncand = c->ss_nslice > 0 ? 4 : 1;
+            int best = lpr;
+            float bestms = 1e30f;
+            for (int k2 = 0; k2 < ncand && ncand > 1; ++k2) {
+                launch_kb_spmv32(c, cand[k2], grid, st, a, p32, q32);
+                cudaEventRecord(c->ev[2], st);
+                for (int r = 0; r < 5; ++r) launch_kb_spmv32(c, cand[k2], grid, st, a, p32, q32);
+                cudaEventRecord(c->ev[3], st);
+                cudaEventSynchronize(c->ev[3]);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+                if (ms < bestms) { bestms = ms; best = cand[k2]; }
+            }
+            c->launches += 6 * ncand;
+            c->bspmv32 = best;
+        }
+        c->spmv_lpr32 = c->bspmv32;
         ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < BCHUNK; ++k) {
             kb_dir<float><<<grid, BBS, 0, st>>>(a, r32, d32, p32);
-            launch_kb_spmv<float, float>(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval32.p, p32, q32);
+            launch_kb_spmv32(c, c->bspmv32, grid, st, a, p32, q32);
             kb_update<float><<<grid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
             // reliable updates of the instances kb_update listed
             kb_wl_scan<<<1, BBS, 0, st>>>(a);

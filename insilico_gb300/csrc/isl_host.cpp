@@ -536,6 +536,7 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->inertia = false; c->nhist = 0; c->dhist.release();
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
+    c->bsell_built = false;
     c->inst_iters.clear(); c->inst_relres.clear();
     c->blocked = false;
     if (n_dofobj) *n_dofobj = c->ndofobj;
@@ -736,6 +737,7 @@ int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
     c->nnz = 0;
     c->pattern_ready = false;
     c->nbblocks = 0;
+    c->bsell_built = false;
     if (c->device < 0) return ISL_OK;
     const size_t ndc = c->status.size();
     ISL_CHECK_CUDA(c, c->deq.alloc(ndc));
@@ -762,6 +764,7 @@ int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
     cudaSetDevice(c->device);
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
+    c->bsell_built = false;
     if (c->neq == 0) {  // every DOF constrained: an empty system, as the reference's Eigen3(0)
         c->nnz = 0;
         c->pattern_ready = true;

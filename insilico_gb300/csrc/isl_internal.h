@@ -219,6 +219,9 @@ struct isl_ctx {
 
     // batched CG (ninst > 1): row ranges of thread blocks and per-instance state
     isl::DBuf<int32_t> dinst_row, dblk_inst, dblk_row0, dblk_row1, dinst_blk;
+    isl::DBuf<int32_t> dblk_s0, dblk_s1;  // slices of every row block in the batched sliced-ELL copy
+    bool bsell_built = false;
+    int bspmv32 = 0;             // FP32 SpMV kind of the batched mixed solve (autotuned once per pattern)
     isl::DBuf<double> dbs;        // per-instance scalars [16][ninst]
     isl::DBuf<int32_t> dbi;       // per-instance ints   [8][ninst]
     isl::DBuf<unsigned int> dbt;  // per-instance tickets [4][ninst]
@@ -283,6 +286,9 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms);
 int time_kernels(isl_ctx* c, int nrep, double* ms);
 int block_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
 int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rowptr);
+int batch_sell_pattern(isl_ctx* c, const std::vector<int32_t>& b0, const std::vector<int32_t>& b1,
+                       std::vector<int32_t>& s0, std::vector<int32_t>& s1);
+int ensure_ssell(isl_ctx* c);
 // One level of n-faces for the device DOF numbering: nfc faces per element of
 // w vertices each (w = 0: the cell itself, not grouped), `stride` DOFs per
 // face starting at local DOF position `begin`.

@@ -372,7 +372,7 @@ __global__ void k_ssell_values(int n, const int* __restrict__ rowptr, const int*
 }
 
 // refresh the sliced-ELL values after an assembly
-static int ensure_ssell(isl_ctx* c) {
+int ensure_ssell(isl_ctx* c) {
     if (c->ss_nslice == 0 || c->ss_serial == c->asm_serial) return ISL_OK;
     k_ssell_values<<<vec_grid(c), BS, 0, c->stream>>>((int)c->neq, c->drowptr.p, c->dss_pos.p, c->dval32.p, c->dss_val.p);
     ISL_CHECK_CUDA(c, cudaGetLastError());
@@ -1844,6 +1844,68 @@ int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
                                              c->dss_row.p, c->dss_col.p, c->dss_pos.p);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));  // the host vectors above go out of scope
+    c->launches += 1;
+    c->ss_nslice = nslice;
+    c->ss_nslot = tot;
+    return ISL_OK;
+}
+
+// Sliced-ELL copy of a batch of instances (setup): each row block of the
+// batched solver (at most 2048 rows of one instance) is a sort window, so its
+// slices never mix instances; s0/s1 return the slice range of every block.
+// Needs 32-bit slot offsets; otherwise no copy is built (CSR only).
+int batch_sell_pattern(isl_ctx* c, const std::vector<int32_t>& b0, const std::vector<int32_t>& b1,
+                       std::vector<int32_t>& s0, std::vector<int32_t>& s1) {
+    c->ss_nslice = c->ss_nslot = 0;
+    c->ss_serial = -1;
+    const int64_t n = c->neq;
+    std::vector<int32_t> rp((size_t)n + 1);
+    cudaStream_t st = c->stream;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(rp.data(), c->drowptr.p, rp.size() * 4, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    const size_t nb = b0.size();
+    s0.assign(nb, 0);
+    s1.assign(nb, 0);
+    std::vector<int32_t> row, wid, off;
+    std::vector<int32_t> idx;
+    int64_t tot = 0;
+    for (size_t b = 0; b < nb; ++b) {
+        const int32_t r0 = b0[b], r1 = b1[b];
+        s0[b] = (int32_t)wid.size();
+        idx.resize((size_t)(r1 - r0));
+        for (int32_t i = r0; i < r1; ++i) idx[(size_t)(i - r0)] = i;
+        std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t bb) { return rp[a + 1] - rp[a] > rp[bb + 1] - rp[bb]; });
+        for (size_t k = 0; k < idx.size(); k += 32) {
+            int32_t w = 0;
+            for (size_t l = 0; l < 32; ++l) {
+                const int32_t r = k + l < idx.size() ? idx[k + l] : -1;
+                row.push_back(r);
+                if (r >= 0) w = std::max(w, rp[r + 1] - rp[r]);
+            }
+            wid.push_back(w);
+            off.push_back((int32_t)tot);
+            tot += (int64_t)w * 32;
+            if (tot >= INT32_MAX) { s0.clear(); s1.clear(); return ISL_OK; }
+        }
+        s1[b] = (int32_t)wid.size();
+    }
+    const int64_t nslice = (int64_t)wid.size();
+    if (nslice == 0) return ISL_OK;
+    off.push_back((int32_t)tot);
+    ISL_CHECK_CUDA(c, c->dss_off.alloc(nslice + 1));
+    ISL_CHECK_CUDA(c, c->dss_wid.alloc(nslice));
+    ISL_CHECK_CUDA(c, c->dss_row.alloc(nslice * 32));
+    ISL_CHECK_CUDA(c, c->dss_pos.alloc(n));
+    ISL_CHECK_CUDA(c, c->dss_col.alloc(tot));
+    ISL_CHECK_CUDA(c, c->dss_val.alloc(tot));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_wid.p, wid.data(), wid.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dss_row.p, row.data(), row.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dss_val.p, 0, (size_t)tot * 4, st));
+    k_ssell_fill<<<vec_grid(c), BS, 0, st>>>((int)nslice, c->drowptr.p, c->dcolind.p, c->dss_off.p, c->dss_wid.p,
+                                             c->dss_row.p, c->dss_col.p, c->dss_pos.p);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
     c->launches += 1;
     c->ss_nslice = nslice;
     c->ss_nslot = tot;
