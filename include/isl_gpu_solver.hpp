@@ -10,6 +10,13 @@
 //   computeResidualForces<FTB>(...)          base/asmb/ForceIntegrator.hpp:37-71   assemble(..., with_residual)
 //   finishAssembly()                         :142-153                         finishAssembly() (no-op)
 //   int cgSolve()                            :265-275                         cgSolve()
+//   int biCGStabSolve()                      :277-289                         biCGStabSolve() (Jacobi, not ILUT)
+//   smf::readMesh / writeMesh                base/io/smf/Reader.hpp, Writer.hpp     readSMF(path, shape), writeSMF(path)
+//   vtk::LegacyWriter + writePointData       base/io/vtk/LegacyWriter.hpp          writeVTK(path, name)
+//   post::errorComputation<ORDER>            base/post/ErrorNorm.hpp:84-123        errorComputation(order, qdeg, f)
+//   heat::Static<Material>                   heat/Static.hpp:98-225                heatStatic(material, param, qdeg)
+//   time::computeInertiaTerms<FTB,MSM>       base/time/ReactionTerms.hpp:62-79     inertia(density, lhs_w, weights)
+//   dof::pushHistory                         (DegreeOfFreedom)                     history(n), pushHistory()
 //   number getValue(i)                       :293-296                         getValue(i)
 //   double norm(), norm(first, last)         :128-138                         norm(), norm(first, last)
 //   insertToLHS / insertToRHS                :81-124                          not offered: assembly runs on the device
@@ -51,6 +58,16 @@ public:
     isl_ctx* ctx() { return ctx_; }
 
     // ---- mesh / field / DOFs (base::Unstructured, base::dof::generate, ...)
+    void readSMF(const std::string& path, int shape) {
+        check(ctx_, isl_mesh_read_smf(ctx_, path.c_str(), shape), "isl_mesh_read_smf");
+    }
+    void writeSMF(const std::string& path) { check(ctx_, isl_mesh_write_smf(ctx_, path.c_str()), "isl_mesh_write_smf"); }
+    // the field's values at the mesh nodes as POINT_DATA, optional per-cell data
+    void writeVTK(const std::string& path, const char* point_name, const char* cell_name = nullptr, int rows = 0,
+                  int cols = 0, const std::vector<double>& cell_values = {}) {
+        check(ctx_, isl_write_vtk(ctx_, path.c_str(), point_name, cell_name, rows, cols,
+                                  cell_values.empty() ? nullptr : cell_values.data()), "isl_write_vtk");
+    }
     void mesh(int shape, int dim, const std::vector<double>& X, const std::vector<int64_t>& conn, int nv) {
         check(ctx_, isl_mesh_upload(ctx_, shape, dim, (int64_t)X.size() / dim, X.data(), (int64_t)conn.size() / nv, conn.data()),
               "isl_mesh_upload");
@@ -98,6 +115,16 @@ public:
     void hyperElastic(int material, const std::vector<double>& lam, const std::vector<double>& mu, int quad_degree) {
         check(ctx_, isl_set_hyperelastic(ctx_, material, lam.data(), mu.data(), quad_degree), "isl_set_hyperelastic");
     }
+    void heatStatic(int material, const std::vector<double>& param, int quad_degree) {
+        check(ctx_, isl_set_heat_static(ctx_, material, param.data(), quad_degree), "isl_set_heat_static");
+    }
+    // time integration: keep n past steps; inertia terms for the next assemblies
+    void history(int n) { check(ctx_, isl_set_history(ctx_, n), "isl_set_history"); }
+    void pushHistory() { check(ctx_, isl_push_history(ctx_), "isl_push_history"); }
+    void inertia(const std::vector<double>& density, double lhs_weight, const std::vector<double>& weights) {
+        check(ctx_, isl_set_inertia(ctx_, density.data(), lhs_weight, (int)weights.size(), weights.data()),
+              "isl_set_inertia");
+    }
     void bodyForceNodal(const std::vector<double>& f) {
         check(ctx_, isl_set_body_force_nodal(ctx_, f.data()), "isl_set_body_force_nodal");
     }
@@ -122,6 +149,29 @@ public:
         check(ctx_, isl_solve(ctx_, ISL_SOLVE_CG_FP32_IR, tol, 0, &it, &rr), "isl_solve");
         cache_.clear();
         return (int)it;
+    }
+    int biCGStabSolve(double tol = 2.220446049250313e-16) {
+        int64_t it = 0;
+        double rr = 0.0;
+        const int st = isl_solve(ctx_, ISL_SOLVE_BICGSTAB, tol, 0, &it, &rr);
+        if (st != ISL_OK && st != ISL_ERR_NOT_CONVERGED) check(ctx_, st, "isl_solve");
+        cache_.clear();
+        return (int)it;
+    }
+    // errorComputation<order>: f(x, out) writes the reference value (order 0:
+    // ncomp values) or gradient (order 1: ncomp x dim) at a quadrature point
+    template <typename FUN>
+    double errorComputation(int order, int quad_degree, int dim, FUN f) {
+        int64_t n = 0;
+        check(ctx_, isl_quadrature_points(ctx_, quad_degree, &n, nullptr), "isl_quadrature_points");
+        std::vector<double> x((size_t)n * dim);
+        check(ctx_, isl_quadrature_points(ctx_, quad_degree, &n, x.data()), "isl_quadrature_points");
+        const int per = ncomp_ * (order == 1 ? dim : 1);
+        std::vector<double> ref((size_t)n * per);
+        for (int64_t i = 0; i < n; ++i) f(&x[(size_t)i * dim], &ref[(size_t)i * per]);
+        double err = 0.0;
+        check(ctx_, isl_error_norm(ctx_, order, quad_degree, ref.data(), &err), "isl_error_norm");
+        return err;
     }
     double getValue(std::size_t i) {
         fill();
