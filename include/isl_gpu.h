@@ -138,7 +138,7 @@ int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_el
 /* Time integration by a linear multi-step method: the inertia terms of
  * base::time::computeInertiaTerms (base/time/ReactionTerms.hpp:62-79,
  * ReactionTerms::operator() :185-254) and the DOF history
- * (DegreeOfFreedom::pushHistory).
+ * (DegreeOfFreedom::pushHistory, base/dof/DegreeOfFreedom.hpp:185-190).
  * isl_set_history: keep the DOF values of the last nhist (<= 4) steps, zeroed.
  * isl_push_history: shift them back one step and store the current values as
  * the latest.
