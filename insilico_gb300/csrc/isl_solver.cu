@@ -390,8 +390,13 @@ static int autotune_spmv32(isl_ctx* c, const float* p, float* q, CGScal* S, doub
     int best = 2;
     while (best < 32 && best < avg / 2) best *= 2;
     if (c->neq < 20000) return best;  // too small to time meaningfully
-    int cand[7] = {4, 8, 16, 32, 102, 104, 108};
+    // preference order; the first within 2 % of the fastest is kept, so that
+    // the choice (and the rounding of p.q, which follows the grid) does not
+    // flip with timing noise
+    int cand[7] = {104, 102, 108, 4, 8, 16, 32};
+    if (c->ss_nslice == 0) { cand[0] = 4; cand[1] = 8; cand[2] = 16; cand[3] = 32; }
     const int ncand = c->ss_nslice > 0 ? 7 : 4;
+    float ms_of[7];
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
     c->launches += 21 * ncand;
@@ -403,8 +408,11 @@ static int autotune_spmv32(isl_ctx* c, const float* p, float* q, CGScal* S, doub
         cudaEventSynchronize(c->ev[3]);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
-        if (ms < bestms) { bestms = ms; best = cand[k]; }
+        ms_of[k] = ms;
+        bestms = std::min(bestms, ms);
     }
+    for (int k = 0; k < ncand; ++k)
+        if (ms_of[k] <= 1.02f * bestms) return cand[k];
     return best;
 }
 
@@ -1701,10 +1709,16 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 }
 
 // autotune of the block SpMV (format and row mapping) on the current matrix
+// The variants launch different grids, so the p.q partial sums, and with them
+// the rounding of alpha, follow the choice: a different variant moves the CG
+// iteration count by a few percent.  To keep the choice, and the iteration
+// count, the same from run to run despite timing noise, the candidates are
+// ranked in a fixed preference order and the first within 2 % of the fastest
+// is taken.
 static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
-    const int cand[9] = {1, 2, 3, 5, 6, 7, 4, 8, 16};
+    const int cand[9] = {7, 6, 5, 1, 2, 3, 4, 8, 16};  // preference order
     if (c->nbr < 8000) return 2;
-    int best = 2;
+    float ms_of[9];
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
     c->launches += 9 * 21;
@@ -1716,9 +1730,12 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
         cudaEventSynchronize(c->ev[3]);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
-        if (ms < bestms) { bestms = ms; best = cand[k]; }
+        ms_of[k] = ms;
+        bestms = std::min(bestms, ms);
     }
-    return best;
+    for (int k = 0; k < 9; ++k)
+        if (ms_of[k] <= 1.02f * bestms) return cand[k];
+    return cand[0];
 }
 
 // detect the node-blocked structure and build the block pattern (setup)
