@@ -1,17 +1,20 @@
 // ORACLE — test infrastructure only.
 //
 // CPU restatement of the inSilico assembly + Krylov path (reference project
-// thrueberg/inSilico, header-only C++).  This file is the checker that the
-// CUDA library is compared against; it is never linked into, called by, or
-// used as a fallback for the product library.  Only tests/, the smoke check
-// and the CPU-baseline leg of bench.py load it.
+// thrueberg/inSilico, header-only C++).  The CUDA library is compared against
+// this oracle; it is never linked into, called by, or used as a fallback for
+// the product library.  Only tests/, the smoke check and the CPU-baseline leg
+// of bench.py load it.
 //
 // Parity pin: the DOF numbering / sparsity output, the linear-elastic and
 // compressible neo-Hookean drivers and the mixed Poisson driver reproduce the
 // reference's golden files (reference/03-doFHandler/sparsity.{1,2,3}.ref.dat,
 // reference/06-elastic/linearElastic{2,3}D.ref.dat,
-// reference/06-elastic/compRefOut{D,N}.dat, reference/05-mixedPoisson/ref);
-// the pins are checked by tests/test_oracle_golden.py.
+// reference/06-elastic/compRefOut{D,N}.dat, reference/05-mixedPoisson/ref,
+// reference/04-heat/nonlinearHeat.ref.dat); the pins are checked by
+// tests/test_oracle_golden.py.  The inertia terms of time integration
+// (ReactionTerms) have no golden output in the reference; they are restated
+// from base/time/ReactionTerms.hpp and base/kernel/Mass.hpp only.
 //
 // Every block cites the reference file:line whose algorithm it restates.
 // Third-party arithmetic the reference delegates to Eigen 3.2.0 (small dense
