@@ -11,6 +11,7 @@ The drivers below re-run the reference's golden applications on the oracle:
 * :func:`linear_elastic` — reference/06-elastic/linearElastic.cpp:80-216
 * :func:`compressible` — reference/06-elastic/compressible.cpp:104-340
 * :func:`mixed_poisson` — reference/05-mixedPoisson/mixedPoisson.cpp:100-230
+* :func:`nonlinear_heat` — reference/04-heat/nonlinearHeat.cpp:88-237
 """
 from __future__ import annotations
 
