@@ -154,6 +154,14 @@ int isl_set_history(isl_ctx* ctx, int nhist);
 int isl_push_history(isl_ctx* ctx);
 int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double lhs_weight, int nweights,
                     const double* weights);
+/* The residual-force history of a multi-step method with RHS weights
+ * (Adams-Moulton; base::time::computeResidualForceHistory,
+ * base/time/ResidualForceHistory.hpp): the next assemblies add
+ * -sum_s weights[s-1] F(x^(s)) to the right-hand side, F the kernel's internal
+ * force (residualForceHistory<s>) at the values s steps back, s = 1..nweights
+ * (<= the stored history, <= 4).  For a MultiStep method at step k: weights =
+ * forceWeights(k).  Scalar kernels; nweights 0 turns it off. */
+int isl_set_force_history(isl_ctx* ctx, int nweights, const double* weights);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
 int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] */);

@@ -42,7 +42,7 @@ EXPORTED = [
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc", "isl_quadrature_points",
     "isl_error_norm", "isl_mesh_read_smf", "isl_mesh_get", "isl_mesh_write_smf", "isl_write_vtk",
-    "isl_set_heat_static", "isl_set_history", "isl_push_history", "isl_set_inertia",
+    "isl_set_heat_static", "isl_set_history", "isl_push_history", "isl_set_inertia", "isl_set_force_history",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND) = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
@@ -110,6 +110,7 @@ def load(build_if_missing: bool = False):
     L.isl_set_history.argtypes = [_P, i]
     L.isl_push_history.argtypes = [_P]
     L.isl_set_inertia.argtypes = [_P, _D, C.c_double, i, _D]
+    L.isl_set_force_history.argtypes = [_P, i, _D]
     L.isl_mesh_get.argtypes = [_P, _I64, _I64, _D, _I64]
     L.isl_mesh_write_smf.argtypes = [_P, C.c_char_p]
     L.isl_write_vtk.argtypes = [_P, C.c_char_p, C.c_char_p, C.c_char_p, i, i, _D]

@@ -112,6 +112,12 @@ struct ElemArgs {
     const double* rho;      // [nelem]
     double mass_w;
     const double* hvec;     // per dofobj comp
+    // residual forces at past states (base/time/ResidualForceHistory.hpp):
+    // F -= sum_s fw[s] F_int(x^(s+1)), x^(s+1) = hist[s * hstride + .]
+    const double* hist;
+    int64_t hstride;
+    int nfw;
+    double fw[4];
 };
 
 // ---------------------------------------------------------------------------
@@ -119,7 +125,9 @@ struct ElemArgs {
 //   K[M][N] += (grad phi_M . grad phi_N) (kappa detJ w)   base/kernel/Laplace.hpp:131-148
 //   F[i]    -= kappa grad u . grad phi_i detJ w           heat/Laplace.hpp:150-183 (x -1)
 //   F[s]    += f(x) phi_s w detJ                          base/asmb/BodyForce.hpp:172-205
-template <int SHAPE, int FDEG, int NQ, typename R>
+// TI: the time-integration terms (mass matrix, weighted history, residual
+// forces at past states) are compiled in; the plain assembly runs without them
+template <int SHAPE, int FDEG, int NQ, typename R, bool TI>
 __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T) {
     constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
     constexpr int NUP = NF * (NF + 1) / 2;
@@ -144,8 +152,8 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
     double Ji[D][D], detJ = 0.0;
     if (aff) detJ = jac<NG, D>(X, T.dN[0], Ji);
     double hloc[NF];
-    const double rho = A.rho ? A.rho[e] : 0.0;
-    if (A.rho) {
+    const double rho = (TI && A.rho) ? A.rho[e] : 0.0;
+    if (TI && A.rho) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) hloc[f] = A.hvec[A.edof[f * E + e]];
     }
@@ -188,7 +196,7 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 #pragma unroll
             for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
         }
-        if (A.rho) {  // base/kernel/Mass.hpp: M[i][j] += rho phi_i phi_j detJ w
+        if (TI && A.rho) {  // base/kernel/Mass.hpp: M[i][j] += rho phi_i phi_j detJ w
             const double m = rho * detJ * T.w[q];
             double hq = 0.0;
 #pragma unroll
@@ -215,6 +223,24 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 #pragma unroll
                 for (int k = 0; k < D; ++k) dp += gu[k] * g[i][k];
                 fe[i] -= dp * detJ * T.w[q];
+            }
+        }
+        for (int sidx = 0; TI && sidx < A.nfw; ++sidx) {  // heat/Laplace.hpp:150-183 at a past state
+            double gu[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) gu[k] = 0.0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double hf = A.hist[(size_t)sidx * A.hstride + A.edof[f * E + e]];
+#pragma unroll
+                for (int k = 0; k < D; ++k) gu[k] += g[f][k] * hf;
+            }
+#pragma unroll
+            for (int i = 0; i < NF; ++i) {
+                double dp = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) dp += kap * gu[k] * g[i][k];
+                fe[i] -= A.fw[sidx] * dp * detJ * T.w[q];
             }
         }
     }
@@ -356,6 +382,26 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
             for (int i = 0; i < NG; ++i) f += T.N[q][i] * A.fnodal[nodes[i]];
 #pragma unroll
             for (int s = 0; s < NF; ++s) fe[s] += f * T.phi[q][s] * T.w[q] * detJ;
+        }
+        for (int sidx = 0; sidx < A.nfw; ++sidx) {  // residualForceHistory at a past state
+            double us = 0.0, gus[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) gus[k] = 0.0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double hf = A.hist[(size_t)sidx * A.hstride + A.edof[f * E + e]];
+                us += T.phi[q][f] * hf;
+#pragma unroll
+                for (int k = 0; k < D; ++k) gus[k] += g[f][k] * hf;
+            }
+            const double ks = A.material == ISL_THERMAL_FENICS ? pow(1.0 + us, prm) : prm;
+#pragma unroll
+            for (int i = 0; i < NF; ++i) {
+                double sum = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) sum += g[i][k] * ks * gus[k];
+                fe[i] -= A.fw[sidx] * sum * dw;
+            }
         }
         if (A.rho) {  // base/kernel/Mass.hpp: M[i][j] += rho phi_i phi_j detJ w
             const double m = rho * dw;
@@ -1083,7 +1129,10 @@ static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
     if (!make_host_tables(SHAPE, FDEG, c->qdeg, h) || h.nq != NQ) ISL_FAIL(c, ISL_ERR_ARG, "quadrature");
     Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T;
     fill_tab<SHAPE, FDEG, NQ>(T, h);
-    k_laplace<SHAPE, FDEG, NQ, R><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    if (A.rho || A.nfw > 0)
+        k_laplace<SHAPE, FDEG, NQ, R, true><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    else
+        k_laplace<SHAPE, FDEG, NQ, R, false><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     return ISL_OK;
@@ -1251,6 +1300,12 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.rho = nullptr;
     A.mass_w = 0.0;
     A.hvec = nullptr;
+    A.hist = c->dhist.p;
+    A.hstride = c->ndofobj * c->ncomp;
+    A.nfw = c->nforce_w;
+    for (int k = 0; k < 4; ++k) A.fw[k] = k < c->nforce_w ? c->force_w[k] : 0.0;
+    if (c->nforce_w > 0 && c->kernel == ISL_KERNEL_HYPERELASTIC)
+        ISL_FAIL(c, ISL_ERR_ARG, "residual force history: scalar kernels only");
     if (c->inertia) {
         if (c->kernel == ISL_KERNEL_HYPERELASTIC) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar kernels only");
         // h = sum_s w_s x^(s): x^(0) the current values, x^(s) the s-th stored step

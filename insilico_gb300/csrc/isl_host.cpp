@@ -533,7 +533,7 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->have64 = c->have32 = c->solved = false;
     // buffers sized by the previous field (a context reused for a new problem)
     c->dcval.release(); c->deq.release(); c->dstatus.release();
-    c->inertia = false; c->nhist = 0; c->dhist.release();
+    c->inertia = false; c->nhist = 0; c->dhist.release(); c->nforce_w = 0;
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
     c->bsell_built = false;
@@ -853,6 +853,16 @@ int isl_set_inertia(isl_ctx* c, const double* density, double lhs_weight, int nw
     c->mass_w = lhs_weight;
     c->nhist_w = nweights;
     for (int k = 0; k < 5; ++k) c->hist_w[k] = k < nweights ? weights[k] : 0.0;
+    return ISL_OK;
+}
+
+int isl_set_force_history(isl_ctx* c, int nweights, const double* weights) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    if (nweights < 0 || nweights > 4 || nweights > c->nhist || (nweights > 0 && !weights))
+        ISL_FAIL(c, ISL_ERR_ARG, "residual force history: at most 4 weights and at most the stored history");
+    if (nweights > 0 && c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "residual force history: scalar fields only");
+    c->nforce_w = nweights;
+    for (int k = 0; k < 4; ++k) c->force_w[k] = k < nweights ? weights[k] : 0.0;
     return ISL_OK;
 }
 

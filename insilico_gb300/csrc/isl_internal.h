@@ -154,6 +154,8 @@ struct isl_ctx {
     int nhist_w = 0;             // history weights in use (index 0: current values)
     double hist_w[5] = {0, 0, 0, 0, 0};
     int nhist = 0;               // stored past steps
+    int nforce_w = 0;            // residual-force history weights in use (x^(1), x^(2), ...)
+    double force_w[4] = {0, 0, 0, 0};
     isl::DBuf<double> drho, dhist, dhvec;  // density per element, [nhist][ndofobj*ncomp], weighted history
     bool pattern_full = false;   // the contribution lists index whole element matrices
     isl::DBuf<double> dcoef;     // SoA [ncoef][nelem]

@@ -154,6 +154,11 @@ class System:
         self._chk(self.L.isl_set_inertia(self.h, A.d(self._rho), float(lhs_weight), len(self._hw), A.d(self._hw)),
                   "isl_set_inertia")
 
+    def set_force_history(self, weights):
+        """computeResidualForceHistory: -sum_s w[s-1] F(x^(s)) into the forces."""
+        self._fw = np.ascontiguousarray(weights, dtype=np.float64) if len(weights) else np.zeros(1)
+        self._chk(self.L.isl_set_force_history(self.h, len(weights), A.d(self._fw)), "isl_set_force_history")
+
     def set_hyperelastic(self, material: str, lam, mu, quad_degree: int):
         m = {"stvenant": A.MAT_STVENANT, "neohooke": A.MAT_NEOHOOKE}[material]
         self._lam = np.ascontiguousarray(lam, dtype=np.float64)

@@ -288,23 +288,54 @@ def inertia_weights(order: int, step: int, dt: float, incremental: bool = True):
     return a0 / dt, w
 
 
-def unsteady_heat(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None):
-    """Implicit BDF time stepping of rho du/dt - div(k grad u) = f on the
-    context's problem (scalar kernel already set, initial values in the DOFs):
-    per step one Newton iteration from the current values (the Laplace problem
-    is linear in u), then pushHistory.  Returns the DOF values after every
-    step."""
+# Adams-Moulton RHS weights b_0..b_{q-1} (base/time/AdamsMoulton.hpp:70-84);
+# its LHS weights are always (1, -1)
+AM_WEIGHTS = {1: [1.0], 2: [0.5, 0.5], 3: [5.0 / 12.0, 2.0 / 3.0, -1.0 / 12.0],
+              4: [3.0 / 8.0, 19.0 / 24.0, -5.0 / 24.0, 1.0 / 24.0]}
+
+
+def multistep_weights(method: str, order: int, step: int):
+    """LHS and RHS weights of BDF<order> or AdamsMoulton<order> at a step, with
+    the ramp-up of base/time/MultiStep.hpp:28-62 (a lower order while the step
+    count cannot feed the full formula)."""
+    if method == "bdf":
+        return bdf_weights(order, step)[1], [1.0]
+    q = order
+    while q > 1 and step + 2 < q:
+        q -= 1
+    return [1.0, -1.0], list(AM_WEIGHTS[q])
+
+
+def time_weights(method: str, order: int, step: int, dt: float, incremental: bool = True):
+    """The arguments of isl_set_inertia and isl_set_force_history for a step:
+    systemMassWeight / dt, -reactionWeights / dt (MultiStep.hpp:104-127) and the
+    forceWeights b_s / b_0, s >= 1 (:129-137)."""
+    a, b = multistep_weights(method, order, step)
+    w = [-(x / b[0]) / dt for x in a]
+    if not incremental:
+        w[0] = 0.0
+    return a[0] / b[0] / dt, w, [x / b[0] for x in b[1:]]
+
+
+def unsteady_heat(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None, scheme="bdf", newton=1):
+    """Implicit multi-step time stepping (BDF or Adams-Moulton) of
+    rho du/dt - div(k grad u) = f on the context's problem (scalar kernel
+    already set, initial values in the DOFs): per step `newton` Newton
+    iterations from the current values (one suffices for Laplace, which is
+    linear in u), then pushHistory.  Returns the DOF values after every step."""
     if method is None:
         method = A.SOLVE_CG_FP64
     out = []
     S.set_history(order)
     S.push_history()
     for k in range(steps):
-        mw, w = inertia_weights(order, k, dt)
-        S.set_inertia(rho, mw, w[: order + 1])
-        S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
-        S.solve(method, tol=lin_tol)
-        S.distribute(add=True)
+        mw, w, fw = time_weights(scheme, order, k, dt)
+        S.set_inertia(rho, mw, w)
+        S.set_force_history(fw)
+        for _ in range(newton):
+            S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+            S.solve(method, tol=lin_tol)
+            S.distribute(add=True)
         S.push_history()
         out.append(S.values())
     return out

@@ -69,7 +69,7 @@ def lib():
         L.orc_set_laplace.argtypes = [_P, _D, C.c_int]
         L.orc_set_hyperelastic.argtypes = [_P, C.c_int, _D, _D, C.c_int]
         L.orc_set_heat_static.argtypes = [_P, C.c_int, _D, C.c_int]
-        L.orc_set_inertia.argtypes = [_P, _D, C.c_double, C.c_int, _D, C.c_int, _D]
+        L.orc_set_inertia.argtypes = [_P, _D, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, _D]
         L.orc_set_body_nodal.argtypes = [_P, _D]
         L.orc_set_body_cosproduct.argtypes = [_P, _D]
         L.orc_set_neumann.argtypes = [_P, C.c_int, C.c_int64, _I64, _I32, _D, C.c_double, C.c_int]
@@ -208,18 +208,21 @@ class Problem:
         self._thermal = np.ascontiguousarray(param, dtype=np.float64)
         self.L.orc_set_heat_static(self.h, {"constant": 0, "fenics": 1}[material], _d(self._thermal), qdeg)
 
-    def set_inertia(self, rho, mass_w, weights, history):
+    def set_inertia(self, rho, mass_w, weights, history, force_weights=()):
         """ReactionTerms (base/time/ReactionTerms.hpp): mass_w * M into the
         matrix, M (sum_s weights[s] x^(s)) into the forces; x^(0) the current
-        values, history = [x^(1), x^(2), ...]; rho None turns them off."""
+        values, history = [x^(1), x^(2), ...]; force_weights[s-1] weighs the
+        residual force at x^(s) (ResidualForceHistory.hpp); rho None turns
+        them off."""
         if rho is None:
-            self.L.orc_set_inertia(self.h, None, 0.0, 0, None, 0, None)
+            self.L.orc_set_inertia(self.h, None, 0.0, 0, None, 0, None, 0, None)
             return
         self._rho = np.ascontiguousarray(rho, dtype=np.float64)
         self._hw = np.ascontiguousarray(weights, dtype=np.float64)
+        self._fw = np.ascontiguousarray(force_weights, dtype=np.float64) if len(force_weights) else np.zeros(1)
         self._hist = np.ascontiguousarray(np.array(history, dtype=np.float64).reshape(-1)) if len(history) else np.zeros(1)
         self.L.orc_set_inertia(self.h, _d(self._rho), float(mass_w), len(self._hw), _d(self._hw), len(history),
-                               _d(self._hist))
+                               _d(self._hist), len(force_weights), _d(self._fw))
 
     def set_body_nodal(self, f):
         self._f = np.ascontiguousarray(f, dtype=np.float64)

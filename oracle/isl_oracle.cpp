@@ -391,6 +391,9 @@ struct Problem {
     double massW = 0.0;             // LHS weight a0 / (b0 dt)
     std::vector<double> histW;      // weight of x^(s), s = 0 (current), 1, ...
     std::vector<double> hist;       // [nhist][ndofobj*ncomp] past DOF values, latest first
+    // residual-force history of a multi-step method with RHS weights
+    // (base/time/ResidualForceHistory.hpp): forces -= sum_s forceW[s-1] F(x^(s))
+    std::vector<double> forceW;     // weights of x^(1), x^(2), ...
     int qdeg = 2;                   // volume quadrature degree
     // forces
     std::vector<double> fnodal;     // [nnodes][ncomp] body force, interpolated by geometry functions
@@ -985,13 +988,15 @@ void orc_set_hyperelastic(void* h, int mat, const double* lam, const double* mu,
     P->lam.assign(lam, lam + P->nelem);
     P->mu.assign(mu, mu + P->nelem);
 }
-void orc_set_inertia(void* h, const double* rho, double massW, int nw, const double* w, int nhist, const double* hist) {
+void orc_set_inertia(void* h, const double* rho, double massW, int nw, const double* w, int nhist, const double* hist,
+                     int nfw, const double* fw) {
     Problem* P = (Problem*)h;
     P->inertia = rho != nullptr;
     if (!rho) return;
     P->rho.assign(rho, rho + P->nelem);
     P->massW = massW;
     P->histW.assign(w, w + nw);
+    P->forceW.assign(fw, fw + nfw);
     const size_t ndc = (size_t)P->ndofobj * P->ncomp;
     P->hist.assign(hist, hist + ndc * nhist);
 }
@@ -1084,6 +1089,23 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
                     if (q >= 0) P->rhs[q] += -1.0 * Fe[a];
                 }
             }
+        }
+        if (P->inertia && !P->forceW.empty()) {
+            // base/time/ResidualForceHistory.hpp: the kernel's residual force at
+            // the past states, weighted, with the residual's factor -1
+            const size_t ndc = (size_t)P->ndofobj * nd;
+            std::vector<double> cur = P->uval;
+            for (size_t sidx = 0; sidx < P->forceW.size(); ++sidx) {
+                P->uval.assign(P->hist.begin() + sidx * ndc, P->hist.begin() + (sidx + 1) * ndc);
+                for (int64_t e = 0; e < P->nelem; ++e) {
+                    elementKernel(*P, Q, e, nullptr, Fe.data());
+                    for (int a = 0; a < nloc; ++a) {
+                        const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
+                        if (q >= 0) P->rhs[q] += -P->forceW[sidx] * Fe[a];
+                    }
+                }
+            }
+            P->uval = cur;
         }
         if (P->bodyKind) {
             for (int64_t e = 0; e < P->nelem; ++e) {

@@ -129,46 +129,63 @@ def test_bicgstab_sliced_ell_and_csr_agree():
     S.close()
 
 
-@pytest.mark.parametrize("kind,shape,deg,sizes,order", [
-    ("quad", A.QUAD, 2, (8, 6), 2), ("quad", A.QUAD, 1, (12, 9), 3), ("tet", A.TET, 2, (3, 3, 2), 2),
+# Adams-Moulton is not A-stable beyond order 2, and the trapezoidal rule
+# oscillates at large steps: the heat::Static cases keep u > -1, where
+# (1 + u)^m is defined, through their step sizes (checked on the oracle)
+@pytest.mark.parametrize("kind,shape,deg,sizes,order,scheme,kernel,dt", [
+    ("quad", A.QUAD, 2, (8, 6), 2, "bdf", "laplace", 0.01), ("quad", A.QUAD, 1, (12, 9), 3, "bdf", "laplace", 0.01),
+    ("tet", A.TET, 2, (3, 3, 2), 2, "bdf", "laplace", 0.01), ("quad", A.QUAD, 2, (8, 6), 2, "am", "laplace", 0.01),
+    ("quad", A.QUAD, 1, (10, 7), 3, "am", "laplace", 0.01), ("quad", A.QUAD, 2, (7, 5), 2, "am", "fenics", 1e-3),
+    ("quad", A.QUAD, 2, (7, 5), 3, "am", "fenics", 2e-5), ("quad", A.QUAD, 2, (7, 5), 2, "bdf", "fenics", 0.01),
 ])
-def test_unsteady_heat_bdf_matches_oracle(kind, shape, deg, sizes, order):
-    """BDF time stepping with the inertia terms of base/time/ReactionTerms.hpp
-    (mass matrix into the tangent, weighted DOF history into the forces): every
-    step's DOF values equal the oracle's to 1e-10.  The reference has no golden
-    output for time integration (its users are sandbox apps), so this pins the
-    device to the oracle's restatement only."""
+def test_unsteady_heat_multistep_matches_oracle(kind, shape, deg, sizes, order, scheme, kernel, dt):
+    """BDF and Adams-Moulton time stepping: the inertia terms of
+    base/time/ReactionTerms.hpp (mass matrix into the tangent, weighted DOF
+    history into the forces) and, for Adams-Moulton, the residual forces at
+    past states (ResidualForceHistory.hpp), with the Laplace kernel and with
+    heat::Static (two Newton iterations per step): every step's DOF values
+    equal the oracle's to 1e-10.  The reference has no golden output for time
+    integration (its users are sandbox apps), so this pins the device to the
+    oracle's restatement only."""
     import scipy.sparse as sp
     from scipy.sparse.linalg import spsolve
     X, conn = W.unit_cube(kind, *sizes)
     rng = np.random.default_rng(3)
     kappa = rng.uniform(0.5, 2.0, len(conn))
     rho = rng.uniform(0.5, 1.5, len(conn))
-    dt, steps = 0.01, 5
+    steps = 5
     S = System(device=0)
     S.upload_mesh(shape, X, conn)
     S.create_field(deg, 1)
     S.constrain_boundary(lambda x: (np.ones((len(x), 1), bool), 0.0))
     S.number_dofs()
     S.register_pattern()
-    S.set_laplace(kappa, 2)
     P = O.Problem({A.QUAD: O.QUAD, A.TET: O.TET, A.HEX: O.HEX}[shape], X, conn, deg, 1)
     x, d = P.boundary_points()
     P.constrain(d, np.zeros(len(d)), np.zeros(len(d)))
     P.number()
-    P.set_laplace(kappa, 2)
-    # initial values: a smooth bump on the free DOFs (the constrained ones are 0)
+    newton = 1
+    method = A.SOLVE_CG_FP64
+    if kernel == "laplace":
+        S.set_laplace(kappa, 2)
+        P.set_laplace(kappa, 2)
+    else:
+        S.set_heat_static("fenics", kappa, 2)
+        P.set_heat_static("fenics", kappa, 2)
+        newton, method = 2, A.SOLVE_BICGSTAB
+    # initial values: random on the free DOFs (the constrained ones are 0)
     u0 = rng.uniform(0.0, 1.0, S.ndofobj) * (S.dof_index() >= 0)
     S.set_values(u0)
-    gpu = W.unsteady_heat(S, rho, steps, dt, order=order)
+    gpu = W.unsteady_heat(S, rho, steps, dt, order=order, scheme=scheme, newton=newton, method=method)
     P.set_values(u0)
     hist = [u0.copy()] + [np.zeros_like(u0)] * (order - 1)
     for k in range(steps):
-        mw, w = W.inertia_weights(order, k, dt)
-        P.set_inertia(rho, mw, w, hist[: len(w) - 1])
-        rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
-        xs = spsolve(sp.csc_matrix(sp.csr_matrix((v, ci, rp))), b)
-        P.distribute(xs, add=True)
+        mw, w, fw = W.time_weights(scheme, order, k, dt)
+        P.set_inertia(rho, mw, w, hist[: max(len(w) - 1, len(fw))], fw)
+        for _ in range(newton):
+            rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+            xs = spsolve(sp.csc_matrix(sp.csr_matrix((v, ci, rp))), b)
+            P.distribute(xs, add=True)
         cur = P.values()
         hist = [cur.copy()] + hist[:-1]
         err = np.linalg.norm(gpu[k] - cur) / np.linalg.norm(cur)
