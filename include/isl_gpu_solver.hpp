@@ -16,7 +16,8 @@
 //   post::errorComputation<ORDER>            base/post/ErrorNorm.hpp:84-123        errorComputation(order, qdeg, f)
 //   heat::Static<Material>                   heat/Static.hpp:98-225                heatStatic(material, param, qdeg)
 //   time::computeInertiaTerms<FTB,MSM>       base/time/ReactionTerms.hpp:62-79     inertia(density, lhs_w, weights)
-//   dof::pushHistory                         (DegreeOfFreedom)                     history(n), pushHistory()
+//   time::computeResidualForceHistory        base/time/ResidualForceHistory.hpp    forceHistory(weights)
+//   dof::pushHistory                         base/dof/DegreeOfFreedom.hpp:185-190  history(n), pushHistory()
 //   number getValue(i)                       :293-296                         getValue(i)
 //   double norm(), norm(first, last)         :128-138                         norm(), norm(first, last)
 //   insertToLHS / insertToRHS                :81-124                          not offered: assembly runs on the device
@@ -124,6 +125,11 @@ public:
     void inertia(const std::vector<double>& density, double lhs_weight, const std::vector<double>& weights) {
         check(ctx_, isl_set_inertia(ctx_, density.data(), lhs_weight, (int)weights.size(), weights.data()),
               "isl_set_inertia");
+    }
+    // computeResidualForceHistory: weights[s-1] of the residual force at x^(s)
+    void forceHistory(const std::vector<double>& weights) {
+        check(ctx_, isl_set_force_history(ctx_, (int)weights.size(), weights.empty() ? nullptr : weights.data()),
+              "isl_set_force_history");
     }
     void bodyForceNodal(const std::vector<double>& f) {
         check(ctx_, isl_set_body_force_nodal(ctx_, f.data()), "isl_set_body_force_nodal");

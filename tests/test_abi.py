@@ -46,3 +46,27 @@ def test_host_only_context_rejects_device_work():
         raise AssertionError("expected failure")
     except A.IslError as e:
         assert e.code == A.ISL_ERR_ARG
+
+
+def test_host_only_argument_checks():
+    """argument checks of the newer entry points on a host-only context: the
+    time-integration and post-processing calls that need a device refuse with
+    ISL_ERR_ARG, and option values out of range are refused"""
+    import pytest
+    from insilico_gb300.system import System
+    S = System(device=-1)
+    X = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=float)
+    S.upload_mesh(A.QUAD, X, np.array([[0, 1, 2, 3]]))
+    S.create_field(1, 1)
+    for call in (lambda: S.set_history(1), lambda: S.quadrature_points(2),
+                 lambda: S.error_norm(0, 2, np.zeros(4)), lambda: S.set_force_history([1.0]),
+                 lambda: S.set_option(A.OPT_BICGSTAB_KIND, 104), lambda: S.set_option(A.OPT_SPMV32_KIND, 3),
+                 lambda: S.set_option(A.OPT_PERSISTENT, 7)):
+        with pytest.raises(A.IslError) as ei:
+            call()
+        assert ei.value.code == A.ISL_ERR_ARG
+    # host-only values round trip (the I/O path reads them)
+    S.set_values(np.arange(4.0))
+    assert np.array_equal(S.values(), np.arange(4.0))
+    S.set_option(A.OPT_HOST_SETUP, 1)
+    assert S.get_option(A.OPT_HOST_SETUP) == 1
