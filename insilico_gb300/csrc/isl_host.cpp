@@ -343,6 +343,7 @@ void group_faces(const std::vector<Key>& keys, std::vector<int64_t>& first, std:
 extern "C" {
 
 int isl_ctx_create(isl_ctx** out, int device, void* stream) {
+    ISL_TRY
     if (!out) return ISL_ERR_ARG;
     *out = nullptr;
     isl_ctx* c = new isl_ctx();
@@ -366,9 +367,11 @@ int isl_ctx_create(isl_ctx** out, int device, void* stream) {
     cudaMemsetAsync(c->dflags.p, 0, 4 * sizeof(int), c->stream);
     *out = c;
     return ISL_OK;
+    ISL_CATCH(nullptr)
 }
 
 int isl_ctx_destroy(isl_ctx* c) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (c->device < 0) { delete c; return ISL_OK; }
     cudaSetDevice(c->device);
@@ -381,6 +384,7 @@ int isl_ctx_destroy(isl_ctx* c) {
     cudaStreamSynchronize(cudaStreamPerThread);
     if (own) cudaStreamDestroy(own);
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 const char* isl_last_error(const isl_ctx* c) { return c ? c->err.c_str() : "null context"; }
@@ -389,14 +393,18 @@ static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, con
                             const int64_t* conn, int64_t n_inst, const int64_t* node_off, const int64_t* elem_off);
 
 int isl_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn) {
+    ISL_TRY
     const int64_t no[2] = {0, n_nodes}, eo[2] = {0, n_elem};
     return mesh_upload_impl(c, shape, dim, n_nodes, X, n_elem, conn, 1, no, eo);
+    ISL_CATCH(c)
 }
 
 int isl_batch_mesh_upload(isl_ctx* c, int shape, int dim, int64_t n_inst, const int64_t* node_off, const double* X,
                           const int64_t* elem_off, const int64_t* conn) {
+    ISL_TRY
     if (!c || n_inst <= 0 || !node_off || !elem_off) return ISL_ERR_ARG;
     return mesh_upload_impl(c, shape, dim, node_off[n_inst], X, elem_off[n_inst], conn, n_inst, node_off, elem_off);
+    ISL_CATCH(c)
 }
 
 static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, const double* X, int64_t n_elem,
@@ -440,6 +448,7 @@ static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, con
 // cells are numbered by first visit in element order, shared n-faces copying
 // the ids of their first occurrence (base/dof/generateDoFIndicesFromFaces.hpp:169-298).
 int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, int* n_fun) {
+    ISL_TRY
     if (!c || c->nelem == 0) return ISL_ERR_ARG;
     if (fe_degree < 1 || fe_degree > 3 || ncomp < 1 || ncomp > 3) ISL_FAIL(c, ISL_ERR_ARG, "unsupported field");
     if (c->shape == ISL_TET && fe_degree > 2) ISL_FAIL(c, ISL_ERR_ARG, "tet degree > 2 unsupported");
@@ -556,12 +565,15 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     if (n_dofobj) *n_dofobj = c->ndofobj;
     if (n_fun) *n_fun = nf;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_field_elem_dofobj(isl_ctx* c, int64_t* out) {
+    ISL_TRY
     if (!c || !c->fedeg || !out) return ISL_ERR_ARG;
     std::copy(c->hedof.begin(), c->hedof.end(), out);
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 static int boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) {
@@ -605,6 +617,7 @@ static int boundary_list(isl_ctx* c, std::vector<std::pair<int64_t, int>>& out) 
 }
 
 int isl_boundary_faces(isl_ctx* c, int64_t* n, int64_t* elem, int* face) {
+    ISL_TRY
     if (!c || !c->nelem || !n) return ISL_ERR_ARG;
     std::vector<std::pair<int64_t, int>> bf;
     const int rc = boundary_list(c, bf);
@@ -613,6 +626,7 @@ int isl_boundary_faces(isl_ctx* c, int64_t* n, int64_t* elem, int* face) {
     if (elem && face)
         for (size_t i = 0; i < bf.size(); ++i) { elem[i] = bf[i].first; face[i] = bf[i].second; }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 // local FE positions on a boundary face: its vertices, interior DOFs of the
@@ -640,6 +654,7 @@ static std::vector<int> face_local_dofs(isl_ctx* c, int face) {
 }
 
 int isl_boundary_points(isl_ctx* c, int64_t* n, double* x, int64_t* dofobj) {
+    ISL_TRY
     if (!c || !c->fedeg || !n) return ISL_ERR_ARG;
     std::vector<std::pair<int64_t, int>> bf;
     const int brc = boundary_list(c, bf);
@@ -690,9 +705,11 @@ int isl_boundary_points(isl_ctx* c, int64_t* n, double* x, int64_t* dofobj) {
     }
     *n = cnt;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_constrain(isl_ctx* c, int64_t n, const int64_t* dofobj, const int* comp, const double* value) {
+    ISL_TRY
     if (!c || !c->fedeg || (n > 0 && (!dofobj || !comp || !value))) return ISL_ERR_ARG;
     for (int64_t i = 0; i < n; ++i) {
         if (dofobj[i] < 0 || dofobj[i] >= c->ndofobj || comp[i] < 0 || comp[i] >= c->ncomp)
@@ -707,9 +724,11 @@ int isl_constrain(isl_ctx* c, int64_t n, const int64_t* dofobj, const int* comp,
         ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_scale_constraints(isl_ctx* c, double factor) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     for (size_t k = 0; k < c->status.size(); ++k) if (c->status[k]) c->cval[k] *= factor;
     if (c->dcval.p) {
@@ -717,10 +736,12 @@ int isl_scale_constraints(isl_ctx* c, double factor) {
         ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 // consecutive numbering of ACTIVE components in DOF-object order
 int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     int64_t k = 0;
     c->inst_eq_off.assign(c->ninst + 1, 0);
@@ -750,15 +771,19 @@ int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
     if (n_active) *n_active = k;
     c->nnz = 0;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_dof_index(isl_ctx* c, int64_t* out) {
+    ISL_TRY
     if (!c || !c->numbered || !out) return ISL_ERR_ARG;
     for (size_t i = 0; i < c->heq.size(); ++i) out[i] = c->heq[i];
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
+    ISL_TRY
     if (!c || !c->numbered) return ISL_ERR_ARG;
     if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: the pattern is built on the device");
     cudaSetDevice(c->device);
@@ -790,9 +815,11 @@ int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
     c->pattern_ready = true;
     if (nnz) *nnz = c->nnz;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_laplace(isl_ctx* c, const double* kappa, int quad_degree) {
+    ISL_TRY
     if (!c || !c->fedeg || !kappa) return ISL_ERR_ARG;
     if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "Laplace needs a scalar field");
     c->kernel = ISL_KERNEL_LAPLACE;
@@ -801,9 +828,11 @@ int isl_set_laplace(isl_ctx* c, const double* kappa, int quad_degree) {
     ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, kappa, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_heat_static(isl_ctx* c, int material, const double* param, int quad_degree) {
+    ISL_TRY
     if (!c || !c->fedeg || !param) return ISL_ERR_ARG;
     if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "heat::Static needs a scalar field");
     if (material != ISL_THERMAL_CONSTANT && material != ISL_THERMAL_FENICS) ISL_FAIL(c, ISL_ERR_ARG, "thermal material");
@@ -814,9 +843,11 @@ int isl_set_heat_static(isl_ctx* c, int material, const double* param, int quad_
     ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, param, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_history(isl_ctx* c, int nhist) {
+    ISL_TRY
     if (!c || !c->fedeg || nhist < 0 || nhist > 4) ISL_FAIL(c, ISL_ERR_ARG, "isl_set_history: 0..4 past steps");
     if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context");
     cudaSetDevice(c->device);
@@ -827,9 +858,11 @@ int isl_set_history(isl_ctx* c, int nhist) {
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dhist.p, 0, n * nhist * 8, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_push_history(isl_ctx* c) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (c->nhist == 0) ISL_FAIL(c, ISL_ERR_ARG, "isl_push_history: no history (isl_set_history)");
     cudaSetDevice(c->device);
@@ -837,9 +870,11 @@ int isl_push_history(isl_ctx* c) {
     if (rc != ISL_OK) return rc;
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_inertia(isl_ctx* c, const double* density, double lhs_weight, int nweights, const double* weights) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (!density) { c->inertia = false; return ISL_OK; }
     if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar fields only");
@@ -854,9 +889,11 @@ int isl_set_inertia(isl_ctx* c, const double* density, double lhs_weight, int nw
     c->nhist_w = nweights;
     for (int k = 0; k < 5; ++k) c->hist_w[k] = k < nweights ? weights[k] : 0.0;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_force_history(isl_ctx* c, int nweights, const double* weights) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (nweights < 0 || nweights > 4 || nweights > c->nhist || (nweights > 0 && !weights))
         ISL_FAIL(c, ISL_ERR_ARG, "residual force history: at most 4 weights and at most the stored history");
@@ -864,9 +901,11 @@ int isl_set_force_history(isl_ctx* c, int nweights, const double* weights) {
     c->nforce_w = nweights;
     for (int k = 0; k < 4; ++k) c->force_w[k] = k < nweights ? weights[k] : 0.0;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_hyperelastic(isl_ctx* c, int material, const double* lambda, const double* mu, int quad_degree) {
+    ISL_TRY
     if (!c || !c->fedeg || !lambda || !mu) return ISL_ERR_ARG;
     if (c->ncomp != c->dim) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic needs ncomp == dim");
     if (material != ISL_MAT_STVENANT && material != ISL_MAT_NEOHOOKE) ISL_FAIL(c, ISL_ERR_ARG, "material");
@@ -878,18 +917,22 @@ int isl_set_hyperelastic(isl_ctx* c, int material, const double* lambda, const d
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, lambda, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p + c->nelem, mu, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_body_force_nodal(isl_ctx* c, const double* f) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (!f) { c->has_body = false; return ISL_OK; }
     ISL_CHECK_CUDA(c, c->dfnodal.alloc(c->nnodes * c->ncomp));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dfnodal.p, f, c->nnodes * c->ncomp * 8, cudaMemcpyHostToDevice, c->stream));
     c->has_body = true;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_neumann(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, const double* traction, int squad_degree) {
+    ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     c->n_neu_elem = 0;
     if (n <= 0) return ISL_OK;
@@ -922,9 +965,11 @@ int isl_set_neumann(isl_ctx* c, int64_t n, const int64_t* elem, const int* face,
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_trac.p, tr.data(), tr.size() * 8, cudaMemcpyHostToDevice, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_values(isl_ctx* c, const double* u) {
+    ISL_TRY
     if (!c || !c->fedeg || !u) return ISL_ERR_ARG;
     const size_t n = (size_t)c->ndofobj * c->ncomp;
     c->u_nonzero = false;
@@ -936,9 +981,11 @@ int isl_set_values(isl_ctx* c, const double* u) {
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->du.p, u, n * 8, cudaMemcpyHostToDevice, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_get_values(isl_ctx* c, double* u) {
+    ISL_TRY
     if (!c || !c->fedeg || !u) return ISL_ERR_ARG;
     const size_t n = (size_t)c->ndofobj * c->ncomp;
     if (c->device < 0) {
@@ -949,9 +996,11 @@ int isl_get_values(isl_ctx* c, double* u) {
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(u, c->du.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (!c->pattern_ready || c->kernel < 0) ISL_FAIL(c, ISL_ERR_ARG, "assemble: pattern or kernel not set");
     if (precision < ISL_PREC_FP64 || precision > ISL_PREC_MIXED) ISL_FAIL(c, ISL_ERR_ARG, "precision");
@@ -967,9 +1016,11 @@ int isl_assemble(isl_ctx* c, int precision, int incremental, int with_residual) 
         if (st != ISL_OK) return st;
     }
     return isl::assemble_device(c, precision, incremental, with_residual);
+    ISL_CATCH(c)
 }
 
 int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* rel_res) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (!c->pattern_ready || !(c->have64 || c->have32)) ISL_FAIL(c, ISL_ERR_ARG, "solve: nothing assembled");
     if (c->neq == 0) {
@@ -989,9 +1040,11 @@ int isl_solve(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* ite
     if (!(tol >= 0.0)) ISL_FAIL(c, ISL_ERR_ARG, "tol");
     cudaSetDevice(c->device);
     return isl::solve_device(c, method, tol, max_iter, iters, rel_res);
+    ISL_CATCH(c)
 }
 
 int isl_get_solution(isl_ctx* c, double* x) {
+    ISL_TRY
     if (!c || !c->pattern_ready) return ISL_ERR_ARG;
     if (c->neq == 0) return ISL_OK;
     if (!x) return ISL_ERR_ARG;
@@ -999,18 +1052,22 @@ int isl_get_solution(isl_ctx* c, double* x) {
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(x, src, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_get_rhs(isl_ctx* c, double* b) {
+    ISL_TRY
     if (!c || !c->pattern_ready) return ISL_ERR_ARG;
     if (c->neq == 0) return ISL_OK;
     if (!b) return ISL_ERR_ARG;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(b, c->drhs.p, c->neq * 8, cudaMemcpyDeviceToHost, c->stream));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_norm(isl_ctx* c, double* out) {
+    ISL_TRY
     if (!c || !c->pattern_ready || !out) return ISL_ERR_ARG;
     if (c->neq == 0) { *out = 0.0; return ISL_OK; }
     std::vector<double> b(c->neq);
@@ -1020,32 +1077,40 @@ int isl_norm(isl_ctx* c, double* out) {
     for (double v : b) s += v * v;
     *out = std::sqrt(s) / (double)c->neq;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_distribute(isl_ctx* c, int add) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (!c->solved) ISL_FAIL(c, ISL_ERR_ARG, "distribute: no solution");
     cudaSetDevice(c->device);
     int st = isl::distribute_device(c, add);
     if (st == ISL_OK) c->u_nonzero = true;
     return st;
+    ISL_CATCH(c)
 }
 
 int isl_quadrature_points(isl_ctx* c, int quad_degree, int64_t* n_points, double* x) {
+    ISL_TRY
     if (!c || !c->fedeg || !n_points) return ISL_ERR_ARG;
     if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: post-processing runs on the device");
     cudaSetDevice(c->device);
     return isl::quadrature_points_device(c, quad_degree, n_points, x);
+    ISL_CATCH(c)
 }
 
 int isl_error_norm(isl_ctx* c, int order, int quad_degree, const double* ref, double* error) {
+    ISL_TRY
     if (!c || !c->fedeg || !ref || !error || (order != 0 && order != 1)) return ISL_ERR_ARG;
     if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: post-processing runs on the device");
     cudaSetDevice(c->device);
     return isl::error_norm_device(c, order, quad_degree, ref, error);
+    ISL_CATCH(c)
 }
 
 int isl_get_csr(isl_ctx* c, int64_t* rowptr, int64_t* colind, double* values) {
+    ISL_TRY
     if (!c || !c->pattern_ready) return ISL_ERR_ARG;
     if (c->neq == 0) {
         if (rowptr) rowptr[0] = 0;
@@ -1073,57 +1138,73 @@ int isl_get_csr(isl_ctx* c, int64_t* rowptr, int64_t* colind, double* values) {
         }
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_sync(isl_ctx* c) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_timing(isl_ctx* c, int on) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     c->timing = on != 0;
     for (int i = 0; i < ISL_NTIMERS; ++i) { c->tms[i] = 0; c->tcount[i] = 0; }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_timings(isl_ctx* c, double* ms, int64_t* counts) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     for (int i = 0; i < ISL_NTIMERS; ++i) {
         if (ms) ms[i] = c->tms[i];
         if (counts) counts[i] = c->tcount[i];
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
+    ISL_TRY
     if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep <= 0) return ISL_ERR_ARG;
     return isl::time_spmv(c, precision, nrep, ms);
+    ISL_CATCH(c)
 }
 
 int isl_mark(isl_ctx* c, int slot) {
+    ISL_TRY
     if (!c || c->device < 0 || slot < 0 || slot >= 8) return ISL_ERR_ARG;
     ISL_CHECK_CUDA(c, cudaEventRecord(c->mark[slot], c->stream));
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_elapsed(isl_ctx* c, int a, int b, double* ms) {
+    ISL_TRY
     if (!c || c->device < 0 || a < 0 || a >= 8 || b < 0 || b >= 8 || !ms) return ISL_ERR_ARG;
     ISL_CHECK_CUDA(c, cudaEventSynchronize(c->mark[b]));
     float t = 0.f;
     ISL_CHECK_CUDA(c, cudaEventElapsedTime(&t, c->mark[a], c->mark[b]));
     *ms = t;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_launch_count(isl_ctx* c, int64_t* n) {
+    ISL_TRY
     if (!c || !n) return ISL_ERR_ARG;
     *n = c->launches;
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_set_option(isl_ctx* c, int key, int64_t value) {
+    ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { c->use_block = value != 0; return ISL_OK; }
     if (key == ISL_OPT_BARRIER_TEST) { c->barrier_test = value != 0; return ISL_OK; }
@@ -1152,9 +1233,11 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
         return ISL_OK;
     }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown or read-only option");
+    ISL_CATCH(c)
 }
 
 int isl_get_option(isl_ctx* c, int key, int64_t* value) {
+    ISL_TRY
     if (!c || !value) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) { *value = c->use_persist; return ISL_OK; }
@@ -1166,9 +1249,11 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_BICGSTAB_KIND) { *value = c->bicg_lpr; return ISL_OK; }
     if (key == ISL_OPT_SCALAR_SLOTS) { *value = c->ss_nslot; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
+    ISL_CATCH(c)
 }
 
 int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {
+    ISL_TRY
     if (!free_bytes || !total_bytes) return ISL_ERR_ARG;
     int cur = 0;
     cudaGetDevice(&cur);
@@ -1180,9 +1265,11 @@ int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {
     *free_bytes = (int64_t)f;
     *total_bytes = (int64_t)t;
     return ISL_OK;
+    ISL_CATCH(nullptr)
 }
 
 int isl_batch_info(isl_ctx* c, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off) {
+    ISL_TRY
     if (!c || !n_inst) return ISL_ERR_ARG;
     *n_inst = c->ninst;
     if (eq_off) {
@@ -1194,21 +1281,26 @@ int isl_batch_info(isl_ctx* c, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj
         std::copy(c->inst_dof_off.begin(), c->inst_dof_off.end(), dofobj_off);
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_batch_solve_stats(isl_ctx* c, int64_t* iters, double* rel_res) {
+    ISL_TRY
     if (!c || c->inst_iters.empty()) return ISL_ERR_ARG;
     for (int64_t k = 0; k < c->ninst; ++k) {
         if (iters) iters[k] = c->inst_iters[k];
         if (rel_res) rel_res[k] = c->inst_relres[k];
     }
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_time_kernels(isl_ctx* c, int nrep, double* ms) {
+    ISL_TRY
     if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep <= 0) return ISL_ERR_ARG;
     cudaSetDevice(c->device);
     return isl::time_kernels(c, nrep, ms);
+    ISL_CATCH(c)
 }
 
 }  // extern "C"

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -276,6 +278,41 @@ struct isl_ctx {
         (ctx)->err = (msg);      \
         return (code);           \
     } while (0)
+
+namespace isl {
+// Status for a C++ exception caught at the C ABI: the message goes to the
+// context when there is one (the assignment itself may fail under memory
+// pressure, which leaves the old message).
+inline int fail_exception(isl_ctx* c, int code, const char* what) noexcept {
+    if (c) {
+        try {
+            c->err = what;
+        } catch (...) {
+        }
+    }
+    return code;
+}
+}  // namespace isl
+
+// Every extern "C" entry point with host allocations runs its body inside
+// ISL_TRY .. ISL_CATCH(ctx): no exception crosses the C ABI.  Allocation
+// failures (std::bad_alloc, or a container size above max_size) return
+// ISL_ERR_NOMEM, anything else ISL_ERR_ARG.
+#define ISL_TRY try {
+#define ISL_CATCH(ctx)                                                                          \
+    }                                                                                           \
+    catch (const std::bad_alloc&) {                                                             \
+        return isl::fail_exception((ctx), ISL_ERR_NOMEM, "host allocation failed");             \
+    }                                                                                           \
+    catch (const std::length_error&) {                                                          \
+        return isl::fail_exception((ctx), ISL_ERR_NOMEM, "host allocation larger than max_size"); \
+    }                                                                                           \
+    catch (const std::exception& _x) {                                                          \
+        return isl::fail_exception((ctx), ISL_ERR_ARG, _x.what());                              \
+    }                                                                                           \
+    catch (...) {                                                                               \
+        return isl::fail_exception((ctx), ISL_ERR_ARG, "unknown exception");                    \
+    }
 
 namespace isl {
 // device-side entry points implemented in the .cu files

@@ -75,6 +75,9 @@ bool parse_int(const char*& p, const char* end, int64_t& v) {
 
 // the starts of the next n lines from position pos (a line = up to '\n')
 bool line_starts(const std::string& s, size_t pos, int64_t n, std::vector<size_t>& starts, size_t& after) {
+    // every line holds at least one byte: a count above the bytes left is
+    // rejected before anything is sized by it
+    if (n < 0 || pos > s.size() || (uint64_t)n > (uint64_t)(s.size() - pos)) return false;
     starts.resize((size_t)n + 1);
     size_t p = pos;
     for (int64_t i = 0; i < n; ++i) {
@@ -179,6 +182,7 @@ void put_node(std::string& out, const double* x, int dim) {
 extern "C" {
 
 int isl_mesh_read_smf(isl_ctx* c, const char* path, int shape) {
+    ISL_TRY
     if (!c || !path) return ISL_ERR_ARG;
     if (!(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) ISL_FAIL(c, ISL_ERR_ARG, "unsupported shape");
     std::string s;
@@ -233,8 +237,8 @@ int isl_mesh_read_smf(isl_ctx* c, const char* path, int shape) {
         pos = next_line((size_t)(p - s.data()));
     }
     const int dim = shape_dim(shape), nv = shape_nodes(shape);
-    std::vector<double> X((size_t)nn * dim);
-    std::vector<int64_t> conn((size_t)ne * nv);
+    std::vector<double> X;
+    std::vector<int64_t> conn;
     std::vector<size_t> starts;
     size_t after = 0;
     // nodes: the first dim numbers of each line (raw/ascii.hpp:108-119)
@@ -248,6 +252,7 @@ int isl_mesh_read_smf(isl_ctx* c, const char* path, int shape) {
             p0 = 0;
         }
         if (!line_starts(*src, p0, nn, starts, after)) ISL_FAIL(c, ISL_ERR_ARG, "Smf: fewer node lines than announced");
+        X.resize((size_t)nn * dim);
         if (!parse_lines(*src, starts, nn, dim, X.data(), parse_double)) ISL_FAIL(c, ISL_ERR_ARG, "Smf: bad coordinate");
         if (ext_nodes.empty()) pos = after;
     }
@@ -262,21 +267,26 @@ int isl_mesh_read_smf(isl_ctx* c, const char* path, int shape) {
             p0 = 0;
         }
         if (!line_starts(*src, p0, ne, starts, after)) ISL_FAIL(c, ISL_ERR_ARG, "Smf: fewer element lines than announced");
+        conn.resize((size_t)ne * nv);
         if (!parse_lines(*src, starts, ne, nv, conn.data(), parse_int)) ISL_FAIL(c, ISL_ERR_ARG, "Smf: bad connectivity");
     }
     return isl_mesh_upload(c, shape, dim, nn, X.data(), ne, conn.data());
+    ISL_CATCH(c)
 }
 
 int isl_mesh_get(isl_ctx* c, int64_t* n_nodes, int64_t* n_elem, double* X, int64_t* conn) {
+    ISL_TRY
     if (!c || !c->nelem) return ISL_ERR_ARG;
     if (n_nodes) *n_nodes = c->nnodes;
     if (n_elem) *n_elem = c->nelem;
     if (X) std::copy(c->hX.begin(), c->hX.end(), X);
     if (conn) std::copy(c->hconn.begin(), c->hconn.end(), conn);
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_mesh_write_smf(isl_ctx* c, const char* path) {
+    ISL_TRY
     if (!c || !path || !c->nelem) return ISL_ERR_ARG;
     FILE* f = std::fopen(path, "wb");
     if (!f) ISL_FAIL(c, ISL_ERR_ARG, std::string("cannot write ") + path);
@@ -292,10 +302,12 @@ int isl_mesh_write_smf(isl_ctx* c, const char* path) {
     ok = (std::fclose(f) == 0) && ok;
     if (!ok) ISL_FAIL(c, ISL_ERR_ARG, std::string("write failed: ") + path);
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 int isl_write_vtk(isl_ctx* c, const char* path, const char* point_name, const char* cell_name, int cell_rows,
                   int cell_cols, const double* cell_values) {
+    ISL_TRY
     if (!c || !path || !c->nelem) return ISL_ERR_ARG;
     if (point_name && !c->fedeg) ISL_FAIL(c, ISL_ERR_ARG, "vtk: point data needs a field");
     if (cell_name && (!cell_values || cell_rows < 0 || cell_cols < 0 || cell_rows > 3 || cell_cols > 3 ||
@@ -378,6 +390,7 @@ int isl_write_vtk(isl_ctx* c, const char* path, const char* point_name, const ch
     ok = (std::fclose(f) == 0) && ok;
     if (!ok) ISL_FAIL(c, ISL_ERR_ARG, std::string("write failed: ") + path);
     return ISL_OK;
+    ISL_CATCH(c)
 }
 
 }  // extern "C"

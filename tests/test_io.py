@@ -87,6 +87,21 @@ def test_smf_reader_rejects_bad_headers(tmp_path, header):
         System(device=-1).read_smf(p, A.QUAD)
 
 
+@pytest.mark.parametrize("counts", ["100000000000000000 1", "4 100000000000000000", "4 1000000000000"])
+def test_smf_reader_rejects_counts_beyond_the_file(tmp_path, counts):
+    """node / element counts larger than the file can hold are an error
+    status, not an allocation sized by the header"""
+    p = tmp_path / "huge.smf"
+    p.write_text("! elementShape quadrilateral\n! elementNumPoints 4\n" + counts +
+                 "\n0 0 0\n1 0 0\n1 1 0\n0 1 0\n0 1 2 3\n")
+    S = System(device=-1)
+    with pytest.raises(A.IslError, match="fewer"):
+        S.read_smf(p, A.QUAD)
+    # the context stays usable
+    X, conn = O.unitcube("quad", 2, 2)
+    S.upload_mesh(A.QUAD, X, conn)
+
+
 @pytest.mark.parametrize("tag,disp,trac", [("D", True, 1000.0), ("N", False, 300.0)])
 def test_vtk_matches_reference_golden(pins, tmp_path, tag, disp, trac):
     """LegacyWriter output of reference/06-elastic/compressible.cpp's final
