@@ -148,8 +148,9 @@ int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_el
  * x^(s), x^(0) the current values, x^(s) the values s steps back.  For a
  * MultiStep method at time step k: lhs_weight = systemMassWeight(k) / dt and
  * weights[s] = -reactionWeights(k)[s] / dt (incremental; weights[0] = 0
- * otherwise).  Scalar kernels (Laplace, heat::Static); density NULL turns the
- * terms off. */
+ * otherwise).  Laplace, heat::Static and HyperElastic (trilinear
+ * hexahedra), where the mass acts on each displacement component
+ * (Mass.hpp:84-86); density NULL turns the terms off. */
 int isl_set_history(isl_ctx* ctx, int nhist);
 int isl_push_history(isl_ctx* ctx);
 int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double lhs_weight, int nweights,
@@ -160,7 +161,8 @@ int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double l
  * -sum_s weights[s-1] F(x^(s)) to the right-hand side, F the kernel's internal
  * force (residualForceHistory<s>) at the values s steps back, s = 1..nweights
  * (<= the stored history, <= 4).  For a MultiStep method at step k: weights =
- * forceWeights(k).  Scalar kernels; nweights 0 turns it off. */
+ * forceWeights(k).  Laplace, heat::Static and HyperElastic (trilinear
+ * hexahedra); nweights 0 turns it off. */
 int isl_set_force_history(isl_ctx* ctx, int nweights, const double* weights);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */

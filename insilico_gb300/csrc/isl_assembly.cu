@@ -438,6 +438,14 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
 //            NeoHookeanCompressible mat/hypel/NeoHookeanCompressible.hpp:77-172.
 // At u == 0 (F = I, S = 0) both reduce to isotropic linear elasticity and the
 // kernel uses  K_MN = c (lam g_M g_N^T + mu g_N g_M^T + mu (g_M.g_N) I).
+// TI compiles in the time-integration terms of a vector field (the plain
+// assembly runs without them):
+//   K[Md+i, Nd+i] += mass_w rho phi_M phi_N detJ w    base/kernel/Mass.hpp:72-101
+//   F[Md+i]       += sum_N (rho phi_M phi_N detJ w) h[Nd+i]   ReactionTerms.hpp
+//   F[Md+i]       -= sum_s fw_s (F_s S_s)_iJ phi_M,J detJ w at the past state s
+//                                           base/time/ResidualForceHistory.hpp
+// The host runs the finite-strain path (general) whenever past-state forces
+// are asked for, so that their contributions have the shared staging.
 __device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
     const int m = (i + 1) * (j + 1);
     return m == 1 ? 0 : m == 4 ? 1 : m == 9 ? 2 : m == 2 ? 3 : m == 3 ? 4 : 5;
@@ -479,7 +487,7 @@ __device__ inline void material_eval(int mat, double lam, double mu, const doubl
                         lam * Ci[A][B] * Ci[Cc][Dd] + f2 * (Ci[A][Cc] * Ci[B][Dd] + Ci[A][Dd] * Ci[B][Cc]);
 }
 
-template <typename R, int EPB>
+template <typename R, int EPB, bool TI>
 __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const Tab<3, 8, 8, 8> T) {
     constexpr int NLOC = 24;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -592,8 +600,32 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
                 for (int i = 0; i < 3; ++i) {
                     const double v = (P[i][0] * g[N][0] + P[i][1] * g[N][1] + P[i][2] * g[N][2]) * c;
                     nan |= !(v == v);
-                    sfq[((q * 8 + N) * 3 + i) * EPB + el] = v;
+                    sfq[((q * 8 + N) * 3 + i) * EPB + el] = (TI && !A.with_residual) ? 0.0 : v;
                 }
+            if (TI) {
+                // residual forces at the past states, weighted (x -1 when summed)
+                for (int sidx = 0; sidx < A.nfw; ++sidx) {
+                    double Fh[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                    for (int f = 0; f < 8; ++f) {
+                        const size_t obj = (size_t)A.edof[f * E + ec];
+                        for (int i = 0; i < 3; ++i) {
+                            const double uf = A.hist[(size_t)sidx * A.hstride + obj * 3 + i];
+                            for (int J = 0; J < 3; ++J) Fh[i][J] += g[f][J] * uf;
+                        }
+                    }
+                    double Sh[3][3], Ch[6][6];
+                    material_eval(A.material, lam, mu, Fh, Sh, Ch);
+                    double Ph[3][3];
+                    for (int i = 0; i < 3; ++i)
+                        for (int J = 0; J < 3; ++J) Ph[i][J] = Fh[i][0] * Sh[0][J] + Fh[i][1] * Sh[1][J] + Fh[i][2] * Sh[2][J];
+                    for (int N = 0; N < 8; ++N)
+                        for (int i = 0; i < 3; ++i) {
+                            const double v = A.fw[sidx] * (Ph[i][0] * g[N][0] + Ph[i][1] * g[N][1] + Ph[i][2] * g[N][2]) * c;
+                            nan |= !(v == v);
+                            sfq[((q * 8 + N) * 3 + i) * EPB + el] += v;
+                        }
+                }
+            }
             if (valid && nan) atomicOr(A.flags, 2);
             // effective elasticity A[iJ][kL] = d_ik S_JL + F_iA C_V(A,J)V(B,L) F_kB
             for (int i = 0; i < 3; ++i)
@@ -668,6 +700,17 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
                     for (int k = 0; k < 3; ++k) acc[N][i * 3 + k] += h[i][k][0] * gN[0] + h[i][k][1] * gN[1] + h[i][k][2] * gN[2];
             }
         }
+        if (TI && A.rho) {  // mass per component: the diagonal of each 3x3 block
+            const R mM = R(A.mass_w * A.rho[ec] * T.phi[q][M]) * c;
+#pragma unroll
+            for (int N = 0; N < 8; ++N) {
+                if (N < M) continue;
+                const R v = mM * R(T.phi[q][N]);
+                acc[N][0] += v;
+                acc[N][4] += v;
+                acc[N][8] += v;
+            }
+        }
     }
     if (!valid) return;
     R* SK = (R*)A.stageK;
@@ -684,10 +727,30 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
     }
     // forces of row node M: -(internal) + body
     double fe[3] = {0.0, 0.0, 0.0};
-    if (A.general && A.with_residual) {
+    if (A.general && (A.with_residual || (TI && A.nfw > 0))) {
         for (int q = 0; q < 8; ++q)
 #pragma unroll
             for (int i = 0; i < 3; ++i) fe[i] -= sfq[((q * 8 + M) * 3 + i) * EPB + el];
+    }
+    if (TI && A.rho) {
+        // F[Md+i] += sum_q rho phi_M(q) detJ w (sum_N phi_N(q) h[Nd+i]), in FP64
+        double hN[8][3];
+        for (int N = 0; N < 8; ++N) {
+            const size_t obj = (size_t)A.edof[N * E + e];
+            for (int i = 0; i < 3; ++i) hN[N][i] = A.hvec[obj * 3 + i];
+        }
+        double X[8][3], Ji[3][3];
+        for (int i = 0; i < 8; ++i)
+            for (int d = 0; d < 3; ++d) X[i][d] = sX[(i * 3 + d) * EPB + el];
+        const double rho = A.rho[e];
+        for (int q = 0; q < 8; ++q) {
+            const double m = rho * jac<8, 3>(X, T.dN[q], Ji) * T.w[q];
+            for (int i = 0; i < 3; ++i) {
+                double hq = 0.0;
+                for (int N = 0; N < 8; ++N) hq += T.phi[q][N] * hN[N][i];
+                fe[i] += m * T.phi[q][M] * hq;
+            }
+        }
     }
     if (A.fnodal) {
         for (int q = 0; q < 8; ++q) {
@@ -1189,7 +1252,8 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
     Tab<3, 8, 8, 8> T;
     fill_tab<ISL_HEX, 1, 8>(T, h);
     if (c->mesh_affine < 0) c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
-    if (!A.general && !A.fnodal && c->mesh_affine == 1) {
+    const bool ti = A.rho || A.nfw > 0;
+    if (!A.general && !A.fnodal && !ti && c->mesh_affine == 1) {
         // small strain on parallelepipeds: reference integrals times the constant Jacobian
         AffineHexTab AT;
         int pr = 0;
@@ -1218,12 +1282,14 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
         constexpr int EPB2 = 16;
         size_t smem2 = (size_t)8 * 3 * EPB2 * 8 * 2 + (size_t)8 * 8 * 3 * EPB2 * 8 + (size_t)8 * 8 * 3 * EPB2 * sizeof(R) +
                        (size_t)8 * EPB2 * sizeof(R) + (size_t)8 * 81 * EPB2 * sizeof(R);
-        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(k_hyper_hex8<R, EPB2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-        k_hyper_hex8<R, EPB2><<<nblk(c->nelem, EPB2), EPB2 * 8, smem2, c->stream>>>(A, T);
+        auto kern = ti ? k_hyper_hex8<R, EPB2, true> : k_hyper_hex8<R, EPB2, false>;
+        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        kern<<<nblk(c->nelem, EPB2), EPB2 * 8, smem2, c->stream>>>(A, T);
         epb_run = EPB2;
     } else {
-        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(k_hyper_hex8<R, EPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_hyper_hex8<R, EPB><<<nblk(c->nelem, EPB), EPB * 8, smem, c->stream>>>(A, T);
+        auto kern = ti ? k_hyper_hex8<R, EPB, true> : k_hyper_hex8<R, EPB, false>;
+        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<nblk(c->nelem, EPB), EPB * 8, smem, c->stream>>>(A, T);
     }
     (void)epb_run;
     ISL_CHECK_CUDA(c, cudaGetLastError());
@@ -1304,10 +1370,13 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.hstride = c->ndofobj * c->ncomp;
     A.nfw = c->nforce_w;
     for (int k = 0; k < 4; ++k) A.fw[k] = k < c->nforce_w ? c->force_w[k] : 0.0;
-    if (c->nforce_w > 0 && c->kernel == ISL_KERNEL_HYPERELASTIC)
-        ISL_FAIL(c, ISL_ERR_ARG, "residual force history: scalar kernels only");
+    // the weights may not reach past the stored history (isl_set_history can
+    // shrink it after the weights were set)
+    if (c->nforce_w > c->nhist || (c->inertia && c->nhist_w > c->nhist + 1))
+        ISL_FAIL(c, ISL_ERR_ARG, "time-integration weights reach past the stored history");
+    // past-state forces of HyperElastic go through the finite-strain path
+    if (c->nforce_w > 0 && c->kernel == ISL_KERNEL_HYPERELASTIC) A.general = 1;
     if (c->inertia) {
-        if (c->kernel == ISL_KERNEL_HYPERELASTIC) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar kernels only");
         // h = sum_s w_s x^(s): x^(0) the current values, x^(s) the s-th stored step
         const int64_t ndc = c->ndofobj * c->ncomp;
         ISL_CHECK_CUDA(c, c->dhvec.alloc(ndc));

@@ -877,7 +877,6 @@ int isl_set_inertia(isl_ctx* c, const double* density, double lhs_weight, int nw
     ISL_TRY
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (!density) { c->inertia = false; return ISL_OK; }
-    if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: scalar fields only");
     if (nweights < 0 || nweights > 5 || nweights > c->nhist + 1 || (nweights > 0 && !weights))
         ISL_FAIL(c, ISL_ERR_ARG, "inertia terms: at most 5 weights and at most the stored history + 1");
     cudaSetDevice(c->device);
@@ -897,7 +896,6 @@ int isl_set_force_history(isl_ctx* c, int nweights, const double* weights) {
     if (!c || !c->fedeg) return ISL_ERR_ARG;
     if (nweights < 0 || nweights > 4 || nweights > c->nhist || (nweights > 0 && !weights))
         ISL_FAIL(c, ISL_ERR_ARG, "residual force history: at most 4 weights and at most the stored history");
-    if (nweights > 0 && c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "residual force history: scalar fields only");
     c->nforce_w = nweights;
     for (int k = 0; k < 4; ++k) c->force_w[k] = k < nweights ? weights[k] : 0.0;
     return ISL_OK;

@@ -317,12 +317,14 @@ def time_weights(method: str, order: int, step: int, dt: float, incremental: boo
     return a[0] / b[0] / dt, w, [x / b[0] for x in b[1:]]
 
 
-def unsteady_heat(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None, scheme="bdf", newton=1):
+def unsteady(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None, scheme="bdf", newton=1):
     """Implicit multi-step time stepping (BDF or Adams-Moulton) of
-    rho du/dt - div(k grad u) = f on the context's problem (scalar kernel
-    already set, initial values in the DOFs): per step `newton` Newton
-    iterations from the current values (one suffices for Laplace, which is
-    linear in u), then pushHistory.  Returns the DOF values after every step."""
+    rho du/dt + F_int(u) = f on the context's problem (kernel already set,
+    initial values in the DOFs): rho du/dt - div(k grad u) = f for Laplace and
+    heat::Static, the same first-order inertia on each displacement component
+    for HyperElastic.  Per step `newton` Newton iterations from the current
+    values (one suffices for Laplace, which is linear in u), then
+    pushHistory.  Returns the DOF values after every step."""
     if method is None:
         method = A.SOLVE_CG_FP64
     out = []
@@ -339,3 +341,7 @@ def unsteady_heat(S, rho, steps, dt, order=2, lin_tol=1e-12, method=None, scheme
         S.push_history()
         out.append(S.values())
     return out
+
+
+# the heat equation's name for the driver
+unsteady_heat = unsteady

@@ -1152,8 +1152,10 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
             elementKernel(*P, Q, e, Ke.data(), nullptr);
             if (P->inertia) {
                 // ReactionTerms: (a0/(b0 dt)) M into the matrix (lifted with the
-                // stiffness), M h into the forces, h = sum_s w_s x^(s)
-                std::vector<double> Me((size_t)nloc * nloc), he(nloc);
+                // stiffness), M h into the forces, h = sum_s w_s x^(s).  For a
+                // vector field the mass acts per component (Mass.hpp:84-86:
+                // M[M*d+i][N*d+i]); Me is the nf x nf scalar mass.
+                std::vector<double> Me((size_t)nf * nf), he(nloc);
                 elementMass(*P, Q, e, Me.data());
                 const size_t ndc = (size_t)P->ndofobj * nd;
                 for (int a = 0; a < nloc; ++a) {
@@ -1164,10 +1166,12 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
                     he[a] = h;
                 }
                 for (int r = 0; r < nloc; ++r) {
+                    const int Mr = r / nd, ir = r % nd;
                     double fr = 0.0;
-                    for (int c2 = 0; c2 < nloc; ++c2) {
-                        Ke[r * nloc + c2] += P->massW * Me[r * nloc + c2];
-                        fr += Me[r * nloc + c2] * he[c2];
+                    for (int N = 0; N < nf; ++N) {
+                        const int c2 = N * nd + ir;
+                        Ke[r * nloc + c2] += P->massW * Me[Mr * nf + N];
+                        fr += Me[Mr * nf + N] * he[c2];
                     }
                     if (st[r] == 0) {
 #ifdef _OPENMP
