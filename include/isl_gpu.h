@@ -123,7 +123,9 @@ int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
  *   heat::Laplace (heat/Laplace.hpp:113-126, base/kernel/Laplace.hpp:100-151)
  *   solid::HyperElastic<StVenant|NeoHookeanCompressible>
  *     (solid/HyperElastic.hpp:110-257, mat/hypel/StVenant.hpp:77-114,
- *      mat/hypel/NeoHookeanCompressible.hpp:77-172)
+ *      mat/hypel/NeoHookeanCompressible.hpp:77-172); on the device for
+ *     trilinear hexahedra and for Q1 / Q2 quadrilaterals (plane strain,
+ *     solid/Deformation.hpp:25-46)
  * quad_degree: base::Quadrature<DEG,SHAPE> degree (base/Quadrature.hpp:113-143). */
 int isl_set_laplace(isl_ctx* ctx, const double* kappa /* [n_elem] */, int quad_degree);
 int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const double* mu, int quad_degree);
@@ -149,7 +151,7 @@ int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_el
  * MultiStep method at time step k: lhs_weight = systemMassWeight(k) / dt and
  * weights[s] = -reactionWeights(k)[s] / dt (incremental; weights[0] = 0
  * otherwise).  Laplace, heat::Static and HyperElastic (trilinear
- * hexahedra), where the mass acts on each displacement component
+ * hexahedra, Q1 / Q2 quadrilaterals), where the mass acts on each displacement component
  * (Mass.hpp:84-86); density NULL turns the terms off. */
 int isl_set_history(isl_ctx* ctx, int nhist);
 int isl_push_history(isl_ctx* ctx);
@@ -162,7 +164,7 @@ int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double l
  * force (residualForceHistory<s>) at the values s steps back, s = 1..nweights
  * (<= the stored history, <= 4).  For a MultiStep method at step k: weights =
  * forceWeights(k).  Laplace, heat::Static and HyperElastic (trilinear
- * hexahedra); nweights 0 turns it off. */
+ * hexahedra, Q1 / Q2 quadrilaterals); nweights 0 turns it off. */
 int isl_set_force_history(isl_ctx* ctx, int nweights, const double* weights);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
@@ -171,6 +173,15 @@ int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] *
  * n == 0 clears it. */
 int isl_set_neumann(isl_ctx* ctx, int64_t n, const int64_t* elem, const int* face, const double* traction,
                     int squad_degree);
+/* Traction given at the vertices of each boundary face ([n][nfv][ncomp], nfv
+ * = 2 on quadrilaterals, 4 on hexahedra, in the face's vertex order) and
+ * interpolated by the face geometry functions: the caller's tabulation of a
+ * traction function (base/asmb/NeumannForce.hpp:132-174 evaluates it at the
+ * surface quadrature points), exact for tractions linear along straight faces
+ * such as reference/06-elastic/PulledSheet.hpp:60-75.  Replaces the faces of
+ * isl_set_neumann; n == 0 clears them. */
+int isl_set_neumann_vertex(isl_ctx* ctx, int64_t n, const int64_t* elem, const int* face, const double* traction,
+                           int squad_degree);
 
 /* Current DOF values (DegreeOfFreedom values_[0]) [n_dofobj*ncomp]. */
 int isl_set_values(isl_ctx* ctx, const double* u);

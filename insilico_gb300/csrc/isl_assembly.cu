@@ -31,7 +31,7 @@ __host__ __device__ inline int upidx(int a, int b, int n) {  // packed upper, ro
 }
 
 template <int D>
-__device__ inline double inv_t(const double J[D][D], double Ji[D][D]) {
+__host__ __device__ inline double inv_t(const double J[D][D], double Ji[D][D]) {
     // Ji = J^{-T}; returns det J  (signed, as the reference)
     if (D == 2) {
         const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
@@ -82,7 +82,7 @@ __device__ inline bool affine(const double X[NG][D]) {
 }
 
 template <int NG, int D>
-__device__ inline double jac(const double X[NG][D], const double dN[NG][D], double Ji[D][D]) {
+__host__ __device__ inline double jac(const double X[NG][D], const double dN[NG][D], double Ji[D][D]) {
     double J[D][D];
     for (int a = 0; a < D; ++a)
         for (int b = 0; b < D; ++b) {
@@ -446,12 +446,12 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
 //                                           base/time/ResidualForceHistory.hpp
 // The host runs the finite-strain path (general) whenever past-state forces
 // are asked for, so that their contributions have the shared staging.
-__device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
+__host__ __device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
     const int m = (i + 1) * (j + 1);
     return m == 1 ? 0 : m == 4 ? 1 : m == 9 ? 2 : m == 2 ? 3 : m == 3 ? 4 : 5;
 }
 
-__device__ inline void material_eval(int mat, double lam, double mu, const double F[3][3], double S[3][3], double C[6][6]) {
+__host__ __device__ inline void material_eval(int mat, double lam, double mu, const double F[3][3], double S[3][3], double C[6][6]) {
     double Cg[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -772,6 +772,158 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
 }
 
 // ---------------------------------------------------------------------------
+// solid::HyperElastic in 2-D on quadrilaterals (Q1, Q2), plane strain: the
+// 2x2 displacement gradient sits in a 3x3 deformation gradient with F_33 = 1
+// (solid/Deformation.hpp:25-46) and the materials are evaluated in 3-D.  The
+// formulas are those of k_hyper_hex8 with the in-plane indices:
+//   K[Md+i, Nd+k] += sum_JL g_M,J (d_ik S_JL + F_iA C_AJBL F_kB) g_N,L detJ w
+//   F[Md+i]       -= sum_J (F S)_iJ g_M,J detJ w          (x -1)
+//   F[Md+i]       += f_i(x) phi_M detJ w                  (nodal body force)
+// and, in the TI variant, the mass per component and the residual forces at
+// past states.  One thread per element, FP64 throughout; the element matrix
+// is accumulated in the element's own staging slice (upper triangle,
+// element-major) instead of registers: a Q2 element has 171 entries.  2-D
+// elasticity is a parity path of the reference's 2-D examples, not a
+// throughput path.
+__host__ __device__ inline void flag_or(int* flags, int v) {
+#ifdef __CUDA_ARCH__
+    atomicOr(flags, v);
+#else
+    *flags |= v;
+#endif
+}
+
+// First Piola stress P = F S, in-plane rows and columns
+__host__ __device__ inline void piola2(const double F[3][3], const double S[3][3], double P[2][2]) {
+    for (int i = 0; i < 2; ++i)
+        for (int J = 0; J < 2; ++J) P[i][J] = F[i][0] * S[0][J] + F[i][1] * S[1][J] + F[i][2] * S[2][J];
+}
+
+template <int FDEG, int NQ, typename R, bool TI>
+__host__ __device__ inline void hyper_quad_element(const ElemArgs& A, const Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ>& T,
+                                                   int e) {
+    constexpr int NG = 4, NF = ET<ISL_QUAD, FDEG>::NF, NLOC = 2 * NF, NUP = NLOC * (NLOC + 1) / 2;
+    const int E = A.nelem;
+    double X[NG][2];
+    int nodes[NG];
+    for (int i = 0; i < NG; ++i) {
+        nodes[i] = A.conn[i * E + e];
+        for (int d = 0; d < 2; ++d) X[i][d] = A.X[(size_t)nodes[i] * 2 + d];
+    }
+    int obj[NF];
+    double uloc[NF][2];
+    for (int f = 0; f < NF; ++f) {
+        obj[f] = A.edof[f * E + e];
+        for (int i = 0; i < 2; ++i) uloc[f][i] = A.u[(size_t)obj[f] * 2 + i];
+    }
+    const double lam = A.coef[e], mu = A.coef[E + e];
+    const bool mass = TI && A.rho;
+    const double rho = mass ? A.rho[e] : 0.0;
+    R* SK = (R*)A.stageK + (size_t)e * NUP;
+    for (int u = 0; u < NUP; ++u) SK[u] = R(0);
+    double fe[NLOC];
+    for (int a = 0; a < NLOC; ++a) fe[a] = 0.0;
+    bool bad = false, nan = false;
+    for (int q = 0; q < NQ; ++q) {
+        double Ji[2][2];
+        const double detJ = jac<NG, 2>(X, T.dN[q], Ji);
+        bad |= !(detJ > 0.0);
+        const double c = detJ * T.w[q];
+        double g[NF][2];
+        for (int M = 0; M < NF; ++M)
+            for (int a = 0; a < 2; ++a) g[M][a] = Ji[a][0] * T.dphi[q][M][0] + Ji[a][1] * T.dphi[q][M][1];
+        double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int f = 0; f < NF; ++f)
+            for (int i = 0; i < 2; ++i)
+                for (int J = 0; J < 2; ++J) F[i][J] += g[f][J] * uloc[f][i];
+        double S[3][3], C[6][6];
+        material_eval(A.material, lam, mu, F, S, C);
+        // effective elasticity Ae[i][J][k][L] = d_ik S_JL + F_iA C_V(A,J)V(B,L) F_kB
+        double Ae[2][2][2][2];
+        for (int i = 0; i < 2; ++i)
+            for (int J = 0; J < 2; ++J)
+                for (int k = 0; k < 2; ++k)
+                    for (int L = 0; L < 2; ++L) {
+                        double v = (i == k) ? S[J][L] : 0.0;
+                        for (int Aa = 0; Aa < 2; ++Aa) {
+                            double t = 0.0;
+                            for (int B = 0; B < 2; ++B) t += C[voigt(Aa, J)][voigt(B, L)] * F[k][B];
+                            v += F[i][Aa] * t;
+                        }
+                        Ae[i][J][k][L] = v;
+                    }
+        for (int M = 0; M < NF; ++M)
+            for (int i = 0; i < 2; ++i) {
+                const int a = 2 * M + i;
+                double h[2][2];  // c sum_J g_M,J Ae[i][J][k][L]
+                for (int k = 0; k < 2; ++k)
+                    for (int L = 0; L < 2; ++L) h[k][L] = c * (g[M][0] * Ae[i][0][k][L] + g[M][1] * Ae[i][1][k][L]);
+                const double mM = mass ? A.mass_w * rho * c * T.phi[q][M] : 0.0;
+                for (int N = M; N < NF; ++N)
+                    for (int k = 0; k < 2; ++k) {
+                        const int b = 2 * N + k;
+                        if (b < a) continue;
+                        double v = h[k][0] * g[N][0] + h[k][1] * g[N][1];
+                        if (mass && i == k) v += mM * T.phi[q][N];
+                        SK[upidx(a, b, NLOC)] += R(v);
+                    }
+            }
+        if (A.with_residual) {
+            double P[2][2];
+            piola2(F, S, P);
+            for (int M = 0; M < NF; ++M)
+                for (int i = 0; i < 2; ++i) {
+                    const double v = (P[i][0] * g[M][0] + P[i][1] * g[M][1]) * c;
+                    nan |= !(v == v);
+                    fe[2 * M + i] -= v;
+                }
+        }
+        if (TI) {
+            for (int sidx = 0; sidx < A.nfw; ++sidx) {  // residual force at a past state
+                double Fh[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                for (int f = 0; f < NF; ++f)
+                    for (int i = 0; i < 2; ++i) {
+                        const double uf = A.hist[(size_t)sidx * A.hstride + (size_t)obj[f] * 2 + i];
+                        for (int J = 0; J < 2; ++J) Fh[i][J] += g[f][J] * uf;
+                    }
+                double Sh[3][3], Ch[6][6], Ph[2][2];
+                material_eval(A.material, lam, mu, Fh, Sh, Ch);
+                piola2(Fh, Sh, Ph);
+                for (int M = 0; M < NF; ++M)
+                    for (int i = 0; i < 2; ++i) {
+                        const double v = A.fw[sidx] * (Ph[i][0] * g[M][0] + Ph[i][1] * g[M][1]) * c;
+                        nan |= !(v == v);
+                        fe[2 * M + i] -= v;
+                    }
+            }
+            if (mass) {  // M h, h the weighted history
+                double hq[2] = {0.0, 0.0};
+                for (int f = 0; f < NF; ++f)
+                    for (int i = 0; i < 2; ++i) hq[i] += T.phi[q][f] * A.hvec[(size_t)obj[f] * 2 + i];
+                for (int M = 0; M < NF; ++M)
+                    for (int i = 0; i < 2; ++i) fe[2 * M + i] += rho * c * T.phi[q][M] * hq[i];
+            }
+        }
+        if (A.fnodal) {
+            double f[2] = {0.0, 0.0};
+            for (int i = 0; i < NG; ++i)
+                for (int d = 0; d < 2; ++d) f[d] += T.N[q][i] * A.fnodal[(size_t)nodes[i] * 2 + d];
+            for (int M = 0; M < NF; ++M)
+                for (int d = 0; d < 2; ++d) fe[2 * M + d] += f[d] * T.phi[q][M] * c;
+        }
+    }
+    if (bad) flag_or(A.flags, 1);
+    if (nan) flag_or(A.flags, 2);
+    for (int a = 0; a < NLOC; ++a) A.stageF[(size_t)a * E + e] = fe[a];
+}
+
+template <int FDEG, int NQ, typename R, bool TI>
+__global__ void __launch_bounds__(128) k_hyper_quad(const ElemArgs A, const Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ> T) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < A.nelem) hyper_quad_element<FDEG, NQ, R, TI>(A, T, e);
+}
+
+// ---------------------------------------------------------------------------
 // Linear elasticity (HyperElastic<StVenant> at u = 0) on affine hexahedra,
 // one thread per element.  With a constant Jacobian the quadrature sum of
 // k_hyper_hex8 factors:
@@ -866,10 +1018,12 @@ struct FaceArgs {
     const int32_t* neu_elem;
     const int32_t* neu_off;
     const int32_t* neu_face;
-    const double* trac;
+    const double* trac;     // [n][NCOMP] per face, or [n][nfv][NCOMP] per face vertex (vert)
+    int vert;
     double* stageF;
     int fv[6][4];
     double w[9];
+    double S[9][4];         // face geometry functions at the surface points
     double dS[9][4][2];
     double phi[6][9][NF];
 };
@@ -903,9 +1057,22 @@ __global__ void k_neumann(const FaceArgs<NF, NCOMP> A) {
                 const double n2 = Tg[0][0] * Tg[1][1] - Tg[1][0] * Tg[0][1];
                 len = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
             }
+            // traction at the point: constant per face, or interpolated from
+            // the face vertices by the face geometry functions (exact for a
+            // traction linear along a straight face)
+            double t[NCOMP];
+            for (int c = 0; c < NCOMP; ++c) {
+                if (A.vert) {
+                    double s = 0.0;
+                    for (int v = 0; v < A.nfv; ++v) s += A.S[q][v] * A.trac[((size_t)j * A.nfv + v) * NCOMP + c];
+                    t[c] = s;
+                } else {
+                    t[c] = A.trac[j * NCOMP + c];
+                }
+            }
             for (int s = 0; s < NF; ++s) {
                 const double wgt = A.phi[f][q][s] * A.w[q] * len;
-                for (int c = 0; c < NCOMP; ++c) fe[s][c] += A.trac[j * NCOMP + c] * wgt;
+                for (int c = 0; c < NCOMP; ++c) fe[s][c] += t[c] * wgt;
             }
         }
     }
@@ -1244,9 +1411,35 @@ static int dispatch_heat_static(isl_ctx* c, ElemArgs A, int with_residual) {
     ISL_FAIL(c, ISL_ERR_ARG, "heat::Static: unsupported element / quadrature combination");
 }
 
+template <int FDEG, int NQ, typename R>
+static int launch_hyper_quad(isl_ctx* c, const ElemArgs& A, const HostTab& h) {
+    Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ> T;
+    fill_tab<ISL_QUAD, FDEG, NQ>(T, h);
+    if (A.rho || A.nfw > 0)
+        k_hyper_quad<FDEG, NQ, R, true><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    else
+        k_hyper_quad<FDEG, NQ, R, false><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    return ISL_OK;
+}
+
+template <typename R>
+static int dispatch_hyper_quad(isl_ctx* c, const ElemArgs& A) {
+    HostTab h;
+    if (!make_host_tables(ISL_QUAD, c->fedeg, c->qdeg, h)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
+    if (c->fedeg == 1 && h.nq == 4) return launch_hyper_quad<1, 4, R>(c, A, h);
+    if (c->fedeg == 1 && h.nq == 9) return launch_hyper_quad<1, 9, R>(c, A, h);
+    if (c->fedeg == 2 && h.nq == 4) return launch_hyper_quad<2, 4, R>(c, A, h);
+    if (c->fedeg == 2 && h.nq == 9) return launch_hyper_quad<2, 9, R>(c, A, h);
+    ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic on quadrilaterals: Q1 or Q2 with 2x2 or 3x3 quadrature");
+}
+
 template <typename R>
 static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
-    if (!(c->shape == ISL_HEX && c->fedeg == 1)) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: only trilinear hexahedra on the device");
+    if (c->shape == ISL_QUAD) return dispatch_hyper_quad<R>(c, A);
+    if (!(c->shape == ISL_HEX && c->fedeg == 1))
+        ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: quadrilaterals (Q1, Q2) and trilinear hexahedra on the device");
     HostTab h;
     if (!make_host_tables(ISL_HEX, 1, c->qdeg, h) || h.nq != 8) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: 2x2x2 quadrature required");
     Tab<3, 8, 8, 8> T;
@@ -1306,11 +1499,12 @@ static int launch_neumann(isl_ctx* c) {
     memset(&A, 0, sizeof(A));
     A.nelem = (int)c->nelem; A.n_neu = (int)c->n_neu_elem; A.nfaces = ft.nfaces; A.nsq = ft.nsq; A.nfv = ft.nfv; A.dim = D;
     A.X = c->dX.p; A.conn = c->dconn.p; A.neu_elem = c->dneu_elem.p; A.neu_off = c->dneu_off.p; A.neu_face = c->dneu_face.p;
-    A.trac = c->dneu_trac.p; A.stageF = c->dstageF.p;
+    A.trac = c->dneu_trac.p; A.vert = c->neu_vertex ? 1 : 0; A.stageF = c->dstageF.p;
     for (int f = 0; f < ft.nfaces; ++f)
         for (int v = 0; v < ft.nfv; ++v) A.fv[f][v] = ft.fv[f * ft.nfv + v];
     for (int q = 0; q < ft.nsq; ++q) {
         A.w[q] = ft.w[q];
+        for (int v = 0; v < ft.nfv; ++v) A.S[q][v] = ft.S[q * ft.nfv + v];
         for (int v = 0; v < ft.nfv; ++v)
             for (int a = 0; a < D - 1; ++a) A.dS[q][v][a] = ft.dS[(q * ft.nfv + v) * (D - 1) + a];
     }

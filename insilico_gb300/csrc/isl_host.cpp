@@ -235,6 +235,7 @@ bool make_face_tables(int shape, int fedeg, int sqdeg, FaceTab& t) {
             }
         }
     }
+    t.S = sval;
     std::vector<double> v, g;
     int nf = 0;
     for (int f = 0; f < t.nfaces; ++f)
@@ -340,6 +341,50 @@ void group_faces(const std::vector<Key>& keys, std::vector<int64_t>& first, std:
 }  // namespace
 
 // ===========================================================================
+namespace {
+
+// Neumann faces grouped by element for k_neumann; traction per face
+// ([n][ncomp]) or, with vertex, per face vertex ([n][nfv][ncomp]).
+int neumann_faces(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, const double* traction, bool vertex,
+                  int squad_degree) {
+    if (!c || !c->fedeg) return ISL_ERR_ARG;
+    c->n_neu_elem = 0;
+    if (n <= 0) return ISL_OK;
+    if (!elem || !face || !traction) return ISL_ERR_ARG;
+    if (c->shape == ISL_TET) ISL_FAIL(c, ISL_ERR_ARG, "Neumann faces on tetrahedra are not supported");
+    const int nfc = c->shape == ISL_QUAD ? 4 : 6;
+    const int nval = (vertex ? (c->shape == ISL_QUAD ? 2 : 4) : 1) * c->ncomp;
+    std::vector<int64_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    for (int64_t i = 0; i < n; ++i)
+        if (elem[i] < 0 || elem[i] >= c->nelem || face[i] < 0 || face[i] >= nfc) ISL_FAIL(c, ISL_ERR_ARG, "Neumann face out of range");
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return elem[a] < elem[b]; });
+    std::vector<int32_t> el, off, fc;
+    std::vector<double> tr;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t i = idx[k];
+        if (el.empty() || el.back() != elem[i]) { el.push_back((int32_t)elem[i]); off.push_back((int32_t)k); }
+        fc.push_back(face[i]);
+        for (int d = 0; d < nval; ++d) tr.push_back(traction[i * nval + d]);
+    }
+    off.push_back((int32_t)n);
+    c->n_neu_elem = (int64_t)el.size();
+    c->neu_vertex = vertex;
+    c->sqdeg = squad_degree;
+    ISL_CHECK_CUDA(c, c->dneu_elem.alloc(el.size()));
+    ISL_CHECK_CUDA(c, c->dneu_off.alloc(off.size()));
+    ISL_CHECK_CUDA(c, c->dneu_face.alloc(fc.size()));
+    ISL_CHECK_CUDA(c, c->dneu_trac.alloc(tr.size()));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_elem.p, el.data(), el.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_face.p, fc.data(), fc.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_trac.p, tr.data(), tr.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int isl_ctx_create(isl_ctx** out, int device, void* stream) {
@@ -931,38 +976,14 @@ int isl_set_body_force_nodal(isl_ctx* c, const double* f) {
 
 int isl_set_neumann(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, const double* traction, int squad_degree) {
     ISL_TRY
-    if (!c || !c->fedeg) return ISL_ERR_ARG;
-    c->n_neu_elem = 0;
-    if (n <= 0) return ISL_OK;
-    if (!elem || !face || !traction) return ISL_ERR_ARG;
-    if (c->shape == ISL_TET) ISL_FAIL(c, ISL_ERR_ARG, "Neumann faces on tetrahedra are not supported");
-    const int nfc = c->shape == ISL_QUAD ? 4 : 6;
-    std::vector<int64_t> idx(n);
-    std::iota(idx.begin(), idx.end(), 0);
-    for (int64_t i = 0; i < n; ++i)
-        if (elem[i] < 0 || elem[i] >= c->nelem || face[i] < 0 || face[i] >= nfc) ISL_FAIL(c, ISL_ERR_ARG, "Neumann face out of range");
-    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return elem[a] < elem[b]; });
-    std::vector<int32_t> el, off, fc;
-    std::vector<double> tr;
-    for (int64_t k = 0; k < n; ++k) {
-        const int64_t i = idx[k];
-        if (el.empty() || el.back() != elem[i]) { el.push_back((int32_t)elem[i]); off.push_back((int32_t)k); }
-        fc.push_back(face[i]);
-        for (int d = 0; d < c->ncomp; ++d) tr.push_back(traction[i * c->ncomp + d]);
-    }
-    off.push_back((int32_t)n);
-    c->n_neu_elem = (int64_t)el.size();
-    c->sqdeg = squad_degree;
-    ISL_CHECK_CUDA(c, c->dneu_elem.alloc(el.size()));
-    ISL_CHECK_CUDA(c, c->dneu_off.alloc(off.size()));
-    ISL_CHECK_CUDA(c, c->dneu_face.alloc(fc.size()));
-    ISL_CHECK_CUDA(c, c->dneu_trac.alloc(tr.size()));
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_elem.p, el.data(), el.size() * 4, cudaMemcpyHostToDevice, c->stream));
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, c->stream));
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_face.p, fc.data(), fc.size() * 4, cudaMemcpyHostToDevice, c->stream));
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dneu_trac.p, tr.data(), tr.size() * 8, cudaMemcpyHostToDevice, c->stream));
-    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
-    return ISL_OK;
+    return neumann_faces(c, n, elem, face, traction, false, squad_degree);
+    ISL_CATCH(c)
+}
+
+int isl_set_neumann_vertex(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, const double* traction,
+                           int squad_degree) {
+    ISL_TRY
+    return neumann_faces(c, n, elem, face, traction, true, squad_degree);
     ISL_CATCH(c)
 }
 

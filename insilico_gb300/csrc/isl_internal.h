@@ -47,6 +47,7 @@ struct FaceTab {
     int nfaces = 0, nsq = 0, nfv = 0, nf = 0, dim = 0;
     std::vector<int> fv;        // [nfaces][nfv] local vertex ids of the face
     std::vector<double> w;      // [nsq]
+    std::vector<double> S;      // [nsq][nfv] face geometry function values
     std::vector<double> phi;    // [nfaces][nsq][nf]
     std::vector<double> dS;     // [nsq][nfv][dim-1] face geometry gradients
 };
@@ -167,6 +168,7 @@ struct isl_ctx {
     int64_t n_neu_elem = 0;
     isl::DBuf<int32_t> dneu_elem, dneu_off, dneu_face;
     isl::DBuf<double> dneu_trac;
+    bool neu_vertex = false;     // dneu_trac holds values per face vertex (isl_set_neumann_vertex)
     // elements with at least one constrained local DOF (for the Dirichlet lift)
     int64_t n_lift = 0;
     isl::DBuf<int32_t> dlift_elem;

@@ -178,6 +178,15 @@ class System:
         t = np.ascontiguousarray(np.broadcast_to(traction, (len(e), self.ncomp)), dtype=np.float64)
         self._chk(self.L.isl_set_neumann(self.h, len(e), A.i64(e), A.i32(f), A.d(t), squad_degree), "isl_set_neumann")
 
+    def set_neumann_vertex(self, elem, face, traction, squad_degree: int = 2):
+        """traction per face vertex [n, nfv, ncomp], interpolated along each face"""
+        e = np.ascontiguousarray(elem, dtype=np.int64)
+        f = np.ascontiguousarray(face, dtype=np.int32)
+        nfv = 2 if self.shape == A.QUAD else 4
+        t = np.ascontiguousarray(np.broadcast_to(traction, (len(e), nfv, self.ncomp)), dtype=np.float64)
+        self._chk(self.L.isl_set_neumann_vertex(self.h, len(e), A.i64(e), A.i32(f), A.d(t), squad_degree),
+                  "isl_set_neumann_vertex")
+
     def set_values(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64)
         self._chk(self.L.isl_set_values(self.h, A.d(u)))

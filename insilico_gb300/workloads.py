@@ -257,6 +257,76 @@ def heat_newton(S, n, max_iter=10, tolerance=1e-8, lin_tol=1e-11, method=None, l
     return rows
 
 
+def pulled_sheet_faces(S, X, conn):
+    """boundary faces on x = 1 and the y coordinate of their two vertices
+    (face vertex order of QUAD_EDGES)"""
+    e, f = S.boundary_faces()
+    e, f = faces_on_plane(A.QUAD, X, conn, e, f, 0, 1.0, tol=1e-5)
+    y = X[conn[e[:, None], QUAD_EDGES[f]], 1]
+    return e, f, y
+
+
+def compressible(S, X, conn, E=1000.0, nu=0.3, max_iter=30, load_steps=5, pull=3.0, traction=1000.0,
+                 disp_controlled=True, tolerance=1e-12, lin_tol=1e-12, method=None):
+    """reference/06-elastic/compressible.cpp through the C-ABI: a Q2 sheet of
+    NeoHookeanCompressible material (E, nu), clamped at x = 0 and pulled at
+    x = 1 (PulledSheet.hpp:35-75): by the displacement pull in x
+    (disp_controlled) or by the traction value (y - 1/2) in x, raised in
+    load_steps equal steps.  Per load step (compressible.cpp:245-330) the
+    Dirichlet values are scaled up (scaleConstraints, :254), then Newton:
+    assemble the tangent and residual, stop when |R| = ||b|| / N < tolerance E
+    (:298-302), solve (cgSolve there, CG to lin_tol here), stop when
+    |x| < tolerance (:315-321), add the increment.  The traction is
+    tabulated at the vertices of the x = 1 faces (isl_set_neumann_vertex),
+    exact for this linear profile.  Returns (ndofs, [(step, iter, |R|, |x| or
+    None)])."""
+    if method is None:
+        method = A.SOLVE_CG_FP64
+    lam, mu = lame(E, nu)
+    S.upload_mesh(A.QUAD, X, conn)
+    S.create_field(2, 2)
+    first_pull = pull / load_steps
+
+    def bc(x):
+        left = np.abs(x[:, 0]) < 1e-6
+        right = np.abs(x[:, 0] - 1.0) < 1e-6
+        mask = np.zeros((len(x), 2), dtype=bool)
+        vals = np.zeros((len(x), 2))
+        mask[left, :] = True
+        if disp_controlled:
+            mask[right, 0] = True
+            vals[right, 0] = first_pull
+        return mask, vals
+    S.constrain_boundary(bc)
+    n = S.number_dofs()
+    S.register_pattern()
+    S.set_hyperelastic("neohooke", np.full(len(conn), lam), np.full(len(conn), mu), 3)
+    if not disp_controlled:
+        fe, ff, fy = pulled_sheet_faces(S, X, conn)
+    rows = []
+    for step in range(load_steps):
+        S.scale_constraints(float(step + 1) if step == 0 else (step + 1) / step)
+        it = 0
+        while it < max_iter:
+            if not disp_controlled:
+                t = np.zeros((len(fe), 2, 2))
+                t[:, :, 0] = traction * (step + 1) / load_steps * (fy - 0.5)
+                S.set_neumann_vertex(fe, ff, t, 3)
+            S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
+            conv1 = S.norm()
+            if conv1 < tolerance * E:
+                rows.append((step, it, conv1, None))
+                break
+            S.solve(method, tol=lin_tol)
+            conv2 = S.norm()
+            S.distribute(add=True)
+            rows.append((step, it, conv1, conv2))
+            it += 1
+            if conv2 < tolerance:
+                break
+    return n, rows
+
+
 # ---------------------------------------------------------------------------
 # Linear multi-step time integration (base/time/BDF.hpp, MultiStep.hpp)
 # BDF LHS weights a_0..a_q as base/time/BDF.hpp:95-104 defines them (its
