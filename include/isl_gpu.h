@@ -174,7 +174,10 @@ int isl_set_body_force_nodal(isl_ctx* ctx, const double* f /* [n_nodes][ncomp] *
 int isl_set_neumann(isl_ctx* ctx, int64_t n, const int64_t* elem, const int* face, const double* traction,
                     int squad_degree);
 /* Traction given at the vertices of each boundary face ([n][nfv][ncomp], nfv
- * = 2 on quadrilaterals, 4 on hexahedra, in the face's vertex order) and
+ * = 2 on quadrilaterals, 4 on hexahedra, in the face's vertex order: element
+ * vertices (0,1) (1,2) (2,3) (3,0) of a quadrilateral's faces 0-3, and
+ * (0,3,2,1) (4,5,6,7) (0,1,5,4) (1,2,6,5) (2,3,7,6) (3,0,4,7) of a
+ * hexahedron's faces 0-5, vertices in hierarchic order) and
  * interpolated by the face geometry functions: the caller's tabulation of a
  * traction function (base/asmb/NeumannForce.hpp:132-174 evaluates it at the
  * surface quadrature points), exact for tractions linear along straight faces

@@ -134,6 +134,15 @@ public:
     void bodyForceNodal(const std::vector<double>& f) {
         check(ctx_, isl_set_body_force_nodal(ctx_, f.data()), "isl_set_body_force_nodal");
     }
+    // neumannForceComputation over the given boundary faces: a traction per
+    // face ([n][ncomp]) or per face vertex ([n][nfv][ncomp], vertex = true)
+    void neumann(const std::vector<int64_t>& elem, const std::vector<int>& face, const std::vector<double>& traction,
+                 int squad_degree, bool vertex = false) {
+        const int64_t n = (int64_t)elem.size();
+        const int st = vertex ? isl_set_neumann_vertex(ctx_, n, elem.data(), face.data(), traction.data(), squad_degree)
+                              : isl_set_neumann(ctx_, n, elem.data(), face.data(), traction.data(), squad_degree);
+        check(ctx_, st, vertex ? "isl_set_neumann_vertex" : "isl_set_neumann");
+    }
 
     // ---- assembly + solve (SOLVER duck type)
     void assemble(int precision = ISL_PREC_FP64, bool incremental = true, bool with_residual = false) {
