@@ -51,7 +51,8 @@ def test_host_only_context_rejects_device_work():
 def test_host_only_argument_checks():
     """argument checks of the newer entry points on a host-only context: the
     time-integration and post-processing calls that need a device refuse with
-    ISL_ERR_ARG, and option values out of range are refused"""
+    ISL_ERR_ARG, and option values out of range, inertia weights beyond the
+    stored history and Neumann faces out of range are refused"""
     import pytest
     from insilico_gb300.system import System
     S = System(device=-1)
@@ -61,7 +62,10 @@ def test_host_only_argument_checks():
     for call in (lambda: S.set_history(1), lambda: S.quadrature_points(2),
                  lambda: S.error_norm(0, 2, np.zeros(4)), lambda: S.set_force_history([1.0]),
                  lambda: S.set_option(A.OPT_BICGSTAB_KIND, 104), lambda: S.set_option(A.OPT_SPMV32_KIND, 3),
-                 lambda: S.set_option(A.OPT_PERSISTENT, 7)):
+                 lambda: S.set_option(A.OPT_PERSISTENT, 7),
+                 lambda: S.set_inertia(np.ones(1), 1.0, [1.0, -1.0]),
+                 lambda: S.set_neumann_vertex([0], [4], np.zeros((1, 2, 1))),
+                 lambda: S.set_neumann_vertex([1], [0], np.zeros((1, 2, 1)))):
         with pytest.raises(A.IslError) as ei:
             call()
         assert ei.value.code == A.ISL_ERR_ARG
