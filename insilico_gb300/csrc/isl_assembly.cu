@@ -20,105 +20,10 @@
 #include <cmath>
 #include <vector>
 
+#include "isl_elem.cuh"
 #include "isl_internal.h"
 
 namespace isl {
-
-// ---------------------------------------------------------------------------
-// small helpers
-__host__ __device__ inline int upidx(int a, int b, int n) {  // packed upper, row-major, a <= b
-    return a * n - (a * (a - 1)) / 2 + (b - a);
-}
-
-template <int D>
-__host__ __device__ inline double inv_t(const double J[D][D], double Ji[D][D]) {
-    // Ji = J^{-T}; returns det J  (signed, as the reference)
-    if (D == 2) {
-        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-        const double id = 1.0 / det;
-        Ji[0][0] = J[1][1] * id;  Ji[0][1] = -J[1][0] * id;
-        Ji[1][0] = -J[0][1] * id; Ji[1][1] = J[0][0] * id;
-        return det;
-    } else {
-        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-        const double id = 1.0 / det;
-        // (J^{-1})^T = cofactor(J) / det
-        Ji[0][0] = c00 * id; Ji[0][1] = c01 * id; Ji[0][2] = c02 * id;
-        Ji[1][0] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        Ji[1][2] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        Ji[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        Ji[2][1] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-        return det;
-    }
-}
-
-// Is the geometry map affine (constant Jacobian)?  Tetrahedra always are;
-// quads/hexes when their bilinear/trilinear coefficients vanish.
-template <int SHAPE, int NG, int D>
-__device__ inline bool affine(const double X[NG][D]) {
-    if (SHAPE == ISL_TET) return true;
-    double scale = 0.0, dev = 0.0;
-    for (int d = 0; d < D; ++d) {
-        if (SHAPE == ISL_QUAD) {
-            const double t = X[0][d] - X[1][d] + X[2][d] - X[3][d];
-            dev = fmax(dev, fabs(t));
-            scale = fmax(scale, fabs(X[1][d] - X[0][d]) + fabs(X[3][d] - X[0][d]));
-        } else {
-            // hierarchic hex vertices: 0 c000, 1 c100, 2 c110, 3 c010, 4 c001, 5 c101, 6 c111, 7 c011
-            const double xy = X[0][d] - X[1][d] + X[2][d] - X[3][d];
-            const double xz = X[0][d] - X[1][d] - X[4][d] + X[5][d];
-            const double yz = X[0][d] - X[3][d] - X[4][d] + X[7][d];
-            const double xyz = -X[0][d] + X[1][d] - X[2][d] + X[3][d] + X[4][d] - X[5][d] + X[6][d] - X[7][d];
-            dev = fmax(dev, fmax(fmax(fabs(xy), fabs(xz)), fmax(fabs(yz), fabs(xyz))));
-            scale = fmax(scale, fabs(X[1][d] - X[0][d]) + fabs(X[3][d] - X[0][d]) + fabs(X[4][d] - X[0][d]));
-        }
-    }
-    return dev <= 1e-13 * scale;
-}
-
-template <int NG, int D>
-__host__ __device__ inline double jac(const double X[NG][D], const double dN[NG][D], double Ji[D][D]) {
-    double J[D][D];
-    for (int a = 0; a < D; ++a)
-        for (int b = 0; b < D; ++b) {
-            double s = 0.0;
-            for (int i = 0; i < NG; ++i) s += X[i][a] * dN[i][b];
-            J[a][b] = s;
-        }
-    return inv_t<D>(J, Ji);
-}
-
-struct ElemArgs {
-    int nelem;
-    const double* X;        // [nnodes][D]
-    const int32_t* conn;    // [NG][nelem]
-    const int32_t* edof;    // [NF][nelem]
-    const double* coef;     // [ncoef][nelem]
-    const double* u;        // per dofobj comp
-    const double* fnodal;   // [nnodes][ncomp] or null
-    int with_residual;
-    int general;            // hyperelastic: 1 = finite strain path, 0 = small-strain at u = 0
-    int material;
-    void* stageK;           // [nup][nelem] (R)
-    double* stageF;         // [nloc][nelem]
-    int* flags;
-    // inertia terms of a multi-step method (base/time/ReactionTerms.hpp):
-    // K += mass_w rho M, F += rho M h, h = the weighted DOF history; rho null: none
-    const double* rho;      // [nelem]
-    double mass_w;
-    const double* hvec;     // per dofobj comp
-    // residual forces at past states (base/time/ResidualForceHistory.hpp):
-    // F -= sum_s fw[s] F_int(x^(s+1)), x^(s+1) = hist[s * hstride + .]
-    const double* hist;
-    int64_t hstride;
-    int nfw;
-    double fw[4];
-};
 
 // ---------------------------------------------------------------------------
 // heat::Laplace element kernel, one thread per element.
@@ -446,47 +351,6 @@ __global__ void __launch_bounds__(128) k_heat_static(const ElemArgs A, const Tab
 //                                           base/time/ResidualForceHistory.hpp
 // The host runs the finite-strain path (general) whenever past-state forces
 // are asked for, so that their contributions have the shared staging.
-__host__ __device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
-    const int m = (i + 1) * (j + 1);
-    return m == 1 ? 0 : m == 4 ? 1 : m == 9 ? 2 : m == 2 ? 3 : m == 3 ? 4 : 5;
-}
-
-__host__ __device__ inline void material_eval(int mat, double lam, double mu, const double F[3][3], double S[3][3], double C[6][6]) {
-    double Cg[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) Cg[a][b] = F[0][a] * F[0][b] + F[1][a] * F[1][b] + F[2][a] * F[2][b];
-    if (mat == ISL_MAT_STVENANT) {
-        double E[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) E[a][b] = 0.5 * (Cg[a][b] - (a == b ? 1.0 : 0.0));
-        const double tr = E[0][0] + E[1][1] + E[2][2];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) S[a][b] = lam * tr * (a == b ? 1.0 : 0.0) + 2.0 * mu * E[a][b];
-        for (int a = 0; a < 6; ++a)
-            for (int b = 0; b < 6; ++b) C[a][b] = (a < 3 && b < 3) ? lam : 0.0;
-        for (int i = 0; i < 3; ++i) C[i][i] += 2.0 * mu;
-        for (int i = 3; i < 6; ++i) C[i][i] += mu;
-        return;
-    }
-    double Ci[3][3];
-    const double detC = inv_t<3>(Cg, Ci);  // Cg symmetric, so Ci = Cg^{-T} = Cg^{-1}
-    (void)detC;
-    const double J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) - F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
-                     F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
-    const double lj = log(J);
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) S[a][b] = (lam * lj - mu) * Ci[a][b] + mu * (a == b ? 1.0 : 0.0);
-    const double f2 = mu - lam * lj;
-    for (int A = 0; A < 3; ++A)
-        for (int B = A; B < 3; ++B)
-            for (int Cc = 0; Cc < 3; ++Cc)
-                for (int Dd = Cc; Dd < 3; ++Dd)
-                    C[voigt(A, B)][voigt(Cc, Dd)] =
-                        lam * Ci[A][B] * Ci[Cc][Dd] + f2 * (Ci[A][Cc] * Ci[B][Dd] + Ci[A][Dd] * Ci[B][Cc]);
-}
-
 template <typename R, int EPB, bool TI>
 __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const Tab<3, 8, 8, 8> T) {
     constexpr int NLOC = 24;
@@ -771,157 +635,6 @@ __global__ void __launch_bounds__(EPB * 8) k_hyper_hex8(const ElemArgs A, const 
     for (int i = 0; i < 3; ++i) A.stageF[(size_t)(3 * M + i) * E + e] = fe[i];
 }
 
-// ---------------------------------------------------------------------------
-// solid::HyperElastic in 2-D on quadrilaterals (Q1, Q2), plane strain: the
-// 2x2 displacement gradient sits in a 3x3 deformation gradient with F_33 = 1
-// (solid/Deformation.hpp:25-46) and the materials are evaluated in 3-D.  The
-// formulas are those of k_hyper_hex8 with the in-plane indices:
-//   K[Md+i, Nd+k] += sum_JL g_M,J (d_ik S_JL + F_iA C_AJBL F_kB) g_N,L detJ w
-//   F[Md+i]       -= sum_J (F S)_iJ g_M,J detJ w          (x -1)
-//   F[Md+i]       += f_i(x) phi_M detJ w                  (nodal body force)
-// and, in the TI variant, the mass per component and the residual forces at
-// past states.  One thread per element, FP64 throughout; the element matrix
-// is accumulated in the element's own staging slice (upper triangle,
-// element-major) instead of registers: a Q2 element has 171 entries.  2-D
-// elasticity is a parity path of the reference's 2-D examples, not a
-// throughput path.
-__host__ __device__ inline void flag_or(int* flags, int v) {
-#ifdef __CUDA_ARCH__
-    atomicOr(flags, v);
-#else
-    *flags |= v;
-#endif
-}
-
-// First Piola stress P = F S, in-plane rows and columns
-__host__ __device__ inline void piola2(const double F[3][3], const double S[3][3], double P[2][2]) {
-    for (int i = 0; i < 2; ++i)
-        for (int J = 0; J < 2; ++J) P[i][J] = F[i][0] * S[0][J] + F[i][1] * S[1][J] + F[i][2] * S[2][J];
-}
-
-template <int FDEG, int NQ, typename R, bool TI>
-__host__ __device__ inline void hyper_quad_element(const ElemArgs& A, const Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ>& T,
-                                                   int e) {
-    constexpr int NG = 4, NF = ET<ISL_QUAD, FDEG>::NF, NLOC = 2 * NF, NUP = NLOC * (NLOC + 1) / 2;
-    const int E = A.nelem;
-    double X[NG][2];
-    int nodes[NG];
-    for (int i = 0; i < NG; ++i) {
-        nodes[i] = A.conn[i * E + e];
-        for (int d = 0; d < 2; ++d) X[i][d] = A.X[(size_t)nodes[i] * 2 + d];
-    }
-    int obj[NF];
-    double uloc[NF][2];
-    for (int f = 0; f < NF; ++f) {
-        obj[f] = A.edof[f * E + e];
-        for (int i = 0; i < 2; ++i) uloc[f][i] = A.u[(size_t)obj[f] * 2 + i];
-    }
-    const double lam = A.coef[e], mu = A.coef[E + e];
-    const bool mass = TI && A.rho;
-    const double rho = mass ? A.rho[e] : 0.0;
-    R* SK = (R*)A.stageK + (size_t)e * NUP;
-    for (int u = 0; u < NUP; ++u) SK[u] = R(0);
-    double fe[NLOC];
-    for (int a = 0; a < NLOC; ++a) fe[a] = 0.0;
-    bool bad = false, nan = false;
-    for (int q = 0; q < NQ; ++q) {
-        double Ji[2][2];
-        const double detJ = jac<NG, 2>(X, T.dN[q], Ji);
-        bad |= !(detJ > 0.0);
-        const double c = detJ * T.w[q];
-        double g[NF][2];
-        for (int M = 0; M < NF; ++M)
-            for (int a = 0; a < 2; ++a) g[M][a] = Ji[a][0] * T.dphi[q][M][0] + Ji[a][1] * T.dphi[q][M][1];
-        double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-        for (int f = 0; f < NF; ++f)
-            for (int i = 0; i < 2; ++i)
-                for (int J = 0; J < 2; ++J) F[i][J] += g[f][J] * uloc[f][i];
-        double S[3][3], C[6][6];
-        material_eval(A.material, lam, mu, F, S, C);
-        // effective elasticity Ae[i][J][k][L] = d_ik S_JL + F_iA C_V(A,J)V(B,L) F_kB
-        double Ae[2][2][2][2];
-        for (int i = 0; i < 2; ++i)
-            for (int J = 0; J < 2; ++J)
-                for (int k = 0; k < 2; ++k)
-                    for (int L = 0; L < 2; ++L) {
-                        double v = (i == k) ? S[J][L] : 0.0;
-                        for (int Aa = 0; Aa < 2; ++Aa) {
-                            double t = 0.0;
-                            for (int B = 0; B < 2; ++B) t += C[voigt(Aa, J)][voigt(B, L)] * F[k][B];
-                            v += F[i][Aa] * t;
-                        }
-                        Ae[i][J][k][L] = v;
-                    }
-        for (int M = 0; M < NF; ++M)
-            for (int i = 0; i < 2; ++i) {
-                const int a = 2 * M + i;
-                double h[2][2];  // c sum_J g_M,J Ae[i][J][k][L]
-                for (int k = 0; k < 2; ++k)
-                    for (int L = 0; L < 2; ++L) h[k][L] = c * (g[M][0] * Ae[i][0][k][L] + g[M][1] * Ae[i][1][k][L]);
-                const double mM = mass ? A.mass_w * rho * c * T.phi[q][M] : 0.0;
-                for (int N = M; N < NF; ++N)
-                    for (int k = 0; k < 2; ++k) {
-                        const int b = 2 * N + k;
-                        if (b < a) continue;
-                        double v = h[k][0] * g[N][0] + h[k][1] * g[N][1];
-                        if (mass && i == k) v += mM * T.phi[q][N];
-                        SK[upidx(a, b, NLOC)] += R(v);
-                    }
-            }
-        if (A.with_residual) {
-            double P[2][2];
-            piola2(F, S, P);
-            for (int M = 0; M < NF; ++M)
-                for (int i = 0; i < 2; ++i) {
-                    const double v = (P[i][0] * g[M][0] + P[i][1] * g[M][1]) * c;
-                    nan |= !(v == v);
-                    fe[2 * M + i] -= v;
-                }
-        }
-        if (TI) {
-            for (int sidx = 0; sidx < A.nfw; ++sidx) {  // residual force at a past state
-                double Fh[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-                for (int f = 0; f < NF; ++f)
-                    for (int i = 0; i < 2; ++i) {
-                        const double uf = A.hist[(size_t)sidx * A.hstride + (size_t)obj[f] * 2 + i];
-                        for (int J = 0; J < 2; ++J) Fh[i][J] += g[f][J] * uf;
-                    }
-                double Sh[3][3], Ch[6][6], Ph[2][2];
-                material_eval(A.material, lam, mu, Fh, Sh, Ch);
-                piola2(Fh, Sh, Ph);
-                for (int M = 0; M < NF; ++M)
-                    for (int i = 0; i < 2; ++i) {
-                        const double v = A.fw[sidx] * (Ph[i][0] * g[M][0] + Ph[i][1] * g[M][1]) * c;
-                        nan |= !(v == v);
-                        fe[2 * M + i] -= v;
-                    }
-            }
-            if (mass) {  // M h, h the weighted history
-                double hq[2] = {0.0, 0.0};
-                for (int f = 0; f < NF; ++f)
-                    for (int i = 0; i < 2; ++i) hq[i] += T.phi[q][f] * A.hvec[(size_t)obj[f] * 2 + i];
-                for (int M = 0; M < NF; ++M)
-                    for (int i = 0; i < 2; ++i) fe[2 * M + i] += rho * c * T.phi[q][M] * hq[i];
-            }
-        }
-        if (A.fnodal) {
-            double f[2] = {0.0, 0.0};
-            for (int i = 0; i < NG; ++i)
-                for (int d = 0; d < 2; ++d) f[d] += T.N[q][i] * A.fnodal[(size_t)nodes[i] * 2 + d];
-            for (int M = 0; M < NF; ++M)
-                for (int d = 0; d < 2; ++d) fe[2 * M + d] += f[d] * T.phi[q][M] * c;
-        }
-    }
-    if (bad) flag_or(A.flags, 1);
-    if (nan) flag_or(A.flags, 2);
-    for (int a = 0; a < NLOC; ++a) A.stageF[(size_t)a * E + e] = fe[a];
-}
-
-template <int FDEG, int NQ, typename R, bool TI>
-__global__ void __launch_bounds__(128) k_hyper_quad(const ElemArgs A, const Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ> T) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < A.nelem) hyper_quad_element<FDEG, NQ, R, TI>(A, T, e);
-}
 
 // ---------------------------------------------------------------------------
 // Linear elasticity (HyperElastic<StVenant> at u = 0) on affine hexahedra,
@@ -1090,7 +803,7 @@ __global__ void k_lift(int nlift, const int32_t* lift_elem, int nelem, int nfun,
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nlift) return;
     const int e = lift_elem[k];
-    const int nloc = nfun * ncomp;
+    const int nloc = nfun * ncomp;  // <= 30, checked by the host
     if (nloc > 30) return;
     double g[30];
     bool act[30];
@@ -1337,21 +1050,6 @@ int pattern_build(isl_ctx* c) {
 }
 
 // ---------------------------------------------------------------------------
-template <int SHAPE, int FDEG, int NQ>
-static void fill_tab(Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ>& T, const HostTab& h) {
-    constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
-    for (int q = 0; q < NQ; ++q) {
-        T.w[q] = h.w[q];
-        for (int f = 0; f < NF; ++f) {
-            T.phi[q][f] = h.phi[q * NF + f];
-            for (int d = 0; d < D; ++d) T.dphi[q][f][d] = h.dphi[(q * NF + f) * D + d];
-        }
-        for (int i = 0; i < NG; ++i) {
-            T.N[q][i] = h.N[q * NG + i];
-            for (int d = 0; d < D; ++d) T.dN[q][i][d] = h.dN[(q * NG + i) * D + d];
-        }
-    }
-}
 
 template <int SHAPE, int FDEG, int NQ, typename R>
 static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
@@ -1411,37 +1109,12 @@ static int dispatch_heat_static(isl_ctx* c, ElemArgs A, int with_residual) {
     ISL_FAIL(c, ISL_ERR_ARG, "heat::Static: unsupported element / quadrature combination");
 }
 
-template <int FDEG, int NQ, typename R>
-static int launch_hyper_quad(isl_ctx* c, const ElemArgs& A, const HostTab& h) {
-    Tab<2, 4, ET<ISL_QUAD, FDEG>::NF, NQ> T;
-    fill_tab<ISL_QUAD, FDEG, NQ>(T, h);
-    if (A.rho || A.nfw > 0)
-        k_hyper_quad<FDEG, NQ, R, true><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
-    else
-        k_hyper_quad<FDEG, NQ, R, false><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
-    ISL_CHECK_CUDA(c, cudaGetLastError());
-    c->launches += 1;
-    return ISL_OK;
-}
-
-template <typename R>
-static int dispatch_hyper_quad(isl_ctx* c, const ElemArgs& A) {
-    HostTab h;
-    if (!make_host_tables(ISL_QUAD, c->fedeg, c->qdeg, h)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
-    if (c->fedeg == 1 && h.nq == 4) return launch_hyper_quad<1, 4, R>(c, A, h);
-    if (c->fedeg == 1 && h.nq == 9) return launch_hyper_quad<1, 9, R>(c, A, h);
-    if (c->fedeg == 2 && h.nq == 4) return launch_hyper_quad<2, 4, R>(c, A, h);
-    if (c->fedeg == 2 && h.nq == 9) return launch_hyper_quad<2, 9, R>(c, A, h);
-    ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic on quadrilaterals: Q1 or Q2 with 2x2 or 3x3 quadrature");
-}
-
 template <typename R>
 static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
-    if (c->shape == ISL_QUAD) return dispatch_hyper_quad<R>(c, A);
-    if (!(c->shape == ISL_HEX && c->fedeg == 1))
-        ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: quadrilaterals (Q1, Q2) and trilinear hexahedra on the device");
+    if (!(c->shape == ISL_HEX && c->fedeg == 1)) return hyper_generic(c, A, sizeof(R) == 4);
     HostTab h;
-    if (!make_host_tables(ISL_HEX, 1, c->qdeg, h) || h.nq != 8) ISL_FAIL(c, ISL_ERR_ARG, "HyperElastic: 2x2x2 quadrature required");
+    if (!make_host_tables(ISL_HEX, 1, c->qdeg, h)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
+    if (h.nq != 8) return hyper_generic(c, A, sizeof(R) == 4);  // the fast path is written for 2x2x2
     Tab<3, 8, 8, 8> T;
     fill_tab<ISL_HEX, 1, 8>(T, h);
     if (c->mesh_affine < 0) c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
@@ -1564,6 +1237,9 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.hstride = c->ndofobj * c->ncomp;
     A.nfw = c->nforce_w;
     for (int k = 0; k < 4; ++k) A.fw[k] = k < c->nforce_w ? c->force_w[k] : 0.0;
+    // k_lift holds one element's constraint values in fixed arrays of 30
+    if (c->n_lift > 0 && c->nloc > 30)
+        ISL_FAIL(c, ISL_ERR_ARG, "Dirichlet values on elements with more than 30 local DOFs are not supported");
     // the weights may not reach past the stored history (isl_set_history can
     // shrink it after the weights were set)
     if (c->nforce_w > c->nhist || (c->inertia && c->nhist_w > c->nhist + 1))
