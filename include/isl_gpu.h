@@ -124,8 +124,8 @@ int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
  *   solid::HyperElastic<StVenant|NeoHookeanCompressible>
  *     (solid/HyperElastic.hpp:110-257, mat/hypel/StVenant.hpp:77-114,
  *      mat/hypel/NeoHookeanCompressible.hpp:77-172); on the device for
- *     trilinear hexahedra and for Q1 / Q2 quadrilaterals (plane strain,
- *     solid/Deformation.hpp:25-46)
+ *     trilinear hexahedra (2x2x2 or 3x3x3 points), P1 / P2 tetrahedra and
+ *     Q1 / Q2 quadrilaterals (plane strain, solid/Deformation.hpp:25-46)
  * quad_degree: base::Quadrature<DEG,SHAPE> degree (base/Quadrature.hpp:113-143). */
 int isl_set_laplace(isl_ctx* ctx, const double* kappa /* [n_elem] */, int quad_degree);
 int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const double* mu, int quad_degree);
@@ -150,8 +150,8 @@ int isl_set_heat_static(isl_ctx* ctx, int material, const double* param /* [n_el
  * x^(s), x^(0) the current values, x^(s) the values s steps back.  For a
  * MultiStep method at time step k: lhs_weight = systemMassWeight(k) / dt and
  * weights[s] = -reactionWeights(k)[s] / dt (incremental; weights[0] = 0
- * otherwise).  Laplace, heat::Static and HyperElastic (trilinear
- * hexahedra, Q1 / Q2 quadrilaterals), where the mass acts on each displacement component
+ * otherwise).  Laplace, heat::Static and HyperElastic (every element it
+ * runs on), where the mass acts on each displacement component
  * (Mass.hpp:84-86); density NULL turns the terms off. */
 int isl_set_history(isl_ctx* ctx, int nhist);
 int isl_push_history(isl_ctx* ctx);
@@ -163,8 +163,8 @@ int isl_set_inertia(isl_ctx* ctx, const double* density /* [n_elem] */, double l
  * -sum_s weights[s-1] F(x^(s)) to the right-hand side, F the kernel's internal
  * force (residualForceHistory<s>) at the values s steps back, s = 1..nweights
  * (<= the stored history, <= 4).  For a MultiStep method at step k: weights =
- * forceWeights(k).  Laplace, heat::Static and HyperElastic (trilinear
- * hexahedra, Q1 / Q2 quadrilaterals); nweights 0 turns it off. */
+ * forceWeights(k).  Laplace, heat::Static and HyperElastic (every element
+ * it runs on); nweights 0 turns it off. */
 int isl_set_force_history(isl_ctx* ctx, int nweights, const double* weights);
 /* Body force interpolated from nodal values by the geometry functions
  * (base/asmb/BodyForce.hpp:172-205 with EvaluateViaElement); NULL clears it. */
