@@ -13,8 +13,11 @@
 // reference/06-elastic/compRefOut{D,N}.dat, reference/05-mixedPoisson/ref,
 // reference/04-heat/nonlinearHeat.ref.dat); the pins are checked by
 // tests/test_oracle_golden.py.  The inertia terms of time integration
-// (ReactionTerms) have no golden output in the reference; they are restated
-// from base/time/ReactionTerms.hpp and base/kernel/Mass.hpp only.
+// (ReactionTerms, for scalar and vector fields) and the residual-force
+// history have no golden output in the reference; they are restated from
+// base/time/ReactionTerms.hpp, base/time/ResidualForceHistory.hpp and
+// base/kernel/Mass.hpp only (parity unpinned for those terms; the vector
+// mass is checked against the scalar one by tests/test_oracle_inertia.py).
 //
 // Every block cites the reference file:line whose algorithm it restates.
 // Third-party arithmetic the reference delegates to Eigen 3.2.0 (small dense
