@@ -2,8 +2,8 @@
 insilico_gb300/csrc/isl_hyper.cu, __host__ __device__) compiled for the host
 and run on the oracle's inputs (CPU, no GPU): the element matrices and
 vectors it stages, assembled with the oracle's equation numbers, equal the
-oracle's system.  This checks the kernel's arithmetic every round on the
-CPU; the GPU tests check the same kernel on the device
+oracle's system.  This checks the kernel's arithmetic in every CPU test
+run; the GPU tests check the same kernel on the device
 (test_gpu_elastic2d.py, test_gpu_hyper_shapes.py)."""
 import os
 import subprocess
