@@ -118,6 +118,16 @@ int isl_dof_index(isl_ctx* ctx, int64_t* out /* [n_dofobj*ncomp] */);
  * TripletContainer::registerFields (base/solver/TripletContainer.hpp:158-301). */
 int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
 
+/* The quadrature rule the element kernels use for a shape and polynomial
+ * degree (base::Quadrature<DEG,SHAPE>, base/Quadrature.hpp:28-80: tensor
+ * Gauss-Legendre on [0,1] for quadrilaterals and hexahedra,
+ * base/quad/GaussLegendre.hpp:115-134; the tetrahedron rules of degree 1 to 5,
+ * base/quad/GaussTetrahedron.hpp:93-175), for callers that tabulate their
+ * functors at the quadrature points.  Weights [n], reference points [n][dim];
+ * NULL arrays give the count.  Host only, no context.  ISL_ERR_ARG for a
+ * shape or degree without a rule. */
+int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi);
+
 /* Kernel functor tabulation (per element coefficients; the reference's
  * ConductivityFun / Material objects are evaluated per element by the caller):
  *   heat::Laplace (heat/Laplace.hpp:113-126, base/kernel/Laplace.hpp:100-151)

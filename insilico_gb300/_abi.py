@@ -36,7 +36,7 @@ EXPORTED = [
     "isl_ctx_create", "isl_ctx_destroy", "isl_last_error", "isl_mesh_upload", "isl_field_create",
     "isl_field_elem_dofobj", "isl_boundary_faces", "isl_boundary_points", "isl_constrain",
     "isl_scale_constraints", "isl_number_dofs", "isl_dof_index", "isl_register_pattern", "isl_set_laplace",
-    "isl_set_hyperelastic", "isl_set_body_force_nodal", "isl_set_neumann", "isl_set_neumann_vertex", "isl_set_values", "isl_get_values",
+    "isl_set_hyperelastic", "isl_set_body_force_nodal", "isl_set_neumann", "isl_set_neumann_vertex", "isl_quadrature_rule", "isl_set_values", "isl_get_values",
     "isl_assemble", "isl_solve", "isl_get_solution", "isl_get_rhs", "isl_norm", "isl_distribute", "isl_get_csr",
     "isl_sync", "isl_set_timing", "isl_timings", "isl_time_spmv", "isl_mark", "isl_elapsed", "isl_launch_count",
     "isl_set_option", "isl_get_option", "isl_device_memory", "isl_batch_mesh_upload", "isl_batch_info",
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = False):
     L.isl_set_body_force_nodal.argtypes = [_P, _D]
     L.isl_set_neumann.argtypes = [_P, C.c_int64, _I64, _I32, _D, i]
     L.isl_set_neumann_vertex.argtypes = [_P, C.c_int64, _I64, _I32, _D, i]
+    L.isl_quadrature_rule.argtypes = [i, i, C.POINTER(C.c_int), _D, _D]
     L.isl_set_values.argtypes = [_P, _D]
     L.isl_get_values.argtypes = [_P, _D]
     L.isl_assemble.argtypes = [_P, i, i, i]
@@ -150,3 +151,19 @@ def i64(a):
 
 def i32(a):
     return a.ctypes.data_as(_I32)
+
+
+def quadrature_rule(shape: int, degree: int):
+    """(weights [n], reference points [n, dim]) of the rule the element
+    kernels use for a shape and polynomial degree (isl_quadrature_rule)."""
+    import numpy as np
+    L = load()
+    n = C.c_int()
+    st = L.isl_quadrature_rule(shape, degree, C.byref(n), None, None)
+    if st != ISL_OK:
+        raise IslError(st, f"isl_quadrature_rule: no rule for shape {shape}, degree {degree}")
+    dim = 2 if shape == QUAD else 3
+    w = np.zeros(n.value)
+    x = np.zeros(n.value * dim)
+    L.isl_quadrature_rule(shape, degree, C.byref(n), d(w), d(x))
+    return w, x.reshape(n.value, dim)

@@ -1077,6 +1077,8 @@ static int dispatch_laplace(isl_ctx* c, const ElemArgs& A) {
     if (c->shape == ISL_QUAD && c->fedeg == 2 && nq == 4) return launch_laplace<ISL_QUAD, 2, 4, R>(c, A);
     if (c->shape == ISL_HEX && c->fedeg == 1 && nq == 8) return launch_laplace<ISL_HEX, 1, 8, R>(c, A);
     if (c->shape == ISL_TET && c->fedeg == 2 && nq == 4) return launch_laplace<ISL_TET, 2, 4, R>(c, A);
+    // 11 points: Quadrature<4,TET>, the drivers' 2 x fieldDeg for P2
+    if (c->shape == ISL_TET && c->fedeg == 2 && nq == 11) return launch_laplace<ISL_TET, 2, 11, R>(c, A);
     if (c->shape == ISL_TET && c->fedeg == 1 && nq == 1) return launch_laplace<ISL_TET, 1, 1, R>(c, A);
     if (c->shape == ISL_TET && c->fedeg == 1 && nq == 4) return launch_laplace<ISL_TET, 1, 4, R>(c, A);
     ISL_FAIL(c, ISL_ERR_ARG, "Laplace: unsupported element / quadrature combination");
@@ -1106,6 +1108,7 @@ static int dispatch_heat_static(isl_ctx* c, ElemArgs A, int with_residual) {
     if (c->shape == ISL_HEX && c->fedeg == 1 && nq == 8) return launch_heat_static<ISL_HEX, 1, 8>(c, A);
     if (c->shape == ISL_TET && c->fedeg == 1 && nq == 1) return launch_heat_static<ISL_TET, 1, 1>(c, A);
     if (c->shape == ISL_TET && c->fedeg == 2 && nq == 4) return launch_heat_static<ISL_TET, 2, 4>(c, A);
+    if (c->shape == ISL_TET && c->fedeg == 2 && nq == 11) return launch_heat_static<ISL_TET, 2, 11>(c, A);
     ISL_FAIL(c, ISL_ERR_ARG, "heat::Static: unsupported element / quadrature combination");
 }
 

@@ -125,18 +125,48 @@ void element_eval(int shape, int k, const double* xi, std::vector<double>& v, st
 // Quadrature: Gauss-Legendre on [0,1] with the reference's 15-digit constants
 // (base/quad/GaussLegendre.hpp:115-134), tensor products with the first
 // coordinate fastest (base/quad/TensorProduct.hpp:123-178), and the
-// tetrahedron rules of base/quad/GaussTetrahedron.hpp:90-111.
+// tetrahedron rules of degree 1 to 5 of base/quad/GaussTetrahedron.hpp.
 bool quadrature(int shape, int qdeg, std::vector<double>& w, std::vector<double>& x) {
     w.clear(); x.clear();
     if (shape == ISL_TET) {
-        if (qdeg <= 1) { w = {0.166666666666666}; x = {0.25, 0.25, 0.25}; return true; }
-        if (qdeg == 2) {
-            const double a = 0.13819660112501051518, b = 0.58541019662496845446, c = 0.04166666666666666667;
-            w = {c, c, c, c};
-            x = {a, a, a, b, a, a, a, b, a, a, a, b};
-            return true;
+        // Keast rules with the reference's truncated constants and point
+        // order (base/quad/GaussTetrahedron.hpp:93-175): both decide the last
+        // digits of every integral.  Orbits: 'c' the centroid; '4' three
+        // coordinates a and one b, in the order (a,a,a) (b,a,a) (a,b,a)
+        // (a,a,b); '6' the order (b,b,a) (b,a,a) (a,b,a) (a,a,b) (b,a,b) (a,b,b).
+        struct Orbit { char type; double w, a, b; };
+        static const Orbit d1[] = {{'c', 0.166666666666666, 0.25, 0.25}};
+        static const Orbit d2[] = {{'4', 0.04166666666666666667, 0.13819660112501051518, 0.58541019662496845446}};
+        static const Orbit d3[] = {{'c', -0.13333333333333333, 0.25, 0.25}, {'4', 0.075, 0.1666666666666667, 0.5}};
+        static const Orbit d4[] = {{'c', -0.01315555555555555556, 0.25, 0.25},
+                                   {'4', 0.0076222222222222, 0.071428571428571, 0.785714285714286},
+                                   {'6', 0.024888888888889, 0.100596423833201, 0.399403576166799}};
+        static const Orbit d5[] = {{'c', 0.030283678097089, 0.25, 0.25},
+                                   {'4', 0.006026785714286, 0.333333333333333, 0.0},
+                                   {'4', 0.011645249086029, 0.090909090909091, 0.727272727272727},
+                                   {'6', 0.010949141561386, 0.066550153573664, 0.433449846426336}};
+        const Orbit* rule;
+        int norb;
+        switch (qdeg <= 1 ? 1 : qdeg) {
+            case 1: rule = d1; norb = 1; break;
+            case 2: rule = d2; norb = 1; break;
+            case 3: rule = d3; norb = 2; break;
+            case 4: rule = d4; norb = 3; break;
+            case 5: rule = d5; norb = 4; break;
+            default: return false;
         }
-        return false;
+        for (int o = 0; o < norb; ++o) {
+            const double a = rule[o].a, b = rule[o].b;
+            const double c4[4][3] = {{a, a, a}, {b, a, a}, {a, b, a}, {a, a, b}};
+            const double c6[6][3] = {{b, b, a}, {b, a, a}, {a, b, a}, {a, a, b}, {b, a, b}, {a, b, b}};
+            const int np = rule[o].type == 'c' ? 1 : rule[o].type == '4' ? 4 : 6;
+            for (int k = 0; k < np; ++k) {
+                const double* pt = rule[o].type == 'c' ? nullptr : rule[o].type == '4' ? c4[k] : c6[k];
+                w.push_back(rule[o].w);
+                for (int d = 0; d < 3; ++d) x.push_back(pt ? pt[d] : 0.25);
+            }
+        }
+        return true;
     }
     std::vector<double> w1, x1;
     switch ((qdeg + 2) / 2) {
@@ -1269,6 +1299,18 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_SCALAR_SLOTS) { *value = c->ss_nslot; return ISL_OK; }
     ISL_FAIL(c, ISL_ERR_ARG, "unknown option");
     ISL_CATCH(c)
+}
+
+int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi) {
+    ISL_TRY
+    if (!n || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
+    std::vector<double> ww, xx;
+    if (!quadrature(shape, degree, ww, xx)) return ISL_ERR_ARG;
+    *n = (int)ww.size();
+    if (w) std::copy(ww.begin(), ww.end(), w);
+    if (xi) std::copy(xx.begin(), xx.end(), xi);
+    return ISL_OK;
+    ISL_CATCH(nullptr)
 }
 
 int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {

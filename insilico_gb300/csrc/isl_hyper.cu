@@ -196,9 +196,10 @@ int dispatch(isl_ctx* c, const ElemArgs& A) {
     if (s == ISL_TET && k == 1 && nq == 4) return launch<ISL_TET, 1, 4, R>(c, A, h);
     if (s == ISL_TET && k == 2 && nq == 1) return launch<ISL_TET, 2, 1, R>(c, A, h);
     if (s == ISL_TET && k == 2 && nq == 4) return launch<ISL_TET, 2, 4, R>(c, A, h);
+    if (s == ISL_TET && k == 2 && nq == 11) return launch<ISL_TET, 2, 11, R>(c, A, h);
     if (s == ISL_HEX && k == 1 && nq == 27) return launch<ISL_HEX, 1, 27, R>(c, A, h);
     ISL_FAIL(c, ISL_ERR_ARG,
-             "HyperElastic: Q1 / Q2 quadrilaterals (2x2, 3x3), P1 / P2 tetrahedra (1, 4 points) or "
+             "HyperElastic: Q1 / Q2 quadrilaterals (2x2, 3x3), P1 / P2 tetrahedra (1, 4 points; 11 for P2) or "
              "trilinear hexahedra (2x2x2, 3x3x3) on the device");
 }
 

@@ -210,7 +210,7 @@ int dispatch(isl_ctx* c, const HostTab& h, double* dxq, int order, const double*
     ISL_POST_CASE(ISL_QUAD, 2, 1) ISL_POST_CASE(ISL_QUAD, 2, 4) ISL_POST_CASE(ISL_QUAD, 2, 9)
     ISL_POST_CASE(ISL_HEX, 1, 1) ISL_POST_CASE(ISL_HEX, 1, 8) ISL_POST_CASE(ISL_HEX, 1, 27)
     ISL_POST_CASE(ISL_TET, 1, 1) ISL_POST_CASE(ISL_TET, 1, 4) ISL_POST_CASE(ISL_TET, 2, 1)
-    ISL_POST_CASE(ISL_TET, 2, 4)
+    ISL_POST_CASE(ISL_TET, 2, 4) ISL_POST_CASE(ISL_TET, 2, 11)
 #undef ISL_POST_CASE
     ISL_FAIL(c, ISL_ERR_ARG, "post-processing: unsupported element / quadrature combination");
 }

@@ -70,6 +70,8 @@ def lib():
         L.orc_set_hyperelastic.argtypes = [_P, C.c_int, _D, _D, C.c_int]
         L.orc_set_heat_static.argtypes = [_P, C.c_int, _D, C.c_int]
         L.orc_set_inertia.argtypes = [_P, _D, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, _D]
+        L.orc_quadrature.argtypes = [C.c_int, C.c_int, _D, _D]
+        L.orc_quadrature.restype = C.c_int
         L.orc_set_body_nodal.argtypes = [_P, _D]
         L.orc_set_body_cosproduct.argtypes = [_P, _D]
         L.orc_set_neumann.argtypes = [_P, C.c_int, C.c_int64, _I64, _I32, _D, C.c_double, C.c_int]
@@ -273,6 +275,20 @@ class Problem:
     def error_norm(self, kind, params, order, qdeg):
         p = np.ascontiguousarray(params, dtype=np.float64)
         return self.L.orc_error_norm(self.h, kind, _d(p), order, qdeg)
+
+
+def quadrature(shape: int, degree: int):
+    """(weights [n], points [n, dim]) of the oracle's rule for a shape
+    (LINE/TRI/QUAD/TET/HEX) and polynomial degree; None without such a rule."""
+    L = lib()
+    n = L.orc_quadrature(shape, degree, None, None)
+    if n < 0:
+        return None
+    dim = {LINE: 1, TRI: 2, QUAD: 2, TET: 3, HEX: 3}[shape]
+    w = np.zeros(n)
+    x = np.zeros(n * dim)
+    L.orc_quadrature(shape, degree, _d(w), _d(x))
+    return w, x.reshape(n, dim)
 
 
 def cg(rowptr, colind, val, b, tol=2.220446049250313e-16, max_iter=None, nthreads=1):

@@ -293,13 +293,41 @@ static QuadRule makeQuadrature(int shape, int degree) {
         return q;
     }
     if (shape == TET) {
-        if (degree <= 1) {
-            q.w = {0.166666666666666}; q.x = {0.25, 0.25, 0.25};
-        } else if (degree == 2) {
-            const double a = 0.13819660112501051518, b = 0.58541019662496845446, w = 0.04166666666666666667;
-            q.w = {w, w, w, w};
-            q.x = {a, a, a, b, a, a, a, b, a, a, a, b};
-        } else throw std::runtime_error("tet quadrature degree");
+        // base/quad/GaussTetrahedron.hpp:93-175 (Keast rules with the
+        // reference's truncated constants, in its point order).  A group is
+        // (weight, x, y, kind): kind 0 the centroid; kind 1 the four points
+        // (x,x,x) (y,x,x) (x,y,x) (x,x,y); kind 2 the six points (y,y,x)
+        // (y,x,x) (x,y,x) (x,x,y) (y,x,y) (x,y,y).
+        struct G { double w, x, y; int kind; };
+        static const G r1[] = {{0.166666666666666, 0.25, 0.25, 0}};
+        static const G r2[] = {{0.04166666666666666667, 0.13819660112501051518, 0.58541019662496845446, 1}};
+        static const G r3[] = {{-0.13333333333333333, 0.25, 0.25, 0}, {0.075, 0.1666666666666667, 0.5, 1}};
+        static const G r4[] = {{-0.01315555555555555556, 0.25, 0.25, 0},
+                               {0.0076222222222222, 0.071428571428571, 0.785714285714286, 1},
+                               {0.024888888888889, 0.100596423833201, 0.399403576166799, 2}};
+        static const G r5[] = {{0.030283678097089, 0.25, 0.25, 0}, {0.006026785714286, 0.333333333333333, 0.0, 1},
+                               {0.011645249086029, 0.090909090909091, 0.727272727272727, 1},
+                               {0.010949141561386, 0.066550153573664, 0.433449846426336, 2}};
+        const G* gs = nullptr;
+        int ng = 0;
+        if (degree <= 1) { gs = r1; ng = 1; }
+        else if (degree == 2) { gs = r2; ng = 1; }
+        else if (degree == 3) { gs = r3; ng = 2; }
+        else if (degree == 4) { gs = r4; ng = 3; }
+        else if (degree == 5) { gs = r5; ng = 4; }
+        else throw std::runtime_error("tet quadrature degree");
+        for (int k = 0; k < ng; ++k) {
+            const G& g = gs[k];
+            const double x = g.x, y = g.y;
+            std::vector<std::array<double, 3>> pts;
+            if (g.kind == 0) pts = {{0.25, 0.25, 0.25}};
+            else if (g.kind == 1) pts = {{x, x, x}, {y, x, x}, {x, y, x}, {x, x, y}};
+            else pts = {{y, y, x}, {y, x, x}, {x, y, x}, {x, x, y}, {y, x, y}, {x, y, y}};
+            for (const auto& pt : pts) {
+                q.w.push_back(g.w);
+                q.x.insert(q.x.end(), pt.begin(), pt.end());
+            }
+        }
         return q;
     }
     if (shape == TRI) {  // 1-point centroid rule, enough for constant tractions on P1 faces
@@ -1002,6 +1030,19 @@ void orc_set_inertia(void* h, const double* rho, double massW, int nw, const dou
     P->forceW.assign(fw, fw + nfw);
     const size_t ndc = (size_t)P->ndofobj * P->ncomp;
     P->hist.assign(hist, hist + ndc * nhist);
+}
+// The quadrature rule of a shape and degree (points in reference
+// coordinates, [n][dim]); returns n, or -1 without such a rule.  Call with
+// null arrays for the count.
+int orc_quadrature(int shape, int degree, double* w, double* x) {
+    try {
+        const QuadRule q = makeQuadrature(shape, degree);
+        if (w) std::copy(q.w.begin(), q.w.end(), w);
+        if (x) std::copy(q.x.begin(), q.x.end(), x);
+        return q.n();
+    } catch (const std::exception&) {
+        return -1;
+    }
 }
 void orc_set_heat_static(void* h, int mat, const double* param, int qdeg) {
     Problem* P = (Problem*)h;

@@ -62,7 +62,7 @@ int main(int argc, char** argv) {
     const bool ti = inertia || nfw > 0;
 #define RUN(S, D, Q) if (shape == S && deg == D && nq == Q) { if (ti) run<S, D, Q, true>(E, nn, nobj, mat, qdeg, body, inertia, massw, nfw, fw, nhist); else run<S, D, Q, false>(E, nn, nobj, mat, qdeg, body, inertia, massw, nfw, fw, nhist); return 0; }
     RUN(ISL_QUAD, 1, 4) RUN(ISL_QUAD, 1, 9) RUN(ISL_QUAD, 2, 4) RUN(ISL_QUAD, 2, 9)
-    RUN(ISL_TET, 1, 1) RUN(ISL_TET, 1, 4) RUN(ISL_TET, 2, 1) RUN(ISL_TET, 2, 4) RUN(ISL_HEX, 1, 27)
+    RUN(ISL_TET, 1, 1) RUN(ISL_TET, 1, 4) RUN(ISL_TET, 2, 1) RUN(ISL_TET, 2, 4) RUN(ISL_TET, 2, 11) RUN(ISL_HEX, 1, 27)
     fprintf(stderr, "combo\n");
     return 1;
 }

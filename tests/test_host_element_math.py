@@ -50,6 +50,7 @@ def _unpack(v, n):
     ("tet", (2, 2, 1), 1, 2, 4, "stvenant", True, False, 0),
     ("tet", (2, 1, 1), 2, 2, 4, "neohooke", True, True, 2),
     ("tet", (2, 1, 1), 2, 1, 1, "stvenant", False, False, 0),
+    ("tet", (2, 1, 1), 2, 4, 11, "neohooke", True, True, 2),
     ("hex", (2, 1, 1), 1, 4, 27, "neohooke", True, True, 1),
 ])
 def test_hyper_element_matches_oracle(harness, tmp_path, kind, sizes, deg, qdeg, nq, material, body, inertia, nfw):
