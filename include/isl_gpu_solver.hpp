@@ -41,6 +41,22 @@ struct gpu_error : std::runtime_error {
     gpu_error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// base::Quadrature<DEG,SHAPE> as the element kernels use it: weights and
+// reference points ([n][dim]), for tabulating functors at the points
+struct QuadratureRule {
+    std::vector<double> w, xi;
+};
+inline QuadratureRule quadratureRule(int shape, int degree) {
+    int n = 0;
+    if (isl_quadrature_rule(shape, degree, &n, nullptr, nullptr) != ISL_OK)
+        throw std::runtime_error("isl_quadrature_rule: no rule for this shape and degree");
+    QuadratureRule r;
+    r.w.resize(n);
+    r.xi.resize((size_t)n * (shape == ISL_QUAD ? 2 : 3));
+    isl_quadrature_rule(shape, degree, &n, r.w.data(), r.xi.data());
+    return r;
+}
+
 inline void check(isl_ctx* ctx, int st, const char* what) {
     if (st != ISL_OK) throw gpu_error(st, std::string(what) + ": " + isl_last_error(ctx));
 }

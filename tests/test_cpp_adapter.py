@@ -28,6 +28,10 @@ int main(int argc, char** argv) {
     const long long n = (long long)s.numberDoFs();
     std::printf("%lld %lld\n", ndofobj, n);
     try { s.registerFields(); } catch (const isl::gpu_error& e) { std::printf("device-only %d\n", e.code); }
+    const isl::QuadratureRule q = isl::quadratureRule(ISL_TET, 4);
+    double sum = 0.0;
+    for (double w : q.w) sum += w;
+    std::printf("%zu %.17g\n", q.w.size(), sum);
     return 0;
 }
 """
@@ -51,6 +55,9 @@ def test_cpp_adapter_builds_and_runs_host_steps(tmp_path):
                          capture_output=True, text=True).stdout.split("\n")
     ndofobj, n = (int(t) for t in out[0].split())
     assert out[1].startswith("device-only")
+    nq, wsum = out[2].split()
+    w, _ = A.quadrature_rule(A.TET, 4)
+    assert int(nq) == 11 and float(wsum) == pytest.approx(w.sum(), rel=1e-15)
     assert (tmp_path / "out.smf").read_text() == (tmp_path / "in.smf").read_text()
     # the same steps through the Python binding
     S.create_field(2, 1)
