@@ -1303,7 +1303,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
 
 int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi) {
     ISL_TRY
-    if (!n || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
+    if (!n || degree < 0 || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
     std::vector<double> ww, xx;
     if (!quadrature(shape, degree, ww, xx)) return ISL_ERR_ARG;
     *n = (int)ww.size();
