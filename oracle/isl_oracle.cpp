@@ -330,8 +330,46 @@ static QuadRule makeQuadrature(int shape, int degree) {
         }
         return q;
     }
-    if (shape == TRI) {  // 1-point centroid rule, enough for constant tractions on P1 faces
-        q.w = {0.5}; q.x = {1.0 / 3.0, 1.0 / 3.0};
+    if (shape == TRI) {
+        // base/quad/GaussTriangle.hpp:97-180, degrees 1-5 (Strang-Fix / Dunavant
+        // rules with the reference's truncated constants and point order):
+        // rows of (weight, x, y)
+        static const double t1[][3] = {{0.5, 0.333333333333333, 0.333333333333333}};
+        static const double t2[][3] = {{0.166666666666666, 0.666666666666667, 0.166666666666667},
+                                       {0.166666666666666, 0.166666666666667, 0.666666666666667},
+                                       {0.166666666666666, 0.166666666666667, 0.166666666666667}};
+        static const double t3[][3] = {{-0.28125, 0.333333333333333, 0.333333333333333},
+                                       {0.260416666666667, 0.6, 0.2},
+                                       {0.260416666666667, 0.2, 0.6},
+                                       {0.260416666666667, 0.2, 0.2}};
+        static const double t4[][3] = {{0.111690794839005, 0.10810301816807, 0.445948490915965},
+                                       {0.054975871827661, 0.816847572980459, 0.091576213509771},
+                                       {0.111690794839005, 0.445948490915965, 0.10810301816807},
+                                       {0.111690794839005, 0.445948490915965, 0.445948490915965},
+                                       {0.054975871827661, 0.091576213509771, 0.816847572980459},
+                                       {0.054975871827661, 0.091576213509771, 0.091576213509771}};
+        static const double t5[][3] = {{0.1125, 0.333333333333333, 0.333333333333333},
+                                       {0.066197076394253, 0.05971587178977, 0.470142064105115},
+                                       {0.0629695902724135, 0.797426985353087, 0.101286507323456},
+                                       {0.066197076394253, 0.470142064105115, 0.05971587178977},
+                                       {0.066197076394253, 0.470142064105115, 0.470142064105115},
+                                       {0.0629695902724135, 0.101286507323456, 0.797426985353087},
+                                       {0.0629695902724135, 0.101286507323456, 0.101286507323456}};
+        const double(*rows)[3] = nullptr;
+        int nr = 0;
+        switch (degree <= 1 ? 1 : degree) {
+            case 1: rows = t1; nr = 1; break;
+            case 2: rows = t2; nr = 3; break;
+            case 3: rows = t3; nr = 4; break;
+            case 4: rows = t4; nr = 6; break;
+            case 5: rows = t5; nr = 7; break;
+            default: throw std::runtime_error("triangle quadrature degree");
+        }
+        for (int k = 0; k < nr; ++k) {
+            q.w.push_back(rows[k][0]);
+            q.x.push_back(rows[k][1]);
+            q.x.push_back(rows[k][2]);
+        }
         return q;
     }
     if (shape == POINT) { q.w = {1.0}; q.x = {}; return q; }

@@ -42,3 +42,17 @@ def test_tet_rule_sizes_and_limits():
         with pytest.raises(A.IslError):
             A.quadrature_rule(A.TET, bad)
     assert O.quadrature(O.TET, 6) is None
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5])
+def test_oracle_triangle_rules_are_exact(degree):
+    """the oracle's surface rules on triangles (base/quad/GaussTriangle.hpp,
+    degrees 1-5, truncated constants): 1, 3, 4, 6, 7 points, exact for
+    monomials up to their degree"""
+    w, x = O.quadrature(O.TRI, degree)
+    assert len(w) == [1, 3, 4, 6, 7][degree - 1]
+    for a in range(degree + 1):
+        for b in range(degree + 1 - a):
+            exact = factorial(a) * factorial(b) / factorial(a + b + 2)
+            got = np.sum(w * x[:, 0] ** a * x[:, 1] ** b)
+            assert abs(got - exact) <= 5e-14 * max(exact, 1e-3) + 2e-15, (a, b, got, exact)
