@@ -6,7 +6,6 @@ import os
 import shutil
 import subprocess
 
-import numpy as np
 import pytest
 
 from insilico_gb300 import _abi as A

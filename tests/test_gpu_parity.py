@@ -16,7 +16,7 @@ import oracle as O
 from insilico_gb300 import _abi as A
 from insilico_gb300 import workloads as W
 
-from helpers import csr_entry_err, oracle_problem, rel_entry_err
+from helpers import csr_entry_err, oracle_problem
 
 pytestmark = pytest.mark.gpu
 
