@@ -124,8 +124,11 @@ int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
  * base/quad/GaussLegendre.hpp:115-134; the tetrahedron rules of degree 1 to 5,
  * base/quad/GaussTetrahedron.hpp:93-175), for callers that tabulate their
  * functors at the quadrature points.  Weights [n], reference points [n][dim];
- * NULL arrays give the count.  Host only, no context.  ISL_ERR_ARG for a
- * shape or degree without a rule. */
+ * NULL arrays give the count.  Host only, no context.  Rules exist for
+ * degrees 1 to 5: Gauss-Legendre with 1, 2 or 3 points per direction
+ * ((degree + 2) / 2, base/quad/GaussLegendre.hpp:33-37) on quadrilaterals and
+ * hexahedra, and 1, 4, 5, 11 or 15 points on tetrahedra; ISL_ERR_ARG for
+ * degree 0, degrees above 5 and other shapes. */
 int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi);
 
 /* Kernel functor tabulation (per element coefficients; the reference's
@@ -356,8 +359,11 @@ int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
  * (max_iter <= 0 means 2n).  Every pointer is a caller-owned device pointer on
  * `device`: the n x n CSR matrix (rowptr[n+1], colind[nnz], val[nnz]), b[n]
  * and the output x[n].  `stream` is a cudaStream_t (NULL: the default
- * stream); the call returns once the solve has finished.  iters/rel_res may
- * be NULL.
+ * stream).  The call reads the CG scalars back to the host and waits on
+ * `stream` after every round of 32 iterations, and returns once the solve has
+ * finished.  iters/rel_res may be NULL; on every status after the solve has
+ * started they hold the iterations and relative residual of the last scalar
+ * record read back.
  *
  * The work vectors live in one scratch array compiled into the library's
  * device code: ISL_NOALLOC_MAX_N entries for each of its four vectors plus
@@ -367,8 +373,9 @@ int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
  * other allocating call.
  *
  * The first call on a device looks the scratch array up on that device
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture.  All calls on a device share the one array, and
+ * (cudaGetSymbolAddress, with that device current), and looks it up again
+ * when the device's context has changed (after cudaDeviceReset); make that
+ * first call before any stream capture.  All calls on a device share the one array, and
  * it keeps the last call's contents: each call clears what has to start at
  * zero, but calls that overlap on the GPU (other streams or host threads)
  * race on it and must be serialised by the caller. */

@@ -1303,7 +1303,9 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
 
 int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi) {
     ISL_TRY
-    if (!n || degree < 0 || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
+    // the reference's rules exist for DEGREE > 0 only (base/quad/GaussLegendre.hpp:61,
+    // base/quad/GaussTetrahedron.hpp:93-175)
+    if (!n || degree < 1 || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
     std::vector<double> ww, xx;
     if (!quadrature(shape, degree, ww, xx)) return ISL_ERR_ARG;
     *n = (int)ww.size();

@@ -2287,23 +2287,52 @@ __global__ void k_noalloc_dinv(int n, const int* __restrict__ rowptr, const int*
 
 struct NoallocDevice {
     double* base = nullptr;  // device address of g_noalloc_scratch on this device
+    void* cuctx = nullptr;   // driver context the address belongs to
     int sms = 0;
 };
 std::mutex g_noalloc_mu;
 NoallocDevice g_noalloc_dev[NA_MAX_DEVICES];
 
-// once per device, with that device current: the scratch array's address
+// cuCtxGetCurrent through the runtime's driver entry point (the library links
+// only the runtime): the current context identifies a device's module
+// instance, which changes when cudaDeviceReset destroys the primary context
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn noalloc_ctx_fn() {
+    static CtxGetCurrentFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return (CtxGetCurrentFn)f;
+    }();
+    return fn;
+}
+
+// once per device context, with that device current: the scratch array's
+// address.  A reset device gets a new primary context and module instance,
+// so the address is looked up again when the current context changes.
 int noalloc_setup(int device, NoallocDevice* out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     NoallocDevice& e = g_noalloc_dev[device];
-    if (!e.base) {
-        double* ptr = nullptr;
+    void* cur = nullptr;
+    CtxGetCurrentFn fn = noalloc_ctx_fn();
+    if (!fn || fn(&cur) != 0) return ISL_ERR_CUDA;
+    double* ptr = nullptr;
+    if (!cur) {
+        // no context current on this thread yet: the runtime call creates
+        // (or binds) the device's primary context
         if (cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return ISL_ERR_CUDA;
+        if (fn(&cur) != 0 || !cur) return ISL_ERR_CUDA;
+    }
+    if (!e.base || e.cuctx != cur) {
+        if (!ptr && (cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch) != cudaSuccess || !ptr)) return ISL_ERR_CUDA;
         int sms = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
             return ISL_ERR_CUDA;
         e.sms = sms;
         e.base = ptr;
+        e.cuctx = cur;
     }
     *out = e;
     return ISL_OK;
@@ -2329,30 +2358,37 @@ int noalloc_cg(const NoallocDevice& dv, cudaStream_t st, int n, const int* rowpt
     const unsigned gdir = (unsigned)((n + BS - 1) / BS);
     // the scalars hold the reduction tickets, the counters and the done flag:
     // they must start at zero; every vector is written before it is read
-    if (cudaMemsetAsync(S, 0, sizeof(CGScal), st) != cudaSuccess) return ISL_ERR_CUDA;
+    // iters / rel_res come from the last scalar record read back, on every
+    // return after the solve started (zero before the first read)
+    CGScal h{};
+    auto report = [&](int rc) {
+        if (iters) *iters = h.iters;
+        if (rel_res) *rel_res = h.rhsNorm2 > 0 ? std::sqrt(h.rr / h.rhsNorm2) : 0.0;
+        return rc;
+    };
+    if (cudaMemsetAsync(S, 0, sizeof(CGScal), st) != cudaSuccess) return report(ISL_ERR_CUDA);
     k_noalloc_dinv<<<gdir, BS, 0, st>>>(n, rowptr, colind, val, dinv);
     k_cg_init<double, double><<<gvec, BS, 0, st>>>(n, b, x, r, p, dinv, S, part, tol, 0.0);
-    if (cudaGetLastError() != cudaSuccess) return ISL_ERR_CUDA;
-    CGScal h;
+    if (cudaGetLastError() != cudaSuccess) return report(ISL_ERR_CUDA);
     const int64_t max_rounds = (int64_t)mi / CHUNK + 3;
     for (int64_t round = 0;; ++round) {
-        if (cudaMemcpyAsync(&h, S, sizeof(CGScal), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        CGScal t;
+        if (cudaMemcpyAsync(&t, S, sizeof(CGScal), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
-            return ISL_ERR_CUDA;
+            return report(ISL_ERR_CUDA);
+        h = t;
         if (h.done) break;
-        if (round > max_rounds) return ISL_ERR_TIMEOUT;
+        if (round > max_rounds) return report(ISL_ERR_TIMEOUT);
         for (int k = 0; k < CHUNK; ++k) {
             k_cg_dir<double><<<gdir, BS, 0, st>>>(n, r, dinv, p, S);
             launch_spmv<double, double>(lpr, gvec, st, n, rowptr, colind, val, p, q, S, part);
             k_cg_update<double><<<gupd, BS, 0, st>>>(n, x, r, p, q, dinv, S, part, mi);
         }
-        if (cudaGetLastError() != cudaSuccess) return ISL_ERR_CUDA;
+        if (cudaGetLastError() != cudaSuccess) return report(ISL_ERR_CUDA);
     }
-    if (iters) *iters = h.iters;
-    if (rel_res) *rel_res = h.rhsNorm2 > 0 ? std::sqrt(h.rr / h.rhsNorm2) : 0.0;
-    if (h.bad) return ISL_ERR_NAN;
-    if (h.done == 2) return ISL_ERR_NOT_CONVERGED;
-    return ISL_OK;
+    if (h.bad) return report(ISL_ERR_NAN);
+    if (h.done == 2) return report(ISL_ERR_NOT_CONVERGED);
+    return report(ISL_OK);
 }
 
 }  // namespace

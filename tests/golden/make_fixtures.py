@@ -5,6 +5,7 @@ reference's own golden files and fixture meshes); the JSON it writes is what
 the tests use, so nothing at test time needs the reference tree.
 
     python tests/golden/make_fixtures.py /path/to/inSilico
+    INSILICO_REFERENCE=/path/to/inSilico python tests/golden/make_fixtures.py
 
 Pins extracted (file paths relative to the reference project):
   reference/03-doFHandler/sparsity.{1,2,3}.ref.dat  -> sha256 + count of the data lines
@@ -141,4 +142,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("INSILICO_REFERENCE")
+    if not ref_root:
+        sys.exit("usage: make_fixtures.py /path/to/inSilico  (or set INSILICO_REFERENCE)")
+    main(ref_root)

@@ -38,9 +38,13 @@ def test_tet_rule_sizes_and_limits():
     sizes = [len(A.quadrature_rule(A.TET, d)[0]) for d in range(1, 6)]
     assert sizes == [1, 4, 5, 11, 15]
     assert A.quadrature_rule(A.TET, 3)[0][0] < 0
-    for bad in (6, -1):
+    for bad in (6, 0, -1):
         with pytest.raises(A.IslError):
             A.quadrature_rule(A.TET, bad)
+    for shape in (A.QUAD, A.HEX):
+        for bad in (0, 6):
+            with pytest.raises(A.IslError):
+                A.quadrature_rule(shape, bad)
     assert O.quadrature(O.TET, 6) is None
 
 

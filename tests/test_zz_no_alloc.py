@@ -6,7 +6,9 @@ Two calls in a row on the same inputs: both must match the context solver
 (relative L2 <= 1e-9, the FP64 CG bar of the parity tests) and each other bit
 for bit, so the second call does not depend on what the first left in the
 shared scratch array.  The device buffers are made by the test (torch); the
-entry point itself allocates nothing.
+entry point itself allocates nothing: the device's free memory is the same
+before and after the second call (the first may still load the library's
+device code, which the CUDA runtime does lazily).
 """
 import ctypes as C
 
@@ -35,8 +37,13 @@ def context_solve(name, n):
     return rp, ci, v, b, x, it
 
 
-def noalloc_solve(L, torch, dev, n):
-    x = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda:0")
+def device_free(L):
+    f, t = C.c_int64(), C.c_int64()
+    assert L.isl_device_memory(0, C.byref(f), C.byref(t)) == A.ISL_OK
+    return f.value
+
+
+def noalloc_solve(L, torch, dev, x, n):
     it, rel = C.c_int64(), C.c_double()
     stream = torch.cuda.current_stream().cuda_stream
     st = L.isl_cg_solve_noalloc(0, stream, n, dev["rp"].data_ptr(), dev["ci"].data_ptr(), dev["v"].data_ptr(),
@@ -58,8 +65,13 @@ def test_noalloc_cg_matches_context_solver_twice(name, n):
         "b": torch.from_numpy(b).to("cuda:0"),
     }
     outs = []
-    for _ in range(2):
-        st, x, it, rel = noalloc_solve(L, torch, dev, neq)
+    for k in range(2):
+        x = torch.full((neq,), float("nan"), dtype=torch.float64, device="cuda:0")
+        torch.cuda.synchronize()
+        free0 = device_free(L)
+        st, x, it, rel = noalloc_solve(L, torch, dev, x, neq)
+        if k == 1:
+            assert device_free(L) == free0, "the no-allocation solve changed the device's free memory"
         assert st == A.ISL_OK, st
         assert np.all(np.isfinite(x))
         assert rel <= TOL
