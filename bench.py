@@ -157,72 +157,119 @@ def calibrate(S, method, x_ref, tols):
     return tols[-1], err, it
 
 
-# smaller instance of each config for the CPU assembly sample (same element
-# type, kernel and coefficient distributions)
-CPU_SAMPLE_N = {"c1": 64, "c2": 16, "c3": 12}
+REF_TOLS = [1e-9, 1e-10, 1e-11, 1e-12]
+ORACLE_TOL = 1e-12  # the FP64 oracle solution every result is compared with
 
 
-def cpu_sample(p, S, iters_ref, threads):
-    """Reference algorithm (oracle port) on host cores: assembly of a smaller
-    instance of the same config (scaled by the element count) + CG iterations
-    on the full CSR matrix of the GPU run (scaled to the iteration count the
-    solve needs)."""
+def workload_config(name, n, neq, nnz, nelem, world):
+    """The `config` object of a c1/c2/c3 line: identical for the GPU arm and
+    the reference arm, which run the same workload."""
+    return {"workload": WORKLOAD_DESC[name].format(n=n), "active_dofs": int(neq), "nnz": int(nnz),
+            "elements": int(nelem), "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (FP64 CSR %.0f MB)" % (nnz * 12 / 1e6) if nnz * 12 > 2 * L2_BYTES
+            else "L2 flushed before every timed step (FP64 CSR %.1f MB)" % (nnz * 12 / 1e6)}
+
+
+def oracle_leg(p, threads):
+    """The reference algorithm (oracle port) on the host cores at the full
+    size of workload p: DOF numbering, constraints and the triplet pattern
+    (setup, untimed), the assembly with the OpenMP element loop (timed), and
+    Eigen-3.2-style Jacobi CG to ORACLE_TOL with its residual history (timed;
+    the iteration count of any looser tolerance follows from the history).
+    Its solution is the FP64 oracle solution of the error reports."""
     import oracle as O
-    from insilico_gb300 import workloads as W
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import oracle_problem
-    ps = W.config(p.name, n=min(CPU_SAMPLE_N[p.name], p.meta["n"]))
-    P, _ = oracle_problem(ps, assemble=False)
     t0 = time.perf_counter()
-    P.assemble(incremental=True, nthreads=threads)
-    t_asm = (time.perf_counter() - t0) * (p.nelem / ps.nelem)
-    rp, ci, v = S.csr()
-    b = S.rhs()
-    k = 8
+    P, _ = oracle_problem(p, assemble=False)
+    P.pattern()
+    t_setup = time.perf_counter() - t0
     t0 = time.perf_counter()
-    O.cg(rp, ci, v, b, tol=0.0, max_iter=k, nthreads=threads)
-    t_it = (time.perf_counter() - t0) / k
-    total = t_asm + iters_ref * t_it
-    return {"value": S.neq / total, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"oracle assembly of the {p.name} config at n={ps.meta['n']} ({ps.nelem} elements, scaled to "
-                      f"{p.nelem}) + {k} Jacobi-CG iterations on the full {S.neq}-DOF matrix (scaled to {iters_ref} "
-                      f"iterations)",
-            "assembly_s_est": t_asm, "cg_iter_s": t_it}
+    rp, ci, v, b = P.assemble(incremental=True, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    x, it, rr, hist = O.cg(rp, ci, v, b, tol=ORACLE_TOL, nthreads=threads, history=True)
+    t_cg = time.perf_counter() - t0
+    return {"P": P, "csr": (rp, ci, v, b), "x": x, "t_setup": t_setup, "t_asm": t_asm, "t_cg": t_cg,
+            "iters": it, "t_iter": t_cg / (it + 1), "hist": hist, "neq": P.neq, "threads": threads}
+
+
+def oracle_rate(leg, tol):
+    """Assembly + solve throughput of the reference algorithm at tolerance
+    tol: the timed full-size assembly plus the CG iterations that tolerance
+    takes (from the residual history) at the timed cost per iteration."""
+    import oracle as O
+    its = O.iters_to(leg["hist"], tol)
+    its = leg["iters"] if its is None else its
+    t = leg["t_asm"] + leg["t_iter"] * (its + 1)
+    return leg["neq"] / t, its, t
 
 
 def run_reference(args):
-    """--impl reference: reference algorithm on host cores, same workload/metric."""
+    """--impl reference: the reference algorithm (the oracle restatement of
+    inSilico's assembly and Eigen CG; the reference itself needs Eigen 3.2 /
+    Boost 1.55, which are not available) on the host cores, on the same c2
+    64^3 workload, metric and config as the GPU arm.  Setup (numbering,
+    constraints, triplet pattern) is outside the timed steps, as on the GPU.
+    The solve tolerance is chosen as on the GPU: the loosest of 1e-9..1e-12
+    at which the FP64 CG solution is within 1e-8 of the FP64 solution to
+    1e-12.  Each step is a bounded sample: the assembly of one eighth of the
+    elements (the element loop's cost is linear in the elements), timed and
+    scaled to all of them, plus 32 CG iterations on the full matrix, timed and
+    scaled to the iteration count of that tolerance."""
     from insilico_gb300 import workloads as W
     import oracle as O
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from helpers import oracle_problem
     threads = os.cpu_count() or 1
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    name = "c2"
     n = args.n or 64
-    p = W.config("c2", n=n)
-    # bounded sample per step: a slab of the mesh, assembled and solved with the
-    # reference algorithm; throughput in active DOFs per second of the slab
-    slab = max(1, min(n, 8))
-    X, conn = W.unit_cube("hex", n, n, slab)
-    sub = W.Problem("slab", p.shape, X * np.array([1.0, 1.0, slab / n]), conn, p.fedeg, p.ncomp, p.kernel, p.qdeg,
-                    lam=p.lam[: len(conn)], mu=p.mu[: len(conn)], material=p.material, dirichlet=p.dirichlet,
-                    neumann_plane=p.neumann_plane)
-    vals = []
+    p = W.config(name, n=n)
+    leg = oracle_leg(p, threads)
+    rp, ci, v, b = leg["csr"]
+    tol = REF_TOLS[-1]
+    for t in REF_TOLS:
+        xt, _, _ = O.cg(rp, ci, v, b, tol=t, nthreads=threads)
+        if np.linalg.norm(xt - leg["x"]) <= ERR_BAR * np.linalg.norm(leg["x"]):
+            tol = t
+            break
+    its = O.iters_to(leg["hist"], tol)
+    kit = 32
+    vals, steps = [], []
+    P = leg["P"]
+    esample = max(1, p.nelem // 8)
     for step in range(args.warmup + args.steps):
+        # the per-assembly cost outside the element loop (clearing the values
+        # and the right-hand side), then the element loop over the sample
+        P.element_range(0, 0)
         t0 = time.perf_counter()
-        P, (rp, ci, v, b) = oracle_problem(sub)
-        O.cg(rp, ci, v, b, tol=1e-10, nthreads=threads)
-        dt = time.perf_counter() - t0
+        P.assemble(incremental=True, nthreads=threads)
+        t_fixed = time.perf_counter() - t0
+        P.element_range(0, esample)
+        t0 = time.perf_counter()
+        P.assemble(incremental=True, nthreads=threads)
+        t_asm = t_fixed + max(0.0, time.perf_counter() - t0 - t_fixed) * (p.nelem / esample)
+        t0 = time.perf_counter()
+        O.cg(rp, ci, v, b, tol=0.0, max_iter=kit, nthreads=threads)
+        t_it = (time.perf_counter() - t0) / kit
+        t_step = t_asm + t_it * (its + 1)
         if step >= args.warmup:
-            vals.append(P.neq / dt)
+            vals.append(leg["neq"] / t_step)
+            steps.append(t_step)
     val = float(statistics.median(vals))
-    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Philox)",
-            "config": {"workload": f"c2 hex8 elasticity slab {n}x{n}x{slab} of the {n}^3 mesh (bounded CPU sample)",
-                       "parallelism": "replicas", "l2": "n/a (CPU)"},
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(statistics.median(steps)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox; no dataset)",
+            "config": workload_config(name, n, leg["neq"], len(ci), p.nelem, world),
+            "solve_tol": tol, "cg_iters": its, "assembly_s": leg["t_asm"], "cg_iter_s": leg["t_iter"],
+            "setup_s": leg["t_setup"],
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{n}x{n}x{slab} slab of the c2 mesh: oracle assembly (OpenMP, {threads} threads) "
-                                       f"+ Jacobi CG to 1e-10 per step"},
+                             "sample": f"per step: the assembly of {esample} of the {p.nelem} elements (OpenMP, "
+                                       f"{threads} threads), its element loop scaled to all, + {kit} Jacobi-CG "
+                                       f"iterations on the full "
+                                       f"{leg['neq']}-DOF matrix, scaled to the {its} iterations of tol {tol:g}; "
+                                       f"numbering and pattern once, outside the steps (full assembly in setup: "
+                                       f"{leg['t_asm']:.2f} s)"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -269,6 +316,21 @@ def run_serve(args, rank, world, local, pg):
         log(f"c5 {m} open loop at {rate:.2f}/s: {out[m]['open']}")
     for srv in servers.values():
         srv.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # the reference algorithm (oracle Newton: assembly + Jacobi CG to the
+        # plain server's 1e-10 per Newton step) on the first request of the
+        # same stream, with all host threads
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from helpers import oracle_newton
+        threads = os.cpu_count() or 1
+        r0 = serve.make_requests(nreq, rate=0.0)[0]
+        t0 = time.perf_counter()
+        oracle_newton(r0, lin_tol=1e-10, nthreads=threads)
+        tc = time.perf_counter() - t0
+        cpu = {"value": 1.0 / tc, "unit": "requests/s", "cores": threads, "kind": "port",
+               "sample": f"request 0 of the stream (side {r0.side}, {3 * (r0.side + 1) ** 3} DOF components, "
+                         f"5 load steps) through the oracle's Newton loop with Jacobi CG to 1e-10: {tc:.1f} s"}
     errs = []
     for rid, u in out["plain"]["u"].items():
         um = out["mixed"]["u"][rid]
@@ -296,7 +358,7 @@ def run_serve(args, rank, world, local, pg):
             "e2e": {"value": mc["solves_per_s"], "unit": "requests/s",
                     "h2d_bytes_per_step": int(out["mixed"]["h2d"] / nreq),
                     "d2h_bytes_per_step": int(out["mixed"]["d2h"] / nreq)},
-            "clocks": clocks, "gpu_launches": int(out["mixed"]["launches"])}
+            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(out["mixed"]["launches"])}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -409,7 +471,10 @@ def batch_groups(inst, pair_budget=1_300_000_000):
 def run_batch(args, rank, world, local, pg):
     """c4: batched Q1/Q2 Poisson instances (C1-style data), assembly + per-
     instance CG to 1e-8 (mixed: FP32 CG + FP64 refinement; plain: FP64 CG),
-    one context per group of instances, all contexts resident."""
+    one context per group of instances, all contexts resident.  The groups'
+    assemblies and solves run concurrently: one host thread and one CUDA
+    stream per context."""
+    import concurrent.futures as cf
     from insilico_gb300 import _abi as A
     from insilico_gb300 import workloads as W
     from insilico_gb300.system import System
@@ -417,7 +482,7 @@ def run_batch(args, rank, world, local, pg):
     seed = W.SEED_BASE + 3
     inst = batch_instances(args.instances, seed)
     groups = batch_groups(inst)
-    systems = []
+    systems, coefs = [], []
     t_setup = time.perf_counter()
     for deg, members in groups:
         S = System(device=local)
@@ -432,7 +497,8 @@ def run_batch(args, rank, world, local, pg):
         S.constrain_boundary(lambda x: (np.ones((len(x), 1), dtype=bool), 0.0))
         S.number_dofs()
         S.register_pattern()
-        S.set_laplace(np.concatenate(kappa), 2 * deg)
+        coefs.append((np.concatenate(kappa), 2 * deg))
+        S.set_laplace(*coefs[-1])
         S.set_body_force_nodal(np.concatenate(body))
         del meshes, kappa, body
         systems.append(S)
@@ -441,24 +507,32 @@ def run_batch(args, rank, world, local, pg):
     neq = sum(S.neq for S in systems)
     nnz = sum(S.nnz for S in systems)
     tol = 1e-8
+    pool = cf.ThreadPoolExecutor(max_workers=len(systems))
 
-    def step(mixed):
-        for S in systems:
-            S.assemble(A.PREC_MIXED if mixed else A.PREC_FP64)
-            S.solve(A.SOLVE_CG_FP32_IR if mixed else A.SOLVE_CG_FP64, tol=tol)
+    def on_all(fn):
+        """fn(context index, context) on every context at once (ctypes releases
+        the GIL inside the library, so each context drives its own stream)."""
+        list(pool.map(lambda kv: fn(*kv), enumerate(systems)))
 
-    def timed(mixed, steps):
+    def one(mixed, k, S, upload=False, download=False):
+        if upload:
+            S.set_laplace(*coefs[k])
+        S.assemble(A.PREC_MIXED if mixed else A.PREC_FP64)
+        S.solve(A.SOLVE_CG_FP32_IR if mixed else A.SOLVE_CG_FP64, tol=tol)
+        if download:
+            return S.solution()
+        S.sync()
+
+    def timed(mixed, steps, **kw):
         for S in systems:
             S.sync()
         t0 = time.perf_counter()
         for _ in range(steps):
-            step(mixed)
-        for S in systems:
-            S.sync()
+            on_all(lambda k, S: one(mixed, k, S, **kw))
         return (time.perf_counter() - t0) / steps
 
     for _ in range(args.warmup):
-        step(True)
+        on_all(lambda k, S: one(True, k, S))
     if args.profile:
         # one mixed step inside the profiler range (ncu --profile-from-start off)
         import ctypes
@@ -466,58 +540,120 @@ def run_batch(args, rank, world, local, pg):
         for S in systems:
             S.sync()
         cudart.cudaProfilerStart()
-        step(True)
-        for S in systems:
-            S.sync()
+        on_all(lambda k, S: one(True, k, S))
         cudart.cudaProfilerStop()
         for S in systems:
             S.close()
         return
-    # accuracy: mixed vs FP64 (tight) per group
-    errs = []
+    # accuracy: mixed and plain at the c4 tolerance against a tight FP64 solve
+    errs, errs64 = [], []
     for S in systems:
         S.assemble(A.PREC_MIXED)
         S.solve(A.SOLVE_CG_FP64, tol=1e-12)
+        xt = S.solution()
+        S.solve(A.SOLVE_CG_FP64, tol=tol)
         x64 = S.solution()
         S.solve(A.SOLVE_CG_FP32_IR, tol=tol)
         xm = S.solution()
         eq_off, _ = S.batch_info()
         for k in range(len(eq_off) - 1):
             a, b = eq_off[k], eq_off[k + 1]
-            errs.append(float(np.linalg.norm(xm[a:b] - x64[a:b]) / max(np.linalg.norm(x64[a:b]), 1e-300)))
+            nt = max(np.linalg.norm(xt[a:b]), 1e-300)
+            errs.append(float(np.linalg.norm(xm[a:b] - xt[a:b]) / nt))
+            errs64.append(float(np.linalg.norm(x64[a:b] - xt[a:b]) / nt))
     l0 = sum(S.launch_count() for S in systems)
     clk = Clocks(local)
     s_mixed = timed(True, args.steps)
     clocks = clk.stop()
-    launches = sum(S.launch_count() for S in systems) - l0
+    launches = (sum(S.launch_count() for S in systems) - l0) // max(1, args.steps)
     s_plain = timed(False, max(1, args.steps // 2))
-    # assembly share
-    for S in systems:
-        S.set_timing(True)
-    step(True)
+    # e2e through the C-ABI with host buffers: per step every group's
+    # conductivity table goes up, assembly and solve run, the solutions come back
+    e2e_s = timed(True, args.steps, upload=True, download=True)
+    h2d = sum(c[0].nbytes for c in coefs)
+    # assembly share (one context at a time, CUDA-event phase timers)
     asm_ms = 0.0
     for S in systems:
+        S.set_timing(True)
+        S.assemble(A.PREC_MIXED)
+        S.solve(A.SOLVE_CG_FP32_IR, tol=tol)
         ms, _ = S.timings()
         asm_ms += ms[A.T_ELEMENT] + ms[A.T_GATHER]
         S.set_timing(False)
     iters = np.concatenate([S.batch_stats()[0] for S in systems])
+    # dominant kernel: the batched FP32 SpMV with every instance active, per
+    # context; achieved = the contexts' algorithmic bytes over their summed times
+    hbm, src = peaks()
+    sp_ms, sp_bytes, kinds = 0.0, 0, []
+    for S in systems:
+        sp_ms += S.time_spmv(A.PREC_FP32, 20)
+        sp_bytes += spmv_bytes(S.nnz, S.neq, 4)
+        kinds.append(S.get_option(A.OPT_SPMV32_KIND))
+    ach = sp_bytes / (sp_ms * 1e-3) / 1e9
+    kname = ", ".join(sorted({("kb_sspmv<%d,%d>" % (k - 100, 8 if k < 108 else 6)) if k >= 100 else
+                              f"kb_spmv<float,float,{k}>" for k in kinds}))
     for S in systems:
         S.close()
+    pool.shutdown()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = batch_cpu_sample(inst, seed, tol)
     line = {"metric": METRIC, "value": neq * world / s_mixed, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": s_mixed * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Philox; no dataset)",
             "config": {"workload": f"c4 {args.instances} batched Poisson instances (unit square, side U{{8..256}}, "
                                    "Q1/Q2 p = 0.5, kappa_e = exp(N(0,0.5)), nodal source U[0,1], g = 0), tol 1e-8",
                        "active_dofs": int(neq), "nnz": int(nnz), "contexts": len(systems),
-                       "parallelism": "single", "l2": "inputs larger than L2 (FP32 CSR %.1f GB)" % (nnz * 8 / 1e9)},
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (FP32 CSR %.1f GB)" % (nnz * 8 / 1e9)},
+            "method": "mixed FP32 CG + FP64 reliable updates per instance; contexts concurrent (one stream each)",
             "assembly_ms": asm_ms, "assembly_gdofs": neq / (asm_ms * 1e-3) / 1e9, "setup_s": t_setup,
             "plain_fp64": {"ms_per_step": s_plain * 1e3, "dofs_per_s": neq / s_plain},
             "speedup_vs_plain_fp64": s_plain / s_mixed,
-            "rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+            "rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs)),
+                                "plain_fp64_max": max(errs64), "reference": "GPU FP64 CG to 1e-12 per instance"},
             "cg_iters": {"min": int(iters.min()), "median": int(np.median(iters)), "max": int(iters.max())},
-            "e2e": None, "clocks": clocks, "gpu_launches": int(launches)}
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                         "traffic": ncu_traffic("spmv_fp32_c4"), "kernel": kname + " (batched FP32 SpMV, all instances)",
+                         "bytes_per_launch": sp_bytes, "ms_per_launch": sp_ms, "peak_source": src},
+            "cpu_baseline": cpu,
+            "e2e": {"value": neq * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(neq * 8), "ms_per_step": e2e_s * 1e3},
+            "clocks": clocks, "gpu_launches": int(launches)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def batch_cpu_sample(inst, seed, tol, budget_s=20.0):
+    """The reference algorithm (oracle) on the first instances of the c4
+    stream, in stream order, with all host threads: assembly + Jacobi CG to
+    tol per instance, until budget_s is spent."""
+    import oracle as O
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import oracle_problem
+    threads = os.cpu_count() or 1
+    dofs, t, done = 0, 0.0, []
+    for k, side, deg in inst:
+        X, conn = W.unit_cube("quad", side, side)
+        p = W.Problem("inst", A.QUAD, X, conn, deg, 1, "laplace", 2 * deg,
+                      kappa=np.exp(W.rng(seed, 16 + 2 * k).normal(0.0, 0.5, len(conn))),
+                      body=W.rng(seed, 17 + 2 * k).uniform(0.0, 1.0, len(X))[:, None],
+                      dirichlet=lambda x: (np.ones((len(x), 1), dtype=bool), 0.0))
+        P, _ = oracle_problem(p, assemble=False)
+        P.pattern()
+        t0 = time.perf_counter()
+        rp, ci, v, b = P.assemble(incremental=True, nthreads=threads)
+        O.cg(rp, ci, v, b, tol=tol, nthreads=threads)
+        t += time.perf_counter() - t0
+        dofs += P.neq
+        done.append(f"Q{deg} side {side}")
+        if t >= budget_s:
+            break
+    return {"value": dofs / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle assembly + Jacobi CG to {tol:g} of the first {len(done)} instances of the stream "
+                      f"({', '.join(done)}; {dofs} DOFs, {t:.1f} s); numbering and pattern outside"}
 
 
 def main():
@@ -592,13 +728,25 @@ def run_single(args, rank, world, local, pg):
         cudart.cudaProfilerStop()
         S.close()
         return
-    # FP64 reference solution (tight tolerance) and the plain path's calibration
+    threads = os.cpu_count() or 1
+    # the FP64 oracle solution: the reference algorithm on the host cores
+    # (rank 0 of a single-GPU run; replicas and --no-cpu fall back to a tight
+    # FP64 GPU solve, and say so)
+    leg = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        t0 = time.perf_counter()
+        leg = oracle_leg(p, threads)
+        log(f"oracle leg: setup {leg['t_setup']:.1f}s assembly {leg['t_asm']:.2f}s cg {leg['t_cg']:.1f}s "
+            f"({leg['iters']} iters) total {time.perf_counter() - t0:.1f}s")
+        assert leg["neq"] == neq
     S.assemble(A.PREC_MIXED)
-    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
-    x_ref = S.solution()
-    tols = [1e-9, 1e-10, 1e-11, 1e-12]
-    tol64, err64, it64 = calibrate(S, A.SOLVE_CG_FP64, x_ref, tols)
-    tolm, errm, itm = calibrate(S, A.SOLVE_CG_FP32_IR, x_ref, tols)
+    if leg is not None:
+        x_ref, ref_kind = leg["x"], f"oracle FP64 CG to {ORACLE_TOL:g} (reference algorithm, host)"
+    else:
+        S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+        x_ref, ref_kind = S.solution(), "GPU FP64 CG to 1e-13 (no oracle run)"
+    tol64, err64, it64 = calibrate(S, A.SOLVE_CG_FP64, x_ref, REF_TOLS)
+    tolm, errm, itm = calibrate(S, A.SOLVE_CG_FP32_IR, x_ref, REF_TOLS)
 
     def step_mixed():
         S.assemble(A.PREC_MIXED)
@@ -658,11 +806,36 @@ def run_single(args, rank, world, local, pg):
         it_plain = step_plain()[0]
     S.mark(3)
     plain_ms = S.elapsed_ms(2, 3) / 2
+    x_p = S.solution()
+    err_p = float(np.linalg.norm(x_p - x_ref) / np.linalg.norm(x_ref))
     S.set_timing(True)
     step_plain()
     ms64, _ = S.timings()
     S.set_timing(False)
     asm64_ms = ms64[A.T_ELEMENT] + ms64[A.T_GATHER]
+
+    # what the speed-up is made of: the mixed solve with the plain path's
+    # point-Jacobi preconditioner and scalar CSR matrix (precision alone),
+    # against the node-block format with block Jacobi
+    split = None
+    if S.get_option(A.OPT_BLOCKED):
+        S.set_option(A.OPT_BLOCK_SOLVER, 0)
+        tolq, errq, _ = calibrate(S, A.SOLVE_CG_FP32_IR, x_ref, REF_TOLS)
+        step_mixed_point = lambda: (S.assemble(A.PREC_MIXED), S.solve(A.SOLVE_CG_FP32_IR, tol=tolq))[1]  # noqa: E731
+        step_mixed_point()
+        S.mark(4)
+        for _ in range(2):
+            it_q = step_mixed_point()[0]
+        S.mark(5)
+        point_ms = S.elapsed_ms(4, 5) / 2
+        S.set_option(A.OPT_BLOCK_SOLVER, 1)
+        split = {"mixed_point_jacobi_csr": {"ms_per_step": point_ms, "iters": it_q, "solve_tol": tolq,
+                                            "rel_err_vs_fp64": errq},
+                 "precision_alone": plain_ms / point_ms,
+                 "block_format_and_block_jacobi": point_ms / ms_step,
+                 "note": "plain FP64 (point Jacobi, CSR) -> mixed with the same point Jacobi and CSR (precision "
+                         "alone) -> mixed with 3x3 node blocks and block Jacobi"}
+        log(f"split: {split}")
 
     # dominant kernel: FP32 SpMV of the inner CG, timed alone (CUDA events)
     S.assemble(A.PREC_MIXED)
@@ -712,26 +885,27 @@ def run_single(args, rank, world, local, pg):
            "d2h_bytes_per_step": int(neq * 8), "ms_per_step": e2e_s * 1e3}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        try:
-            cpu = cpu_sample(p, S, it64, os.cpu_count() or 1)
-        except Exception as ex:  # reported, not fatal
-            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+    if leg is not None:
+        rate, its_cpu, t_cpu = oracle_rate(leg, tol64)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the full workload on the oracle: assembly timed ({leg['t_asm']:.2f} s, OpenMP) + Jacobi CG "
+                         f"to {ORACLE_TOL:g} timed ({leg['t_cg']:.1f} s, {leg['iters']} iterations), counted at the "
+                         f"{its_cpu} iterations of the plain path's tolerance {tol64:g}; numbering and pattern "
+                         f"({leg['t_setup']:.1f} s) outside, as on the GPU",
+               "assembly_s": leg["t_asm"], "cg_iter_s": leg["t_iter"], "cg_iters": its_cpu, "step_s": t_cpu}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Philox; no dataset)",
-        "config": {"workload": WORKLOAD_DESC[args.workload].format(n=args.n) +
-                   ", mixed FP32 CG + FP64 refinement", "active_dofs": neq, "nnz": nnz, "elements": int(p.nelem),
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": ("L2 flushed before every timed step (working set %.1f MB)" % (working_set / 1e6)) if flush_l2
-                   else "inputs larger than L2 (FP64 CSR %.0f MB)" % (nnz * 12 / 1e6)},
+        "config": workload_config(args.workload, args.n, neq, nnz, p.nelem, world),
+        "method": "mixed FP32 CG + FP64 reliable updates" + (", 3x3 node blocks + block Jacobi" if blocked else ""),
         "assembly_gdofs": neq / (asm_ms * 1e-3) / 1e9, "assembly_ms": asm_ms, "solve_ms": solve_ms_m,
         "solve_tol": tolm, "inner_iters_per_step": int(np.median(its)), "rel_err_vs_fp64": err_m,
+        "fp64_reference": ref_kind,
         "plain_fp64": {"ms_per_step": plain_ms, "dofs_per_s": neq / (plain_ms * 1e-3), "assembly_ms": asm64_ms,
-                       "solve_ms": ms64[A.T_SOLVE], "iters": it_plain, "solve_tol": tol64, "rel_err_vs_fp64": err64},
-        "speedup_vs_plain_fp64": plain_ms / ms_step,
+                       "solve_ms": ms64[A.T_SOLVE], "iters": it_plain, "solve_tol": tol64, "rel_err_vs_fp64": err_p},
+        "speedup_vs_plain_fp64": plain_ms / ms_step, "speedup_split": split,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                      "traffic": traffic, "kernel": kname, "blocks": nblk, "slots": nslot,
                      "bytes_per_launch": b32, "ms_per_launch": spmv32_ms, "peak_source": src,

@@ -337,7 +337,9 @@ int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes);
  * context since creation. */
 int isl_launch_count(isl_ctx* ctx, int64_t* n);
 /* Average device time (ms) of one launch of the solver's SpMV kernel on the
- * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches. */
+ * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches.
+ * On a batch: the batched SpMV of isl_solve with every instance active (the
+ * FP32 kind the last mixed solve chose). */
 int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
 
 /* Warm per-kernel device time (ms per launch, CUDA events over nrep launches)

@@ -4,8 +4,11 @@
 // kernel launches.  Thread blocks are assigned to row ranges of a single
 // instance; each instance's reductions are summed by the last of its blocks
 // (per-instance ticket), in a fixed order.  CHUNK iterations are captured
-// into one CUDA graph and replayed until every instance is done; blocks of
-// finished instances return at once.
+// into one CUDA graph and replayed until every instance is done.  The
+// iteration kernels run on a fixed grid that loops over a device list of the
+// row blocks of unfinished instances; the list is rebuilt at the start of
+// every replay (kb_compact), so the launches shrink with the set of
+// instances still iterating instead of sweeping every row block of the batch.
 //
 // Mixed method: FP32 CG with FP64 reliable updates per instance, inside the
 // graph: an instance whose iterated residual dropped 10x (or met the
@@ -13,6 +16,7 @@
 // FP64 residual b - A64 x and resumes; it finishes when the FP64 residual
 // meets the tolerance.
 #include <cmath>
+#include <functional>
 #include <vector>
 
 #include "isl_device.cuh"
@@ -39,6 +43,8 @@ enum { T_SPMV, T_UPD, T_RES, T_NT };
 
 struct BArgs {
     int ninst;
+    int nblk;             // row blocks of the batch (partial-sum slots per sum)
+    const int* act;       // act[0]: listed row blocks, act[1..]: their ids (unfinished instances)
     const int* blk_inst;
     const int* blk_r0;
     const int* blk_r1;
@@ -70,7 +76,38 @@ __device__ inline void finish(const BArgs& a, int k, int code) {
 
 __device__ inline double inst_sum(const BArgs& a, int k, int off, double* sh) {
     const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
-    return reduce_parts(a.part + (size_t)off * gridDim.x + b0, b1 - b0, 1, 0, sh);
+    return reduce_parts(a.part + (size_t)off * a.nblk + b0, b1 - b0, 1, 0, sh);
+}
+
+// The listed row blocks, one per loop trip of a CTA: w-th entry of the list.
+// Every thread of a CTA takes the same trips, so block barriers inside the
+// body stay uniform.
+#define FOR_LISTED_BLOCKS(a, blk)                                                   \
+    for (int _w = blockIdx.x, _n = (a).act[0]; _w < _n; _w += gridDim.x)             \
+        if (const int blk = (a).act[1 + _w]; true)
+
+// The row blocks of every unfinished instance, in block order (one CTA; a
+// block-wide scan over the instances' block counts).
+__global__ void __launch_bounds__(1024) kb_compact(BArgs a, int* __restrict__ act) {
+    __shared__ int sums[1024];
+    const int per = (a.ninst + 1023) / 1024;
+    const int k0 = min(a.ninst, (int)threadIdx.x * per), k1 = min(a.ninst, k0 + per);
+    int cnt = 0;
+    for (int k = k0; k < k1; ++k)
+        if (!II(a, I_DONE, k)) cnt += a.inst_blk[k + 1] - a.inst_blk[k];
+    sums[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+        const int v = threadIdx.x >= o ? sums[threadIdx.x - o] : 0;
+        __syncthreads();
+        sums[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int pos = sums[threadIdx.x] - cnt;
+    for (int k = k0; k < k1; ++k)
+        if (!II(a, I_DONE, k))
+            for (int b = a.inst_blk[k]; b < a.inst_blk[k + 1]; ++b) act[1 + pos++] = b;
+    if (threadIdx.x == 1023) act[0] = sums[1023];
 }
 
 template <typename TB, typename TX>
@@ -89,7 +126,7 @@ __global__ void __launch_bounds__(BBS) kb_init(BArgs a, const TB* __restrict__ b
         bz += (double)ri * (double)(dinv[i] * ri);
     }
     const double s1 = block_sum(bb, sh), s2 = block_sum(bz, sh);
-    if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[gridDim.x + blockIdx.x] = s2; }
+    if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[a.nblk + blockIdx.x] = s2; }
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {
         const double tbb = inst_sum(a, k, 0, sh), tbz = inst_sum(a, k, 1, sh);
@@ -112,20 +149,23 @@ __global__ void __launch_bounds__(BBS) kb_init(BArgs a, const TB* __restrict__ b
 
 template <typename TX>
 __global__ void __launch_bounds__(BBS) kb_dir(BArgs a, const TX* __restrict__ r, const TX* __restrict__ dinv, TX* __restrict__ p) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k)) return;
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
-    const TX beta = (TX)SS(a, S_BETA, k);
-    for (int i = r0 + threadIdx.x; i < r1; i += BBS) p[i] = dinv[i] * r[i] + beta * p[i];
+    FOR_LISTED_BLOCKS(a, blk) {
+        const int k = a.blk_inst[blk];
+        if (II(a, I_DONE, k)) continue;
+        const int r0 = a.blk_r0[blk], r1 = a.blk_r1[blk];
+        const TX beta = (TX)SS(a, S_BETA, k);
+        for (int i = r0 + threadIdx.x; i < r1; i += BBS) p[i] = dinv[i] * r[i] + beta * p[i];
+    }
 }
 
 template <typename TV, typename TX, int LPR>
 __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ rowptr, const int* __restrict__ colind,
                                                const TV* __restrict__ val, const TX* __restrict__ p, TX* __restrict__ q) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k)) return;
     __shared__ double sh[32];
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    FOR_LISTED_BLOCKS(a, blk) {
+    const int k = a.blk_inst[blk];
+    if (II(a, I_DONE, k)) continue;
+    const int r0 = a.blk_r0[blk], r1 = a.blk_r1[blk];
     const int lane = threadIdx.x % LPR, grp = threadIdx.x / LPR;
     const int wgrp = grp - grp % (32 / LPR);  // warp-uniform loop (full-mask shuffles)
     TX loc = TX(0);  // in the vectors' precision; warp sums are added in FP64
@@ -173,7 +213,7 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
         }
     }
     const double s1 = block_sum_t(loc, sh);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    if (threadIdx.x == 0) a.part[blk] = s1;
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
         const double tot = inst_sum(a, k, 0, sh);
@@ -181,6 +221,7 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
             SS(a, S_ALPHA, k) = SS(a, S_ABSNEW, k) / tot;
             a.t[T_SPMV * a.ninst + k] = 0;
         }
+    }
     }
 }
 
@@ -193,11 +234,12 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
                                                    const int* __restrict__ srow, const int* __restrict__ scol,
                                                    const float* __restrict__ sv, const float* __restrict__ p,
                                                    float* __restrict__ q) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k)) return;
     __shared__ double sh[32];
+    FOR_LISTED_BLOCKS(a, blk) {
+    const int k = a.blk_inst[blk];
+    if (II(a, I_DONE, k)) continue;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sl0 = a.blk_s0[blockIdx.x], sl1 = a.blk_s1[blockIdx.x];
+    const int sl0 = a.blk_s0[blk], sl1 = a.blk_s1[blk];
     float loc = 0.f;
     for (int s = sl0 + warp; s < sl1; s += BBS / 32) {
         const int o = soff[s] + lane, w = swid[s];
@@ -223,7 +265,7 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
         }
     }
     const double s1 = block_sum_t(loc, sh);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = s1;
+    if (threadIdx.x == 0) a.part[blk] = s1;
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
         const double tot = inst_sum(a, k, 0, sh);
@@ -232,6 +274,7 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
             a.t[T_SPMV * a.ninst + k] = 0;
         }
     }
+    }
 }
 
 // mixed = 1: convergence or a 10x drop of the iterated residual requests a
@@ -239,10 +282,11 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
 template <typename TX>
 __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX* __restrict__ r, const TX* __restrict__ p,
                                                  const TX* __restrict__ q, const TX* __restrict__ dinv, int mixed) {
-    const int k = a.blk_inst[blockIdx.x];
-    if (II(a, I_DONE, k)) return;
     __shared__ double sh[32];
-    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    FOR_LISTED_BLOCKS(a, blk) {
+    const int k = a.blk_inst[blk];
+    if (II(a, I_DONE, k)) continue;
+    const int r0 = a.blk_r0[blk], r1 = a.blk_r1[blk];
     const TX alpha = (TX)SS(a, S_ALPHA, k);
     TX rr = TX(0), rz = TX(0);
     for (int i = r0 + threadIdx.x; i < r1; i += BBS) {
@@ -253,7 +297,7 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
         rz += ri * (dinv[i] * ri);
     }
     const double s1 = block_sum_t(rr, sh), s2 = block_sum_t(rz, sh);
-    if (threadIdx.x == 0) { a.part[blockIdx.x] = s1; a.part[gridDim.x + blockIdx.x] = s2; }
+    if (threadIdx.x == 0) { a.part[blk] = s1; a.part[a.nblk + blk] = s2; }
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {
         const double trr = inst_sum(a, k, 0, sh), trz = inst_sum(a, k, 1, sh);
@@ -273,6 +317,7 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
             }
             a.t[T_UPD * a.ninst + k] = 0;
         }
+    }
     }
 }
 
@@ -470,6 +515,7 @@ int ensure_batch_state(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dbt.alloc((size_t)T_NT * c->ninst));
     ISL_CHECK_CUDA(c, c->dbpart.alloc((size_t)SUB * bi.size()));
     ISL_CHECK_CUDA(c, c->dbwl.alloc((size_t)2 * c->ninst + 3));
+    ISL_CHECK_CUDA(c, c->dbact.alloc(bi.size() + 1));
     cudaStream_t st = c->stream;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_inst.p, bi.data(), bi.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row0.p, b0.data(), b0.size() * 4, cudaMemcpyHostToDevice, st));
@@ -481,19 +527,12 @@ int ensure_batch_state(isl_ctx* c) {
     return ISL_OK;
 }
 
-}  // namespace
-
-int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
-    int rc = ensure_batch_state(c);
-    if (rc != ISL_OK) return rc;
-    const size_t n = (size_t)c->neq;
-    if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
-    if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
-    cudaStream_t st = c->stream;
-    const unsigned grid = (unsigned)c->nbblocks;
+BArgs batch_args(isl_ctx* c, int64_t max_iter, double tol) {
     const int ni = (int)c->ninst;
     BArgs a;
     a.ninst = ni;
+    a.nblk = (int)c->nbblocks;
+    a.act = c->dbact.p;
     a.blk_inst = c->dblk_inst.p;
     a.blk_r0 = c->dblk_row0.p;
     a.blk_r1 = c->dblk_row1.p;
@@ -511,6 +550,75 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     a.tol = tol;
     a.blk_s0 = nullptr;
     a.blk_s1 = nullptr;
+    return a;
+}
+
+}  // namespace
+
+// Average device time of one batched SpMV launch with every instance active
+// (the kernel and grid the batched solve uses: FP32 = the autotuned kind of
+// the last mixed solve, FP64 = CSR with the solve's lanes per row).
+int time_spmv_batched(isl_ctx* c, int precision, int nrep, double* ms) {
+    int rc = ensure_batch_state(c);
+    if (rc != ISL_OK) return rc;
+    const size_t n = (size_t)c->neq;
+    if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
+    if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
+    cudaStream_t st = c->stream;
+    const int ni = (int)c->ninst;
+    BArgs a = batch_args(c, 1, 0.0);
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbs.p, 0, (size_t)S_NS * ni * 8, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbi.p, 0, ((size_t)I_NI * ni + 1) * 4, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbt.p, 0, (size_t)T_NT * ni * 4, st));
+    kb_compact<<<1, 1024, 0, st>>>(a, c->dbact.p);
+    const unsigned lgrid = (unsigned)std::min<int64_t>(c->nbblocks, (int64_t)c->sm_count * 8);
+    const unsigned sgrid = (unsigned)std::min<int64_t>(c->nbblocks, (int64_t)c->sm_count * 6);
+    std::function<void()> launch;
+    if (precision == ISL_PREC_FP32) {
+        if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
+        rc = ensure_ssell(c);
+        if (rc != ISL_OK) return rc;
+        int kind = c->bspmv32 ? c->bspmv32 : pick_lpr(c);
+        if (kind >= 100 && c->bsell_built && c->ss_nslice > 0) {
+            a.blk_s0 = c->dblk_s0.p;
+            a.blk_s1 = c->dblk_s1.p;
+        } else if (kind >= 100) {
+            kind = pick_lpr(c);
+        }
+        float* V = c->w32.p;
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
+        const unsigned g = kind >= 100 ? sgrid : lgrid;
+        launch = [=] { launch_kb_spmv32(c, kind, g, st, a, V + 2 * n, V + 3 * n); };
+    } else {
+        if (!c->have64) ISL_FAIL(c, ISL_ERR_ARG, "no FP64 matrix");
+        double* W = c->w64.p;
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(W + 2 * n, 0, n * 8, st));
+        const int lpr = pick_lpr(c);
+        launch = [=] { launch_kb_spmv<double, double>(lpr, lgrid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n); };
+    }
+    launch();
+    cudaEventRecord(c->ev[2], st);
+    for (int r = 0; r < nrep; ++r) launch();
+    cudaEventRecord(c->ev[3], st);
+    c->launches += nrep + 2;
+    ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
+    *ms = t / nrep;
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    return ISL_OK;
+}
+
+int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
+    int rc = ensure_batch_state(c);
+    if (rc != ISL_OK) return rc;
+    const size_t n = (size_t)c->neq;
+    if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
+    if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
+    cudaStream_t st = c->stream;
+    const unsigned grid = (unsigned)c->nbblocks;
+    const int ni = (int)c->ninst;
+    BArgs a = batch_args(c, max_iter, tol);
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbs.p, 0, (size_t)S_NS * ni * 8, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbi.p, 0, ((size_t)I_NI * ni + 1) * 4, st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dbt.p, 0, (size_t)T_NT * ni * 4, st));
@@ -518,6 +626,10 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(a.remaining, &ni, 4, cudaMemcpyHostToDevice, st));
     const int lpr = pick_lpr(c);
     const unsigned vg = (unsigned)c->sm_count * 8;
+    // the iteration kernels' fixed grids over the listed row blocks: as many
+    // CTAs as fit on the GPU at once (never more than the batch's blocks)
+    const unsigned lgrid = (unsigned)std::min<int64_t>(c->nbblocks, (int64_t)c->sm_count * 8);
+    const unsigned sgrid = (unsigned)std::min<int64_t>(c->nbblocks, (int64_t)c->sm_count * 6);
     const unsigned wgrid = (unsigned)c->sm_count * 4;  // the reliable-update worklist kernels
     const bool mixed = (method == ISL_SOLVE_CG_FP32_IR);
     if (mixed && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "batched mixed solve needs the FP64 matrix (ISL_PREC_MIXED)");
@@ -531,10 +643,11 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         kb_init<double, double><<<grid, BBS, 0, st>>>(a, c->drhs.p, x, r, p, dinv);
         ISL_CHECK_CUDA(c, cudaGetLastError());
         ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        kb_compact<<<1, 1024, 0, st>>>(a, c->dbact.p);
         for (int k = 0; k < BCHUNK; ++k) {
-            kb_dir<double><<<grid, BBS, 0, st>>>(a, r, dinv, p);
-            launch_kb_spmv<double, double>(lpr, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, p, q);
-            kb_update<double><<<grid, BBS, 0, st>>>(a, x, r, p, q, dinv, 0);
+            kb_dir<double><<<lgrid, BBS, 0, st>>>(a, r, dinv, p);
+            launch_kb_spmv<double, double>(lpr, lgrid, st, a, c->drowptr.p, c->dcolind.p, c->dval64.p, p, q);
+            kb_update<double><<<lgrid, BBS, 0, st>>>(a, x, r, p, q, dinv, 0);
         }
         ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     } else {
@@ -567,6 +680,8 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
             a.blk_s0 = c->dblk_s0.p;
             a.blk_s1 = c->dblk_s1.p;
         }
+        kb_compact<<<1, 1024, 0, st>>>(a, c->dbact.p);
+        c->launches += 1;
         if (c->spmv32_forced > 0 && (c->spmv32_forced < 100 || c->ss_nslice > 0)) {
             c->bspmv32 = c->spmv32_forced;
         } else if (!c->bspmv32) {
@@ -578,9 +693,10 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
             int best = lpr;
             float bestms = 1e30f;
             for (int k2 = 0; k2 < ncand && ncand > 1; ++k2) {
-                launch_kb_spmv32(c, cand[k2], grid, st, a, p32, q32);
+                const unsigned g2 = cand[k2] >= 100 ? sgrid : lgrid;
+                launch_kb_spmv32(c, cand[k2], g2, st, a, p32, q32);
                 cudaEventRecord(c->ev[2], st);
-                for (int r = 0; r < 5; ++r) launch_kb_spmv32(c, cand[k2], grid, st, a, p32, q32);
+                for (int r = 0; r < 5; ++r) launch_kb_spmv32(c, cand[k2], g2, st, a, p32, q32);
                 cudaEventRecord(c->ev[3], st);
                 cudaEventSynchronize(c->ev[3]);
                 float ms = 0.f;
@@ -591,11 +707,13 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
             c->bspmv32 = best;
         }
         c->spmv_lpr32 = c->bspmv32;
+        const unsigned g32 = c->bspmv32 >= 100 ? sgrid : lgrid;
         ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        kb_compact<<<1, 1024, 0, st>>>(a, c->dbact.p);
         for (int k = 0; k < BCHUNK; ++k) {
-            kb_dir<float><<<grid, BBS, 0, st>>>(a, r32, d32, p32);
-            launch_kb_spmv32(c, c->bspmv32, grid, st, a, p32, q32);
-            kb_update<float><<<grid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
+            kb_dir<float><<<lgrid, BBS, 0, st>>>(a, r32, d32, p32);
+            launch_kb_spmv32(c, c->bspmv32, g32, st, a, p32, q32);
+            kb_update<float><<<lgrid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
             // reliable updates of the instances kb_update listed
             kb_wl_scan<<<1, BBS, 0, st>>>(a);
             kb_fold_w<<<wgrid, BBS, 0, st>>>(a, x32, x64);
@@ -610,7 +728,7 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         cudaGraphDestroy(graph);
         ISL_CHECK_CUDA(c, e);
     }
-    const int per_iter = mixed ? 7 : 3;
+    const int per_iter = mixed ? 7 : 3;  // plus the list rebuild once per replay
     const int64_t max_replays = (int64_t)a.max_iter / BCHUNK + 8;
     int remaining = ni;
     int64_t replays = 0;
@@ -621,7 +739,7 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         if (remaining <= 0) break;
         if (++replays > max_replays) { rc = ISL_ERR_TIMEOUT; c->err = "batched CG made no progress"; break; }
         if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
-        c->launches += (int64_t)per_iter * BCHUNK;
+        c->launches += (int64_t)per_iter * BCHUNK + 1;
     }
     cudaGraphExecDestroy(exec);
     if (rc != ISL_OK) return rc;

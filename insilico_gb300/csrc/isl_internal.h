@@ -233,6 +233,7 @@ struct isl_ctx {
     isl::DBuf<unsigned int> dbt;  // per-instance tickets [4][ninst]
     isl::DBuf<double> dbpart;     // per-block partials [8][nblocks]
     isl::DBuf<int32_t> dbwl;      // reliable-update worklist: instances, append count, count, block offsets
+    isl::DBuf<int32_t> dbact;     // row blocks of unfinished instances: count, then the block ids
     int64_t nbblocks = 0;
     std::vector<int64_t> inst_iters;
     std::vector<double> inst_relres;
@@ -344,6 +345,7 @@ int device_dofobj_numbering(isl_ctx* c, const std::vector<DeviceLevel>& levels, 
 int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t>& slots);
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
+int time_spmv_batched(isl_ctx* c, int precision, int nrep, double* ms);
 int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc);
 bool bicgstab_kind_valid(const isl_ctx* c, int kind);
 }  // namespace isl

@@ -2137,6 +2137,7 @@ int distribute_device(isl_ctx* c, int add) {
 }
 
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
+    if (c->ninst > 1) return time_spmv_batched(c, precision, nrep, ms);
     int rc = ensure_work(c);
     if (rc != ISL_OK) return rc;
     const size_t n = (size_t)c->neq;

@@ -80,9 +80,14 @@ def lib():
         L.orc_assemble.restype = C.c_int64
         L.orc_assemble.argtypes = [_P, C.c_int, C.c_int, C.c_int]
         L.orc_get_csr.argtypes = [_P, _I64, _I64, _D, _D]
+        L.orc_build_pattern.restype = C.c_int64
+        L.orc_build_pattern.argtypes = [_P]
+        L.orc_set_element_range.argtypes = [_P, C.c_int64, C.c_int64]
         L.orc_element_matrices.argtypes = [_P, C.c_int64, C.c_int64, _D]
         L.orc_cg.restype = C.c_int64
         L.orc_cg.argtypes = [C.c_int64, _I64, _I64, _D, _D, C.c_double, C.c_int64, _D, _D, C.c_int]
+        L.orc_cg_hist.restype = C.c_int64
+        L.orc_cg_hist.argtypes = [C.c_int64, _I64, _I64, _D, _D, C.c_double, C.c_int64, _D, _D, C.c_int, _D]
         L.orc_distribute.argtypes = [_P, _D, C.c_int]
         L.orc_eval_refsol.argtypes = [C.c_int, _D, C.c_int, C.c_int64, _D, _D]
         L.orc_error_norm.restype = C.c_double
@@ -262,6 +267,18 @@ class Problem:
         self.L.orc_get_csr(self.h, _i64(rp), _i64(ci), _d(v), _d(b))
         return rp, ci, v, b
 
+    def element_range(self, e0=0, e1=-1):
+        """Limit later assemblies to elements [e0, e1) (timing samples); e1 < 0: all."""
+        self.L.orc_set_element_range(self.h, e0, e1)
+
+    def pattern(self):
+        """CSR rowptr / colind of the current numbering (no assembly)."""
+        nnz = self.L.orc_build_pattern(self.h)
+        rp = np.zeros(self.neq + 1, dtype=np.int64)
+        ci = np.zeros(nnz, dtype=np.int64)
+        self.L.orc_get_csr(self.h, _i64(rp), _i64(ci), None, None)
+        return rp, ci
+
     def element_matrices(self, e0, ne):
         nloc = self.nfun * self.ncomp
         out = np.zeros((ne, nloc, nloc))
@@ -291,8 +308,11 @@ def quadrature(shape: int, degree: int):
     return w, x.reshape(n, dim)
 
 
-def cg(rowptr, colind, val, b, tol=2.220446049250313e-16, max_iter=None, nthreads=1):
-    """Eigen-3.2 ConjugateGradient semantics (Jacobi preconditioner, x0 = 0)."""
+def cg(rowptr, colind, val, b, tol=2.220446049250313e-16, max_iter=None, nthreads=1, history=False):
+    """Eigen-3.2 ConjugateGradient semantics (Jacobi preconditioner, x0 = 0).
+
+    Returns (x, iterations, relative residual); with history=True also the
+    array of ||r||^2 / ||b||^2 after every iteration (see iters_to)."""
     n = len(b)
     if max_iter is None:
         max_iter = 2 * n
@@ -302,8 +322,19 @@ def cg(rowptr, colind, val, b, tol=2.220446049250313e-16, max_iter=None, nthread
     bb = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(n)
     rr = C.c_double(0.0)
-    it = lib().orc_cg(n, _i64(rp), _i64(ci), _d(v), _d(bb), tol, max_iter, _d(x), C.byref(rr), nthreads)
-    return x, int(it), rr.value
+    if not history:
+        it = lib().orc_cg(n, _i64(rp), _i64(ci), _d(v), _d(bb), tol, max_iter, _d(x), C.byref(rr), nthreads)
+        return x, int(it), rr.value
+    hist = np.full(max(1, max_iter), np.inf)
+    it = lib().orc_cg_hist(n, _i64(rp), _i64(ci), _d(v), _d(bb), tol, max_iter, _d(x), C.byref(rr), nthreads, _d(hist))
+    return x, int(it), rr.value, hist[:min(len(hist), int(it) + 1)]
+
+
+def iters_to(history, tol):
+    """Iterations Eigen's CG takes to ||r|| < tol ||b||, from a cg(...,
+    history=True) residual history of a solve to a tighter tolerance."""
+    hit = np.nonzero(np.asarray(history) < tol * tol)[0]
+    return int(hit[0]) if len(hit) else None
 
 
 def eval_refsol(kind, params, x):

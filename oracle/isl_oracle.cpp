@@ -448,6 +448,8 @@ struct Problem {
     std::vector<double> uval;       // current value (values_[0])
     std::vector<int64_t> eq;        // equation index or -1
     int64_t neq = 0;
+    bool patternReady = false;      // rowptr/colind hold the pattern of the current numbering
+    int64_t eBegin = 0, eEnd = -1;  // element range of orc_assemble (timing samples; -1: all)
     // kernel
     int kernel = 0;                 // 0 laplace, 1 hyperelastic, 2 heat::Static
     int material = 0;               // 0 StVenant, 1 NeoHookeanCompressible; heat::Static: 0 IsotropicConstant, 1 FenicsTest
@@ -1039,6 +1041,7 @@ int64_t orc_number(void* h) {
     int64_t c = 0;
     for (size_t k = 0; k < P->status.size(); ++k) P->eq[k] = (P->status[k] == 0) ? c++ : -1;
     P->neq = c;
+    P->patternReady = false;
     return c;
 }
 void orc_eq_index(void* h, int64_t* out) {
@@ -1141,6 +1144,25 @@ static void buildPattern(Problem& P) {
         P.rowptr[r + 1] = (int64_t)P.colind.size();
         std::vector<int64_t>().swap(v);
     }
+    P.patternReady = true;
+}
+
+// Restrict the next assemblies to elements [e0, e1) (e1 < 0: all): a bounded
+// timing sample of the element loop, whose cost is linear in the elements.
+void orc_set_element_range(void* h, int64_t e0, int64_t e1) {
+    Problem* P = (Problem*)h;
+    P->eBegin = e0;
+    P->eEnd = e1;
+}
+
+// The pattern alone (TripletContainer::registerFields,
+// base/solver/TripletContainer.hpp:158-301); returns nnz.  Later assemblies
+// of the same numbering reuse it, as the reference's pre-structured triplet
+// store does.
+int64_t orc_build_pattern(void* h) {
+    Problem* P = (Problem*)h;
+    if (!P->patternReady) buildPattern(*P);
+    return (int64_t)P->colind.size();
 }
 
 // Stiffness + force assembly following base/asmb/StiffnessMatrix.hpp:159-225,
@@ -1154,8 +1176,10 @@ static void buildPattern(Problem& P) {
 // base/solver/TripletContainer.hpp:94-102).
 int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) {
     Problem* P = (Problem*)h;
-    buildPattern(*P);
+    if (!P->patternReady) buildPattern(*P);
     const int64_t nnz = (int64_t)P->colind.size();
+    const int64_t e0 = std::max<int64_t>(0, std::min(P->eBegin, P->nelem));
+    const int64_t e1 = P->eEnd < 0 ? P->nelem : std::max(e0, std::min(P->eEnd, P->nelem));
     P->val.assign(nnz, 0.0);
     P->rhs.assign(P->neq, 0.0);
     const QuadRule Q = makeQuadrature(P->shape, P->qdeg);
@@ -1164,7 +1188,7 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
     {
         std::vector<double> Fe(nloc);
         if (with_residual) {
-            for (int64_t e = 0; e < P->nelem; ++e) {
+            for (int64_t e = e0; e < e1; ++e) {
                 elementKernel(*P, Q, e, nullptr, Fe.data());
                 for (int a = 0; a < nloc; ++a) {
                     const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
@@ -1179,7 +1203,7 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
             std::vector<double> cur = P->uval;
             for (size_t sidx = 0; sidx < P->forceW.size(); ++sidx) {
                 P->uval.assign(P->hist.begin() + sidx * ndc, P->hist.begin() + (sidx + 1) * ndc);
-                for (int64_t e = 0; e < P->nelem; ++e) {
+                for (int64_t e = e0; e < e1; ++e) {
                     elementKernel(*P, Q, e, nullptr, Fe.data());
                     for (int a = 0; a < nloc; ++a) {
                         const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
@@ -1190,7 +1214,7 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
             P->uval = cur;
         }
         if (P->bodyKind) {
-            for (int64_t e = 0; e < P->nelem; ++e) {
+            for (int64_t e = e0; e < e1; ++e) {
                 elementBody(*P, Q, e, Fe.data());
                 for (int a = 0; a < nloc; ++a) {
                     const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
@@ -1201,6 +1225,7 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
         if (P->neumannKind) {
             for (size_t i = 0; i < P->nElem.size(); ++i) {
                 const int64_t e = P->nElem[i];
+                if (e < e0 || e >= e1) continue;
                 elementNeumann(*P, e, P->nFace[i], &P->nTrac[i * nd], Fe.data());
                 for (int a = 0; a < nloc; ++a) {
                     const int64_t q = P->eq[P->edof[e * nf + a / nd] * nd + a % nd];
@@ -1221,7 +1246,7 @@ int64_t orc_assemble(void* h, int incremental, int with_residual, int nthreads) 
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
-        for (int64_t e = 0; e < P->nelem; ++e) {
+        for (int64_t e = e0; e < e1; ++e) {
             bool any = false;
             for (int a = 0; a < nloc; ++a) {
                 const size_t k = (size_t)P->edof[e * nf + a / nd] * nd + a % nd;
@@ -1314,8 +1339,17 @@ void orc_element_matrices(void* h, int64_t e0, int64_t ne, double* out) {
 // ||r||^2 < tol^2 ||b||^2 or after maxIter iterations.  Initial guess zero.
 // Works on CSR (row, col) — the matrix is symmetric, so the product equals
 // the self-adjoint product Eigen forms from the lower triangle.
+int64_t orc_cg_hist(int64_t n, const int64_t* rowptr, const int64_t* colind, const double* val, const double* b,
+                    double tol, int64_t maxIter, double* x, double* relres, int nthreads, double* rrhist);
 int64_t orc_cg(int64_t n, const int64_t* rowptr, const int64_t* colind, const double* val, const double* b, double tol,
                int64_t maxIter, double* x, double* relres, int nthreads) {
+    return orc_cg_hist(n, rowptr, colind, val, b, tol, maxIter, x, relres, nthreads, nullptr);
+}
+// The same CG; rrhist (may be NULL, else maxIter entries) receives ||r||^2 /
+// ||b||^2 after each iteration's update, so the iteration count of any looser
+// tolerance follows from one solve: the first k with rrhist[k] < tol^2.
+int64_t orc_cg_hist(int64_t n, const int64_t* rowptr, const int64_t* colind, const double* val, const double* b,
+                    double tol, int64_t maxIter, double* x, double* relres, int nthreads, double* rrhist) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -1366,6 +1400,7 @@ int64_t orc_cg(int64_t n, const int64_t* rowptr, const int64_t* colind, const do
             rr += r[i] * r[i];
         }
         resNorm2 = rr;
+        if (rrhist) rrhist[it] = resNorm2 / rhsNorm2;
         if (resNorm2 < threshold) break;
         const double absOld = absNew;
         double an = 0.0;

@@ -45,7 +45,7 @@ def rel_entry_err(a, b, floor_frac=1e-12):
     return float(np.max(np.abs(a - b) / scale))
 
 
-def oracle_newton(req, rtol=1e-10, max_newton=30, lin_tol=1e-12):
+def oracle_newton(req, rtol=1e-10, max_newton=30, lin_tol=1e-12, nthreads=1):
     """The served Newton problem on the oracle: neo-Hookean hex8 cube, x = 0
     clamped, u_x prescribed on x = 1, load steps scaled as
     solid/CompressibleDriver.hpp:165-172, Newton as :180-211."""
@@ -68,13 +68,13 @@ def oracle_newton(req, rtol=1e-10, max_newton=30, lin_tol=1e-12):
     for step in range(req.load_steps):
         P.scale_constraints(float(step + 1) if step == 0 else (step + 1) / step)
         for it in range(max_newton):
-            rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
+            rp, ci, v, b = P.assemble(incremental=True, with_residual=True, nthreads=nthreads)
             conv1 = np.linalg.norm(b) / neq
             if it == 0:
                 norm0 = conv1
             if conv1 <= rtol * norm0 and it > 0:
                 break
-            xs, _, _ = O.cg(rp, ci, v, b, tol=lin_tol)
+            xs, _, _ = O.cg(rp, ci, v, b, tol=lin_tol, nthreads=nthreads)
             P.distribute(xs, add=True)
     return P.values()
 

@@ -82,3 +82,52 @@ def test_jittered_tets_are_positive():
     a, b, c, d = (X[conn[:, i]] for i in range(4))
     det = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a)
     assert (det > 0).all()
+
+
+def _pins():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fullsize_hashes.json")) as f:
+        return json.load(f)
+
+
+def _h64(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_oracle_reproduces_c4_instance_pins(deg):
+    """The committed full-size pins are the oracle's own: the c4 instances are
+    recomputed here (the c2 / c3 pins take the same code path at 64^3)."""
+    pins = _pins()["c4_instances"]
+    for side in (8, 131, 256):
+        X, conn = W.unit_cube("quad", side, side)
+        P = O.Problem(O.QUAD, X, conn, deg, 1)
+        x, d = P.boundary_points()
+        P.constrain(d, np.zeros(len(d), dtype=np.int32), np.zeros(len(d)))
+        P.number()
+        rp, ci = P.pattern()
+        pin = pins[f"Q{deg}_side{side}"]
+        assert (P.neq, len(ci)) == (pin["neq"], pin["nnz"])
+        assert _h64(P.elem_dofobj()) == pin["elem_dofobj_sha256"]
+        assert _h64(P.eq_index()) == pin["eq_index_sha256"]
+        assert _h64(rp) == pin["rowptr_sha256"] and _h64(ci) == pin["colind_sha256"]
+
+
+@pytest.mark.parametrize("name", ["c2", "c3"])
+def test_host_pipeline_matches_full_size_pins(name):
+    """The product's host DOF pipeline at the full c2 / c3 sizes: DOF-object ids
+    and equation indices against the oracle's pins (the GPU tests check the
+    device pipeline and the CSR pattern against the same pins)."""
+    p = W.config(name)
+    pin = _pins()["configs"][name]
+    S = System(device=-1)
+    S.upload_mesh(p.shape, p.X, p.conn)
+    S.create_field(p.fedeg, p.ncomp)
+    S.constrain_boundary(p.dirichlet)
+    assert S.number_dofs() == pin["neq"]
+    assert S.ndofobj == pin["n_dofobj"]
+    assert _h64(S.elem_dofobj()) == pin["elem_dofobj_sha256"]
+    assert _h64(S.dof_index()) == pin["eq_index_sha256"]
+    S.close()

@@ -3,7 +3,11 @@
 * c1 (Q1 Poisson 64^2): the whole system against the oracle (pattern
   bit-exact, entries and RHS to 1e-12, CG solutions to 1e-9 / 1e-8).
 * c2 (hex8 elasticity 64^3, 811,200 DOFs) and c3 (tet10 Poisson 64^3,
-  2,146,689 DOF objects): properties that do not depend on size:
+  2,146,689 DOF objects): the complete per-element DOF-object ids, equation
+  indices and CSR row pointers / column indices bit for bit against the
+  oracle's (SHA-256 pins in tests/golden/fullsize_hashes.json, written by
+  tests/golden/make_fullsize_hashes.py), and properties that do not depend on
+  size:
   - patch parity: the rows of sampled DOFs (a vertex and, for tet10, the edge
     DOFs incident to it) equal the oracle's assembly of only the elements
     touching that vertex.  DOFs are mapped through (element, local function).
@@ -16,6 +20,10 @@
   - the returned solutions: the FP64 residual ||b - A x|| recomputed on the
     host, and the FP64 and mixed solutions within 1e-8 of a tight FP64 solve.
 """
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -29,6 +37,24 @@ from helpers import csr_entry_err, oracle_problem
 pytestmark = pytest.mark.gpu
 
 ENTRY_TOL = 1e-12
+with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fullsize_hashes.json")) as _f:
+    PINS = json.load(_f)
+
+
+def h64(a) -> str:
+    """SHA-256 of an integer array as little-endian int64 (the pins' format)."""
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i8").tobytes()).hexdigest()
+
+
+def check_pins(pin, S, rp, ci):
+    """The library's numbering and pattern against the oracle's pins."""
+    assert (S.nelem, S.ndofobj, S.neq, S.nnz) == (pin["n_elem"], pin["n_dofobj"], pin["neq"], pin["nnz"])
+    assert h64(S.elem_dofobj()) == pin["elem_dofobj_sha256"]
+    assert h64(S.dof_index()) == pin["eq_index_sha256"]
+    assert h64(rp) == pin["rowptr_sha256"]
+    assert h64(ci) == pin["colind_sha256"]
+
+
 TET_EDGES = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]  # local edges of tet10 DOF objects 4..9
 
 
@@ -195,6 +221,7 @@ def test_full_size_properties(name):
     S.assemble(A.PREC_FP64)
     rp, ci, v = S.csr()
     b = S.rhs()
+    check_pins(PINS["configs"][name], S, rp, ci)
     assert check_patch_rows(p, S, rp, ci, v, b) > 0
     # symmetry: both triangles come from the same staged entries
     A64 = sp.csr_matrix((v, ci, rp), shape=(S.neq, S.neq))
@@ -225,9 +252,11 @@ def poisson_instance(side, deg, seed):
 @pytest.mark.parametrize("deg", [1, 2])
 def test_c4_batch_at_full_instance_sizes(deg):
     """Batched instances at the c4 extremes (side 8 to 256): each instance's
-    numbering, pattern and FP64 values are bitwise those of the instance solved
-    alone; FP64 and mixed solves meet 1e-8 with their own convergence, and the
-    mixed solution is within 1e-8 of the tight FP64 one."""
+    pattern equals the oracle's (bit for bit; sides 8, 131 and 256 also against
+    the pinned hashes), its FP64 values and right-hand side are within 1e-12 of
+    the oracle's and bitwise those of the instance solved alone; FP64 and
+    mixed solves meet 1e-8 with their own convergence, and both solutions are
+    within 1e-8 of the oracle's FP64 CG solution."""
     from insilico_gb300.system import System
     sides = [256, 8, 131, 64, 9]
     probs = [poisson_instance(s, deg, 500 + s) for s in sides]
@@ -261,14 +290,25 @@ def test_c4_batch_at_full_instance_sizes(deg):
         np.testing.assert_array_equal(v[rp[r0]:rp[r1]], ov)
         np.testing.assert_array_equal(b[r0:r1], one.rhs())
         one.close()
+        # the oracle: the reference's pattern, entries and FP64 CG solution
+        P, (prp, pci, pv, pb) = oracle_problem(p)
+        np.testing.assert_array_equal(orp, prp)
+        np.testing.assert_array_equal(oci, pci)
+        pin = PINS["c4_instances"].get(f"Q{deg}_side{sides[k]}")
+        if pin is not None:
+            assert (P.neq, len(pci)) == (pin["neq"], pin["nnz"])
+            assert h64(orp) == pin["rowptr_sha256"] and h64(oci) == pin["colind_sha256"]
+        assert csr_entry_err(prp, pci, ov, pv) <= ENTRY_TOL
+        assert np.max(np.abs(b[r0:r1] - pb)) <= ENTRY_TOL * np.max(np.abs(pb))
+        xo, _, _ = O.cg(prp, pci, pv, pb, tol=1e-12, nthreads=os.cpu_count() or 1)
         Ak = sp.csr_matrix((ov, oci, orp), shape=(r1 - r0, r1 - r0))
         bk, tk = b[r0:r1], xt[r0:r1]
         assert np.linalg.norm(bk - Ak @ x64[r0:r1]) <= 10 * 1e-8 * np.linalg.norm(bk)
         assert np.linalg.norm(bk - Ak @ xm[r0:r1]) <= 10 * 1e-8 * np.linalg.norm(bk)
-        # at a residual tolerance the solution error follows the conditioning:
-        # the mixed solve must be as accurate as the FP64 solve at that tolerance
-        e64 = np.linalg.norm(x64[r0:r1] - tk)
-        assert np.linalg.norm(xm[r0:r1] - tk) <= max(1e-8 * np.linalg.norm(tk), 10 * e64)
+        on = np.linalg.norm(xo)
+        assert np.linalg.norm(tk - xo) <= 1e-9 * on
+        assert np.linalg.norm(x64[r0:r1] - xo) <= 1e-8 * on
+        assert np.linalg.norm(xm[r0:r1] - xo) <= 1e-8 * on
         assert it[k] > 0
     S.close()
 
