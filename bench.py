@@ -274,91 +274,147 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def serve_batch_spmv(requests, local):
+    """The dominant kernel of the served mixed path, timed alone: the batched
+    FP32 SpMV of a batch built as the server builds one (the first 16 requests
+    of the stream as instances of one context, FP32 tangent)."""
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import serve
+    from insilico_gb300.system import System
+    S = System(device=local)
+    arrs = [serve.request_arrays(r) for r in requests]
+    S.upload_batch(A.HEX, [(a["X"], a["conn"]) for a in arrs])
+    S.create_field(1, 3)
+    off = np.cumsum([0] + [len(a["X"]) for a in arrs])
+    S.constrain(np.concatenate([a["node"] + off[k] for k, a in enumerate(arrs)]),
+                np.concatenate([a["comp"] for a in arrs]), np.concatenate([a["val"] for a in arrs]))
+    S.number_dofs()
+    S.register_pattern()
+    S.set_hyperelastic("neohooke", np.concatenate([a["lam"] for a in arrs]), np.concatenate([a["mu"] for a in arrs]), 3)
+    S.set_option(A.OPT_BATCHED_SOLVE, 1)
+    S.set_option(A.OPT_SPMV32_KIND, 104)
+    S.assemble(A.PREC_FP32, incremental=True, with_residual=True)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-6, check=False)
+    ms = S.time_spmv(A.PREC_FP32, 30)
+    b = spmv_bytes(S.nnz, S.neq, 4)
+    out = {"ms": ms, "bytes": b, "neq": S.neq, "nnz": S.nnz, "instances": len(requests)}
+    S.close()
+    return out
+
+
 def run_serve(args, rank, world, local, pg):
     """c5: served neo-Hookean Newton requests (PulledSheet boundary conditions,
-    5 load steps to stretch 1.3), continuous batching over K slots.  The same
-    seeded request stream runs through the mixed server (FP32 tangent + FP32
-    CG, FP64 residual) and the plain FP64 server: closed loop (all requests
-    queued at t = 0: throughput and latency under full load) and open loop
-    (Poisson arrivals at half the plain server's closed-loop throughput)."""
+    5 load steps to stretch 1.3) through the native continuous-batching
+    server.  The same seeded request stream runs through
+      * the mixed server: batches of requests sharing every launch, FP32
+        tangent + FP32 CG to 1e-6 per Newton step (inexact Newton), FP64
+        residual;
+      * the mixed server at the plain path's linear tolerance: FP64 + FP32
+        matrices, FP32 CG with FP64 reliable updates to 1e-10;
+      * the plain path: one request per batch (no shared launches), FP64
+        tangent + FP64 CG to 1e-10, up to 8 requests at once;
+    closed loop (all requests queued at t = 0: throughput and latency under
+    full load) and open loop (Poisson arrivals at half the plain path's
+    closed-loop throughput)."""
     from insilico_gb300 import _abi as A
     from insilico_gb300 import serve
     A.load(build_if_missing=True)
     nreq = args.requests
+    arms = {
+        "mixed": dict(precision=A.PREC_FP32, max_batch=64, max_batches=4),
+        "mixed_equal_tol": dict(precision=A.PREC_MIXED, max_batch=64, max_batches=4, lin_tol=1e-10),
+        "plain": dict(precision=A.PREC_FP64, max_batch=1, max_batches=8),
+    }
     out = {}
-
-    def launches(srv):
-        return sum(sl.S.launch_count() for sl in srv.slots)
-
-    servers = {m: serve.Server(slots=args.slots, device=local, mixed=(m == "mixed")) for m in ("plain", "mixed")}
-    for m, srv in servers.items():
+    clocks = None
+    for m, kw in arms.items():
+        srv = serve.Server(device=local, **kw)
         warm = serve.make_requests(max(3, args.slots), rate=0.0, seed=W_SEED_WARM, side_range=(8, 16))
         srv.run(warm, realtime=False)
-    clk = None
-    for m in ("plain", "mixed"):
-        srv = servers[m]
-        if m == "mixed":
-            clk = Clocks(local)
-        l0 = launches(srv)
+        l0, b0 = srv.counters()
+        srv.h2d_bytes = srv.d2h_bytes = 0
+        clk = Clocks(local) if m == "mixed" else None
         done, wall = srv.run(serve.make_requests(nreq, rate=0.0), realtime=False)
-        if m == "mixed":
+        if clk is not None:
             clocks = clk.stop()
+        l1, b1 = srv.counters()
+        bad = [r.rid for r in done if r.status != A.ISL_OK]
+        if bad:
+            raise RuntimeError(f"c5 {m}: requests failed: {bad[:5]}")
         out[m] = {"closed": serve.latency_stats(done, wall), "u": {r.rid: r.u for r in done},
-                  "converged": all(r.converged for r in done), "launches": launches(srv) - l0,
-                  # per request: coordinates, connectivity (int32 on the device), lambda and mu
-                  "h2d": sum((r.side + 1) ** 3 * 24 + r.side ** 3 * (32 + 16) for r in done),
-                  "d2h": sum((r.side + 1) ** 3 * 3 * 8 for r in done)}
+                  "converged": all(r.converged for r in done), "launches": l1 - l0, "batches": b1 - b0,
+                  "h2d": srv.h2d_bytes, "d2h": srv.d2h_bytes, "srv": srv}
         log(f"c5 {m} closed loop: {out[m]['closed']}")
     rate = 0.5 * out["plain"]["closed"]["solves_per_s"]
     for m in ("plain", "mixed"):
-        done, wall = servers[m].run(serve.make_requests(nreq, rate=rate), realtime=True)
+        done, wall = out[m]["srv"].run(serve.make_requests(nreq, rate=rate), realtime=True)
         out[m]["open"] = serve.latency_stats(done, wall)
         log(f"c5 {m} open loop at {rate:.2f}/s: {out[m]['open']}")
-    for srv in servers.values():
-        srv.close()
-    cpu = None
+    for m in arms:
+        out[m]["srv"].close()
+    reqs = serve.make_requests(nreq, rate=0.0)
+    sp = serve_batch_spmv(reqs[:16], local)
+    hbm, src = peaks()
+    ach = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
+    cpu, err_oracle = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        # the reference algorithm (oracle Newton: assembly + Jacobi CG to the
-        # plain server's 1e-10 per Newton step) on the first request of the
-        # same stream, with all host threads
+        # the reference algorithm (the oracle running the reference driver:
+        # assembly + Jacobi CG to 1e-10 per Newton step) on the first request
+        # of the same stream, with all host threads
         sys.path.insert(0, os.path.join(ROOT, "tests"))
-        from helpers import oracle_newton
+        from helpers import oracle_newton_driver
         threads = os.cpu_count() or 1
-        r0 = serve.make_requests(nreq, rate=0.0)[0]
+        r0 = reqs[0]
         t0 = time.perf_counter()
-        oracle_newton(r0, lin_tol=1e-10, nthreads=threads)
+        u0, _ = oracle_newton_driver(r0, serve.NEWTON_TOL, serve.MAX_NEWTON, lin_tol=1e-10, nthreads=threads)
         tc = time.perf_counter() - t0
+        err_oracle = {m: float(np.linalg.norm(out[m]["u"][r0.rid] - u0) / np.linalg.norm(u0)) for m in arms}
         cpu = {"value": 1.0 / tc, "unit": "requests/s", "cores": threads, "kind": "port",
                "sample": f"request 0 of the stream (side {r0.side}, {3 * (r0.side + 1) ** 3} DOF components, "
-                         f"5 load steps) through the oracle's Newton loop with Jacobi CG to 1e-10: {tc:.1f} s"}
-    errs = []
-    for rid, u in out["plain"]["u"].items():
-        um = out["mixed"]["u"][rid]
-        errs.append(float(np.linalg.norm(um - u) / max(np.linalg.norm(u), 1e-300)))
-    mc, pc = out["mixed"]["closed"], out["plain"]["closed"]
+                         f"5 load steps) through the oracle's run of the reference driver with Jacobi CG to 1e-10: "
+                         f"{tc:.1f} s"}
+
+    def errs_vs_plain(m):
+        e = [float(np.linalg.norm(out[m]["u"][rid] - u) / max(np.linalg.norm(u), 1e-300))
+             for rid, u in out["plain"]["u"].items()]
+        return {"max": max(e), "median": float(np.median(e))}
+    mc, pc, ec = out["mixed"]["closed"], out["plain"]["closed"], out["mixed_equal_tol"]["closed"]
     line = {"metric": "served Newton requests/s (closed loop) at rel err<=1e-8 vs plain FP64 GPU; p50/p99 latency",
-            "value": mc["solves_per_s"], "unit": "requests/s", "n_gpus": world, "steps": nreq, "warmup": max(3, args.slots),
-            "ms_per_step": 1e3 * mc["wall_s"] / nreq, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64", "data": "synthetic (seeded Philox; no dataset)",
+            "value": mc["solves_per_s"] * world, "unit": "requests/s", "n_gpus": world, "steps": nreq,
+            "warmup": max(3, args.slots), "ms_per_step": 1e3 * mc["wall_s"] / nreq, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Philox; no dataset)",
             "config": {"workload": "c5 served hex8 neo-Hookean Newton requests, side U{8..48}, mu log-U[0.1,10], "
                                    "kappa = 10 mu, 5 load steps to stretch 1.3",
-                       "requests": nreq, "slots": args.slots, "parallelism": "single",
-                       "l2": "per-request meshes are built, assembled and solved from host inputs"},
+                       "requests": nreq, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "per-request meshes are set up, assembled and solved from host inputs"},
+            "method": "native server: batches of up to 64 requests share every launch of a Newton iteration, "
+                      "4 batches at once; FP32 tangent + FP32 CG to 1e-6, FP64 residual",
             "latency_s": {"mixed_closed": {"p50": mc["p50_s"], "p99": mc["p99_s"]},
                           "plain_closed": {"p50": pc["p50_s"], "p99": pc["p99_s"]},
                           "open_loop_rate_per_s": rate,
                           "mixed_open": {"p50": out["mixed"]["open"]["p50_s"], "p99": out["mixed"]["open"]["p99_s"]},
                           "plain_open": {"p50": out["plain"]["open"]["p50_s"], "p99": out["plain"]["open"]["p99_s"]}},
             "plain_fp64": {"requests_per_s": pc["solves_per_s"], "newton_iters": pc["newton_iters"],
-                           "cg_iters": pc["cg_iters"]},
-            "mixed": {"newton_iters": mc["newton_iters"], "cg_iters": mc["cg_iters"]},
+                           "cg_iters": pc["cg_iters"], "batches": out["plain"]["batches"]},
+            "mixed": {"newton_iters": mc["newton_iters"], "cg_iters": mc["cg_iters"], "batches": out["mixed"]["batches"],
+                      "max_batch": mc["max_batch"]},
+            "mixed_equal_lin_tol": {"requests_per_s": ec["solves_per_s"], "p50": ec["p50_s"], "p99": ec["p99_s"],
+                                    "newton_iters": ec["newton_iters"], "cg_iters": ec["cg_iters"],
+                                    "speedup_vs_plain_fp64": ec["solves_per_s"] / pc["solves_per_s"],
+                                    "rel_err_vs_plain_fp64": errs_vs_plain("mixed_equal_tol")},
             "speedup_vs_plain_fp64": mc["solves_per_s"] / pc["solves_per_s"],
-            "rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
-            "converged": out["mixed"]["converged"] and out["plain"]["converged"],
-            "e2e": {"value": mc["solves_per_s"], "unit": "requests/s",
+            "rel_err_vs_fp64": errs_vs_plain("mixed"), "rel_err_vs_oracle_request0": err_oracle,
+            "converged": all(out[m]["converged"] for m in arms),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                         "traffic": None, "kernel": "kb_sspmv<4,8> (batched FP32 SpMV of a 16-request batch, "
+                                                    "all instances active)",
+                         "bytes_per_launch": sp["bytes"], "ms_per_launch": sp["ms"], "peak_source": src,
+                         "batch": {k: sp[k] for k in ("neq", "nnz", "instances")}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": mc["solves_per_s"] * world, "unit": "requests/s",
                     "h2d_bytes_per_step": int(out["mixed"]["h2d"] / nreq),
                     "d2h_bytes_per_step": int(out["mixed"]["d2h"] / nreq)},
-            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(out["mixed"]["launches"])}
+            "clocks": clocks, "gpu_launches": int(out["mixed"]["launches"])}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -820,6 +876,7 @@ def run_single(args, rank, world, local, pg):
     split = None
     if S.get_option(A.OPT_BLOCKED):
         S.set_option(A.OPT_BLOCK_SOLVER, 0)
+        S.assemble(A.PREC_MIXED)
         tolq, errq, _ = calibrate(S, A.SOLVE_CG_FP32_IR, x_ref, REF_TOLS)
         step_mixed_point = lambda: (S.assemble(A.PREC_MIXED), S.solve(A.SOLVE_CG_FP32_IR, tol=tolq))[1]  # noqa: E731
         step_mixed_point()

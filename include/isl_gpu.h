@@ -87,6 +87,21 @@ int isl_batch_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_inst, cons
 int isl_batch_info(isl_ctx* ctx, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off);
 /* Per-instance CG iterations and final relative residuals of the last solve. */
 int isl_batch_solve_stats(isl_ctx* ctx, int64_t* iters, double* rel_res);
+/* Eigen3::norm (base/solver/Eigen3.hpp:128-138) of every instance's own
+ * system: ||v_k|| / N_k with v the solution after a solve, else the
+ * right-hand side; reduced on the device, out [n_inst].  The batched form of
+ * the convergence test of solid/CompressibleDriver.hpp:190-210. */
+int isl_batch_norms(isl_ctx* ctx, double* out);
+/* base::dof::scaleConstraints (base/dof/Distribute.hpp:75-81) with one factor
+ * per instance (factors [n_inst]): instances at different load steps. */
+int isl_batch_scale_constraints(isl_ctx* ctx, const double* factors);
+/* Instances that take part in the next solves and distributes (keep
+ * [n_inst], nonzero = take part; NULL: all).  A solve clears the right-hand
+ * side of the others, which then finish at once with x = 0, and
+ * isl_distribute leaves their DOF values as they are.  Kept until the next
+ * call or renumbering.  No reference counterpart: it lets instances whose
+ * Newton loops are at different points share one batched solve. */
+int isl_batch_set_mask(isl_ctx* ctx, const uint8_t* keep);
 
 /* Field of Lagrange degree fe_degree with ncomp components per DOF object;
  * generates the DOF-object ids per element.
@@ -236,7 +251,9 @@ int isl_solve(isl_ctx* ctx, int method, double tol, int64_t max_iter, int64_t* i
  * (b_ holds x; Eigen3::getValue base/solver/Eigen3.hpp:293-296). */
 int isl_get_solution(isl_ctx* ctx, double* x /* [n_active] */);
 int isl_get_rhs(isl_ctx* ctx, double* b /* [n_active] */);
-/* Eigen3::norm: ||b||_2 / N (base/solver/Eigen3.hpp:128-138) */
+/* Eigen3::norm: ||b||_2 / N (base/solver/Eigen3.hpp:128-138), b the
+ * right-hand side after an assembly and the solution after a solve (Eigen3's
+ * b_ holds x), reduced on the device; one double comes back. */
 int isl_norm(isl_ctx* ctx, double* out);
 /* setDoFsFromSolver (add=0) / addToDoFsFromSolver (add=1)
  * (base/dof/Distribute.hpp:139-215) */
@@ -322,7 +339,11 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * of the last solve. */
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
-       ISL_OPT_BICGSTAB_KIND = 9 };
+       ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10 };
+/* ISL_OPT_BATCHED_SOLVE (default 0): 1 runs the CG of a context holding one
+ * instance through the batched solver (per-instance scalars and reductions),
+ * so that its result is bitwise the same as when it is solved inside a batch
+ * of instances; batches always use it. */
 int isl_set_option(isl_ctx* ctx, int key, int64_t value);
 int isl_get_option(isl_ctx* ctx, int key, int64_t* value);
 
@@ -348,6 +369,98 @@ int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
  * SpMV, ms[4] FP64 update, ms[5] FP64 direction, ms[6] FP64 residual, ms[7]
  * the autotuned block SpMV variant (-1 entries: not applicable). */
 int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
+
+/* Served solves with continuous batching.  No single reference counterpart:
+ * each request is one run of solid::CompressibleDriver's load stepping and
+ * Newton loop (solid/CompressibleDriver.hpp:156-214) on its own mesh and
+ * field, and the server runs many requests on one GPU at once.
+ *
+ * A request: an isoparametric field (geometry and field of degree 1, one DOF
+ * object per node) on its own mesh; heat::Laplace (ncomp 1, coef0 = the
+ * conductivity per element) or solid::HyperElastic (ncomp = dim, material
+ * ISL_MAT_*, coef0 / coef1 = lambda / mu per element); an optional nodal body
+ * force; Dirichlet values per (node, component) for the first load step,
+ * scaled by (k+1)/k at load step k as the driver does (:164-172).  Per load
+ * step, Newton: assemble tangent and residual (incremental), stop when
+ * ||R||/N < tolerance, solve (CG to lin_tol), add the increment, stop when
+ * ||dU||/N < tolerance or after max_newton iterations (:180-211).  The
+ * request's arrays are copied at submit.
+ *
+ * The server forms batches from the queue in arrival order (same shape,
+ * ncomp, kernel, material, quadrature and lin_tol; at most max_batch
+ * requests; within the 32-bit contribution budget max_pairs and the free HBM
+ * minus reserve_bytes) and runs each batch as one context of instances on
+ * its own stream and host thread; at most max_batches batches run at once,
+ * so requests that arrive while others run are admitted as batches finish
+ * and memory frees up.  A batch shares every launch of a Newton iteration
+ * between its requests (assembly, norms, CG with per-request convergence,
+ * distribute); each request follows its own Newton loop and completes as
+ * soon as it finishes.  A request's result does not depend on its batch.
+ * precision: ISL_PREC_FP64 (FP64 tangent and CG), ISL_PREC_FP32 (FP32
+ * tangent and FP32 CG, FP64 residual: inexact Newton steps) or
+ * ISL_PREC_MIXED (FP64 and FP32 matrices, FP32 CG with FP64 reliable
+ * updates).  A failure inside a batch (for example a degenerate element)
+ * fails every request of that batch with the status and message.
+ * test_budget_bytes > 0 replaces the free-HBM figure by a fixed budget, and
+ * test_fake_us_per_elem > 0 replaces the GPU work by a sleep of that many
+ * microseconds per element (scheduler tests without a GPU). */
+typedef struct isl_server isl_server;
+typedef struct {
+    int max_batch;            /* requests per batch */
+    int max_batches;          /* batches running at once */
+    int precision;            /* ISL_PREC_* */
+    int64_t reserve_bytes;    /* HBM kept free */
+    int64_t max_pairs;        /* element pairs (n_elem * nloc^2) per batch; <= 0: 1.3e9 */
+    int64_t test_budget_bytes;
+    double test_fake_us_per_elem;
+} isl_serve_config;
+typedef struct {
+    int shape;                /* ISL_QUAD, ISL_TET, ISL_HEX */
+    int64_t n_nodes;
+    const double* coords;     /* [n_nodes][dim] */
+    int64_t n_elem;
+    const int64_t* conn;      /* [n_elem][n_vertices], hierarchic order, ids < n_nodes */
+    int ncomp;
+    int kernel;               /* ISL_KERNEL_LAPLACE or ISL_KERNEL_HYPERELASTIC */
+    int material;             /* ISL_MAT_* (HyperElastic) */
+    int quad_degree;
+    const double* coef0;      /* [n_elem] */
+    const double* coef1;      /* [n_elem] or NULL */
+    const double* body;       /* [n_nodes][ncomp] or NULL */
+    int64_t n_fixed;
+    const int64_t* fixed_node;
+    const int* fixed_comp;
+    const double* fixed_value;
+    int load_steps;
+    int max_newton;
+    double tolerance;         /* on ||R||/N and ||dU||/N */
+    double lin_tol;           /* CG: ||r|| <= lin_tol ||b|| */
+} isl_serve_request;
+typedef struct {
+    int64_t newton_iters, cg_iters, load_steps_done;
+    int converged;            /* every load step met the tolerance within max_newton */
+    int status;               /* ISL_OK or the failing isl_status */
+    double t_submit, t_admit, t_finish;  /* seconds since isl_serve_create */
+    int64_t batch_id;
+    int batch_size;
+} isl_serve_stats;
+int isl_serve_create(isl_server** out, int device, const isl_serve_config* cfg);
+/* queue a request; *ticket identifies it */
+int isl_serve_submit(isl_server* s, const isl_serve_request* req, int64_t* ticket);
+/* state: 0 queued, 1 running, 2 done, 3 failed */
+int isl_serve_poll(isl_server* s, int64_t ticket, int* state);
+/* wait up to timeout_s for the request to finish (ISL_ERR_TIMEOUT if it has not) */
+int isl_serve_wait(isl_server* s, int64_t ticket, double timeout_s, int* state);
+/* DOF values [n_nodes][ncomp] (u may be NULL) and statistics of a finished
+ * request; returns its status */
+int isl_serve_result(isl_server* s, int64_t ticket, double* u, isl_serve_stats* stats);
+const char* isl_serve_error(isl_server* s, int64_t ticket);
+/* forget a finished request */
+int isl_serve_release(isl_server* s, int64_t ticket);
+/* kernel launches of the finished batches and batches formed so far */
+int isl_serve_counters(isl_server* s, int64_t* launches, int64_t* batches);
+/* waits for the running batches; queued requests fail */
+int isl_serve_destroy(isl_server* s);
 
 /* Allocation-free FP64 CG.  This entry point has no counterpart in the
  * reference; it serves callers that must not allocate device memory while

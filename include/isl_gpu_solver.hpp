@@ -19,7 +19,8 @@
 //   time::computeResidualForceHistory        base/time/ResidualForceHistory.hpp    forceHistory(weights)
 //   dof::pushHistory                         base/dof/DegreeOfFreedom.hpp:185-190  history(n), pushHistory()
 //   number getValue(i)                       :293-296                         getValue(i)
-//   double norm(), norm(first, last)         :128-138                         norm(), norm(first, last)
+//   double norm(), norm(first, last)         :128-138                         norm() (device-reduced), norm(first, last)
+//   CompressibleDriver::solve per request    solid/CompressibleDriver.hpp:156-214  Gb300Server::submit / wait / result
 //   insertToLHS / insertToRHS                :81-124                          not offered: assembly runs on the device
 //
 // Errors: the reference aborts through VERIFY_MSG (base/verify.hpp:63-65);
@@ -124,6 +125,14 @@ public:
         int64_t nnz = 0;
         check(ctx_, isl_register_pattern(ctx_, &nnz), "isl_register_pattern");
     }
+    // base::mesh::MeshBoundary: the (element, local face) pairs seen once
+    void boundaryFaces(std::vector<int64_t>& elem, std::vector<int>& face) {
+        int64_t n = 0;
+        check(ctx_, isl_boundary_faces(ctx_, &n, nullptr, nullptr), "isl_boundary_faces");
+        elem.resize(n);
+        face.resize(n);
+        check(ctx_, isl_boundary_faces(ctx_, &n, elem.data(), face.data()), "isl_boundary_faces");
+    }
 
     // ---- kernels (per-element tabulated coefficients)
     void laplace(const std::vector<double>& kappa, int quad_degree) {
@@ -208,7 +217,13 @@ public:
         fill();
         return cache_.at(i);
     }
-    double norm() { return norm(0, n_); }
+    // ||b|| / N after an assembly, ||x|| / N after a solve (Eigen3's b_ holds
+    // x), reduced on the device
+    double norm() {
+        double v = 0.0;
+        check(ctx_, isl_norm(ctx_, &v), "isl_norm");
+        return v;
+    }
     double norm(std::size_t first, std::size_t last) {
         fill();
         double s = 0.0;
@@ -228,6 +243,47 @@ private:
     int ncomp_ = 1;
     std::size_t n_ = 0;
     std::vector<double> cache_;
+};
+
+// The served path: many CompressibleDriver runs on one GPU, batched by the
+// native server (isl_serve_*).  submit copies the request's arrays.
+class Gb300Server {
+public:
+    explicit Gb300Server(int device = 0, int precision = ISL_PREC_FP32, int max_batch = 64, int max_batches = 4,
+                         int64_t reserve_bytes = 0) {
+        isl_serve_config cfg{};
+        cfg.max_batch = max_batch;
+        cfg.max_batches = max_batches;
+        cfg.precision = precision;
+        cfg.reserve_bytes = reserve_bytes;
+        const int st = isl_serve_create(&s_, device, &cfg);
+        if (st != ISL_OK) throw gpu_error(st, "isl_serve_create");
+    }
+    ~Gb300Server() { if (s_) isl_serve_destroy(s_); }
+    Gb300Server(const Gb300Server&) = delete;
+    Gb300Server& operator=(const Gb300Server&) = delete;
+
+    int64_t submit(const isl_serve_request& r) {
+        int64_t t = 0;
+        const int st = isl_serve_submit(s_, &r, &t);
+        if (st != ISL_OK) throw gpu_error(st, "isl_serve_submit");
+        return t;
+    }
+    // blocks until the request has finished; its DOF values and statistics
+    std::vector<double> result(int64_t ticket, std::size_t ndof, isl_serve_stats* stats = nullptr) {
+        int state = 0;
+        int st = isl_serve_wait(s_, ticket, 1e9, &state);
+        if (st != ISL_OK) throw gpu_error(st, "isl_serve_wait");
+        std::vector<double> u(ndof);
+        isl_serve_stats local{};
+        st = isl_serve_result(s_, ticket, u.data(), stats ? stats : &local);
+        if (st != ISL_OK) throw gpu_error(st, std::string("served request failed: ") + isl_serve_error(s_, ticket));
+        isl_serve_release(s_, ticket);
+        return u;
+    }
+
+private:
+    isl_server* s_ = nullptr;
 };
 
 }  // namespace isl

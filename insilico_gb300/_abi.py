@@ -43,9 +43,36 @@ EXPORTED = [
     "isl_batch_solve_stats", "isl_time_kernels", "isl_cg_solve_noalloc", "isl_quadrature_points",
     "isl_error_norm", "isl_mesh_read_smf", "isl_mesh_get", "isl_mesh_write_smf", "isl_write_vtk",
     "isl_set_heat_static", "isl_set_history", "isl_push_history", "isl_set_inertia", "isl_set_force_history",
+    "isl_batch_norms", "isl_batch_scale_constraints", "isl_batch_set_mask",
+    "isl_serve_create", "isl_serve_submit", "isl_serve_poll", "isl_serve_wait", "isl_serve_result", "isl_serve_error",
+    "isl_serve_release", "isl_serve_destroy", "isl_serve_counters",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
- OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND) = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
+ OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND, OPT_BATCHED_SOLVE) = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+
+
+class ServeConfig(C.Structure):
+    """isl_serve_config"""
+    _fields_ = [("max_batch", C.c_int), ("max_batches", C.c_int), ("precision", C.c_int),
+                ("reserve_bytes", C.c_int64), ("max_pairs", C.c_int64), ("test_budget_bytes", C.c_int64),
+                ("test_fake_us_per_elem", C.c_double)]
+
+
+class ServeRequest(C.Structure):
+    """isl_serve_request"""
+    _fields_ = [("shape", C.c_int), ("n_nodes", C.c_int64), ("coords", C.POINTER(C.c_double)), ("n_elem", C.c_int64),
+                ("conn", C.POINTER(C.c_int64)), ("ncomp", C.c_int), ("kernel", C.c_int), ("material", C.c_int),
+                ("quad_degree", C.c_int), ("coef0", C.POINTER(C.c_double)), ("coef1", C.POINTER(C.c_double)),
+                ("body", C.POINTER(C.c_double)), ("n_fixed", C.c_int64), ("fixed_node", C.POINTER(C.c_int64)),
+                ("fixed_comp", C.POINTER(C.c_int)), ("fixed_value", C.POINTER(C.c_double)), ("load_steps", C.c_int),
+                ("max_newton", C.c_int), ("tolerance", C.c_double), ("lin_tol", C.c_double)]
+
+
+class ServeStats(C.Structure):
+    """isl_serve_stats"""
+    _fields_ = [("newton_iters", C.c_int64), ("cg_iters", C.c_int64), ("load_steps_done", C.c_int64),
+                ("converged", C.c_int), ("status", C.c_int), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_finish", C.c_double), ("batch_id", C.c_int64), ("batch_size", C.c_int)]
 
 
 class IslError(RuntimeError):
@@ -133,9 +160,22 @@ def load(build_if_missing: bool = False):
     L.isl_time_kernels.argtypes = [_P, i, _D]
     # device pointers are passed as integers (c_void_p)
     L.isl_cg_solve_noalloc.argtypes = [i, _P, i, _P, _P, _P, _P, _P, C.c_double, C.c_int64, _I64, _D]
+    L.isl_batch_norms.argtypes = [_P, _D]
+    L.isl_batch_scale_constraints.argtypes = [_P, _D]
+    L.isl_batch_set_mask.argtypes = [_P, C.POINTER(C.c_uint8)]
+    L.isl_serve_create.argtypes = [C.POINTER(_P), i, C.POINTER(ServeConfig)]
+    L.isl_serve_submit.argtypes = [_P, C.POINTER(ServeRequest), _I64]
+    L.isl_serve_poll.argtypes = [_P, C.c_int64, C.POINTER(C.c_int)]
+    L.isl_serve_wait.argtypes = [_P, C.c_int64, C.c_double, C.POINTER(C.c_int)]
+    L.isl_serve_result.argtypes = [_P, C.c_int64, _D, C.POINTER(ServeStats)]
+    L.isl_serve_error.argtypes = [_P, C.c_int64]
+    L.isl_serve_error.restype = C.c_char_p
+    L.isl_serve_release.argtypes = [_P, C.c_int64]
+    L.isl_serve_destroy.argtypes = [_P]
+    L.isl_serve_counters.argtypes = [_P, _I64, _I64]
     for name in EXPORTED:
         f = getattr(L, name)
-        if name != "isl_last_error":
+        if name not in ("isl_last_error", "isl_serve_error"):
             f.restype = C.c_int
     _lib = L
     return L

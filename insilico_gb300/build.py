@@ -16,7 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libisl_gpu.so")
-SOURCES = ["isl_host.cpp", "isl_assembly.cu", "isl_hyper.cu", "isl_solver.cu", "isl_batch.cu", "isl_dofmap.cu", "isl_post.cu", "isl_io.cpp", "isl_krylov.cu"]
+SOURCES = ["isl_host.cpp", "isl_assembly.cu", "isl_hyper.cu", "isl_solver.cu", "isl_batch.cu", "isl_dofmap.cu", "isl_post.cu",
+           "isl_io.cpp", "isl_krylov.cu", "isl_serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -457,6 +457,57 @@ __global__ void kb_copy(int n, const double* __restrict__ a, double* __restrict_
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
 }
 
+__global__ void kb_f2d(int n, const float* __restrict__ a, double* __restrict__ b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+
+// sum of squares of v over each row block (grid = the batch's row blocks)
+__global__ void __launch_bounds__(BBS) kb_sumsq(BArgs a, const double* __restrict__ v) {
+    __shared__ double sh[32];
+    const int r0 = a.blk_r0[blockIdx.x], r1 = a.blk_r1[blockIdx.x];
+    double s = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += BBS) s += v[i] * v[i];
+    const double t = block_sum(s, sh);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = t;
+}
+
+// ||v_k|| / N_k per instance (Eigen3::norm of each instance's system): one
+// thread per instance adds its row blocks' sums in block order
+__global__ void kb_inst_norm(BArgs a, double* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.ninst) return;
+    const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
+    double s = 0.0;
+    for (int b = b0; b < b1; ++b) s += a.part[b];
+    const int nk = a.blk_r1[b1 - 1] - a.blk_r0[b0];
+    out[k] = nk > 0 ? sqrt(s) / (double)nk : 0.0;
+}
+
+// clears the right-hand side of the instances the mask leaves out
+__global__ void __launch_bounds__(BBS) kb_mask_rhs(BArgs a, const int* __restrict__ keep, double* __restrict__ b) {
+    if (keep[a.blk_inst[blockIdx.x]]) return;
+    for (int i = a.blk_r0[blockIdx.x] + threadIdx.x; i < a.blk_r1[blockIdx.x]; i += BBS) b[i] = 0.0;
+}
+
+// setDoFsFromSolver / addToDoFsFromSolver restricted to the instances the
+// mask keeps (DOF objects of instance k: [inst_dof[k], inst_dof[k+1]))
+__global__ void kb_distribute_masked(int64_t ndc, int ncomp, const int32_t* __restrict__ eq,
+                                     const uint8_t* __restrict__ status, const double* __restrict__ cval,
+                                     const double* __restrict__ x, double* __restrict__ u, int add,
+                                     const int* __restrict__ keep, const int* __restrict__ inst_dof, int ninst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ndc; i += (int64_t)gridDim.x * blockDim.x) {
+        const int obj = (int)(i / ncomp);
+        int lo = 0, hi = ninst;  // largest lo with inst_dof[lo] <= obj
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (inst_dof[mid] <= obj) lo = mid; else hi = mid;
+        }
+        if (!keep[lo]) continue;
+        if (status[i] == 0) u[i] = add ? u[i] + x[eq[i]] : x[eq[i]];
+        else u[i] = cval[i];
+    }
+}
+
 template <typename TV, typename TX>
 void launch_kb_spmv(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, const int* rp, const int* ci, const TV* v,
                     const TX* p, TX* q) {
@@ -516,11 +567,16 @@ int ensure_batch_state(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dbpart.alloc((size_t)SUB * bi.size()));
     ISL_CHECK_CUDA(c, c->dbwl.alloc((size_t)2 * c->ninst + 3));
     ISL_CHECK_CUDA(c, c->dbact.alloc(bi.size() + 1));
+    ISL_CHECK_CUDA(c, c->dinst_dof.alloc((size_t)c->ninst + 1));
+    ISL_CHECK_CUDA(c, c->dinst_norm.alloc((size_t)c->ninst));
     cudaStream_t st = c->stream;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_inst.p, bi.data(), bi.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row0.p, b0.data(), b0.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dblk_row1.p, b1.data(), b1.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dinst_blk.p, ib.data(), ib.size() * 4, cudaMemcpyHostToDevice, st));
+    std::vector<int32_t> idof(c->ninst + 1);
+    for (int64_t k = 0; k <= c->ninst; ++k) idof[k] = (int32_t)c->inst_dof_off[k];
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dinst_dof.p, idof.data(), idof.size() * 4, cudaMemcpyHostToDevice, st));
     ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
     c->inst_iters.assign(c->ninst, 0);
     c->inst_relres.assign(c->ninst, 0.0);
@@ -609,6 +665,38 @@ int time_spmv_batched(isl_ctx* c, int precision, int nrep, double* ms) {
     return ISL_OK;
 }
 
+// ||v_k|| / N_k of every instance, v = the solution after a solve, else the
+// right-hand side (Eigen3::norm, base/solver/Eigen3.hpp:128-138, per
+// instance), reduced on the device; out: ninst host doubles.
+int inst_norms_device(isl_ctx* c, double* out) {
+    int rc = ensure_batch_state(c);
+    if (rc != ISL_OK) return rc;
+    cudaStream_t st = c->stream;
+    BArgs a = batch_args(c, 1, 0.0);
+    const double* v = c->solved ? c->dsol.p : c->drhs.p;
+    kb_sumsq<<<(unsigned)c->nbblocks, BBS, 0, st>>>(a, v);
+    kb_inst_norm<<<(unsigned)((c->ninst + 255) / 256), 256, 0, st>>>(a, c->dinst_norm.p);
+    c->launches += 2;
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(out, c->dinst_norm.p, (size_t)c->ninst * 8, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    return ISL_OK;
+}
+
+// distribute restricted to the instances of the mask (isl_batch_set_mask)
+int distribute_masked(isl_ctx* c, int add) {
+    int rc = ensure_batch_state(c);
+    if (rc != ISL_OK) return rc;
+    const int64_t ndc = c->ndofobj * c->ncomp;
+    kb_distribute_masked<<<(unsigned)c->sm_count * 8, BBS, 0, c->stream>>>(
+        ndc, c->ncomp, c->deq.p, c->dstatus.p, c->dcval.p, c->dsol.p, c->du.p, add, c->dinst_mask.p, c->dinst_dof.p,
+        (int)c->ninst);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return ISL_OK;
+}
+
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
     int rc = ensure_batch_state(c);
     if (rc != ISL_OK) return rc;
@@ -632,7 +720,15 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     const unsigned sgrid = (unsigned)std::min<int64_t>(c->nbblocks, (int64_t)c->sm_count * 6);
     const unsigned wgrid = (unsigned)c->sm_count * 4;  // the reliable-update worklist kernels
     const bool mixed = (method == ISL_SOLVE_CG_FP32_IR);
-    if (mixed && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "batched mixed solve needs the FP64 matrix (ISL_PREC_MIXED)");
+    // FP32 iterations with FP64 reliable updates when the FP64 matrix exists;
+    // after an ISL_PREC_FP32 assembly a plain FP32 CG on the iterated residual
+    const bool refine = mixed && c->have64;
+    if (mixed && !c->have32) ISL_FAIL(c, ISL_ERR_ARG, "batched FP32 solve needs an FP32 matrix");
+    if (!mixed && !c->have64) ISL_FAIL(c, ISL_ERR_ARG, "batched FP64 solve needs the FP64 matrix");
+    if (c->mask_on) {
+        kb_mask_rhs<<<grid, BBS, 0, st>>>(a, c->dinst_mask.p, c->drhs.p);
+        c->launches += 1;
+    }
     double* W = c->w64.p;
     float* V = c->w32.p;
     cudaGraph_t graph;
@@ -653,7 +749,7 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     } else {
         double *x64 = W, *r64 = W + n;
         float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n, *d32 = V + 4 * n;
-        ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
+        if (refine) ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
         kb_dinv<float, float><<<vg, BBS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
         kb_init<double, float><<<grid, BBS, 0, st>>>(a, c->drhs.p, x32, r32, p32, d32);
         ISL_CHECK_CUDA(c, cudaGetLastError());
@@ -713,12 +809,14 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         for (int k = 0; k < BCHUNK; ++k) {
             kb_dir<float><<<lgrid, BBS, 0, st>>>(a, r32, d32, p32);
             launch_kb_spmv32(c, c->bspmv32, g32, st, a, p32, q32);
-            kb_update<float><<<lgrid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, 1);
-            // reliable updates of the instances kb_update listed
-            kb_wl_scan<<<1, BBS, 0, st>>>(a);
-            kb_fold_w<<<wgrid, BBS, 0, st>>>(a, x32, x64);
-            kb_residual_w<<<wgrid, BBS, 0, st>>>(a, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64);
-            kb_restart_w<<<wgrid, BBS, 0, st>>>(a, r64, r32, d32);
+            kb_update<float><<<lgrid, BBS, 0, st>>>(a, x32, r32, p32, q32, d32, refine ? 1 : 0);
+            if (refine) {
+                // reliable updates of the instances kb_update listed
+                kb_wl_scan<<<1, BBS, 0, st>>>(a);
+                kb_fold_w<<<wgrid, BBS, 0, st>>>(a, x32, x64);
+                kb_residual_w<<<wgrid, BBS, 0, st>>>(a, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64);
+                kb_restart_w<<<wgrid, BBS, 0, st>>>(a, r64, r32, d32);
+            }
         }
         ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     }
@@ -728,7 +826,7 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
         cudaGraphDestroy(graph);
         ISL_CHECK_CUDA(c, e);
     }
-    const int per_iter = mixed ? 7 : 3;  // plus the list rebuild once per replay
+    const int per_iter = refine ? 7 : 3;  // plus the list rebuild once per replay
     const int64_t max_replays = (int64_t)a.max_iter / BCHUNK + 8;
     int remaining = ni;
     int64_t replays = 0;
@@ -743,7 +841,8 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
     }
     cudaGraphExecDestroy(exec);
     if (rc != ISL_OK) return rc;
-    kb_copy<<<vg, BBS, 0, st>>>((int)n, W, c->dsol.p);  // x (plain) or x64 (mixed) both live at W
+    if (mixed && !refine) kb_f2d<<<vg, BBS, 0, st>>>((int)n, V, c->dsol.p);  // the FP32 iterate
+    else kb_copy<<<vg, BBS, 0, st>>>((int)n, W, c->dsol.p);  // x (plain) or x64 (mixed) both live at W
     c->launches += 1;
     std::vector<int> hi((size_t)I_NI * ni);
     std::vector<double> hs((size_t)S_NS * ni);

@@ -620,6 +620,7 @@ int isl_field_create(isl_ctx* c, int fe_degree, int ncomp, int64_t* n_dofobj, in
     c->inertia = false; c->nhist = 0; c->dhist.release(); c->nforce_w = 0;
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
+    c->mask_on = false;
     c->bsell_built = false;
     c->inst_iters.clear(); c->inst_relres.clear();
     c->blocked = false;
@@ -833,6 +834,7 @@ int isl_number_dofs(isl_ctx* c, int64_t* n_active) {
     c->nnz = 0;
     c->pattern_ready = false;
     c->nbblocks = 0;
+    c->mask_on = false;
     c->bsell_built = false;
     if (c->device < 0) return ISL_OK;
     const size_t ndc = c->status.size();
@@ -864,6 +866,7 @@ int isl_register_pattern(isl_ctx* c, int64_t* nnz) {
     cudaSetDevice(c->device);
     c->spmv_lpr64 = c->spmv_lpr32 = c->bspmv_lpb = 0;
     c->nbblocks = 0;
+    c->mask_on = false;
     c->bsell_built = false;
     if (c->neq == 0) {  // every DOF constrained: an empty system, as the reference's Eigen3(0)
         c->nnz = 0;
@@ -1119,12 +1122,60 @@ int isl_norm(isl_ctx* c, double* out) {
     ISL_TRY
     if (!c || !c->pattern_ready || !out) return ISL_ERR_ARG;
     if (c->neq == 0) { *out = 0.0; return ISL_OK; }
-    std::vector<double> b(c->neq);
-    int st = isl_get_solution(c, b.data());
-    if (st) return st;
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: no system");
+    cudaSetDevice(c->device);
+    if (c->ninst == 1) return isl::inst_norms_device(c, out);
+    // one system made of the instances: sqrt(sum_k (N_k n_k)^2) / N
+    std::vector<double> per((size_t)c->ninst);
+    const int st = isl::inst_norms_device(c, per.data());
+    if (st != ISL_OK) return st;
     double s = 0.0;
-    for (double v : b) s += v * v;
+    for (int64_t k = 0; k < c->ninst; ++k) {
+        const double nk = (double)(c->inst_eq_off[k + 1] - c->inst_eq_off[k]) * per[k];
+        s += nk * nk;
+    }
     *out = std::sqrt(s) / (double)c->neq;
+    return ISL_OK;
+    ISL_CATCH(c)
+}
+
+int isl_batch_norms(isl_ctx* c, double* out) {
+    ISL_TRY
+    if (!c || !c->pattern_ready || !out) return ISL_ERR_ARG;
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context: no system");
+    if (c->neq == 0) { std::fill(out, out + c->ninst, 0.0); return ISL_OK; }
+    cudaSetDevice(c->device);
+    return isl::inst_norms_device(c, out);
+    ISL_CATCH(c)
+}
+
+int isl_batch_scale_constraints(isl_ctx* c, const double* factors) {
+    ISL_TRY
+    if (!c || !c->fedeg || !factors) return ISL_ERR_ARG;
+    if ((int64_t)c->inst_dof_off.size() != c->ninst + 1) ISL_FAIL(c, ISL_ERR_ARG, "no instances");
+    for (int64_t k = 0; k < c->ninst; ++k)
+        for (int64_t i = c->inst_dof_off[k] * c->ncomp; i < c->inst_dof_off[k + 1] * c->ncomp; ++i)
+            if (c->status[i]) c->cval[i] *= factors[k];
+    if (c->dcval.p) {
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p, c->cval.data(), c->cval.size() * 8, cudaMemcpyHostToDevice, c->stream));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return ISL_OK;
+    ISL_CATCH(c)
+}
+
+int isl_batch_set_mask(isl_ctx* c, const uint8_t* keep) {
+    ISL_TRY
+    if (!c || c->device < 0) return ISL_ERR_ARG;
+    if (!keep) { c->mask_on = false; return ISL_OK; }
+    if (c->ninst < 2) ISL_FAIL(c, ISL_ERR_ARG, "isl_batch_set_mask: a batch of instances only");
+    cudaSetDevice(c->device);
+    std::vector<int32_t> m((size_t)c->ninst);
+    for (int64_t k = 0; k < c->ninst; ++k) m[k] = keep[k] ? 1 : 0;
+    ISL_CHECK_CUDA(c, c->dinst_mask.alloc(m.size()));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dinst_mask.p, m.data(), m.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->mask_on = true;
     return ISL_OK;
     ISL_CATCH(c)
 }
@@ -1134,7 +1185,7 @@ int isl_distribute(isl_ctx* c, int add) {
     if (!c) return ISL_ERR_ARG;
     if (!c->solved) ISL_FAIL(c, ISL_ERR_ARG, "distribute: no solution");
     cudaSetDevice(c->device);
-    int st = isl::distribute_device(c, add);
+    int st = (c->mask_on && c->ninst > 1) ? isl::distribute_masked(c, add) : isl::distribute_device(c, add);
     if (st == ISL_OK) c->u_nonzero = true;
     return st;
     ISL_CATCH(c)
@@ -1256,6 +1307,7 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     ISL_TRY
     if (!c) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { c->use_block = value != 0; return ISL_OK; }
+    if (key == ISL_OPT_BATCHED_SOLVE) { c->force_batched = value != 0; return ISL_OK; }
     if (key == ISL_OPT_BARRIER_TEST) { c->barrier_test = value != 0; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) {
         if (value < 0 || value > 2) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_PERSISTENT takes 0, 1 or 2");
@@ -1289,6 +1341,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     ISL_TRY
     if (!c || !value) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
+    if (key == ISL_OPT_BATCHED_SOLVE) { *value = c->force_batched; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) { *value = c->use_persist; return ISL_OK; }
     if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
     if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }

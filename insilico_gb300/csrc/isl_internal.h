@@ -234,6 +234,11 @@ struct isl_ctx {
     isl::DBuf<double> dbpart;     // per-block partials [8][nblocks]
     isl::DBuf<int32_t> dbwl;      // reliable-update worklist: instances, append count, count, block offsets
     isl::DBuf<int32_t> dbact;     // row blocks of unfinished instances: count, then the block ids
+    isl::DBuf<int32_t> dinst_dof; // DOF-object offsets of the instances [ninst+1]
+    isl::DBuf<double> dinst_norm; // per-instance norms (isl_batch_norms)
+    isl::DBuf<int32_t> dinst_mask;// instances that take part in the next solves and distributes (isl_batch_set_mask)
+    bool mask_on = false;
+    bool force_batched = false;   // ISL_OPT_BATCHED_SOLVE: one instance through the batched solver
     int64_t nbblocks = 0;
     std::vector<int64_t> inst_iters;
     std::vector<double> inst_relres;
@@ -346,6 +351,8 @@ int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int time_spmv_batched(isl_ctx* c, int precision, int nrep, double* ms);
+int inst_norms_device(isl_ctx* c, double* out);
+int distribute_masked(isl_ctx* c, int add);
 int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc);
 bool bicgstab_kind_valid(const isl_ctx* c, int kind);
 }  // namespace isl

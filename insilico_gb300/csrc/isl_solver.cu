@@ -2093,7 +2093,7 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
     int64_t it = 0;
     double rel = 0.0;
     bool nc = false;
-    if (c->ninst > 1) {
+    if (c->ninst > 1 || (c->force_batched && method != ISL_SOLVE_BICGSTAB)) {
         rc = solve_batched(c, method, tol, max_iter, &it, &rel);
         nc = (rc == ISL_ERR_NOT_CONVERGED);
         if (rc == ISL_ERR_NOT_CONVERGED) rc = ISL_OK;
@@ -2137,7 +2137,7 @@ int distribute_device(isl_ctx* c, int add) {
 }
 
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
-    if (c->ninst > 1) return time_spmv_batched(c, precision, nrep, ms);
+    if (c->ninst > 1 || c->force_batched) return time_spmv_batched(c, precision, nrep, ms);
     int rc = ensure_work(c);
     if (rc != ISL_OK) return rc;
     const size_t n = (size_t)c->neq;

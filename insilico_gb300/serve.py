@@ -1,29 +1,24 @@
-"""Continuous-batching server for hyperelastic Newton solves (served Newton workload).
+"""Served hyperelastic Newton solves: the workload and a thin binding of the
+native server (isl_serve_* in include/isl_gpu.h, insilico_gb300/csrc/isl_serve.cpp).
 
 Each request is a compressible neo-Hookean cube (solid::HyperElastic with
 mat::hypel::NeoHookeanCompressible) on a hex8 mesh of side s, pulled along x
-in 5 load steps (reference/06-elastic/PulledSheet.hpp:35-58 boundary
-conditions, solid/CompressibleDriver.hpp:156-214 load stepping and Newton
-loop).  The server keeps every admitted request's mesh, CSR pattern, matrix
-and iterate resident on the GPU across its Newton iterations.
+in 5 load steps: x = 0 clamped, u_x prescribed on x = 1
+(reference/06-elastic/PulledSheet.hpp:35-60), the prescribed value scaled
+by (k+1)/k at load step k and Newton iterations until ||R||/N or ||dU||/N
+falls below the tolerance (solid/CompressibleDriver.hpp:156-214).
 
-Scheduling:
-  * K slots, each an isl_ctx with its own CUDA stream driven by its own host
-    thread (ctypes releases the GIL inside every library call), so the
-    assembly and CG kernels of all admitted requests overlap on the device;
-  * a request is admitted when it has arrived, a slot is free and its
-    estimated device footprint fits the free HBM minus a reserve;
-  * finished requests free their slot immediately and the next arrival is
-    admitted (continuous batching, not a FIFO of whole batches).
-
-Precision: the mixed mode assembles the tangent in FP32 with FP64 internal
-forces (ISL_PREC_FP32) and solves each Newton step inexactly with FP32 CG;
-the plain mode uses FP64 throughout (ISL_PREC_FP64 + FP64 CG).  A request's
-result does not depend on what else is running: every context computes with
-fixed-order reductions on its own buffers.
+The server (C++) forms batches of queued requests in arrival order, admits
+them by free HBM, runs each batch's Newton iterations in shared launches on
+its own stream, runs several batches at once, and completes each request as
+soon as its own Newton loop ends.  This module builds the request arrays,
+submits them (all at once, or at their Poisson arrival times from a host
+thread) and collects results and latencies; the timing is the server's own
+clock (seconds since the server was created).
 """
 from __future__ import annotations
 
+import ctypes as C
 import threading
 import time
 from dataclasses import dataclass, field
@@ -32,8 +27,14 @@ from typing import List, Optional
 import numpy as np
 
 from . import _abi as A
-from .system import System
 from . import workloads as W
+
+# Newton tolerance on ||R||/N and ||dU||/N (absolute, as the reference
+# driver's): the quadratic phase takes both below 1e-12 in 4 iterations per
+# load step for mu in [0.1, 10] on the unit cube, far above the round-off
+# floor (about 1e-19 mu)
+NEWTON_TOL = 1e-12
+MAX_NEWTON = 12
 
 
 @dataclass
@@ -47,10 +48,14 @@ class Request:
     # results
     start: float = 0.0
     finish: float = 0.0
+    submit: float = 0.0
     newton_iters: int = 0
     cg_iters: int = 0
     u: Optional[np.ndarray] = None
     converged: bool = True
+    status: int = 0
+    batch_id: int = -1
+    batch_size: int = 0
     history: list = field(default_factory=list)
 
     @property
@@ -60,7 +65,7 @@ class Request:
 
     @property
     def latency(self):
-        return self.finish - self.arrival
+        return self.finish - self.submit
 
 
 def make_requests(n: int, rate: float, seed: int = W.SEED_BASE + 4, side_range=(8, 48)) -> List[Request]:
@@ -74,162 +79,146 @@ def make_requests(n: int, rate: float, seed: int = W.SEED_BASE + 4, side_range=(
     return [Request(i, int(sides[i]), float(mus[i]), float(t[i])) for i in range(n)]
 
 
+def request_arrays(r: Request):
+    """Mesh, coefficients and first-load-step Dirichlet values of a request."""
+    X, conn = W.unit_cube("hex", r.side, r.side, r.side)
+    ne = len(conn)
+    left = np.nonzero(np.abs(X[:, 0]) < 1e-9)[0]
+    right = np.nonzero(np.abs(X[:, 0] - 1.0) < 1e-9)[0]
+    nodes = np.concatenate([np.repeat(left, 3), right]).astype(np.int64)
+    comps = np.concatenate([np.tile(np.arange(3), len(left)), np.zeros(len(right), dtype=np.int64)]).astype(np.int32)
+    vals = np.concatenate([np.zeros(3 * len(left)), np.full(len(right), r.pull / r.load_steps)])
+    return {"X": np.ascontiguousarray(X), "conn": np.ascontiguousarray(conn, dtype=np.int64),
+            "lam": np.full(ne, r.lam), "mu": np.full(ne, r.mu), "node": nodes, "comp": comps, "val": vals}
+
+
 def footprint_bytes(side: int) -> int:
-    """Estimated peak device memory of one request (pattern build included)."""
+    """Rough peak device memory of one request (the server's own estimate is
+    the one that admits)."""
     ne = side ** 3
     neq = 3 * (side + 1) ** 3
     nnz = 81 * neq
     pairs = ne * 576
-    persistent = nnz * (4 + 4 + 4 + 8) + pairs * 4 + ne * (300 * 8 + 24 * 12) + neq * 120
-    transient = pairs * 24
-    return int(persistent + transient)
-
-
-class NewtonSolver:
-    """Runs requests on one isl_ctx (one slot)."""
-
-    def __init__(self, device: int = 0, mixed: bool = True):
-        self.S = System(device=device)
-        self.mixed = mixed
-
-    def close(self):
-        self.S.close()
-
-    def run(self, r: Request, max_newton: int = 30, rtol: float = 1e-10, lin_tol_mixed: float = 1e-6,
-            lin_tol_plain: float = 1e-10):
-        S = self.S
-        X, conn = W.unit_cube("hex", r.side, r.side, r.side)
-        S.upload_mesh(A.HEX, X, conn)
-        S.create_field(1, 3)
-        first = r.pull / r.load_steps
-
-        def diri(x):
-            m = np.zeros((len(x), 3), dtype=bool)
-            v = np.zeros((len(x), 3))
-            left = np.abs(x[:, 0]) < 1e-9
-            right = np.abs(x[:, 0] - 1.0) < 1e-9
-            m[left] = True
-            m[right, 0] = True
-            v[right, 0] = first
-            return m, v
-        S.constrain_boundary(diri)
-        neq = S.number_dofs()
-        S.register_pattern()
-        ne = len(conn)
-        S.set_hyperelastic("neohooke", np.full(ne, r.lam), np.full(ne, r.mu), 3)
-        S.set_values(np.zeros(S.ndofobj * 3))
-        prec = A.PREC_FP32 if self.mixed else A.PREC_FP64
-        meth = A.SOLVE_CG_FP32_IR if self.mixed else A.SOLVE_CG_FP64
-        lin_tol = lin_tol_mixed if self.mixed else lin_tol_plain
-        r.newton_iters = r.cg_iters = 0
-        r.converged = True
-        norm0 = None
-        for step in range(r.load_steps):
-            S.scale_constraints(float(step + 1) if step == 0 else (step + 1) / step)
-            for it in range(max_newton):
-                S.assemble(prec, incremental=True, with_residual=True)
-                b = S.rhs()
-                conv1 = float(np.linalg.norm(b)) / neq
-                if norm0 is None or it == 0:
-                    norm0 = conv1 if it == 0 else norm0
-                r.history.append((step, it, conv1))
-                if conv1 <= rtol * max(norm0, 1e-300) and it > 0:
-                    break
-                cg_it, _, st = S.solve(meth, tol=lin_tol, check=False)
-                if st not in (A.ISL_OK, A.ISL_ERR_NOT_CONVERGED):
-                    S._chk(st, "isl_solve")
-                r.cg_iters += cg_it
-                S.distribute(add=True)
-                r.newton_iters += 1
-            else:
-                r.converged = False
-        r.u = S.values()
-        return r
+    return int(nnz * 28 + pairs * 28 + ne * 300 * 8 + neq * 160)
 
 
 class Server:
-    """Continuous batching over K slots with admission by free HBM."""
+    """Binding of the native continuous-batching server."""
 
-    def __init__(self, slots: int = 8, device: int = 0, mixed: bool = True, reserve_bytes: int = 8 << 30,
-                 memory_budget: Optional[int] = None, solver_factory=None):
-        make = solver_factory or (lambda: NewtonSolver(device, mixed))
-        self.slots = [make() for _ in range(slots)]
-        self.device = device
-        self.reserve = reserve_bytes
-        self.budget = memory_budget  # simulated free-HBM budget (tests); None = cudaMemGetInfo
-        self.lock = threading.Lock()
-        self.in_use = 0
+    def __init__(self, device: int = 0, precision: int = A.PREC_FP32, max_batch: int = 64, max_batches: int = 4,
+                 reserve_bytes: int = 8 << 30, lin_tol: Optional[float] = None, test_budget_bytes: int = 0,
+                 test_fake_us_per_elem: float = 0.0):
+        self.L = A.load()
+        self.precision = precision
+        self.lin_tol = lin_tol if lin_tol is not None else (1e-6 if precision == A.PREC_FP32 else 1e-10)
+        cfg = A.ServeConfig(max_batch, max_batches, precision, reserve_bytes, 0, test_budget_bytes,
+                            test_fake_us_per_elem)
+        self.h = C.c_void_p()
+        st = self.L.isl_serve_create(C.byref(self.h), device, C.byref(cfg))
+        if st != A.ISL_OK:
+            raise A.IslError(st, "isl_serve_create")
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
 
     def close(self):
-        for s in self.slots:
-            s.close()
+        if self.h:
+            self.L.isl_serve_destroy(self.h)
+            self.h = None
 
-    def free_hbm(self) -> int:
-        if self.budget is not None:
-            return self.budget - self.in_use
-        import ctypes as C
-        f, t = C.c_int64(), C.c_int64()
-        A.load().isl_device_memory(self.device, C.byref(f), C.byref(t))
-        # reservations of admitted requests count in full (conservative: part
-        # of them is already allocated and visible in the free figure)
-        return f.value - self.in_use
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
-    def run(self, requests: List[Request], realtime: bool = True):
-        """Serve requests (sorted by arrival); returns them with timings."""
-        pending = sorted(requests, key=lambda q: q.arrival)
-        free_slots = list(range(len(self.slots)))
-        done: List[Request] = []
-        cv = threading.Condition()
-        t0 = time.perf_counter()
-        active = {}
+    def submit(self, r: Request, arrays: Optional[dict] = None) -> int:
+        """Queue request r (its arrays from request_arrays unless given)."""
+        a = arrays if arrays is not None else request_arrays(r)
+        q = A.ServeRequest()
+        q.shape, q.n_nodes, q.coords = A.HEX, len(a["X"]), A.d(a["X"])
+        q.n_elem, q.conn = len(a["conn"]), A.i64(a["conn"])
+        q.ncomp, q.kernel, q.material, q.quad_degree = 3, A.KERNEL_HYPERELASTIC, A.MAT_NEOHOOKE, 3
+        q.coef0, q.coef1, q.body = A.d(a["lam"]), A.d(a["mu"]), None
+        q.n_fixed, q.fixed_node, q.fixed_comp, q.fixed_value = len(a["node"]), A.i64(a["node"]), A.i32(a["comp"]), A.d(a["val"])
+        q.load_steps, q.max_newton, q.tolerance, q.lin_tol = r.load_steps, MAX_NEWTON, NEWTON_TOL, self.lin_tol
+        t = C.c_int64()
+        st = self.L.isl_serve_submit(self.h, C.byref(q), C.byref(t))
+        if st != A.ISL_OK:
+            raise A.IslError(st, "isl_serve_submit")
+        # inputs the server copied: coordinates, connectivity, lambda, mu, Dirichlet lists
+        self.h2d_bytes += sum(v.nbytes for v in a.values())
+        return t.value
+
+    def collect(self, ticket: int, r: Request, n_nodes: int):
+        u = np.zeros(n_nodes * 3)
+        s = A.ServeStats()
+        st = self.L.isl_serve_result(self.h, ticket, A.d(u), C.byref(s))
+        r.status = st
+        if st != A.ISL_OK:
+            r.converged = False
+            r.u = None
+        else:
+            r.u = u
+            r.converged = bool(s.converged)
+            self.d2h_bytes += u.nbytes
+        r.newton_iters, r.cg_iters = int(s.newton_iters), int(s.cg_iters)
+        r.submit, r.start, r.finish = s.t_submit, s.t_admit, s.t_finish
+        r.batch_id, r.batch_size = int(s.batch_id), int(s.batch_size)
+        self.L.isl_serve_release(self.h, ticket)
+        return r
+
+    def counters(self):
+        """(kernel launches of the finished batches, batches formed)"""
+        n, b = C.c_int64(), C.c_int64()
+        self.L.isl_serve_counters(self.h, C.byref(n), C.byref(b))
+        return n.value, b.value
+
+    def error(self, ticket: int) -> str:
+        return self.L.isl_serve_error(self.h, ticket).decode()
+
+    def run(self, requests: List[Request], realtime: bool = True, timeout_s: float = 3600.0):
+        """Serve the requests; realtime: submit each at its arrival time (a
+        host thread), else all at once.  Returns (requests with results, wall
+        seconds from the first submit to the last finish)."""
+        order = sorted(requests, key=lambda q: q.arrival)
+        tickets = {}
         errors = []
 
-        def worker(slot: int, req: Request, need: int):
-            try:
-                req.start = time.perf_counter() - t0
-                self.slots[slot].run(req)
-                req.finish = time.perf_counter() - t0
-            except Exception as ex:  # reported to the caller
-                errors.append((req.rid, repr(ex)))
-                req.finish = time.perf_counter() - t0
-                req.converged = False
-            with cv:
-                free_slots.append(slot)
-                self.in_use -= need
-                done.append(req)
-                active.pop(req.rid, None)
-                cv.notify_all()
-
-        i = 0
-        with cv:
-            while i < len(pending) or active:
-                now = time.perf_counter() - t0
-                if i < len(pending) and free_slots:
-                    req = pending[i]
-                    if not realtime:
-                        req.arrival = min(req.arrival, now)
-                    need = footprint_bytes(req.side)
-                    fits = self.free_hbm() - need >= self.reserve
-                    if req.arrival <= now and (fits or not active):
-                        # a request larger than the budget still runs alone
-                        slot = free_slots.pop()
-                        self.in_use += need
-                        th = threading.Thread(target=worker, args=(slot, req, need), daemon=True)
-                        active[req.rid] = th
-                        i += 1
-                        th.start()
-                        continue
-                    wait = max(0.0, req.arrival - now) if req.arrival > now else 0.05
-                    cv.wait(timeout=min(wait, 0.05) if wait > 0 else 0.05)
-                else:
-                    cv.wait(timeout=0.05)
+        def submitter():
+            t0 = time.perf_counter()
+            for r in order:
+                if realtime:
+                    wait = r.arrival - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(wait)
+                try:
+                    tickets[r.rid] = self.submit(r)
+                except Exception as ex:  # reported to the caller
+                    errors.append((r.rid, repr(ex)))
+        th = threading.Thread(target=submitter, daemon=True)
+        th.start()
+        th.join()
+        failed = []
+        for r in order:
+            if r.rid not in tickets:
+                continue
+            state = C.c_int()
+            st = self.L.isl_serve_wait(self.h, tickets[r.rid], timeout_s, C.byref(state))
+            if st != A.ISL_OK:
+                raise A.IslError(st, f"request {r.rid} did not finish")
+            self.collect(tickets[r.rid], r, (r.side + 1) ** 3)
+            if r.status != A.ISL_OK:
+                failed.append((r.rid, r.status))
         if errors:
-            raise RuntimeError(f"requests failed: {errors[:3]}")
-        return sorted(done, key=lambda q: q.rid), time.perf_counter() - t0
+            raise RuntimeError(f"requests not submitted: {errors[:3]}")
+        done = sorted(order, key=lambda q: q.rid)
+        wall = max(r.finish for r in done) - min(r.submit for r in done)
+        return done, wall
 
 
 def latency_stats(reqs: List[Request], wall: float):
     lat = np.array([r.latency for r in reqs])
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "solves_per_s": len(reqs) / wall, "n": len(reqs), "wall_s": wall,
-            "newton_iters": int(sum(r.newton_iters for r in reqs)), "cg_iters": int(sum(r.cg_iters for r in reqs))}
+            "newton_iters": int(sum(r.newton_iters for r in reqs)), "cg_iters": int(sum(r.cg_iters for r in reqs)),
+            "batches": len({r.batch_id for r in reqs}), "max_batch": max(r.batch_size for r in reqs)}

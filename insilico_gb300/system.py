@@ -223,6 +223,25 @@ class System:
         self._chk(self.L.isl_norm(self.h, C.byref(v)))
         return v.value
 
+    def batch_norms(self):
+        """||v_k|| / N_k of every instance (isl_batch_norms)."""
+        n = C.c_int64()
+        self._chk(self.L.isl_batch_info(self.h, C.byref(n), None, None))
+        out = np.zeros(n.value)
+        self._chk(self.L.isl_batch_norms(self.h, A.d(out)), "isl_batch_norms")
+        return out
+
+    def batch_scale_constraints(self, factors):
+        f = np.ascontiguousarray(factors, dtype=np.float64)
+        self._chk(self.L.isl_batch_scale_constraints(self.h, A.d(f)), "isl_batch_scale_constraints")
+
+    def batch_set_mask(self, keep):
+        if keep is None:
+            self._chk(self.L.isl_batch_set_mask(self.h, None), "isl_batch_set_mask")
+            return
+        m = np.ascontiguousarray(np.asarray(keep, dtype=bool).astype(np.uint8))
+        self._chk(self.L.isl_batch_set_mask(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8))), "isl_batch_set_mask")
+
     def distribute(self, add: bool = False):
         self._chk(self.L.isl_distribute(self.h, int(add)), "isl_distribute")
 

@@ -95,3 +95,40 @@ def csr_entry_err(rowptr, colind, a, b):
     scale = np.maximum(np.abs(b), np.sqrt(diag[rows] * diag[colind]))
     scale = np.maximum(scale, 1e-300)
     return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / scale))
+
+
+def oracle_newton_driver(req, tol, max_newton, lin_tol=1e-12, nthreads=1):
+    """The served request on the oracle with solid/CompressibleDriver.hpp:156-214
+    itself: per load step scale the constraints by (k+1)/k, then Newton:
+    assemble, stop when ||R||/N < tol, solve, add, stop when ||dU||/N < tol
+    or after max_newton iterations.  Returns (values, Newton iterations)."""
+    X, conn = W.unit_cube("hex", req.side, req.side, req.side)
+    P = O.Problem(O.HEX, X, conn, 1, 3)
+    x, d = P.boundary_points()
+    first = req.pull / req.load_steps
+    dofs, comps, vals = [], [], []
+    for xi, di in zip(x, d):
+        if abs(xi[0]) < 1e-9:
+            for c in range(3):
+                dofs.append(di); comps.append(c); vals.append(0.0)
+        if abs(xi[0] - 1.0) < 1e-9:
+            dofs.append(di); comps.append(0); vals.append(first)
+    P.constrain(dofs, comps, vals)
+    neq = P.number()
+    ne = len(conn)
+    P.set_hyperelastic("neohooke", np.full(ne, req.lam), np.full(ne, req.mu), 3)
+    newton = 0
+    for step in range(req.load_steps):
+        P.scale_constraints(float(step + 1) if step == 0 else (step + 1) / step)
+        it = 0
+        while it < max_newton:
+            rp, ci, v, b = P.assemble(incremental=True, with_residual=True, nthreads=nthreads)
+            if np.linalg.norm(b) / neq < tol:
+                break
+            xs, _, _ = O.cg(rp, ci, v, b, tol=lin_tol, nthreads=nthreads)
+            P.distribute(xs, add=True)
+            it += 1
+            newton += 1
+            if np.linalg.norm(xs) / neq < tol:
+                break
+    return P.values(), newton

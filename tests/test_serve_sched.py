@@ -1,76 +1,88 @@
-"""Scheduler of the continuous-batching server, on CPU with a fake slot solver:
-admission by (simulated) free HBM, slots refilled as requests finish, arrival
-order respected, a failing request reported."""
-import threading
-import time
-
+"""The native server's scheduler on CPU (isl_serve_* with simulated work, no
+GPU): batches formed in arrival order up to max_batch, at most max_batches
+running at once, admission by a (simulated) free-HBM budget, arrivals
+respected, invalid requests refused at submit."""
+import numpy as np
 import pytest
 
+from insilico_gb300 import _abi as A
 from insilico_gb300 import serve
 
 
-class FakeSolver:
-    active = 0
-    peak = 0
-    lock = threading.Lock()
-
-    def __init__(self, dt=0.02, fail_rid=None):
-        self.dt = dt
-        self.fail_rid = fail_rid
-
-    def run(self, r):
-        with FakeSolver.lock:
-            FakeSolver.active += 1
-            FakeSolver.peak = max(FakeSolver.peak, FakeSolver.active)
-        time.sleep(self.dt * r.side / 8)
-        with FakeSolver.lock:
-            FakeSolver.active -= 1
-        if r.rid == self.fail_rid:
-            raise RuntimeError("injected failure")
-        r.newton_iters = 1
-        return r
-
-    def close(self):
-        pass
+def fake_server(max_batch=4, max_batches=2, budget=1 << 50, us_per_elem=0.2):
+    return serve.Server(device=0, max_batch=max_batch, max_batches=max_batches, reserve_bytes=0,
+                        test_budget_bytes=budget, test_fake_us_per_elem=us_per_elem)
 
 
-def reset():
-    FakeSolver.active = FakeSolver.peak = 0
+def max_overlap(done):
+    """Largest number of batches running at the same time."""
+    spans = {}
+    for r in done:
+        a, b = spans.get(r.batch_id, (r.start, r.finish))
+        spans[r.batch_id] = (min(a, r.start), max(b, r.finish))
+    events = sorted([(a, 1) for a, _ in spans.values()] + [(b, -1) for _, b in spans.values()])
+    cur = peak = 0
+    for _, d in events:
+        cur += d
+        peak = max(peak, cur)
+    return peak
 
 
-def test_slots_bound_concurrency_and_all_requests_finish():
-    reset()
-    reqs = serve.make_requests(24, rate=0.0)
-    srv = serve.Server(slots=4, memory_budget=1 << 50, reserve_bytes=0, solver_factory=lambda: FakeSolver(0.005))
+def test_batches_bounded_and_all_requests_finish():
+    reqs = serve.make_requests(24, rate=0.0, side_range=(4, 12))
+    srv = fake_server(max_batch=4, max_batches=2)
     done, wall = srv.run(reqs, realtime=False)
-    assert len(done) == 24 and FakeSolver.peak == 4
-    assert all(r.finish >= r.start >= r.arrival - 1e-9 for r in done)
+    srv.close()
+    assert len(done) == 24 and all(r.status == A.ISL_OK and r.converged for r in done)
+    sizes = {}
+    for r in done:
+        sizes.setdefault(r.batch_id, []).append(r.rid)
+        assert r.batch_size <= 4 and r.finish >= r.start >= r.submit
+    assert len(sizes) >= 6 and all(len(v) == done[v[0]].batch_size for v in sizes.values())
+    # batches take the queue in arrival order
+    first = {b: min(v) for b, v in sizes.items()}
+    assert [first[b] for b in sorted(first)] == sorted(first.values())
+    assert max_overlap(done) <= 2
+    assert all(np.array_equal(r.u, np.zeros(3 * (r.side + 1) ** 3)) for r in done)
 
 
-def test_admission_by_memory_budget_serialises_large_requests():
-    reset()
-    reqs = [serve.Request(i, 40, 1.0, 0.0) for i in range(6)]
-    need = serve.footprint_bytes(40)
-    srv = serve.Server(slots=4, memory_budget=int(1.5 * need), reserve_bytes=0, solver_factory=lambda: FakeSolver(0.005))
+def test_admission_by_memory_budget_runs_large_requests_one_at_a_time():
+    # a budget smaller than any request: each runs alone, admitted only when
+    # the GPU is idle (so an oversized request still runs)
+    reqs = [serve.Request(i, 20, 1.0, 0.0) for i in range(6)]
+    srv = fake_server(max_batch=8, max_batches=4, budget=1)
     done, _ = srv.run(reqs, realtime=False)
-    assert len(done) == 6 and FakeSolver.peak == 1
+    srv.close()
+    assert len(done) == 6 and all(r.batch_size == 1 for r in done)
+    assert max_overlap(done) == 1
 
 
 def test_arrivals_are_respected():
-    reset()
-    reqs = serve.make_requests(6, rate=50.0)
-    srv = serve.Server(slots=2, memory_budget=1 << 50, reserve_bytes=0, solver_factory=lambda: FakeSolver(0.002))
+    reqs = serve.make_requests(6, rate=40.0, side_range=(4, 6))
+    srv = fake_server(max_batch=8, max_batches=2)
     done, _ = srv.run(reqs, realtime=True)
+    srv.close()
+    subs = [r.submit for r in sorted(done, key=lambda q: q.arrival)]
+    assert subs == sorted(subs)
     for r in done:
-        assert r.start + 1e-3 >= r.arrival
+        assert r.start >= r.submit - 1e-9
 
 
-def test_failed_request_is_reported():
-    reset()
-    reqs = serve.make_requests(5, rate=0.0)
-    srv = serve.Server(slots=2, memory_budget=1 << 50, reserve_bytes=0, solver_factory=lambda: FakeSolver(0.001, fail_rid=3))
-    with pytest.raises(RuntimeError, match="injected failure"):
-        srv.run(reqs, realtime=False)
+def test_invalid_requests_are_refused_at_submit():
+    srv = fake_server()
+    r = serve.Request(0, 4, 1.0)
+    a = serve.request_arrays(r)
+    bad = dict(a)
+    bad["conn"] = a["conn"].copy()
+    bad["conn"][0, 0] = len(a["X"])  # node id out of range
+    with pytest.raises(A.IslError):
+        srv.submit(r, bad)
+    bad = dict(a)
+    bad["comp"] = a["comp"].copy()
+    bad["comp"][0] = 3  # component out of range
+    with pytest.raises(A.IslError):
+        srv.submit(r, bad)
+    srv.close()
 
 
 def test_footprint_grows_with_side():
