@@ -339,7 +339,23 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * of the last solve. */
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
-       ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10 };
+       ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
+       ISL_OPT_ELEM_VARIANT = 13 };
+/* ISL_OPT_TUNE_RUNS (read-only): autotunes of this context that timed their
+ * candidates; the others took their choice from the tuning cache.
+ * ISL_OPT_ELEM_VARIANT (read-only): the launch shape the element kernel
+ * autotune chose (threads per block of the one-thread-per-element kernels,
+ * elements per block of the eight-threads-per-element hexahedron kernel);
+ * 0 before the first assembly. */
+/* ISL_OPT_DIRECT_BLOCKS (read-only): 1 when the last assembly formed the
+ * matrix blocks directly: ISL_PREC_MIXED small-strain HyperElastic<StVenant>
+ * (u = 0, no body force or time-integration terms) on trilinear
+ * parallelepipeds with 2x2x2 points and a node-blocked pattern, the block
+ * solver on.  One thread per stored 3x3 block adds the blocks of the
+ * elements its two DOF objects share, in element order, in double-float
+ * arithmetic (about 48 bits), and writes the FP64 CSR values and the FP32
+ * block copies; no element matrices are staged.  The scalar FP32 CSR values
+ * are then derived from the FP64 ones when a scalar FP32 path needs them. */
 /* ISL_OPT_BATCHED_SOLVE (default 0): 1 runs the CG of a context holding one
  * instance through the batched solver (per-instance scalars and reductions),
  * so that its result is bitwise the same as when it is solved inside a batch
@@ -369,6 +385,17 @@ int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
  * SpMV, ms[4] FP64 update, ms[5] FP64 direction, ms[6] FP64 residual, ms[7]
  * the autotuned block SpMV variant (-1 entries: not applicable). */
 int isl_time_kernels(isl_ctx* ctx, int nrep, double* ms /* [8] */);
+
+/* Tuning cache of the autotuned kernel variants (the SpMV formats of the
+ * solvers, the element kernels' launch shapes), keyed by the problem class:
+ * tuner, shape, field degree, components, kernel, material, node-blocked,
+ * batched, and floor(log2(equations)).  Kept in memory for the process; with
+ * a path (or the environment variable ISL_TUNE_CACHE, read on first use) the
+ * entries are read from and appended to that text file, so later processes
+ * take the same variants without timing them.  path NULL: memory only.
+ * No reference counterpart (the reference's only knob is the compile-time
+ * thread count of its element loop, base/auxi/parallel.hpp:37-56). */
+int isl_tune_cache(const char* path);
 
 /* Served solves with continuous batching.  No single reference counterpart:
  * each request is one run of solid::CompressibleDriver's load stepping and

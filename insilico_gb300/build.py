@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libisl_gpu.so")
 SOURCES = ["isl_host.cpp", "isl_assembly.cu", "isl_hyper.cu", "isl_solver.cu", "isl_batch.cu", "isl_dofmap.cu", "isl_post.cu",
-           "isl_io.cpp", "isl_krylov.cu", "isl_serve.cpp"]
+           "isl_io.cpp", "isl_krylov.cu", "isl_serve.cpp", "isl_blocks.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

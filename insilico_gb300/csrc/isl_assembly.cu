@@ -18,6 +18,7 @@
 #include <cub/cub.cuh>
 
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include "isl_elem.cuh"
@@ -1051,16 +1052,57 @@ int pattern_build(isl_ctx* c) {
 
 // ---------------------------------------------------------------------------
 
+// Autotune of an element kernel's launch shape: on the first assembly of a
+// problem class every candidate runs once (each writes the same staged
+// values: the per-element arithmetic does not depend on the launch shape),
+// timed with CUDA events; the first candidate within 2 % of the fastest, in
+// the given preference order, is kept in the tuning cache.  Problems too small
+// to time take the first candidate.
+template <typename LAUNCH>
+static int tune_elem(isl_ctx* c, const char* tuner, const int* cand, int ncand, LAUNCH launch) {
+    int v = 0;
+    if (tune_lookup(c, tuner, &v))
+        for (int k = 0; k < ncand; ++k)
+            if (cand[k] == v) return v;
+    if (c->nelem < 20000) return cand[0];
+    float ms_of[8], best = 1e30f;
+    for (int k = 0; k < ncand && k < 8; ++k) {
+        cudaEventRecord(c->ev[2], c->stream);
+        launch(cand[k]);
+        cudaEventRecord(c->ev[3], c->stream);
+        cudaEventSynchronize(c->ev[3]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        ms_of[k] = ms;
+        best = std::min(best, ms);
+    }
+    c->launches += ncand;
+    v = cand[0];
+    for (int k = 0; k < ncand && k < 8; ++k)
+        if (ms_of[k] <= 1.02f * best) { v = cand[k]; break; }
+    tune_store(c, tuner, v);
+    return v;
+}
+
 template <int SHAPE, int FDEG, int NQ, typename R>
 static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
     HostTab h;
     if (!make_host_tables(SHAPE, FDEG, c->qdeg, h) || h.nq != NQ) ISL_FAIL(c, ISL_ERR_ARG, "quadrature");
     Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T;
     fill_tab<SHAPE, FDEG, NQ>(T, h);
-    if (A.rho || A.nfw > 0)
-        k_laplace<SHAPE, FDEG, NQ, R, true><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
-    else
-        k_laplace<SHAPE, FDEG, NQ, R, false><<<nblk(c->nelem, 128), 128, 0, c->stream>>>(A, T);
+    const bool ti = A.rho || A.nfw > 0;
+    // one thread per element: the threads per block decide the occupancy and
+    // the width of the element-major loads
+    auto launch = [&](int bs) {
+        if (ti) k_laplace<SHAPE, FDEG, NQ, R, true><<<nblk(c->nelem, bs), bs, 0, c->stream>>>(A, T);
+        else k_laplace<SHAPE, FDEG, NQ, R, false><<<nblk(c->nelem, bs), bs, 0, c->stream>>>(A, T);
+    };
+    static const int cand[3] = {128, 64, 32};
+    char tuner[48];
+    std::snprintf(tuner, sizeof tuner, "elem_laplace_q%d_r%d_t%d", NQ, (int)sizeof(R), ti ? 1 : 0);
+    const int bs = tune_elem(c, tuner, cand, 3, launch);
+    launch(bs);
+    c->elem_variant = bs;
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     return ISL_OK;
@@ -1141,26 +1183,37 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
         c->launches += 1;
         return ISL_OK;
     }
-    constexpr int EPB = 32;
-    const size_t base = (size_t)8 * 3 * EPB * 8 * 2;
-    size_t smem = base + (A.general ? (size_t)8 * 8 * 3 * EPB * 8 : 0) + (size_t)8 * 8 * 3 * EPB * sizeof(R) +
-                  (size_t)8 * EPB * sizeof(R) + (A.general ? (size_t)8 * 81 * EPB * sizeof(R) : 0);
-    int epb_run = EPB;
-    if (smem > 200 * 1024) {
-        // general FP64: halve the elements per block
-        constexpr int EPB2 = 16;
-        size_t smem2 = (size_t)8 * 3 * EPB2 * 8 * 2 + (size_t)8 * 8 * 3 * EPB2 * 8 + (size_t)8 * 8 * 3 * EPB2 * sizeof(R) +
-                       (size_t)8 * EPB2 * sizeof(R) + (size_t)8 * 81 * EPB2 * sizeof(R);
-        auto kern = ti ? k_hyper_hex8<R, EPB2, true> : k_hyper_hex8<R, EPB2, false>;
-        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-        kern<<<nblk(c->nelem, EPB2), EPB2 * 8, smem2, c->stream>>>(A, T);
-        epb_run = EPB2;
-    } else {
-        auto kern = ti ? k_hyper_hex8<R, EPB, true> : k_hyper_hex8<R, EPB, false>;
-        ISL_CHECK_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<nblk(c->nelem, EPB), EPB * 8, smem, c->stream>>>(A, T);
-    }
-    (void)epb_run;
+    // shared memory of a block of epb elements (8 threads each)
+    auto smem_of = [&](int epb) {
+        return (size_t)8 * 3 * epb * 8 * 2 + (A.general ? (size_t)8 * 8 * 3 * epb * 8 : 0) +
+               (size_t)8 * 8 * 3 * epb * sizeof(R) + (size_t)8 * epb * sizeof(R) +
+               (A.general ? (size_t)8 * 81 * epb * sizeof(R) : 0);
+    };
+    auto launch = [&](int epb) {
+        const size_t smem = smem_of(epb);
+        if (epb == 32) {
+            auto kern = ti ? k_hyper_hex8<R, 32, true> : k_hyper_hex8<R, 32, false>;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<nblk(c->nelem, 32), 32 * 8, smem, c->stream>>>(A, T);
+        } else if (epb == 16) {
+            auto kern = ti ? k_hyper_hex8<R, 16, true> : k_hyper_hex8<R, 16, false>;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<nblk(c->nelem, 16), 16 * 8, smem, c->stream>>>(A, T);
+        } else {
+            auto kern = ti ? k_hyper_hex8<R, 8, true> : k_hyper_hex8<R, 8, false>;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<nblk(c->nelem, 8), 8 * 8, smem, c->stream>>>(A, T);
+        }
+    };
+    // elements per block: the candidates whose shared memory fits
+    int cand[3], ncand = 0;
+    for (int epb : {32, 16, 8})
+        if (smem_of(epb) <= 200 * 1024) cand[ncand++] = epb;
+    char tuner[48];
+    std::snprintf(tuner, sizeof tuner, "elem_hex8_r%d_g%d_t%d", (int)sizeof(R), A.general ? 1 : 0, ti ? 1 : 0);
+    const int epb = tune_elem(c, tuner, cand, ncand, launch);
+    launch(epb);
+    c->elem_variant = epb;
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     return ISL_OK;
@@ -1210,13 +1263,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     // heat::Static, whose kernel runs in FP64 only)
     const bool k32 = (precision == ISL_PREC_FP32) && c->kernel != ISL_KERNEL_HEAT_STATIC;
     const size_t nstage = c->stage_full ? (size_t)c->nloc * c->nloc : (size_t)c->nup;
-    if (k32) {
-        ISL_CHECK_CUDA(c, c->dstageK32.alloc(nstage * E));
-    } else {
-        ISL_CHECK_CUDA(c, c->dstageK64.alloc(nstage * E));
-    }
     if (precision != ISL_PREC_FP32) ISL_CHECK_CUDA(c, c->dval64.alloc(c->nnz));
-    if (precision != ISL_PREC_FP64) ISL_CHECK_CUDA(c, c->dval32.alloc(c->nnz));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p, 0, sizeof(int), st));
     if (c->timing) cudaEventRecord(c->ev[0], st);
     ElemArgs A;
@@ -1263,7 +1310,19 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
         A.hvec = c->dhvec.p;
     }
     int rc;
-    if (c->kernel == ISL_KERNEL_LAPLACE) rc = k32 ? dispatch_laplace<float>(c, A) : dispatch_laplace<double>(c, A);
+    // mixed precision on parallelepiped hexahedra (small strain, node-blocked):
+    // element blocks straight into the FP64 CSR and the FP32 block copies
+    if (c->kernel == ISL_KERNEL_HYPERELASTIC && c->mesh_affine < 0 && c->shape == ISL_HEX && c->fedeg == 1)
+        c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
+    const bool direct = precision == ISL_PREC_MIXED && c->qdeg == 3 && !c->stage_full && affine_blocks_eligible(c, A);
+    if (!direct) {
+        if (k32) ISL_CHECK_CUDA(c, c->dstageK32.alloc(nstage * E));
+        else ISL_CHECK_CUDA(c, c->dstageK64.alloc(nstage * E));
+        if (precision != ISL_PREC_FP64) ISL_CHECK_CUDA(c, c->dval32.alloc(c->nnz));
+        A.stageK = k32 ? (void*)c->dstageK32.p : (void*)c->dstageK64.p;
+    }
+    if (direct) rc = assemble_affine_blocks(c, A);
+    else if (c->kernel == ISL_KERNEL_LAPLACE) rc = k32 ? dispatch_laplace<float>(c, A) : dispatch_laplace<double>(c, A);
     else if (c->kernel == ISL_KERNEL_HEAT_STATIC) rc = dispatch_heat_static(c, A, with_residual);
     else rc = k32 ? dispatch_hyper<float>(c, A) : dispatch_hyper<double>(c, A);
     if (rc != ISL_OK) return rc;
@@ -1271,7 +1330,10 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
         rc = dispatch_neumann(c);
         if (rc != ISL_OK) return rc;
     }
-    if (c->n_lift > 0) {
+    if (c->n_lift > 0 && direct) {
+        rc = affine_lift(c, incremental);
+        if (rc != ISL_OK) return rc;
+    } else if (c->n_lift > 0) {
         if (k32)
             k_lift<float><<<nblk(c->n_lift, 64), 64, 0, st>>>((int)c->n_lift, c->dlift_elem.p, E, c->nfun, c->ncomp, c->dedof.p,
                                                               c->dstatus.p, c->dcval.p, c->du.p, incremental, c->dstageK32.p, c->dstageF.p,
@@ -1285,15 +1347,20 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     }
     if (c->timing) cudaEventRecord(c->ev[1], st);
     const unsigned gblocks = (unsigned)std::min<long long>(nblk(c->nnz, 256), (long long)c->sm_count * 8);
-    if (k32)
+    if (direct) {
+        // the values are in place
+    } else if (k32) {
         k_gather_mat<float><<<gblocks, 256, 0, st>>>((int)c->nnz, c->dseg.p, c->dsrc.p, c->dstageK32.p, nullptr, c->dval32.p);
-    else
+        c->launches += 1;
+    } else {
         k_gather_mat<double><<<gblocks, 256, 0, st>>>((int)c->nnz, c->dseg.p, c->dsrc.p, c->dstageK64.p, c->dval64.p,
                                                       precision == ISL_PREC_MIXED ? c->dval32.p : nullptr);
+        c->launches += 1;
+    }
     const unsigned vblocks = (unsigned)std::min<long long>(nblk(c->neq, 256), (long long)c->sm_count * 8);
     k_gather_vec<<<vblocks, 256, 0, st>>>((int)c->neq, c->dsegF.p, c->dsrcF.p, c->dstageF.p, c->drhs.p);
     ISL_CHECK_CUDA(c, cudaGetLastError());
-    c->launches += 2;
+    c->launches += 1;
     if (c->timing) cudaEventRecord(c->ev[2], st);
     int flags = 0;
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(&flags, c->dflags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1308,6 +1375,11 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     c->have64 = (precision != ISL_PREC_FP32);
     c->have32 = (precision != ISL_PREC_FP64);
     c->asm_serial++;
+    // the direct path writes the FP32 block copies, not the scalar FP32 CSR
+    // values (derived on demand from the FP64 ones)
+    if (direct) c->bvals_serial = c->asm_serial;
+    else if (c->have32) c->val32_serial = c->asm_serial;
+    c->last_direct = direct;
     c->solved = false;
     if (flags & 2) ISL_FAIL(c, ISL_ERR_NAN, "non-finite stress (det F <= 0?)");
     if (flags & 1) ISL_FAIL(c, ISL_ERR_DEGENERATE, "element with det J <= 0");

@@ -786,9 +786,12 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
             // first iteration recomputes)
             const int cand[4] = {lpr, 102, 104, 108};
             const int ncand = c->ss_nslice > 0 ? 4 : 1;
-            int best = lpr;
+            int best = lpr, cached = 0;
+            if (ncand > 1 && tune_lookup(c, "bspmv_batch", &cached) &&
+                (cached == lpr || cached == 102 || cached == 104 || cached == 108))
+                c->bspmv32 = cached;
             float bestms = 1e30f;
-            for (int k2 = 0; k2 < ncand && ncand > 1; ++k2) {
+            for (int k2 = 0; k2 < ncand && ncand > 1 && !c->bspmv32; ++k2) {
                 const unsigned g2 = cand[k2] >= 100 ? sgrid : lgrid;
                 launch_kb_spmv32(c, cand[k2], g2, st, a, p32, q32);
                 cudaEventRecord(c->ev[2], st);
@@ -799,8 +802,11 @@ int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t*
                 cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
                 if (ms < bestms) { bestms = ms; best = cand[k2]; }
             }
-            c->launches += 6 * ncand;
-            c->bspmv32 = best;
+            if (!c->bspmv32) {
+                c->launches += 6 * ncand;
+                c->bspmv32 = best;
+                if (ncand > 1) tune_store(c, "bspmv_batch", best);
+            }
         }
         c->spmv_lpr32 = c->bspmv32;
         const unsigned g32 = c->bspmv32 >= 100 ? sgrid : lgrid;

@@ -107,6 +107,10 @@ struct ElemArgs {
     double fw[4];
 };
 
+// direct block assembly of small-strain elasticity on parallelepipeds (isl_blocks.cu)
+bool affine_blocks_eligible(const isl_ctx* c, const ElemArgs& A);
+int assemble_affine_blocks(isl_ctx* c, const ElemArgs& A);
+
 __host__ __device__ inline int voigt(int i, int j) {  // mat/TensorAlgebra.hpp:141-164
     const int m = (i + 1) * (j + 1);
     return m == 1 ? 0 : m == 4 ? 1 : m == 9 ? 2 : m == 2 ? 3 : m == 3 ? 4 : 5;

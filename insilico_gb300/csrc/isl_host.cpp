@@ -5,8 +5,13 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <string>
 
 #include "isl_internal.h"
 
@@ -416,6 +421,86 @@ int neumann_faces(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, c
 }  // namespace
 
 extern "C" {
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Tuning cache.  Key: tuner, element shape, field degree, components,
+// kernel, node-blocked, batched, and the size class floor(log2(equations))
+// (the rows per launch that decide which variant wins).  File format: one
+// "key value" line per entry, appended as entries are found.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+std::string g_tune_path;
+bool g_tune_init = false;
+
+void tune_read_locked(const std::string& path) {
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return;
+    char key[256];
+    int v = 0;
+    while (std::fscanf(f, "%255s %d", key, &v) == 2) g_tune[key] = v;
+    std::fclose(f);
+}
+
+void tune_init_locked() {
+    if (g_tune_init) return;
+    g_tune_init = true;
+    const char* env = std::getenv("ISL_TUNE_CACHE");
+    if (env && *env) {
+        g_tune_path = env;
+        tune_read_locked(g_tune_path);
+    }
+}
+
+std::string tune_key(const isl_ctx* c, const char* tuner) {
+    int cls = 0;
+    for (int64_t n = std::max<int64_t>(1, c->neq); n > 1; n >>= 1) ++cls;
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "%s:s%d:p%d:c%d:k%d:m%d:b%d:i%d:n%d", tuner, c->shape, c->fedeg, c->ncomp, c->kernel,
+                  c->material, c->blocked ? 1 : 0, c->ninst > 1 ? 1 : 0, cls);
+    return buf;
+}
+}  // namespace
+
+namespace isl {
+bool tune_lookup(const isl_ctx* c, const char* tuner, int* value) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_init_locked();
+    auto it = g_tune.find(tune_key(c, tuner));
+    if (it == g_tune.end()) return false;
+    *value = it->second;
+    return true;
+}
+
+void tune_store(isl_ctx* c, const char* tuner, int value) {
+    c->tune_runs++;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_init_locked();
+    const std::string key = tune_key(c, tuner);
+    g_tune[key] = value;
+    if (!g_tune_path.empty()) {
+        if (FILE* f = std::fopen(g_tune_path.c_str(), "a")) {
+            std::fprintf(f, "%s %d\n", key.c_str(), value);
+            std::fclose(f);
+        }
+    }
+}
+}  // namespace isl
+
+extern "C" {
+
+int isl_tune_cache(const char* path) {
+    ISL_TRY
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_init = true;
+    g_tune.clear();
+    g_tune_path = path ? path : "";
+    if (!g_tune_path.empty()) tune_read_locked(g_tune_path);
+    return ISL_OK;
+    ISL_CATCH(nullptr)
+}
 
 int isl_ctx_create(isl_ctx** out, int device, void* stream) {
     ISL_TRY
@@ -1153,13 +1238,17 @@ int isl_batch_scale_constraints(isl_ctx* c, const double* factors) {
     ISL_TRY
     if (!c || !c->fedeg || !factors) return ISL_ERR_ARG;
     if ((int64_t)c->inst_dof_off.size() != c->ninst + 1) ISL_FAIL(c, ISL_ERR_ARG, "no instances");
-    for (int64_t k = 0; k < c->ninst; ++k)
-        for (int64_t i = c->inst_dof_off[k] * c->ncomp; i < c->inst_dof_off[k + 1] * c->ncomp; ++i)
+    // only the instances whose factor is not 1 change (and go to the device)
+    for (int64_t k = 0; k < c->ninst; ++k) {
+        if (factors[k] == 1.0) continue;
+        const int64_t i0 = c->inst_dof_off[k] * c->ncomp, i1 = c->inst_dof_off[k + 1] * c->ncomp;
+        for (int64_t i = i0; i < i1; ++i)
             if (c->status[i]) c->cval[i] *= factors[k];
-    if (c->dcval.p) {
-        ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p, c->cval.data(), c->cval.size() * 8, cudaMemcpyHostToDevice, c->stream));
-        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->dcval.p && i1 > i0)
+            ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcval.p + i0, c->cval.data() + i0, (size_t)(i1 - i0) * 8,
+                                              cudaMemcpyHostToDevice, c->stream));
     }
+    if (c->dcval.p) ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return ISL_OK;
     ISL_CATCH(c)
 }
@@ -1342,6 +1431,9 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (!c || !value) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_BATCHED_SOLVE) { *value = c->force_batched; return ISL_OK; }
+    if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }
+    if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }
+    if (key == ISL_OPT_ELEM_VARIANT) { *value = c->elem_variant; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) { *value = c->use_persist; return ISL_OK; }
     if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
     if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }

@@ -212,6 +212,16 @@ struct isl_ctx {
     int bspmv_kind = 0;          // autotuned: 1..3 sliced-ELL (unroll 1,2,4), 4/8/16 block-row CSR lanes per row
     isl::DBuf<float> dbinv;      // SoA [9][nbr] inverse diagonal blocks
     int64_t asm_serial = 0, bsr_serial = -1;
+    int64_t val32_serial = -1;   // assembly whose values dval32 holds
+    int64_t bvals_serial = -1;   // assembly that wrote the FP32 block copies directly
+    // direct block assembly of small-strain elasticity on parallelepipeds (isl_blocks.cu)
+    isl::DBuf<float4> dgeo;      // per element: detJ Ji, Ji, lam, mu as double-float
+    isl::DBuf<int32_t> dbrobj, dadj_off, dadj, dsblk;
+    int64_t bmap_serial = -1;
+    bool last_direct = false;    // the last assembly wrote the blocks directly (ISL_OPT_DIRECT_BLOCKS)
+    int64_t tune_runs = 0;       // autotunes that timed candidates (the others came from the tuning cache)
+    int elem_variant = 0;        // autotuned launch shape of the element kernel (0: not yet chosen)
+    int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
 
     // scalar sliced-ELL copy of the FP32 matrix for the mixed solver of a
@@ -323,6 +333,11 @@ inline int fail_exception(isl_ctx* c, int code, const char* what) noexcept {
     }
 
 namespace isl {
+// Tuning cache: autotuned kernel variants per (tuner, problem class), kept
+// in memory and, when a file is set (isl_tune_cache or ISL_TUNE_CACHE), in
+// that file, so that later contexts and processes skip the timing.
+bool tune_lookup(const isl_ctx* c, const char* tuner, int* value);
+void tune_store(isl_ctx* c, const char* tuner, int value);
 // device-side entry points implemented in the .cu files
 int pattern_build(isl_ctx* c);
 int push_history_device(isl_ctx* c);
@@ -351,6 +366,8 @@ int device_boundary_slots(isl_ctx* c, const DeviceLevel& lv, std::vector<int64_t
 bool spmv32_kind_valid(const isl_ctx* c, int kind);
 int solve_batched(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres);
 int time_spmv_batched(isl_ctx* c, int precision, int nrep, double* ms);
+int ensure_val32(isl_ctx* c);
+int affine_lift(isl_ctx* c, int incremental);
 int inst_norms_device(isl_ctx* c, double* out);
 int distribute_masked(isl_ctx* c, int add);
 int solve_bicgstab(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc);

@@ -387,6 +387,8 @@ int tune_kind(isl_ctx* c) {
         while (lpr < 16 && lpr < avg / 4) lpr *= 2;
         return lpr;
     }
+    int cached = 0;
+    if (tune_lookup(c, "bicg", &cached) && cached != 0 && bicgstab_kind_valid(c, cached)) return cached;
     const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((n + KB - 1) / KB, 4LL * c->sm_count));
     if (c->wbi.n < (size_t)10 * n && c->wbi.alloc((size_t)10 * n) != cudaSuccess) return 4;
     if (c->dbis.n < 16 && c->dbis.alloc(16) != cudaSuccess) return 4;
@@ -410,6 +412,7 @@ int tune_kind(isl_ctx* c) {
         if (ms < bestms) { bestms = ms; best = cand[k]; }
     }
     c->launches += 21 * ncand;
+    tune_store(c, "bicg", best);
     return best;
 }
 

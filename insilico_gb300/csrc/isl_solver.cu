@@ -390,6 +390,8 @@ static int autotune_spmv32(isl_ctx* c, const float* p, float* q, CGScal* S, doub
     int best = 2;
     while (best < 32 && best < avg / 2) best *= 2;
     if (c->neq < 20000) return best;  // too small to time meaningfully
+    int cached = 0;
+    if (tune_lookup(c, "spmv32", &cached) && spmv32_kind_valid(c, cached)) return cached;
     // preference order; the first within 2 % of the fastest is kept, so that
     // the choice (and the rounding of p.q, which follows the grid) does not
     // flip with timing noise
@@ -412,7 +414,8 @@ static int autotune_spmv32(isl_ctx* c, const float* p, float* q, CGScal* S, doub
         bestms = std::min(bestms, ms);
     }
     for (int k = 0; k < ncand; ++k)
-        if (ms_of[k] <= 1.02f * bestms) return cand[k];
+        if (ms_of[k] <= 1.02f * bestms) { best = cand[k]; break; }
+    tune_store(c, "spmv32", best);
     return best;
 }
 
@@ -424,6 +427,9 @@ static int autotune_lpr(isl_ctx* c, const TV* val, const TX* p, TX* q, CGScal* S
     int best = 2;
     while (best < 32 && best < avg / 2) best *= 2;
     if (c->neq < 20000) return best;  // too small to time meaningfully
+    const char* tuner = sizeof(TV) == 8 ? "spmv64" : "spmv32csr";
+    int cached = 0;
+    if (tune_lookup(c, tuner, &cached) && (cached == 4 || cached == 8 || cached == 16 || cached == 32)) return cached;
     const int cand[4] = {4, 8, 16, 32};
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
@@ -440,6 +446,7 @@ static int autotune_lpr(isl_ctx* c, const TV* val, const TX* p, TX* q, CGScal* S
         cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
         if (ms < bestms) { bestms = ms; best = lpr; }
     }
+    tune_store(c, tuner, best);
     return best;
 }
 
@@ -1718,6 +1725,8 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double* part) {
     const int cand[9] = {7, 6, 5, 1, 2, 3, 4, 8, 16};  // preference order
     if (c->nbr < 8000) return 2;
+    int cached = 0;
+    if (tune_lookup(c, "bspmv", &cached) && std::find(cand, cand + 9, cached) != cand + 9) return cached;
     float ms_of[9];
     float bestms = 1e30f;
     cudaMemsetAsync(S, 0, sizeof(CGScal), c->stream);
@@ -1733,9 +1742,11 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
         ms_of[k] = ms;
         bestms = std::min(bestms, ms);
     }
+    int best = cand[0];
     for (int k = 0; k < 9; ++k)
-        if (ms_of[k] <= 1.02f * bestms) return cand[k];
-    return cand[0];
+        if (ms_of[k] <= 1.02f * bestms) { best = cand[k]; break; }
+    tune_store(c, "bspmv", best);
+    return best;
 }
 
 // detect the node-blocked structure and build the block pattern (setup)
@@ -1935,14 +1946,19 @@ static int ensure_bsr(isl_ctx* c) {
     ISL_CHECK_CUDA(c, c->dbinv.alloc((size_t)9 * c->nbr));
     ISL_CHECK_CUDA(c, c->dbval.alloc((size_t)9 * c->nblk));
     const unsigned grid = vec_grid(c);
-    k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p, c->dsdst.p,
-                                             c->dsval.p, c->dbval.p);
+    if (c->bvals_serial != c->asm_serial) {  // block copies from the FP32 CSR values
+        const int rc = ensure_val32(c);
+        if (rc != ISL_OK) return rc;
+        k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p,
+                                                 c->dsdst.p, c->dsval.p, c->dbval.p);
+        c->launches += 1;
+    }
     if (c->have64)
         k_block_jacobi<double><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval64.p, c->dbinv.p);
     else
         k_block_jacobi<float><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval32.p, c->dbinv.p);
     ISL_CHECK_CUDA(c, cudaGetLastError());
-    c->launches += 2;
+    c->launches += 1;
     c->bsr_serial = c->asm_serial;
     return ISL_OK;
 }
@@ -2087,6 +2103,11 @@ int time_bspmv(isl_ctx* c, int nrep, double* ms) {
 int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* iters, double* relres) {
     int rc = ensure_work(c);
     if (rc != ISL_OK) return rc;
+    // every FP32 path but the node-blocked one reads the scalar FP32 CSR values
+    if (method == ISL_SOLVE_CG_FP32_IR && !(c->blocked && c->use_block && c->have64 && c->ninst == 1 && !c->force_batched)) {
+        rc = ensure_val32(c);
+        if (rc != ISL_OK) return rc;
+    }
     cudaStream_t st = c->stream;
     if (max_iter <= 0) max_iter = 2 * (int64_t)c->neq;
     if (c->timing) cudaEventRecord(c->ev[0], st);
@@ -2150,6 +2171,8 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     }
     if (precision == ISL_PREC_FP32) {
         if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
+        rc = ensure_val32(c);
+        if (rc != ISL_OK) return rc;
         float* V = c->w32.p;
         ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
         rc = ensure_ssell(c);
