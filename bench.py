@@ -338,9 +338,9 @@ def run_serve(args, rank, world, local, pg):
         if clk is not None:
             clocks = clk.stop()
         l1, b1 = srv.counters()
-        bad = [r.rid for r in done if r.status != A.ISL_OK]
+        bad = [(r.rid, r.status, r.error) for r in done if r.status != A.ISL_OK]
         if bad:
-            raise RuntimeError(f"c5 {m}: requests failed: {bad[:5]}")
+            raise RuntimeError(f"c5 {m}: requests failed: {bad[:3]}")
         out[m] = {"closed": serve.latency_stats(done, wall), "u": {r.rid: r.u for r in done},
                   "converged": all(r.converged for r in done), "launches": l1 - l0, "batches": b1 - b0,
                   "h2d": srv.h2d_bytes, "d2h": srv.d2h_bytes, "srv": srv}

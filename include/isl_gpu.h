@@ -156,6 +156,13 @@ int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi);
  *     Q1 / Q2 quadrilaterals (plane strain, solid/Deformation.hpp:25-46)
  * quad_degree: base::Quadrature<DEG,SHAPE> degree (base/Quadrature.hpp:113-143). */
 int isl_set_laplace(isl_ctx* ctx, const double* kappa /* [n_elem] */, int quad_degree);
+/* heat::Laplace with a conductivity that varies inside the elements: the
+ * value of the ConductivityFun at every quadrature point
+ * (heat/Laplace.hpp:119-120 evaluates conductivityFun_(geomEp, xi) there),
+ * kappa[e * nq + q] in the order of isl_quadrature_points for the same
+ * quad_degree (nq from isl_quadrature_rule); the tangent and the residual
+ * use it.  Replaces the per-element table of isl_set_laplace. */
+int isl_set_laplace_qp(isl_ctx* ctx, const double* kappa, int quad_degree);
 int isl_set_hyperelastic(isl_ctx* ctx, int material, const double* lambda, const double* mu, int quad_degree);
 /* heat::Static (heat/Static.hpp:98-225), the nonlinear heat conduction kernel,
  * with an isotropic mat::thermal material per element: ISL_THERMAL_CONSTANT
@@ -325,8 +332,9 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
  * ISL_OPT_SPMV32_KIND: the FP32 SpMV of the scalar mixed solve, 0 (default)
  * autotuned on the matrix, 2, 4, 8, 16 or 32 CSR with that many lanes per
  * row, 102, 104 or 108 the sliced-ELL copy with 2, 4 or 8 slots of loads in
- * flight per lane (only where the copy exists); read back, the kind in use
- * (0 before the first mixed solve).  ISL_OPT_SCALAR_SLOTS (read-only): slots
+ * flight per lane (only where the copy exists, or on a batch, which builds
+ * its copy at its first mixed solve); read back, the kind in use (0 before
+ * the first mixed solve).  ISL_OPT_SCALAR_SLOTS (read-only): slots
  * of the scalar sliced-ELL copy, padding included; 0 when there is none
  * (node-blocked, batched, or fewer than 20,000 equations).
  * ISL_OPT_HOST_SETUP (default 0): with a device, isl_field_create numbers the

@@ -45,7 +45,7 @@ EXPORTED = [
     "isl_set_heat_static", "isl_set_history", "isl_push_history", "isl_set_inertia", "isl_set_force_history",
     "isl_batch_norms", "isl_batch_scale_constraints", "isl_batch_set_mask",
     "isl_serve_create", "isl_serve_submit", "isl_serve_poll", "isl_serve_wait", "isl_serve_result", "isl_serve_error",
-    "isl_serve_release", "isl_serve_destroy", "isl_serve_counters", "isl_tune_cache",
+    "isl_serve_release", "isl_serve_destroy", "isl_serve_counters", "isl_tune_cache", "isl_set_laplace_qp",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND, OPT_BATCHED_SOLVE, OPT_DIRECT_BLOCKS, OPT_TUNE_RUNS,
@@ -175,6 +175,7 @@ def load(build_if_missing: bool = False):
     L.isl_serve_destroy.argtypes = [_P]
     L.isl_serve_counters.argtypes = [_P, _I64, _I64]
     L.isl_tune_cache.argtypes = [C.c_char_p]
+    L.isl_set_laplace_qp.argtypes = [_P, _D, i]
     for name in EXPORTED:
         f = getattr(L, name)
         if name not in ("isl_last_error", "isl_serve_error"):

@@ -84,7 +84,8 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
                 for (int b = 0; b < D; ++b) s += Ji[a][b] * T.dphi[q][M][b];
                 g[M][a] = s;
             }
-        const double c = kap * detJ * T.w[q];
+        const double kq = A.kqp ? A.kqp[(size_t)q * E + e] : kap;
+        const double c = kq * detJ * T.w[q];
         const R cr = R(c);
 #pragma unroll
         for (int M = 0; M < NF; ++M)
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
                 double s = 0.0;
 #pragma unroll
                 for (int f = 0; f < NF; ++f) s += g[f][k] * uloc[f];
-                gu[k] = kap * s;
+                gu[k] = kq * s;
             }
 #pragma unroll
             for (int i = 0; i < NF; ++i) {
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
             for (int i = 0; i < NF; ++i) {
                 double dp = 0.0;
 #pragma unroll
-                for (int k = 0; k < D; ++k) dp += kap * gu[k] * g[i][k];
+                for (int k = 0; k < D; ++k) dp += kq * gu[k] * g[i][k];
                 fe[i] -= A.fw[sidx] * dp * detJ * T.w[q];
             }
         }
@@ -1287,6 +1288,7 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     A.hstride = c->ndofobj * c->ncomp;
     A.nfw = c->nforce_w;
     for (int k = 0; k < 4; ++k) A.fw[k] = k < c->nforce_w ? c->force_w[k] : 0.0;
+    A.kqp = (c->kernel == ISL_KERNEL_LAPLACE && c->has_kqp) ? c->dkqp.p : nullptr;
     // k_lift holds one element's constraint values in fixed arrays of 30
     if (c->n_lift > 0 && c->nloc > 30)
         ISL_FAIL(c, ISL_ERR_ARG, "Dirichlet values on elements with more than 30 local DOFs are not supported");

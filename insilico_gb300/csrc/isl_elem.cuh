@@ -105,6 +105,10 @@ struct ElemArgs {
     int64_t hstride;
     int nfw;
     double fw[4];
+    // heat::Laplace conductivity per quadrature point [nq][nelem] (the
+    // conductivity function at the point, heat/Laplace.hpp:119-120); null:
+    // one value per element (coef)
+    const double* kqp;
 };
 
 // direct block assembly of small-strain elasticity on parallelepipeds (isl_blocks.cu)

@@ -988,8 +988,34 @@ int isl_set_laplace(isl_ctx* c, const double* kappa, int quad_degree) {
     c->kernel = ISL_KERNEL_LAPLACE;
     c->qdeg = quad_degree;
     c->stage_full = false;
+    c->has_kqp = false;
     ISL_CHECK_CUDA(c, c->dcoef.alloc(c->nelem));
     ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dcoef.p, kappa, c->nelem * 8, cudaMemcpyHostToDevice, c->stream));
+    return ISL_OK;
+    ISL_CATCH(c)
+}
+
+int isl_set_laplace_qp(isl_ctx* c, const double* kappa, int quad_degree) {
+    ISL_TRY
+    if (!c || !c->fedeg || !kappa) return ISL_ERR_ARG;
+    if (c->ncomp != 1) ISL_FAIL(c, ISL_ERR_ARG, "Laplace needs a scalar field");
+    if (c->device < 0) ISL_FAIL(c, ISL_ERR_ARG, "host-only context");
+    std::vector<double> w, xi;
+    if (quad_degree < 1 || !quadrature(c->shape, quad_degree, w, xi)) ISL_FAIL(c, ISL_ERR_ARG, "quadrature degree");
+    const size_t nq = w.size(), E = (size_t)c->nelem;
+    // [nelem][nq] (the order of isl_quadrature_points) -> [nq][nelem]
+    std::vector<double> t(nq * E);
+    for (size_t e = 0; e < E; ++e)
+        for (size_t q = 0; q < nq; ++q) t[q * E + e] = kappa[e * nq + q];
+    c->kernel = ISL_KERNEL_LAPLACE;
+    c->qdeg = quad_degree;
+    c->stage_full = false;
+    ISL_CHECK_CUDA(c, c->dcoef.alloc(E));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dcoef.p, 0, E * 8, c->stream));
+    ISL_CHECK_CUDA(c, c->dkqp.alloc(nq * E));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dkqp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_kqp = true;
     return ISL_OK;
     ISL_CATCH(c)
 }

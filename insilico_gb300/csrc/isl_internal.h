@@ -162,6 +162,8 @@ struct isl_ctx {
     isl::DBuf<double> drho, dhist, dhvec;  // density per element, [nhist][ndofobj*ncomp], weighted history
     bool pattern_full = false;   // the contribution lists index whole element matrices
     isl::DBuf<double> dcoef;     // SoA [ncoef][nelem]
+    isl::DBuf<double> dkqp;      // Laplace conductivity per quadrature point, SoA [nq][nelem]
+    bool has_kqp = false;
     bool has_body = false;
     isl::DBuf<double> dfnodal;   // [nnodes][ncomp]
     // Neumann: faces grouped by element

@@ -359,7 +359,10 @@ static void launch_spmv32(isl_ctx* c, int kind, unsigned grid, cudaStream_t st, 
 
 bool spmv32_kind_valid(const isl_ctx* c, int kind) {
     if (kind == 0 || kind == 2 || kind == 4 || kind == 8 || kind == 16 || kind == 32) return true;
-    return (kind == 102 || kind == 104 || kind == 108) && c->ss_nslice > 0;
+    // a batch builds its sliced-ELL copy at its first mixed solve (and, should
+    // the copy not fit 32-bit slot offsets, autotunes the CSR kernels instead)
+    const bool batched = c->ninst > 1 || c->force_batched;
+    return (kind == 102 || kind == 104 || kind == 108) && (c->ss_nslice > 0 || batched);
 }
 
 // FP32 values into the scalar sliced-ELL slots (padding slots stay zero)

@@ -56,6 +56,7 @@ class Request:
     status: int = 0
     batch_id: int = -1
     batch_size: int = 0
+    error: str = ""
     history: list = field(default_factory=list)
 
     @property
@@ -157,6 +158,7 @@ class Server:
         if st != A.ISL_OK:
             r.converged = False
             r.u = None
+            r.error = self.error(ticket)
         else:
             r.u = u
             r.converged = bool(s.converged)

@@ -129,6 +129,11 @@ class System:
         self._kappa = np.ascontiguousarray(kappa, dtype=np.float64)
         self._chk(self.L.isl_set_laplace(self.h, A.d(self._kappa), quad_degree), "isl_set_laplace")
 
+    def set_laplace_qp(self, kappa, quad_degree: int):
+        """Conductivity at every quadrature point, [nelem, nq] (isl_set_laplace_qp)."""
+        self._kqp = np.ascontiguousarray(kappa, dtype=np.float64)
+        self._chk(self.L.isl_set_laplace_qp(self.h, A.d(self._kqp), quad_degree), "isl_set_laplace_qp")
+
     def set_heat_static(self, material: str, param, quad_degree: int):
         """heat::Static with mat::thermal IsotropicConstant ("constant", param =
         conductivity) or FenicsTest ("fenics", param = m), per element."""

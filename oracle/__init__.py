@@ -67,6 +67,7 @@ def lib():
         L.orc_number.argtypes = [_P]
         L.orc_eq_index.argtypes = [_P, _I64]
         L.orc_set_laplace.argtypes = [_P, _D, C.c_int]
+        L.orc_set_laplace_qp.argtypes = [_P, _D, C.c_int]
         L.orc_set_hyperelastic.argtypes = [_P, C.c_int, _D, _D, C.c_int]
         L.orc_set_heat_static.argtypes = [_P, C.c_int, _D, C.c_int]
         L.orc_set_inertia.argtypes = [_P, _D, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, _D]
@@ -203,6 +204,11 @@ class Problem:
     def set_laplace(self, kappa, qdeg):
         self._kappa = np.ascontiguousarray(kappa, dtype=np.float64)
         self.L.orc_set_laplace(self.h, _d(self._kappa), qdeg)
+
+    def set_laplace_qp(self, kappa, qdeg):
+        """heat::Laplace with the conductivity at every quadrature point, [nelem, nq]."""
+        self._kappa = np.ascontiguousarray(kappa, dtype=np.float64)
+        self.L.orc_set_laplace_qp(self.h, _d(self._kappa), qdeg)
 
     def set_hyperelastic(self, material, lam, mu, qdeg):
         self._lam = np.ascontiguousarray(lam, dtype=np.float64)

@@ -454,6 +454,7 @@ struct Problem {
     int kernel = 0;                 // 0 laplace, 1 hyperelastic, 2 heat::Static
     int material = 0;               // 0 StVenant, 1 NeoHookeanCompressible; heat::Static: 0 IsotropicConstant, 1 FenicsTest
     std::vector<double> kappa;      // per element
+    std::vector<double> kappaQ;     // per quadrature point [nelem][nq] (empty: per element)
     std::vector<double> lam, mu;    // per element
     std::vector<double> thermal;    // per element: conductivity (IsotropicConstant) or exponent m (FenicsTest)
     // inertia terms of a multi-step method (base/time/ReactionTerms.hpp:185-254)
@@ -669,7 +670,8 @@ static void elementKernel(const Problem& P, const QuadRule& Q, int64_t e, double
                 }
             }
         } else if (P.kernel == 0) {
-            const double kap = P.kappa[e];
+            // heat/Laplace.hpp:119-120: the conductivity function at the point
+            const double kap = P.kappaQ.empty() ? P.kappa[e] : P.kappaQ[(size_t)e * Q.n() + q];
             if (Ke) {
                 const double scalar = kap * detJ * w;
                 for (int M = 0; M < nf; ++M)
@@ -1053,6 +1055,16 @@ void orc_set_laplace(void* h, const double* kappa, int qdeg) {
     Problem* P = (Problem*)h;
     P->kernel = 0; P->qdeg = qdeg;
     P->kappa.assign(kappa, kappa + P->nelem);
+    P->kappaQ.clear();
+}
+// conductivity at every quadrature point of every element, [nelem][nq] in the
+// rule's point order
+void orc_set_laplace_qp(void* h, const double* kappa, int qdeg) {
+    Problem* P = (Problem*)h;
+    P->kernel = 0; P->qdeg = qdeg;
+    const QuadRule Q = makeQuadrature(P->shape, qdeg);
+    P->kappaQ.assign(kappa, kappa + (size_t)P->nelem * Q.n());
+    P->kappa.assign(P->nelem, 0.0);
 }
 void orc_set_hyperelastic(void* h, int mat, const double* lam, const double* mu, int qdeg) {
     Problem* P = (Problem*)h;

@@ -314,15 +314,18 @@ def test_c4_batch_at_full_instance_sizes(deg):
 
 
 def test_c5_requests_at_full_size():
-    """Served neo-Hookean requests at the largest c5 sides: the plain FP64 and
-    the mixed servers converge and agree within 1e-8."""
+    """Served neo-Hookean requests at the largest c5 sides, batched together:
+    the plain FP64 server (one request per batch) and the mixed server
+    converge and agree within 1e-8."""
     from insilico_gb300 import serve
     reqs = [serve.Request(0, side=48, mu=0.37), serve.Request(1, side=29, mu=6.1)]
     out = {}
-    for mixed in (False, True):
-        solver = serve.NewtonSolver(mixed=mixed)
-        out[mixed] = [solver.run(serve.Request(r.rid, r.side, r.mu)) for r in reqs]
-        solver.close()
-    for rp_, rm in zip(out[False], out[True]):
+    for prec, mb in ((A.PREC_FP64, 1), (A.PREC_FP32, 8)):
+        srv = serve.Server(precision=prec, max_batch=mb, max_batches=2)
+        out[prec], _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
+        srv.close()
+    assert out[A.PREC_FP32][0].batch_size == 2
+    for rp_, rm in zip(out[A.PREC_FP64], out[A.PREC_FP32]):
+        assert rp_.status == A.ISL_OK and rm.status == A.ISL_OK
         assert rp_.converged and rm.converged
         assert np.linalg.norm(rm.u - rp_.u) <= 1e-8 * np.linalg.norm(rp_.u)

@@ -15,7 +15,7 @@ from helpers import csr_entry_err
 pytestmark = pytest.mark.gpu
 
 
-def _both(kind, shape, deg, sizes, material, seed):
+def _both(kind, shape, deg, sizes, material, seed, qdeg=2):
     """the same heat::Static problem on the GPU and on the oracle, at random
     nonnegative DOF values (u > -1 for the FenicsTest law)"""
     X, conn = W.unit_cube(kind, *sizes)
@@ -28,7 +28,7 @@ def _both(kind, shape, deg, sizes, material, seed):
     S.constrain_boundary(mask_fun)
     S.number_dofs()
     S.register_pattern()
-    S.set_heat_static(material, prm, 2)
+    S.set_heat_static(material, prm, qdeg)
     u = rng.uniform(0.0, 0.5, S.ndofobj)
     S.set_values(u)
     P = O.Problem({A.QUAD: O.QUAD, A.TET: O.TET, A.HEX: O.HEX}[shape], X, conn, deg, 1)
@@ -36,17 +36,18 @@ def _both(kind, shape, deg, sizes, material, seed):
     on = np.abs(x[:, 0]) < 1e-9
     P.constrain(d[on], np.zeros(on.sum()), np.full(on.sum(), 0.25))
     P.number()
-    P.set_heat_static(material, prm, 2)
+    P.set_heat_static(material, prm, qdeg)
     P.set_values(u)
     return S, P
 
 
-@pytest.mark.parametrize("kind,shape,deg,sizes", [
-    ("quad", A.QUAD, 2, (6, 5)), ("quad", A.QUAD, 1, (9, 7)), ("tet", A.TET, 2, (3, 2, 2)), ("hex", A.HEX, 1, (3, 3, 2)),
+@pytest.mark.parametrize("kind,shape,deg,sizes,qdeg", [
+    ("quad", A.QUAD, 2, (6, 5), 2), ("quad", A.QUAD, 1, (9, 7), 2), ("tet", A.TET, 2, (3, 2, 2), 2),
+    ("hex", A.HEX, 1, (3, 3, 2), 2), ("tet", A.TET, 2, (3, 2, 2), 4),  # 11-point rule (2 x field degree)
 ])
 @pytest.mark.parametrize("material", ["fenics", "constant"])
-def test_heat_static_tangent_and_residual_match_oracle(kind, shape, deg, sizes, material):
-    S, P = _both(kind, shape, deg, sizes, material, 5)
+def test_heat_static_tangent_and_residual_match_oracle(kind, shape, deg, sizes, qdeg, material):
+    S, P = _both(kind, shape, deg, sizes, material, 5, qdeg)
     S.assemble(A.PREC_FP64, incremental=True, with_residual=True)
     rp, ci, v, b = P.assemble(incremental=True, with_residual=True)
     srp, sci, sv = S.csr()

@@ -75,6 +75,7 @@ def _cos_product(alpha, x):
 @pytest.mark.parametrize("kind,shape,deg,sizes,qdeg", [
     ("quad", A.QUAD, 2, (9, 7), 3), ("quad", A.QUAD, 1, (12, 10), 2), ("tet", A.TET, 2, (3, 4, 2), 2),
     ("hex", A.HEX, 1, (4, 3, 5), 3), ("tet", A.TET, 1, (3, 3, 3), 1),
+    ("tet", A.TET, 2, (3, 4, 2), 4),  # the 11-point rule of P2 tetrahedra
 ])
 def test_error_norms_match_oracle(kind, shape, deg, sizes, qdeg):
     """L2 and H1 errors of an arbitrary field against u = prod cos(alpha x):

@@ -27,7 +27,7 @@ def test_served_newton_matches_oracle_driver(precision):
     srv = serve.Server(precision=precision, max_batch=8, max_batches=2)
     done, _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
     srv.close()
-    assert all(r.status == A.ISL_OK and r.converged for r in done)
+    assert all(r.status == A.ISL_OK and r.converged for r in done), [(r.status, r.error) for r in done]
     assert len({r.batch_id for r in done}) == 1  # one batch of three
     for r, got in zip(reqs, done):
         uo, newton = oracle_newton_driver(r, serve.NEWTON_TOL, serve.MAX_NEWTON)
