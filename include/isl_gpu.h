@@ -83,7 +83,7 @@ int isl_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_nodes, const dou
 int isl_batch_mesh_upload(isl_ctx* ctx, int shape, int dim, int64_t n_inst, const int64_t* node_off, const double* coords,
                           const int64_t* elem_off, const int64_t* conn);
 /* n_inst, equation offsets [n_inst+1] and DOF-object offsets [n_inst+1] of the
- * instances (either array may be NULL). */
+ * instances (any of the three may be NULL). */
 int isl_batch_info(isl_ctx* ctx, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off);
 /* Per-instance CG iterations and final relative residuals of the last solve. */
 int isl_batch_solve_stats(isl_ctx* ctx, int64_t* iters, double* rel_res);

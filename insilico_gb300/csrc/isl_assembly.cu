@@ -19,8 +19,10 @@
 
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 #include <vector>
 
+#include "isl_df.cuh"
 #include "isl_elem.cuh"
 #include "isl_internal.h"
 
@@ -32,9 +34,20 @@ namespace isl {
 //   F[i]    -= kappa grad u . grad phi_i detJ w           heat/Laplace.hpp:150-183 (x -1)
 //   F[s]    += f(x) phi_s w detJ                          base/asmb/BodyForce.hpp:172-205
 // TI: the time-integration terms (mass matrix, weighted history, residual
-// forces at past states) are compiled in; the plain assembly runs without them
-template <int SHAPE, int FDEG, int NQ, typename R, bool TI>
-__global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T) {
+// forces at past states) are compiled in; the plain assembly runs without them.
+// DF (mixed precision): the stiffness sum runs in double-float on the FP32 pipe
+// (isl_df.cuh: about 48 significant bits; FP32 runs at about 64 times the
+// FP64 rate here), from the FP64 Jacobian and the double-float shape-function
+// gradients TD.dphi; one FP64 addition per entry forms the staged FP64 value.
+// The forces stay in FP64.
+template <int D, int NF, int NQ>
+struct TabDF {
+    df dphi[NQ][NF][D];
+};
+
+template <int SHAPE, int FDEG, int NQ, typename R, bool TI, bool DF = false>
+__global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T,
+                                                 const TabDF<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NF, NQ> TD) {
     constexpr int D = ET<SHAPE, FDEG>::D, NG = ET<SHAPE, FDEG>::NG, NF = ET<SHAPE, FDEG>::NF;
     constexpr int NUP = NF * (NF + 1) / 2;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -63,39 +76,76 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 #pragma unroll
         for (int f = 0; f < NF; ++f) hloc[f] = A.hvec[A.edof[f * E + e]];
     }
-    R acc[NUP];
+    constexpr int NACC = DF ? 1 : NUP;
+    R acc[NACC];
 #pragma unroll
-    for (int u = 0; u < NUP; ++u) acc[u] = R(0);
+    for (int u = 0; u < NACC; ++u) acc[u] = R(0);
+    constexpr int NACCD = DF ? NUP : 1;
+    df accd[NACCD];
+#pragma unroll
+    for (int u = 0; u < NACCD; ++u) accd[u] = df{0.f, 0.f};
     double fe[NF];
 #pragma unroll
     for (int f = 0; f < NF; ++f) fe[f] = 0.0;
     bool bad = false;
+    // the FP64 gradients feed the forces (and the FP64 / FP32 stiffness)
+    const bool need_g = !DF || A.fnodal || A.with_residual || TI;
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
         if (!aff) detJ = jac<NG, D>(X, T.dN[q], Ji);
         bad |= !(detJ > 0.0);
         double g[NF][D];
+        if (need_g) {
 #pragma unroll
-        for (int M = 0; M < NF; ++M)
+            for (int M = 0; M < NF; ++M)
 #pragma unroll
-            for (int a = 0; a < D; ++a) {
-                double s = 0.0;
+                for (int a = 0; a < D; ++a) {
+                    double s = 0.0;
 #pragma unroll
-                for (int b = 0; b < D; ++b) s += Ji[a][b] * T.dphi[q][M][b];
-                g[M][a] = s;
-            }
+                    for (int b = 0; b < D; ++b) s += Ji[a][b] * T.dphi[q][M][b];
+                    g[M][a] = s;
+                }
+        }
         const double kq = A.kqp ? A.kqp[(size_t)q * E + e] : kap;
         const double c = kq * detJ * T.w[q];
-        const R cr = R(c);
+        if constexpr (DF) {
+            df Jd[D][D];
 #pragma unroll
-        for (int M = 0; M < NF; ++M)
+            for (int a = 0; a < D; ++a)
 #pragma unroll
-            for (int N = M; N < NF; ++N) {
-                R dot = R(0);
+                for (int b = 0; b < D; ++b) Jd[a][b] = df_from_double(Ji[a][b]);
+            df gd[NF][D];
 #pragma unroll
-                for (int k = 0; k < D; ++k) dot += R(g[M][k]) * R(g[N][k]);
-                acc[upidx(M, N, NF)] += dot * cr;
-            }
+            for (int M = 0; M < NF; ++M)
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    df s = df_mul(Jd[a][0], TD.dphi[q][M][0]);
+#pragma unroll
+                    for (int b = 1; b < D; ++b) s = df_add(s, df_mul(Jd[a][b], TD.dphi[q][M][b]));
+                    gd[M][a] = s;
+                }
+            const df cd = df_from_double(c);
+#pragma unroll
+            for (int M = 0; M < NF; ++M)
+#pragma unroll
+                for (int N = M; N < NF; ++N) {
+                    df dot = df_mul(gd[M][0], gd[N][0]);
+#pragma unroll
+                    for (int k = 1; k < D; ++k) dot = df_add(dot, df_mul(gd[M][k], gd[N][k]));
+                    accd[upidx(M, N, NF)] = df_add_acc(accd[upidx(M, N, NF)], df_mul(dot, cd));
+                }
+        } else {
+            const R cr = R(c);
+#pragma unroll
+            for (int M = 0; M < NF; ++M)
+#pragma unroll
+                for (int N = M; N < NF; ++N) {
+                    R dot = R(0);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) dot += R(g[M][k]) * R(g[N][k]);
+                    acc[upidx(M, N, NF)] += dot * cr;
+                }
+        }
         if (A.fnodal) {
             double f = 0.0;
 #pragma unroll
@@ -111,7 +161,11 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
 #pragma unroll
             for (int M = 0; M < NF; ++M) {
 #pragma unroll
-                for (int N = M; N < NF; ++N) acc[upidx(M, N, NF)] += R(A.mass_w * m * T.phi[q][M] * T.phi[q][N]);
+                for (int N = M; N < NF; ++N) {
+                    const double mv = A.mass_w * m * T.phi[q][M] * T.phi[q][N];
+                    if constexpr (DF) accd[upidx(M, N, NF)] = df_add_acc(accd[upidx(M, N, NF)], df_from_double(mv));
+                    else acc[upidx(M, N, NF)] += R(mv);
+                }
                 fe[M] += m * T.phi[q][M] * hq;
             }
         }
@@ -153,8 +207,13 @@ __global__ void __launch_bounds__(128) k_laplace(const ElemArgs A, const Tab<ET<
     }
     if (bad) atomicOr(A.flags, 1);
     R* SK = (R*)A.stageK;
+    if constexpr (DF) {
 #pragma unroll
-    for (int u = 0; u < NUP; ++u) SK[(size_t)e * NUP + u] = acc[u];
+        for (int u = 0; u < NUP; ++u) SK[(size_t)e * NUP + u] = R(df_to_double(accd[u]));
+    } else {
+#pragma unroll
+        for (int u = 0; u < NUP; ++u) SK[(size_t)e * NUP + u] = acc[u];
+    }
 #pragma unroll
     for (int s = 0; s < NF; ++s) A.stageF[(size_t)s * E + e] = fe[s];
 }
@@ -1092,15 +1151,27 @@ static int launch_laplace(isl_ctx* c, const ElemArgs& A) {
     Tab<ET<SHAPE, FDEG>::D, ET<SHAPE, FDEG>::NG, ET<SHAPE, FDEG>::NF, NQ> T;
     fill_tab<SHAPE, FDEG, NQ>(T, h);
     const bool ti = A.rho || A.nfw > 0;
+    constexpr int D = ET<SHAPE, FDEG>::D, NF = ET<SHAPE, FDEG>::NF;
+    TabDF<D, NF, NQ> TD;
+    for (int q = 0; q < NQ; ++q)
+        for (int f = 0; f < NF; ++f)
+            for (int d = 0; d < D; ++d) TD.dphi[q][f][d] = df_from_double(T.dphi[q][f][d]);
+    // the mixed assembly (FP64 stage from double-float sums; its FP64 values
+    // feed the FP32 copy and the reliable updates); the plain FP64 path keeps
+    // FP64 arithmetic
+    constexpr bool R64 = std::is_same<R, double>::value;
+    const bool dfm = R64 && c->asm_precision == ISL_PREC_MIXED;
     // one thread per element: the threads per block decide the occupancy and
     // the width of the element-major loads
     auto launch = [&](int bs) {
-        if (ti) k_laplace<SHAPE, FDEG, NQ, R, true><<<nblk(c->nelem, bs), bs, 0, c->stream>>>(A, T);
-        else k_laplace<SHAPE, FDEG, NQ, R, false><<<nblk(c->nelem, bs), bs, 0, c->stream>>>(A, T);
+        const unsigned g = nblk(c->nelem, bs);
+        if (ti) k_laplace<SHAPE, FDEG, NQ, R, true><<<g, bs, 0, c->stream>>>(A, T, TD);
+        else if (dfm) k_laplace<SHAPE, FDEG, NQ, R, false, R64><<<g, bs, 0, c->stream>>>(A, T, TD);
+        else k_laplace<SHAPE, FDEG, NQ, R, false><<<g, bs, 0, c->stream>>>(A, T, TD);
     };
     static const int cand[3] = {128, 64, 32};
     char tuner[48];
-    std::snprintf(tuner, sizeof tuner, "elem_laplace_q%d_r%d_t%d", NQ, (int)sizeof(R), ti ? 1 : 0);
+    std::snprintf(tuner, sizeof tuner, "elem_laplace_q%d_r%d_t%d_d%d", NQ, (int)sizeof(R), ti ? 1 : 0, dfm ? 1 : 0);
     const int bs = tune_elem(c, tuner, cand, 3, launch);
     launch(bs);
     c->elem_variant = bs;
@@ -1259,6 +1330,7 @@ static int dispatch_neumann(isl_ctx* c) {
 
 int assemble_device(isl_ctx* c, int precision, int incremental, int with_residual) {
     cudaStream_t st = c->stream;
+    c->asm_precision = precision;
     const int E = (int)c->nelem;
     // the tangent (stiffness) is staged in FP32 only for ISL_PREC_FP32 (not for
     // heat::Static, whose kernel runs in FP64 only)

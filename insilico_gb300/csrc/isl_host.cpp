@@ -1504,8 +1504,8 @@ int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes) {
 
 int isl_batch_info(isl_ctx* c, int64_t* n_inst, int64_t* eq_off, int64_t* dofobj_off) {
     ISL_TRY
-    if (!c || !n_inst) return ISL_ERR_ARG;
-    *n_inst = c->ninst;
+    if (!c) return ISL_ERR_ARG;
+    if (n_inst) *n_inst = c->ninst;
     if (eq_off) {
         if (!c->numbered) ISL_FAIL(c, ISL_ERR_ARG, "batch info: DOFs not numbered");
         std::copy(c->inst_eq_off.begin(), c->inst_eq_off.end(), eq_off);

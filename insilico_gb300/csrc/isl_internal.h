@@ -220,6 +220,7 @@ struct isl_ctx {
     isl::DBuf<float4> dgeo;      // per element: detJ Ji, Ji, lam, mu as double-float
     isl::DBuf<int32_t> dbrobj, dadj_off, dadj, dsblk;
     int64_t bmap_serial = -1;
+    int asm_precision = 0;       // precision of the assembly in progress
     bool last_direct = false;    // the last assembly wrote the blocks directly (ISL_OPT_DIRECT_BLOCKS)
     int64_t tune_runs = 0;       // autotunes that timed candidates (the others came from the tuning cache)
     int elem_variant = 0;        // autotuned launch shape of the element kernel (0: not yet chosen)

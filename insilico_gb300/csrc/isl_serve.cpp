@@ -248,7 +248,8 @@ void run_batch(isl_server* s, Batch& b) {
     SV_CHECK(isl_set_option(c, ISL_OPT_BATCHED_SOLVE, 1));
     if (s->cfg.precision != ISL_PREC_FP64) SV_CHECK(isl_set_option(c, ISL_OPT_SPMV32_KIND, 104));
     std::vector<int64_t> eq_off(n + 1), dof_off(n + 1);
-    SV_CHECK(isl_batch_info(c, nullptr, eq_off.data(), dof_off.data()));
+    int64_t ninst = 0;
+    SV_CHECK(isl_batch_info(c, &ninst, eq_off.data(), dof_off.data()));
 
     const int prec = s->cfg.precision;
     const int method = prec == ISL_PREC_FP64 ? ISL_SOLVE_CG_FP64 : ISL_SOLVE_CG_FP32_IR;

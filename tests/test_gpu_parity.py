@@ -36,14 +36,18 @@ def gpu_problem(p):
     return S
 
 
+@pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_MIXED])
 @pytest.mark.parametrize("name,n", CASES)
-def test_pattern_values_rhs_match_oracle(name, n):
+def test_pattern_values_rhs_match_oracle(name, n, precision):
+    """FP64 element kernels (the plain path) and the mixed assembly
+    (double-float element arithmetic on the FP32 pipe) both give entries
+    and right-hand sides within 1e-12 of the oracle."""
     p = W.config(name, n=n)
     S = gpu_problem(p)
     P, (rp, ci, v, b) = oracle_problem(p)
     assert S.neq == P.neq
     np.testing.assert_array_equal(S.dof_index(), P.eq_index())
-    S.assemble(A.PREC_FP64)
+    S.assemble(precision)
     grp, gci, gv = S.csr()
     np.testing.assert_array_equal(grp, rp)
     np.testing.assert_array_equal(gci, ci)
