@@ -205,6 +205,21 @@ def oracle_rate(leg, tol):
     return leg["neq"] / t, its, t
 
 
+def assembly_roofline(p, S, asm_ms, hbm, src):
+    """The mixed assembly against the HBM roofline with the algorithmic bytes
+    of one assembly: coordinates, connectivity, per-element coefficients, DOF
+    status and values, the FP64 values and their FP32 copy, the right-hand
+    side; element matrices, contribution lists and element lists are
+    implementation cost and not counted."""
+    ncoef = 1 if p.kernel == "laplace" else 2
+    b = (len(p.X) * p.X.shape[1] * 8 + p.nelem * p.conn.shape[1] * 4 + p.nelem * ncoef * 8 +
+         S.ndofobj * p.ncomp * (1 + 8) + S.nnz * (8 + 4) + S.neq * 8)
+    ach = b / (asm_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "bytes": int(b),
+            "ms": asm_ms, "peak_source": src, "kernels": "element phase + gather phase of one mixed assembly "
+                                                       "(CUDA-event phase timers)"}
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm (the oracle restatement of
     inSilico's assembly and Eigen CG; the reference itself needs Eigen 3.2 /
@@ -320,11 +335,15 @@ def run_serve(args, rank, world, local, pg):
     from insilico_gb300 import serve
     A.load(build_if_missing=True)
     nreq = args.requests
+    win = args.batch_window_us
     arms = {
-        "mixed": dict(precision=A.PREC_FP32, max_batch=64, max_batches=4),
-        "mixed_equal_tol": dict(precision=A.PREC_MIXED, max_batch=64, max_batches=4, lin_tol=1e-10),
+        "mixed": dict(precision=A.PREC_FP32, max_batch=args.batch, max_batches=args.slots, batch_window_us=win),
+        "mixed_equal_tol": dict(precision=A.PREC_MIXED, max_batch=args.batch, max_batches=args.slots, lin_tol=1e-10,
+                                batch_window_us=win),
         "plain": dict(precision=A.PREC_FP64, max_batch=1, max_batches=8),
     }
+    if args.c5_mixed_only:  # configuration sweeps of the mixed server (no line is printed)
+        arms = {"mixed": arms["mixed"]}
     out = {}
     clocks = None
     for m, kw in arms.items():
@@ -343,8 +362,11 @@ def run_serve(args, rank, world, local, pg):
             raise RuntimeError(f"c5 {m}: requests failed: {bad[:3]}")
         out[m] = {"closed": serve.latency_stats(done, wall), "u": {r.rid: r.u for r in done},
                   "converged": all(r.converged for r in done), "launches": l1 - l0, "batches": b1 - b0,
-                  "h2d": srv.h2d_bytes, "d2h": srv.d2h_bytes, "srv": srv}
-        log(f"c5 {m} closed loop: {out[m]['closed']}")
+                  "h2d": srv.h2d_bytes, "d2h": srv.d2h_bytes, "srv": srv, "times": srv.times()}
+        log(f"c5 {m} closed loop: {out[m]['closed']} host: {out[m]['times']}")
+    if args.c5_mixed_only:
+        out["mixed"]["srv"].close()
+        return
     rate = 0.5 * out["plain"]["closed"]["solves_per_s"]
     for m in ("plain", "mixed"):
         done, wall = out[m]["srv"].run(serve.make_requests(nreq, rate=rate), realtime=True)
@@ -387,8 +409,10 @@ def run_serve(args, rank, world, local, pg):
                                    "kappa = 10 mu, 5 load steps to stretch 1.3",
                        "requests": nreq, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "per-request meshes are set up, assembled and solved from host inputs"},
-            "method": "native server: batches of up to 64 requests share every launch of a Newton iteration, "
-                      "4 batches at once; FP32 tangent + FP32 CG to 1e-6, FP64 residual",
+            "method": f"native server: batches of up to {args.batch} requests share every launch of a Newton "
+                      f"iteration, {args.slots} batches at once, batching window {win} us; FP32 tangent + FP32 CG "
+                      f"to 1e-6, FP64 residual; plain: one request per batch, 8 at once, FP64",
+            "server_host_seconds": {m: out[m]["times"] for m in arms},
             "latency_s": {"mixed_closed": {"p50": mc["p50_s"], "p99": mc["p99_s"]},
                           "plain_closed": {"p50": pc["p50_s"], "p99": pc["p99_s"]},
                           "open_loop_rate_per_s": rate,
@@ -724,7 +748,10 @@ def main():
                          "64^3; c4: 4096 batched Q1/Q2 Poisson instances; c5: served neo-Hookean Newton requests; "
                          "heat: nonlinear heat Newton run (heat::Static, BiCGSTAB), square 200")
     ap.add_argument("--requests", type=int, default=48, help="c5: requests per run")
-    ap.add_argument("--slots", type=int, default=8, help="c5: server slots")
+    ap.add_argument("--slots", type=int, default=4, help="c5: batches the mixed server runs at once")
+    ap.add_argument("--batch", type=int, default=12, help="c5: requests per batch of the mixed server")
+    ap.add_argument("--batch-window-us", type=int, default=20000, help="c5: batching window of the mixed server")
+    ap.add_argument("--c5-mixed-only", action="store_true", help="c5: the mixed server's closed loop only (sweeps)")
     ap.add_argument("--instances", type=int, default=4096, help="c4: batched instances")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
@@ -968,6 +995,7 @@ def run_single(args, rank, world, local, pg):
                      "bytes_per_launch": b32, "ms_per_launch": spmv32_ms, "peak_source": src,
                      "fp64_spmv": {"ms_per_launch": spmv64_ms,
                                    "achieved": spmv_bytes(nnz, neq, 8) / (spmv64_ms * 1e-3) / 1e9}},
+        "assembly_roofline": assembly_roofline(p, S, asm_ms, hbm, src),
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": int(launches),
         "kernel_ms": kernels,
     }

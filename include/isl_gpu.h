@@ -424,13 +424,17 @@ int isl_tune_cache(const char* path);
  * The server forms batches from the queue in arrival order (same shape,
  * ncomp, kernel, material, quadrature and lin_tol; at most max_batch
  * requests; within the 32-bit contribution budget max_pairs and the free HBM
- * minus reserve_bytes) and runs each batch as one context of instances on
- * its own stream and host thread; at most max_batches batches run at once,
+ * minus reserve_bytes; a partial batch waits up to batch_window_us after its
+ * oldest request arrived, to take in requests submitted together) and runs
+ * each batch as one context of instances on its own stream and host thread;
+ * at most max_batches batches run at once,
  * so requests that arrive while others run are admitted as batches finish
  * and memory frees up.  A batch shares every launch of a Newton iteration
  * between its requests (assembly, norms, CG with per-request convergence,
  * distribute); each request follows its own Newton loop and completes as
- * soon as it finishes.  A request's result does not depend on its batch.
+ * soon as it finishes.  With max_batch > 1 every batch (a batch of one too)
+ * runs the batched solver, so a request's result does not depend on its
+ * batch; with max_batch = 1 each request runs the single-system solvers.
  * precision: ISL_PREC_FP64 (FP64 tangent and CG), ISL_PREC_FP32 (FP32
  * tangent and FP32 CG, FP64 residual: inexact Newton steps) or
  * ISL_PREC_MIXED (FP64 and FP32 matrices, FP32 CG with FP64 reliable
@@ -448,6 +452,7 @@ typedef struct {
     int64_t max_pairs;        /* element pairs (n_elem * nloc^2) per batch; <= 0: 1.3e9 */
     int64_t test_budget_bytes;
     double test_fake_us_per_elem;
+    int64_t batch_window_us;  /* a partial batch waits this long after its oldest request arrived (0: none) */
 } isl_serve_config;
 typedef struct {
     int shape;                /* ISL_QUAD, ISL_TET, ISL_HEX */
@@ -494,6 +499,11 @@ const char* isl_serve_error(isl_server* s, int64_t ticket);
 int isl_serve_release(isl_server* s, int64_t ticket);
 /* kernel launches of the finished batches and batches formed so far */
 int isl_serve_counters(isl_server* s, int64_t* launches, int64_t* batches);
+/* host wall time of the finished batches (any pointer may be NULL): context
+ * setup, assembly with the residual norms, solve with the distribute and the
+ * increment norms, whole batches; and the Newton iterations they ran */
+int isl_serve_times(isl_server* s, double* setup_s, double* assemble_s, double* solve_s, double* batch_s,
+                    int64_t* newton_ticks);
 /* waits for the running batches; queued requests fail */
 int isl_serve_destroy(isl_server* s);
 

@@ -46,6 +46,7 @@ EXPORTED = [
     "isl_batch_norms", "isl_batch_scale_constraints", "isl_batch_set_mask",
     "isl_serve_create", "isl_serve_submit", "isl_serve_poll", "isl_serve_wait", "isl_serve_result", "isl_serve_error",
     "isl_serve_release", "isl_serve_destroy", "isl_serve_counters", "isl_tune_cache", "isl_set_laplace_qp",
+    "isl_serve_times",
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND, OPT_BATCHED_SOLVE, OPT_DIRECT_BLOCKS, OPT_TUNE_RUNS,
@@ -56,7 +57,7 @@ class ServeConfig(C.Structure):
     """isl_serve_config"""
     _fields_ = [("max_batch", C.c_int), ("max_batches", C.c_int), ("precision", C.c_int),
                 ("reserve_bytes", C.c_int64), ("max_pairs", C.c_int64), ("test_budget_bytes", C.c_int64),
-                ("test_fake_us_per_elem", C.c_double)]
+                ("test_fake_us_per_elem", C.c_double), ("batch_window_us", C.c_int64)]
 
 
 class ServeRequest(C.Structure):
@@ -174,6 +175,7 @@ def load(build_if_missing: bool = False):
     L.isl_serve_release.argtypes = [_P, C.c_int64]
     L.isl_serve_destroy.argtypes = [_P]
     L.isl_serve_counters.argtypes = [_P, _I64, _I64]
+    L.isl_serve_times.argtypes = [_P, _D, _D, _D, _D, _I64]
     L.isl_tune_cache.argtypes = [C.c_char_p]
     L.isl_set_laplace_qp.argtypes = [_P, _D, i]
     for name in EXPORTED:

@@ -98,6 +98,10 @@ struct isl_server {
     int running = 0;
     int64_t reserved = 0;  // footprints of running batches
     int64_t launches = 0;  // kernel launches of finished batches
+    // host wall time of the finished batches: setup, assembly (+ norms),
+    // solve (+ distribute, norms), whole batch; Newton iterations run
+    double t_setup = 0, t_assemble = 0, t_solve = 0, t_batches = 0;
+    int64_t ticks = 0;
     int64_t next_ticket = 1, next_batch = 0;
     bool stop = false;
     std::thread sched;
@@ -177,6 +181,7 @@ void run_fake(isl_server* s, Batch& b) {
 // One batch: setup of the batched context, then the Newton iterations of all
 // its requests in shared launches (see the file comment).
 void run_batch(isl_server* s, Batch& b) {
+    const double t_begin = std::chrono::duration<double>(Clock::now().time_since_epoch()).count();
     const int n = (int)b.reqs.size();
     const Req& r0 = *b.reqs[0];
     const int dim = sdim(r0.shape), nv = nverts(r0.shape), nc = r0.ncomp;
@@ -243,10 +248,15 @@ void run_batch(isl_server* s, Batch& b) {
     if (r0.kernel == ISL_KERNEL_LAPLACE) SV_CHECK(isl_set_laplace(c, c0.data(), r0.qdeg));
     else SV_CHECK(isl_set_hyperelastic(c, r0.material, c0.data(), c1.data(), r0.qdeg));
     if (body) SV_CHECK(isl_set_body_force_nodal(c, fb.data()));
-    // the batched solver for every batch size, with a fixed FP32 SpMV kind
-    // (per-instance reductions in a fixed order: results independent of the batch)
-    SV_CHECK(isl_set_option(c, ISL_OPT_BATCHED_SOLVE, 1));
-    if (s->cfg.precision != ISL_PREC_FP64) SV_CHECK(isl_set_option(c, ISL_OPT_SPMV32_KIND, 104));
+    // a batching server runs the batched solver for every batch size, with a
+    // fixed FP32 SpMV kind (per-instance reductions in a fixed order: results
+    // independent of the batch); a server of one request per batch runs the
+    // single-system solvers
+    const bool batched = s->cfg.max_batch > 1;
+    if (batched) {
+        SV_CHECK(isl_set_option(c, ISL_OPT_BATCHED_SOLVE, 1));
+        if (s->cfg.precision != ISL_PREC_FP64) SV_CHECK(isl_set_option(c, ISL_OPT_SPMV32_KIND, 104));
+    }
     std::vector<int64_t> eq_off(n + 1), dof_off(n + 1);
     int64_t ninst = 0;
     SV_CHECK(isl_batch_info(c, &ninst, eq_off.data(), dof_off.data()));
@@ -273,7 +283,27 @@ void run_batch(isl_server* s, Batch& b) {
         else factor[k] = (double)(step[k] + 1) / (double)step[k];
     };
 
+    double t_asm = 0.0, t_solve = 0.0;
+    int64_t ticks = 0;
+    auto stamp = [] { return std::chrono::duration<double>(Clock::now().time_since_epoch()).count(); };
+    const double t_setup = stamp() - t_begin;
+    struct Account {  // the batch's phase times go to the server's totals however the loop ends
+        isl_server* s;
+        const double &setup, &as, &so;
+        const int64_t& ticks;
+        double t0;
+        ~Account() {
+            const double tot = std::chrono::duration<double>(Clock::now().time_since_epoch()).count() - t0;
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->t_setup += setup;
+            s->t_assemble += as;
+            s->t_solve += so;
+            s->t_batches += tot;
+            s->ticks += ticks;
+        }
+    } account{s, t_setup, t_asm, t_solve, ticks, t_begin};
     for (int64_t tick = 0; nactive > 0; ++tick) {
+        ++ticks;
         if (tick > max_ticks) {  // cannot happen: every iteration advances an instance
             fail_batch(s, b, ISL_ERR_TIMEOUT, "served Newton loop made no progress");
             return;
@@ -285,8 +315,10 @@ void run_batch(isl_server* s, Batch& b) {
             SV_CHECK(isl_batch_scale_constraints(c, factor.data()));
             std::fill(factor.begin(), factor.end(), 1.0);
         }
+        double t0 = stamp();
         SV_CHECK(isl_assemble(c, prec, 1, 1));
         SV_CHECK(isl_batch_norms(c, normR.data()));
+        t_asm += stamp() - t0;
         std::vector<int> done_now;
         int nsolve = 0;
         for (int k = 0; k < n; ++k) {
@@ -297,6 +329,7 @@ void run_batch(isl_server* s, Batch& b) {
             ++nsolve;
         }
         if (nsolve > 0) {
+            t0 = stamp();
             if (n > 1) SV_CHECK(isl_batch_set_mask(c, solve.data()));
             int64_t it = 0;
             double rr = 0.0;
@@ -306,9 +339,11 @@ void run_batch(isl_server* s, Batch& b) {
                 fail_batch(s, b, st, std::string("isl_solve: ") + isl_last_error(c));
                 return;
             }
-            SV_CHECK(isl_batch_solve_stats(c, cgit.data(), relres.data()));
+            if (batched) SV_CHECK(isl_batch_solve_stats(c, cgit.data(), relres.data()));
+            else cgit[0] = it;
             SV_CHECK(isl_distribute(c, 1));
             SV_CHECK(isl_batch_norms(c, normDU.data()));
+            t_solve += stamp() - t0;
             for (int k = 0; k < n; ++k) {
                 if (!solve[k]) continue;
                 Req& r = *b.reqs[k];
@@ -376,6 +411,16 @@ void scheduler_main(isl_server* s) {
                 it = s->workers.erase(it);
             } else {
                 ++it;
+            }
+        }
+        // batching window: a partial batch waits for more arrivals until its
+        // oldest request has queued for batch_window_us
+        if (s->cfg.batch_window_us > 0 && (int)s->queue.size() < s->cfg.max_batch && !s->stop) {
+            const double waited = s->now() - s->queue.front()->t_submit;
+            const double window = 1e-6 * (double)s->cfg.batch_window_us;
+            if (waited < window) {
+                s->cv.wait_for(lk, std::chrono::duration<double>(window - waited));
+                continue;
             }
         }
         auto b = std::make_shared<Batch>();
@@ -542,6 +587,18 @@ const char* isl_serve_error(isl_server* s, int64_t ticket) {
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end()) return "unknown ticket";
     return it->second->err.c_str();
+}
+
+int isl_serve_times(isl_server* s, double* setup_s, double* assemble_s, double* solve_s, double* batch_s,
+                    int64_t* newton_ticks) {
+    if (!s) return ISL_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (setup_s) *setup_s = s->t_setup;
+    if (assemble_s) *assemble_s = s->t_assemble;
+    if (solve_s) *solve_s = s->t_solve;
+    if (batch_s) *batch_s = s->t_batches;
+    if (newton_ticks) *newton_ticks = s->ticks;
+    return ISL_OK;
 }
 
 int isl_serve_counters(isl_server* s, int64_t* launches, int64_t* batches) {

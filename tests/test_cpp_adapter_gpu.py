@@ -94,7 +94,7 @@ int main(int argc, char** argv) {
 
     // served path: two neo-Hookean cubes of sides 3 and 4 (PulledSheet
     // conditions, 5 load steps), one batch
-    isl::Gb300Server srv(0, ISL_PREC_FP32, 8, 1);
+    isl::Gb300Server srv(0, ISL_PREC_FP32, 8, 1, 0, 200000);  // requests submitted together: one batch
     const int sides[2] = {3, 4};
     const double mus[2] = {1.7, 0.4};
     std::vector<int64_t> tickets;

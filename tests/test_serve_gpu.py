@@ -5,8 +5,8 @@
   (solid/CompressibleDriver.hpp:156-214, absolute tolerance on ||R||/N and
   ||dU||/N) within 1e-8 relative L2, with the same Newton iteration count on
   the plain path;
-* a request's result is bitwise the same alone and inside a batch of other
-  requests (shared launches with per-request reductions);
+* a request's result is bitwise the same alone (a batch of one) and inside a
+  batch of other requests (shared launches with per-request reductions);
 * a request that fails (a degenerate element) is reported with its status,
   and requests in other batches are not affected.
 """
@@ -20,11 +20,13 @@ from helpers import oracle_newton_driver
 
 pytestmark = pytest.mark.gpu
 
+WINDOW = 200_000  # us: requests submitted together form one batch
+
 
 @pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_FP32, A.PREC_MIXED])
 def test_served_newton_matches_oracle_driver(precision):
     reqs = [serve.Request(0, side=3, mu=1.7), serve.Request(1, side=5, mu=0.3), serve.Request(2, side=4, mu=6.0)]
-    srv = serve.Server(precision=precision, max_batch=8, max_batches=2)
+    srv = serve.Server(precision=precision, max_batch=8, max_batches=2, batch_window_us=WINDOW)
     done, _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
     srv.close()
     assert all(r.status == A.ISL_OK and r.converged for r in done), [(r.status, r.error) for r in done]
@@ -38,10 +40,11 @@ def test_served_newton_matches_oracle_driver(precision):
 
 def test_result_same_alone_and_in_a_batch():
     reqs = serve.make_requests(6, rate=0.0, side_range=(3, 7))
-    alone = serve.Server(max_batch=1, max_batches=1)
+    # alone: a batching server given a single request (a batch of one)
+    alone = serve.Server(max_batch=8, max_batches=1, batch_window_us=WINDOW)
     ref, _ = alone.run([serve.Request(reqs[2].rid, reqs[2].side, reqs[2].mu)], realtime=False)
     alone.close()
-    mix = serve.Server(max_batch=8, max_batches=2)
+    mix = serve.Server(max_batch=8, max_batches=2, batch_window_us=WINDOW)
     done, wall = mix.run(reqs, realtime=False)
     mix.close()
     got = [r for r in done if r.rid == reqs[2].rid][0]
