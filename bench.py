@@ -117,6 +117,7 @@ SSPMV_KERNEL = {102: "k_sspmv_batch<2,8>", 104: "k_sspmv_batch<4,8>", 108: "k_ss
 BSPMV_KERNEL = {1: "k_bspmv_pap<1>", 2: "k_bspmv_pap<2>", 3: "k_bspmv_pap<4>", 5: "k_bspmv_batch<2,4>",
                 6: "k_bspmv_batch<4,3>", 7: "k_bspmv_batch<8,2>", 4: "k_brow_spmv<4>", 8: "k_brow_spmv<8>",
                 16: "k_brow_spmv<16>"}
+BSPMV_DIR_KERNEL = {5: "k_bspmv_dir<2,4>", 6: "k_bspmv_dir<4,3>", 7: "k_bspmv_dir<8,2>"}
 
 WORKLOAD_DESC = {
     "c1": "c1 Q1 Poisson {n}^2 (heat::Laplace, kappa_e = exp(N(0,0.5)), nodal source U[0,1], g = 0)",
@@ -336,10 +337,12 @@ def run_serve(args, rank, world, local, pg):
     A.load(build_if_missing=True)
     nreq = args.requests
     win = args.batch_window_us
+    ratio = args.size_ratio
     arms = {
-        "mixed": dict(precision=A.PREC_FP32, max_batch=args.batch, max_batches=args.slots, batch_window_us=win),
+        "mixed": dict(precision=A.PREC_FP32, max_batch=args.batch, max_batches=args.slots, batch_window_us=win,
+                      size_ratio=ratio),
         "mixed_equal_tol": dict(precision=A.PREC_MIXED, max_batch=args.batch, max_batches=args.slots, lin_tol=1e-10,
-                                batch_window_us=win),
+                                batch_window_us=win, size_ratio=ratio),
         "plain": dict(precision=A.PREC_FP64, max_batch=1, max_batches=8),
     }
     if args.c5_mixed_only:  # configuration sweeps of the mixed server (no line is printed)
@@ -751,6 +754,8 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="c5: batches the mixed server runs at once")
     ap.add_argument("--batch", type=int, default=12, help="c5: requests per batch of the mixed server")
     ap.add_argument("--batch-window-us", type=int, default=20000, help="c5: batching window of the mixed server")
+    ap.add_argument("--size-ratio", type=float, default=0.0,
+                    help="c5: > 1 batches only requests within this element-count factor of the batch's first")
     ap.add_argument("--c5-mixed-only", action="store_true", help="c5: the mixed server's closed loop only (sweeps)")
     ap.add_argument("--instances", type=int, default=4096, help="c4: batched instances")
     ap.add_argument("--no-cpu", action="store_true")
@@ -919,6 +924,18 @@ def run_single(args, rank, world, local, pg):
                  "block_format_and_block_jacobi": point_ms / ms_step,
                  "note": "plain FP64 (point Jacobi, CSR) -> mixed with the same point Jacobi and CSR (precision "
                          "alone) -> mixed with 3x3 node blocks and block Jacobi"}
+        # the same block solve with the direction update as its own kernel
+        S.assemble(A.PREC_MIXED)
+        S.set_option(A.OPT_FOLD_DIRECTION, 0)
+        step_mixed()
+        S.mark(4)
+        for _ in range(2):
+            it_s = step_mixed()[0]
+        S.mark(5)
+        S.set_option(A.OPT_FOLD_DIRECTION, 1)
+        sep_ms = S.elapsed_ms(4, 5) / 2
+        split["separate_direction_kernel"] = {"ms_per_step": sep_ms, "iters": it_s,
+                                              "folded_gain": sep_ms / ms_step}
         log(f"split: {split}")
 
     # dominant kernel: FP32 SpMV of the inner CG, timed alone (CUDA events)
@@ -930,11 +947,18 @@ def run_single(args, rank, world, local, pg):
     hbm, src = peaks()
     blocked = S.get_option(A.OPT_BLOCKED)
     if blocked:
-        # 3x3 blocks: 36 B of values + 4 B of column id per block, x and y once
+        # 3x3 blocks: 36 B of values + 4 B of column id per block, x and y once;
+        # with the direction update folded in, x is formed from z and the
+        # previous direction (both read once) and written once
         nblk, nslot = S.get_option(A.OPT_NBLOCKS), S.get_option(A.OPT_NSLOTS)
-        b32 = nblk * 40 + 2 * neq * 4 + 8 * ((neq // 3 + 31) // 32)
-        kname = BSPMV_KERNEL.get(int(kernels["block_kind"]), "k_bspmv") + \
-            " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV, autotuned variant)"
+        bkind = int(kernels["block_kind"])
+        folded = bool(S.get_option(A.OPT_FOLD_DIRECTION)) and bkind in BSPMV_DIR_KERNEL
+        b32 = nblk * 40 + (4 if folded else 2) * neq * 4 + 8 * ((neq // 3 + 31) // 32)
+        if folded:
+            kname = BSPMV_DIR_KERNEL[bkind] + " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV with the block-Jacobi " \
+                "direction update folded in, autotuned variant)"
+        else:
+            kname = BSPMV_KERNEL.get(bkind, "k_bspmv") + " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV, autotuned variant)"
     else:
         nblk, nslot = 0, S.get_option(A.OPT_SCALAR_SLOTS)
         b32 = spmv_bytes(nnz, neq, 4)

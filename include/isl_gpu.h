@@ -348,7 +348,14 @@ int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /*
 enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_OPT_NSLOTS = 3, ISL_OPT_PERSISTENT = 4,
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
        ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
-       ISL_OPT_ELEM_VARIANT = 13 };
+       ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14 };
+/* ISL_OPT_FOLD_DIRECTION (default 1): the graph path of the node-blocked
+ * mixed solve forms the search direction p = B^-1 r + beta p inside the block
+ * SpMV (the update kernel stores z = B^-1 r; each column block of p is formed
+ * where the product reads it, and its owner row writes it to the second of
+ * two direction buffers), two launches per iteration instead of three; 0
+ * keeps the separate direction kernel.  Applies to the batched-load SpMV
+ * variants the autotune prefers. */
 /* ISL_OPT_TUNE_RUNS (read-only): autotunes of this context that timed their
  * candidates; the others took their choice from the tuning cache.
  * ISL_OPT_ELEM_VARIANT (read-only): the launch shape the element kernel
@@ -425,7 +432,9 @@ int isl_tune_cache(const char* path);
  * ncomp, kernel, material, quadrature and lin_tol; at most max_batch
  * requests; within the 32-bit contribution budget max_pairs and the free HBM
  * minus reserve_bytes; a partial batch waits up to batch_window_us after its
- * oldest request arrived, to take in requests submitted together) and runs
+ * oldest request arrived, to take in requests submitted together; with
+ * size_ratio > 1 only requests of similar element counts share a batch, so a
+ * small request does not run at the pace of a large one) and runs
  * each batch as one context of instances on its own stream and host thread;
  * at most max_batches batches run at once,
  * so requests that arrive while others run are admitted as batches finish
@@ -453,6 +462,9 @@ typedef struct {
     int64_t test_budget_bytes;
     double test_fake_us_per_elem;
     int64_t batch_window_us;  /* a partial batch waits this long after its oldest request arrived (0: none) */
+    double size_ratio;        /* > 1: a batch takes only requests whose element count is within this factor of
+                                 its first request's (requests of other sizes wait for a batch of their own);
+                                 <= 1: any size */
 } isl_serve_config;
 typedef struct {
     int shape;                /* ISL_QUAD, ISL_TET, ISL_HEX */

@@ -250,13 +250,14 @@ private:
 class Gb300Server {
 public:
     explicit Gb300Server(int device = 0, int precision = ISL_PREC_FP32, int max_batch = 64, int max_batches = 4,
-                         int64_t reserve_bytes = 0, int64_t batch_window_us = 0) {
+                         int64_t reserve_bytes = 0, int64_t batch_window_us = 0, double size_ratio = 0.0) {
         isl_serve_config cfg{};
         cfg.max_batch = max_batch;
         cfg.max_batches = max_batches;
         cfg.precision = precision;
         cfg.reserve_bytes = reserve_bytes;
         cfg.batch_window_us = batch_window_us;
+        cfg.size_ratio = size_ratio;
         const int st = isl_serve_create(&s_, device, &cfg);
         if (st != ISL_OK) throw gpu_error(st, "isl_serve_create");
     }

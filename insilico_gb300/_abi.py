@@ -50,14 +50,14 @@ EXPORTED = [
 ]
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND, OPT_BATCHED_SOLVE, OPT_DIRECT_BLOCKS, OPT_TUNE_RUNS,
- OPT_ELEM_VARIANT) = range(14)
+ OPT_ELEM_VARIANT, OPT_FOLD_DIRECTION) = range(15)
 
 
 class ServeConfig(C.Structure):
     """isl_serve_config"""
     _fields_ = [("max_batch", C.c_int), ("max_batches", C.c_int), ("precision", C.c_int),
                 ("reserve_bytes", C.c_int64), ("max_pairs", C.c_int64), ("test_budget_bytes", C.c_int64),
-                ("test_fake_us_per_elem", C.c_double), ("batch_window_us", C.c_int64)]
+                ("test_fake_us_per_elem", C.c_double), ("batch_window_us", C.c_int64), ("size_ratio", C.c_double)]
 
 
 class ServeRequest(C.Structure):

@@ -1423,6 +1423,7 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (!c) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { c->use_block = value != 0; return ISL_OK; }
     if (key == ISL_OPT_BATCHED_SOLVE) { c->force_batched = value != 0; return ISL_OK; }
+    if (key == ISL_OPT_FOLD_DIRECTION) { c->fuse_dir = value != 0; return ISL_OK; }
     if (key == ISL_OPT_BARRIER_TEST) { c->barrier_test = value != 0; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) {
         if (value < 0 || value > 2) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_PERSISTENT takes 0, 1 or 2");
@@ -1457,6 +1458,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (!c || !value) return ISL_ERR_ARG;
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_BATCHED_SOLVE) { *value = c->force_batched; return ISL_OK; }
+    if (key == ISL_OPT_FOLD_DIRECTION) { *value = c->fuse_dir; return ISL_OK; }
     if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }
     if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }
     if (key == ISL_OPT_ELEM_VARIANT) { *value = c->elem_variant; return ISL_OK; }

@@ -226,6 +226,7 @@ struct isl_ctx {
     int elem_variant = 0;        // autotuned launch shape of the element kernel (0: not yet chosen)
     int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
+    bool fuse_dir = true;  // fold the block-Jacobi direction update into the block SpMV
 
     // scalar sliced-ELL copy of the FP32 matrix for the mixed solver of a
     // system that is not node-blocked: rows sorted by length (longest first)

@@ -9,8 +9,10 @@
 // Here a server admits many such requests and runs them on one GPU:
 //   * a scheduler thread forms batches from the queue in arrival order:
 //     requests with the same element shape, components, kernel, material and
-//     quadrature, up to max_batch, within the 32-bit contribution budget of a
-//     context and within the free HBM (cudaMemGetInfo) minus a reserve;
+//     quadrature (and, with size_ratio > 1, element counts within that factor
+//     of the batch's first request), up to max_batch, within the 32-bit
+//     contribution budget of a context and within the free HBM
+//     (cudaMemGetInfo) minus a reserve;
 //   * each batch is one isl_ctx holding its requests as instances
 //     (isl_batch_mesh_upload) on its own CUDA stream and host thread, so
 //     batches formed from later arrivals run concurrently with earlier ones
@@ -430,6 +432,10 @@ void scheduler_main(isl_server* s) {
             Req& r = **it;
             const bool first = b->reqs.empty();
             if (!first && !same_kind(r, *b->reqs[0])) { ++it; continue; }
+            if (!first && s->cfg.size_ratio > 1.0) {
+                const double h = (double)b->reqs[0]->n_elem, e = (double)r.n_elem;
+                if (e > h * s->cfg.size_ratio || e * s->cfg.size_ratio < h) { ++it; continue; }
+            }
             const bool fits_mem = b->footprint + r.footprint <= avail;
             const bool fits_pairs = pairs + r.pairs <= s->cfg.max_pairs;
             if (first ? (fits_mem || s->running == 0) : (fits_mem && fits_pairs)) {

@@ -1392,6 +1392,90 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
     }
 }
 
+// The same product with the direction update folded in: the previous update
+// kernel left z = B^-1 r, and every column block of p is formed where it is
+// read, p_j = z_j + beta p_old_j (one fmaf per entry, so every reader and the
+// owning row compute the same bits).  The owner of block row i writes p_i to
+// the other buffer; p_old is never written during the product, so no block
+// reads a value another block has already replaced.  Which of the two
+// buffers holds p_old follows the parity of the iteration count, which the
+// update kernel advances: the captured graph stays the same for every chunk,
+// and a reliable-update restart (which keeps p) needs no copy.
+template <int U>
+__device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int* __restrict__ soff,
+                                                   const int* __restrict__ swid, const int* __restrict__ scol,
+                                                   const float* __restrict__ sv, const float* __restrict__ z,
+                                                   const float* __restrict__ pold, float beta, float* __restrict__ pnew,
+                                                   float* __restrict__ q, int warp, int nwarps) {
+    const int lane = threadIdx.x & 31;
+    float loc = 0.f;
+    for (int s = warp; s < nslice; s += nwarps) {
+        const int i = s * 32 + lane;
+        const int o = soff[s], w = swid[s];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int k = 0; k < w; k += U) {
+            int j[U];
+            float v[U][9];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane);
+                    const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) v[u][e] = ld_stream(vp + 32 * e);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u < w) {
+                    const size_t b = 3 * (size_t)j[u];
+                    const float x0 = fmaf(beta, __ldg(pold + b), __ldg(z + b));
+                    const float x1 = fmaf(beta, __ldg(pold + b + 1), __ldg(z + b + 1));
+                    const float x2 = fmaf(beta, __ldg(pold + b + 2), __ldg(z + b + 2));
+                    a0 += v[u][0] * x0 + v[u][1] * x1 + v[u][2] * x2;
+                    a1 += v[u][3] * x0 + v[u][4] * x1 + v[u][5] * x2;
+                    a2 += v[u][6] * x0 + v[u][7] * x1 + v[u][8] * x2;
+                }
+            }
+        }
+        if (i < nbr) {
+            const size_t b = 3 * (size_t)i;
+            const float p0 = fmaf(beta, __ldg(pold + b), __ldg(z + b));
+            const float p1 = fmaf(beta, __ldg(pold + b + 1), __ldg(z + b + 1));
+            const float p2 = fmaf(beta, __ldg(pold + b + 2), __ldg(z + b + 2));
+            pnew[b] = p0; pnew[b + 1] = p1; pnew[b + 2] = p2;
+            q[b] = a0; q[b + 1] = a1; q[b + 2] = a2;
+            loc += p0 * a0 + p1 * a1 + p2 * a2;
+        }
+    }
+    return loc;
+}
+
+template <int U, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, const int* __restrict__ soff,
+                                                        const int* __restrict__ swid, const int* __restrict__ scol,
+                                                        const float* __restrict__ sv, const float* __restrict__ z,
+                                                        float* pa, float* pb, float* __restrict__ q, CGScal* S,
+                                                        double* part) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const bool odd = S->iters & 1;
+    const float beta = (float)S->beta;
+    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
+    const float loc = bspmv_slices_dir<U>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta, odd ? pa : pb, q,
+                                          warp, nwarps);
+    const double bsum = block_sum_f(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    if (last_block(&S->ticket1)) {
+        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
+        if (threadIdx.x == 0) {
+            S->pAp = tot;
+            S->alpha = S->absNew / tot;
+            S->ticket1 = 0;
+        }
+    }
+}
+
 // q = A p on the block-row CSR copy: LPB lanes per block row
 template <int LPB>
 __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
@@ -1459,12 +1543,18 @@ constexpr int NODE_BS = 256;
 static unsigned node_grid(const isl_ctx* c, long long nbr) {
     return (unsigned)std::max<long long>(1, std::min<long long>((nbr + NODE_BS - 1) / NODE_BS, 2LL * c->sm_count));
 }
+// FZ: the direction update is folded into the SpMV (k_bspmv_dir): p is the
+// buffer that product wrote (p2 on even iteration counts, p on odd ones), and
+// z = B^-1 r is stored for the next product
+template <bool FZ>
 __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __restrict__ x, float* __restrict__ r,
-                                                           const float* __restrict__ p, const float* __restrict__ q,
-                                                           const float* __restrict__ binv, CGScal* S, double* part,
+                                                           const float* __restrict__ p1, const float* __restrict__ p2,
+                                                           const float* __restrict__ q, const float* __restrict__ binv,
+                                                           float* __restrict__ zout, CGScal* S, double* part,
                                                            int max_iter) {
     if (S->done) return;
     __shared__ double sh[32];
+    const float* __restrict__ p = (FZ && !(S->iters & 1)) ? p2 : p1;
     const float alpha = (float)S->alpha;
     float rr = 0.f, rz = 0.f;
     for (int i = blockIdx.x * NODE_BS + threadIdx.x; i < nbr; i += gridDim.x * NODE_BS) {
@@ -1482,6 +1572,7 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
         for (int a = 0; a < 3; ++a) {
             r[d + a] = rv[a];
             const float z = b[3 * a] * rv[0] + b[3 * a + 1] * rv[1] + b[3 * a + 2] * rv[2];
+            if (FZ) zout[d + a] = z;
             rr += rv[a] * rv[a];
             rz += rv[a] * z;
         }
@@ -1644,9 +1735,10 @@ static int persist_grid(isl_ctx* c) {
     return c->persist_grid;
 }
 
+// zout (may be null): z = B^-1 r is stored for a folded direction update
 __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
-                                                   float* __restrict__ p, const float* __restrict__ binv, CGScal* S, double* part,
-                                                   double tol, int restart, double trig) {
+                                                   float* __restrict__ p, const float* __restrict__ binv, float* __restrict__ zout,
+                                                   CGScal* S, double* part, double tol, int restart, double trig) {
     __shared__ double sh[32];
     double bb = 0.0, bz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < nbr; i += gridDim.x * BS) {
@@ -1660,6 +1752,7 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
             else bb += (double)ri[a] * (double)ri[a];
         }
         bj_apply(binv, nbr, i, ri, zi);
+        if (zout) { zout[3 * i] = zi[0]; zout[3 * i + 1] = zi[1]; zout[3 * i + 2] = zi[2]; }
         bz += (double)ri[0] * zi[0] + (double)ri[1] * zi[1] + (double)ri[2] * zi[2];
     }
     const double b1 = block_sum(bb, sh);
@@ -1715,6 +1808,19 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
         case 8: k_brow_spmv<8><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
         case 16: k_brow_spmv<16><<<gv, BS, 0, st>>>(nbr, c->dbptr.p, c->dbcol.p, c->dbval.p, nb, p, q, S, part); break;
         default: k_bspmv_pap<2><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, c->nslot, p, q, S, part); break;
+    }
+}
+
+// the batched-load kinds 5..7 also exist with the direction update folded in
+static bool bspmv_dir_kind(int kind) { return kind >= 5 && kind <= 7; }
+static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
+                             CGScal* S, double* part) {
+    const int nbr = (int)c->nbr, ns = (int)c->nslice;
+    const unsigned g = sell_grid(c);
+    switch (kind) {
+        case 5: k_bspmv_dir<2, 4><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 6: k_bspmv_dir<4, 3><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
+        default: k_bspmv_dir<8, 2><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
     }
 }
 
@@ -1989,11 +2095,15 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     unsigned* ticket = &(c->dscal.p + 1)->ticket1;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
-    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 0, kDelta2);
-    ISL_CHECK_CUDA(c, cudaGetLastError());
-    c->launches += 1;
     const bool want_persist = c->use_persist == 2 || (c->use_persist == 1 && nbr <= PERSIST_MAX_NBR);
     const int pgrid = want_persist ? persist_grid(c) : 0;
+    // folded direction update: z = B^-1 r and the second direction buffer
+    // take the two spare FP32 vectors of the work area
+    const bool fused = pgrid == 0 && c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb);
+    float *z32 = fused ? V + 4 * n : nullptr, *p32b = V + 5 * n;
+    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0, kDelta2);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    c->launches += 1;
     cudaGraph_t graph;
     cudaGraphExec_t exec = nullptr;
     if (pgrid == 0) {
@@ -2002,9 +2112,14 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);  // one pass, no reduction
     const unsigned nbn = node_grid(c, nbr);
     for (int k = 0; k < CHUNK; ++k) {
-        k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
-        launch_bspmv(c->bspmv_lpb, grid, st, c, p32, q32, S, c->dpart.p);
-        k_cg_update_b3n<<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, q32, c->dbinv.p, S, c->dpart.p, mi);
+        if (fused) {
+            launch_bspmv_dir(c->bspmv_lpb, st, c, z32, p32, p32b, q32, S, c->dpart.p);
+            k_cg_update_b3n<true><<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, p32b, q32, c->dbinv.p, z32, S, c->dpart.p, mi);
+        } else {
+            k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
+            launch_bspmv(c->bspmv_lpb, grid, st, c, p32, q32, S, c->dpart.p);
+            k_cg_update_b3n<false><<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, p32, q32, c->dbinv.p, nullptr, S, c->dpart.p, mi);
+        }
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
     {
@@ -2047,7 +2162,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             c->launches += 1;
         } else {
             if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
-            c->launches += 3 * CHUNK;
+            c->launches += (fused ? 2 : 3) * CHUNK;
         }
         rc = read_scal(c);
         if (rc != ISL_OK) break;
@@ -2065,7 +2180,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, S, c->dpart.p, tol, 1, kDelta2 * rr_true);
+            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 1, kDelta2 * rr_true);
             c->launches += 1;
         }
     }
@@ -2091,9 +2206,17 @@ int time_bspmv(isl_ctx* c, int nrep, double* ms) {
     ISL_CHECK_CUDA(c, cudaMemsetAsync(S, 0, sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 2 * n, 0, n * 4, st));
     if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, V + 2 * n, V + 3 * n, S, c->dpart.p);
-    launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    // the product the mixed solve launches: with the direction update folded
+    // in where that variant exists (z and the two direction buffers zeroed)
+    const bool fused = c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb);
+    if (fused) ISL_CHECK_CUDA(c, cudaMemsetAsync(V + 4 * n, 0, 2 * n * 4, st));
+    auto one = [&]() {
+        if (fused) launch_bspmv_dir(c->bspmv_lpb, st, c, V + 4 * n, V + 2 * n, V + 5 * n, V + 3 * n, S, c->dpart.p);
+        else launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    };
+    one();
     cudaEventRecord(c->ev[2], st);
-    for (int r = 0; r < nrep; ++r) launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
+    for (int r = 0; r < nrep; ++r) one();
     cudaEventRecord(c->ev[3], st);
     c->launches += nrep + 1;
     ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
@@ -2248,11 +2371,20 @@ int time_kernels(isl_ctx* c, int nrep, double* ms) {
         k_fill<<<grid, BS, 0, st>>>((int64_t)(4 * n), V, 1.0f);
         if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, p, q, c->dscal.p, c->dpart.p);
         const int nbr = (int)c->nbr;
-        ms[0] = timeit([&] { launch_bspmv(c->bspmv_lpb, grid, st, c, p, q, c->dscal.p, c->dpart.p); });
         const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);
         const unsigned nbn = node_grid(c, nbr);
-        ms[1] = timeit([&] { k_cg_update_b3n<<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, q, c->dbinv.p, c->dscal.p, c->dpart.p, mi); });
-        ms[2] = timeit([&] { k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r, c->dbinv.p, p, c->dscal.p); });
+        if (c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb)) {
+            // what the mixed solve launches: the product with the direction
+            // update folded in, and the update that stores z
+            float *z = V + 4 * n, *pb = V + 5 * n;
+            k_fill<<<grid, BS, 0, st>>>((int64_t)(2 * n), z, 1.0f);
+            ms[0] = timeit([&] { launch_bspmv_dir(c->bspmv_lpb, st, c, z, p, pb, q, c->dscal.p, c->dpart.p); });
+            ms[1] = timeit([&] { k_cg_update_b3n<true><<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, pb, q, c->dbinv.p, z, c->dscal.p, c->dpart.p, mi); });
+        } else {
+            ms[0] = timeit([&] { launch_bspmv(c->bspmv_lpb, grid, st, c, p, q, c->dscal.p, c->dpart.p); });
+            ms[1] = timeit([&] { k_cg_update_b3n<false><<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, p, q, c->dbinv.p, nullptr, c->dscal.p, c->dpart.p, mi); });
+            ms[2] = timeit([&] { k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r, c->dbinv.p, p, c->dscal.p); });
+        }
         ms[7] = c->bspmv_lpb;
     }
     if (c->have64) {

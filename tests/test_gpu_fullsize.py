@@ -314,10 +314,40 @@ def test_c4_batch_at_full_instance_sizes(deg):
     S.close()
 
 
+def served_residual(req, u):
+    """||R(u)||/N of a served result on the oracle: the request's constraints
+    at their final load step, the values set to u, the FP64 residual of
+    HyperElastic<NeoHookeanCompressible> assembled at u."""
+    X, conn = W.unit_cube("hex", req.side, req.side, req.side)
+    P = O.Problem(O.HEX, X, conn, 1, 3)
+    x, d = P.boundary_points()
+    dofs, comps, vals = [], [], []
+    for xi, di in zip(x, d):
+        if abs(xi[0]) < 1e-9:
+            for c in range(3):
+                dofs.append(di); comps.append(c); vals.append(0.0)
+        if abs(xi[0] - 1.0) < 1e-9:
+            dofs.append(di); comps.append(0); vals.append(req.pull)
+    P.constrain(dofs, comps, vals)
+    neq = P.number()
+    ne = len(conn)
+    P.set_hyperelastic("neohooke", np.full(ne, req.lam), np.full(ne, req.mu), 3)
+    P.set_values(u)
+    _, _, _, b = P.assemble(incremental=True, with_residual=True, nthreads=os.cpu_count() or 1)
+    return np.linalg.norm(b) / neq
+
+
 def test_c5_requests_at_full_size():
-    """Served neo-Hookean requests at the largest c5 sides, batched together:
-    the plain FP64 server (one request per batch) and the mixed server
-    converge and agree within 1e-8."""
+    """Served neo-Hookean requests at the largest c5 sides, batched together,
+    on the plain FP64 server (one request per batch) and on the mixed server
+    (FP32 tangent and CG to 1e-6, FP64 residual).  Both stop by the
+    reference's test (||R||/N or ||dU||/N below 1e-12,
+    solid/CompressibleDriver.hpp:190-211), and the oracle's FP64 residual at
+    each served u confirms it: ||R(u)||/N below 1e-11 (the ||dU|| stop leaves
+    the residual of one more inexact step).  Two results that meet that test
+    differ by about K^-1 R: for the side-48 cube with mu = 0.37, 4e-6 of
+    ||u|| = 59, so the two servers agree within 1e-6 relative, not to the
+    round-off level."""
     from insilico_gb300 import serve
     reqs = [serve.Request(0, side=48, mu=0.37), serve.Request(1, side=29, mu=6.1)]
     out = {}
@@ -326,7 +356,11 @@ def test_c5_requests_at_full_size():
         out[prec], _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
         srv.close()
     assert out[A.PREC_FP32][0].batch_size == 2
-    for rp_, rm in zip(out[A.PREC_FP64], out[A.PREC_FP32]):
+    for req, rp_, rm in zip(reqs, out[A.PREC_FP64], out[A.PREC_FP32]):
         assert rp_.status == A.ISL_OK and rm.status == A.ISL_OK
         assert rp_.converged and rm.converged
-        assert np.linalg.norm(rm.u - rp_.u) <= 1e-8 * np.linalg.norm(rp_.u)
+        rn_p, rn_m = served_residual(req, rp_.u), served_residual(req, rm.u)
+        print(f"side {req.side}: ||R||/N plain {rn_p:.3e} mixed {rn_m:.3e}, "
+              f"rel diff {np.linalg.norm(rm.u - rp_.u) / np.linalg.norm(rp_.u):.3e}")
+        assert rn_p <= 1e-11 and rn_m <= 1e-11
+        assert np.linalg.norm(rm.u - rp_.u) <= 1e-6 * np.linalg.norm(rp_.u)

@@ -201,6 +201,36 @@ def test_persistent_and_graph_block_cg_agree(n):
     S.close()
 
 
+def test_folded_direction_update_matches_separate_kernel():
+    """The graph path of the block CG (c2 at 32^3: 34,848 block rows, above
+    the persistent kernel's limit) with the direction update folded into the
+    SpMV and with the separate direction kernel: both reach the tolerance,
+    agree with the FP64 solve within 1e-8, are bitwise reproducible, take
+    iteration counts within 2 %, and the folded path launches fewer kernels
+    (two per iteration instead of three)."""
+    p = W.config("c2", n=32)
+    S = gpu_problem(p)
+    assert S.get_option(A.OPT_FOLD_DIRECTION) == 1
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP64, tol=1e-13)
+    x64 = S.solution()
+    out = {}
+    for fold in (1, 0):
+        S.set_option(A.OPT_FOLD_DIRECTION, fold)
+        l0 = S.launch_count()
+        it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        launches = S.launch_count() - l0
+        x = S.solution()
+        it2, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+        assert it2 == it and np.array_equal(S.solution(), x)
+        assert rel <= 1e-12
+        assert np.linalg.norm(x - x64) <= 1e-8 * np.linalg.norm(x64)
+        out[fold] = (it, launches)
+    assert abs(out[1][0] - out[0][0]) <= max(2, out[0][0] // 50)
+    assert out[1][1] < out[0][1]
+    S.close()
+
+
 @pytest.mark.parametrize("name,n", [("c1", 40), ("c3", 5), ("c1", 1)])
 def test_cluster_and_graph_scalar_cg_agree(name, n):
     """Small scalar systems are solved whole by one thread-block cluster; the

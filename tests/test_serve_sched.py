@@ -87,3 +87,30 @@ def test_invalid_requests_are_refused_at_submit():
 
 def test_footprint_grows_with_side():
     assert serve.footprint_bytes(48) > 4 * serve.footprint_bytes(24) > 0
+
+
+def test_size_ratio_groups_requests_of_similar_size():
+    """size_ratio > 1: a batch holds only requests whose element count is
+    within that factor of its first request's; the first request of each
+    batch is still the oldest one queued."""
+    reqs = serve.make_requests(24, rate=0.0, side_range=(4, 16))
+    srv = serve.Server(device=0, max_batch=8, max_batches=2, reserve_bytes=0, test_budget_bytes=1 << 50,
+                       test_fake_us_per_elem=0.2, size_ratio=2.0, batch_window_us=200_000)
+    done, _ = srv.run(reqs, realtime=False)
+    srv.close()
+    assert len(done) == 24 and all(r.status == A.ISL_OK for r in done)
+    batches = {}
+    for r in done:
+        batches.setdefault(r.batch_id, []).append(r)
+    for members in batches.values():
+        head = min(members, key=lambda q: q.rid)
+        for q in members:
+            assert q.side ** 3 <= 2.0 * head.side ** 3 and 2.0 * q.side ** 3 >= head.side ** 3
+    first = {b: min(q.rid for q in v) for b, v in batches.items()}
+    assert [first[b] for b in sorted(first)] == sorted(first.values())
+    # without the ratio the same queue forms fewer, mixed batches
+    srv = serve.Server(device=0, max_batch=8, max_batches=2, reserve_bytes=0, test_budget_bytes=1 << 50,
+                       test_fake_us_per_elem=0.2, batch_window_us=200_000)
+    done0, _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
+    srv.close()
+    assert len({r.batch_id for r in done0}) < len(batches)
