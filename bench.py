@@ -58,6 +58,19 @@ def ncu_traffic(name="spmv_fp32_c2"):
     return None
 
 
+def ncu_traffic_ratio(name):
+    """DRAM traffic over algorithmic bytes of a kernel from its committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"{name}.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.strip().startswith("traffic_ratio_to_algorithmic"):
+                    return float(line.split("=")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
 class Clocks:
     """nvidia-smi sampler for the timed region."""
 
@@ -697,7 +710,8 @@ def run_batch(args, rank, world, local, pg):
                                 "plain_fp64_max": max(errs64), "reference": "GPU FP64 CG to 1e-12 per instance"},
             "cg_iters": {"min": int(iters.min()), "median": int(np.median(iters)), "max": int(iters.max())},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "traffic": ncu_traffic("spmv_fp32_c4"), "kernel": kname + " (batched FP32 SpMV, all instances)",
+                         "traffic": (lambda r: None if r is None else r * sp_bytes)(ncu_traffic_ratio("spmv_fp32_c4")),
+                         "kernel": kname + " (batched FP32 SpMV, all instances)",
                          "bytes_per_launch": sp_bytes, "ms_per_launch": sp_ms, "peak_source": src},
             "cpu_baseline": cpu,
             "e2e": {"value": neq * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -313,11 +313,15 @@ int isl_get_csr(isl_ctx* ctx, int64_t* rowptr, int64_t* colind, double* values);
 int isl_sync(isl_ctx* ctx);
 int isl_set_timing(isl_ctx* ctx, int on);
 int isl_timings(isl_ctx* ctx, double* ms /* [ISL_NTIMERS] */, int64_t* counts /* [ISL_NTIMERS] */);
-/* Solver options.  ISL_OPT_BLOCK_SOLVER (default 1): the mixed solve uses a
- * 3x3 node-block copy of the FP32 matrix with block-Jacobi preconditioning
- * when every DOF object's three components are all active or all
- * constrained; 0 keeps the scalar CSR + Jacobi path.  Read-only through
- * isl_get_option: ISL_OPT_BLOCKED (the pattern is node-blocked),
+/* Solver options.  ISL_OPT_BLOCK_SOLVER (default 1): the mixed solve (and
+ * the FP32 solve of a system assembled in ISL_PREC_FP32 alone) of a single
+ * 3-component field uses a 3x3 node-block copy of the FP32 matrix with
+ * block-Jacobi preconditioning; 0 keeps the scalar CSR + Jacobi path.  DOF
+ * objects with some components constrained keep padded blocks (zero rows
+ * and columns at the constrained components, identity in their Jacobi
+ * block; the solver vectors carry zeros there).  Read-only through
+ * isl_get_option: ISL_OPT_BLOCKED (1: node-blocked, 2: node-blocked with
+ * padded blocks, 0: scalar),
  * ISL_OPT_NBLOCKS (stored 3x3 blocks), ISL_OPT_NSLOTS (block slots of the
  * sliced-ELL copy, padding included).  ISL_OPT_PERSISTENT selects the
  * one-launch CG kernels of the mixed solve: 0 never (CUDA graphs of separate

@@ -289,7 +289,7 @@ int ensure_block_maps(isl_ctx* c) {
 // time-integration terms), 2x2x2 points, when the block solver is in use.
 bool affine_blocks_eligible(const isl_ctx* c, const ElemArgs& A) {
     return c->kernel == ISL_KERNEL_HYPERELASTIC && c->shape == ISL_HEX && c->fedeg == 1 && c->ncomp == 3 &&
-           c->blocked && c->use_block && c->ninst == 1 && !A.general && !A.fnodal && !A.rho && A.nfw == 0 &&
+           c->blocked && !c->bpad && c->use_block && c->ninst == 1 && !A.general && !A.fnodal && !A.rho && A.nfw == 0 &&
            c->mesh_affine == 1 && c->nfun == 8 && c->nelem < (1 << 28) && c->nslot < INT32_MAX;
 }
 

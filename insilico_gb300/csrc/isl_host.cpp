@@ -1463,7 +1463,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }
     if (key == ISL_OPT_ELEM_VARIANT) { *value = c->elem_variant; return ISL_OK; }
     if (key == ISL_OPT_PERSISTENT) { *value = c->use_persist; return ISL_OK; }
-    if (key == ISL_OPT_BLOCKED) { *value = c->blocked; return ISL_OK; }
+    if (key == ISL_OPT_BLOCKED) { *value = c->blocked ? (c->bpad ? 2 : 1) : 0; return ISL_OK; }
     if (key == ISL_OPT_NBLOCKS) { *value = c->blocked ? c->nblk : 0; return ISL_OK; }
     if (key == ISL_OPT_NSLOTS) { *value = c->blocked ? c->nslot : 0; return ISL_OK; }
     if (key == ISL_OPT_SPMV32_KIND) { *value = c->spmv_lpr32; return ISL_OK; }

@@ -227,6 +227,12 @@ struct isl_ctx {
     int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
     bool fuse_dir = true;  // fold the block-Jacobi direction update into the block SpMV
+    // padded node blocks: DOF objects with some components constrained keep a
+    // 3x3 block row; the solver vectors live in the padded space (3 nbr
+    // entries, zero at constrained components) and map to equations here
+    bool bpad = false;
+    isl::DBuf<int32_t> dbaeq;    // [3 nbr] equation of each block-row component, -1 constrained
+    isl::DBuf<int32_t> dbcb;     // [nblk] CSR position base: value (r, c) at rowptr[eq_r] + dbcb + eq_c
 
     // scalar sliced-ELL copy of the FP32 matrix for the mixed solver of a
     // system that is not node-blocked: rows sorted by length (longest first)

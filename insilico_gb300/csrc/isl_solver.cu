@@ -489,8 +489,10 @@ static int read_scal(isl_ctx* c) {
 
 static int ensure_work(isl_ctx* c) {
     const size_t n = (size_t)c->neq;
+    // FP32 vectors of the block solver live in the (padded) block space
+    const size_t n32 = std::max(n, c->blocked ? (size_t)(3 * c->nbr) : (size_t)0);
     if (c->w64.n < 6 * n) ISL_CHECK_CUDA(c, c->w64.alloc(6 * n));
-    if (c->w32.n < 6 * n) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n));
+    if (c->w32.n < 6 * n32) ISL_CHECK_CUDA(c, c->w32.alloc(6 * n32));
     // partial sums: two per block of every grid used (at most 16 blocks per SM)
     const size_t maxgrid = (size_t)16 * c->sm_count;
     if (c->dpart.n < 2 * maxgrid + 64) ISL_CHECK_CUDA(c, c->dpart.alloc(2 * maxgrid + 64));
@@ -1210,6 +1212,84 @@ __global__ void k_bsr_values(int nblk, const int* __restrict__ brow, const int* 
     }
 }
 
+// Padded node blocks.  A DOF object with some of its three components
+// constrained keeps a block row; aeq[3 I + c] is the equation of component c
+// of block row I (-1: constrained).  The equations of a DOF object's active
+// components are consecutive and increase with the object, so the lead row
+// (first active component) of I lists, for every block column J, the run of
+// J's equations eqf(J) .. eqf(J) + nact(J) - 1 in order.  Pass 0 counts the
+// runs of every block row (and flags any row that is not of this form: a run
+// that does not start at eqf(J), has the wrong length, or an active row of I
+// whose columns differ from the lead row's); pass 1 writes the block columns,
+// the block rows and the CSR position base of each block.
+__device__ __forceinline__ int pad_first_eq(const int* __restrict__ aeq, int i) {
+    const int e0 = aeq[3 * i], e1 = aeq[3 * i + 1], e2 = aeq[3 * i + 2];
+    return e0 >= 0 ? e0 : (e1 >= 0 ? e1 : e2);
+}
+__device__ __forceinline__ int pad_nact(const int* __restrict__ aeq, int i) {
+    return (aeq[3 * i] >= 0) + (aeq[3 * i + 1] >= 0) + (aeq[3 * i + 2] >= 0);
+}
+__global__ void k_bsr_pattern_pad(int nbr, int pass, const int* __restrict__ aeq, const int* __restrict__ eqblk,
+                                  const int* __restrict__ rowptr, const int* __restrict__ colind, int* __restrict__ cnt,
+                                  const int* __restrict__ bptr, int* __restrict__ bcol, int* __restrict__ brow,
+                                  int* __restrict__ bcb, int* __restrict__ bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbr; i += gridDim.x * blockDim.x) {
+        const int e0 = pad_first_eq(aeq, i);
+        const int lo = rowptr[e0], len = rowptr[e0 + 1] - lo;
+        int nb = 0, bad_i = 0;
+        for (int k = 0; k < len;) {
+            const int j = eqblk[colind[lo + k]];
+            const int f = pad_first_eq(aeq, j), m = pad_nact(aeq, j);
+            if (colind[lo + k] != f || k + m > len) { bad_i = 1; break; }
+            for (int t = 1; t < m; ++t)
+                if (colind[lo + k + t] != f + t) bad_i = 1;
+            if (pass == 1) {
+                const int b = bptr[i] + nb;
+                bcol[b] = j;
+                brow[b] = i;
+                bcb[b] = k - f;
+            }
+            ++nb;
+            k += m;
+        }
+        if (pass == 0) {
+            for (int r = 0; r < 3 && !bad_i; ++r) {
+                const int e = aeq[3 * i + r];
+                if (e < 0 || e == e0) continue;
+                if (rowptr[e + 1] - rowptr[e] != len) { bad_i = 1; break; }
+                for (int k = 0; k < len; ++k)
+                    if (colind[rowptr[e] + k] != colind[lo + k]) { bad_i = 1; break; }
+            }
+            cnt[i] = nb;
+            if (bad_i) atomicOr(bad, 1);
+        }
+    }
+}
+
+// padded block values from the FP32 CSR values: constrained rows and columns
+// hold zeros
+__global__ void k_bsr_values_pad(int nblk, const int* __restrict__ brow, const int* __restrict__ bcol,
+                                 const int* __restrict__ bcb, const int* __restrict__ aeq, const int* __restrict__ rowptr,
+                                 const float* __restrict__ v32, const int* __restrict__ sdst, float* __restrict__ sv,
+                                 float* __restrict__ bv) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblk; b += gridDim.x * blockDim.x) {
+        const int i = brow[b], j = bcol[b], cb = bcb[b];
+        const size_t slot = (size_t)sdst[b];
+        const size_t g = slot >> 5, l = slot & 31;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const int er = aeq[3 * i + r];
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                const int ec = aeq[3 * j + cc];
+                const float v = (er >= 0 && ec >= 0) ? v32[rowptr[er] + cb + ec] : 0.f;
+                sv[(g * 9 + r * 3 + cc) * 32 + l] = v;
+                bv[(size_t)(r * 3 + cc) * nblk + b] = v;
+            }
+        }
+    }
+}
+
 // slice widths (longest block row of each slice of 32)
 __global__ void k_sell_width(int nbr, int nslice, const int* __restrict__ bptr, int* __restrict__ swid) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslice; s += gridDim.x * blockDim.x) {
@@ -1243,6 +1323,30 @@ __global__ void k_sell_fill(int nbr, int nslice, const int* __restrict__ bptr, c
     }
 }
 
+// inverse of a 3x3 block in FP64 (identity for a singular or non-finite block)
+__device__ inline void bj_invert(const double A[3][3], float* __restrict__ out) {
+    const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+    const double c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+    const double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+    double Bi[3][3];
+    if (det != 0.0 && det == det) {
+        const double id = 1.0 / det;
+        Bi[0][0] = c00 * id; Bi[1][0] = c01 * id; Bi[2][0] = c02 * id;
+        Bi[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
+        Bi[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
+        Bi[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) * id;
+        Bi[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
+        Bi[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
+        Bi[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
+    } else {
+        for (int r = 0; r < 3; ++r)
+            for (int cc = 0; cc < 3; ++cc) Bi[r][cc] = (r == cc) ? 1.0 : 0.0;
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int cc = 0; cc < 3; ++cc) out[r * 3 + cc] = (float)Bi[r][cc];
+}
+
 // inverse of the 3x3 diagonal blocks, computed in FP64 from the FP64 values
 // when they exist
 template <typename TV>
@@ -1253,26 +1357,35 @@ __global__ void k_block_jacobi(int nbr, const int* __restrict__ rowptr, const in
         double A[3][3];
         for (int r = 0; r < 3; ++r)
             for (int cc = 0; cc < 3; ++cc) A[r][cc] = (double)val[rowptr[3 * i + r] + 3 * k + cc];
-        const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
-        const double c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
-        const double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
-        const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
-        double Bi[3][3];
-        if (det != 0.0 && det == det) {
-            const double id = 1.0 / det;
-            Bi[0][0] = c00 * id; Bi[1][0] = c01 * id; Bi[2][0] = c02 * id;
-            Bi[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
-            Bi[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
-            Bi[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) * id;
-            Bi[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
-            Bi[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
-            Bi[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
-        } else {
-            for (int r = 0; r < 3; ++r)
-                for (int cc = 0; cc < 3; ++cc) Bi[r][cc] = (r == cc) ? 1.0 : 0.0;
+        bj_invert(A, binv + (size_t)i * 9);
+    }
+}
+
+// the same on padded blocks: the active components' sub-block, the identity
+// on constrained components (whose residual entries stay zero)
+template <typename TV>
+__global__ void k_block_jacobi_pad(int nbr, const int* __restrict__ aeq, const int* __restrict__ diag,
+                                   const TV* __restrict__ val, float* __restrict__ binv) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbr; i += gridDim.x * blockDim.x) {
+        double A[3][3];
+        for (int r = 0; r < 3; ++r) {
+            const int er = aeq[3 * i + r];
+            for (int cc = 0; cc < 3; ++cc) {
+                const int ec = aeq[3 * i + cc];
+                A[r][cc] = (er >= 0 && ec >= 0) ? (double)val[diag[er] + (ec - er)] : (r == cc ? 1.0 : 0.0);
+            }
         }
-        for (int r = 0; r < 3; ++r)
-            for (int cc = 0; cc < 3; ++cc) binv[(size_t)i * 9 + r * 3 + cc] = (float)Bi[r][cc];
+        bj_invert(A, binv + (size_t)i * 9);
+    }
+}
+
+// padded blocks, reliable update part 1: fold the FP32 increment (padded
+// space) into the FP64 iterate (equations)
+__global__ void k_fold_pad(int na, const int* __restrict__ aeq, float* __restrict__ x32, double* __restrict__ x64) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
+        const int e = aeq[a];
+        if (e >= 0) x64[e] += (double)x32[a];
+        x32[a] = 0.0f;
     }
 }
 
@@ -1735,8 +1848,11 @@ static int persist_grid(isl_ctx* c) {
     return c->persist_grid;
 }
 
-// zout (may be null): z = B^-1 r is stored for a folded direction update
-__global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
+// zout (may be null): z = B^-1 r is stored for a folded direction update;
+// aeq (may be null): padded blocks, b is indexed by equation through aeq
+// (zero at constrained components)
+__global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, const int* __restrict__ aeq,
+                                                   float* __restrict__ x, float* __restrict__ r,
                                                    float* __restrict__ p, const float* __restrict__ binv, float* __restrict__ zout,
                                                    CGScal* S, double* part, double tol, int restart, double trig) {
     __shared__ double sh[32];
@@ -1745,7 +1861,8 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
         float ri[3], zi[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const double bi = b[3 * i + a];
+            const int e = aeq ? aeq[3 * i + a] : 3 * i + a;
+            const double bi = e >= 0 ? b[e] : 0.0;
             ri[a] = (float)bi;
             r[3 * i + a] = ri[a];
             if (!restart) { x[3 * i + a] = 0.f; p[3 * i + a] = 0.f; bb += bi * bi; }
@@ -1859,34 +1976,106 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
 }
 
 // detect the node-blocked structure and build the block pattern (setup)
-int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
-    c->blocked = false;
-    if (c->ncomp != 3 || c->neq % 3 != 0) return ISL_OK;
-    for (int64_t o = 0; o < c->ndofobj; ++o) {
-        const uint8_t s0 = c->status[(size_t)o * 3];
-        if (c->status[(size_t)o * 3 + 1] != s0 || c->status[(size_t)o * 3 + 2] != s0) return ISL_OK;
+// padded node blocks (some DOF objects partly constrained): the equation map
+// of the block rows from the host numbering, then the block pattern on the
+// device (k_bsr_pattern_pad); false when the pattern is not of that form
+static int block_pattern_pad(isl_ctx* c, bool* ok) {
+    *ok = false;
+    const int64_t ndo = c->ndofobj, n = c->neq;
+    std::vector<int32_t> aeq, eqblk((size_t)n, -1);
+    aeq.reserve((size_t)3 * ndo);
+    int64_t nbr = 0, next = 0;
+    for (int64_t o = 0; o < ndo; ++o) {
+        const int32_t* q = &c->heq[(size_t)o * 3];
+        if (q[0] < 0 && q[1] < 0 && q[2] < 0) continue;
+        for (int a = 0; a < 3; ++a) {
+            if (q[a] < 0) continue;
+            if (q[a] != next) return ISL_OK;  // equations not consecutive per object
+            eqblk[(size_t)q[a]] = (int32_t)nbr;
+            ++next;
+        }
+        aeq.insert(aeq.end(), q, q + 3);
+        ++nbr;
     }
-    const int64_t nbr = c->neq / 3;
-    for (int64_t i = 0; i < nbr; ++i) {
-        const int32_t len = rp[3 * i + 1] - rp[3 * i];
-        if (rp[3 * i] % 9 || len % 3 || rp[3 * i + 2] - rp[3 * i + 1] != len || rp[3 * i + 3] - rp[3 * i + 2] != len) return ISL_OK;
-    }
+    if (next != n || nbr == 0) return ISL_OK;
+    cudaStream_t st = c->stream;
+    DBuf<int32_t> deqblk, cnt;
+    ISL_CHECK_CUDA(c, c->dbaeq.alloc((size_t)3 * nbr));
+    ISL_CHECK_CUDA(c, deqblk.alloc((size_t)n));
+    ISL_CHECK_CUDA(c, cnt.alloc((size_t)nbr));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dbaeq.p, aeq.data(), aeq.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(deqblk.p, eqblk.data(), eqblk.size() * 4, cudaMemcpyHostToDevice, st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), st));
+    k_bsr_pattern_pad<<<vec_grid(c), BS, 0, st>>>((int)nbr, 0, c->dbaeq.p, deqblk.p, c->drowptr.p, c->dcolind.p, cnt.p,
+                                                  nullptr, nullptr, nullptr, nullptr, c->dflags.p + 1);
+    int bad = 0;
+    std::vector<int32_t> hc((size_t)nbr), bp((size_t)nbr + 1, 0);
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&bad, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(hc.data(), cnt.p, hc.size() * 4, cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    c->launches += 1;
+    if (bad) return ISL_OK;
+    int64_t tot = 0;
+    for (int64_t i = 0; i < nbr; ++i) { bp[(size_t)i] = (int32_t)tot; tot += hc[(size_t)i]; }
+    if (tot >= INT32_MAX / 9) return ISL_OK;
+    bp[(size_t)nbr] = (int32_t)tot;
     c->nbr = nbr;
-    c->nblk = c->nnz / 9;
+    c->nblk = tot;
     ISL_CHECK_CUDA(c, c->dbptr.alloc(nbr + 1));
     ISL_CHECK_CUDA(c, c->dbcol.alloc(c->nblk));
     ISL_CHECK_CUDA(c, c->dbrow.alloc(c->nblk));
-    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), c->stream));
-    k_bsr_pattern<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, c->drowptr.p, c->dcolind.p, c->dbptr.p, c->dbcol.p, c->dbrow.p,
-                                                     c->dflags.p + 1);
-    int bad = 0;
-    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&bad, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    ISL_CHECK_CUDA(c, c->dbcb.alloc(c->nblk));
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(c->dbptr.p, bp.data(), bp.size() * 4, cudaMemcpyHostToDevice, st));
+    k_bsr_pattern_pad<<<vec_grid(c), BS, 0, st>>>((int)nbr, 1, c->dbaeq.p, deqblk.p, c->drowptr.p, c->dcolind.p, cnt.p,
+                                                  c->dbptr.p, c->dbcol.p, c->dbrow.p, c->dbcb.p, c->dflags.p + 1);
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
     c->launches += 1;
-    c->blocked = (bad == 0);
+    *ok = true;
+    return ISL_OK;
+}
+
+int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
+    c->blocked = false;
+    c->bpad = false;
+    c->dbaeq.release();
+    c->dbcb.release();
+    if (c->ncomp != 3 || c->ninst > 1) return ISL_OK;
+    bool uniform = c->neq % 3 == 0;
+    for (int64_t o = 0; uniform && o < c->ndofobj; ++o) {
+        const uint8_t s0 = c->status[(size_t)o * 3];
+        if (c->status[(size_t)o * 3 + 1] != s0 || c->status[(size_t)o * 3 + 2] != s0) uniform = false;
+    }
+    if (uniform) {
+        const int64_t nbr = c->neq / 3;
+        for (int64_t i = 0; i < nbr; ++i) {
+            const int32_t len = rp[3 * i + 1] - rp[3 * i];
+            if (rp[3 * i] % 9 || len % 3 || rp[3 * i + 2] - rp[3 * i + 1] != len || rp[3 * i + 3] - rp[3 * i + 2] != len) return ISL_OK;
+        }
+        c->nbr = nbr;
+        c->nblk = c->nnz / 9;
+        ISL_CHECK_CUDA(c, c->dbptr.alloc(nbr + 1));
+        ISL_CHECK_CUDA(c, c->dbcol.alloc(c->nblk));
+        ISL_CHECK_CUDA(c, c->dbrow.alloc(c->nblk));
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), c->stream));
+        k_bsr_pattern<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, c->drowptr.p, c->dcolind.p, c->dbptr.p, c->dbcol.p, c->dbrow.p,
+                                                         c->dflags.p + 1);
+        int bad = 0;
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(&bad, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+        c->launches += 1;
+        c->blocked = (bad == 0);
+    } else {
+        bool ok = false;
+        const int rc = block_pattern_pad(c, &ok);
+        if (rc != ISL_OK) return rc;
+        c->blocked = c->bpad = ok;
+        if (!ok) { c->dbaeq.release(); c->dbcb.release(); }
+    }
     c->bsr_serial = -1;
     c->bspmv_lpb = 0;
     if (!c->blocked) return ISL_OK;
+    const int64_t nbr = c->nbr;
     // sliced-ELL layout
     c->nslice = (nbr + 31) / 32;
     ISL_CHECK_CUDA(c, c->dswid.alloc(c->nslice));
@@ -2058,36 +2247,55 @@ static int ensure_bsr(isl_ctx* c) {
     if (c->bvals_serial != c->asm_serial) {  // block copies from the FP32 CSR values
         const int rc = ensure_val32(c);
         if (rc != ISL_OK) return rc;
-        k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p,
-                                                 c->dsdst.p, c->dsval.p, c->dbval.p);
+        if (c->bpad)
+            k_bsr_values_pad<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbcol.p, c->dbcb.p, c->dbaeq.p,
+                                                         c->drowptr.p, c->dval32.p, c->dsdst.p, c->dsval.p, c->dbval.p);
+        else
+            k_bsr_values<<<grid, BS, 0, c->stream>>>((int)c->nblk, c->dbrow.p, c->dbptr.p, c->drowptr.p, c->dval32.p,
+                                                     c->dsdst.p, c->dsval.p, c->dbval.p);
         c->launches += 1;
     }
-    if (c->have64)
+    if (c->bpad) {
+        if (c->have64)
+            k_block_jacobi_pad<double><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->dbaeq.p, c->ddiag.p, c->dval64.p, c->dbinv.p);
+        else
+            k_block_jacobi_pad<float><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->dbaeq.p, c->ddiag.p, c->dval32.p, c->dbinv.p);
+    } else if (c->have64) {
         k_block_jacobi<double><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval64.p, c->dbinv.p);
-    else
+    } else {
         k_block_jacobi<float><<<grid, BS, 0, c->stream>>>((int)c->nbr, c->drowptr.p, c->ddiag.p, c->dval32.p, c->dbinv.p);
+    }
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     c->bsr_serial = c->asm_serial;
     return ISL_OK;
 }
 
-// mixed solve on the block copy: FP32 block-Jacobi CG with FP64 reliable updates
+// mixed solve on the block copy: FP32 block-Jacobi CG with FP64 reliable
+// updates; without the FP64 matrix, plain FP32 block-Jacobi CG to the
+// tolerance on its recursive residual (inexact Newton tangents).  The FP32
+// vectors have 3 nbr entries: the equations themselves, or with padded blocks
+// the block rows' components (zero where constrained), mapped to equations
+// when the right-hand side comes in and the increment goes out.
 static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters, double* rel, bool* nc) {
     int rc = ensure_bsr(c);
     if (rc != ISL_OK) return rc;
     cudaStream_t st = c->stream;
     const size_t n = (size_t)c->neq;
     const int nbr = (int)c->nbr;
+    const size_t na = (size_t)3 * nbr;
+    const int* aeq = c->bpad ? c->dbaeq.p : nullptr;
+    const bool exact64 = c->have64;
     double* W = c->w64.p;
     double *x64 = W, *r64 = W + n;
     float* V = c->w32.p;
-    float *x32 = V, *r32 = V + n, *p32 = V + 2 * n, *q32 = V + 3 * n;
+    float *x32 = V, *r32 = V + na, *p32 = V + 2 * na, *q32 = V + 3 * na;
     if (!c->bspmv_lpb) {
-        ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, n * 4, st));
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(p32, 0, na * 4, st));
         c->bspmv_lpb = autotune_lpb(c, p32, q32, c->dscal.p, c->dpart.p);
     }
-    if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
+    if (exact64 && !c->spmv_lpr64)
+        c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, c->drhs.p, W + 3 * n, c->dscal.p, c->dpart.p);
     const int mi = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
     const unsigned grid = vec_grid(c);
     CGScal* S = c->dscal.p;
@@ -2100,8 +2308,9 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     // folded direction update: z = B^-1 r and the second direction buffer
     // take the two spare FP32 vectors of the work area
     const bool fused = pgrid == 0 && c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb);
-    float *z32 = fused ? V + 4 * n : nullptr, *p32b = V + 5 * n;
-    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0, kDelta2);
+    float *z32 = fused ? V + 4 * na : nullptr, *p32b = V + 5 * na;
+    k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0,
+                                      exact64 ? kDelta2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     cudaGraph_t graph;
@@ -2170,17 +2379,27 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
         if (h.fault) { rc = ISL_ERR_TIMEOUT; c->err = "persistent CG: a grid barrier timed out"; break; }
         if (h.bad) { rc = ISL_ERR_NAN; c->err = "CG breakdown (non-finite reduction)"; break; }
         const bool at_max = h.iters >= mi;
-        if (h.done || at_max) {
-            k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
+        if (!(h.done || at_max)) continue;
+        if (aeq) k_fold_pad<<<grid, BS, 0, st>>>((int)na, aeq, x32, x64);
+        else k_fold<<<grid, BS, 0, st>>>((int)n, x32, x64);
+        c->launches += 1;
+        if (!exact64) {
+            rr_true = h.rr;
+            converged = h.done == 1;
+            if (!converged) *nc = true;
+            break;
+        }
+        {
             launch_residual(c->spmv_lpr64, grid, st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, x64, c->drhs.p, r64,
                             c->dpart.p, ticket, dres);
-            c->launches += 2;
+            c->launches += 1;
             ISL_CHECK_CUDA(c, cudaMemcpyAsync(&rr_true, dres, 8, cudaMemcpyDeviceToHost, st));
             ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 1, kDelta2 * rr_true);
+            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 1,
+                                              kDelta2 * rr_true);
             c->launches += 1;
         }
     }
@@ -2197,9 +2416,10 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
 }
 
 int time_bspmv(isl_ctx* c, int nrep, double* ms) {
-    int rc = ensure_bsr(c);
+    int rc = ensure_work(c);
+    if (rc == ISL_OK) rc = ensure_bsr(c);
     if (rc != ISL_OK) return rc;
-    const size_t n = (size_t)c->neq;
+    const size_t n = (size_t)3 * c->nbr;  // the block space (padded blocks included)
     CGScal* S = c->dscal.p;
     float* V = c->w32.p;
     cudaStream_t st = c->stream;
@@ -2230,7 +2450,8 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
     int rc = ensure_work(c);
     if (rc != ISL_OK) return rc;
     // every FP32 path but the node-blocked one reads the scalar FP32 CSR values
-    if (method == ISL_SOLVE_CG_FP32_IR && !(c->blocked && c->use_block && c->have64 && c->ninst == 1 && !c->force_batched)) {
+    if (method == ISL_SOLVE_CG_FP32_IR && !(c->blocked && c->use_block && (c->have64 || c->have32) && c->ninst == 1 &&
+                                            !c->force_batched)) {
         rc = ensure_val32(c);
         if (rc != ISL_OK) return rc;
     }
@@ -2246,7 +2467,7 @@ int solve_device(isl_ctx* c, int method, double tol, int64_t max_iter, int64_t* 
         if (rc == ISL_ERR_NOT_CONVERGED) rc = ISL_OK;
     } else if (method == ISL_SOLVE_BICGSTAB) rc = solve_bicgstab(c, tol, max_iter, &it, &rel, &nc);
     else if (method == ISL_SOLVE_CG_FP64) rc = solve_fp64(c, tol, max_iter, &it, &rel, &nc);
-    else if (c->blocked && c->use_block && c->have64) rc = solve_mixed_b3(c, tol, max_iter, &it, &rel, &nc);
+    else if (c->blocked && c->use_block && (c->have64 || c->have32)) rc = solve_mixed_b3(c, tol, max_iter, &it, &rel, &nc);
     else rc = solve_mixed(c, tol, max_iter, &it, &rel, &nc);
     if (rc != ISL_OK) return rc;
     ISL_CHECK_CUDA(c, cudaGetLastError());
@@ -2367,8 +2588,9 @@ int time_kernels(isl_ctx* c, int nrep, double* ms) {
         rc = ensure_bsr(c);
         if (rc != ISL_OK) return rc;
         float* V = c->w32.p;
-        float *x = V, *r = V + n, *p = V + 2 * n, *q = V + 3 * n;
-        k_fill<<<grid, BS, 0, st>>>((int64_t)(4 * n), V, 1.0f);
+        const size_t na = (size_t)3 * c->nbr;  // the block space (padded blocks included)
+        float *x = V, *r = V + na, *p = V + 2 * na, *q = V + 3 * na;
+        k_fill<<<grid, BS, 0, st>>>((int64_t)(4 * na), V, 1.0f);
         if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, p, q, c->dscal.p, c->dpart.p);
         const int nbr = (int)c->nbr;
         const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);
@@ -2376,8 +2598,8 @@ int time_kernels(isl_ctx* c, int nrep, double* ms) {
         if (c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb)) {
             // what the mixed solve launches: the product with the direction
             // update folded in, and the update that stores z
-            float *z = V + 4 * n, *pb = V + 5 * n;
-            k_fill<<<grid, BS, 0, st>>>((int64_t)(2 * n), z, 1.0f);
+            float *z = V + 4 * na, *pb = V + 5 * na;
+            k_fill<<<grid, BS, 0, st>>>((int64_t)(2 * na), z, 1.0f);
             ms[0] = timeit([&] { launch_bspmv_dir(c->bspmv_lpb, st, c, z, p, pb, q, c->dscal.p, c->dpart.p); });
             ms[1] = timeit([&] { k_cg_update_b3n<true><<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, pb, q, c->dbinv.p, z, c->dscal.p, c->dpart.p, mi); });
         } else {
