@@ -1710,6 +1710,83 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
     }
 }
 
+// The same update with the node records staged through shared memory: a
+// block takes tiles of UT nodes, reads the tile's 3 UT entries of x, r, p, q
+// and its 9 UT inverse-block entries with consecutive threads on consecutive
+// words (every warp load is 128 contiguous bytes, against 384 B and 1,152 B
+// spans of the node-per-thread loads), updates one node per thread from
+// shared memory (strides 3 and 9 words: no bank conflicts), and writes x, r
+// and z back the same coalesced way.  Per-node arithmetic is that of
+// k_cg_update_b3n.
+constexpr int UT = 256;
+template <bool FZ>
+__global__ void __launch_bounds__(UT) k_cg_update_b3t(int nbr, float* __restrict__ x, float* __restrict__ r,
+                                                      const float* __restrict__ p1, const float* __restrict__ p2,
+                                                      const float* __restrict__ q, const float* __restrict__ binv,
+                                                      float* __restrict__ zout, CGScal* S, double* part, int max_iter) {
+    if (S->done) return;
+    __shared__ float sx[3 * UT], sr[3 * UT], sp[3 * UT], sq[3 * UT], sb[9 * UT];
+    __shared__ double sh[32];
+    const float* __restrict__ p = (FZ && !(S->iters & 1)) ? p2 : p1;
+    const float alpha = (float)S->alpha;
+    float rr = 0.f, rz = 0.f;
+    const int ntile = (nbr + UT - 1) / UT;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int nn = min(UT, nbr - t * UT);
+        const size_t d0 = (size_t)3 * UT * t, b0 = (size_t)9 * UT * t;
+        for (int k = threadIdx.x; k < 3 * nn; k += UT) {
+            sx[k] = x[d0 + k];
+            sr[k] = r[d0 + k];
+            sp[k] = __ldg(p + d0 + k);
+            sq[k] = __ldg(q + d0 + k);
+        }
+        for (int k = threadIdx.x; k < 9 * nn; k += UT) sb[k] = __ldg(binv + b0 + k);
+        __syncthreads();
+        if (threadIdx.x < nn) {
+            const int i = threadIdx.x;
+            float rv[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                sx[3 * i + a] += alpha * sp[3 * i + a];
+                rv[a] = sr[3 * i + a] - alpha * sq[3 * i + a];
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                sr[3 * i + a] = rv[a];
+                const float z = sb[9 * i + 3 * a] * rv[0] + sb[9 * i + 3 * a + 1] * rv[1] + sb[9 * i + 3 * a + 2] * rv[2];
+                if (FZ) sp[3 * i + a] = z;  // the node's own p entry is consumed: the slot carries z out
+                rr += rv[a] * rv[a];
+                rz += rv[a] * z;
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < 3 * nn; k += UT) {
+            x[d0 + k] = sx[k];
+            r[d0 + k] = sr[k];
+            if (FZ) zout[d0 + k] = sp[k];
+        }
+        __syncthreads();
+    }
+    const double b1 = block_sum_f(rr, sh);
+    const double b2 = block_sum_f(rz, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (!last_block(&S->ticket2)) return;
+    double trr, trz;
+    reduce_parts2_blk<UT>(part, gridDim.x, sh, trr, trz);
+    if (threadIdx.x == 0) {
+        S->rr = trr;
+        S->iters += 1;
+        S->absOld = S->absNew;
+        S->beta = trz / S->absNew;
+        S->absNew = trz;
+        if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
+        else if (trr < S->threshold) S->done = 1;
+        else if (trr < S->rrtrig) S->done = 3;
+        else if (S->iters >= max_iter) S->done = 2;
+        S->ticket2 = 0;
+    }
+}
+
 __global__ void __launch_bounds__(NBS) k_cg_dir_b3(int nbr, const float* __restrict__ r, const float* __restrict__ binv,
                                                    float* __restrict__ p, const CGScal* S) {
     if (S->done) return;
@@ -1975,6 +2052,70 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
     return best;
 }
 
+// constant fill (timing inputs)
+__global__ void k_fill(int64_t n, float* __restrict__ a, float v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+__global__ void k_fill64(int64_t n, double* __restrict__ a, double v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+// update kernel of the block CG: 1 one thread per node (k_cg_update_b3n, two
+// blocks per SM); 2, 4, 8: tiles of UT nodes staged through shared memory
+// (k_cg_update_b3t) with that many blocks per SM
+static void launch_update(isl_ctx* c, int kind, bool fz, cudaStream_t st, float* x, float* r, const float* p1,
+                          const float* p2, const float* q, float* z, CGScal* S, int mi) {
+    const int nbr = (int)c->nbr;
+    if (kind <= 1) {
+        const unsigned g = node_grid(c, nbr);
+        if (fz) k_cg_update_b3n<true><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+        else k_cg_update_b3n<false><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+        return;
+    }
+    const long long ntile = (nbr + UT - 1) / UT;
+    const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(ntile, (long long)kind * c->sm_count));
+    if (fz) k_cg_update_b3t<true><<<g, UT, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+    else k_cg_update_b3t<false><<<g, UT, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+}
+
+// choose the update kernel by timing each on the current system (vectors
+// filled with ones, a scalar record that never converges); the CG starts
+// from its own initialisation afterwards
+static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
+    if (c->nbr < 8000) return 1;
+    int cached = 0;
+    if (tune_lookup(c, fz ? "bupdate_fz" : "bupdate", &cached) && (cached == 1 || cached == 2 || cached == 4 || cached == 8))
+        return cached;
+    cudaStream_t st = c->stream;
+    k_fill<<<vec_grid(c), BS, 0, st>>>((int64_t)(6 * na), V, 1.0f);
+    CGScal h;
+    memset(&h, 0, sizeof(h));
+    h.absNew = 1.0; h.absOld = 1.0; h.alpha = 1e-6; h.beta = 0.5; h.threshold = -1.0; h.rrtrig = -1.0;
+    const int cand[4] = {1, 2, 4, 8};
+    float ms_of[4];
+    float best = 1e30f;
+    for (int k = 0; k < 4; ++k) {
+        cudaMemcpyAsync(c->dscal.p, &h, sizeof(h), cudaMemcpyHostToDevice, st);
+        auto one = [&]() { launch_update(c, cand[k], fz, st, V, V + na, V + 2 * na, V + 5 * na, V + 3 * na, V + 4 * na,
+                                         c->dscal.p, INT32_MAX - 1); };
+        one();
+        cudaEventRecord(c->ev[2], st);
+        for (int r = 0; r < 20; ++r) one();
+        cudaEventRecord(c->ev[3], st);
+        cudaEventSynchronize(c->ev[3]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        ms_of[k] = ms;
+        best = std::min(best, ms);
+    }
+    c->launches += 4 * 21 + 1;
+    int pick = 1;
+    for (int k = 0; k < 4; ++k)
+        if (ms_of[k] <= 1.02f * best) { pick = cand[k]; break; }
+    tune_store(c, fz ? "bupdate_fz" : "bupdate", pick);
+    return pick;
+}
+
 // detect the node-blocked structure and build the block pattern (setup)
 // padded node blocks (some DOF objects partly constrained): the equation map
 // of the block rows from the host numbering, then the block pattern on the
@@ -2074,6 +2215,7 @@ int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
     }
     c->bsr_serial = -1;
     c->bspmv_lpb = 0;
+    c->bupd_kind[0] = c->bupd_kind[1] = 0;
     if (!c->blocked) return ISL_OK;
     const int64_t nbr = c->nbr;
     // sliced-ELL layout
@@ -2301,14 +2443,17 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     CGScal* S = c->dscal.p;
     double* dres = (double*)(c->dscal.p + 1);
     unsigned* ticket = &(c->dscal.p + 1)->ticket1;
-    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
-    ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     const bool want_persist = c->use_persist == 2 || (c->use_persist == 1 && nbr <= PERSIST_MAX_NBR);
     const int pgrid = want_persist ? persist_grid(c) : 0;
     // folded direction update: z = B^-1 r and the second direction buffer
     // take the two spare FP32 vectors of the work area
     const bool fused = pgrid == 0 && c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb);
     float *z32 = fused ? V + 4 * na : nullptr, *p32b = V + 5 * na;
+    int& ukind = c->bupd_kind[fused ? 1 : 0];
+    if (pgrid == 0 && ukind == 0) ukind = autotune_update(c, V, na, fused);  // before the CG state is set up
+    ISL_CHECK_CUDA(c, cudaGetLastError());
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0,
                                       exact64 ? kDelta2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
@@ -2319,15 +2464,14 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     // DOF-linear vector kernels: one wave of 192-thread blocks
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);  // one pass, no reduction
-    const unsigned nbn = node_grid(c, nbr);
     for (int k = 0; k < CHUNK; ++k) {
         if (fused) {
             launch_bspmv_dir(c->bspmv_lpb, st, c, z32, p32, p32b, q32, S, c->dpart.p);
-            k_cg_update_b3n<true><<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, p32b, q32, c->dbinv.p, z32, S, c->dpart.p, mi);
+            launch_update(c, ukind, true, st, x32, r32, p32, p32b, q32, z32, S, mi);
         } else {
             k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r32, c->dbinv.p, p32, S);
             launch_bspmv(c->bspmv_lpb, grid, st, c, p32, q32, S, c->dpart.p);
-            k_cg_update_b3n<false><<<nbn, NODE_BS, 0, st>>>(nbr, x32, r32, p32, p32, q32, c->dbinv.p, nullptr, S, c->dpart.p, mi);
+            launch_update(c, ukind, false, st, x32, r32, p32, p32, q32, nullptr, S, mi);
         }
     }
     ISL_CHECK_CUDA(c, cudaStreamEndCapture(st, &graph));
@@ -2549,12 +2693,6 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     return ISL_OK;
 }
 
-__global__ void k_fill(int64_t n, float* __restrict__ a, float v) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
-}
-__global__ void k_fill64(int64_t n, double* __restrict__ a, double v) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
-}
 
 // Warm per-kernel timing of one CG iteration's kernels (CUDA events around nrep
 // back-to-back launches each).  ms[0] block SpMV (autotuned kind), ms[1]
@@ -2594,17 +2732,18 @@ int time_kernels(isl_ctx* c, int nrep, double* ms) {
         if (!c->bspmv_lpb) c->bspmv_lpb = autotune_lpb(c, p, q, c->dscal.p, c->dpart.p);
         const int nbr = (int)c->nbr;
         const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);
-        const unsigned nbn = node_grid(c, nbr);
         if (c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb)) {
             // what the mixed solve launches: the product with the direction
             // update folded in, and the update that stores z
             float *z = V + 4 * na, *pb = V + 5 * na;
             k_fill<<<grid, BS, 0, st>>>((int64_t)(2 * na), z, 1.0f);
             ms[0] = timeit([&] { launch_bspmv_dir(c->bspmv_lpb, st, c, z, p, pb, q, c->dscal.p, c->dpart.p); });
-            ms[1] = timeit([&] { k_cg_update_b3n<true><<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, pb, q, c->dbinv.p, z, c->dscal.p, c->dpart.p, mi); });
+            const int uk = c->bupd_kind[1] ? c->bupd_kind[1] : 1;
+            ms[1] = timeit([&] { launch_update(c, uk, true, st, x, r, p, pb, q, z, c->dscal.p, mi); });
         } else {
             ms[0] = timeit([&] { launch_bspmv(c->bspmv_lpb, grid, st, c, p, q, c->dscal.p, c->dpart.p); });
-            ms[1] = timeit([&] { k_cg_update_b3n<false><<<nbn, NODE_BS, 0, st>>>(nbr, x, r, p, p, q, c->dbinv.p, nullptr, c->dscal.p, c->dpart.p, mi); });
+            const int uk = c->bupd_kind[0] ? c->bupd_kind[0] : 1;
+            ms[1] = timeit([&] { launch_update(c, uk, false, st, x, r, p, p, q, nullptr, c->dscal.p, mi); });
             ms[2] = timeit([&] { k_cg_dir_b3<<<nbd, NBS, 0, st>>>(nbr, r, c->dbinv.p, p, c->dscal.p); });
         }
         ms[7] = c->bspmv_lpb;
