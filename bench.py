@@ -331,17 +331,66 @@ def serve_batch_spmv(requests, local):
     return out
 
 
+def serve_request_spmv(requests, local):
+    """The dominant kernel of the served mixed path with one request per
+    batch, timed alone: the FP32 block SpMV (padded node blocks; the direction
+    update folded in where the autotuned variant has it) of each of the given
+    requests, each in its own context set up as the server sets one up.  The
+    contexts' launches go round-robin, one launch each and no launch before
+    it, so each matrix (up to about 130 MB) comes from HBM: the other
+    contexts' matrices have pushed it out of L2."""
+    from insilico_gb300 import _abi as A
+    from insilico_gb300 import serve
+    from insilico_gb300.system import System
+    systems, nbytes = [], []
+    for r in requests:
+        a = serve.request_arrays(r)
+        S = System(device=local)
+        S.upload_mesh(A.HEX, a["X"], a["conn"])
+        S.create_field(1, 3)
+        S.constrain(a["node"], a["comp"], a["val"])
+        S.number_dofs()
+        S.register_pattern()
+        S.set_hyperelastic("neohooke", a["lam"], a["mu"], 3)
+        S.set_option(A.OPT_PERSISTENT, 0)
+        S.assemble(A.PREC_FP32, incremental=True, with_residual=True)
+        S.solve(A.SOLVE_CG_FP32_IR, tol=1e-6, check=False)
+        S.time_spmv(A.PREC_FP32, 1)
+        nbr = (r.side + 1) ** 2 * r.side  # DOF objects left active: all but the clamped x = 0 face
+        kind = S.get_option(A.OPT_SPMV32_KIND) if not S.get_option(A.OPT_BLOCKED) else None
+        folded = bool(S.get_option(A.OPT_BLOCKED)) and S.get_option(A.OPT_FOLD_DIRECTION) and \
+            S.time_kernels(1)["block_kind"] in BSPMV_DIR_KERNEL
+        nbytes.append(S.get_option(A.OPT_NBLOCKS) * 40 + (16 if folded else 8) * 3 * nbr + 8 * ((nbr + 31) // 32))
+        systems.append(S)
+        assert kind is None, "c5 requests are node-blocked (padded blocks)"
+    ms = 0.0
+    rounds = 3
+    for _ in range(rounds):
+        for S in systems:
+            ms += S.time_spmv(A.PREC_FP32, -1)
+    out = {"ms": ms / (rounds * len(systems)), "bytes": sum(nbytes) / len(systems),
+           "neq": int(np.mean([S.neq for S in systems])), "nblocks": int(np.mean([S.get_option(A.OPT_NBLOCKS) for S in systems])),
+           "requests": len(systems), "sides": [r.side for r in requests], "folded": bool(folded)}
+    for S in systems:
+        S.close()
+    return out
+
+
 def run_serve(args, rank, world, local, pg):
     """c5: served neo-Hookean Newton requests (PulledSheet boundary conditions,
-    5 load steps to stretch 1.3) through the native continuous-batching
-    server.  The same seeded request stream runs through
-      * the mixed server: batches of requests sharing every launch, FP32
-        tangent + FP32 CG to 1e-6 per Newton step (inexact Newton), FP64
-        residual;
-      * the mixed server at the plain path's linear tolerance: FP64 + FP32
+    5 load steps to stretch 1.3) through the native server.  The same seeded
+    request stream runs through
+      * the mixed server (--batch requests per batch, --slots batches at
+        once; by default one request per batch and 8 at once, each request's
+        FP32 block CG on padded node blocks): FP32 tangent + FP32 CG to 1e-6
+        per Newton step (inexact Newton), FP64 residual;
+      * the same server at the plain path's linear tolerance: FP64 + FP32
         matrices, FP32 CG with FP64 reliable updates to 1e-10;
-      * the plain path: one request per batch (no shared launches), FP64
-        tangent + FP64 CG to 1e-10, up to 8 requests at once;
+      * the shared-launch server: batches of up to 12 requests sharing every
+        launch of a Newton iteration (batched scalar CG), 4 batches at once,
+        FP32 as the mixed server;
+      * the plain path: one request per batch, FP64 tangent + FP64 CG (point
+        Jacobi, CSR: the reference's algorithm) to 1e-10, 8 at once;
     closed loop (all requests queued at t = 0: throughput and latency under
     full load) and open loop (Poisson arrivals at half the plain path's
     closed-loop throughput)."""
@@ -356,8 +405,11 @@ def run_serve(args, rank, world, local, pg):
                       size_ratio=ratio),
         "mixed_equal_tol": dict(precision=A.PREC_MIXED, max_batch=args.batch, max_batches=args.slots, lin_tol=1e-10,
                                 batch_window_us=win, size_ratio=ratio),
+        "mixed_shared_launches": dict(precision=A.PREC_FP32, max_batch=12, max_batches=4, batch_window_us=20000),
         "plain": dict(precision=A.PREC_FP64, max_batch=1, max_batches=8),
     }
+    for kw in arms.values():
+        kw["persistent"] = args.persist
     if args.c5_mixed_only:  # configuration sweeps of the mixed server (no line is printed)
         arms = {"mixed": arms["mixed"]}
     out = {}
@@ -391,7 +443,17 @@ def run_serve(args, rank, world, local, pg):
     for m in arms:
         out[m]["srv"].close()
     reqs = serve.make_requests(nreq, rate=0.0)
-    sp = serve_batch_spmv(reqs[:16], local)
+    if args.batch == 1:
+        big = sorted(reqs, key=lambda q: -q.side)[:8]
+        sp = serve_request_spmv(big, local)
+        sp_kernel = ("k_bspmv_dir<U,MINB>" if sp["folded"] else "k_bspmv") + \
+            f" (FP32 padded 3x3 block SpMV of one request, the 8 largest of the stream, sides {sp['sides']}, " \
+            "launched round-robin from HBM)"
+        sp_batch = {k: sp[k] for k in ("neq", "nblocks", "requests")}
+    else:
+        sp = serve_batch_spmv(reqs[:16], local)
+        sp_kernel = "kb_sspmv<4,8> (batched FP32 SpMV of a 16-request batch, all instances active)"
+        sp_batch = {k: sp[k] for k in ("neq", "nnz", "instances")}
     hbm, src = peaks()
     ach = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
     cpu, err_oracle = None, None
@@ -425,9 +487,19 @@ def run_serve(args, rank, world, local, pg):
                                    "kappa = 10 mu, 5 load steps to stretch 1.3",
                        "requests": nreq, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "per-request meshes are set up, assembled and solved from host inputs"},
-            "method": f"native server: batches of up to {args.batch} requests share every launch of a Newton "
-                      f"iteration, {args.slots} batches at once, batching window {win} us; FP32 tangent + FP32 CG "
-                      f"to 1e-6, FP64 residual; plain: one request per batch, 8 at once, FP64",
+            "method": (f"native server: one request per batch, {args.slots} at once, each request's FP32 block CG "
+                       f"(padded 3x3 node blocks, block Jacobi) on its own stream" if args.batch == 1 else
+                       f"native server: batches of up to {args.batch} requests share every launch of a Newton "
+                       f"iteration, {args.slots} batches at once, batching window {win} us") +
+                      "; FP32 tangent + FP32 CG to 1e-6, FP64 residual; plain: one request per batch, 8 at once, "
+                      "FP64 tangent + FP64 point-Jacobi CSR CG to 1e-10",
+            "mixed_shared_launches": {"requests_per_s": out["mixed_shared_launches"]["closed"]["solves_per_s"],
+                                      "p50": out["mixed_shared_launches"]["closed"]["p50_s"],
+                                      "p99": out["mixed_shared_launches"]["closed"]["p99_s"],
+                                      "cg_iters": out["mixed_shared_launches"]["closed"]["cg_iters"],
+                                      "batches": out["mixed_shared_launches"]["batches"],
+                                      "config": "batches of up to 12 requests sharing every launch (batched scalar "
+                                                "FP32 CG), 4 at once, batching window 20 ms"},
             "server_host_seconds": {m: out[m]["times"] for m in arms},
             "latency_s": {"mixed_closed": {"p50": mc["p50_s"], "p99": mc["p99_s"]},
                           "plain_closed": {"p50": pc["p50_s"], "p99": pc["p99_s"]},
@@ -446,10 +518,9 @@ def run_serve(args, rank, world, local, pg):
             "rel_err_vs_fp64": errs_vs_plain("mixed"), "rel_err_vs_oracle_request0": err_oracle,
             "converged": all(out[m]["converged"] for m in arms),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "traffic": None, "kernel": "kb_sspmv<4,8> (batched FP32 SpMV of a 16-request batch, "
-                                                    "all instances active)",
+                         "traffic": None, "kernel": sp_kernel,
                          "bytes_per_launch": sp["bytes"], "ms_per_launch": sp["ms"], "peak_source": src,
-                         "batch": {k: sp[k] for k in ("neq", "nnz", "instances")}},
+                         "batch": sp_batch},
             "cpu_baseline": cpu,
             "e2e": {"value": mc["solves_per_s"] * world, "unit": "requests/s",
                     "h2d_bytes_per_step": int(out["mixed"]["h2d"] / nreq),
@@ -765,8 +836,10 @@ def main():
                          "64^3; c4: 4096 batched Q1/Q2 Poisson instances; c5: served neo-Hookean Newton requests; "
                          "heat: nonlinear heat Newton run (heat::Static, BiCGSTAB), square 200")
     ap.add_argument("--requests", type=int, default=48, help="c5: requests per run")
-    ap.add_argument("--slots", type=int, default=4, help="c5: batches the mixed server runs at once")
-    ap.add_argument("--batch", type=int, default=12, help="c5: requests per batch of the mixed server")
+    ap.add_argument("--slots", type=int, default=8, help="c5: batches the mixed server runs at once")
+    ap.add_argument("--batch", type=int, default=1, help="c5: requests per batch of the mixed server")
+    ap.add_argument("--persist", type=int, default=0,
+                    help="c5: 1 lets single-request batches solve small systems in one launch (ISL_OPT_PERSISTENT)")
     ap.add_argument("--batch-window-us", type=int, default=20000, help="c5: batching window of the mixed server")
     ap.add_argument("--size-ratio", type=float, default=0.0,
                     help="c5: > 1 batches only requests within this element-count factor of the batch's first")

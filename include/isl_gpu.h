@@ -398,7 +398,9 @@ int isl_device_memory(int device, int64_t* free_bytes, int64_t* total_bytes);
  * context since creation. */
 int isl_launch_count(isl_ctx* ctx, int64_t* n);
 /* Average device time (ms) of one launch of the solver's SpMV kernel on the
- * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches.
+ * current matrix, precision ISL_PREC_FP64 or ISL_PREC_FP32, over nrep launches
+ * that follow one untimed launch; nrep < 0: over -nrep launches with no
+ * launch before them (the first starts from whatever the caches hold).
  * On a batch: the batched SpMV of isl_solve with every instance active (the
  * FP32 kind the last mixed solve chose). */
 int isl_time_spmv(isl_ctx* ctx, int precision, int nrep, double* ms_per_launch);
@@ -474,6 +476,10 @@ typedef struct {
     double size_ratio;        /* > 1: a batch takes only requests whose element count is within this factor of
                                  its first request's (requests of other sizes wait for a batch of their own);
                                  <= 1: any size */
+    int persistent;           /* ISL_OPT_PERSISTENT of single-request batches' contexts: 0 (default) CUDA graphs
+                                 of separate kernels, which overlap with the other batches' launches; 1 the
+                                 library default (small systems solved in one launch: a cooperative grid over
+                                 every SM, or one thread-block cluster) */
 } isl_serve_config;
 typedef struct {
     int shape;                /* ISL_QUAD, ISL_TET, ISL_HEX */

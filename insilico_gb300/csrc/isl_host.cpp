@@ -1386,7 +1386,7 @@ int isl_timings(isl_ctx* c, double* ms, int64_t* counts) {
 
 int isl_time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     ISL_TRY
-    if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep <= 0) return ISL_ERR_ARG;
+    if (!c || !c->pattern_ready || c->neq == 0 || !ms || nrep == 0) return ISL_ERR_ARG;
     return isl::time_spmv(c, precision, nrep, ms);
     ISL_CATCH(c)
 }

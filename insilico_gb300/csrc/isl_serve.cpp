@@ -258,6 +258,10 @@ void run_batch(isl_server* s, Batch& b) {
     if (batched) {
         SV_CHECK(isl_set_option(c, ISL_OPT_BATCHED_SOLVE, 1));
         if (s->cfg.precision != ISL_PREC_FP64) SV_CHECK(isl_set_option(c, ISL_OPT_SPMV32_KIND, 104));
+    } else {
+        // a one-launch solve of a small system holds every SM (cooperative
+        // grid) and would serialise the batches that run at the same time
+        SV_CHECK(isl_set_option(c, ISL_OPT_PERSISTENT, s->cfg.persistent == 1 ? 1 : 0));
     }
     std::vector<int64_t> eq_off(n + 1), dof_off(n + 1);
     int64_t ninst = 0;

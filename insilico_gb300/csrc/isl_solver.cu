@@ -222,8 +222,11 @@ __global__ void __launch_bounds__(BS) k_residual64(int n, const int* __restrict_
 }
 
 // reliable update, part 2: r32 = r64; beta = (r.z)_new / (r.z)_previous; resume
+// fresh != 0: the true residual has not dropped since the previous reliable
+// update, so the FP32 directions have lost conjugacy: restart them (beta = 0)
 __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restrict__ r64, float* __restrict__ r32,
-                                                  const float* __restrict__ dinv, CGScal* S, double* part, double rrtrig) {
+                                                  const float* __restrict__ dinv, CGScal* S, double* part, double rrtrig,
+                                                  int fresh) {
     __shared__ double sh[32];
     double rr = 0.0, rz = 0.0;
     for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(BS) k_restart32(int n, const double* __restric
         reduce_parts2_blk<BS>(part, gridDim.x, sh, trr, trz);
         if (threadIdx.x == 0) {
             S->rr = trr;
-            S->beta = trz / S->absOld;
+            S->beta = fresh ? 0.0 : trz / S->absOld;
             S->absNew = trz;
             S->rrtrig = rrtrig;
             S->done = 0;
@@ -624,7 +627,7 @@ __device__ inline void cluster_sum2(T a, T b, double (*red)[2], int& slot, doubl
 // FP64 divisions and tests run once per CTA instead of once per thread.
 struct ClusterScalars {
     double rz, rz_old, beta, rr, thr, trig, rr_true;
-    int iters, max_iter, exact64, bad;
+    int iters, max_iter, exact64, bad, nupd;
 };
 enum { CTL_GO = 0, CTL_DONE = 1, CTL_MAX = 2, CTL_UPDATE = 3, CTL_BAD = 4 };
 
@@ -661,16 +664,20 @@ __device__ inline int cs_update(ClusterScalars& s, double trr, double trz, float
 
 // after the FP64 residual of a reliable update: converged, iteration limit,
 // breakdown, or a restart from the true residual with the same direction
+// (fresh directions, beta = 0, when the true residual has not dropped since
+// the previous reliable update: the FP32 directions have lost conjugacy)
 __device__ inline int cs_residual(ClusterScalars& s, double rr_true, double rr_restart, double rz_restart, float* sf, int* si) {
     if (threadIdx.x == 0) {
+        const bool fresh = s.nupd > 0 && rr_true >= s.rr_true;
         s.rr_true = rr_true;
+        s.nupd += 1;
         int ctl = CTL_GO;
         if (!(rr_true == rr_true)) { s.bad = 1; ctl = CTL_BAD; }
         else if (rr_true <= s.thr) ctl = CTL_DONE;
         else if (s.iters >= s.max_iter) ctl = CTL_MAX;
         else {
             s.rr = rr_restart;
-            s.beta = rz_restart / s.rz_old;
+            s.beta = fresh ? 0.0 : rz_restart / s.rz_old;
             s.rz = rz_restart;
             s.trig = kDelta2 * rr_true;
             sf[1] = (float)s.beta;
@@ -694,6 +701,7 @@ __device__ inline ClusterScalars cs_load(const CGScal* S, int max_iter, int exac
     s.max_iter = max_iter;
     s.exact64 = exact64;
     s.bad = 0;
+    s.nupd = 0;
     return s;
 }
 
@@ -1110,6 +1118,7 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
     double rr_true = bnorm2;
+    double rr_last = 0.0;  // true residual of the previous reliable update
     const int64_t max_replays = (int64_t)mi + 64;
     int64_t replays = 0;
     bool converged = (bnorm2 == 0.0);
@@ -1144,7 +1153,9 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p, kDelta2 * rr_true);
+            const int fresh = (rr_last > 0.0 && rr_true >= rr_last) ? 1 : 0;
+            rr_last = rr_true;
+            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p, kDelta2 * rr_true, fresh);
             c->launches += 1;
         }
     }
@@ -1928,6 +1939,8 @@ static int persist_grid(isl_ctx* c) {
 // zout (may be null): z = B^-1 r is stored for a folded direction update;
 // aeq (may be null): padded blocks, b is indexed by equation through aeq
 // (zero at constrained components)
+// restart == 2: a reliable update after which the FP32 directions restart
+// (beta = 0): the true residual has not dropped since the previous update
 __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __restrict__ b, const int* __restrict__ aeq,
                                                    float* __restrict__ x, float* __restrict__ r,
                                                    float* __restrict__ p, const float* __restrict__ binv, float* __restrict__ zout,
@@ -1970,7 +1983,7 @@ __global__ void __launch_bounds__(BS) k_cg_init_b3(int nbr, const double* __rest
                 S->ticket1 = 0;
             } else {
                 S->rr = tbb;
-                S->beta = tbz / S->absOld;
+                S->beta = restart == 2 ? 0.0 : tbz / S->absOld;
                 S->absNew = tbz;
                 S->rrtrig = trig;
                 S->done = 0;
@@ -2495,6 +2508,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     rc = read_scal(c);
     const double bnorm2 = c->hscal->rhsNorm2;
     double rr_true = bnorm2;
+    double rr_last = 0.0;  // true residual of the previous reliable update
     const int64_t max_replays = (int64_t)mi + 64;
     int64_t replays = 0;
     bool converged = (bnorm2 == 0.0);
@@ -2542,8 +2556,10 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             if (!(rr_true == rr_true)) { rc = ISL_ERR_NAN; c->err = "refinement residual is not finite"; break; }
             if (rr_true <= tol * tol * bnorm2) { converged = true; break; }
             if (at_max) { *nc = true; break; }
-            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 1,
-                                              kDelta2 * rr_true);
+            const int fresh = (rr_last > 0.0 && rr_true >= rr_last) ? 1 : 0;
+            rr_last = rr_true;
+            k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol,
+                                              fresh ? 2 : 1, kDelta2 * rr_true);
             c->launches += 1;
         }
     }
@@ -2560,6 +2576,8 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
 }
 
 int time_bspmv(isl_ctx* c, int nrep, double* ms) {
+    const bool warm = nrep > 0;  // one untimed launch first
+    nrep = std::abs(nrep);
     int rc = ensure_work(c);
     if (rc == ISL_OK) rc = ensure_bsr(c);
     if (rc != ISL_OK) return rc;
@@ -2578,11 +2596,11 @@ int time_bspmv(isl_ctx* c, int nrep, double* ms) {
         if (fused) launch_bspmv_dir(c->bspmv_lpb, st, c, V + 4 * n, V + 2 * n, V + 5 * n, V + 3 * n, S, c->dpart.p);
         else launch_bspmv(c->bspmv_lpb, vec_grid(c), st, c, V + 2 * n, V + 3 * n, S, c->dpart.p);
     };
-    one();
+    if (warm) one();
     cudaEventRecord(c->ev[2], st);
     for (int r = 0; r < nrep; ++r) one();
     cudaEventRecord(c->ev[3], st);
-    c->launches += nrep + 1;
+    c->launches += nrep + (warm ? 1 : 0);
     ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
     float t = 0.f;
     cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
@@ -2649,7 +2667,9 @@ int distribute_device(isl_ctx* c, int add) {
 }
 
 int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
-    if (c->ninst > 1 || c->force_batched) return time_spmv_batched(c, precision, nrep, ms);
+    if (c->ninst > 1 || c->force_batched) return time_spmv_batched(c, precision, std::abs(nrep), ms);
+    const bool warm = nrep > 0;  // one untimed launch first
+    nrep = std::abs(nrep);
     int rc = ensure_work(c);
     if (rc != ISL_OK) return rc;
     const size_t n = (size_t)c->neq;
@@ -2658,7 +2678,7 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
     ISL_CHECK_CUDA(c, cudaMemsetAsync(S, 0, sizeof(CGScal), st));
     if (precision == ISL_PREC_FP32 && c->blocked && c->use_block) {
         if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
-        return time_bspmv(c, nrep, ms);
+        return time_bspmv(c, warm ? nrep : -nrep, ms);
     }
     if (precision == ISL_PREC_FP32) {
         if (!c->have32) ISL_FAIL(c, ISL_ERR_ARG, "no FP32 matrix");
@@ -2669,7 +2689,7 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
         rc = ensure_ssell(c);
         if (rc != ISL_OK) return rc;
         if (!c->spmv_lpr32) c->spmv_lpr32 = autotune_spmv32(c, V + 2 * n, V + 3 * n, S, c->dpart.p);
-        launch_spmv32(c, c->spmv_lpr32, vec_grid(c), st, V + 2 * n, V + 3 * n, S, c->dpart.p);
+        if (warm) launch_spmv32(c, c->spmv_lpr32, vec_grid(c), st, V + 2 * n, V + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[2], st);
         for (int r = 0; r < nrep; ++r) launch_spmv32(c, c->spmv_lpr32, vec_grid(c), st, V + 2 * n, V + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[3], st);
@@ -2678,13 +2698,14 @@ int time_spmv(isl_ctx* c, int precision, int nrep, double* ms) {
         double* W = c->w64.p;
         ISL_CHECK_CUDA(c, cudaMemsetAsync(W + 2 * n, 0, n * 8, st));
         if (!c->spmv_lpr64) c->spmv_lpr64 = autotune_lpr<double, double>(c, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
-        launch_spmv<double, double>(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
+        if (warm)
+            launch_spmv<double, double>(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[2], st);
         for (int r = 0; r < nrep; ++r)
             launch_spmv<double, double>(c->spmv_lpr64, vec_grid(c), st, (int)n, c->drowptr.p, c->dcolind.p, c->dval64.p, W + 2 * n, W + 3 * n, S, c->dpart.p);
         cudaEventRecord(c->ev[3], st);
     }
-    c->launches += nrep + 1;
+    c->launches += nrep + (warm ? 1 : 0);
     ISL_CHECK_CUDA(c, cudaEventSynchronize(c->ev[3]));
     float t = 0.f;
     cudaEventElapsedTime(&t, c->ev[2], c->ev[3]);
