@@ -38,6 +38,32 @@ def test_served_newton_matches_oracle_driver(precision):
             assert got.newton_iters == newton
 
 
+@pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("precision", [A.PREC_FP32, A.PREC_MIXED])
+def test_one_request_per_batch_matches_oracle_driver(precision, persistent):
+    """max_batch = 1: every request on its own context and stream, through
+    the single-system solvers (the block CG on padded node blocks: the x = 1
+    face fixes u_x only), several at once; the graph path (persistent 0, the
+    server's default) and the one-launch solve (1).  Sides 10 and 12 give
+    1,210 and 2,028 block rows.  Each result reproduces the oracle's run of
+    the reference driver within 1e-8, and the same request gives the same
+    bits in a second run."""
+    reqs = [serve.Request(0, side=3, mu=1.7), serve.Request(1, side=10, mu=0.3), serve.Request(2, side=12, mu=6.0),
+            serve.Request(3, side=4, mu=0.12)]
+    out = []
+    for _ in range(2):
+        srv = serve.Server(precision=precision, max_batch=1, max_batches=3, persistent=persistent)
+        done, _ = srv.run([serve.Request(r.rid, r.side, r.mu) for r in reqs], realtime=False)
+        srv.close()
+        assert all(r.status == A.ISL_OK and r.converged and r.batch_size == 1 for r in done), \
+            [(r.status, r.error) for r in done]
+        out.append(done)
+    for r, got, again in zip(reqs, out[0], out[1]):
+        uo, _ = oracle_newton_driver(r, serve.NEWTON_TOL, serve.MAX_NEWTON)
+        assert np.linalg.norm(got.u - uo) <= 1e-8 * np.linalg.norm(uo), (precision, r.rid)
+        assert np.array_equal(got.u, again.u) and got.cg_iters == again.cg_iters
+
+
 def test_result_same_alone_and_in_a_batch():
     reqs = serve.make_requests(6, rate=0.0, side_range=(3, 7))
     # alone: a batching server given a single request (a batch of one)
