@@ -355,9 +355,10 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
        ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14, ISL_OPT_BLOCK_UPDATE = 15 };
 /* ISL_OPT_BLOCK_UPDATE: the update kernel of the graph path of the block CG
  * (x, r, z = B^-1 r, r.r, r.z): 1 one thread per node, 2, 4 or 8 tiles of 256
- * nodes staged through shared memory with that many blocks per SM; 0
- * (default) autotuned at the first such solve.  Read back: the kernel in use
- * (0 before the first solve). */
+ * nodes staged through shared memory with that many blocks per SM, 12 or 14
+ * two or four nodes per thread with their loads issued together; 0 (default)
+ * autotuned at the first such solve.  Read back: the kernel in use (0 before
+ * the first solve). */
 /* ISL_OPT_FOLD_DIRECTION (default 1): the graph path of the node-blocked
  * mixed solve forms the search direction p = B^-1 r + beta p inside the block
  * SpMV (the update kernel stores z = B^-1 r; each column block of p is formed

@@ -1425,8 +1425,8 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (key == ISL_OPT_BATCHED_SOLVE) { c->force_batched = value != 0; return ISL_OK; }
     if (key == ISL_OPT_FOLD_DIRECTION) { c->fuse_dir = value != 0; return ISL_OK; }
     if (key == ISL_OPT_BLOCK_UPDATE) {
-        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
-            ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_BLOCK_UPDATE takes 0, 1, 2, 4 or 8");
+        if (value != 0 && !isl::update_kind_valid((int)value))
+            ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_BLOCK_UPDATE takes 0, 1, 2, 4, 8, 12 or 14");
         c->bupd_kind[0] = c->bupd_kind[1] = (int)value;
         return ISL_OK;
     }

@@ -348,6 +348,7 @@ namespace isl {
 // in memory and, when a file is set (isl_tune_cache or ISL_TUNE_CACHE), in
 // that file, so that later contexts and processes skip the timing.
 bool tune_lookup(const isl_ctx* c, const char* tuner, int* value);
+bool update_kind_valid(int kind);  // ISL_OPT_BLOCK_UPDATE values other than 0
 void tune_store(isl_ctx* c, const char* tuner, int value);
 // device-side entry points implemented in the .cu files
 int pattern_build(isl_ctx* c);

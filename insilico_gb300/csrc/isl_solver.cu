@@ -1721,6 +1721,83 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
     }
 }
 
+// The same update with UN nodes per thread whose loads (9 inverse-block and
+// 12 vector entries each) are all issued before any of them is used: one
+// memory round trip per UN nodes instead of one per node.  Nodes of one pass
+// are UN runs of NODE_BS consecutive nodes, so each warp load spans the same
+// 32 nodes as in the one-node kernel.  Per-node arithmetic is that of
+// k_cg_update_b3n; r.r and r.z are accumulated in pass order.
+template <bool FZ, int UN>
+__global__ void __launch_bounds__(NODE_BS) k_cg_update_b3m(int nbr, float* __restrict__ x, float* __restrict__ r,
+                                                           const float* __restrict__ p1, const float* __restrict__ p2,
+                                                           const float* __restrict__ q, const float* __restrict__ binv,
+                                                           float* __restrict__ zout, CGScal* S, double* part,
+                                                           int max_iter) {
+    if (S->done) return;
+    __shared__ double sh[32];
+    const float* __restrict__ p = (FZ && !(S->iters & 1)) ? p2 : p1;
+    const float alpha = (float)S->alpha;
+    float rr = 0.f, rz = 0.f;
+    for (int base = blockIdx.x * NODE_BS * UN; base < nbr; base += gridDim.x * NODE_BS * UN) {
+        float b[UN][9], xv[UN][3], rv[UN][3], pv[UN][3], qv[UN][3];
+#pragma unroll
+        for (int u = 0; u < UN; ++u) {
+            const int i = base + u * NODE_BS + (int)threadIdx.x;
+            if (i < nbr) {
+                const size_t d = 3 * (size_t)i;
+#pragma unroll
+                for (int k = 0; k < 9; ++k) b[u][k] = ld(binv + 9 * (size_t)i + k);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    xv[u][a] = x[d + a];
+                    rv[u][a] = r[d + a];
+                    pv[u][a] = ld(p + d + a);
+                    qv[u][a] = ld(q + d + a);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UN; ++u) {
+            const int i = base + u * NODE_BS + (int)threadIdx.x;
+            if (i < nbr) {
+                const size_t d = 3 * (size_t)i;
+                float rn[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    x[d + a] = xv[u][a] + alpha * pv[u][a];
+                    rn[a] = rv[u][a] - alpha * qv[u][a];
+                }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    r[d + a] = rn[a];
+                    const float z = b[u][3 * a] * rn[0] + b[u][3 * a + 1] * rn[1] + b[u][3 * a + 2] * rn[2];
+                    if (FZ) zout[d + a] = z;
+                    rr += rn[a] * rn[a];
+                    rz += rn[a] * z;
+                }
+            }
+        }
+    }
+    const double b1 = block_sum_f(rr, sh);
+    const double b2 = block_sum_f(rz, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    if (!last_block(&S->ticket2)) return;
+    double trr, trz;
+    reduce_parts2_blk<NODE_BS>(part, gridDim.x, sh, trr, trz);
+    if (threadIdx.x == 0) {
+        S->rr = trr;
+        S->iters += 1;
+        S->absOld = S->absNew;
+        S->beta = trz / S->absNew;
+        S->absNew = trz;
+        if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
+        else if (trr < S->threshold) S->done = 1;
+        else if (trr < S->rrtrig) S->done = 3;
+        else if (S->iters >= max_iter) S->done = 2;
+        S->ticket2 = 0;
+    }
+}
+
 // The same update with the node records staged through shared memory: a
 // block takes tiles of UT nodes, reads the tile's 3 UT entries of x, r, p, q
 // and its 9 UT inverse-block entries with consecutive threads on consecutive
@@ -2065,6 +2142,8 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
     return best;
 }
 
+bool update_kind_valid(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 12 || k == 14; }
+
 // constant fill (timing inputs)
 __global__ void k_fill(int64_t n, float* __restrict__ a, float v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
@@ -2075,10 +2154,25 @@ __global__ void k_fill64(int64_t n, double* __restrict__ a, double v) {
 
 // update kernel of the block CG: 1 one thread per node (k_cg_update_b3n, two
 // blocks per SM); 2, 4, 8: tiles of UT nodes staged through shared memory
-// (k_cg_update_b3t) with that many blocks per SM
+// (k_cg_update_b3t) with that many blocks per SM; 12, 14: 2 or 4 nodes per
+// thread with all their loads issued first (k_cg_update_b3m), at most two
+// blocks per SM
 static void launch_update(isl_ctx* c, int kind, bool fz, cudaStream_t st, float* x, float* r, const float* p1,
                           const float* p2, const float* q, float* z, CGScal* S, int mi) {
     const int nbr = (int)c->nbr;
+    if (kind == 12 || kind == 14) {
+        const int un = kind == 12 ? 2 : 4;
+        const long long per = (long long)NODE_BS * un;
+        const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((nbr + per - 1) / per, 2LL * c->sm_count));
+        if (kind == 12) {
+            if (fz) k_cg_update_b3m<true, 2><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+            else k_cg_update_b3m<false, 2><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+        } else {
+            if (fz) k_cg_update_b3m<true, 4><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+            else k_cg_update_b3m<false, 4><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
+        }
+        return;
+    }
     if (kind <= 1) {
         const unsigned g = node_grid(c, nbr);
         if (fz) k_cg_update_b3n<true><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
@@ -2097,17 +2191,16 @@ static void launch_update(isl_ctx* c, int kind, bool fz, cudaStream_t st, float*
 static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
     if (c->nbr < 8000) return 1;
     int cached = 0;
-    if (tune_lookup(c, fz ? "bupdate_fz" : "bupdate", &cached) && (cached == 1 || cached == 2 || cached == 4 || cached == 8))
-        return cached;
+    if (tune_lookup(c, fz ? "bupdate_fz" : "bupdate", &cached) && update_kind_valid(cached)) return cached;
     cudaStream_t st = c->stream;
     k_fill<<<vec_grid(c), BS, 0, st>>>((int64_t)(6 * na), V, 1.0f);
     CGScal h;
     memset(&h, 0, sizeof(h));
     h.absNew = 1.0; h.absOld = 1.0; h.alpha = 1e-6; h.beta = 0.5; h.threshold = -1.0; h.rrtrig = -1.0;
-    const int cand[4] = {1, 2, 4, 8};
-    float ms_of[4];
+    const int cand[6] = {1, 14, 12, 2, 4, 8};  // preference order
+    float ms_of[6];
     float best = 1e30f;
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 6; ++k) {
         cudaMemcpyAsync(c->dscal.p, &h, sizeof(h), cudaMemcpyHostToDevice, st);
         auto one = [&]() { launch_update(c, cand[k], fz, st, V, V + na, V + 2 * na, V + 5 * na, V + 3 * na, V + 4 * na,
                                          c->dscal.p, INT32_MAX - 1); };
@@ -2121,9 +2214,9 @@ static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
         ms_of[k] = ms;
         best = std::min(best, ms);
     }
-    c->launches += 4 * 21 + 1;
+    c->launches += 6 * 21 + 1;
     int pick = 1;
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 6; ++k)
         if (ms_of[k] <= 1.02f * best) { pick = cand[k]; break; }
     tune_store(c, fz ? "bupdate_fz" : "bupdate", pick);
     return pick;
