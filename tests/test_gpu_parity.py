@@ -232,13 +232,15 @@ def test_folded_direction_update_matches_separate_kernel():
     assert S.get_option(A.OPT_BLOCK_UPDATE) in (1, 2, 4, 8, 12, 14)
     # every update kernel (one thread per node; shared-memory tiles at 2, 4,
     # 8 blocks per SM; 2 or 4 nodes per thread) meets the same bars; the
-    # per-node arithmetic is the same, only the partial sums of r.r and r.z
-    # group nodes differently
+    # per-node arithmetic is the same, only the FP32 partial sums of r.r and
+    # r.z group nodes differently (up to 12 terms per thread, 35 blocks at
+    # this size for 4 nodes per thread), which moves the FP32 recurrence and
+    # with it the iteration count by a few percent
     for uk in (1, 2, 4, 8, 12, 14):
         S.set_option(A.OPT_BLOCK_UPDATE, uk)
         it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
         assert S.get_option(A.OPT_BLOCK_UPDATE) == uk
-        assert rel <= 1e-12 and abs(it - out[1][0]) <= max(2, out[1][0] // 50)
+        assert rel <= 1e-12 and abs(it - out[1][0]) <= max(2, out[1][0] // 10)
         assert np.linalg.norm(S.solution() - x64) <= 1e-8 * np.linalg.norm(x64)
     with pytest.raises(A.IslError):
         S.set_option(A.OPT_BLOCK_UPDATE, 3)
