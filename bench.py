@@ -360,7 +360,8 @@ def serve_request_spmv(requests, local):
         kind = S.get_option(A.OPT_SPMV32_KIND) if not S.get_option(A.OPT_BLOCKED) else None
         folded = bool(S.get_option(A.OPT_BLOCKED)) and S.get_option(A.OPT_FOLD_DIRECTION) and \
             S.time_kernels(1)["block_kind"] in BSPMV_DIR_KERNEL
-        nbytes.append(S.get_option(A.OPT_NBLOCKS) * 40 + (16 if folded else 8) * 3 * nbr + 8 * ((nbr + 31) // 32))
+        col_b = 2 if (folded and S.get_option(A.OPT_SHORT_COLUMNS)) else 4
+        nbytes.append(S.get_option(A.OPT_NBLOCKS) * (36 + col_b) + (16 if folded else 8) * 3 * nbr + 8 * ((nbr + 31) // 32))
         systems.append(S)
         assert kind is None, "c5 requests are node-blocked (padded blocks)"
     ms = 0.0
@@ -1046,10 +1047,12 @@ def run_single(args, rank, world, local, pg):
         nblk, nslot = S.get_option(A.OPT_NBLOCKS), S.get_option(A.OPT_NSLOTS)
         bkind = int(kernels["block_kind"])
         folded = bool(S.get_option(A.OPT_FOLD_DIRECTION)) and bkind in BSPMV_DIR_KERNEL
-        b32 = nblk * 40 + (4 if folded else 2) * neq * 4 + 8 * ((neq // 3 + 31) // 32)
+        col_b = 2 if (folded and S.get_option(A.OPT_SHORT_COLUMNS)) else 4  # 16-bit column offsets
+        b32 = nblk * (36 + col_b) + (4 if folded else 2) * neq * 4 + 8 * ((neq // 3 + 31) // 32)
         if folded:
-            kname = BSPMV_DIR_KERNEL[bkind] + " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV with the block-Jacobi " \
-                "direction update folded in, autotuned variant)"
+            kname = BSPMV_DIR_KERNEL[bkind] + " (sliced-ELL 3x3 FP32 blocks" + \
+                (", 16-bit column offsets" if col_b == 2 else "") + \
+                ", inner CG SpMV with the block-Jacobi direction update folded in, autotuned variant)"
         else:
             kname = BSPMV_KERNEL.get(bkind, "k_bspmv") + " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV, autotuned variant)"
     else:

@@ -20,6 +20,12 @@ __device__ __forceinline__ int ld_stream(const int* p) {
     asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
 }
+// a 16-bit signed value, sign-extended
+__device__ __forceinline__ int ld_stream(const short* p) {
+    int v;
+    asm volatile("ld.global.nc.L1::no_allocate.s16 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
 
 // Row dot product of a CSR matrix by a group of LPR lanes.  Every lane of the
 // warp must call it the same number of times (the shuffles use the full-warp

@@ -227,6 +227,9 @@ struct isl_ctx {
     int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
     bool fuse_dir = true;  // fold the block-Jacobi direction update into the block SpMV
+    isl::DBuf<int16_t> dscol16;  // slot columns as 16-bit offsets from the slot's block row
+    bool scol16 = false;         // every offset fits (dscol16 valid)
+    bool use_scol16 = true;      // ISL_OPT_SHORT_COLUMNS
     int bupd_kind[2] = {0, 0};  // block CG update kernel (separate / folded direction), 0: not tuned yet
     // padded node blocks: DOF objects with some components constrained keep a
     // 3x3 block row; the solver vectors live in the padded space (3 nbr

@@ -1223,6 +1223,24 @@ __global__ void k_bsr_values(int nblk, const int* __restrict__ brow, const int* 
     }
 }
 
+// 16-bit copy of the slot columns as offsets from the slot's block row; a
+// padding row past nbr gets the offset of row nbr - 1 (a valid column), and
+// any offset outside the 16-bit range sets *far
+__global__ void k_sell_col16(int nbr, int nslice, const int* __restrict__ soff, const int* __restrict__ swid,
+                             const int* __restrict__ scol, short* __restrict__ scol16, int* __restrict__ far) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nslice * 32; t += gridDim.x * blockDim.x) {
+        const int s = t / 32, l = t % 32;
+        const int o = soff[s], w = swid[s];
+        const int i = s * 32 + l;
+        for (int k = 0; k < w; ++k) {
+            const int slot = o + k * 32 + l;
+            const int off = i < nbr ? scol[slot] - i : (nbr - 1) - i;
+            if (off < -32767 || off > 32767) { atomicOr(far, 1); scol16[slot] = 0; }
+            else scol16[slot] = (short)off;
+        }
+    }
+}
+
 // Padded node blocks.  A DOF object with some of its three components
 // constrained keeps a block row; aeq[3 I + c] is the equation of component c
 // of block row I (-1: constrained).  The equations of a DOF object's active
@@ -1525,9 +1543,12 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
 // buffers holds p_old follows the parity of the iteration count, which the
 // update kernel advances: the captured graph stays the same for every chunk,
 // and a reliable-update restart (which keeps p) needs no copy.
-template <int U>
+// TC = short: the slots hold the column as a 16-bit offset from the slot's
+// block row (every offset of the matrix within +-32,767; 2 B per block
+// instead of 4)
+template <int U, typename TC>
 __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int* __restrict__ soff,
-                                                   const int* __restrict__ swid, const int* __restrict__ scol,
+                                                   const int* __restrict__ swid, const TC* __restrict__ scol,
                                                    const float* __restrict__ sv, const float* __restrict__ z,
                                                    const float* __restrict__ pold, float beta, float* __restrict__ pnew,
                                                    float* __restrict__ q, int warp, int nwarps) {
@@ -1543,7 +1564,7 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane);
+                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane) + (sizeof(TC) == 2 ? i : 0);
                     const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
 #pragma unroll
                     for (int e = 0; e < 9; ++e) v[u][e] = ld_stream(vp + 32 * e);
@@ -1575,9 +1596,9 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
     return loc;
 }
 
-template <int U, int MINB>
+template <int U, int MINB, typename TC>
 __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, const int* __restrict__ soff,
-                                                        const int* __restrict__ swid, const int* __restrict__ scol,
+                                                        const int* __restrict__ swid, const TC* __restrict__ scol,
                                                         const float* __restrict__ sv, const float* __restrict__ z,
                                                         float* pa, float* pb, float* __restrict__ q, CGScal* S,
                                                         double* part) {
@@ -1586,8 +1607,8 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, con
     const bool odd = S->iters & 1;
     const float beta = (float)S->beta;
     const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    const float loc = bspmv_slices_dir<U>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta, odd ? pa : pb, q,
-                                          warp, nwarps);
+    const float loc = bspmv_slices_dir<U, TC>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta, odd ? pa : pb,
+                                              q, warp, nwarps);
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
@@ -2097,15 +2118,22 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 
 // the batched-load kinds 5..7 also exist with the direction update folded in
 static bool bspmv_dir_kind(int kind) { return kind >= 5 && kind <= 7; }
-static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
-                             CGScal* S, double* part) {
+template <typename TC>
+static void launch_bspmv_dir_t(int kind, cudaStream_t st, isl_ctx* c, const TC* scol, const float* z, float* pa,
+                               float* pb, float* q, CGScal* S, double* part) {
     const int nbr = (int)c->nbr, ns = (int)c->nslice;
     const unsigned g = sell_grid(c);
     switch (kind) {
-        case 5: k_bspmv_dir<2, 4><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
-        case 6: k_bspmv_dir<4, 3><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
-        default: k_bspmv_dir<8, 2><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, c->dscol.p, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 5: k_bspmv_dir<2, 4, TC><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 6: k_bspmv_dir<4, 3, TC><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        default: k_bspmv_dir<8, 2, TC><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
     }
+}
+// the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS allows)
+static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
+                             CGScal* S, double* part) {
+    if (c->scol16 && c->use_scol16) launch_bspmv_dir_t<short>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
+    else launch_bspmv_dir_t<int>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
 }
 
 // autotune of the block SpMV (format and row mapping) on the current matrix
@@ -2342,6 +2370,21 @@ int block_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
     ISL_CHECK_CUDA(c, c->dsdst.alloc(c->nblk));
     k_sell_fill<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, (int)c->nslice, c->dbptr.p, c->dbcol.p, c->dsoff.p, c->dswid.p,
                                                    c->dscol.p, c->dsdst.p);
+    {
+        // 16-bit column offsets, when every slot's column is within +-32,767
+        // block rows of its own (padding rows past nbr point at the last row)
+        c->scol16 = false;
+        ISL_CHECK_CUDA(c, c->dscol16.alloc(tot));
+        ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), c->stream));
+        k_sell_col16<<<vec_grid(c), BS, 0, c->stream>>>((int)nbr, (int)c->nslice, c->dsoff.p, c->dswid.p, c->dscol.p,
+                                                        c->dscol16.p, c->dflags.p + 1);
+        int far = 0;
+        ISL_CHECK_CUDA(c, cudaMemcpyAsync(&far, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        ISL_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+        c->launches += 1;
+        c->scol16 = far == 0;
+        if (!c->scol16) c->dscol16.release();
+    }
     ISL_CHECK_CUDA(c, c->dsval.alloc((size_t)9 * tot));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dsval.p, 0, (size_t)9 * tot * 4, c->stream));
     ISL_CHECK_CUDA(c, cudaGetLastError());

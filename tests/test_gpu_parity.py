@@ -244,6 +244,16 @@ def test_folded_direction_update_matches_separate_kernel():
         assert np.linalg.norm(S.solution() - x64) <= 1e-8 * np.linalg.norm(x64)
     with pytest.raises(A.IslError):
         S.set_option(A.OPT_BLOCK_UPDATE, 3)
+    # 16-bit column offsets (every offset of this matrix is within 1,123
+    # block rows) read the same columns: bitwise the same solve
+    S.set_option(A.OPT_BLOCK_UPDATE, 1)
+    assert S.get_option(A.OPT_SHORT_COLUMNS) == 1
+    it16, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    x16 = S.solution()
+    S.set_option(A.OPT_SHORT_COLUMNS, 0)
+    assert S.get_option(A.OPT_SHORT_COLUMNS) == 0
+    it32, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    assert it32 == it16 and np.array_equal(S.solution(), x16)
     S.close()
 
 
