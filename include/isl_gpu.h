@@ -353,7 +353,10 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
        ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
        ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14, ISL_OPT_BLOCK_UPDATE = 15,
-       ISL_OPT_SHORT_COLUMNS = 16 };
+       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_MATRIX_EVICT_FIRST = 17 };
+/* ISL_OPT_MATRIX_EVICT_FIRST (default 0): the block SpMV with the folded
+ * direction update loads the matrix values and columns with an evict-first
+ * L2 policy, so that the vectors the update kernel reads next stay in L2. */
 /* ISL_OPT_SHORT_COLUMNS (default 1): the block SpMV with the folded direction
  * update reads each slot's column as a 16-bit offset from its block row (2 B
  * per stored block instead of 4) when every offset of the matrix fits; 0
@@ -361,10 +364,9 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
  * (the option on and the offsets fitting). */
 /* ISL_OPT_BLOCK_UPDATE: the update kernel of the graph path of the block CG
  * (x, r, z = B^-1 r, r.r, r.z): 1 one thread per node, 2, 4 or 8 tiles of 256
- * nodes staged through shared memory with that many blocks per SM, 12 or 14
- * two or four nodes per thread with their loads issued together; 0 (default)
- * autotuned at the first such solve.  Read back: the kernel in use (0 before
- * the first solve). */
+ * nodes staged through shared memory with that many blocks per SM; 0
+ * (default) autotuned at the first such solve.  Read back: the kernel in use
+ * (0 before the first solve). */
 /* ISL_OPT_FOLD_DIRECTION (default 1): the graph path of the node-blocked
  * mixed solve forms the search direction p = B^-1 r + beta p inside the block
  * SpMV (the update kernel stores z = B^-1 r; each column block of p is formed

@@ -1545,14 +1545,15 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
 // and a reliable-update restart (which keeps p) needs no copy.
 // TC = short: the slots hold the column as a 16-bit offset from the slot's
 // block row (every offset of the matrix within +-32,767; 2 B per block
-// instead of 4)
-template <int U, typename TC>
+// instead of 4).  EF: the values and columns are loaded evict-first in L2.
+template <int U, typename TC, bool EF>
 __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int* __restrict__ soff,
                                                    const int* __restrict__ swid, const TC* __restrict__ scol,
                                                    const float* __restrict__ sv, const float* __restrict__ z,
                                                    const float* __restrict__ pold, float beta, float* __restrict__ pnew,
                                                    float* __restrict__ q, int warp, int nwarps) {
     const int lane = threadIdx.x & 31;
+    const unsigned long long pol = EF ? l2_evict_first_policy() : 0ull;
     float loc = 0.f;
     for (int s = warp; s < nslice; s += nwarps) {
         const int i = s * 32 + lane;
@@ -1564,10 +1565,11 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane) + (sizeof(TC) == 2 ? i : 0);
+                    const TC* cp = scol + o + (k + u) * 32 + lane;
+                    j[u] = (EF ? ld_stream_ef(cp, pol) : ld_stream(cp)) + (sizeof(TC) == 2 ? i : 0);
                     const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) v[u][e] = ld_stream(vp + 32 * e);
+                    for (int e = 0; e < 9; ++e) v[u][e] = EF ? ld_stream_ef(vp + 32 * e, pol) : ld_stream(vp + 32 * e);
                 }
             }
 #pragma unroll
@@ -1596,7 +1598,7 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
     return loc;
 }
 
-template <int U, int MINB, typename TC>
+template <int U, int MINB, typename TC, bool EF>
 __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, const int* __restrict__ soff,
                                                         const int* __restrict__ swid, const TC* __restrict__ scol,
                                                         const float* __restrict__ sv, const float* __restrict__ z,
@@ -1607,8 +1609,8 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, con
     const bool odd = S->iters & 1;
     const float beta = (float)S->beta;
     const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    const float loc = bspmv_slices_dir<U, TC>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta, odd ? pa : pb,
-                                              q, warp, nwarps);
+    const float loc = bspmv_slices_dir<U, TC, EF>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta,
+                                                  odd ? pa : pb, q, warp, nwarps);
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
@@ -1720,83 +1722,6 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
             if (FZ) zout[d + a] = z;
             rr += rv[a] * rv[a];
             rz += rv[a] * z;
-        }
-    }
-    const double b1 = block_sum_f(rr, sh);
-    const double b2 = block_sum_f(rz, sh);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
-    if (!last_block(&S->ticket2)) return;
-    double trr, trz;
-    reduce_parts2_blk<NODE_BS>(part, gridDim.x, sh, trr, trz);
-    if (threadIdx.x == 0) {
-        S->rr = trr;
-        S->iters += 1;
-        S->absOld = S->absNew;
-        S->beta = trz / S->absNew;
-        S->absNew = trz;
-        if (!(trr == trr) || !(trz == trz)) { S->bad = 1; S->done = 1; }
-        else if (trr < S->threshold) S->done = 1;
-        else if (trr < S->rrtrig) S->done = 3;
-        else if (S->iters >= max_iter) S->done = 2;
-        S->ticket2 = 0;
-    }
-}
-
-// The same update with UN nodes per thread whose loads (9 inverse-block and
-// 12 vector entries each) are all issued before any of them is used: one
-// memory round trip per UN nodes instead of one per node.  Nodes of one pass
-// are UN runs of NODE_BS consecutive nodes, so each warp load spans the same
-// 32 nodes as in the one-node kernel.  Per-node arithmetic is that of
-// k_cg_update_b3n; r.r and r.z are accumulated in pass order.
-template <bool FZ, int UN>
-__global__ void __launch_bounds__(NODE_BS) k_cg_update_b3m(int nbr, float* __restrict__ x, float* __restrict__ r,
-                                                           const float* __restrict__ p1, const float* __restrict__ p2,
-                                                           const float* __restrict__ q, const float* __restrict__ binv,
-                                                           float* __restrict__ zout, CGScal* S, double* part,
-                                                           int max_iter) {
-    if (S->done) return;
-    __shared__ double sh[32];
-    const float* __restrict__ p = (FZ && !(S->iters & 1)) ? p2 : p1;
-    const float alpha = (float)S->alpha;
-    float rr = 0.f, rz = 0.f;
-    for (int base = blockIdx.x * NODE_BS * UN; base < nbr; base += gridDim.x * NODE_BS * UN) {
-        float b[UN][9], xv[UN][3], rv[UN][3], pv[UN][3], qv[UN][3];
-#pragma unroll
-        for (int u = 0; u < UN; ++u) {
-            const int i = base + u * NODE_BS + (int)threadIdx.x;
-            if (i < nbr) {
-                const size_t d = 3 * (size_t)i;
-#pragma unroll
-                for (int k = 0; k < 9; ++k) b[u][k] = ld(binv + 9 * (size_t)i + k);
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    xv[u][a] = x[d + a];
-                    rv[u][a] = r[d + a];
-                    pv[u][a] = ld(p + d + a);
-                    qv[u][a] = ld(q + d + a);
-                }
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < UN; ++u) {
-            const int i = base + u * NODE_BS + (int)threadIdx.x;
-            if (i < nbr) {
-                const size_t d = 3 * (size_t)i;
-                float rn[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    x[d + a] = xv[u][a] + alpha * pv[u][a];
-                    rn[a] = rv[u][a] - alpha * qv[u][a];
-                }
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    r[d + a] = rn[a];
-                    const float z = b[u][3 * a] * rn[0] + b[u][3 * a + 1] * rn[1] + b[u][3 * a + 2] * rn[2];
-                    if (FZ) zout[d + a] = z;
-                    rr += rn[a] * rn[a];
-                    rz += rn[a] * z;
-                }
-            }
         }
     }
     const double b1 = block_sum_f(rr, sh);
@@ -2118,22 +2043,29 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 
 // the batched-load kinds 5..7 also exist with the direction update folded in
 static bool bspmv_dir_kind(int kind) { return kind >= 5 && kind <= 7; }
-template <typename TC>
+template <typename TC, bool EF>
 static void launch_bspmv_dir_t(int kind, cudaStream_t st, isl_ctx* c, const TC* scol, const float* z, float* pa,
                                float* pb, float* q, CGScal* S, double* part) {
     const int nbr = (int)c->nbr, ns = (int)c->nslice;
     const unsigned g = sell_grid(c);
     switch (kind) {
-        case 5: k_bspmv_dir<2, 4, TC><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
-        case 6: k_bspmv_dir<4, 3, TC><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
-        default: k_bspmv_dir<8, 2, TC><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 5: k_bspmv_dir<2, 4, TC, EF><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 6: k_bspmv_dir<4, 3, TC, EF><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        default: k_bspmv_dir<8, 2, TC, EF><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
     }
 }
-// the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS allows)
+// the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS
+// allows); the evict-first matrix stream where ISL_OPT_MATRIX_EVICT_FIRST asks
 static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
                              CGScal* S, double* part) {
-    if (c->scol16 && c->use_scol16) launch_bspmv_dir_t<short>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
-    else launch_bspmv_dir_t<int>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
+    const bool s16 = c->scol16 && c->use_scol16;
+    if (c->mat_ef) {
+        if (s16) launch_bspmv_dir_t<short, true>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
+        else launch_bspmv_dir_t<int, true>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
+    } else {
+        if (s16) launch_bspmv_dir_t<short, false>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
+        else launch_bspmv_dir_t<int, false>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
+    }
 }
 
 // autotune of the block SpMV (format and row mapping) on the current matrix
@@ -2170,7 +2102,7 @@ static int autotune_lpb(isl_ctx* c, const float* p, float* q, CGScal* S, double*
     return best;
 }
 
-bool update_kind_valid(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 12 || k == 14; }
+bool update_kind_valid(int k) { return k == 1 || k == 2 || k == 4 || k == 8; }
 
 // constant fill (timing inputs)
 __global__ void k_fill(int64_t n, float* __restrict__ a, float v) {
@@ -2182,25 +2114,10 @@ __global__ void k_fill64(int64_t n, double* __restrict__ a, double v) {
 
 // update kernel of the block CG: 1 one thread per node (k_cg_update_b3n, two
 // blocks per SM); 2, 4, 8: tiles of UT nodes staged through shared memory
-// (k_cg_update_b3t) with that many blocks per SM; 12, 14: 2 or 4 nodes per
-// thread with all their loads issued first (k_cg_update_b3m), at most two
-// blocks per SM
+// (k_cg_update_b3t) with that many blocks per SM
 static void launch_update(isl_ctx* c, int kind, bool fz, cudaStream_t st, float* x, float* r, const float* p1,
                           const float* p2, const float* q, float* z, CGScal* S, int mi) {
     const int nbr = (int)c->nbr;
-    if (kind == 12 || kind == 14) {
-        const int un = kind == 12 ? 2 : 4;
-        const long long per = (long long)NODE_BS * un;
-        const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((nbr + per - 1) / per, 2LL * c->sm_count));
-        if (kind == 12) {
-            if (fz) k_cg_update_b3m<true, 2><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
-            else k_cg_update_b3m<false, 2><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
-        } else {
-            if (fz) k_cg_update_b3m<true, 4><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
-            else k_cg_update_b3m<false, 4><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
-        }
-        return;
-    }
     if (kind <= 1) {
         const unsigned g = node_grid(c, nbr);
         if (fz) k_cg_update_b3n<true><<<g, NODE_BS, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
@@ -2225,10 +2142,10 @@ static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
     CGScal h;
     memset(&h, 0, sizeof(h));
     h.absNew = 1.0; h.absOld = 1.0; h.alpha = 1e-6; h.beta = 0.5; h.threshold = -1.0; h.rrtrig = -1.0;
-    const int cand[6] = {1, 14, 12, 2, 4, 8};  // preference order
-    float ms_of[6];
+    const int cand[4] = {1, 2, 4, 8};  // preference order
+    float ms_of[4];
     float best = 1e30f;
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 4; ++k) {
         cudaMemcpyAsync(c->dscal.p, &h, sizeof(h), cudaMemcpyHostToDevice, st);
         auto one = [&]() { launch_update(c, cand[k], fz, st, V, V + na, V + 2 * na, V + 5 * na, V + 3 * na, V + 4 * na,
                                          c->dscal.p, INT32_MAX - 1); };
@@ -2242,9 +2159,9 @@ static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
         ms_of[k] = ms;
         best = std::min(best, ms);
     }
-    c->launches += 6 * 21 + 1;
+    c->launches += 4 * 21 + 1;
     int pick = 1;
-    for (int k = 0; k < 6; ++k)
+    for (int k = 0; k < 4; ++k)
         if (ms_of[k] <= 1.02f * best) { pick = cand[k]; break; }
     tune_store(c, fz ? "bupdate_fz" : "bupdate", pick);
     return pick;
