@@ -353,10 +353,7 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
        ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
        ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14, ISL_OPT_BLOCK_UPDATE = 15,
-       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_MATRIX_EVICT_FIRST = 17 };
-/* ISL_OPT_MATRIX_EVICT_FIRST (default 0): the block SpMV with the folded
- * direction update loads the matrix values and columns with an evict-first
- * L2 policy, so that the vectors the update kernel reads next stay in L2. */
+       ISL_OPT_SHORT_COLUMNS = 16 };
 /* ISL_OPT_SHORT_COLUMNS (default 1): the block SpMV with the folded direction
  * update reads each slot's column as a 16-bit offset from its block row (2 B
  * per stored block instead of 4) when every offset of the matrix fits; 0

@@ -20,30 +20,6 @@ __device__ __forceinline__ int ld_stream(const int* p) {
     asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
 }
-// The same loads marked evict-first in L2 (an access policy made once per
-// thread by createpolicy): a matrix streamed once per iteration then yields
-// L2 to the vectors the next kernel reads
-__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
-    unsigned long long p;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-__device__ __forceinline__ float ld_stream_ef(const float* p, unsigned long long pol) {
-    float v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ int ld_stream_ef(const int* p, unsigned long long pol) {
-    int v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ int ld_stream_ef(const short* p, unsigned long long pol) {
-    int v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.s16 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-    return v;
-}
-
 // a 16-bit signed value, sign-extended
 __device__ __forceinline__ int ld_stream(const short* p) {
     int v;

@@ -1545,15 +1545,14 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_batch(int nbr, int nslice, c
 // and a reliable-update restart (which keeps p) needs no copy.
 // TC = short: the slots hold the column as a 16-bit offset from the slot's
 // block row (every offset of the matrix within +-32,767; 2 B per block
-// instead of 4).  EF: the values and columns are loaded evict-first in L2.
-template <int U, typename TC, bool EF>
+// instead of 4)
+template <int U, typename TC>
 __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int* __restrict__ soff,
                                                    const int* __restrict__ swid, const TC* __restrict__ scol,
                                                    const float* __restrict__ sv, const float* __restrict__ z,
                                                    const float* __restrict__ pold, float beta, float* __restrict__ pnew,
                                                    float* __restrict__ q, int warp, int nwarps) {
     const int lane = threadIdx.x & 31;
-    const unsigned long long pol = EF ? l2_evict_first_policy() : 0ull;
     float loc = 0.f;
     for (int s = warp; s < nslice; s += nwarps) {
         const int i = s * 32 + lane;
@@ -1565,11 +1564,10 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    const TC* cp = scol + o + (k + u) * 32 + lane;
-                    j[u] = (EF ? ld_stream_ef(cp, pol) : ld_stream(cp)) + (sizeof(TC) == 2 ? i : 0);
+                    j[u] = ld_stream(scol + o + (k + u) * 32 + lane) + (sizeof(TC) == 2 ? i : 0);
                     const float* vp = sv + (size_t)((o >> 5) + k + u) * 288 + lane;
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) v[u][e] = EF ? ld_stream_ef(vp + 32 * e, pol) : ld_stream(vp + 32 * e);
+                    for (int e = 0; e < 9; ++e) v[u][e] = ld_stream(vp + 32 * e);
                 }
             }
 #pragma unroll
@@ -1598,7 +1596,7 @@ __device__ __forceinline__ float bspmv_slices_dir(int nbr, int nslice, const int
     return loc;
 }
 
-template <int U, int MINB, typename TC, bool EF>
+template <int U, int MINB, typename TC>
 __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, const int* __restrict__ soff,
                                                         const int* __restrict__ swid, const TC* __restrict__ scol,
                                                         const float* __restrict__ sv, const float* __restrict__ z,
@@ -1609,8 +1607,8 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, con
     const bool odd = S->iters & 1;
     const float beta = (float)S->beta;
     const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    const float loc = bspmv_slices_dir<U, TC, EF>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta,
-                                                  odd ? pa : pb, q, warp, nwarps);
+    const float loc = bspmv_slices_dir<U, TC>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, beta, odd ? pa : pb,
+                                              q, warp, nwarps);
     const double bsum = block_sum_f(loc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = bsum;
     if (last_block(&S->ticket1)) {
@@ -2043,29 +2041,22 @@ static void launch_bspmv(int kind, unsigned grid, cudaStream_t st, isl_ctx* c, c
 
 // the batched-load kinds 5..7 also exist with the direction update folded in
 static bool bspmv_dir_kind(int kind) { return kind >= 5 && kind <= 7; }
-template <typename TC, bool EF>
+template <typename TC>
 static void launch_bspmv_dir_t(int kind, cudaStream_t st, isl_ctx* c, const TC* scol, const float* z, float* pa,
                                float* pb, float* q, CGScal* S, double* part) {
     const int nbr = (int)c->nbr, ns = (int)c->nslice;
     const unsigned g = sell_grid(c);
     switch (kind) {
-        case 5: k_bspmv_dir<2, 4, TC, EF><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
-        case 6: k_bspmv_dir<4, 3, TC, EF><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
-        default: k_bspmv_dir<8, 2, TC, EF><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 5: k_bspmv_dir<2, 4, TC><<<std::min(g, 4u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        case 6: k_bspmv_dir<4, 3, TC><<<std::min(g, 3u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
+        default: k_bspmv_dir<8, 2, TC><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
     }
 }
-// the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS
-// allows); the evict-first matrix stream where ISL_OPT_MATRIX_EVICT_FIRST asks
+// the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS allows)
 static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
                              CGScal* S, double* part) {
-    const bool s16 = c->scol16 && c->use_scol16;
-    if (c->mat_ef) {
-        if (s16) launch_bspmv_dir_t<short, true>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
-        else launch_bspmv_dir_t<int, true>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
-    } else {
-        if (s16) launch_bspmv_dir_t<short, false>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
-        else launch_bspmv_dir_t<int, false>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
-    }
+    if (c->scol16 && c->use_scol16) launch_bspmv_dir_t<short>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, part);
+    else launch_bspmv_dir_t<int>(kind, st, c, c->dscol.p, z, pa, pb, q, S, part);
 }
 
 // autotune of the block SpMV (format and row mapping) on the current matrix

@@ -253,11 +253,6 @@ def test_folded_direction_update_matches_separate_kernel():
     assert S.get_option(A.OPT_SHORT_COLUMNS) == 0
     it32, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
     assert it32 == it16 and np.array_equal(S.solution(), x16)
-    # the evict-first L2 policy on the matrix stream changes no value
-    S.set_option(A.OPT_SHORT_COLUMNS, 1)
-    S.set_option(A.OPT_MATRIX_EVICT_FIRST, 1 - S.get_option(A.OPT_MATRIX_EVICT_FIRST))
-    ite, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
-    assert ite == it16 and np.array_equal(S.solution(), x16)
     S.close()
 
 
