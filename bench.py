@@ -673,6 +673,7 @@ def run_batch(args, rank, world, local, pg):
         coefs.append((np.concatenate(kappa), 2 * deg))
         S.set_laplace(*coefs[-1])
         S.set_body_force_nodal(np.concatenate(body))
+        S.set_option(A.OPT_RELIABLE_DROP, args.reliable_drop)
         del meshes, kappa, body
         systems.append(S)
         log(f"c4 group Q{deg}: {len(members)} instances, {S.nelem} elements, {S.neq} DOFs, {S.nnz} nnz")
@@ -779,7 +780,8 @@ def run_batch(args, rank, world, local, pg):
                        "active_dofs": int(neq), "nnz": int(nnz), "contexts": len(systems),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (FP32 CSR %.1f GB)" % (nnz * 8 / 1e9)},
-            "method": "mixed FP32 CG + FP64 reliable updates per instance; contexts concurrent (one stream each)",
+            "method": "mixed FP32 CG + FP64 reliable updates per instance (when the FP32 r.r has dropped "
+                      f"1e{args.reliable_drop}x since the last one); contexts concurrent (one stream each)",
             "assembly_ms": asm_ms, "assembly_gdofs": neq / (asm_ms * 1e-3) / 1e9, "setup_s": t_setup,
             "plain_fp64": {"ms_per_step": s_plain * 1e3, "dofs_per_s": neq / s_plain},
             "speedup_vs_plain_fp64": s_plain / s_mixed,
@@ -844,6 +846,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="c5: requests per run")
     ap.add_argument("--slots", type=int, default=8, help="c5: batches the mixed server runs at once")
     ap.add_argument("--batch", type=int, default=1, help="c5: requests per batch of the mixed server")
+    ap.add_argument("--reliable-drop", type=int, default=2,
+                    help="c4: reliable update after the FP32 r.r drops by 10^value (ISL_OPT_RELIABLE_DROP)")
     ap.add_argument("--persist", type=int, default=0,
                     help="c5: 1 lets single-request batches solve small systems in one launch (ISL_OPT_PERSISTENT)")
     ap.add_argument("--batch-window-us", type=int, default=20000, help="c5: batching window of the mixed server")

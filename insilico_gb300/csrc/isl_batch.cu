@@ -60,6 +60,7 @@ struct BArgs {
     int* wl_cum;          // [ninst+1] row blocks of the listed instances before each entry
     int max_iter;
     double tol;
+    double trig2;         // reliable update when r.r has dropped by this factor since the last one
     const int* blk_s0;    // batched sliced-ELL copy: slices of every row block
     const int* blk_s1;
 };
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
             else if (!mixed) {
                 if (trr < SS(a, S_THRESH, k)) finish(a, k, 1);
                 else if (it >= a.max_iter) finish(a, k, 2);
-            } else if (trr < SS(a, S_THRESH, k) || trr < 1e-2 * SS(a, S_RRLAST, k) || it >= a.max_iter) {
+            } else if (trr < SS(a, S_THRESH, k) || trr < a.trig2 * SS(a, S_RRLAST, k) || it >= a.max_iter) {
                 II(a, I_UPDATE, k) = 1;
                 a.wl[atomicAdd(a.wl_n, 1)] = k;  // list order varies; each instance's sums do not
             }
@@ -603,6 +604,7 @@ BArgs batch_args(isl_ctx* c, int64_t max_iter, double tol) {
     a.wl_cur = c->dbwl.p + ni + 1;
     a.wl_cum = c->dbwl.p + ni + 2;
     a.max_iter = (int)std::min<int64_t>(max_iter, INT32_MAX - 1);
+    a.trig2 = c->ru_drop2;
     a.tol = tol;
     a.blk_s0 = nullptr;
     a.blk_s1 = nullptr;

@@ -1425,6 +1425,11 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (key == ISL_OPT_BATCHED_SOLVE) { c->force_batched = value != 0; return ISL_OK; }
     if (key == ISL_OPT_FOLD_DIRECTION) { c->fuse_dir = value != 0; return ISL_OK; }
     if (key == ISL_OPT_SHORT_COLUMNS) { c->use_scol16 = value != 0; return ISL_OK; }
+    if (key == ISL_OPT_RELIABLE_DROP) {
+        if (value < 1 || value > 8) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_RELIABLE_DROP takes 1..8");
+        c->ru_drop2 = std::pow(10.0, -(double)value);
+        return ISL_OK;
+    }
     if (key == ISL_OPT_BLOCK_UPDATE) {
         if (value != 0 && !isl::update_kind_valid((int)value))
             ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_BLOCK_UPDATE takes 0, 1, 2, 4 or 8");
@@ -1467,6 +1472,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_BATCHED_SOLVE) { *value = c->force_batched; return ISL_OK; }
     if (key == ISL_OPT_FOLD_DIRECTION) { *value = c->fuse_dir; return ISL_OK; }
     if (key == ISL_OPT_SHORT_COLUMNS) { *value = (c->blocked && c->scol16 && c->use_scol16) ? 1 : 0; return ISL_OK; }
+    if (key == ISL_OPT_RELIABLE_DROP) { *value = (int64_t)std::lround(-std::log10(c->ru_drop2)); return ISL_OK; }
     if (key == ISL_OPT_BLOCK_UPDATE) { *value = c->bupd_kind[c->fuse_dir ? 1 : 0]; return ISL_OK; }
     if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }
     if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }

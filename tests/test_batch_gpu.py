@@ -98,3 +98,35 @@ def test_batch_sliced_ell_and_csr_agree(deg):
         for kind in (4, 104):
             assert np.linalg.norm(out[kind][r0:r1] - xo) <= 1e-7 * np.linalg.norm(xo)
     S.close()
+
+
+@pytest.mark.parametrize("drop", [2, 4])
+def test_batch_reliable_update_spacing(drop):
+    """ISL_OPT_RELIABLE_DROP spaces the FP64 reliable updates (an update when
+    the FP32 r.r has dropped by 10^drop): every instance still reaches the
+    tolerance on its true residual and the oracle's solution within 1e-8."""
+    probs = [instance(s, 2, 500 + s) for s in (30, 4, 45, 12)]
+    S = System()
+    S.upload_batch(A.QUAD, [(p.X, p.conn) for p in probs])
+    S.create_field(2, 1)
+    S.constrain_boundary(lambda x: (np.ones((len(x), 1), dtype=bool), 0.0))
+    S.number_dofs()
+    S.register_pattern()
+    S.set_laplace(np.concatenate([p.kappa for p in probs]), 4)
+    S.set_body_force_nodal(np.concatenate([p.body for p in probs]))
+    S.set_option(A.OPT_RELIABLE_DROP, drop)
+    assert S.get_option(A.OPT_RELIABLE_DROP) == drop
+    eq_off, _ = S.batch_info()
+    S.assemble(A.PREC_MIXED)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-10)
+    xm = S.solution()
+    _, rel = S.batch_stats()
+    assert np.all(np.asarray(rel) <= 1e-10)
+    for k, p in enumerate(probs):
+        P, (orp, oci, ov, ob) = oracle_problem(p)
+        r0, r1 = eq_off[k], eq_off[k + 1]
+        xo, _, _ = O.cg(orp, oci, ov, ob, tol=1e-13)
+        assert np.linalg.norm(xm[r0:r1] - xo) <= 1e-8 * np.linalg.norm(xo)
+    with pytest.raises(A.IslError):
+        S.set_option(A.OPT_RELIABLE_DROP, 0)
+    S.close()
