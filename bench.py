@@ -1040,7 +1040,7 @@ def run_single(args, rank, world, local, pg):
     spmv32_ms = S.time_spmv(A.PREC_FP32, 50)
     spmv64_ms = S.time_spmv(A.PREC_FP64, 50)
     kernels = S.time_kernels(30)
-    kernels["update_kind"] = S.get_option(A.OPT_BLOCK_UPDATE) if S.get_option(A.OPT_BLOCKED) else 0
+    kernels["update_kind"] = (S.get_option(A.OPT_BLOCK_UPDATE) or 1) if S.get_option(A.OPT_BLOCKED) else 0
     log("kernel ms:", {k: round(v, 4) for k, v in kernels.items()})
     hbm, src = peaks()
     blocked = S.get_option(A.OPT_BLOCKED)

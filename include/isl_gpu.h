@@ -363,10 +363,9 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
  * keeps the 32-bit columns.  Read back: 1 when the 16-bit columns are in use
  * (the option on and the offsets fitting). */
 /* ISL_OPT_BLOCK_UPDATE: the update kernel of the graph path of the block CG
- * (x, r, z = B^-1 r, r.r, r.z): 1 one thread per node, 2, 4 or 8 tiles of 256
- * nodes staged through shared memory with that many blocks per SM; 0
- * (default) autotuned at the first such solve.  Read back: the kernel in use
- * (0 before the first solve). */
+ * (x, r, z = B^-1 r, r.r, r.z): 1 one thread per node (what 0, the default,
+ * selects), 2, 4 or 8 tiles of 256 nodes staged through shared memory with
+ * that many blocks per SM.  Read back: the value set (0: the default). */
 /* ISL_OPT_FOLD_DIRECTION (default 1): the graph path of the node-blocked
  * mixed solve forms the search direction p = B^-1 r + beta p inside the block
  * SpMV (the update kernel stores z = B^-1 r; each column block of p is formed

@@ -2121,43 +2121,6 @@ static void launch_update(isl_ctx* c, int kind, bool fz, cudaStream_t st, float*
     else k_cg_update_b3t<false><<<g, UT, 0, st>>>(nbr, x, r, p1, p2, q, c->dbinv.p, z, S, c->dpart.p, mi);
 }
 
-// choose the update kernel by timing each on the current system (vectors
-// filled with ones, a scalar record that never converges); the CG starts
-// from its own initialisation afterwards
-static int autotune_update(isl_ctx* c, float* V, size_t na, bool fz) {
-    if (c->nbr < 8000) return 1;
-    int cached = 0;
-    if (tune_lookup(c, fz ? "bupdate_fz" : "bupdate", &cached) && update_kind_valid(cached)) return cached;
-    cudaStream_t st = c->stream;
-    k_fill<<<vec_grid(c), BS, 0, st>>>((int64_t)(6 * na), V, 1.0f);
-    CGScal h;
-    memset(&h, 0, sizeof(h));
-    h.absNew = 1.0; h.absOld = 1.0; h.alpha = 1e-6; h.beta = 0.5; h.threshold = -1.0; h.rrtrig = -1.0;
-    const int cand[4] = {1, 2, 4, 8};  // preference order
-    float ms_of[4];
-    float best = 1e30f;
-    for (int k = 0; k < 4; ++k) {
-        cudaMemcpyAsync(c->dscal.p, &h, sizeof(h), cudaMemcpyHostToDevice, st);
-        auto one = [&]() { launch_update(c, cand[k], fz, st, V, V + na, V + 2 * na, V + 5 * na, V + 3 * na, V + 4 * na,
-                                         c->dscal.p, INT32_MAX - 1); };
-        one();
-        cudaEventRecord(c->ev[2], st);
-        for (int r = 0; r < 20; ++r) one();
-        cudaEventRecord(c->ev[3], st);
-        cudaEventSynchronize(c->ev[3]);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
-        ms_of[k] = ms;
-        best = std::min(best, ms);
-    }
-    c->launches += 4 * 21 + 1;
-    int pick = 1;
-    for (int k = 0; k < 4; ++k)
-        if (ms_of[k] <= 1.02f * best) { pick = cand[k]; break; }
-    tune_store(c, fz ? "bupdate_fz" : "bupdate", pick);
-    return pick;
-}
-
 // detect the node-blocked structure and build the block pattern (setup)
 // padded node blocks (some DOF objects partly constrained): the equation map
 // of the block rows from the host numbering, then the block pattern on the
@@ -2506,9 +2469,11 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     // take the two spare FP32 vectors of the work area
     const bool fused = pgrid == 0 && c->fuse_dir && bspmv_dir_kind(c->bspmv_lpb);
     float *z32 = fused ? V + 4 * na : nullptr, *p32b = V + 5 * na;
-    int& ukind = c->bupd_kind[fused ? 1 : 0];
-    if (pgrid == 0 && ukind == 0) ukind = autotune_update(c, V, na, fused);  // before the CG state is set up
-    ISL_CHECK_CUDA(c, cudaGetLastError());
+    // update kernel: one thread per node unless ISL_OPT_BLOCK_UPDATE picks a
+    // tiled one (timed alone, with its vectors in L2, the tiled kernels can
+    // look faster; inside the solve, after the SpMV has streamed the matrix
+    // through L2, they are slower at 64^3)
+    const int ukind = c->bupd_kind[fused ? 1 : 0] ? c->bupd_kind[fused ? 1 : 0] : 1;
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0,
