@@ -411,6 +411,7 @@ def run_serve(args, rank, world, local, pg):
     }
     for kw in arms.values():
         kw["persistent"] = args.persist
+        kw["order"] = args.order
     if args.c5_mixed_only:  # configuration sweeps of the mixed server (no line is printed)
         arms = {"mixed": arms["mixed"]}
     out = {}
@@ -846,6 +847,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="c5: requests per run")
     ap.add_argument("--slots", type=int, default=8, help="c5: batches the mixed server runs at once")
     ap.add_argument("--batch", type=int, default=1, help="c5: requests per batch of the mixed server")
+    ap.add_argument("--order", type=int, default=0,
+                    help="c5: 1 starts batches from the largest queued request (isl_serve_config.order)")
     ap.add_argument("--reliable-drop", type=int, default=2,
                     help="c4: reliable update after the FP32 r.r drops by 10^value (ISL_OPT_RELIABLE_DROP)")
     ap.add_argument("--persist", type=int, default=0,

@@ -488,6 +488,9 @@ typedef struct {
                                  of separate kernels, which overlap with the other batches' launches; 1 the
                                  library default (small systems solved in one launch: a cooperative grid over
                                  every SM, or one thread-block cluster) */
+    int order;                /* 0 (default): batches start from the oldest queued request; 1: from the
+                                 largest (elements; the oldest among equals), which shortens the time to
+                                 finish a queue of requests submitted together */
 } isl_serve_config;
 typedef struct {
     int shape;                /* ISL_QUAD, ISL_TET, ISL_HEX */

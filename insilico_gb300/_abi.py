@@ -59,7 +59,7 @@ class ServeConfig(C.Structure):
     _fields_ = [("max_batch", C.c_int), ("max_batches", C.c_int), ("precision", C.c_int),
                 ("reserve_bytes", C.c_int64), ("max_pairs", C.c_int64), ("test_budget_bytes", C.c_int64),
                 ("test_fake_us_per_elem", C.c_double), ("batch_window_us", C.c_int64), ("size_ratio", C.c_double),
-                ("persistent", C.c_int)]
+                ("persistent", C.c_int), ("order", C.c_int)]
 
 
 class ServeRequest(C.Structure):

@@ -7,7 +7,8 @@
 // increment to the DOFs, stop when ||dU||/N < tol.
 //
 // Here a server admits many such requests and runs them on one GPU:
-//   * a scheduler thread forms batches from the queue in arrival order:
+//   * a scheduler thread forms batches from the queue in arrival order (or,
+//     with order = 1, starting from the largest queued request):
 //     requests with the same element shape, components, kernel, material and
 //     quadrature (and, with size_ratio > 1, element counts within that factor
 //     of the batch's first request), up to max_batch, within the 32-bit
@@ -427,6 +428,18 @@ void scheduler_main(isl_server* s) {
             if (waited < window) {
                 s->cv.wait_for(lk, std::chrono::duration<double>(window - waited));
                 continue;
+            }
+        }
+        if (s->cfg.order == 1 && s->queue.size() > 1) {
+            // largest first: the first of the largest requests leads the batch
+            auto big = std::max_element(s->queue.begin(), s->queue.end(),
+                                        [](const std::shared_ptr<Req>& a, const std::shared_ptr<Req>& b) {
+                                            return a->n_elem < b->n_elem;
+                                        });
+            if (big != s->queue.begin()) {
+                auto r = *big;
+                s->queue.erase(big);
+                s->queue.push_front(r);
             }
         }
         auto b = std::make_shared<Batch>();

@@ -109,12 +109,12 @@ class Server:
     def __init__(self, device: int = 0, precision: int = A.PREC_FP32, max_batch: int = 64, max_batches: int = 4,
                  reserve_bytes: int = 8 << 30, lin_tol: Optional[float] = None, test_budget_bytes: int = 0,
                  test_fake_us_per_elem: float = 0.0, batch_window_us: int = 0, size_ratio: float = 0.0,
-                 persistent: int = 0):
+                 persistent: int = 0, order: int = 0):
         self.L = A.load()
         self.precision = precision
         self.lin_tol = lin_tol if lin_tol is not None else (1e-6 if precision == A.PREC_FP32 else 1e-10)
         cfg = A.ServeConfig(max_batch, max_batches, precision, reserve_bytes, 0, test_budget_bytes,
-                            test_fake_us_per_elem, batch_window_us, size_ratio, persistent)
+                            test_fake_us_per_elem, batch_window_us, size_ratio, persistent, order)
         self.h = C.c_void_p()
         st = self.L.isl_serve_create(C.byref(self.h), device, C.byref(cfg))
         if st != A.ISL_OK:
