@@ -149,9 +149,10 @@ def max_over_ranks(value, pg):
     return float(t.item())
 
 
-def spmv_bytes(nnz, n, v):
-    """Algorithmic bytes of one CSR SpMV: nnz (v + 4) + 4 (N + 1) + 2 N v."""
-    return nnz * (v + 4) + 4 * (n + 1) + 2 * n * v
+def spmv_bytes(nnz, n, v, col=4):
+    """Algorithmic bytes of one CSR SpMV: nnz (v + col) + 4 (N + 1) + 2 N v
+    (col = 2 with 16-bit column offsets)."""
+    return nnz * (v + col) + 4 * (n + 1) + 2 * n * v
 
 
 def log(*a):
@@ -325,7 +326,7 @@ def serve_batch_spmv(requests, local):
     S.assemble(A.PREC_FP32, incremental=True, with_residual=True)
     S.solve(A.SOLVE_CG_FP32_IR, tol=1e-6, check=False)
     ms = S.time_spmv(A.PREC_FP32, 30)
-    b = spmv_bytes(S.nnz, S.neq, 4)
+    b = spmv_bytes(S.nnz, S.neq, 4, 2 if S.get_option(A.OPT_SHORT_COLUMNS) else 4)
     out = {"ms": ms, "bytes": b, "neq": S.neq, "nnz": S.nnz, "instances": len(requests)}
     S.close()
     return out
@@ -762,7 +763,7 @@ def run_batch(args, rank, world, local, pg):
     sp_ms, sp_bytes, kinds = 0.0, 0, []
     for S in systems:
         sp_ms += S.time_spmv(A.PREC_FP32, 20)
-        sp_bytes += spmv_bytes(S.nnz, S.neq, 4)
+        sp_bytes += spmv_bytes(S.nnz, S.neq, 4, 2 if S.get_option(A.OPT_SHORT_COLUMNS) else 4)
         kinds.append(S.get_option(A.OPT_SPMV32_KIND))
     ach = sp_bytes / (sp_ms * 1e-3) / 1e9
     kname = ", ".join(sorted({("kb_sspmv<%d,%d>" % (k - 100, 8 if k < 108 else 6)) if k >= 100 else
@@ -1064,11 +1065,12 @@ def run_single(args, rank, world, local, pg):
             kname = BSPMV_KERNEL.get(bkind, "k_bspmv") + " (sliced-ELL 3x3 FP32 blocks, inner CG SpMV, autotuned variant)"
     else:
         nblk, nslot = 0, S.get_option(A.OPT_SCALAR_SLOTS)
-        b32 = spmv_bytes(nnz, neq, 4)
+        b32 = spmv_bytes(nnz, neq, 4, 2 if S.get_option(A.OPT_SHORT_COLUMNS) else 4)
         kind = S.get_option(A.OPT_SPMV32_KIND)
         if kind >= 100:
             kname = SSPMV_KERNEL.get(kind, "k_sspmv_batch") + \
-                " (scalar sliced-ELL FP32, rows length-sorted in windows of 2048, inner CG SpMV, autotuned)"
+                " (scalar sliced-ELL FP32, rows length-sorted in windows of 2048" + \
+                (", 16-bit column offsets" if S.get_option(A.OPT_SHORT_COLUMNS) else "") + ", inner CG SpMV, autotuned)"
         else:
             kname = f"k_spmv_pap<float,float,{kind}> (FP32 CSR, {kind} lanes per row, inner CG SpMV, autotuned)"
     ach = b32 / (spmv32_ms * 1e-3) / 1e9

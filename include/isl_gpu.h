@@ -359,9 +359,11 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
  * 10^value since the last one (2: 100x in r.r, i.e. 10x in ||r||); 1..8. */
 /* ISL_OPT_SHORT_COLUMNS (default 1): the block SpMV with the folded direction
  * update reads each slot's column as a 16-bit offset from its block row (2 B
- * per stored block instead of 4) when every offset of the matrix fits; 0
- * keeps the 32-bit columns.  Read back: 1 when the 16-bit columns are in use
- * (the option on and the offsets fitting). */
+ * per stored block instead of 4), and the FP32 scalar sliced-ELL SpMVs (one
+ * system, or a batch) as an offset from the slot's row (6 B per stored entry
+ * instead of 8), when every offset of the matrix fits; 0 keeps the 32-bit
+ * columns.  Read back: 1 when the 16-bit columns are in use (the option on
+ * and the offsets fitting). */
 /* ISL_OPT_BLOCK_UPDATE: the update kernel of the graph path of the block CG
  * (x, r, z = B^-1 r, r.r, r.z): 1 one thread per node (what 0, the default,
  * selects), 2, 4 or 8 tiles of 256 nodes staged through shared memory with

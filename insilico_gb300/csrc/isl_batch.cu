@@ -230,9 +230,11 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
 // length into slices of 32 (one lane per row); the block's 8 warps take its
 // slices in turn and keep the loads of U slots in flight per lane.  The
 // instance's p.q follows as in kb_spmv.
-template <int U, int MINB>
+// TC = short: 16-bit column offsets from each lane's row (row 0 for a
+// padding lane)
+template <int U, int MINB, typename TC>
 __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __restrict__ soff, const int* __restrict__ swid,
-                                                   const int* __restrict__ srow, const int* __restrict__ scol,
+                                                   const int* __restrict__ srow, const TC* __restrict__ scol,
                                                    const float* __restrict__ sv, const float* __restrict__ p,
                                                    float* __restrict__ q) {
     __shared__ double sh[32];
@@ -244,6 +246,8 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
     float loc = 0.f;
     for (int s = sl0 + warp; s < sl1; s += BBS / 32) {
         const int o = soff[s] + lane, w = swid[s];
+        const int row = srow[s * 32 + lane];
+        const int base = sizeof(TC) == 2 ? max(row, 0) : 0;
         float acc = 0.f;
         for (int kk = 0; kk < w; kk += U) {
             int j[U];
@@ -251,7 +255,7 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (kk + u < w) {
-                    j[u] = ld_stream(scol + o + (kk + u) * 32);
+                    j[u] = ld_stream(scol + o + (kk + u) * 32) + base;
                     v[u] = ld_stream(sv + o + (kk + u) * 32);
                 }
             }
@@ -259,7 +263,6 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
             for (int u = 0; u < U; ++u)
                 if (kk + u < w) acc += v[u] * __ldg(p + j[u]);
         }
-        const int row = srow[s * 32 + lane];
         if (row >= 0) {
             q[row] = acc;
             loc += p[row] * acc;
@@ -524,10 +527,20 @@ void launch_kb_spmv(int lpr, unsigned grid, cudaStream_t st, const BArgs& a, con
 // FP32 SpMV of the batched mixed solve: kind 2..32 CSR lanes per row,
 // 100 + U the batched sliced-ELL copy
 void launch_kb_spmv32(isl_ctx* c, int kind, unsigned grid, cudaStream_t st, const BArgs& a, const float* p, float* q) {
+    const bool s16 = c->ss16 && c->use_scol16;  // 16-bit column offsets
     switch (kind) {
-        case 102: kb_sspmv<2, 8><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
-        case 104: kb_sspmv<4, 8><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
-        case 108: kb_sspmv<8, 6><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q); break;
+        case 102:
+            if (s16) kb_sspmv<2, 8, short><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q);
+            else kb_sspmv<2, 8, int><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q);
+            break;
+        case 104:
+            if (s16) kb_sspmv<4, 8, short><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q);
+            else kb_sspmv<4, 8, int><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q);
+            break;
+        case 108:
+            if (s16) kb_sspmv<8, 6, short><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q);
+            else kb_sspmv<8, 6, int><<<grid, BBS, 0, st>>>(a, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q);
+            break;
         default: launch_kb_spmv<float, float>(kind, grid, st, a, c->drowptr.p, c->dcolind.p, c->dval32.p, p, q); break;
     }
 }

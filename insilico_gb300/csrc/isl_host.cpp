@@ -1471,7 +1471,10 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     if (key == ISL_OPT_BLOCK_SOLVER) { *value = c->use_block; return ISL_OK; }
     if (key == ISL_OPT_BATCHED_SOLVE) { *value = c->force_batched; return ISL_OK; }
     if (key == ISL_OPT_FOLD_DIRECTION) { *value = c->fuse_dir; return ISL_OK; }
-    if (key == ISL_OPT_SHORT_COLUMNS) { *value = (c->blocked && c->scol16 && c->use_scol16) ? 1 : 0; return ISL_OK; }
+    if (key == ISL_OPT_SHORT_COLUMNS) {
+        *value = c->use_scol16 && (c->blocked ? c->scol16 : c->ss16) ? 1 : 0;
+        return ISL_OK;
+    }
     if (key == ISL_OPT_RELIABLE_DROP) { *value = (int64_t)std::lround(-std::log10(c->ru_drop2)); return ISL_OK; }
     if (key == ISL_OPT_BLOCK_UPDATE) { *value = c->bupd_kind[c->fuse_dir ? 1 : 0]; return ISL_OK; }
     if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }

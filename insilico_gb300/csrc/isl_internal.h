@@ -231,6 +231,8 @@ struct isl_ctx {
     isl::DBuf<int16_t> dscol16;  // slot columns as 16-bit offsets from the slot's block row
     bool scol16 = false;         // every offset fits (dscol16 valid)
     bool use_scol16 = true;      // ISL_OPT_SHORT_COLUMNS
+    isl::DBuf<int16_t> dss_col16;  // scalar sliced-ELL columns as 16-bit offsets from each lane's row
+    bool ss16 = false;           // every offset fits (dss_col16 valid)
     int bupd_kind[2] = {0, 0};  // block CG update kernel (separate / folded direction), 0: not tuned yet
     // padded node blocks: DOF objects with some components constrained keep a
     // 3x3 block row; the solver vectors live in the padded space (3 nbr

@@ -296,10 +296,12 @@ static void launch_residual(int lpr, unsigned grid, cudaStream_t st, int n, cons
 // run at full occupancy (U = 2, 4: 8 blocks of 256 per SM within 32
 // registers; U = 8: 6 blocks), which measured faster on the GB300 than deeper
 // batches at lower occupancy.
-template <int U, int MINB>
+// TC = short: each slot holds its column as a 16-bit offset from the lane's
+// row (row 0 for a padding lane), 6 B per stored entry instead of 8
+template <int U, int MINB, typename TC>
 __global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int* __restrict__ soff,
                                                           const int* __restrict__ swid, const int* __restrict__ srow,
-                                                          const int* __restrict__ scol, const float* __restrict__ sv,
+                                                          const TC* __restrict__ scol, const float* __restrict__ sv,
                                                           const float* __restrict__ p, float* __restrict__ q, CGScal* S,
                                                           double* part) {
     if (S->done) return;
@@ -309,6 +311,8 @@ __global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int*
     float loc = 0.f;
     for (int s = warp; s < nslice; s += nwarps) {
         const int o = soff[s] + lane, w = swid[s];  // w: warp-uniform
+        const int row = srow[s * 32 + lane];
+        const int base = sizeof(TC) == 2 ? max(row, 0) : 0;
         float acc = 0.f;
         for (int k = 0; k < w; k += U) {
             int j[U];
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int*
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (k + u < w) {
-                    j[u] = ld_stream(scol + o + (k + u) * 32);
+                    j[u] = ld_stream(scol + o + (k + u) * 32) + base;
                     v[u] = ld_stream(sv + o + (k + u) * 32);
                 }
             }
@@ -324,7 +328,6 @@ __global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int*
             for (int u = 0; u < U; ++u)
                 if (k + u < w) acc += v[u] * __ldg(p + j[u]);
         }
-        const int row = srow[s * 32 + lane];
         if (row >= 0) {
             q[row] = acc;
             loc += p[row] * acc;
@@ -352,10 +355,20 @@ static unsigned ssell_grid(const isl_ctx* c, unsigned per_sm) {
 static void launch_spmv32(isl_ctx* c, int kind, unsigned grid, cudaStream_t st, const float* p, float* q, CGScal* S,
                           double* part) {
     const int ns = (int)c->ss_nslice;
+    const bool s16 = c->ss16 && c->use_scol16;  // 16-bit column offsets
     switch (kind) {
-        case 102: k_sspmv_batch<2, 8><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
-        case 104: k_sspmv_batch<4, 8><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
-        case 108: k_sspmv_batch<8, 6><<<ssell_grid(c, 6), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part); break;
+        case 102:
+            if (s16) k_sspmv_batch<2, 8, short><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q, S, part);
+            else k_sspmv_batch<2, 8, int><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part);
+            break;
+        case 104:
+            if (s16) k_sspmv_batch<4, 8, short><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q, S, part);
+            else k_sspmv_batch<4, 8, int><<<ssell_grid(c, 8), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part);
+            break;
+        case 108:
+            if (s16) k_sspmv_batch<8, 6, short><<<ssell_grid(c, 6), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col16.p, c->dss_val.p, p, q, S, part);
+            else k_sspmv_batch<8, 6, int><<<ssell_grid(c, 6), BS, 0, st>>>(ns, c->dss_off.p, c->dss_wid.p, c->dss_row.p, c->dss_col.p, c->dss_val.p, p, q, S, part);
+            break;
         default: launch_spmv<float, float>(kind, grid, st, (int)c->neq, c->drowptr.p, c->dcolind.p, c->dval32.p, p, q, S, part); break;
     }
 }
@@ -2280,6 +2293,43 @@ __global__ void k_ssell_fill(int nslice, const int* __restrict__ rowptr, const i
     }
 }
 
+// 16-bit copy of the scalar sliced-ELL columns as offsets from each lane's
+// row (row 0 for a padding lane, whose slots hold column 0); any offset
+// outside the 16-bit range sets *far
+__global__ void k_ssell_col16(int nslice, const int* __restrict__ srow, const int* __restrict__ soff,
+                              const int* __restrict__ swid, const int* __restrict__ scol, short* __restrict__ scol16,
+                              int* __restrict__ far) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nslice * 32; t += gridDim.x * blockDim.x) {
+        const int s = t / 32, l = t % 32;
+        const int base = max(srow[t], 0);
+        const int o = soff[s] + l, w = swid[s];
+        for (int k = 0; k < w; ++k) {
+            const int off = scol[o + k * 32] - base;
+            if (off < -32767 || off > 32767) { atomicOr(far, 1); scol16[o + k * 32] = 0; }
+            else scol16[o + k * 32] = (short)off;
+        }
+    }
+}
+
+// the 16-bit column copy of the scalar sliced-ELL layout, when every offset fits
+static int build_ssell16(isl_ctx* c) {
+    c->ss16 = false;
+    c->dss_col16.release();
+    if (c->ss_nslot == 0) return ISL_OK;
+    cudaStream_t st = c->stream;
+    ISL_CHECK_CUDA(c, c->dss_col16.alloc(c->ss_nslot));
+    ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dflags.p + 1, 0, sizeof(int), st));
+    k_ssell_col16<<<vec_grid(c), BS, 0, st>>>((int)c->ss_nslice, c->dss_row.p, c->dss_off.p, c->dss_wid.p, c->dss_col.p,
+                                              c->dss_col16.p, c->dflags.p + 1);
+    int far = 0;
+    ISL_CHECK_CUDA(c, cudaMemcpyAsync(&far, c->dflags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ISL_CHECK_CUDA(c, cudaStreamSynchronize(st));
+    c->launches += 1;
+    c->ss16 = far == 0;
+    if (!c->ss16) c->dss_col16.release();
+    return ISL_OK;
+}
+
 // Scalar sliced-ELL copy of a system that is not node-blocked (setup).  Rows
 // are sorted by length, longest first and stably, within windows of 2048 rows
 // (a multiple of 32, so no slice spans two windows); the sort keeps the
@@ -2335,7 +2385,7 @@ int scalar_sell_pattern(isl_ctx* c, const std::vector<int32_t>& rp) {
     c->launches += 1;
     c->ss_nslice = nslice;
     c->ss_nslot = tot;
-    return ISL_OK;
+    return build_ssell16(c);
 }
 
 // Sliced-ELL copy of a batch of instances (setup): each row block of the
@@ -2397,7 +2447,7 @@ int batch_sell_pattern(isl_ctx* c, const std::vector<int32_t>& b0, const std::ve
     c->launches += 1;
     c->ss_nslice = nslice;
     c->ss_nslot = tot;
-    return ISL_OK;
+    return build_ssell16(c);
 }
 
 // refresh the block values and the block-Jacobi inverses after an assembly

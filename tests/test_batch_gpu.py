@@ -91,6 +91,13 @@ def test_batch_sliced_ell_and_csr_agree(deg):
         out[kind] = S.solution()
     for kind in (102, 108):
         assert np.array_equal(out[kind], out[104])
+    # 16-bit column offsets (on by default where they fit) against 32-bit ones
+    assert S.get_option(A.OPT_SHORT_COLUMNS) == 1
+    S.set_option(A.OPT_SHORT_COLUMNS, 0)
+    S.set_option(A.OPT_SPMV32_KIND, 104)
+    S.solve(A.SOLVE_CG_FP32_IR, tol=1e-10)
+    assert np.array_equal(S.solution(), out[104])
+    S.set_option(A.OPT_SHORT_COLUMNS, 1)
     for k, p in enumerate(probs):
         P, (orp, oci, ov, ob) = oracle_problem(p)
         r0, r1 = eq_off[k], eq_off[k + 1]

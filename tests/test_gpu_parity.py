@@ -388,6 +388,14 @@ def test_scalar_sliced_ell_and_csr_agree(case):
     for kind in (102, 108):
         assert out[kind][0] == out[104][0] and np.array_equal(out[kind][1], out[104][1])
     assert abs(out[104][0] - out[4][0]) <= max(2, out[4][0] // 50)
+    # 16-bit column offsets from each row (on by default where they fit)
+    # read the same columns: the same bits with 32-bit columns
+    assert S.get_option(A.OPT_SHORT_COLUMNS) == 1
+    S.set_option(A.OPT_SHORT_COLUMNS, 0)
+    S.set_option(A.OPT_SPMV32_KIND, 104)
+    it32, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    assert it32 == out[104][0] and np.array_equal(S.solution(), out[104][1])
+    S.set_option(A.OPT_SHORT_COLUMNS, 1)
     # autotuned choice is one of the candidates and solves to the same bar
     S.set_option(A.OPT_SPMV32_KIND, 0)
     it, rel, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
