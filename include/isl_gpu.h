@@ -353,7 +353,13 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
        ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
        ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14, ISL_OPT_BLOCK_UPDATE = 15,
-       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_RELIABLE_DROP = 17 };
+       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_RELIABLE_DROP = 17, ISL_OPT_SHARED_GEOMETRY = 18 };
+/* ISL_OPT_SHARED_GEOMETRY (default 1): the direct block assembly
+ * (ISL_OPT_DIRECT_BLOCKS) of a mesh whose hexahedra are all translates of the
+ * first (edge vectors equal within 1e-13) forms the 64 local pairs' Lame
+ * blocks once from the first element's Jacobian and adds lam_e and mu_e
+ * multiples of them per element; 0 forms every element's blocks from its own
+ * Jacobian.  Read back: 1 when the last assembly used the shared blocks. */
 /* ISL_OPT_RELIABLE_DROP (default 2): the batched mixed CG of an instance takes
  * an FP64 reliable update when its FP32 residual norm has dropped by
  * 10^value since the last one (2: 100x in r.r, i.e. 10x in ||r||); 1..8. */

@@ -781,6 +781,33 @@ static bool mesh_is_affine_hex(const isl_ctx* c) {
     return true;
 }
 
+// every element a translate of the first: its three edge vectors from the
+// first vertex (hierarchic order 0->1, 0->3, 0->4) equal the first
+// element's within 1e-13 of their length, so all the parallelepipeds share
+// one Jacobian
+static bool mesh_is_uniform_hex(const isl_ctx* c) {
+    const int64_t E = c->nelem;
+    if (E == 0) return false;
+    auto edges = [&](int64_t e, double r[3][3]) {
+        const int64_t* v = &c->hconn[(size_t)e * 8];
+        const int idx[3] = {1, 3, 4};
+        for (int k = 0; k < 3; ++k)
+            for (int d = 0; d < 3; ++d) r[k][d] = c->hX[(size_t)v[idx[k]] * 3 + d] - c->hX[(size_t)v[0] * 3 + d];
+    };
+    double r0[3][3], scale = 0.0;
+    edges(0, r0);
+    for (int k = 0; k < 3; ++k)
+        for (int d = 0; d < 3; ++d) scale = std::max(scale, std::fabs(r0[k][d]));
+    for (int64_t e = 1; e < E; ++e) {
+        double r[3][3];
+        edges(e, r);
+        for (int k = 0; k < 3; ++k)
+            for (int d = 0; d < 3; ++d)
+                if (!(std::fabs(r[k][d] - r0[k][d]) <= 1e-13 * scale)) return false;
+    }
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Neumann tractions (base/asmb/NeumannForce.hpp:132-174): one thread per
 // element owning Neumann faces; f_s += t phi_s(xi(eta)) w |J_s|.
@@ -1234,7 +1261,10 @@ static int dispatch_hyper(isl_ctx* c, const ElemArgs& A) {
     if (h.nq != 8) return hyper_generic(c, A, sizeof(R) == 4);  // the fast path is written for 2x2x2
     Tab<3, 8, 8, 8> T;
     fill_tab<ISL_HEX, 1, 8>(T, h);
-    if (c->mesh_affine < 0) c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
+    if (c->mesh_affine < 0) {
+        c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
+        c->mesh_uniform = (c->mesh_affine == 1 && mesh_is_uniform_hex(c)) ? 1 : 0;
+    }
     const bool ti = A.rho || A.nfw > 0;
     if (!A.general && !A.fnodal && !ti && c->mesh_affine == 1) {
         // small strain on parallelepipeds: reference integrals times the constant Jacobian
@@ -1386,8 +1416,10 @@ int assemble_device(isl_ctx* c, int precision, int incremental, int with_residua
     int rc;
     // mixed precision on parallelepiped hexahedra (small strain, node-blocked):
     // element blocks straight into the FP64 CSR and the FP32 block copies
-    if (c->kernel == ISL_KERNEL_HYPERELASTIC && c->mesh_affine < 0 && c->shape == ISL_HEX && c->fedeg == 1)
+    if (c->kernel == ISL_KERNEL_HYPERELASTIC && c->mesh_affine < 0 && c->shape == ISL_HEX && c->fedeg == 1) {
         c->mesh_affine = mesh_is_affine_hex(c) ? 1 : 0;
+        c->mesh_uniform = (c->mesh_affine == 1 && mesh_is_uniform_hex(c)) ? 1 : 0;
+    }
     const bool direct = precision == ISL_PREC_MIXED && c->qdeg == 3 && !c->stage_full && affine_blocks_eligible(c, A);
     if (!direct) {
         if (k32) ISL_CHECK_CUDA(c, c->dstageK32.alloc(nstage * E));

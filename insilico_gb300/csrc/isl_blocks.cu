@@ -166,6 +166,89 @@ __global__ void __launch_bounds__(256) k_affine_blocks(BlockArgs P, AffinePairs 
     }
 }
 
+// The same blocks on a mesh whose elements all share the first element's
+// geometry (translates of one parallelepiped): the 64 local pairs' Lame
+// blocks W_ab (the lambda part) and W_ab^T + tr(W_ab) I (the mu part) are
+// formed once per CTA in shared memory, from the first element's G and Ji,
+// and each (block, element) pair adds lam_e WL + mu_e WM in double-float
+// (36 operations instead of about 130).  Element order and the final
+// expression per entry are those of k_affine_blocks.
+__global__ void __launch_bounds__(256) k_affine_blocks_u(BlockArgs P, AffinePairs T) {
+    __shared__ df sL[64][9], sM[64][9];
+    if (threadIdx.x < 64) {
+        const int pr = threadIdx.x;
+        df G[9], Ji[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { G[k] = ldf(P.geo, k); Ji[k] = ldf(P.geo, 9 + k); }
+        df T1[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+                T1[i * 3 + bb] = df_add(df_add(df_mul(G[i * 3], T.I[pr][bb]), df_mul(G[i * 3 + 1], T.I[pr][3 + bb])),
+                                        df_mul(G[i * 3 + 2], T.I[pr][6 + bb]));
+        df W[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                W[i * 3 + k] = df_add(df_add(df_mul(T1[i * 3], Ji[k * 3]), df_mul(T1[i * 3 + 1], Ji[k * 3 + 1])),
+                                      df_mul(T1[i * 3 + 2], Ji[k * 3 + 2]));
+        const df tr = df_add(df_add(W[0], W[4]), W[8]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                df m = W[k * 3 + i];
+                if (i == k) m = df_add(m, tr);
+                sL[pr][i * 3 + k] = W[i * 3 + k];
+                sM[pr][i * 3 + k] = m;
+            }
+    }
+    __syncthreads();
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < P.nslot; s += gridDim.x * blockDim.x) {
+        const int b = P.sblk[s];
+        if (b < 0) continue;  // padding slot: its values stay 0
+        const int br = P.brow[b], bc = P.bcol[b], j = b - P.bptr[br];
+        const int o = P.brobj[br], c = P.brobj[bc];
+        int ia = P.adj_off[o];
+        const int ea = P.adj_off[o + 1];
+        int ib = P.adj_off[c];
+        const int eb = P.adj_off[c + 1];
+        df acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = df{0.f, 0.f};
+        while (ia < ea && ib < eb) {
+            const int va = P.adj[ia], vb = P.adj[ib];
+            const int e1 = va >> 3, e2 = vb >> 3;
+            if (e1 != e2) {
+                if (e1 < e2) ++ia; else ++ib;
+                continue;
+            }
+            ++ia;
+            ++ib;
+            const int pr = (va & 7) * 8 + (vb & 7);
+            const float4* g = P.geo + (size_t)e1 * GEO_F4;
+            const df lam = ldf(g, 18), mu = ldf(g, 19);
+#pragma unroll
+            for (int k = 0; k < 9; ++k)
+                acc[k] = df_add_acc(acc[k], df_add(df_mul(lam, sL[pr][k]), df_mul(mu, sM[pr][k])));
+        }
+        const size_t g = (size_t)s >> 5, l = (size_t)s & 31;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double* out = P.v64 + P.rowptr[3 * br + r] + 3 * j;
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                const df v = acc[r * 3 + cc];
+                out[cc] = df_to_double(v);
+                P.sv[(g * 9 + r * 3 + cc) * 32 + l] = v.hi;
+                if (P.bv) P.bv[(size_t)(r * 3 + cc) * P.nblk + b] = v.hi;
+            }
+        }
+    }
+}
+
 // Dirichlet lift of the listed elements (those owning constrained DOFs):
 // F[a] -= sum_c K[a][c] g_c over active a and constrained c, with
 // g_c = constraint (- current value when incremental); K in FP64 from the
@@ -326,7 +409,9 @@ int assemble_affine_blocks(isl_ctx* c, const ElemArgs& A) {
     const bool need_bv = c->bspmv_lpb == 0 || c->bspmv_lpb == 4 || c->bspmv_lpb == 8 || c->bspmv_lpb == 16;
     P.bv = need_bv ? c->dbval.p : nullptr;
     const unsigned grid = (unsigned)std::min<int64_t>((c->nslot + 255) / 256, (int64_t)c->sm_count * 8);
-    k_affine_blocks<<<grid, 256, 0, st>>>(P, T);
+    c->last_shared_geo = c->use_shared_geo && c->mesh_uniform == 1;
+    if (c->last_shared_geo) k_affine_blocks_u<<<grid, 256, 0, st>>>(P, T);
+    else k_affine_blocks<<<grid, 256, 0, st>>>(P, T);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 2;
     return ISL_OK;

@@ -588,7 +588,7 @@ static int mesh_upload_impl(isl_ctx* c, int shape, int dim, int64_t n_nodes, con
     c->ninst = n_inst;
     c->inst_node_off.assign(node_off, node_off + n_inst + 1);
     c->inst_elem_off.assign(elem_off, elem_off + n_inst + 1);
-    c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false; c->mesh_affine = -1;
+    c->fedeg = 0; c->numbered = false; c->nnz = 0; c->solved = false; c->mesh_affine = -1; c->mesh_uniform = -1;
     c->bf_valid = false; c->bf_cache.clear();
     if (c->device < 0) return ISL_OK;
     cudaSetDevice(c->device);
@@ -1425,6 +1425,7 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (key == ISL_OPT_BATCHED_SOLVE) { c->force_batched = value != 0; return ISL_OK; }
     if (key == ISL_OPT_FOLD_DIRECTION) { c->fuse_dir = value != 0; return ISL_OK; }
     if (key == ISL_OPT_SHORT_COLUMNS) { c->use_scol16 = value != 0; return ISL_OK; }
+    if (key == ISL_OPT_SHARED_GEOMETRY) { c->use_shared_geo = value != 0; return ISL_OK; }
     if (key == ISL_OPT_RELIABLE_DROP) {
         if (value < 1 || value > 8) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_RELIABLE_DROP takes 1..8");
         c->ru_drop2 = std::pow(10.0, -(double)value);
@@ -1476,6 +1477,7 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
         return ISL_OK;
     }
     if (key == ISL_OPT_RELIABLE_DROP) { *value = (int64_t)std::lround(-std::log10(c->ru_drop2)); return ISL_OK; }
+    if (key == ISL_OPT_SHARED_GEOMETRY) { *value = c->last_shared_geo ? 1 : 0; return ISL_OK; }
     if (key == ISL_OPT_BLOCK_UPDATE) { *value = c->bupd_kind[c->fuse_dir ? 1 : 0]; return ISL_OK; }
     if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }
     if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }

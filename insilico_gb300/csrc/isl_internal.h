@@ -197,6 +197,9 @@ struct isl_ctx {
     bool use_block = true;
     std::vector<int32_t> hrp_small;  // host row pointers of a system small enough for the one-cluster solve
     int mesh_affine = -1;        // every element a parallelepiped / parallelogram (-1: not yet checked)
+    int mesh_uniform = -1;       // every hexahedron a translate of the first (set with mesh_affine)
+    bool use_shared_geo = true;  // ISL_OPT_SHARED_GEOMETRY
+    bool last_shared_geo = false;  // the last direct block assembly formed its blocks from shared tables
     int use_persist = 1;         // one-launch CG kernels: 0 never, 1 for small systems, 2 always where supported
     int cluster_size = -1;       // CTAs of the small-system cluster solve (-1: not yet probed, 0: unavailable)
     int persist_grid = -1;       // blocks of the persistent kernel (-1: not yet probed, 0: unavailable)

@@ -7,6 +7,9 @@ staged FP64 assembly of the same system:
   right-hand side within 1e-12 of the oracle;
 * a sheared parallelepiped mesh with nonzero Dirichlet values (the lift runs on
   the boundary elements) and per-element materials: the same bars;
+* both are translates of one element, so their blocks come from tables formed
+  once (ISL_OPT_SHARED_GEOMETRY), within 1e-13 of the per-element blocks; a
+  graded mesh (boxes of varying width) forms every element's own;
 * the mixed solve on the direct assembly is within 1e-8 of the oracle's FP64 CG
   solution, bitwise reproducible over a second assembly, and the scalar
   point-Jacobi path (FP32 CSR values derived from the FP64 ones) agrees.
@@ -46,9 +49,20 @@ def sheared(n):
                      dirichlet=diri)
 
 
-@pytest.mark.parametrize("case", ["c2", "sheared"])
+def graded(n):
+    """c2-style elasticity on boxes of varying width along x (x -> x^1.5 of
+    the unit-cube nodes): parallelepipeds that are not translates of one
+    another, so every element's blocks come from its own Jacobian."""
+    p = W.config("c2", n=n)
+    X = p.X.copy()
+    X[:, 0] = X[:, 0] ** 1.5
+    p.X = X
+    return p
+
+
+@pytest.mark.parametrize("case", ["c2", "sheared", "graded"])
 def test_direct_blocks_match_oracle_and_staged_fp64(case):
-    p = W.config("c2", n=6) if case == "c2" else sheared(5)
+    p = {"c2": lambda: W.config("c2", n=6), "sheared": lambda: sheared(5), "graded": lambda: graded(5)}[case]()
     S = W.setup_system(p)
     assert S.get_option(A.OPT_BLOCKED) == 1
     S.assemble(A.PREC_FP64)
@@ -59,6 +73,18 @@ def test_direct_blocks_match_oracle_and_staged_fp64(case):
     assert S.get_option(A.OPT_DIRECT_BLOCKS) == 1
     _, _, vd = S.csr()
     bd = S.rhs()
+    # translates of one element (c2, the sheared cube) share the blocks of
+    # the first element's Jacobian; the graded boxes form their own.  The
+    # shared blocks agree with the per-element ones to rounding.
+    assert S.get_option(A.OPT_SHARED_GEOMETRY) == (0 if case == "graded" else 1)
+    S.set_option(A.OPT_SHARED_GEOMETRY, 0)
+    S.assemble(A.PREC_MIXED)
+    assert S.get_option(A.OPT_SHARED_GEOMETRY) == 0
+    _, _, vpe = S.csr()
+    assert csr_entry_err(rp, ci, vd, vpe) <= 1e-13
+    np.testing.assert_array_equal(S.rhs(), bd)
+    S.set_option(A.OPT_SHARED_GEOMETRY, 1)
+    S.assemble(A.PREC_MIXED)
     P, (orp, oci, ov, ob) = oracle_problem(p)
     np.testing.assert_array_equal(rp, orp)
     np.testing.assert_array_equal(ci, oci)
