@@ -119,9 +119,9 @@ def test_size_ratio_groups_requests_of_similar_size():
 def test_largest_first_order():
     """order = 1: each batch starts from the largest queued request (the
     oldest among equals).  One batch at a time, one request per batch: the
-    first request starts at once and runs for 10 ms (simulated), while the
+    first request starts at once and runs for 1.3 s (simulated), while the
     others queue; they then run largest first."""
-    reqs = [serve.Request(i, s, 1.0, 0.0) for i, s in enumerate([8, 5, 9, 7, 9, 3, 6])]
+    reqs = [serve.Request(i, s, 1.0, 0.0) for i, s in enumerate([40, 5, 9, 7, 9, 3, 6])]
     srv = serve.Server(device=0, max_batch=1, max_batches=1, reserve_bytes=0, test_budget_bytes=1 << 50,
                        test_fake_us_per_elem=20.0, order=1)
     done, _ = srv.run(reqs, realtime=False)
