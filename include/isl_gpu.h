@@ -353,12 +353,7 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
        ISL_OPT_BARRIER_TEST = 5, ISL_OPT_SPMV32_KIND = 6, ISL_OPT_SCALAR_SLOTS = 7, ISL_OPT_HOST_SETUP = 8,
        ISL_OPT_BICGSTAB_KIND = 9, ISL_OPT_BATCHED_SOLVE = 10, ISL_OPT_DIRECT_BLOCKS = 11, ISL_OPT_TUNE_RUNS = 12,
        ISL_OPT_ELEM_VARIANT = 13, ISL_OPT_FOLD_DIRECTION = 14, ISL_OPT_BLOCK_UPDATE = 15,
-       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_RELIABLE_DROP = 17, ISL_OPT_SHARED_GEOMETRY = 18,
-       ISL_OPT_CONSUMER_REDUCE = 19 };
-/* ISL_OPT_CONSUMER_REDUCE (default 0): on the folded graph path of the block
- * CG no kernel ends in a last-block reduction; every block of the product
- * reduces the update's partial r.r and r.z itself, and every block of the
- * update the product's partial p.q (fixed order: all blocks agree). */
+       ISL_OPT_SHORT_COLUMNS = 16, ISL_OPT_RELIABLE_DROP = 17, ISL_OPT_SHARED_GEOMETRY = 18 };
 /* ISL_OPT_SHARED_GEOMETRY (default 1): the direct block assembly
  * (ISL_OPT_DIRECT_BLOCKS) of a mesh whose hexahedra are all translates of the
  * first (edge vectors equal within 1e-13) forms the 64 local pairs' Lame

@@ -51,7 +51,7 @@ EXPORTED = [
 (OPT_BLOCK_SOLVER, OPT_BLOCKED, OPT_NBLOCKS, OPT_NSLOTS, OPT_PERSISTENT, OPT_BARRIER_TEST, OPT_SPMV32_KIND,
  OPT_SCALAR_SLOTS, OPT_HOST_SETUP, OPT_BICGSTAB_KIND, OPT_BATCHED_SOLVE, OPT_DIRECT_BLOCKS, OPT_TUNE_RUNS,
  OPT_ELEM_VARIANT, OPT_FOLD_DIRECTION, OPT_BLOCK_UPDATE, OPT_SHORT_COLUMNS,
- OPT_RELIABLE_DROP, OPT_SHARED_GEOMETRY, OPT_CONSUMER_REDUCE) = range(20)
+ OPT_RELIABLE_DROP, OPT_SHARED_GEOMETRY) = range(19)
 
 
 class ServeConfig(C.Structure):

@@ -521,7 +521,6 @@ int isl_ctx_create(isl_ctx** out, int device, void* stream) {
     }
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaMallocHost(&c->hscal, sizeof(isl::CGScal)) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
-    if (cudaMallocHost(&c->hbase, sizeof(int)) != cudaSuccess) { cudaFreeHost(c->hscal); delete c; return ISL_ERR_NOMEM; }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     for (auto& ev : c->mark) cudaEventCreate(&ev);
     if (c->dflags.alloc(4) != cudaSuccess) { delete c; return ISL_ERR_NOMEM; }
@@ -540,7 +539,6 @@ int isl_ctx_destroy(isl_ctx* c) {
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
     for (auto& ev : c->mark) if (ev) cudaEventDestroy(ev);
     if (c->hscal) cudaFreeHost(c->hscal);
-    if (c->hbase) cudaFreeHost(c->hbase);
     cudaStream_t own = c->own_stream ? c->stream : nullptr;
     delete c;  // frees the device buffers (stream-ordered)
     cudaStreamSynchronize(cudaStreamPerThread);
@@ -1428,7 +1426,6 @@ int isl_set_option(isl_ctx* c, int key, int64_t value) {
     if (key == ISL_OPT_FOLD_DIRECTION) { c->fuse_dir = value != 0; return ISL_OK; }
     if (key == ISL_OPT_SHORT_COLUMNS) { c->use_scol16 = value != 0; return ISL_OK; }
     if (key == ISL_OPT_SHARED_GEOMETRY) { c->use_shared_geo = value != 0; return ISL_OK; }
-    if (key == ISL_OPT_CONSUMER_REDUCE) { c->reduce_at_consumer = value != 0; return ISL_OK; }
     if (key == ISL_OPT_RELIABLE_DROP) {
         if (value < 1 || value > 8) ISL_FAIL(c, ISL_ERR_ARG, "ISL_OPT_RELIABLE_DROP takes 1..8");
         c->ru_drop2 = std::pow(10.0, -(double)value);
@@ -1481,7 +1478,6 @@ int isl_get_option(isl_ctx* c, int key, int64_t* value) {
     }
     if (key == ISL_OPT_RELIABLE_DROP) { *value = (int64_t)std::lround(-std::log10(c->ru_drop2)); return ISL_OK; }
     if (key == ISL_OPT_SHARED_GEOMETRY) { *value = c->last_shared_geo ? 1 : 0; return ISL_OK; }
-    if (key == ISL_OPT_CONSUMER_REDUCE) { *value = c->reduce_at_consumer ? 1 : 0; return ISL_OK; }
     if (key == ISL_OPT_BLOCK_UPDATE) { *value = c->bupd_kind[c->fuse_dir ? 1 : 0]; return ISL_OK; }
     if (key == ISL_OPT_DIRECT_BLOCKS) { *value = c->last_direct; return ISL_OK; }
     if (key == ISL_OPT_TUNE_RUNS) { *value = c->tune_runs; return ISL_OK; }

@@ -230,9 +230,6 @@ struct isl_ctx {
     int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
     bool fuse_dir = true;  // fold the block-Jacobi direction update into the block SpMV
-    bool reduce_at_consumer = false;  // ISL_OPT_CONSUMER_REDUCE
-    isl::DBuf<double> dpart_tl;  // partial sums of the consumer-reduction CG
-    isl::DBuf<int> dbase;        // first iteration of the running chunk
     double ru_drop2 = 1e-2;      // batched mixed CG: reliable update after r.r drops by this factor (ISL_OPT_RELIABLE_DROP)
     isl::DBuf<int16_t> dscol16;  // slot columns as 16-bit offsets from the slot's block row
     bool scol16 = false;         // every offset fits (dscol16 valid)
@@ -292,7 +289,6 @@ struct isl_ctx {
     int64_t bicg_serial = -1, pattern_serial = 0;
     isl::DBuf<isl::CGScal> dscal;
     isl::CGScal* hscal = nullptr;  // pinned host mirror
-    int* hbase = nullptr;          // pinned: first iteration of the next CG chunk (reductions at their consumers)
     int spmv_lpr64 = 0, spmv_lpr32 = 0;  // autotuned lanes per row (FP32: 100 + U = sliced-ELL, U slots in flight)
     int spmv32_forced = 0;               // FP32 SpMV kind set through ISL_OPT_SPMV32_KIND (0: autotune)
 

@@ -1634,73 +1634,6 @@ __global__ void __launch_bounds__(BS, MINB) k_bspmv_dir(int nbr, int nslice, con
     }
 }
 
-// ---------------------------------------------------------------------------
-// The folded block CG with the reductions moved to their consumers: no
-// kernel ends in a last-block reduction.  Every block of the product reduces
-// the update kernel's partial r.r and r.z itself (fixed order, so all blocks
-// hold the same beta and decisions), and every block of the update reduces
-// the product's partial p.q the same way.  Iteration it = *base + k, the
-// chunk's first iteration (written by the host before each replay) plus the
-// kernel's place in the captured chunk: no kernel reads a counter that
-// another block of the same kernel writes.  The update's partials are kept
-// for two iterations (pr[it & 1] holds iteration it's), so the product of
-// iteration it reads rz_it from pr[(it + 1) & 1] and rz_{it-1} from
-// pr[it & 1] before the update of iteration it overwrites them.  A product
-// that finds the solve done (converged, reliable update due, iteration
-// limit, breakdown) returns at once; its block 0 leaves the scalar record as
-// the last-block kernels do, and the later kernels of the chunk return on
-// S->done.
-struct TLPart {
-    double* pr;   // [2][2 GU] update partials (r.r, r.z per block), by iteration parity
-    double* pq;   // [GS] product partials (p.q per block)
-    int gu, gs;   // update and product grids
-    const int* base;  // first iteration of the chunk
-};
-
-template <int U, int MINB, typename TC>
-__global__ void __launch_bounds__(BS, MINB) k_bspmv_tl(int nbr, int nslice, const int* __restrict__ soff,
-                                                       const int* __restrict__ swid, const TC* __restrict__ scol,
-                                                       const float* __restrict__ sv, const float* __restrict__ z,
-                                                       float* pa, float* pb, float* __restrict__ q, CGScal* S,
-                                                       TLPart T, int k, int max_iter) {
-    if (S->done) return;
-    __shared__ double sh[32];
-    __shared__ double bc[2];
-    const int it = *T.base + k;
-    const double* cur = T.pr + (size_t)((it + 1) & 1) * 2 * T.gu;  // the update of iteration it - 1
-    const double* prv = T.pr + (size_t)(it & 1) * 2 * T.gu;        // the update of iteration it - 2
-    double rr, rz;
-    reduce_parts2_blk<BS>(cur, T.gu, sh, rr, rz);
-    const double rzp = reduce_parts_blk<BS>(prv, T.gu, 2, 1, sh);
-    if (threadIdx.x == 0) {
-        int done = 0, bad = 0;
-        if (!(rr == rr) || !(rz == rz)) { bad = 1; done = 1; }
-        else if (rr < S->threshold) done = 1;
-        else if (rr < S->rrtrig) done = 3;
-        else if (it >= max_iter) done = 2;
-        const double beta = rzp != 0.0 ? rz / rzp : 0.0;
-        bc[0] = beta;
-        bc[1] = (double)done;
-        if (done && blockIdx.x == 0) {
-            S->rr = rr;
-            S->iters = it;
-            S->absOld = rzp;
-            S->absNew = rz;
-            S->beta = beta;
-            if (bad) S->bad = 1;
-            S->done = done;
-        }
-    }
-    __syncthreads();
-    if (bc[1] != 0.0) return;
-    const bool odd = it & 1;
-    const int warp = (blockIdx.x * BS + threadIdx.x) >> 5, nwarps = gridDim.x * (BS / 32);
-    const float loc = bspmv_slices_dir<U, TC>(nbr, nslice, soff, swid, scol, sv, z, odd ? pb : pa, (float)bc[0],
-                                              odd ? pa : pb, q, warp, nwarps);
-    const double bsum = block_sum_f(loc, sh);
-    if (threadIdx.x == 0) T.pq[blockIdx.x] = bsum;
-}
-
 // q = A p on the block-row CSR copy: LPB lanes per block row
 template <int LPB>
 __global__ void __launch_bounds__(BS, 8) k_brow_spmv(int nbr, const int* __restrict__ bptr, const int* __restrict__ bcol,
@@ -1896,64 +1829,6 @@ __global__ void __launch_bounds__(UT) k_cg_update_b3t(int nbr, float* __restrict
         else if (trr < S->rrtrig) S->done = 3;
         else if (S->iters >= max_iter) S->done = 2;
         S->ticket2 = 0;
-    }
-}
-
-// x += alpha p, r -= alpha q, z = B^-1 r; alpha = rz_it / p.q with both sums
-// reduced at the start; partial r.r and r.z of iteration it into pr[it & 1]
-__global__ void __launch_bounds__(NODE_BS) k_cg_update_tl(int nbr, float* __restrict__ x, float* __restrict__ r,
-                                                          const float* __restrict__ pa, const float* __restrict__ pb,
-                                                          const float* __restrict__ q, const float* __restrict__ binv,
-                                                          float* __restrict__ zout, CGScal* S, TLPart T, int k) {
-    if (S->done) return;
-    __shared__ double sh[32];
-    __shared__ float fa;
-    const int it = *T.base + k;
-    const double rz = reduce_parts_blk<NODE_BS>(T.pr + (size_t)((it + 1) & 1) * 2 * T.gu, T.gu, 2, 1, sh);
-    const double pap = reduce_parts_blk<NODE_BS>(T.pq, T.gs, 1, 0, sh);
-    if (threadIdx.x == 0) fa = (float)(rz / pap);
-    __syncthreads();
-    const float alpha = fa;
-    const float* __restrict__ p = (it & 1) ? pa : pb;  // the product of iteration it wrote the other buffer
-    float rr = 0.f, rzl = 0.f;
-    for (int i = blockIdx.x * NODE_BS + threadIdx.x; i < nbr; i += gridDim.x * NODE_BS) {
-        const size_t d = 3 * (size_t)i;
-        float b[9];
-#pragma unroll
-        for (int kk = 0; kk < 9; ++kk) b[kk] = ld(binv + 9 * (size_t)i + kk);
-        float rv[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            x[d + a] += alpha * ld(p + d + a);
-            rv[a] = r[d + a] - alpha * ld(q + d + a);
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            r[d + a] = rv[a];
-            const float zz = b[3 * a] * rv[0] + b[3 * a + 1] * rv[1] + b[3 * a + 2] * rv[2];
-            zout[d + a] = zz;
-            rr += rv[a] * rv[a];
-            rzl += rv[a] * zz;
-        }
-    }
-    const double b1 = block_sum_f(rr, sh);
-    const double b2 = block_sum_f(rzl, sh);
-    double* mine = T.pr + (size_t)(it & 1) * 2 * T.gu;
-    if (threadIdx.x == 0) { mine[2 * blockIdx.x] = b1; mine[2 * blockIdx.x + 1] = b2; }
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->iters = it + 1;
-}
-
-// after the initial or a restart residual (S->rr, S->absNew; S->absOld the
-// r.z before it): the update partials of the two iterations before the next
-// one, so that its product reads rr, rz and, as the previous r.z, rzp (rzp =
-// rz at the start: beta = 1 on p = 0)
-__global__ void k_tl_seed(CGScal* S, TLPart T, int restart) {
-    const int it = S->iters;
-    double* cur = T.pr + (size_t)((it + 1) & 1) * 2 * T.gu;
-    double* prv = T.pr + (size_t)(it & 1) * 2 * T.gu;
-    for (int i = threadIdx.x; i < 2 * T.gu; i += blockDim.x) {
-        cur[i] = i == 0 ? S->rr : (i == 1 ? S->absNew : 0.0);
-        prv[i] = i == 1 ? (restart ? S->absOld : S->absNew) : 0.0;
     }
 }
 
@@ -2190,28 +2065,6 @@ static void launch_bspmv_dir_t(int kind, cudaStream_t st, isl_ctx* c, const TC* 
         default: k_bspmv_dir<8, 2, TC><<<std::min(g, 2u * c->sm_count), BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, part); break;
     }
 }
-// grid of the folded product of a batched-load kind (5, 6, 7)
-static unsigned bspmv_dir_grid(isl_ctx* c, int kind) {
-    const unsigned g = sell_grid(c);
-    return std::min(g, (kind == 5 ? 4u : kind == 6 ? 3u : 2u) * c->sm_count);
-}
-template <typename TC>
-static void launch_bspmv_tl_t(int kind, cudaStream_t st, isl_ctx* c, const TC* scol, const float* z, float* pa,
-                              float* pb, float* q, CGScal* S, const TLPart& T, int k, int mi) {
-    const int nbr = (int)c->nbr, ns = (int)c->nslice;
-    const unsigned g = bspmv_dir_grid(c, kind);
-    switch (kind) {
-        case 5: k_bspmv_tl<2, 4, TC><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, T, k, mi); break;
-        case 6: k_bspmv_tl<4, 3, TC><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, T, k, mi); break;
-        default: k_bspmv_tl<8, 2, TC><<<g, BS, 0, st>>>(nbr, ns, c->dsoff.p, c->dswid.p, scol, c->dsval.p, z, pa, pb, q, S, T, k, mi); break;
-    }
-}
-static void launch_bspmv_tl(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
-                            CGScal* S, const TLPart& T, int k, int mi) {
-    if (c->scol16 && c->use_scol16) launch_bspmv_tl_t<short>(kind, st, c, c->dscol16.p, z, pa, pb, q, S, T, k, mi);
-    else launch_bspmv_tl_t<int>(kind, st, c, c->dscol.p, z, pa, pb, q, S, T, k, mi);
-}
-
 // the 16-bit column offsets where the matrix has them (and ISL_OPT_SHORT_COLUMNS allows)
 static void launch_bspmv_dir(int kind, cudaStream_t st, isl_ctx* c, const float* z, float* pa, float* pb, float* q,
                              CGScal* S, double* part) {
@@ -2671,30 +2524,12 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     // look faster; inside the solve, after the SpMV has streamed the matrix
     // through L2, they are slower at 64^3)
     const int ukind = c->bupd_kind[fused ? 1 : 0] ? c->bupd_kind[fused ? 1 : 0] : 1;
-    // reductions at their consumers (ISL_OPT_CONSUMER_REDUCE): the update's
-    // partials kept for two iterations, the product's, and the chunk's first
-    // iteration, written before each replay
-    const bool tl = fused && c->reduce_at_consumer;
-    TLPart T{};
-    if (tl) {
-        T.gu = (int)node_grid(c, nbr);
-        T.gs = (int)bspmv_dir_grid(c, c->bspmv_lpb);
-        ISL_CHECK_CUDA(c, c->dpart_tl.alloc((size_t)4 * T.gu + T.gs));
-        ISL_CHECK_CUDA(c, c->dbase.alloc(1));
-        T.pr = c->dpart_tl.p;
-        T.pq = c->dpart_tl.p + 4 * T.gu;
-        T.base = c->dbase.p;
-    }
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0,
                                       exact64 ? kDelta2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
-    if (tl) {
-        k_tl_seed<<<1, 256, 0, st>>>(S, T, 0);
-        c->launches += 1;
-    }
     cudaGraph_t graph;
     cudaGraphExec_t exec = nullptr;
     if (pgrid == 0) {
@@ -2702,10 +2537,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     ISL_CHECK_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const unsigned nbd = (unsigned)std::max<long long>(1, (3LL * nbr + NBS - 1) / NBS);  // one pass, no reduction
     for (int k = 0; k < CHUNK; ++k) {
-        if (tl) {
-            launch_bspmv_tl(c->bspmv_lpb, st, c, z32, p32, p32b, q32, S, T, k, mi);
-            k_cg_update_tl<<<T.gu, NODE_BS, 0, st>>>(nbr, x32, r32, p32, p32b, q32, c->dbinv.p, z32, S, T, k);
-        } else if (fused) {
+        if (fused) {
             launch_bspmv_dir(c->bspmv_lpb, st, c, z32, p32, p32b, q32, S, c->dpart.p);
             launch_update(c, ukind, true, st, x32, r32, p32, p32b, q32, z32, S, mi);
         } else {
@@ -2755,12 +2587,6 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             }
             c->launches += 1;
         } else {
-            if (tl) {  // the chunk's first iteration: the count the last read of the scalar record gave
-                *c->hbase = c->hscal->iters;
-                if (cudaMemcpyAsync(c->dbase.p, c->hbase, sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess) {
-                    rc = ISL_ERR_CUDA; c->err = "chunk base copy failed"; break;
-                }
-            }
             if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = ISL_ERR_CUDA; c->err = "graph launch failed"; break; }
             c->launches += (fused ? 2 : 3) * CHUNK;
         }
@@ -2794,13 +2620,6 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol,
                                               fresh ? 2 : 1, kDelta2 * rr_true);
             c->launches += 1;
-            if (tl) {
-                // the next product reads p_old from the buffer of the next
-                // iteration's parity; fresh directions: that buffer cleared
-                if (fresh) ISL_CHECK_CUDA(c, cudaMemsetAsync((h.iters & 1) ? p32b : p32, 0, na * 4, st));
-                k_tl_seed<<<1, 256, 0, st>>>(S, T, 1);
-                c->launches += 1;
-            }
         }
     }
     if (exec) cudaGraphExecDestroy(exec);

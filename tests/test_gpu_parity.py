@@ -253,18 +253,6 @@ def test_folded_direction_update_matches_separate_kernel():
     assert S.get_option(A.OPT_SHORT_COLUMNS) == 0
     it32, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
     assert it32 == it16 and np.array_equal(S.solution(), x16)
-    # reductions at their consumers: every block of the next kernel reduces
-    # the partial sums itself (no last-block tails); the same recurrence with
-    # the sums grouped differently, the same bars, bitwise reproducible
-    S.set_option(A.OPT_SHORT_COLUMNS, 1)
-    S.set_option(A.OPT_CONSUMER_REDUCE, 1)
-    assert S.get_option(A.OPT_CONSUMER_REDUCE) == 1
-    itc, relc, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
-    xc = S.solution()
-    itc2, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
-    assert itc2 == itc and np.array_equal(S.solution(), xc)
-    assert relc <= 1e-12 and abs(itc - it16) <= max(2, it16 // 50)
-    assert np.linalg.norm(xc - x64) <= 1e-8 * np.linalg.norm(x64)
     S.close()
 
 
@@ -336,10 +324,6 @@ def test_partially_constrained_nodes_use_padded_blocks(n):
     assert rel <= 1e-12 and np.linalg.norm(xb - xo) <= 1e-8 * on
     it_b2, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
     assert it_b2 == it_b and np.array_equal(S.solution(), xb)
-    S.set_option(A.OPT_CONSUMER_REDUCE, 1)
-    _, relc, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
-    assert relc <= 1e-12 and np.linalg.norm(S.solution() - xo) <= 1e-8 * on
-    S.set_option(A.OPT_CONSUMER_REDUCE, 0)
     S.solve(A.SOLVE_CG_FP64, tol=1e-13)
     assert np.linalg.norm(S.solution() - xo) <= 1e-8 * on
     S.set_option(A.OPT_BLOCK_SOLVER, 0)
