@@ -360,9 +360,10 @@ enum { ISL_OPT_BLOCK_SOLVER = 0, ISL_OPT_BLOCKED = 1, ISL_OPT_NBLOCKS = 2, ISL_O
  * blocks once from the first element's Jacobian and adds lam_e and mu_e
  * multiples of them per element; 0 forms every element's blocks from its own
  * Jacobian.  Read back: 1 when the last assembly used the shared blocks. */
-/* ISL_OPT_RELIABLE_DROP (default 2): the batched mixed CG of an instance takes
- * an FP64 reliable update when its FP32 residual norm has dropped by
- * 10^value since the last one (2: 100x in r.r, i.e. 10x in ||r||); 1..8. */
+/* ISL_OPT_RELIABLE_DROP (default 2): the mixed CG (one system on the graph
+ * path, or each instance of a batch) takes an FP64 reliable update when its
+ * FP32 r.r has dropped by 10^value since the last one (2: 100x in r.r, i.e.
+ * 10x in ||r||); 1..8.  The one-launch solves of small systems keep 2. */
 /* ISL_OPT_SHORT_COLUMNS (default 1): the block SpMV with the folded direction
  * update reads each slot's column as a 16-bit offset from its block row (2 B
  * per stored block instead of 4), and the FP32 scalar sliced-ELL SpMVs (one

@@ -230,7 +230,7 @@ struct isl_ctx {
     int64_t elem_variant_key = -1;
     int bspmv_lpb = 0;
     bool fuse_dir = true;  // fold the block-Jacobi direction update into the block SpMV
-    double ru_drop2 = 1e-2;      // batched mixed CG: reliable update after r.r drops by this factor (ISL_OPT_RELIABLE_DROP)
+    double ru_drop2 = 1e-2;      // mixed CG: reliable update after r.r drops by this factor (ISL_OPT_RELIABLE_DROP)
     isl::DBuf<int16_t> dscol16;  // slot columns as 16-bit offsets from the slot's block row
     bool scol16 = false;         // every offset fits (dscol16 valid)
     bool use_scol16 = true;      // ISL_OPT_SHORT_COLUMNS

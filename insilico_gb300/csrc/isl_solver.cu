@@ -37,7 +37,9 @@ namespace isl {
 
 constexpr int BS = 256;
 constexpr int CHUNK = 32;
-// reliable update when the iterated residual has dropped 10x (squared: 1e-2)
+// reliable update when the iterated residual has dropped 10x (squared: 1e-2);
+// the one-cluster solve of small systems uses this, the graph paths the
+// context's ISL_OPT_RELIABLE_DROP (default the same)
 constexpr double kDelta2 = 1e-2;
 
 // q = A p; partial p.q; last block: alpha = absNew / p.q
@@ -1122,7 +1124,7 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_dinv<float, float><<<grid, BS, 0, st>>>((int)n, c->ddiag.p, c->dval32.p, d32);
     k_cg_init<double, float><<<grid, BS, 0, st>>>((int)n, c->drhs.p, x32, r32, p32, d32, S, c->dpart.p, tol,
-                                                   c->have64 ? kDelta2 : 0.0);
+                                                   c->have64 ? c->ru_drop2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 2;
     cudaGraphExec_t exec;
@@ -1168,7 +1170,7 @@ static int solve_mixed(isl_ctx* c, double tol, int64_t max_iter, int64_t* iters,
             if (at_max) { *nc = true; break; }
             const int fresh = (rr_last > 0.0 && rr_true >= rr_last) ? 1 : 0;
             rr_last = rr_true;
-            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p, kDelta2 * rr_true, fresh);
+            k_restart32<<<grid, BS, 0, st>>>((int)n, r64, r32, d32, S, c->dpart.p, c->ru_drop2 * rr_true, fresh);
             c->launches += 1;
         }
     }
@@ -2527,7 +2529,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dscal.p, 0, 2 * sizeof(CGScal), st));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(x64, 0, n * 8, st));
     k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, c->drhs.p, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol, 0,
-                                      exact64 ? kDelta2 : 0.0);
+                                      exact64 ? c->ru_drop2 : 0.0);
     ISL_CHECK_CUDA(c, cudaGetLastError());
     c->launches += 1;
     cudaGraph_t graph;
@@ -2618,7 +2620,7 @@ static int solve_mixed_b3(isl_ctx* c, double tol, int64_t max_iter, int64_t* ite
             const int fresh = (rr_last > 0.0 && rr_true >= rr_last) ? 1 : 0;
             rr_last = rr_true;
             k_cg_init_b3<<<grid, BS, 0, st>>>(nbr, r64, aeq, x32, r32, p32, c->dbinv.p, z32, S, c->dpart.p, tol,
-                                              fresh ? 2 : 1, kDelta2 * rr_true);
+                                              fresh ? 2 : 1, c->ru_drop2 * rr_true);
             c->launches += 1;
         }
     }
