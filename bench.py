@@ -205,8 +205,25 @@ def oracle_leg(p, threads):
     t0 = time.perf_counter()
     x, it, rr, hist = O.cg(rp, ci, v, b, tol=ORACLE_TOL, nthreads=threads, history=True)
     t_cg = time.perf_counter() - t0
+    # one thread: the assembly's fixed part (clearing values and right-hand
+    # side) plus the element loop over one element in 32, scaled, and 8 CG
+    # iterations (the element loop and the iterations cost in proportion)
+    esample = max(1, p.nelem // 32)
+    P.element_range(0, 0)
+    t0 = time.perf_counter()
+    P.assemble(incremental=True, nthreads=1)
+    t_fixed1 = time.perf_counter() - t0
+    P.element_range(0, esample)
+    t0 = time.perf_counter()
+    P.assemble(incremental=True, nthreads=1)
+    t_asm1 = t_fixed1 + max(0.0, time.perf_counter() - t0 - t_fixed1) * p.nelem / esample
+    P.element_range(0, -1)
+    t0 = time.perf_counter()
+    O.cg(rp, ci, v, b, tol=0.0, max_iter=8, nthreads=1)
+    t_iter1 = (time.perf_counter() - t0) / 9
     return {"P": P, "csr": (rp, ci, v, b), "x": x, "t_setup": t_setup, "t_asm": t_asm, "t_cg": t_cg,
-            "iters": it, "t_iter": t_cg / (it + 1), "hist": hist, "neq": P.neq, "threads": threads}
+            "iters": it, "t_iter": t_cg / (it + 1), "hist": hist, "neq": P.neq, "threads": threads,
+            "t_asm1": t_asm1, "t_iter1": t_iter1}
 
 
 def oracle_rate(leg, tol):
@@ -1105,7 +1122,11 @@ def run_single(args, rank, world, local, pg):
                          f"to {ORACLE_TOL:g} timed ({leg['t_cg']:.1f} s, {leg['iters']} iterations), counted at the "
                          f"{its_cpu} iterations of the plain path's tolerance {tol64:g}; numbering and pattern "
                          f"({leg['t_setup']:.1f} s) outside, as on the GPU",
-               "assembly_s": leg["t_asm"], "cg_iter_s": leg["t_iter"], "cg_iters": its_cpu, "step_s": t_cpu}
+               "assembly_s": leg["t_asm"], "cg_iter_s": leg["t_iter"], "cg_iters": its_cpu, "step_s": t_cpu,
+               "one_thread": {"value": neq / (leg["t_asm1"] + leg["t_iter1"] * (its_cpu + 1)), "unit": UNIT,
+                              "assembly_s": leg["t_asm1"], "cg_iter_s": leg["t_iter1"],
+                              "sample": "assembly of 1/32 of the elements and 8 CG iterations on one thread, "
+                                        "scaled to the full step"}}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
