@@ -253,6 +253,12 @@ def test_folded_direction_update_matches_separate_kernel():
     assert S.get_option(A.OPT_SHORT_COLUMNS) == 0
     it32, _, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
     assert it32 == it16 and np.array_equal(S.solution(), x16)
+    # reliable updates after every 10x drop of the FP32 r.r instead of 100x
+    S.set_option(A.OPT_SHORT_COLUMNS, 1)
+    S.set_option(A.OPT_RELIABLE_DROP, 1)
+    itd, reld, _ = S.solve(A.SOLVE_CG_FP32_IR, tol=1e-12)
+    assert reld <= 1e-12 and np.linalg.norm(S.solution() - x64) <= 1e-8 * np.linalg.norm(x64)
+    S.set_option(A.OPT_RELIABLE_DROP, 2)
     S.close()
 
 
