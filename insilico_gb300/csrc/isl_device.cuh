@@ -176,7 +176,8 @@ __device__ inline double reduce_parts(const double* part, int n, int stride, int
             v[u] = i < n ? __ldcg(part + (size_t)i * stride + off) : 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
+        for (int u = 0; u < 8; ++u)
+            if (base + u * 32 + l < n) s += v[u];
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return s;
@@ -198,7 +199,8 @@ __device__ inline void reduce_parts2(const double* part, int n, double* sh, doub
             v[u] = i < n ? __ldcg(p2 + i) : make_double2(0.0, 0.0);
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) { s0 += v[u].x; s1 += v[u].y; }
+        for (int u = 0; u < 8; ++u)
+            if (base + u * 32 + l < n) { s0 += v[u].x; s1 += v[u].y; }
     }
     for (int o = 16; o > 0; o >>= 1) {
         s0 += __shfl_xor_sync(0xffffffffu, s0, o);
@@ -225,8 +227,11 @@ __device__ inline double reduce_parts_blk(const double* part, int n, int stride,
             const int i = base + u * NT + (int)threadIdx.x;
             v[u] = i < n ? __ldcg(part + (size_t)i * stride + off) : 0.0;
         }
+        // only the loaded entries are added (adding the zeros changes no
+        // sum, and FP64 adds are scarce on this GPU)
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
+        for (int u = 0; u < 8; ++u)
+            if (base + u * NT + (int)threadIdx.x < n) s += v[u];
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     __syncthreads();  // sh may still be read by an earlier block sum
@@ -251,7 +256,8 @@ __device__ inline void reduce_parts2_blk(const double* part, int n, double* sh, 
             v[u] = i < n ? __ldcg(p2 + i) : make_double2(0.0, 0.0);
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) { s0 += v[u].x; s1 += v[u].y; }
+        for (int u = 0; u < 8; ++u)
+            if (base + u * NT + (int)threadIdx.x < n) { s0 += v[u].x; s1 += v[u].y; }
     }
     for (int o = 16; o > 0; o >>= 1) {
         s0 += __shfl_xor_sync(0xffffffffu, s0, o);
