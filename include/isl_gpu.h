@@ -45,6 +45,9 @@ typedef enum {
 /* element shapes (geometry degree 1, hierarchic vertex order of
  * base/mesh/HierarchicOrder.hpp) */
 enum { ISL_QUAD = 3, ISL_TET = 4, ISL_HEX = 5 };
+/* ISL_TRI: the faces of tetrahedra; a shape of isl_quadrature_rule only (the
+ * surface rules of Neumann tractions on tetrahedra) */
+enum { ISL_TRI = 2 };
 /* kernel functors */
 enum { ISL_KERNEL_LAPLACE = 0, ISL_KERNEL_HYPERELASTIC = 1, ISL_KERNEL_HEAT_STATIC = 2 };
 /* materials of solid::HyperElastic */
@@ -142,8 +145,10 @@ int isl_register_pattern(isl_ctx* ctx, int64_t* nnz);
  * NULL arrays give the count.  Host only, no context.  Rules exist for
  * degrees 1 to 5: Gauss-Legendre with 1, 2 or 3 points per direction
  * ((degree + 2) / 2, base/quad/GaussLegendre.hpp:33-37) on quadrilaterals and
- * hexahedra, and 1, 4, 5, 11 or 15 points on tetrahedra; ISL_ERR_ARG for
- * degree 0, degrees above 5 and other shapes. */
+ * hexahedra, 1, 4, 5, 11 or 15 points on tetrahedra, and 1, 3, 4, 6 or 7
+ * points on triangles (ISL_TRI, the surface rules of tetrahedron faces,
+ * base/quad/GaussTriangle.hpp:97-180); ISL_ERR_ARG for degree 0, degrees
+ * above 5 and other shapes. */
 int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi);
 
 /* Kernel functor tabulation (per element coefficients; the reference's

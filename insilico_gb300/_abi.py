@@ -14,6 +14,7 @@ from . import build as _build
  ISL_ERR_CAPACITY) = range(9)
 NOALLOC_MAX_N = 65536  # ISL_NOALLOC_MAX_N
 QUAD, TET, HEX = 3, 4, 5
+TRI = 2  # tetrahedron faces: isl_quadrature_rule only
 KERNEL_LAPLACE, KERNEL_HYPERELASTIC, KERNEL_HEAT_STATIC = 0, 1, 2
 MAT_STVENANT, MAT_NEOHOOKE = 0, 1
 THERMAL_CONSTANT, THERMAL_FENICS = 0, 1
@@ -209,7 +210,7 @@ def quadrature_rule(shape: int, degree: int):
     st = L.isl_quadrature_rule(shape, degree, C.byref(n), None, None)
     if st != ISL_OK:
         raise IslError(st, f"isl_quadrature_rule: no rule for shape {shape}, degree {degree}")
-    dim = 2 if shape == QUAD else 3
+    dim = 2 if shape in (QUAD, TRI) else 3
     w = np.zeros(n.value)
     x = np.zeros(n.value * dim)
     L.isl_quadrature_rule(shape, degree, C.byref(n), d(w), d(x))

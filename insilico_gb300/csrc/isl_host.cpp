@@ -131,8 +131,53 @@ void element_eval(int shape, int k, const double* xi, std::vector<double>& v, st
 // (base/quad/GaussLegendre.hpp:115-134), tensor products with the first
 // coordinate fastest (base/quad/TensorProduct.hpp:123-178), and the
 // tetrahedron rules of degree 1 to 5 of base/quad/GaussTetrahedron.hpp.
+// surface rules of tetrahedron faces (ISL_TRI: a shape of isl_quadrature_rule only)
+constexpr int kTriFace = ISL_TRI;
+
 bool quadrature(int shape, int qdeg, std::vector<double>& w, std::vector<double>& x) {
     w.clear(); x.clear();
+    if (shape == kTriFace) {
+        // triangle rules of degree 1-5 with the reference's truncated
+        // constants and point order (base/quad/GaussTriangle.hpp:97-180):
+        // per point the weight, then the two local coordinates
+        static const double r1[] = {0.5, 0.333333333333333, 0.333333333333333};
+        static const double r2[] = {0.166666666666666, 0.666666666666667, 0.166666666666667,
+                                    0.166666666666666, 0.166666666666667, 0.666666666666667,
+                                    0.166666666666666, 0.166666666666667, 0.166666666666667};
+        static const double r3[] = {-0.28125, 0.333333333333333, 0.333333333333333,
+                                    0.260416666666667, 0.6, 0.2,
+                                    0.260416666666667, 0.2, 0.6,
+                                    0.260416666666667, 0.2, 0.2};
+        static const double r4[] = {0.111690794839005, 0.10810301816807, 0.445948490915965,
+                                    0.054975871827661, 0.816847572980459, 0.091576213509771,
+                                    0.111690794839005, 0.445948490915965, 0.10810301816807,
+                                    0.111690794839005, 0.445948490915965, 0.445948490915965,
+                                    0.054975871827661, 0.091576213509771, 0.816847572980459,
+                                    0.054975871827661, 0.091576213509771, 0.091576213509771};
+        static const double r5[] = {0.1125, 0.333333333333333, 0.333333333333333,
+                                    0.066197076394253, 0.05971587178977, 0.470142064105115,
+                                    0.0629695902724135, 0.797426985353087, 0.101286507323456,
+                                    0.066197076394253, 0.470142064105115, 0.05971587178977,
+                                    0.066197076394253, 0.470142064105115, 0.470142064105115,
+                                    0.0629695902724135, 0.101286507323456, 0.797426985353087,
+                                    0.0629695902724135, 0.101286507323456, 0.101286507323456};
+        const double* r;
+        int np;
+        switch (qdeg <= 1 ? 1 : qdeg) {
+            case 1: r = r1; np = 1; break;
+            case 2: r = r2; np = 3; break;
+            case 3: r = r3; np = 4; break;
+            case 4: r = r4; np = 6; break;
+            case 5: r = r5; np = 7; break;
+            default: return false;
+        }
+        for (int k = 0; k < np; ++k) {
+            w.push_back(r[3 * k]);
+            x.push_back(r[3 * k + 1]);
+            x.push_back(r[3 * k + 2]);
+        }
+        return true;
+    }
     if (shape == ISL_TET) {
         // Keast rules with the reference's truncated constants and point
         // order (base/quad/GaussTetrahedron.hpp:93-175): both decide the last
@@ -242,20 +287,30 @@ bool make_face_tables(int shape, int fedeg, int sqdeg, FaceTab& t) {
     int sshape;
     if (shape == ISL_QUAD) { t.nfaces = 4; t.nfv = 2; sshape = 0; }
     else if (shape == ISL_HEX) { t.nfaces = 6; t.nfv = 4; sshape = ISL_QUAD; }
-    else return false;  // triangle faces are not needed by the configured workloads
+    else { t.nfaces = 4; t.nfv = 3; sshape = kTriFace; }
     if (!quadrature(sshape, sqdeg, sw, sx)) return false;
     t.nsq = (int)sw.size();
     t.w = sw;
     for (int f = 0; f < t.nfaces; ++f)
-        for (int v = 0; v < t.nfv; ++v) t.fv.push_back(shape == ISL_QUAD ? kQuadEdges[f][v] : kHexFaces[f][v]);
+        for (int v = 0; v < t.nfv; ++v)
+            t.fv.push_back(shape == ISL_QUAD ? kQuadEdges[f][v] : shape == ISL_HEX ? kHexFaces[f][v] : kTetFaces[f][v]);
     std::vector<double> vc;
     vertex_local_coords(shape, vc);
     const int sd = t.dim - 1;
-    // surface geometry functions: line [1-e, e] or hierarchic bilinear quad
+    // surface geometry functions: line [1-e, e], linear triangle [1-a-b, a, b]
+    // or hierarchic bilinear quad
     t.dS.assign((size_t)t.nsq * t.nfv * sd, 0.0);
     std::vector<double> sval((size_t)t.nsq * t.nfv);
     for (int q = 0; q < t.nsq; ++q) {
-        if (sd == 1) {
+        if (t.nfv == 3) {
+            const double a = sx[q * 2], b = sx[q * 2 + 1];
+            const double vv[3] = {1 - a - b, a, b}, da[3] = {-1, 1, 0}, db[3] = {-1, 0, 1};
+            for (int v = 0; v < 3; ++v) {
+                sval[q * 3 + v] = vv[v];
+                t.dS[(q * 3 + v) * 2 + 0] = da[v];
+                t.dS[(q * 3 + v) * 2 + 1] = db[v];
+            }
+        } else if (sd == 1) {
             const double e = sx[q];
             sval[q * 2 + 0] = 1 - e; sval[q * 2 + 1] = e;
             t.dS[(q * 2 + 0)] = -1; t.dS[(q * 2 + 1)] = 1;
@@ -386,9 +441,8 @@ int neumann_faces(isl_ctx* c, int64_t n, const int64_t* elem, const int* face, c
     c->n_neu_elem = 0;
     if (n <= 0) return ISL_OK;
     if (!elem || !face || !traction) return ISL_ERR_ARG;
-    if (c->shape == ISL_TET) ISL_FAIL(c, ISL_ERR_ARG, "Neumann faces on tetrahedra are not supported");
-    const int nfc = c->shape == ISL_QUAD ? 4 : 6;
-    const int nval = (vertex ? (c->shape == ISL_QUAD ? 2 : 4) : 1) * c->ncomp;
+    const int nfc = c->shape == ISL_HEX ? 6 : 4;
+    const int nval = (vertex ? (c->shape == ISL_QUAD ? 2 : c->shape == ISL_TET ? 3 : 4) : 1) * c->ncomp;
     std::vector<int64_t> idx(n);
     std::iota(idx.begin(), idx.end(), 0);
     for (int64_t i = 0; i < n; ++i)
@@ -1498,7 +1552,8 @@ int isl_quadrature_rule(int shape, int degree, int* n, double* w, double* xi) {
     ISL_TRY
     // the reference's rules exist for DEGREE > 0 only (base/quad/GaussLegendre.hpp:61,
     // base/quad/GaussTetrahedron.hpp:93-175)
-    if (!n || degree < 1 || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX)) return ISL_ERR_ARG;
+    if (!n || degree < 1 || !(shape == ISL_QUAD || shape == ISL_TET || shape == ISL_HEX || shape == ISL_TRI))
+        return ISL_ERR_ARG;
     std::vector<double> ww, xx;
     if (!quadrature(shape, degree, ww, xx)) return ISL_ERR_ARG;
     *n = (int)ww.size();

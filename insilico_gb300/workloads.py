@@ -30,6 +30,7 @@ SEED_BASE = 0x15111C0
 
 HEX_FACES = np.array([[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7]])
 QUAD_EDGES = np.array([[0, 1], [1, 2], [2, 3], [3, 0]])
+TET_FACES = np.array([[0, 2, 1], [0, 1, 3], [1, 2, 3], [2, 0, 3]])  # base/mesh/ElementFaces.hpp
 TET_SPLIT = np.array([[0, 1, 3, 4], [1, 3, 4, 5], [3, 4, 5, 7], [1, 3, 5, 2], [3, 5, 2, 7], [5, 2, 7, 6]])
 HEX_LEX_OF_HIER = np.array([0, 1, 3, 2, 4, 5, 7, 6])
 
@@ -70,7 +71,7 @@ def unit_cube(kind: str, n1: int, n2: int, n3: int = 0):
 
 def faces_on_plane(shape: int, X, conn, elem, face, axis: int, value: float, tol: float = 1e-9):
     """Select boundary faces whose vertices all lie on x[axis] == value."""
-    table = HEX_FACES if shape == A.HEX else QUAD_EDGES
+    table = HEX_FACES if shape == A.HEX else (TET_FACES if shape == A.TET else QUAD_EDGES)
     verts = conn[elem[:, None], table[face]]
     on = np.all(np.abs(X[verts, axis] - value) < tol, axis=1)
     return elem[on], face[on]

@@ -2,7 +2,8 @@
 device library tabulates (isl_quadrature_rule) equal the oracle's bit for
 bit, and integrate monomials up to their degree exactly up to the
 reference's truncated constants (base/quad/GaussLegendre.hpp:115-134,
-base/quad/GaussTetrahedron.hpp:93-175)."""
+base/quad/GaussTetrahedron.hpp:93-175, and the triangle surface rules of
+base/quad/GaussTriangle.hpp:97-180)."""
 from math import factorial
 
 import numpy as np
@@ -12,7 +13,7 @@ import oracle as O
 from insilico_gb300 import _abi as A
 
 
-@pytest.mark.parametrize("shape,oshape", [(A.TET, O.TET), (A.QUAD, O.QUAD), (A.HEX, O.HEX)])
+@pytest.mark.parametrize("shape,oshape", [(A.TET, O.TET), (A.QUAD, O.QUAD), (A.HEX, O.HEX), (A.TRI, O.TRI)])
 @pytest.mark.parametrize("degree", [1, 2, 3, 4, 5])
 def test_rules_match_oracle_and_are_exact(shape, oshape, degree):
     w, x = A.quadrature_rule(shape, degree)
@@ -21,10 +22,10 @@ def test_rules_match_oracle_and_are_exact(shape, oshape, degree):
     dim = x.shape[1]
     worst = 0.0
     for p in np.ndindex(*([degree + 1] * dim)):
-        if shape == A.TET:
+        if shape in (A.TET, A.TRI):  # simplex: exact for total degree up to the rule's
             if sum(p) > degree:
                 continue
-            exact = np.prod([factorial(k) for k in p]) / factorial(sum(p) + 3)
+            exact = np.prod([factorial(k) for k in p]) / factorial(sum(p) + dim)
         else:  # tensor rule on [0,1]^dim: exact per coordinate up to the degree
             exact = np.prod([1.0 / (k + 1) for k in p])
         got = np.sum(w * np.prod(x ** np.array(p), axis=1))
