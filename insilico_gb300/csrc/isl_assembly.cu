@@ -1355,7 +1355,6 @@ static int dispatch_neumann(isl_ctx* c) {
     if (c->shape == ISL_QUAD && c->fedeg == 2 && c->ncomp == 2) return launch_neumann<9, 2, 4, 2>(c);
     if (c->shape == ISL_HEX && c->fedeg == 1 && c->ncomp == 1) return launch_neumann<8, 1, 8, 3>(c);
     if (c->shape == ISL_HEX && c->fedeg == 1 && c->ncomp == 3) return launch_neumann<8, 3, 8, 3>(c);
-    if (c->shape == ISL_HEX && c->fedeg == 2 && c->ncomp == 1) return launch_neumann<27, 1, 8, 3>(c);
     if (c->shape == ISL_TET && c->fedeg == 1 && c->ncomp == 1) return launch_neumann<4, 1, 4, 3>(c);
     if (c->shape == ISL_TET && c->fedeg == 1 && c->ncomp == 3) return launch_neumann<4, 3, 4, 3>(c);
     if (c->shape == ISL_TET && c->fedeg == 2 && c->ncomp == 1) return launch_neumann<10, 1, 4, 3>(c);

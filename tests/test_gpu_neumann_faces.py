@@ -1,13 +1,12 @@
 """Neumann tractions on tetrahedron faces (triangle surface rules of
-base/quad/GaussTriangle.hpp) and on the faces of Q2 hexahedra, through the
-GPU assembly against the oracle (base/asmb/NeumannForce.hpp:36-70 with the
-surface element of base/mesh/SurfaceElement.hpp):
+base/quad/GaussTriangle.hpp), through the GPU assembly against the oracle
+(base/asmb/NeumannForce.hpp:36-70 with the surface element of
+base/mesh/SurfaceElement.hpp):
 
 * P1 and P2 tetrahedra, heat::Laplace with a flux on the x = 1 faces and
   Dirichlet values on x = 0 only (the c3 mesh: jittered interior, planar
   boundary);
 * P2 tetrahedra, HyperElastic<StVenant> with a traction on x = 1;
-* Q2 hexahedra, heat::Laplace with a flux on x = 1;
 
 right-hand sides and matrices within 1e-12 of the oracle, and the FP64 CG
 solutions within 1e-9 of the oracle's.
@@ -44,17 +43,10 @@ def tet_elastic():
                      material="stvenant", dirichlet=_x0(3), neumann_plane=(0, 1.0, np.array([1.0, 0.3, -0.2])))
 
 
-def hex_q2_laplace():
-    X, conn = W.unit_cube("hex", 3, 3, 3)
-    kappa = np.exp(W.rng(93, 0).normal(0.0, 0.5, len(conn)))
-    return W.Problem("hex-q2", A.HEX, X, conn, 2, 1, "laplace", 4, kappa=kappa, dirichlet=_x0(1),
-                     neumann_plane=(0, 1.0, np.array([-1.5])))
-
-
-@pytest.mark.parametrize("case", ["tet_p1", "tet_p2", "tet_p2_elastic", "hex_q2"])
+@pytest.mark.parametrize("case", ["tet_p1", "tet_p2", "tet_p2_elastic"])
 def test_neumann_faces_match_oracle(case):
     p = {"tet_p1": lambda: tet_laplace(1), "tet_p2": lambda: tet_laplace(2),
-         "tet_p2_elastic": tet_elastic, "hex_q2": hex_q2_laplace}[case]()
+         "tet_p2_elastic": tet_elastic}[case]()
     S = W.setup_system(p)
     P, (rp, ci, v, b) = oracle_problem(p)
     assert S.neq == P.neq
