@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include "isl_df.cuh"
+
 namespace isl {
 
 template <typename T>
@@ -156,6 +158,27 @@ __device__ inline double block_sum_f(float v, double* sh) {
     return t;
 }
 
+// The same block sum with the warp sums added in double-float (about 48
+// significant bits) on the FP32 pipe instead of FP64: a butterfly of df adds
+// in warp 0 (TwoSum is exact, so both partners of a butterfly step compute
+// the same bits).  sh: 32 floats.  Fixed order; valid in warp 0.
+__device__ inline df block_sum_df(float v, float* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    df t = {0.f, 0.f};
+    if (w == 0) {
+        t.hi = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const df u = {__shfl_xor_sync(0xffffffffu, t.hi, o), __shfl_xor_sync(0xffffffffu, t.lo, o)};
+            t = df_add_acc(t, u);
+        }
+    }
+    return t;
+}
+
 // the block sum matching the precision of the summed values
 __device__ inline double block_sum_t(float v, double* sh) { return block_sum_f(v, sh); }
 __device__ inline double block_sum_t(double v, double* sh) { return block_sum(v, sh); }
@@ -269,6 +292,82 @@ __device__ inline void reduce_parts2_blk(const double* part, int n, double* sh, 
     out0 = out1 = 0.0;
     if (threadIdx.x == 0)
         for (int w = 0; w < NT / 32; ++w) { out0 += sh[2 * w]; out1 += sh[2 * w + 1]; }
+}
+
+// Double-float counterparts of reduce_parts_blk / reduce_parts2_blk for
+// partial sums stored as (hi, lo) float pairs (block_sum_df): the same
+// loads (eight in flight per thread), df adds on the FP32 pipe where those
+// use FP64 (GB300 runs FP64 at 1/64 of the FP32 rate, and these sums sit in
+// the serial tail of every CG kernel).  sh: 32 doubles of shared memory,
+// reused as 32 df.  Fixed order; the result (rounded to FP64) is valid in
+// thread 0.
+__device__ inline df warp_sum_df(df s) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const df u = {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+        s = df_add_acc(s, u);
+    }
+    return s;
+}
+
+__device__ inline double df_value(df a) { return (double)a.hi + (double)a.lo; }
+
+template <int NT>
+__device__ inline double reduce_parts_df_blk(const float2* part, int n, double* sh) {
+    static_assert(NT % 32 == 0 && NT / 32 <= 32, "sh holds one df per warp");
+    df* shd = reinterpret_cast<df*>(sh);
+    df s = {0.f, 0.f};
+    for (int base = 0; base < n; base += 8 * NT) {
+        float2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * NT + (int)threadIdx.x;
+            v[u] = i < n ? __ldcg(part + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (base + u * NT + (int)threadIdx.x < n) s = df_add_acc(s, df{v[u].x, v[u].y});
+    }
+    s = warp_sum_df(s);
+    __syncthreads();  // sh may still be read by an earlier block sum
+    if ((threadIdx.x & 31) == 0) shd[threadIdx.x >> 5] = s;
+    __syncthreads();
+    df t = {0.f, 0.f};
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) t = df_add_acc(t, shd[w]);
+    return df_value(t);
+}
+
+template <int NT>
+__device__ inline void reduce_parts2_df_blk(const float4* part, int n, double* sh, double& out0, double& out1) {
+    static_assert(NT % 32 == 0 && NT / 16 <= 32, "sh holds two df per warp");
+    df* shd = reinterpret_cast<df*>(sh);
+    df s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
+    for (int base = 0; base < n; base += 8 * NT) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * NT + (int)threadIdx.x;
+            v[u] = i < n ? __ldcg(part + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (base + u * NT + (int)threadIdx.x < n) {
+                s0 = df_add_acc(s0, df{v[u].x, v[u].y});
+                s1 = df_add_acc(s1, df{v[u].z, v[u].w});
+            }
+    }
+    s0 = warp_sum_df(s0);
+    s1 = warp_sum_df(s1);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) { shd[2 * (threadIdx.x >> 5)] = s0; shd[2 * (threadIdx.x >> 5) + 1] = s1; }
+    __syncthreads();
+    out0 = out1 = 0.0;
+    if (threadIdx.x == 0) {
+        df t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+        for (int w = 0; w < NT / 32; ++w) { t0 = df_add_acc(t0, shd[2 * w]); t1 = df_add_acc(t1, shd[2 * w + 1]); }
+        out0 = df_value(t0);
+        out1 = df_value(t1);
+    }
 }
 
 }  // namespace isl

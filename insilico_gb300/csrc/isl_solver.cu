@@ -1737,12 +1737,13 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
             rz += rv[a] * z;
         }
     }
-    const double b1 = block_sum_f(rr, sh);
-    const double b2 = block_sum_f(rz, sh);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+    // r.r and r.z: block and grid sums in double-float, as in k_bspmv_dir
+    const df b1 = block_sum_df(rr, reinterpret_cast<float*>(sh));
+    const df b2 = block_sum_df(rz, reinterpret_cast<float*>(sh));
+    if (threadIdx.x == 0) reinterpret_cast<float4*>(part)[blockIdx.x] = make_float4(b1.hi, b1.lo, b2.hi, b2.lo);
     if (!last_block(&S->ticket2)) return;
     double trr, trz;
-    reduce_parts2_blk<NODE_BS>(part, gridDim.x, sh, trr, trz);
+    reduce_parts2_df_blk<NODE_BS>(reinterpret_cast<const float4*>(part), gridDim.x, sh, trr, trz);
     if (threadIdx.x == 0) {
         S->rr = trr;
         S->iters += 1;
