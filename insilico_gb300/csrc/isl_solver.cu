@@ -62,15 +62,23 @@ __global__ void __launch_bounds__(BS) k_spmv_pap(int n, const int* __restrict__ 
             loc += p[row] * acc;
         }
     }
-    const double bs = block_sum_t(loc, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
-        if (threadIdx.x == 0) {
-            S->pAp = tot;
-            S->alpha = S->absNew / tot;
-            S->ticket1 = 0;
-        }
+    double tot = 0.0;
+    bool last;
+    if constexpr (std::is_same<TX, float>::value) {  // FP32 vectors: double-float block and grid sums
+        const df bs = block_sum_df(loc, reinterpret_cast<float*>(sh));
+        if (threadIdx.x == 0) reinterpret_cast<float2*>(part)[blockIdx.x] = make_float2(bs.hi, bs.lo);
+        last = last_block(&S->ticket1);
+        if (last) tot = reduce_parts_df_blk<BS>(reinterpret_cast<const float2*>(part), gridDim.x, sh);
+    } else {
+        const double bs = block_sum_t(loc, sh);
+        if (threadIdx.x == 0) part[blockIdx.x] = bs;
+        last = last_block(&S->ticket1);
+        if (last) tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
+    }
+    if (last && threadIdx.x == 0) {
+        S->pAp = tot;
+        S->alpha = S->absNew / tot;
+        S->ticket1 = 0;
     }
 }
 
@@ -110,12 +118,22 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
         rr += ri * ri;
         rz += ri * (dinv[i] * ri);
     }
-    const double b1 = block_sum_t(rr, sh);
-    const double b2 = block_sum_t(rz, sh);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
-    if (last_block(&S->ticket2)) {
-        double trr, trz;
-        reduce_parts2_blk<BS>(part, gridDim.x, sh, trr, trz);
+    bool last;
+    double trr = 0.0, trz = 0.0;
+    if constexpr (std::is_same<TX, float>::value) {  // FP32 vectors: double-float block and grid sums
+        const df b1 = block_sum_df(rr, reinterpret_cast<float*>(sh));
+        const df b2 = block_sum_df(rz, reinterpret_cast<float*>(sh));
+        if (threadIdx.x == 0) reinterpret_cast<float4*>(part)[blockIdx.x] = make_float4(b1.hi, b1.lo, b2.hi, b2.lo);
+        last = last_block(&S->ticket2);
+        if (last) reduce_parts2_df_blk<BS>(reinterpret_cast<const float4*>(part), gridDim.x, sh, trr, trz);
+    } else {
+        const double b1 = block_sum_t(rr, sh);
+        const double b2 = block_sum_t(rz, sh);
+        if (threadIdx.x == 0) { part[2 * blockIdx.x] = b1; part[2 * blockIdx.x + 1] = b2; }
+        last = last_block(&S->ticket2);
+        if (last) reduce_parts2_blk<BS>(part, gridDim.x, sh, trr, trz);
+    }
+    if (last) {
         if (threadIdx.x == 0) {
             S->rr = trr;
             S->iters += 1;
@@ -335,10 +353,10 @@ __global__ void __launch_bounds__(BS, MINB) k_sspmv_batch(int nslice, const int*
             loc += p[row] * acc;
         }
     }
-    const double bsum = block_sum_f(loc, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = bsum;
+    const df bsum = block_sum_df(loc, reinterpret_cast<float*>(sh));
+    if (threadIdx.x == 0) reinterpret_cast<float2*>(part)[blockIdx.x] = make_float2(bsum.hi, bsum.lo);
     if (last_block(&S->ticket1)) {
-        const double tot = reduce_parts_blk<BS>(part, gridDim.x, 1, 0, sh);
+        const double tot = reduce_parts_df_blk<BS>(reinterpret_cast<const float2*>(part), gridDim.x, sh);
         if (threadIdx.x == 0) {
             S->pAp = tot;
             S->alpha = S->absNew / tot;
