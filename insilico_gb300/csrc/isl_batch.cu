@@ -17,6 +17,7 @@
 // meets the tolerance.
 #include <cmath>
 #include <functional>
+#include <type_traits>
 #include <vector>
 
 #include "isl_device.cuh"
@@ -78,6 +79,18 @@ __device__ inline void finish(const BArgs& a, int k, int code) {
 __device__ inline double inst_sum(const BArgs& a, int k, int off, double* sh) {
     const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
     return reduce_parts(a.part + (size_t)off * a.nblk + b0, b1 - b0, 1, 0, sh);
+}
+
+// FP32 vectors: a row block's partial sum as a double-float pair in its part
+// slot, and an instance's total summed in double-float (the serial tails of
+// the iteration kernels stay off the FP64 pipe)
+__device__ inline void put_part_df(const BArgs& a, int off, int blk, float v, double* sh) {
+    const df s = block_sum_df(v, reinterpret_cast<float*>(sh));
+    if (threadIdx.x == 0) reinterpret_cast<float2*>(a.part)[(size_t)off * a.nblk + blk] = make_float2(s.hi, s.lo);
+}
+__device__ inline double inst_sum_df(const BArgs& a, int k, int off) {
+    const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
+    return reduce_parts_df(reinterpret_cast<const float2*>(a.part) + (size_t)off * a.nblk + b0, b1 - b0);
 }
 
 // The listed row blocks, one per loop trip of a CTA: w-th entry of the list.
@@ -213,11 +226,16 @@ __global__ void __launch_bounds__(BBS) kb_spmv(BArgs a, const int* __restrict__ 
             }
         }
     }
-    const double s1 = block_sum_t(loc, sh);
-    if (threadIdx.x == 0) a.part[blk] = s1;
+    constexpr bool F32 = std::is_same<TX, float>::value;
+    if constexpr (F32) {
+        put_part_df(a, 0, blk, loc, sh);
+    } else {
+        const double s1 = block_sum_t(loc, sh);
+        if (threadIdx.x == 0) a.part[blk] = s1;
+    }
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
-        const double tot = inst_sum(a, k, 0, sh);
+        const double tot = F32 ? inst_sum_df(a, k, 0) : inst_sum(a, k, 0, sh);
         if (threadIdx.x == 0) {
             SS(a, S_ALPHA, k) = SS(a, S_ABSNEW, k) / tot;
             a.t[T_SPMV * a.ninst + k] = 0;
@@ -268,11 +286,10 @@ __global__ void __launch_bounds__(BBS, MINB) kb_sspmv(BArgs a, const int* __rest
             loc += p[row] * acc;
         }
     }
-    const double s1 = block_sum_t(loc, sh);
-    if (threadIdx.x == 0) a.part[blk] = s1;
+    put_part_df(a, 0, blk, loc, sh);
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_SPMV * a.ninst + k], cnt)) {
-        const double tot = inst_sum(a, k, 0, sh);
+        const double tot = inst_sum_df(a, k, 0);
         if (threadIdx.x == 0) {
             SS(a, S_ALPHA, k) = SS(a, S_ABSNEW, k) / tot;
             a.t[T_SPMV * a.ninst + k] = 0;
@@ -300,11 +317,18 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
         rr += ri * ri;
         rz += ri * (dinv[i] * ri);
     }
-    const double s1 = block_sum_t(rr, sh), s2 = block_sum_t(rz, sh);
-    if (threadIdx.x == 0) { a.part[blk] = s1; a.part[a.nblk + blk] = s2; }
+    constexpr bool F32 = std::is_same<TX, float>::value;
+    if constexpr (F32) {
+        put_part_df(a, 0, blk, rr, sh);
+        put_part_df(a, 1, blk, rz, sh);
+    } else {
+        const double s1 = block_sum_t(rr, sh), s2 = block_sum_t(rz, sh);
+        if (threadIdx.x == 0) { a.part[blk] = s1; a.part[a.nblk + blk] = s2; }
+    }
     const unsigned cnt = a.inst_blk[k + 1] - a.inst_blk[k];
     if (last_of(&a.t[T_UPD * a.ninst + k], cnt)) {
-        const double trr = inst_sum(a, k, 0, sh), trz = inst_sum(a, k, 1, sh);
+        const double trr = F32 ? inst_sum_df(a, k, 0) : inst_sum(a, k, 0, sh);
+        const double trz = F32 ? inst_sum_df(a, k, 1) : inst_sum(a, k, 1, sh);
         if (threadIdx.x == 0) {
             SS(a, S_RR, k) = trr;
             const int it = ++II(a, I_ITERS, k);

@@ -311,6 +311,27 @@ __device__ inline df warp_sum_df(df s) {
 
 __device__ inline double df_value(df a) { return (double)a.hi + (double)a.lo; }
 
+// Sum of the (hi, lo) pairs part[i], i < n, by warp 0 (the double-float
+// counterpart of reduce_parts): eight loads in flight per lane, df adds,
+// a fixed butterfly.  Valid in warp 0.
+__device__ inline double reduce_parts_df(const float2* part, int n) {
+    if (threadIdx.x >= 32) return 0.0;
+    const int l = threadIdx.x;
+    df s = {0.f, 0.f};
+    for (int base = 0; base < n; base += 256) {
+        float2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = base + u * 32 + l;
+            v[u] = i < n ? __ldcg(part + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (base + u * 32 + l < n) s = df_add_acc(s, df{v[u].x, v[u].y});
+    }
+    return df_value(warp_sum_df(s));
+}
+
 template <int NT>
 __device__ inline double reduce_parts_df_blk(const float2* part, int n, double* sh) {
     static_assert(NT % 32 == 0 && NT / 32 <= 32, "sh holds one df per warp");
