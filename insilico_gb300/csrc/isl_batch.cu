@@ -88,6 +88,14 @@ __device__ inline void put_part_df(const BArgs& a, int off, int blk, float v, do
     const df s = block_sum_df(v, reinterpret_cast<float*>(sh));
     if (threadIdx.x == 0) reinterpret_cast<float2*>(a.part)[(size_t)off * a.nblk + blk] = make_float2(s.hi, s.lo);
 }
+__device__ inline void put_part_df2(const BArgs& a, int blk, float v0, float v1, double* sh) {
+    df s0, s1;
+    block_sum_df2(v0, v1, reinterpret_cast<float*>(sh), s0, s1);
+    if (threadIdx.x == 0) {
+        reinterpret_cast<float2*>(a.part)[blk] = make_float2(s0.hi, s0.lo);
+        reinterpret_cast<float2*>(a.part)[(size_t)a.nblk + blk] = make_float2(s1.hi, s1.lo);
+    }
+}
 __device__ inline double inst_sum_df(const BArgs& a, int k, int off) {
     const int b0 = a.inst_blk[k], b1 = a.inst_blk[k + 1];
     return reduce_parts_df(reinterpret_cast<const float2*>(a.part) + (size_t)off * a.nblk + b0, b1 - b0);
@@ -319,8 +327,7 @@ __global__ void __launch_bounds__(BBS) kb_update(BArgs a, TX* __restrict__ x, TX
     }
     constexpr bool F32 = std::is_same<TX, float>::value;
     if constexpr (F32) {
-        put_part_df(a, 0, blk, rr, sh);
-        put_part_df(a, 1, blk, rz, sh);
+        put_part_df2(a, blk, rr, rz, sh);
     } else {
         const double s1 = block_sum_t(rr, sh), s2 = block_sum_t(rz, sh);
         if (threadIdx.x == 0) { a.part[blk] = s1; a.part[a.nblk + blk] = s2; }

@@ -179,6 +179,31 @@ __device__ inline df block_sum_df(float v, float* sh) {
     return t;
 }
 
+// Two block sums at once (one pair of barriers): the bits of two
+// block_sum_df calls.  sh: 64 floats.  Valid in warp 0.
+__device__ inline void block_sum_df2(float a, float b, float* sh, df& oa, df& ob) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) { sh[w] = a; sh[32 + w] = b; }
+    __syncthreads();
+    oa = ob = df{0.f, 0.f};
+    if (w == 0) {
+        const bool in = l < (int)(blockDim.x >> 5);
+        oa.hi = in ? sh[l] : 0.f;
+        ob.hi = in ? sh[32 + l] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const df ua = {__shfl_xor_sync(0xffffffffu, oa.hi, o), __shfl_xor_sync(0xffffffffu, oa.lo, o)};
+            const df ub = {__shfl_xor_sync(0xffffffffu, ob.hi, o), __shfl_xor_sync(0xffffffffu, ob.lo, o)};
+            oa = df_add_acc(oa, ua);
+            ob = df_add_acc(ob, ub);
+        }
+    }
+}
+
 // the block sum matching the precision of the summed values
 __device__ inline double block_sum_t(float v, double* sh) { return block_sum_f(v, sh); }
 __device__ inline double block_sum_t(double v, double* sh) { return block_sum(v, sh); }

@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(BS) k_cg_update(int n, TX* __restrict__ x, TX*
     bool last;
     double trr = 0.0, trz = 0.0;
     if constexpr (std::is_same<TX, float>::value) {  // FP32 vectors: double-float block and grid sums
-        const df b1 = block_sum_df(rr, reinterpret_cast<float*>(sh));
-        const df b2 = block_sum_df(rz, reinterpret_cast<float*>(sh));
+        df b1, b2;
+        block_sum_df2(rr, rz, reinterpret_cast<float*>(sh), b1, b2);
         if (threadIdx.x == 0) reinterpret_cast<float4*>(part)[blockIdx.x] = make_float4(b1.hi, b1.lo, b2.hi, b2.lo);
         last = last_block(&S->ticket2);
         if (last) reduce_parts2_df_blk<BS>(reinterpret_cast<const float4*>(part), gridDim.x, sh, trr, trz);
@@ -1756,8 +1756,8 @@ __global__ void __launch_bounds__(NODE_BS) k_cg_update_b3n(int nbr, float* __res
         }
     }
     // r.r and r.z: block and grid sums in double-float, as in k_bspmv_dir
-    const df b1 = block_sum_df(rr, reinterpret_cast<float*>(sh));
-    const df b2 = block_sum_df(rz, reinterpret_cast<float*>(sh));
+    df b1, b2;
+    block_sum_df2(rr, rz, reinterpret_cast<float*>(sh), b1, b2);
     if (threadIdx.x == 0) reinterpret_cast<float4*>(part)[blockIdx.x] = make_float4(b1.hi, b1.lo, b2.hi, b2.lo);
     if (!last_block(&S->ticket2)) return;
     double trr, trz;
