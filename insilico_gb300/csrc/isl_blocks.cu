@@ -50,10 +50,10 @@ __device__ __forceinline__ df ldf(const float4* p, int k) {  // k-th double-floa
 // per element: the Jacobian at the first quadrature point (constant on a
 // parallelepiped), its inverse transpose and det J in FP64, stored as
 // double-float with the element's Lame parameters
-__global__ void k_affine_geo(int E, const double* __restrict__ X, const int32_t* __restrict__ conn,
+__global__ void k_affine_geo(int E, int nel, const double* __restrict__ X, const int32_t* __restrict__ conn,
                              const double* __restrict__ coef, AffinePairs T, float4* __restrict__ geo, int* flags) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;  // the first nel of the E elements
+    if (e >= nel) return;
     double Xe[8][3];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -79,6 +79,17 @@ __global__ void k_affine_geo(int E, const double* __restrict__ X, const int32_t*
     for (int k = 0; k < GEO_F4; ++k) g[k] = make_float4(v[2 * k].hi, v[2 * k].lo, v[2 * k + 1].hi, v[2 * k + 1].lo);
 }
 
+// per element: lam and mu as double-float (lam.hi, lam.lo, mu.hi, mu.lo), the
+// values k_affine_geo stores in the last float4 of its record; on a mesh of
+// translates of one element the geometry record of element 0 is all the
+// block kernel reads besides these
+__global__ void k_affine_lame(int E, const double* __restrict__ coef, float4* __restrict__ lame) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+        const df lam = df_from_double(coef[e]), mu = df_from_double(coef[E + e]);
+        lame[e] = make_float4(lam.hi, lam.lo, mu.hi, mu.lo);
+    }
+}
+
 struct BlockArgs {
     int nslot, nblk;
     const int* sblk;      // block of every sliced-ELL slot, -1 for padding
@@ -90,6 +101,7 @@ struct BlockArgs {
     const int* adj;
     const int* rowptr;
     const float4* geo;
+    const float4* lame;   // per element lam, mu (k_affine_blocks_u)
     double* v64;
     float* sv;            // [slot/32][9][32]
     float* bv;            // [9][nblk] block-row copy, or null
@@ -228,8 +240,8 @@ __global__ void __launch_bounds__(256) k_affine_blocks_u(BlockArgs P, AffinePair
             ++ia;
             ++ib;
             const int pr = (va & 7) * 8 + (vb & 7);
-            const float4* g = P.geo + (size_t)e1 * GEO_F4;
-            const df lam = ldf(g, 18), mu = ldf(g, 19);
+            const float4 lm = __ldg(P.lame + e1);
+            const df lam = {lm.x, lm.y}, mu = {lm.z, lm.w};
 #pragma unroll
             for (int k = 0; k < 9; ++k)
                 acc[k] = df_add_acc(acc[k], df_add(df_mul(lam, sL[pr][k]), df_mul(mu, sM[pr][k])));
@@ -386,10 +398,22 @@ int assemble_affine_blocks(isl_ctx* c, const ElemArgs& A) {
     if (rc != ISL_OK) return rc;
     cudaStream_t st = c->stream;
     const int E = (int)c->nelem;
-    ISL_CHECK_CUDA(c, c->dgeo.alloc((size_t)E * GEO_F4));
+    c->last_shared_geo = c->use_shared_geo && c->mesh_uniform == 1;
+    ISL_CHECK_CUDA(c, c->dgeo.alloc((size_t)(c->last_shared_geo ? 1 : E) * GEO_F4));
     ISL_CHECK_CUDA(c, c->dbval.alloc((size_t)9 * c->nblk));
     ISL_CHECK_CUDA(c, cudaMemsetAsync(c->dstageF.p, 0, (size_t)c->nloc * E * 8, st));
-    k_affine_geo<<<(unsigned)((E + 127) / 128), 128, 0, st>>>(E, c->dX.p, c->dconn.p, c->dcoef.p, T, c->dgeo.p, A.flags);
+    if (c->last_shared_geo) {
+        // translates of element 0: its geometry record (their Jacobians, and with them the
+        // sign of det J, are element 0's), and lam, mu of every element
+        ISL_CHECK_CUDA(c, c->dlame.alloc((size_t)E));
+        k_affine_geo<<<1, 32, 0, st>>>(E, 1, c->dX.p, c->dconn.p, c->dcoef.p, T, c->dgeo.p, A.flags);
+        k_affine_lame<<<(unsigned)std::min<int64_t>((E + 255) / 256, (int64_t)c->sm_count * 8), 256, 0, st>>>(
+            E, c->dcoef.p, c->dlame.p);
+        c->launches += 1;
+    } else {
+        k_affine_geo<<<(unsigned)((E + 127) / 128), 128, 0, st>>>(E, E, c->dX.p, c->dconn.p, c->dcoef.p, T, c->dgeo.p,
+                                                                  A.flags);
+    }
     BlockArgs P;
     P.nslot = (int)c->nslot;
     P.nblk = (int)c->nblk;
@@ -402,6 +426,7 @@ int assemble_affine_blocks(isl_ctx* c, const ElemArgs& A) {
     P.adj = c->dadj.p;
     P.rowptr = c->drowptr.p;
     P.geo = c->dgeo.p;
+    P.lame = c->last_shared_geo ? c->dlame.p : nullptr;
     P.v64 = c->dval64.p;
     P.sv = c->dsval.p;
     // the block-row copy only feeds the block-row SpMV variants (and their
@@ -409,7 +434,6 @@ int assemble_affine_blocks(isl_ctx* c, const ElemArgs& A) {
     const bool need_bv = c->bspmv_lpb == 0 || c->bspmv_lpb == 4 || c->bspmv_lpb == 8 || c->bspmv_lpb == 16;
     P.bv = need_bv ? c->dbval.p : nullptr;
     const unsigned grid = (unsigned)std::min<int64_t>((c->nslot + 255) / 256, (int64_t)c->sm_count * 8);
-    c->last_shared_geo = c->use_shared_geo && c->mesh_uniform == 1;
     if (c->last_shared_geo) k_affine_blocks_u<<<grid, 256, 0, st>>>(P, T);
     else k_affine_blocks<<<grid, 256, 0, st>>>(P, T);
     ISL_CHECK_CUDA(c, cudaGetLastError());

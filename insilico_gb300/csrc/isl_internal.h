@@ -220,7 +220,8 @@ struct isl_ctx {
     int64_t val32_serial = -1;   // assembly whose values dval32 holds
     int64_t bvals_serial = -1;   // assembly that wrote the FP32 block copies directly
     // direct block assembly of small-strain elasticity on parallelepipeds (isl_blocks.cu)
-    isl::DBuf<float4> dgeo;      // per element: detJ Ji, Ji, lam, mu as double-float
+    isl::DBuf<float4> dgeo;      // per element: detJ Ji, Ji, lam, mu as double-float (element 0 only on a mesh of translates)
+    isl::DBuf<float4> dlame;     // per element lam, mu as double-float (mesh of translates)
     isl::DBuf<int32_t> dbrobj, dadj_off, dadj, dsblk;
     int64_t bmap_serial = -1;
     int asm_precision = 0;       // precision of the assembly in progress
