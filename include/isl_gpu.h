@@ -586,8 +586,10 @@ int isl_serve_destroy(isl_server* s);
  *
  * The first call on a device looks the scratch array up on that device
  * (cudaGetSymbolAddress, with that device current), and looks it up again
- * when the device's context has changed (after cudaDeviceReset); make that
- * first call before any stream capture.  All calls on a device share the one array, and
+ * when the device's context has changed (after cudaDeviceReset).  Every call
+ * copies to the host and waits on `stream`, so no call may run while that
+ * stream (or the legacy default stream) is being captured into a graph.
+ * All calls on a device share the one array, and
  * it keeps the last call's contents: each call clears what has to start at
  * zero, but calls that overlap on the GPU (other streams or host threads)
  * race on it and must be serialised by the caller. */
